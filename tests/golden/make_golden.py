@@ -1,0 +1,276 @@
+"""Generate the golden fixtures under tests/golden/ from the FFTHomPy reference.
+
+This script is the only place that runs the reference.  It imports the
+unmodified reference package from REFERENCE_DIR (default /root/reference),
+with a small runtime shim for the NumPy/SciPy/Python names it still uses
+(np.int/np.float/np.complex, time.clock, collections.Callable,
+scipy.setdiff1d).  It writes plain .npz files (arrays + a JSON metadata
+string), so the tests never need the reference at run time.
+
+Fixture families
+----------------
+ref_<file>_<prob>.npz
+    The reference's own golden pickles test_results/python3/<file>_<prob>
+    (compared by run_unittests.py:57-64 at delta 1e-9), flattened: the
+    problem definition stored in the pickle, the homogenised matrices, the CG
+    iteration counts / final residuals and the solution fields.
+run_<name>.npz
+    Problems this script defines and runs through the reference's
+    Problem(...).calculate() (ffthompy/problem.py:70-83): config-1 (2D GaNi
+    45^2 square, tol 1e-8), seeded random 'fun' materials on odd, even,
+    prime and anisotropic grids, Ga and GaNi, scalar and elasticity.
+op_<name>.npz
+    Single applications of the reference operator FiGFA = G o A
+    (ffthompy/applications.py:24-58) to seeded random fields; this pins the
+    Green projection, the Ga scale factor of Tensor.enlarge and the r2c FFT
+    conventions independently of CG.
+
+Usage:  python tests/golden/make_golden.py [REFERENCE_DIR]
+"""
+import collections
+import collections.abc
+import contextlib
+import glob
+import io
+import json
+import os
+import pickle
+import sys
+import time
+
+import numpy as np
+import scipy
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REFERENCE_DIR = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
+
+
+def _install_shim():
+    np.int = int
+    np.float = float
+    np.complex = complex
+    time.clock = time.perf_counter
+    collections.Callable = collections.abc.Callable
+    scipy.setdiff1d = np.setdiff1d
+    os.environ.setdefault('PYTHONDONTWRITEBYTECODE', '1')
+    sys.dont_write_bytecode = True
+    sys.path.insert(0, REFERENCE_DIR)
+    sys.path.insert(0, os.path.join(REFERENCE_DIR, 'examples', 'scalar'))
+
+
+def _jsonable(v):
+    if isinstance(v, np.ndarray):
+        return {'__nd__': v.tolist(), 'dtype': str(v.dtype)}
+    if isinstance(v, (np.integer,)):
+        return int(v)
+    if isinstance(v, (np.floating,)):
+        return float(v)
+    if isinstance(v, dict):
+        return {k: _jsonable(x) for k, x in v.items() if not callable(x)}
+    if isinstance(v, (list, tuple)):
+        return [_jsonable(x) for x in v]
+    return v
+
+
+def _problem_meta(physics, material, solve, solver, postprocess):
+    mat = {k: v for k, v in material.items() if k != 'fun'}
+    return dict(physics=physics, material=_jsonable(mat), solve=_jsonable(solve),
+                solver=_jsonable(solver), postprocess=_jsonable(postprocess),
+                has_fun=('fun' in material))
+
+
+def _flatten_output(out, primaldual, arrays):
+    for pd in primaldual:
+        for key, val in out['mat_' + pd].items():
+            arrays['mat__%s__%s' % (pd, key)] = np.asarray(val, dtype=np.float64)
+        res = out['res_' + pd]
+        arrays['kit__' + pd] = np.array([r['info']['kit'] for r in res], dtype=np.int64)
+        arrays['normres__' + pd] = np.array([float(r['info']['norm_res']) for r in res])
+        arrays['sol__' + pd] = np.stack([s.val for s in out['sol_' + pd]])
+
+
+def _save(name, meta, arrays):
+    path = os.path.join(HERE, name + '.npz')
+    np.savez_compressed(path, meta=np.array(json.dumps(meta)), **arrays)
+    print('wrote', os.path.relpath(path, HERE), sorted(arrays)[:4], '...')
+
+
+def golden_pickles():
+    """Flatten the reference's own golden pickles (run_unittests.py:46-64)."""
+    for path in sorted(glob.glob(os.path.join(REFERENCE_DIR, 'test_results', 'python3', '*'))):
+        with open(path, 'rb') as f:
+            r = pickle.load(f)
+        meta = _problem_meta(r['physics'], r['material'], r['solve'], r['solver'],
+                             r['postprocess'])
+        arrays = {}
+        if 'fun' in r['material']:
+            # examples/scalar/from_file.py:411-419: values do not depend on coord
+            arrays['fun_values'] = np.asarray(r['material']['fun'](None), dtype=np.float64)
+        _flatten_output(r, r['solve']['primaldual'], arrays)
+        _save('ref_' + os.path.basename(path), meta, arrays)
+
+
+def _run_problem(physics, material, solve, solver, postprocess):
+    from ffthompy.problem import Problem
+    conf_problem = {'name': 'p', 'physics': physics, 'material': material,
+                    'solve': solve, 'solver': solver, 'postprocess': postprocess}
+    pb = Problem(conf_problem, None)
+    with contextlib.redirect_stdout(io.StringIO()):
+        t0 = time.perf_counter()
+        pb.calculate()
+        t1 = time.perf_counter()
+    return pb, t1 - t0
+
+
+def _fun_material(values, Y, order=0, P=None):
+    values = np.asarray(values, dtype=np.float64)
+    grid = values.shape[2:]
+
+    def fun(coord):
+        assert tuple(coord.shape[1:]) == tuple(grid), (coord.shape, grid)
+        return values.copy()
+    mat = {'fun': fun, 'Y': np.asarray(Y, dtype=np.float64), 'order': order,
+           'P': np.array(grid if P is None else P)}
+    return mat
+
+
+def _iso_field(dim, a):
+    return np.einsum('ij,...->ij...', np.eye(dim), a)
+
+
+def _elastic_field(bulk, mu):
+    from ffthompy.mechanics.matcoef import ElasticTensor
+    dim = bulk.ndim
+    D = dim * (dim + 1) // 2
+    out = np.zeros((D, D) + bulk.shape)
+    plane = None if dim == 3 else 'strain'
+    for idx in np.ndindex(*bulk.shape):
+        out[(slice(None), slice(None)) + idx] = ElasticTensor(
+            bulk=float(bulk[idx]), mu=float(mu[idx]), plane=plane).mandel
+    return out
+
+
+def run_cases():
+    rng = np.random.default_rng(20261203)
+    cases = []
+
+    # config-1: 2D GaNi 45^2, centred square 0.6, 11*I / 1*I, tol 1e-8
+    dim = 2
+    N = np.array([45, 45])
+    mat_sq = {'inclusions': ['square', 'otherwise'], 'positions': [np.zeros(dim), ''],
+              'params': [0.6 * np.ones(dim), ''], 'vals': [11 * np.eye(dim), np.eye(dim)],
+              'Y': np.ones(dim), 'order': None}
+    cases.append(('cfg1_square45', 'scalar', mat_sq,
+                  {'kind': 'GaNi', 'N': N, 'primaldual': ['primal', 'dual']},
+                  {'kind': 'CG', 'tol': 1e-8, 'maxiter': 1e3},
+                  [{'kind': 'GaNi'}, {'kind': 'Ga', 'order': None},
+                   {'kind': 'Ga', 'order': 0, 'P': N}], None))
+
+    # seeded random isotropic 'fun' materials, scalar
+    for name, Nl, Y, kind, tol in [
+            ('s2_gani_15', [15, 15], [1., 1.], 'GaNi', 1e-8),
+            ('s2_ga_15', [15, 15], [1., 1.], 'Ga', 1e-8),          # Nbar = 29 (prime)
+            ('s2_gani_even_12', [12, 12], [1., 1.], 'GaNi', 1e-8),  # Nyquist zeroing
+            ('s2_ga_even_8', [8, 8], [1., 1.], 'Ga', 1e-8),         # Nbar = 15
+            ('s2_gani_aniso', [9, 21], [1., 2.5], 'GaNi', 1e-9),
+            ('s2_ga_aniso', [7, 11], [2., 1.], 'Ga', 1e-9),          # Nbar = 13 x 21
+            ('s3_gani_7', [7, 7, 7], [1., 1., 1.], 'GaNi', 1e-8),
+            ('s3_ga_7', [7, 7, 7], [1., 1., 1.], 'Ga', 1e-8),       # Nbar = 13
+            ('s3_gani_aniso', [5, 9, 6], [1., 1.5, 0.7], 'GaNi', 1e-8),
+            ('s3_ga_aniso', [5, 7, 9], [1., 1., 1.], 'Ga', 1e-8)]:
+        Nl = np.array(Nl)
+        d = Nl.size
+        a = 1. + 99. * (rng.random(tuple(Nl)) < 0.3) * rng.random(tuple(Nl))
+        values = _iso_field(d, a)
+        pp = [{'kind': 'GaNi'}] if kind == 'GaNi' else [{'kind': 'Ga'}]
+        if kind == 'GaNi':
+            pp.append({'kind': 'Ga', 'order': 0, 'P': Nl})
+        cases.append((name, 'scalar', _fun_material(values, Y),
+                      {'kind': kind, 'N': Nl, 'primaldual': ['primal', 'dual']},
+                      {'kind': 'CG', 'tol': tol, 'maxiter': 1e3}, pp, values))
+
+    # a full (anisotropic, symmetric positive definite) scalar coefficient
+    Nl = np.array([11, 9])
+    B = rng.standard_normal((2, 2) + tuple(Nl))
+    values = np.einsum('ik...,jk...->ij...', B, B) + 0.5 * _iso_field(2, np.ones(tuple(Nl)))
+    cases.append(('s2_full_gani', 'scalar', _fun_material(values, [1., 1.]),
+                  {'kind': 'GaNi', 'N': Nl, 'primaldual': ['primal', 'dual']},
+                  {'kind': 'CG', 'tol': 1e-9, 'maxiter': 1e3},
+                  [{'kind': 'GaNi'}, {'kind': 'Ga', 'order': 0, 'P': Nl}], values))
+
+    # elasticity with random isotropic phases (Mandel 6x6 / 3x3)
+    for name, Nl, kind in [('e3_gani_5', [5, 5, 5], 'GaNi'), ('e3_ga_5', [5, 5, 5], 'Ga'),
+                           ('e3_gani_7', [7, 7, 7], 'GaNi'),
+                           ('e2_gani_9', [9, 9], 'GaNi'), ('e2_ga_7', [7, 7], 'Ga')]:
+        Nl = np.array(Nl)
+        incl = rng.random(tuple(Nl)) < 0.35
+        bulk = np.where(incl, 5.5556, 0.8333)
+        mu = np.where(incl, 4.1667, 0.3846)
+        values = _elastic_field(bulk, mu)
+        pp = [{'kind': 'GaNi'}, {'kind': 'Ga', 'order': 0, 'P': Nl}] if kind == 'GaNi' \
+            else [{'kind': 'Ga'}]
+        cases.append((name, 'elasticity', _fun_material(values, np.ones(Nl.size)),
+                      {'kind': kind, 'N': Nl, 'primaldual': ['primal', 'dual']},
+                      {'kind': 'CG', 'tol': 1e-8, 'maxiter': 1e3}, pp, values))
+
+    for name, physics, material, solve, solver, pp, values in cases:
+        pb, seconds = _run_problem(physics, material, solve, solver, pp)
+        meta = _problem_meta(physics, material, solve, solver, pp)
+        meta['reference_seconds'] = seconds
+        arrays = {}
+        if values is not None:
+            arrays['fun_values'] = values
+        _flatten_output(pb.output, solve['primaldual'], arrays)
+        _save('run_' + name, meta, arrays)
+
+
+def operator_cases():
+    """Single G o A applications (ffthompy/applications.py:24-58)."""
+    import ffthompy.projections as proj
+    from ffthompy.tensors import Tensor, DFT, Operator
+    rng = np.random.default_rng(7)
+    for name, physics, Nl, Y, kind in [
+            ('s2_gani_9', 'scalar', [9, 9], [1., 1.], 'GaNi'),
+            ('s2_ga_9', 'scalar', [9, 9], [1., 1.], 'Ga'),
+            ('s2_gani_even_10', 'scalar', [10, 8], [1., 2.], 'GaNi'),
+            ('s2_ga_even_6', 'scalar', [6, 7], [1., 1.], 'Ga'),
+            ('s3_gani_5x7x9', 'scalar', [5, 7, 9], [1., 2., 1.5], 'GaNi'),
+            ('s3_ga_5', 'scalar', [5, 5, 5], [1., 1., 1.], 'Ga'),
+            ('e2_gani_9', 'elasticity', [9, 9], [1., 1.], 'GaNi'),
+            ('e3_gani_5x7x9', 'elasticity', [5, 7, 9], [1., 1., 1.], 'GaNi'),
+            ('e3_ga_5', 'elasticity', [5, 5, 5], [1., 1., 1.], 'Ga')]:
+        N = np.array(Nl)
+        d = N.size
+        Nbar = N if kind == 'GaNi' else 2 * N - 1
+        dv = d if physics == 'scalar' else d * (d + 1) // 2
+        if physics == 'scalar':
+            _, G1, G2 = proj.scalar(N, np.array(Y), NyqNul=True, tensor=True)
+            Gs = [G1, G2]
+        else:
+            _, G1h, G1s, G2h, G2s = proj.elasticity(N, np.array(Y), NyqNul=True)
+            Gs = [G1h + G1s, G2h + G2s]
+        if kind == 'Ga':
+            Gs = [G.enlarge(Nbar) for G in Gs]
+        FN = DFT(name='FN', inverse=False, N=Nbar)
+        FiN = DFT(name='FiN', inverse=True, N=Nbar)
+        B = rng.standard_normal((dv, dv) + tuple(Nbar))
+        Aval = np.einsum('ik...,jk...->ij...', B, B) + np.einsum(
+            'ij,...->ij...', np.eye(dv), np.ones(tuple(Nbar)))
+        A = Tensor(name='A', val=Aval, order=2, N=Nbar, multype=21)
+        x = Tensor(name='x', val=rng.standard_normal((dv,) + tuple(Nbar)), order=1, N=Nbar)
+        arrays = {'A': Aval, 'x': x.val}
+        for ip, G in enumerate(Gs):
+            GN = Operator(name='G', mat=[[FiN, G, FN]])
+            Afun = Operator(name='FiGFA', mat=[[GN, A]])
+            arrays['y%d' % (ip + 1)] = Afun(x).val
+        meta = dict(physics=physics, N=Nl, Y=Y, kind=kind, Nbar=[int(v) for v in Nbar])
+        _save('op_' + name, meta, arrays)
+
+
+if __name__ == '__main__':
+    _install_shim()
+    import warnings
+    warnings.simplefilter('ignore')
+    golden_pickles()
+    run_cases()
+    operator_cases()
