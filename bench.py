@@ -1,0 +1,417 @@
+"""Benchmark of the GB300 Fourier-Galerkin homogenisation (one JSON line).
+
+Workload (default 'spheres509', the 3D scalar configuration): seeded spheres
+of radius 0.08, union volume fraction >= 0.3 on a 255^3 voxel image, phases
+1 / 100, Galerkin with exact integration (grid-based, order 0, P = 255) on the
+509^3 double grid, the 3 unit loads solved together.  One step = one
+time-to-A_H: right-hand sides, batched CG to the tolerance that gives A_H
+within 1e-6 of the FP64-refined value, and the A_H energy assembly, with the
+coefficient resident in HBM.  Fields (4.7 GB per vector) exceed L2.
+
+--impl reference runs the NumPy restatement of the reference (the oracle: the
+reference itself is Python and cannot be installed on the GPU host) on a
+bounded sample of the same workload (Ga N=31 -> 61^3 grid, same sphere
+statistics, 3 loads, a few CG iterations per load), one worker process per
+host core.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (N (solve on 2N-1), P image, L loads, radius, vf, contrast, tol)
+    'spheres509': dict(N=255, P=255, radius=0.08, vf=0.3, contrast=100., tol=1e-3, seed=2026),
+    'spheres125': dict(N=63, P=63, radius=0.08, vf=0.3, contrast=100., tol=1e-3, seed=2026),
+}
+SAMPLE = dict(N=31, P=31, iters=4)    # CPU baseline sample (61^3 grid)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=3)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
+    ap.add_argument('--workload', default='spheres509', choices=sorted(WORKLOADS))
+    ap.add_argument('--precision', default='f32', choices=['f32', 'mixed'])
+    ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--no-fp64', action='store_true')
+    return ap.parse_args()
+
+
+# ----------------------------------------------------------------------------
+# distributed helpers (one process per GPU; replicas of the workload)
+# ----------------------------------------------------------------------------
+def dist_init():
+    ws = int(os.environ.get('WORLD_SIZE', '1'))
+    if ws <= 1:
+        return 0, 1, None
+    import torch.distributed as dist
+    backend = 'nccl' if __import__('torch').cuda.is_available() else 'gloo'
+    dist.init_process_group(backend=backend)
+    return dist.get_rank(), dist.get_world_size(), dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def reduce_max(dist, v):
+    if dist is None:
+        return v
+    import torch
+    dev = 'cuda' if torch.cuda.is_available() and dist.get_backend() == 'nccl' else 'cpu'
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ----------------------------------------------------------------------------
+# workload construction
+# ----------------------------------------------------------------------------
+def image_values(w):
+    from ffthompy_gb300.workloads import spheres_coefficient
+    return spheres_coefficient((w['P'],) * 3, radius=w['radius'], vf=w['vf'],
+                               contrast=w['contrast'], seed=w['seed'])
+
+
+def ga_coefficient(vals, w):
+    """Grid-based Ga coefficient (order 0) on 2N-1, assembled on the GPU."""
+    from ffthompy_gb300.materials import Material
+    N = np.array([w['N']] * 3)
+    mat = Material({'fun': lambda coord, _v=vals: _v, 'Y': np.ones(3), 'order': 0,
+                    'P': np.array([w['P']] * 3)})
+    return mat.get_A_Ga(Nbar=2 * N - 1, primaldual='primal')
+
+
+# ----------------------------------------------------------------------------
+# clocks during the timed region
+# ----------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+             'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+             'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, gpu_index=0):
+        self.f = tempfile.NamedTemporaryFile('w+', suffix='.csv', delete=False)
+        self.gpu = gpu_index
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(['nvidia-smi', '-i', str(self.gpu),
+                                       '--query-gpu=' + self.QUERY, '--format=csv,noheader,nounits',
+                                       '-lms', '200'], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, smax, power, reasons = [], [], [], set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for line in self.f.read().strip().splitlines():
+            parts = [x.strip() for x in line.split(',')]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == 'active':
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        if not sm:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['no samples']}
+        loaded = [s for s, p in zip(sm, power) if p > 0.5 * max(power)] or sm
+        return {'sm_mhz': statistics.median(loaded), 'sm_max_mhz': max(smax),
+                'reasons': sorted(reasons), 'samples': len(sm),
+                'power_w_max': max(power)}
+
+
+# ----------------------------------------------------------------------------
+# CPU baseline: the oracle (NumPy restatement of the reference) on a sample
+# ----------------------------------------------------------------------------
+def _cpu_sample(args):
+    """One worker: Ga spheres sample, 3 loads x iters CG iterations (solver only)."""
+    seed, N, iters = args
+    sys.path.insert(0, ROOT)
+    import oracle
+    from ffthompy_gb300.workloads import spheres_coefficient
+    Nn = np.array([N] * 3)
+    vals = spheres_coefficient((N,) * 3, radius=0.08, vf=0.3, contrast=100., seed=seed)
+    mat = oracle.Material({'fun': lambda c, _v=vals: _v, 'Y': np.ones(3), 'order': 0, 'P': Nn})
+    A = mat.get_A_Ga(2 * Nn - 1, 'primal')
+    G, Ns = oracle.green_operator('scalar', Nn, np.ones(3), 'Ga', 1)
+    Afun = lambda v: oracle.apply_GA(G, A, v)
+    M = int(np.prod(Ns))
+    t = 0.
+    vox_it = 0
+    for l in range(3):
+        E = np.zeros((3,) + tuple(Ns))
+        E[l] = 1.
+        B = Afun(-E)
+        t0 = time.perf_counter()
+        _, info = oracle.cg(Afun, B, np.zeros_like(E), tol=0., maxiter=iters)
+        t += time.perf_counter() - t0
+        vox_it += M * info['kit']
+    return vox_it, t
+
+
+def cpu_baseline():
+    vox_it, t = _cpu_sample((7, SAMPLE['N'], SAMPLE['iters']))
+    return {'value': vox_it / t / 1e6, 'unit': 'Mvoxel-iter/s', 'cores': 1, 'kind': 'port',
+            'sample': 'NumPy restatement of the reference CG (rfftn G o A, solver only), '
+                      'Ga %d^3 -> %d^3 grid, spheres r=0.08 vf=0.3 contrast 100, 3 loads x %d '
+                      'iterations, 1 core' % (SAMPLE['N'], 2 * SAMPLE['N'] - 1, SAMPLE['iters'])}
+
+
+def run_reference(args):
+    rank, world, dist = dist_init()
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context('spawn')
+    jobs = [(100 + i, SAMPLE['N'], SAMPLE['iters']) for i in range(cores)]
+    times = []
+    with ctx.Pool(cores) as pool:
+        for step in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            res = pool.map(_cpu_sample, jobs)
+            # the workers' CG phases run concurrently: aggregate over the slowest
+            dt = max(r[1] for r in res)
+            if step >= args.warmup:
+                times.append((sum(r[0] for r in res), dt))
+    vox = sum(v for v, _ in times)
+    tot = sum(t for _, t in times)
+    value = vox / tot / 1e6
+    w = WORKLOADS[args.workload]
+    out = {
+        'impl': 'reference', 'metric': 'Mvoxel-iter/s', 'value': value, 'unit': 'Mvoxel-iter/s',
+        'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': 1e3 * tot / len(times), 'higher_is_better': True, 'scaling': 'weak',
+        'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
+        'config': {'workload': '%s (sample: Ga %d^3 -> %d^3, one sample per core)'
+                               % (args.workload, SAMPLE['N'], 2 * SAMPLE['N'] - 1),
+                   'grid': [2 * w['N'] - 1] * 3, 'loads': 3},
+        'cpu_baseline': {'value': value, 'unit': 'Mvoxel-iter/s', 'cores': cores, 'kind': 'port',
+                         'sample': '%d processes x (Ga %d^3 -> %d^3 spheres, 3 loads x %d CG '
+                                   'iterations), NumPy restatement of the reference'
+                                   % (cores, SAMPLE['N'], 2 * SAMPLE['N'] - 1, SAMPLE['iters'])},
+        'e2e': {'value': value, 'unit': 'Mvoxel-iter/s', 'h2d_bytes_per_step': 0,
+                'd2h_bytes_per_step': 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+# ----------------------------------------------------------------------------
+# the GPU arm
+# ----------------------------------------------------------------------------
+def run_gpu(args):
+    import torch
+    rank, world, dist = dist_init()
+    torch.cuda.set_device(int(os.environ.get('LOCAL_RANK', rank)))
+    import __graft_entry__
+    __graft_entry__.build()
+    from ffthompy_gb300.engine import GalerkinPlan
+
+    w = WORKLOADS[args.workload]
+    N = w['N']
+    Ns = 2 * N - 1
+    M = Ns ** 3
+    vals = image_values(w)
+    A = ga_coefficient(vals, w)                       # (3,3)+Nbar on the GPU, FP64
+    A_iso = A.data[0, 0].contiguous()
+    extras = {}
+
+    # FP64-refined reference A_H (mixed plan, FP64 outer residual, tight tol)
+    ref = GalerkinPlan((Ns,) * 3, np.ones(3), physics='scalar', nloads=3, band=(N,) * 3,
+                       precision='mixed')
+    ref.set_coefficient(A.data)
+    t0 = time.perf_counter()
+    Xr, info_r = ref.cg(ref.rhs_macro(1), tol=w['tol'] * 1e-3, maxiter=2000)
+    AH_ref = ref.energy(Xr)
+    extras['AH_fp64_refined'] = AH_ref.tolist()
+    extras['fp64_refined_kit'] = info_r['kit']
+    extras['fp64_refined_seconds'] = time.perf_counter() - t0
+    del Xr, ref
+    torch.cuda.empty_cache()
+
+    plan = GalerkinPlan((Ns,) * 3, np.ones(3), physics='scalar', nloads=3, band=(N,) * 3,
+                        precision=args.precision)
+    plan.set_coefficient(A.data)
+    tol = w['tol']
+
+    def step():
+        B = plan.rhs_macro(1)
+        X, info = plan.cg(B, tol=tol, maxiter=2000, log_rows=1)
+        AH = plan.energy(X)
+        return AH, info
+
+    for _ in range(args.warmup):
+        AH, info = step()
+    torch.cuda.synchronize()
+    barrier(dist)
+    launches0 = plan.launches()
+    plan.profile(True)
+    clk = ClockSampler(torch.cuda.current_device())
+    clk.start()
+    stream = torch.cuda.current_stream()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    kits = []
+    for _ in range(args.steps):
+        AH, info = step()
+        kits.append(sum(info['kit']))
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    barrier(dist)
+    ms = ev0.elapsed_time(ev1)
+    ms = reduce_max(dist, ms)
+    launches = plan.launches() - launches0
+    prof = plan.profile_read()
+    plan.profile(False)
+    vox_it = M * sum(kits) * world
+    value = vox_it / (ms / 1e3) / 1e6
+    AH_err = float(np.abs(AH - AH_ref).max() / np.abs(AH_ref).max())
+
+    # roofline of the dominant kernel (largest total time in the timed region)
+    import json as _json
+    peaks = {}
+    try:
+        peaks = _json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json')))
+    except (OSError, ValueError):
+        pass
+    peak = float(peaks.get('hbm_gbs', 6800.0))
+    peak_src = 'measured' if 'hbm_gbs' in peaks else 'fallback'
+    top = max(prof.items(), key=lambda kv: kv[1]['ms'])
+    tname, t = top
+    per_launch_s = t['ms'] / 1e3 / max(1, t['launches'])
+    achieved = t['bytes_per_launch'] / per_launch_s / 1e9
+    kernels = {k: {'launches': v['launches'], 'ms_total': round(v['ms'], 3),
+                   'share': round(v['ms'] / max(1e-9, sum(x['ms'] for x in prof.values())), 4),
+                   'GBps': round(v['bytes_per_launch'] / (v['ms'] / 1e3 / max(1, v['launches']))
+                                 / 1e9, 1)}
+               for k, v in sorted(prof.items(), key=lambda kv: -kv[1]['ms'])}
+    traffic = None
+    tf = os.path.join(ROOT, 'profiles', 'traffic.json')
+    if os.path.exists(tf):
+        try:
+            traffic = _json.load(open(tf)).get(tname, {}).get('bytes_per_launch')
+        except (OSError, ValueError):
+            traffic = None
+    roofline = {'bound': 'hbm', 'achieved': round(achieved, 1), 'peak': peak, 'unit': 'GB/s',
+                'frac': round(achieved / peak, 4), 'traffic': traffic, 'kernel': tname,
+                'peak_source': peak_src + ' hbm_gbs'}
+
+    # FP64 GPU CG (plain form) for the mixed-vs-FP64 ratio: bounded iterations
+    if not args.no_fp64:
+        p64 = GalerkinPlan((Ns,) * 3, np.ones(3), physics='scalar', nloads=3, band=(N,) * 3,
+                           precision='f64')
+        p64.set_coefficient(A.data)
+        B64 = p64.rhs_macro(1)
+        k64 = 3
+        p64.cg(B64, tol=0., maxiter=1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        p64.cg(B64, tol=0., maxiter=k64)
+        torch.cuda.synchronize()
+        it64 = (time.perf_counter() - t0) / k64
+        per_it = ms / 1e3 / args.steps / max(1, max(info['kit']))
+        extras['fp64_seconds_per_iteration'] = it64
+        extras['fp64_time_to_AH_s_extrapolated'] = it64 * max(info['kit'])
+        extras['mixed_seconds_per_iteration'] = per_it
+        extras['speedup_vs_fp64_gpu'] = it64 / per_it
+        del p64, B64
+        torch.cuda.empty_cache()
+
+    # end to end through the host-buffer C-ABI entry point
+    host_A = torch.empty(A_iso.shape, dtype=torch.float64, pin_memory=True)
+    host_A.copy_(A_iso)
+    A_host = host_A.numpy()
+    e2e_plan = GalerkinPlan((Ns,) * 3, np.ones(3), physics='scalar', nloads=3, band=(N,) * 3,
+                            precision=args.precision)
+    from ffthompy_gb300 import _lib
+    e2e_plan.homogenize_host(packed=A_host, kind=_lib.FHP_COEF_ISO, proj=1, tol=tol,
+                             maxiter=2000)   # warm
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, 2))
+    kit_e = 0
+    for _ in range(e2e_steps):
+        AHe, kit, _, _ = e2e_plan.homogenize_host(packed=A_host, kind=_lib.FHP_COEF_ISO, proj=1,
+                                                  tol=tol, maxiter=2000)
+        kit_e += sum(kit)
+    e2e_s = (time.perf_counter() - t0)
+    e2e_s = reduce_max(dist, e2e_s)
+    e2e = {'value': M * kit_e * world / e2e_s / 1e6, 'unit': 'Mvoxel-iter/s',
+           'h2d_bytes_per_step': int(A_host.nbytes), 'd2h_bytes_per_step': 9 * 8,
+           'seconds_per_step': e2e_s / e2e_steps}
+    extras['AH_e2e_rel_diff'] = float(np.abs(AHe - AH).max() / np.abs(AH).max())
+    del e2e_plan
+
+    if rank != 0:
+        return
+    out = {
+        'metric': 'Mvoxel-iter/s', 'value': round(value, 2), 'unit': 'Mvoxel-iter/s',
+        'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': round(ms / args.steps, 3), 'higher_is_better': True, 'scaling': 'weak',
+        'vs_baseline': None, 'dtype': 'f32' if args.precision == 'f32' else 'f64+f32',
+        'data': 'synthetic',
+        'config': {'workload': '%s: 3D scalar Ga, spheres r=%.2f vf>=%.1f contrast %g, image '
+                               '%d^3 -> %d^3 grid, 3 loads batched, CG tol %g (A_H within 1e-6)'
+                               % (args.workload, w['radius'], w['vf'], w['contrast'], w['P'],
+                                  Ns, w['tol']),
+                   'grid': [Ns] * 3, 'loads': 3, 'precision': args.precision,
+                   'l2': 'inputs larger than L2 (one field vector %.1f GB)'
+                         % (3 * 3 * M * (4 if args.precision == 'f32' else 8) / 1e9)},
+        'time_to_AH_s': round(ms / 1e3 / args.steps, 4),
+        'cg_iterations': info['kit'],
+        'AH': AH.tolist(), 'AH_rel_err_vs_fp64': AH_err,
+        'roofline': roofline,
+        'kernels': kernels,
+        'gpu_launches': int(launches),
+        'clocks': clocks,
+        'e2e': e2e,
+    }
+    out.update(extras)
+    if not args.no_cpu_baseline:
+        out['cpu_baseline'] = cpu_baseline()
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == 'reference':
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == '__main__':
+    main()

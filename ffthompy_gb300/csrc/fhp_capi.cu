@@ -1,0 +1,438 @@
+// extern "C" entry points of libffthompy_gb300.so (declared in
+// include/ffthompy_gb300.h).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/ffthompy_gb300.h"
+#include "fhp_engine.h"
+
+struct fhp_plan_s {
+  std::unique_ptr<fhp::EngineBase> eng;  // FP64 (F64, MIXED) or FP32 (F32)
+  std::unique_ptr<fhp::EngineBase> lo;   // MIXED: FP32 engine of the inner CG
+  double eta = 1e-4;                     // MIXED: inner relative tolerance floor
+  int max_outer = 30;
+};
+
+namespace {
+
+int bad(const char* msg) {
+  fhp::set_error(msg);
+  return FHP_BAD_ARG;
+}
+
+cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+int cuda_status(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return FHP_OK;
+  fhp::set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? FHP_OOM : FHP_CUDA;
+}
+
+
+// Mixed-precision CG by iterative refinement: the residual r = b - A x is
+// formed with the FP64 operator, each load's residual is normalised and solved
+// approximately by the FP32 CG (FP64 reductions) to relative tolerance eta,
+// and the correction is accumulated in FP64.  Stops per load when
+// sqrt(<r,r>) <= tol (the reference's absolute test, solver.py:120-123), when
+// the summed inner iterations reach maxiter, or when an outer step stops
+// reducing the residual.
+int cg_mixed(fhp_plan_s& p, int proj, const void* b, const void* x0, double tol, int maxiter,
+             void* xv, fhp::SolveResult& res, int log_rows, cudaStream_t s) {
+  fhp::EngineBase& hi = *p.eng;
+  fhp::EngineBase& lo = *p.lo;
+  const int L = hi.loads();
+  const double M = (double)hi.voxels();
+  const size_t n = (size_t)L * hi.dv() * hi.voxels();
+  double* x = static_cast<double*>(xv);
+  void *ax = nullptr, *r = nullptr, *r32 = nullptr, *d32 = nullptr;
+  int st = cuda_status(cudaMallocAsync(&ax, n * 8, s), "alloc");
+  if (st == FHP_OK) st = cuda_status(cudaMallocAsync(&r, n * 8, s), "alloc");
+  if (st == FHP_OK) st = cuda_status(cudaMallocAsync(&r32, n * 4, s), "alloc");
+  if (st == FHP_OK) st = cuda_status(cudaMallocAsync(&d32, n * 4, s), "alloc");
+  std::vector<double> sumsq(L), norm(L), sc_in(L), sc_out(L);
+  std::vector<int> kit(L, 0), status(L, 0), active(L, 1);
+  res.res_log.assign((size_t)std::max(1, log_rows) * L, 0.0);
+  if (st == FHP_OK) {
+    if (x0) {
+      st = cuda_status(cudaMemcpyAsync(x, x0, n * 8, cudaMemcpyDeviceToDevice, s), "copy");
+      if (st == FHP_OK) st = hi.apply(proj, x, ax, s);
+    } else {
+      st = cuda_status(cudaMemsetAsync(x, 0, n * 8, s), "memset");
+      if (st == FHP_OK) st = cuda_status(cudaMemsetAsync(ax, 0, n * 8, s), "memset");
+    }
+  }
+  if (st == FHP_OK) st = hi.residual(b, ax, r, sumsq.data(), s);
+  for (int l = 0; l < L; ++l) {
+    norm[l] = std::sqrt(sumsq[l] / M);
+    res.res_log[l] = norm[l];
+    if (!std::isfinite(norm[l])) { status[l] = FHP_NONFINITE; active[l] = 0; }
+    if (!(norm[l] > tol && maxiter > 0)) active[l] = 0;
+  }
+  for (int outer = 0; st == FHP_OK && outer < p.max_outer; ++outer) {
+    int any = 0, room = maxiter;
+    double eta = 0.5;
+    for (int l = 0; l < L; ++l) {
+      if (!active[l]) continue;
+      any = 1;
+      room = std::min(room, maxiter - kit[l]);
+      eta = std::min(eta, std::max(p.eta, 0.5 * tol / norm[l]));
+    }
+    if (!any || room <= 0) break;
+    for (int l = 0; l < L; ++l) {
+      sc_in[l] = active[l] ? 1.0 / norm[l] : 0.0;
+      sc_out[l] = active[l] ? norm[l] : 0.0;
+    }
+    if ((st = lo.scale_from64(static_cast<const double*>(r), sc_in.data(), r32, s)) != FHP_OK) break;
+    fhp::SolveResult in;
+    if ((st = lo.cg_solve(proj, r32, nullptr, eta, room, d32, in, 1, s)) != FHP_OK) break;
+    if ((st = hi.add_scaled_to64(d32, sc_out.data(), x, s)) != FHP_OK) break;
+    if ((st = hi.apply(proj, x, ax, s)) != FHP_OK) break;
+    if ((st = hi.residual(b, ax, r, sumsq.data(), s)) != FHP_OK) break;
+    for (int l = 0; l < L; ++l) {
+      if (!active[l]) continue;
+      const double prev = norm[l];
+      kit[l] += in.kit[l];
+      norm[l] = std::sqrt(sumsq[l] / M);
+      if (kit[l] < log_rows) res.res_log[(size_t)kit[l] * L + l] = norm[l];
+      if (!std::isfinite(norm[l])) { status[l] = FHP_NONFINITE; active[l] = 0; continue; }
+      if (norm[l] <= tol) { active[l] = 0; continue; }
+      if (kit[l] >= maxiter || in.kit[l] == 0 || norm[l] > 0.5 * prev) {
+        status[l] = FHP_NONCONVERGED;  // stagnation of the refinement
+        active[l] = 0;
+      }
+    }
+  }
+  for (void* q : {ax, r, r32, d32})
+    if (q) cudaFreeAsync(q, s);
+  if (st == FHP_OK) st = cuda_status(cudaStreamSynchronize(s), "sync");
+  res.kit = kit;
+  res.norm_res.resize(L);
+  res.status = status;
+  res.iterations_run = 0;
+  for (int l = 0; l < L; ++l) {
+    res.norm_res[l] = kit[l] == 0 ? 0.0 : norm[l];
+    if (status[l] == 0 && norm[l] > tol && kit[l] > 0) res.status[l] = FHP_NONCONVERGED;
+    res.iterations_run = std::max(res.iterations_run, kit[l]);
+  }
+  return st;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fhp_version(void) { return 100; }
+
+const char* fhp_status_string(int status) {
+  switch (status) {
+    case FHP_OK: return "ok";
+    case FHP_NONCONVERGED: return "not converged (maxiter reached)";
+    case FHP_BREAKDOWN: return "CG breakdown (<P,AP> <= 0)";
+    case FHP_NONFINITE: return "non-finite value in a reduction";
+    case FHP_TIMEOUT: return "timeout";
+    case FHP_BAD_ARG: return "bad argument";
+    case FHP_OOM: return "out of device memory";
+    case FHP_CUDA: return "CUDA error";
+    default: return "unknown status";
+  }
+}
+
+const char* fhp_last_error(void) { return fhp::last_error(); }
+
+int fhp_plan_create(fhp_plan* out, int dim, const int* n, const int* n_band, const double* Y,
+                    int physics, int nloads, double g_scale, int precision) {
+  if (!out) return bad("out is NULL");
+  *out = nullptr;
+  if (dim != 2 && dim != 3) return bad("dim must be 2 or 3");
+  if (!n || !n_band || !Y) return bad("n, n_band and Y are required");
+  if (physics != FHP_SCALAR && physics != FHP_ELASTICITY) return bad("unknown physics");
+  if (!(g_scale > 0) || !std::isfinite(g_scale)) return bad("g_scale must be positive");
+  fhp::PlanConfig cfg;
+  cfg.dim = dim;
+  for (int i = 0; i < dim; ++i) {
+    if (n[i] < 1 || n_band[i] < 1 || n_band[i] > n[i]) return bad("bad grid sizes");
+    if (n[i] > 4096) return bad("grid size per axis must be <= 4096");
+    cfg.N[i] = n[i];
+    cfg.band[i] = n_band[i];
+    cfg.Y[i] = Y[i];
+  }
+  cfg.physics = physics;
+  cfg.nloads = nloads;
+  cfg.scale = g_scale;
+  int st = FHP_OK;
+  std::unique_ptr<fhp::EngineBase> e, lo;
+  if (precision == FHP_F64 || precision == FHP_MIXED) e = fhp::make_engine_f64(cfg, &st);
+  else if (precision == FHP_F32) e = fhp::make_engine_f32(cfg, &st);
+  else return bad("unknown precision");
+  if (!e) return st == FHP_OK ? FHP_CUDA : st;
+  if (precision == FHP_MIXED) {
+    lo = fhp::make_engine_f32(cfg, &st);
+    if (!lo) return st == FHP_OK ? FHP_CUDA : st;
+  }
+  auto* p = new (std::nothrow) fhp_plan_s;
+  if (!p) return FHP_OOM;
+  p->eng = std::move(e);
+  p->lo = std::move(lo);
+  *out = p;
+  return FHP_OK;
+}
+
+int fhp_plan_set_refinement(fhp_plan plan, double eta, int max_outer) {
+  if (!plan || !plan->lo) return bad("refinement parameters apply to FHP_MIXED plans");
+  if (!(eta > 0 && eta < 1) || max_outer < 1) return bad("need 0 < eta < 1, max_outer >= 1");
+  plan->eta = eta;
+  plan->max_outer = max_outer;
+  return FHP_OK;
+}
+
+int fhp_plan_destroy(fhp_plan plan) {
+  delete plan;
+  return FHP_OK;
+}
+
+int fhp_plan_query(fhp_plan plan, long long* voxels, int* components, int* loads,
+                   int* elem_bytes) {
+  if (!plan) return bad("plan is NULL");
+  if (voxels) *voxels = plan->eng->voxels();
+  if (components) *components = plan->eng->dv();
+  if (loads) *loads = plan->eng->loads();
+  if (elem_bytes) *elem_bytes = (int)plan->eng->elem_size();
+  return FHP_OK;
+}
+
+int fhp_set_coefficient(fhp_plan plan, int kind, const double* values, int on_device,
+                        void* stream) {
+  if (!plan || !values) return bad("plan and values are required");
+  int st = plan->eng->set_coefficient(kind, values, on_device != 0, as_stream(stream));
+  if (st == FHP_OK && plan->lo)
+    st = plan->lo->set_coefficient(kind, values, on_device != 0, as_stream(stream));
+  return st;
+}
+
+int fhp_apply(fhp_plan plan, int proj, const void* x, void* y, void* stream) {
+  if (!plan || !x || !y) return bad("plan, x and y are required");
+  if (proj != 1 && proj != 2) return bad("proj must be 1 or 2");
+  return plan->eng->apply(proj, x, y, as_stream(stream));
+}
+
+int fhp_rhs_macro(fhp_plan plan, int proj, void* b, void* stream) {
+  if (!plan || !b) return bad("plan and b are required");
+  if (proj != 1 && proj != 2) return bad("proj must be 1 or 2");
+  return plan->eng->rhs_macro(proj, b, as_stream(stream));
+}
+
+int fhp_cg_solve(fhp_plan plan, int proj, const void* b, const void* x0, double tol,
+                 int maxiter, void* x, int* kit, double* norm_res, int* status,
+                 double* res_log, int log_rows, void* stream) {
+  if (!plan || !b || !x) return bad("plan, b and x are required");
+  if (proj != 1 && proj != 2) return bad("proj must be 1 or 2");
+  if (maxiter < 0) return bad("maxiter must be >= 0");
+  if (!(tol >= 0)) return bad("tol must be >= 0");
+  fhp::SolveResult r;
+  const int rows = res_log ? std::max(1, log_rows) : 1;
+  int st = plan->lo ? cg_mixed(*plan, proj, b, x0, tol, maxiter, x, r, rows, as_stream(stream))
+                    : plan->eng->cg_solve(proj, b, x0, tol, maxiter, x, r, rows,
+                                          as_stream(stream));
+  if (st != FHP_OK && r.kit.empty()) return st;
+  const int L = plan->eng->loads();
+  for (int l = 0; l < L && l < (int)r.kit.size(); ++l) {
+    if (kit) kit[l] = r.kit[l];
+    if (norm_res) norm_res[l] = r.norm_res[l];
+    if (status) status[l] = r.status[l];
+  }
+  if (res_log && !r.res_log.empty())
+    std::memcpy(res_log, r.res_log.data(),
+                std::min<size_t>((size_t)rows * L, r.res_log.size()) * sizeof(double));
+  return st;
+}
+
+int fhp_energy_matrix(fhp_plan plan, const void* X, int add_macro, double* AH, void* stream) {
+  if (!plan || !X || !AH) return bad("plan, X and AH are required");
+  return plan->eng->energy(X, add_macro, AH, as_stream(stream));
+}
+
+int fhp_fourier_interp(fhp_plan src, fhp_plan dst, const void* x_src, void* x_dst,
+                       void* stream) {
+  if (!src || !dst || !x_src || !x_dst) return bad("plans and fields are required");
+  const fhp::PlanConfig& a = src->eng->config();
+  const fhp::PlanConfig& b = dst->eng->config();
+  if (a.dim != b.dim || a.physics != b.physics || a.nloads != b.nloads ||
+      src->eng->precision() != dst->eng->precision())
+    return bad("plans differ in dim, physics, loads or precision");
+  for (int i = 0; i < a.dim; ++i)
+    if (b.N[i] < a.N[i]) return bad("destination grid must not be smaller");
+  cudaStream_t s = as_stream(stream);
+  const size_t es = 2 * src->eng->elem_size();
+  void* ss = nullptr;
+  void* sd = nullptr;
+  int st = cuda_status(cudaMallocAsync(&ss, src->eng->spectrum_elems() * es, s), "alloc");
+  if (st != FHP_OK) return st;
+  st = cuda_status(cudaMallocAsync(&sd, dst->eng->spectrum_elems() * es, s), "alloc");
+  if (st == FHP_OK) st = src->eng->forward_spectrum(x_src, ss, s);
+  if (st == FHP_OK) st = dst->eng->pad_spectrum(ss, a, sd, s);
+  double pn = 1.0;
+  for (int i = 0; i < a.dim; ++i) pn *= a.N[i];
+  if (st == FHP_OK) st = dst->eng->inverse_spectrum(sd, x_dst, 1.0 / pn, s);
+  if (sd) cudaFreeAsync(sd, s);
+  if (ss) cudaFreeAsync(ss, s);
+  return st;
+}
+
+int fhp_homogenize_host(fhp_plan plan, int proj, int coef_kind, const double* coef_host,
+                        double tol, int maxiter, double* AH_host, int* kit_host,
+                        double* norm_res_host, void* x_host, void* stream) {
+  if (!plan || !coef_host || !AH_host) return bad("plan, coef_host and AH_host are required");
+  cudaStream_t s = as_stream(stream);
+  fhp::EngineBase& e = *plan->eng;
+  int st = fhp_set_coefficient(plan, coef_kind, coef_host, 0, stream);
+  if (st != FHP_OK) return st;
+  const size_t bytes = (size_t)e.loads() * e.dv() * e.voxels() * e.elem_size();
+  void* b = nullptr;
+  void* x = nullptr;
+  st = cuda_status(cudaMallocAsync(&b, bytes, s), "alloc");
+  if (st == FHP_OK) st = cuda_status(cudaMallocAsync(&x, bytes, s), "alloc");
+  if (st == FHP_OK) st = e.rhs_macro(proj, b, s);
+  fhp::SolveResult r;
+  if (st == FHP_OK)
+    st = plan->lo ? cg_mixed(*plan, proj, b, nullptr, tol, maxiter, x, r, 1, s)
+                  : e.cg_solve(proj, b, nullptr, tol, maxiter, x, r, 1, s);
+  if (st == FHP_OK) st = e.energy(x, 1, AH_host, s);
+  if (st == FHP_OK && x_host)
+    st = cuda_status(cudaMemcpyAsync(x_host, x, bytes, cudaMemcpyDeviceToHost, s), "copy");
+  if (st == FHP_OK) st = cuda_status(cudaStreamSynchronize(s), "sync");
+  const int L = e.loads();
+  for (int l = 0; l < L && l < (int)r.kit.size(); ++l) {
+    if (kit_host) kit_host[l] = r.kit[l];
+    if (norm_res_host) norm_res_host[l] = r.norm_res[l];
+  }
+  if (x) cudaFreeAsync(x, s);
+  if (b) cudaFreeAsync(b, s);
+  return st;
+}
+
+int fhp_fft_plan_create(fhp_plan* out, int dim, const int* n, int ncomp, int precision) {
+  if (!out) return bad("out is NULL");
+  *out = nullptr;
+  if (dim != 2 && dim != 3) return bad("dim must be 2 or 3");
+  if (!n) return bad("n is required");
+  if (ncomp < 1 || ncomp > 6) return bad("ncomp must be in 1..6");
+  fhp::PlanConfig cfg;
+  cfg.dim = dim;
+  for (int i = 0; i < dim; ++i) {
+    if (n[i] < 1 || n[i] > 4096) return bad("bad grid sizes");
+    cfg.N[i] = n[i];
+    cfg.band[i] = n[i];
+    cfg.Y[i] = 1.0;
+  }
+  cfg.physics = -1;
+  cfg.ncomp = ncomp;
+  cfg.nloads = 1;
+  int st = FHP_OK;
+  std::unique_ptr<fhp::EngineBase> e;
+  if (precision == FHP_F64) e = fhp::make_engine_f64(cfg, &st);
+  else if (precision == FHP_F32) e = fhp::make_engine_f32(cfg, &st);
+  else return bad("unknown precision");
+  if (!e) return st == FHP_OK ? FHP_CUDA : st;
+  auto* p = new (std::nothrow) fhp_plan_s;
+  if (!p) return FHP_OOM;
+  p->eng = std::move(e);
+  *out = p;
+  return FHP_OK;
+}
+
+int fhp_ga_grid_coefficient(fhp_plan plan_img, fhp_plan plan_out, const void* image,
+                            const int* src_index, const double* weights, void* out,
+                            void* stream) {
+  if (!plan_img || !plan_out || !image || !src_index || !weights || !out)
+    return bad("plans, image, tables and out are required");
+  const fhp::PlanConfig& a = plan_img->eng->config();
+  const fhp::PlanConfig& b = plan_out->eng->config();
+  if (a.dim != b.dim || plan_img->eng->dv() * plan_img->eng->loads() !=
+                            plan_out->eng->dv() * plan_out->eng->loads() ||
+      plan_img->eng->precision() != plan_out->eng->precision())
+    return bad("plans differ in dim, field count or precision");
+  cudaStream_t s = as_stream(stream);
+  int nt = 0;
+  for (int i = 0; i < b.dim; ++i) nt += b.N[i];
+  // tables in the padded 3-axis order used by the kernels (n0 = 1 for 2D)
+  std::vector<int> idx;
+  std::vector<double> w;
+  if (b.dim == 2) { idx.push_back(0); w.push_back(1.0); }
+  idx.insert(idx.end(), src_index, src_index + nt);
+  w.insert(w.end(), weights, weights + nt);
+  for (int i = 0; i < b.dim; ++i) {
+    int off = 0;
+    for (int j = 0; j < i; ++j) off += b.N[j];
+    for (int t = 0; t < b.N[i]; ++t) {
+      const int v = src_index[off + t];
+      if (v < 0 || v >= a.N[i]) return bad("source index out of range");
+    }
+  }
+  const size_t es = 2 * plan_img->eng->elem_size();
+  void *ss = nullptr, *sd = nullptr, *di = nullptr, *dw = nullptr;
+  int st = cuda_status(cudaMallocAsync(&ss, plan_img->eng->spectrum_elems() * es, s), "alloc");
+  if (st == FHP_OK) st = cuda_status(cudaMallocAsync(&sd, plan_out->eng->spectrum_elems() * es, s), "alloc");
+  if (st == FHP_OK) st = cuda_status(cudaMallocAsync(&di, idx.size() * sizeof(int), s), "alloc");
+  if (st == FHP_OK) st = cuda_status(cudaMallocAsync(&dw, w.size() * sizeof(double), s), "alloc");
+  if (st == FHP_OK)
+    st = cuda_status(cudaMemcpyAsync(di, idx.data(), idx.size() * sizeof(int),
+                                     cudaMemcpyHostToDevice, s), "copy");
+  if (st == FHP_OK)
+    st = cuda_status(cudaMemcpyAsync(dw, w.data(), w.size() * sizeof(double),
+                                     cudaMemcpyHostToDevice, s), "copy");
+  if (st == FHP_OK) st = plan_img->eng->forward_spectrum(image, ss, s);
+  if (st == FHP_OK)
+    st = plan_out->eng->ga_gather(ss, a, static_cast<const int*>(di),
+                                  static_cast<const double*>(dw), sd, s);
+  if (st == FHP_OK) st = plan_out->eng->inverse_spectrum(sd, out, 1.0, s);
+  if (st == FHP_OK) st = cuda_status(cudaStreamSynchronize(s), "sync");
+  for (void* p : {ss, sd, di, dw})
+    if (p) cudaFreeAsync(p, s);
+  return st;
+}
+
+int fhp_profile_enable(fhp_plan plan, int enable) {
+  if (!plan) return bad("plan is NULL");
+  for (fhp::EngineBase* e : {plan->eng.get(), plan->lo.get()}) {
+    if (!e) continue;
+    e->prof.reset();
+    e->prof.on = enable != 0;
+  }
+  return FHP_OK;
+}
+
+int fhp_profile_read(fhp_plan plan, int max_kinds, char* names, long long* launches,
+                     double* total_ms, double* bytes_per_launch, int* nkinds) {
+  if (!plan || !nkinds) return bad("plan and nkinds are required");
+  int k = 0;
+  for (fhp::EngineBase* e : {plan->eng.get(), plan->lo.get()}) {
+    if (!e) continue;
+    e->prof.collect();
+    for (const fhp::ProfEntry& p : e->prof.kinds) {
+      if (k < max_kinds) {
+        if (names) {
+          std::strncpy(names + 64 * k, p.name.c_str(), 63);
+          names[64 * k + 63] = 0;
+        }
+        if (launches) launches[k] = p.launches;
+        if (total_ms) total_ms[k] = p.ms;
+        if (bytes_per_launch) bytes_per_launch[k] = p.bytes;
+      }
+      ++k;
+    }
+  }
+  *nkinds = k;
+  return FHP_OK;
+}
+
+long long fhp_plan_launches(fhp_plan plan) {
+  if (!plan) return 0;
+  return plan->eng->launches + (plan->lo ? plan->lo->launches : 0);
+}
+
+}  // extern "C"

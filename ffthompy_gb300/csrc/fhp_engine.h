@@ -1,0 +1,123 @@
+// Host-side engine of the Fourier-Galerkin operator: one grid, one precision.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <complex>
+#include <memory>
+#include <string>
+#include <vector>
+
+namespace fhp {
+
+// status codes (match include/ffthompy_gb300.h)
+enum Status {
+  ST_OK = 0,
+  ST_NONCONVERGED = 1,
+  ST_BREAKDOWN = 2,
+  ST_NONFINITE = 3,
+  ST_TIMEOUT = 4,
+  ST_BAD_ARG = 5,
+  ST_OOM = 6,
+  ST_CUDA = 7,
+};
+
+void set_error(const std::string& msg);
+const char* last_error();
+
+// 1D line plan built on the host (long double tables).
+struct LinePlanHost {
+  int n = 0, nf = 0, blue = 0, nst = 0;
+  std::vector<int> rad;                          // core radices
+  std::vector<int> pos;                          // n entries (direct lines)
+  std::vector<std::complex<long double>> tw;     // nf
+  std::vector<std::complex<long double>> chirp;  // n   (Bluestein)
+  std::vector<std::complex<long double>> bhat;   // nf  (Bluestein, digit-reversed, / nf)
+};
+bool build_line_plan(int n, LinePlanHost& out);
+bool factor_radices(int n, std::vector<int>& rad);
+
+struct PlanConfig {
+  int dim = 3;
+  int N[3] = {1, 1, 1};      // solve grid (real axes)
+  int band[3] = {1, 1, 1};   // grid whose band |k| <= (Nodd-1)/2 carries the projection
+  double Y[3] = {1, 1, 1};
+  int physics = 0;           // 0 scalar, 1 elasticity, -1 plain FFT plan of ncomp fields
+  int ncomp = 1;             // fields of a plain FFT plan
+  int nloads = 1;
+  double scale = 1.0;        // Ga: prod(2N-1)/prod(N)
+};
+
+struct SolveResult {
+  std::vector<int> kit;
+  std::vector<double> norm_res;
+  std::vector<int> status;
+  std::vector<double> res_log;  // (log_rows) x L
+  int iterations_run = 0;       // max kit
+};
+
+// Per-kernel CUDA-event timing of the passes (off unless enabled).
+struct ProfEntry {
+  std::string name;
+  long long launches = 0;
+  double ms = 0.0;
+  double bytes = 0.0;  // algorithmic bytes per launch
+};
+
+struct Profiler {
+  bool on = false;
+  struct Rec { int kind; cudaEvent_t a, b; };
+  std::vector<Rec> recs;
+  std::vector<ProfEntry> kinds;
+  std::vector<cudaEvent_t> pool;
+  int kind_of(const std::string& name, double bytes);
+  void begin(int kind, cudaStream_t s);
+  void end(cudaStream_t s);
+  void collect();   // synchronises the recorded events
+  void reset();
+  ~Profiler();
+};
+
+class EngineBase {
+ public:
+  virtual ~EngineBase() = default;
+  Profiler prof;
+  virtual int precision() const = 0;  // 0: f64, 1: f32
+  virtual long long voxels() const = 0;
+  virtual int dv() const = 0;
+  virtual int loads() const = 0;
+  virtual size_t elem_size() const = 0;
+  // coefficient (c values per voxel, component-major, f64 on host or device)
+  virtual int set_coefficient(int kind, const double* values, bool on_device, cudaStream_t s) = 0;
+  virtual int coef_kind() const = 0;
+  virtual int apply(int proj, const void* x, void* y, cudaStream_t s) = 0;
+  virtual int rhs_macro(int proj, void* b, cudaStream_t s) = 0;
+  virtual int cg_solve(int proj, const void* b, const void* x0, double tol, int maxiter, void* x,
+                       SolveResult& res, int log_cap, cudaStream_t s) = 0;
+  virtual int energy(const void* X, int add_macro, double* AH, cudaStream_t s) = 0;
+  // forward r2c spectrum of X (all comps) into `spec` (natural order, half spectrum)
+  virtual int forward_spectrum(const void* x, void* spec, cudaStream_t s) = 0;
+  // inverse of a half spectrum into x with scale
+  virtual int inverse_spectrum(void* spec, void* x, double scale, cudaStream_t s) = 0;
+  virtual size_t spectrum_elems() const = 0;
+  virtual const PlanConfig& config() const = 0;
+  virtual int pad_spectrum(const void* spec_src, const PlanConfig& src, void* spec_dst,
+                           cudaStream_t s) = 0;
+  // spec_dst (this grid) = weights * gathered source spectrum (Ga grid-based coefficient)
+  virtual int ga_gather(const void* spec_src, const PlanConfig& src, const int* d_index,
+                        const double* d_weight, void* spec_dst, cudaStream_t s) = 0;
+  // refinement helpers: r = b - ax with per-load sum r^2 (host); dst = s_l*src64;
+  // x64 += s_l*d
+  virtual int residual(const void* b, const void* ax, void* r, double* sumsq,
+                       cudaStream_t s) = 0;
+  virtual int scale_from64(const double* src, const double* scale, void* dst,
+                           cudaStream_t s) = 0;
+  virtual int add_scaled_to64(const void* d, const double* scale, double* x,
+                              cudaStream_t s) = 0;
+  // kernel launch count of the last call (instrumentation)
+  long long launches = 0;
+};
+
+std::unique_ptr<EngineBase> make_engine_f64(const PlanConfig& cfg, int* status);
+std::unique_ptr<EngineBase> make_engine_f32(const PlanConfig& cfg, int* status);
+
+}  // namespace fhp

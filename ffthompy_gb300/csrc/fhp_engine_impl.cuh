@@ -1,0 +1,615 @@
+// Engine<R>: device buffers, launch configuration and the call sequences of
+// the operator, CG, energy and spectral interpolation.  Instantiated for
+// double (fhp_engine_f64.cu) and float (fhp_engine_f32.cu).
+#pragma once
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fhp_engine.h"
+#include "fhp_kernels.cuh"
+
+namespace fhp {
+
+#define FHP_CHECK(call)                                                              \
+  do {                                                                               \
+    cudaError_t _e = (call);                                                         \
+    if (_e != cudaSuccess) {                                                         \
+      set_error(std::string("CUDA error: ") + cudaGetErrorString(_e) + " at " +     \
+                __FILE__ + ":" + std::to_string(__LINE__));                          \
+      return _e == cudaErrorMemoryAllocation ? ST_OOM : ST_CUDA;                     \
+    }                                                                                \
+  } while (0)
+
+#define FHP_LAUNCHED()                                                               \
+  do {                                                                               \
+    ++launches;                                                                      \
+    cudaError_t _e = cudaGetLastError();                                             \
+    if (_e != cudaSuccess) {                                                         \
+      set_error(std::string("kernel launch: ") + cudaGetErrorString(_e) + " at " +  \
+                __FILE__ + ":" + std::to_string(__LINE__));                          \
+      return ST_CUDA;                                                                \
+    }                                                                                \
+  } while (0)
+
+constexpr int kThreads = 256;
+constexpr size_t kSmemBudget = 96 * 1024;   // two CTAs per SM
+constexpr size_t kSmemMax = 227 * 1024;
+constexpr int kTargetElems = 8192;          // complex elements per CTA
+
+template <typename T>
+static int set_smem_attr(T* kernel) {
+  cudaError_t e = cudaFuncSetAttribute(reinterpret_cast<const void*>(kernel),
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)kSmemMax);
+  if (e != cudaSuccess) {
+    set_error(std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
+    return ST_CUDA;
+  }
+  return ST_OK;
+}
+
+template <typename R>
+struct DevLine {
+  LineDev<R> dev{};
+  void* mem = nullptr;
+};
+
+template <typename R>
+class Engine final : public EngineBase {
+ public:
+  explicit Engine(const PlanConfig& cfg) : cfg_(cfg) {}
+  ~Engine() override { release(); }
+
+  int init() {
+    const int d = cfg_.dim;
+    if (d != 2 && d != 3) { set_error("dim must be 2 or 3"); return ST_BAD_ARG; }
+    for (int i = 0; i < d; ++i)
+      if (cfg_.N[i] < 1 || cfg_.band[i] < 1 || !(cfg_.Y[i] > 0)) {
+        set_error("grid sizes and cell lengths must be positive");
+        return ST_BAD_ARG;
+      }
+    g_.dim = d;
+    g_.n0 = d == 3 ? cfg_.N[0] : 1;
+    g_.n1 = cfg_.N[d - 2];
+    g_.n2 = cfg_.N[d - 1];
+    g_.n2h = g_.n2 / 2 + 1;
+    g_.dv = cfg_.physics == 0 ? d : cfg_.physics == 1 ? d * (d + 1) / 2 : cfg_.ncomp;
+    g_.L = cfg_.nloads;
+    if (cfg_.physics < 0 && (g_.dv < 1 || g_.dv > kMaxDv)) {
+      set_error("ncomp must be in 1..6");
+      return ST_BAD_ARG;
+    }
+    if (g_.L < 1 || g_.L > kMaxLoads) { set_error("nloads must be in 1..6"); return ST_BAD_ARG; }
+    g_.M = (long long)g_.n0 * g_.n1 * g_.n2;
+    gp_.physics = cfg_.physics;
+    gp_.scale = cfg_.scale;
+    for (int i = 0; i < 3; ++i) {
+      const int b = i < d ? cfg_.band[i] : 1;
+      const int bodd = b - ((b + 1) % 2);
+      gp_.h[i] = (bodd - 1) / 2;
+      gp_.Y[i] = i < d ? cfg_.Y[i] : 1.0;
+    }
+    int st;
+    if ((st = make_line(g_.n2, l2_)) != ST_OK) return st;
+    if ((st = make_line(g_.n1, l1_)) != ST_OK) return st;
+    if (d == 3 && (st = make_line(g_.n0, l0_)) != ST_OK) return st;
+    const int C = g_.L * g_.dv;
+    spec_elems_ = (size_t)C * g_.n0 * g_.n1 * g_.n2h;
+    FHP_CHECK(cudaMalloc(&S_, spec_elems_ * sizeof(cplx<R>)));
+    // launch geometry
+    const int np = (C + 1) / 2;
+    const size_t srow = (size_t)np * l2_.dev.nf * sizeof(cplx<R>);
+    rows_ = std::max(1, kTargetElems / (np * l2_.dev.nf));
+    rows_ = (int)std::min<size_t>(rows_, std::max<size_t>(1, kSmemBudget / srow));
+    smem_rows_ = std::max<size_t>((size_t)rows_ * srow, 8 * kMaxLoads * sizeof(double));
+    if (smem_rows_ > kSmemMax) { set_error("line too long for shared memory"); return ST_BAD_ARG; }
+    row_ctas_ = (int)(((long long)g_.n0 * g_.n1 + rows_ - 1) / rows_);
+    // strided c2c on axis 1 (3D) and projection on the first real axis
+    if (d == 3) {
+      T1_ = tile_cols(l1_.dev.nf, 1, (long long)g_.n2h);
+    }
+    const LineDev<R>& lp = (d == 3) ? l0_.dev : l1_.dev;
+    const long long pin = (d == 3) ? (long long)g_.n1 * g_.n2h : (long long)g_.n2h;
+    Tp_ = tile_cols(lp.nf, g_.dv, pin);
+    if ((size_t)Tp_ * g_.dv * lp.nf * sizeof(cplx<R>) > kSmemMax) {
+      set_error("projection line too long for shared memory");
+      return ST_BAD_ARG;
+    }
+    if (d == 3) T0_ = tile_cols(l0_.dev.nf, 1, (long long)g_.n1 * g_.n2h);
+    // reduction scratch
+    int dev = 0;
+    FHP_CHECK(cudaGetDevice(&dev));
+    FHP_CHECK(cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, dev));
+    red_ctas_ = (int)std::max<long long>(1, std::min<long long>(4LL * nsm_, (g_.M + kThreads - 1) / kThreads));
+    nparts_max_ = std::max(row_ctas_, red_ctas_);
+    FHP_CHECK(cudaMalloc(&partials_, (size_t)nparts_max_ * kMaxLoads * kMaxLoads * sizeof(double)));
+    FHP_CHECK(cudaMalloc(&st_, kMaxLoads * sizeof(LoadState)));
+    FHP_CHECK(cudaMalloc(&all_done_, sizeof(int)));
+    FHP_CHECK(cudaMallocHost(&h_done_, sizeof(int)));
+    FHP_CHECK(cudaMallocHost(&h_st_, kMaxLoads * sizeof(LoadState)));
+    FHP_CHECK(cudaMalloc(&ad_, 2 * kMaxLoads * kMaxLoads * sizeof(double)));
+    return set_attrs();
+  }
+
+  int precision() const override { return sizeof(R) == 8 ? 0 : 1; }
+  long long voxels() const override { return g_.M; }
+  int dv() const override { return g_.dv; }
+  int loads() const override { return g_.L; }
+  size_t elem_size() const override { return sizeof(R); }
+  size_t spectrum_elems() const override { return spec_elems_; }
+  const PlanConfig& config() const override { return cfg_; }
+  int coef_kind() const override { return coef_kind_; }
+
+  int set_coefficient(int kind, const double* values, bool on_device, cudaStream_t s) override {
+    if (kind < COEF_ISO || kind > COEF_FULL) { set_error("bad coefficient kind"); return ST_BAD_ARG; }
+    const int dv = g_.dv;
+    const int c = kind == COEF_ISO ? 1 : kind == COEF_SYM ? dv * (dv + 1) / 2 : dv * dv;
+    const size_t n = (size_t)c * g_.M;
+    if (A_) { cudaFree(A_); A_ = nullptr; }
+    FHP_CHECK(cudaMalloc(&A_, n * sizeof(R)));
+    double* tmp = nullptr;
+    const double* src = values;
+    if (!on_device) {
+      FHP_CHECK(cudaMalloc(&tmp, n * sizeof(double)));
+      FHP_CHECK(cudaMemcpyAsync(tmp, values, n * sizeof(double), cudaMemcpyHostToDevice, s));
+      src = tmp;
+    }
+    k_convert<R, double><<<grid_for(n), kThreads, 0, s>>>((long long)n, src, A_);
+    FHP_LAUNCHED();
+    if (tmp) {
+      FHP_CHECK(cudaStreamSynchronize(s));
+      cudaFree(tmp);
+    }
+    coef_kind_ = kind;
+    return ST_OK;
+  }
+
+  // y = iF G F (A x) for all loads (ffthompy/tensors/operators.py:136-144)
+  int apply(int proj, const void* x, void* y, cudaStream_t s) override {
+    if (!A_) { set_error("coefficient not set"); return ST_BAD_ARG; }
+    gp_.proj = proj;
+    return run_operator(coef_kind_, false, static_cast<const R*>(x), nullptr, nullptr,
+                        static_cast<R*>(y), nullptr, s, false, false);
+  }
+
+  int rhs_macro(int proj, void* b, cudaStream_t s) override {
+    R* tmp = nullptr;
+    const size_t n = (size_t)g_.L * g_.dv * g_.M;
+    FHP_CHECK(cudaMallocAsync(&tmp, n * sizeof(R), s));
+    k_fill_macro<R><<<grid_for(n), kThreads, 0, s>>>(tmp, g_, -1.0);
+    FHP_LAUNCHED();
+    int st = apply(proj, tmp, b, s);
+    cudaFreeAsync(tmp, s);
+    return st;
+  }
+
+  int cg_solve(int proj, const void* bv, const void* x0v, double tol, int maxiter, void* xv,
+               SolveResult& res, int log_cap, cudaStream_t s) override {
+    if (!A_) { set_error("coefficient not set"); return ST_BAD_ARG; }
+    gp_.proj = proj;
+    const R* b = static_cast<const R*>(bv);
+    const R* x0 = static_cast<const R*>(x0v);
+    R* x = static_cast<R*>(xv);
+    const size_t n = (size_t)g_.L * g_.dv * g_.M;
+    int st = ensure_cg_buffers();
+    if (st != ST_OK) return st;
+    // x = x0 ; R = B - A x0 ; P = R   (solver.py:114-117)
+    if (x0) {
+      FHP_CHECK(cudaMemcpyAsync(x, x0, n * sizeof(R), cudaMemcpyDeviceToDevice, s));
+      if ((st = apply(proj, x, ap_, s)) != ST_OK) return st;
+      FHP_CHECK(cudaMemcpyAsync(r_, b, n * sizeof(R), cudaMemcpyDeviceToDevice, s));
+      k_axpby<R><<<grid_for(n), kThreads, 0, s>>>((long long)n, -1.0, ap_, 1.0, r_);
+      FHP_LAUNCHED();
+    } else {
+      FHP_CHECK(cudaMemsetAsync(x, 0, n * sizeof(R), s));
+      FHP_CHECK(cudaMemcpyAsync(r_, b, n * sizeof(R), cudaMemcpyDeviceToDevice, s));
+    }
+    FHP_CHECK(cudaMemcpyAsync(p_, r_, n * sizeof(R), cudaMemcpyDeviceToDevice, s));
+    x_cur_ = x;
+    // state
+    for (int l = 0; l < g_.L; ++l) {
+      LoadState& h = h_st_[l];
+      std::memset(&h, 0, sizeof(LoadState));
+      h.tol = tol;
+      h.maxiter = maxiter;
+    }
+    FHP_CHECK(cudaMemcpyAsync(st_, h_st_, g_.L * sizeof(LoadState), cudaMemcpyHostToDevice, s));
+    FHP_CHECK(cudaMemsetAsync(all_done_, 0, sizeof(int), s));
+    const int log_rows = std::max(1, std::min(log_cap, maxiter + 1));
+    double* dlog = nullptr;
+    FHP_CHECK(cudaMallocAsync(&dlog, (size_t)log_rows * g_.L * sizeof(double), s));
+    FHP_CHECK(cudaMemsetAsync(dlog, 0, (size_t)log_rows * g_.L * sizeof(double), s));
+    k_dot<R><<<red_ctas_, kThreads, 0, s>>>(r_, r_, partials_, g_);
+    FHP_LAUNCHED();
+    k_fin_init<<<1, 32, 0, s>>>(partials_, red_ctas_, st_, g_.L, 1.0 / (double)g_.M, dlog,
+                                log_rows);
+    FHP_LAUNCHED();
+    k_update_all_done<<<1, 1, 0, s>>>(st_, g_.L, all_done_);
+    FHP_LAUNCHED();
+    // iterations, in chunks between host checks of all_done
+    int done_iters = 0;
+    int chunk = 2;
+    while (done_iters < maxiter) {
+      FHP_CHECK(cudaMemcpyAsync(h_done_, all_done_, sizeof(int), cudaMemcpyDeviceToHost, s));
+      FHP_CHECK(cudaStreamSynchronize(s));
+      if (*h_done_) break;
+      const int nit = std::min(chunk, maxiter - done_iters);
+      for (int it = 0; it < nit; ++it) {
+        if ((st = cg_iteration(dlog, log_rows, s)) != ST_OK) { cudaFreeAsync(dlog, s); return st; }
+      }
+      done_iters += nit;
+      chunk = std::min(chunk * 2, 32);
+    }
+    FHP_CHECK(cudaMemcpyAsync(h_st_, st_, g_.L * sizeof(LoadState), cudaMemcpyDeviceToHost, s));
+    res.res_log.assign((size_t)log_rows * g_.L, 0.0);
+    FHP_CHECK(cudaMemcpyAsync(res.res_log.data(), dlog, (size_t)log_rows * g_.L * sizeof(double),
+                              cudaMemcpyDeviceToHost, s));
+    FHP_CHECK(cudaStreamSynchronize(s));
+    cudaFreeAsync(dlog, s);
+    res.kit.resize(g_.L);
+    res.norm_res.resize(g_.L);
+    res.status.resize(g_.L);
+    int worst = ST_OK;
+    res.iterations_run = 0;
+    for (int l = 0; l < g_.L; ++l) {
+      const LoadState& h = h_st_[l];
+      res.kit[l] = h.kit;
+      res.norm_res[l] = h.kit == 0 ? 0.0 : h.norm_res;  // solver.py:137-138
+      int sl = h.status;
+      if (sl == 0 && h.norm_res > tol && h.kit > 0) sl = ST_NONCONVERGED;
+      res.status[l] = sl;
+      worst = std::max(worst, sl);
+      res.iterations_run = std::max(res.iterations_run, h.kit);
+    }
+    (void)worst;
+    return ST_OK;  // per-load statuses are reported in res.status
+  }
+
+  // A_H[i][j] = <A u_i, u_j>, u_i = X_i (+ E_i)  (postprocess.py:53-70)
+  int energy(const void* Xv, int add_macro, double* AH, cudaStream_t s) override {
+    if (!A_) { set_error("coefficient not set"); return ST_BAD_ARG; }
+    const R* X = static_cast<const R*>(Xv);
+    const int L = g_.L;
+    switch (coef_kind_) {
+      case COEF_ISO: k_energy<R, COEF_ISO><<<red_ctas_, 128, 0, s>>>(X, A_, partials_, g_, add_macro); break;
+      case COEF_SYM: k_energy<R, COEF_SYM><<<red_ctas_, 128, 0, s>>>(X, A_, partials_, g_, add_macro); break;
+      default: k_energy<R, COEF_FULL><<<red_ctas_, 128, 0, s>>>(X, A_, partials_, g_, add_macro); break;
+    }
+    FHP_LAUNCHED();
+    k_sum_partials<<<1, kThreads, 0, s>>>(partials_, red_ctas_, L * L, 1.0 / (double)g_.M, ad_);
+    FHP_LAUNCHED();
+    FHP_CHECK(cudaMemcpyAsync(AH, ad_, (size_t)L * L * sizeof(double), cudaMemcpyDeviceToHost, s));
+    FHP_CHECK(cudaStreamSynchronize(s));
+    return ST_OK;
+  }
+
+  int forward_spectrum(const void* xv, void* spec, cudaStream_t s) override {
+    cplx<R>* Sp = static_cast<cplx<R>*>(spec);
+    int st = fwd_passes(COEF_NONE, false, static_cast<const R*>(xv), nullptr, nullptr, Sp,
+                        false, s);
+    if (st != ST_OK) return st;
+    // complete the forward transform on the first real axis
+    const int d = g_.dim;
+    const LineDev<R>& lf = d == 3 ? l0_.dev : l1_.dev;
+    const long long inner = d == 3 ? (long long)g_.n1 * g_.n2h : (long long)g_.n2h;
+    const int T = d == 3 ? T0_ : tile_cols(lf.nf, 1, inner);
+    dim3 grid((unsigned)((inner + T - 1) / T), (unsigned)(g_.L * g_.dv));
+    k_c2c_axis<R, false><<<grid, kThreads, (size_t)T * lf.nf * sizeof(cplx<R>), s>>>(
+        Sp, d == 3 ? g_.n0 : g_.n1, inner, lf, T, nullptr, nullptr, 0);
+    FHP_LAUNCHED();
+    return ST_OK;
+  }
+
+  int inverse_spectrum(void* spec, void* xv, double scale, cudaStream_t s) override {
+    cplx<R>* Sp = static_cast<cplx<R>*>(spec);
+    const int d = g_.dim;
+    const LineDev<R>& lf = d == 3 ? l0_.dev : l1_.dev;
+    const long long inner = d == 3 ? (long long)g_.n1 * g_.n2h : (long long)g_.n2h;
+    const int T = d == 3 ? T0_ : tile_cols(lf.nf, 1, inner);
+    dim3 grid((unsigned)((inner + T - 1) / T), (unsigned)(g_.L * g_.dv));
+    k_c2c_axis<R, true><<<grid, kThreads, (size_t)T * lf.nf * sizeof(cplx<R>), s>>>(
+        Sp, d == 3 ? g_.n0 : g_.n1, inner, lf, T, nullptr, nullptr, 0);
+    FHP_LAUNCHED();
+    return inv_passes(Sp, static_cast<R*>(xv), (R)scale, false, nullptr, false, s);
+  }
+
+  int residual(const void* b, const void* ax, void* r, double* sumsq,
+               cudaStream_t s) override {
+    k_residual<R><<<red_ctas_, kThreads, 0, s>>>(static_cast<const R*>(b),
+                                                 static_cast<const R*>(ax), static_cast<R*>(r),
+                                                 partials_, g_);
+    FHP_LAUNCHED();
+    k_sum_partials<<<1, kThreads, 0, s>>>(partials_, red_ctas_, g_.L, 1.0, ad_);
+    FHP_LAUNCHED();
+    FHP_CHECK(cudaMemcpyAsync(sumsq, ad_, g_.L * sizeof(double), cudaMemcpyDeviceToHost, s));
+    FHP_CHECK(cudaStreamSynchronize(s));
+    return ST_OK;
+  }
+
+  int scale_from64(const double* src, const double* scale, void* dst, cudaStream_t s) override {
+    LoadScale ls{};
+    for (int l = 0; l < g_.L; ++l) ls.v[l] = scale[l];
+    const size_t n = (size_t)g_.L * g_.dv * g_.M;
+    k_scale_from64<R><<<grid_for(n), kThreads, 0, s>>>(src, static_cast<R*>(dst), g_, ls);
+    FHP_LAUNCHED();
+    return ST_OK;
+  }
+
+  int add_scaled_to64(const void* d, const double* scale, double* x, cudaStream_t s) override {
+    LoadScale ls{};
+    for (int l = 0; l < g_.L; ++l) ls.v[l] = scale[l];
+    const size_t n = (size_t)g_.L * g_.dv * g_.M;
+    k_add_scaled_to64<R><<<grid_for(n), kThreads, 0, s>>>(static_cast<const R*>(d), x, g_, ls);
+    FHP_LAUNCHED();
+    return ST_OK;
+  }
+
+  int ga_gather(const void* spec_src, const PlanConfig& src, const int* d_index,
+                const double* d_weight, void* spec_dst, cudaStream_t s) override {
+    const int d = cfg_.dim;
+    const int P0 = d == 3 ? src.N[0] : 1, P1 = src.N[d - 2], P2 = src.N[d - 1];
+    k_ga_gather<R><<<grid_for(spec_elems_), kThreads, 0, s>>>(
+        static_cast<const cplx<R>*>(spec_src), static_cast<cplx<R>*>(spec_dst), g_.L * g_.dv,
+        P0, P1, P2, g_.n0, g_.n1, g_.n2, d_index, d_weight);
+    FHP_LAUNCHED();
+    return ST_OK;
+  }
+
+  int pad_spectrum(const void* spec_src, const PlanConfig& src, void* spec_dst,
+                   cudaStream_t s) override {
+    const int d = cfg_.dim;
+    const int N0 = d == 3 ? src.N[0] : 1, N1 = src.N[d - 2], N2 = src.N[d - 1];
+    const size_t tot = spec_elems_;
+    k_spectrum_pad<R><<<grid_for(tot), kThreads, 0, s>>>(
+        static_cast<const cplx<R>*>(spec_src), static_cast<cplx<R>*>(spec_dst), g_.L * g_.dv, d,
+        N0, N1, N2, g_.n0, g_.n1, g_.n2);
+    FHP_LAUNCHED();
+    return ST_OK;
+  }
+
+ private:
+  PlanConfig cfg_;
+  GridDims g_{};
+  GreenParams gp_{};
+  DevLine<R> l0_, l1_, l2_;
+  cplx<R>* S_ = nullptr;
+  size_t spec_elems_ = 0;
+  R* A_ = nullptr;
+  int coef_kind_ = 0;
+  R *r_ = nullptr, *p_ = nullptr, *ap_ = nullptr;
+  double* partials_ = nullptr;
+  double* ad_ = nullptr;
+  LoadState* st_ = nullptr;
+  LoadState* h_st_ = nullptr;
+  int* all_done_ = nullptr;
+  int* h_done_ = nullptr;
+  int rows_ = 1, row_ctas_ = 1, T1_ = 1, Tp_ = 1, T0_ = 1;
+  size_t smem_rows_ = 0;
+  int nsm_ = 1, red_ctas_ = 1, nparts_max_ = 1;
+
+  // algorithmic bytes of the passes (each input read once, each output written once)
+  double field_bytes() const { return (double)g_.L * g_.dv * g_.M * sizeof(R); }
+  double spec_bytes() const { return (double)spec_elems_ * 2 * sizeof(R); }
+  double coef_bytes() const {
+    const int dv = g_.dv;
+    const int c = coef_kind_ == COEF_ISO ? 1 : coef_kind_ == COEF_SYM ? dv * (dv + 1) / 2
+                : coef_kind_ == COEF_FULL ? dv * dv : 0;
+    return (double)c * g_.M * sizeof(R);
+  }
+  int pbeg(const char* name, double bytes, cudaStream_t s) {
+    if (!prof.on) return -1;
+    const std::string tag = std::string(name) + (sizeof(R) == 8 ? "<f64>" : "<f32>");
+    const int k = prof.kind_of(tag, bytes);
+    prof.begin(k, s);
+    return k;
+  }
+  void pend(int k, cudaStream_t s) {
+    if (k >= 0) prof.end(s);
+  }
+
+  static unsigned grid_for(size_t n) {
+    size_t b = (n + kThreads - 1) / kThreads;
+    return (unsigned)std::max<size_t>(1, std::min<size_t>(b, 65535 * 4));
+  }
+
+  int tile_cols(int nf, int lines_per_col, long long inner) const {
+    const size_t per = (size_t)lines_per_col * nf * sizeof(cplx<R>);
+    int T = std::max(1, kTargetElems / (lines_per_col * nf));
+    T = std::min(T, 32);
+    T = (int)std::min<size_t>(T, std::max<size_t>(1, kSmemBudget / per));
+    T = (int)std::min<long long>(T, inner);
+    return std::max(T, 1);
+  }
+
+  int make_line(int n, DevLine<R>& out) {
+    LinePlanHost h;
+    if (!build_line_plan(n, h)) { set_error("cannot plan FFT length " + std::to_string(n)); return ST_BAD_ARG; }
+    if (h.nst > kMaxStages) { set_error("too many FFT stages"); return ST_BAD_ARG; }
+    const size_t ntw = h.tw.size(), nch = h.chirp.size(), nbh = h.bhat.size();
+    const size_t bytes = (ntw + nch + nbh) * sizeof(cplx<R>) + h.pos.size() * sizeof(int) + 64;
+    FHP_CHECK(cudaMalloc(&out.mem, bytes));
+    std::vector<unsigned char> host(bytes, 0);
+    cplx<R>* c = reinterpret_cast<cplx<R>*>(host.data());
+    auto put = [&](const std::vector<std::complex<long double>>& v, size_t off) {
+      for (size_t i = 0; i < v.size(); ++i) c[off + i] = mkc<R>((R)v[i].real(), (R)v[i].imag());
+    };
+    put(h.tw, 0);
+    put(h.chirp, ntw);
+    put(h.bhat, ntw + nch);
+    int* ip = reinterpret_cast<int*>(c + ntw + nch + nbh);
+    std::memcpy(ip, h.pos.data(), h.pos.size() * sizeof(int));
+    FHP_CHECK(cudaMemcpy(out.mem, host.data(), bytes, cudaMemcpyHostToDevice));
+    cplx<R>* dc = reinterpret_cast<cplx<R>*>(out.mem);
+    LineDev<R>& L = out.dev;
+    L.n = h.n;
+    L.nf = h.nf;
+    L.blue = h.blue;
+    L.nst = h.nst;
+    for (int i = 0; i < kMaxStages; ++i) L.rad[i] = i < h.nst ? h.rad[i] : 1;
+    L.tw = dc;
+    L.chirp = nch ? dc + ntw : nullptr;
+    L.bhat = nbh ? dc + ntw + nch : nullptr;
+    L.pos = reinterpret_cast<const int*>(dc + ntw + nch + nbh);
+    return ST_OK;
+  }
+
+  int set_attrs() {
+    int st = ST_OK;
+#define FHP_ATTR(k) if ((st = set_smem_attr(k)) != ST_OK) return st
+    FHP_ATTR((k_r2c_last<R, COEF_NONE, false>));
+    FHP_ATTR((k_r2c_last<R, COEF_ISO, false>));
+    FHP_ATTR((k_r2c_last<R, COEF_SYM, false>));
+    FHP_ATTR((k_r2c_last<R, COEF_FULL, false>));
+    FHP_ATTR((k_r2c_last<R, COEF_ISO, true>));
+    FHP_ATTR((k_r2c_last<R, COEF_SYM, true>));
+    FHP_ATTR((k_r2c_last<R, COEF_FULL, true>));
+    FHP_ATTR((k_c2c_axis<R, false>));
+    FHP_ATTR((k_c2c_axis<R, true>));
+    FHP_ATTR((k_proj_first<R>));
+    FHP_ATTR((k_c2r_last<R, false>));
+    FHP_ATTR((k_c2r_last<R, true>));
+#undef FHP_ATTR
+    return ST_OK;
+  }
+
+  int ensure_cg_buffers() {
+    const size_t n = (size_t)g_.L * g_.dv * g_.M * sizeof(R);
+    if (!r_) FHP_CHECK(cudaMalloc(&r_, n));
+    if (!p_) FHP_CHECK(cudaMalloc(&p_, n));
+    if (!ap_) FHP_CHECK(cudaMalloc(&ap_, n));
+    return ST_OK;
+  }
+
+  void release() {
+    for (DevLine<R>* l : {&l0_, &l1_, &l2_})
+      if (l->mem) { cudaFree(l->mem); l->mem = nullptr; }
+    if (S_) cudaFree(S_);
+    if (A_) cudaFree(A_);
+    if (r_) cudaFree(r_);
+    if (p_) cudaFree(p_);
+    if (ap_) cudaFree(ap_);
+    if (partials_) cudaFree(partials_);
+    if (ad_) cudaFree(ad_);
+    if (st_) cudaFree(st_);
+    if (all_done_) cudaFree(all_done_);
+    if (h_done_) cudaFreeHost(h_done_);
+    if (h_st_) cudaFreeHost(h_st_);
+    S_ = nullptr; A_ = nullptr; r_ = p_ = ap_ = nullptr;
+  }
+
+  // pass 1 (+ axis-1 forward for 3D); leaves the spectrum ready for the
+  // first-axis pass
+  int fwd_passes(int coef, bool pupd, const R* x, R* pio, const R* rvec, cplx<R>* Sp,
+                 bool cg, cudaStream_t s) {
+    const int* ad = cg ? all_done_ : nullptr;
+    const LoadState* st = cg ? st_ : nullptr;
+    const dim3 grid1(row_ctas_);
+    const double b1 = (pupd ? 3.0 : 1.0) * field_bytes() + (coef ? coef_bytes() : 0.0) +
+                      spec_bytes();
+    const int pk1 = pbeg(pupd ? "r2c_coef_pupd" : (coef ? "r2c_coef" : "r2c"), b1, s);
+#define FHP_R2C(C, P)                                                                     \
+  k_r2c_last<R, C, P><<<grid1, kThreads, smem_rows_, s>>>(x, pio, rvec, A_, Sp, g_, l2_.dev, \
+                                                            rows_, st_, ad)
+    if (pupd) {
+      switch (coef) {
+        case COEF_ISO: FHP_R2C(COEF_ISO, true); break;
+        case COEF_SYM: FHP_R2C(COEF_SYM, true); break;
+        default: FHP_R2C(COEF_FULL, true); break;
+      }
+    } else {
+      switch (coef) {
+        case COEF_NONE: FHP_R2C(COEF_NONE, false); break;
+        case COEF_ISO: FHP_R2C(COEF_ISO, false); break;
+        case COEF_SYM: FHP_R2C(COEF_SYM, false); break;
+        default: FHP_R2C(COEF_FULL, false); break;
+      }
+    }
+#undef FHP_R2C
+    pend(pk1, s);
+    FHP_LAUNCHED();
+    if (g_.dim == 3) {
+      dim3 grid((unsigned)((g_.n2h + T1_ - 1) / T1_), (unsigned)(g_.L * g_.dv * g_.n0));
+      const int pk = pbeg("c2c_axis1_fwd", 2.0 * spec_bytes(), s);
+      k_c2c_axis<R, false><<<grid, kThreads, (size_t)T1_ * l1_.dev.nf * sizeof(cplx<R>), s>>>(
+          Sp, g_.n1, (long long)g_.n2h, l1_.dev, T1_, ad, st, g_.dv * g_.n0);
+      pend(pk, s);
+      FHP_LAUNCHED();
+    }
+    return ST_OK;
+  }
+
+  // axis-1 inverse (3D) + c2r last axis with scale and optional dot
+  int inv_passes(cplx<R>* Sp, R* y, R scale, bool dot, const R* pdot, bool cg, cudaStream_t s) {
+    const int* ad = cg ? all_done_ : nullptr;
+    const LoadState* st = cg ? st_ : nullptr;
+    if (g_.dim == 3) {
+      dim3 grid((unsigned)((g_.n2h + T1_ - 1) / T1_), (unsigned)(g_.L * g_.dv * g_.n0));
+      const int pk = pbeg("c2c_axis1_inv", 2.0 * spec_bytes(), s);
+      k_c2c_axis<R, true><<<grid, kThreads, (size_t)T1_ * l1_.dev.nf * sizeof(cplx<R>), s>>>(
+          Sp, g_.n1, (long long)g_.n2h, l1_.dev, T1_, ad, st, g_.dv * g_.n0);
+      pend(pk, s);
+      FHP_LAUNCHED();
+    }
+    const dim3 grid1(row_ctas_);
+    const int pk2 = pbeg(dot ? "c2r_dot" : "c2r", spec_bytes() + (dot ? 2.0 : 1.0) * field_bytes(), s);
+    if (dot)
+      k_c2r_last<R, true><<<grid1, kThreads, smem_rows_, s>>>(Sp, y, pdot, partials_, g_, l2_.dev,
+                                                              rows_, scale, ad);
+    else
+      k_c2r_last<R, false><<<grid1, kThreads, smem_rows_, s>>>(Sp, y, nullptr, nullptr, g_,
+                                                               l2_.dev, rows_, scale, ad);
+    pend(pk2, s);
+    FHP_LAUNCHED();
+    return ST_OK;
+  }
+
+  int proj_pass(cplx<R>* Sp, bool cg, cudaStream_t s) {
+    const int d = g_.dim;
+    const LineDev<R>& lp = d == 3 ? l0_.dev : l1_.dev;
+    const long long inner = d == 3 ? (long long)g_.n1 * g_.n2h : (long long)g_.n2h;
+    dim3 grid((unsigned)((inner + Tp_ - 1) / Tp_), (unsigned)g_.L);
+    const size_t smem = (size_t)Tp_ * g_.dv * lp.nf * sizeof(cplx<R>);
+    const int pk = pbeg("proj_axis0", 2.0 * spec_bytes(), s);
+    k_proj_first<R><<<grid, kThreads, smem, s>>>(Sp, g_, d == 3 ? g_.n0 : g_.n1, inner, lp, Tp_,
+                                                 gp_, cg ? all_done_ : nullptr,
+                                                 cg ? st_ : nullptr);
+    pend(pk, s);
+    FHP_LAUNCHED();
+    return ST_OK;
+  }
+
+  int run_operator(int coef, bool pupd, const R* x, R* pio, const R* rvec, R* y, const R* pdot,
+                   cudaStream_t s, bool cg, bool dot) {
+    int st;
+    if ((st = fwd_passes(coef, pupd, x, pio, rvec, S_, cg, s)) != ST_OK) return st;
+    if ((st = proj_pass(S_, cg, s)) != ST_OK) return st;
+    return inv_passes(S_, y, (R)(1.0 / (double)g_.M), dot, pdot, cg, s);
+  }
+
+  // one CG iteration on all loads (solver.py:124-134), P update fused into pass 1
+  int cg_iteration(double* dlog, int log_rows, cudaStream_t s) {
+    int st = run_operator(coef_kind_, true, nullptr, p_, r_, ap_, p_, s, true, true);
+    if (st != ST_OK) return st;
+    k_fin_pap<<<g_.L, kThreads, 0, s>>>(partials_, row_ctas_, st_, g_.L, 1.0 / (double)g_.M,
+                                        all_done_);
+    FHP_LAUNCHED();
+    const int pk = pbeg("cg_update", 6.0 * field_bytes(), s);
+    k_cg_update<R><<<red_ctas_, kThreads, 0, s>>>(x_cur_, r_, p_, ap_, partials_, g_, st_,
+                                                  all_done_);
+    pend(pk, s);
+    FHP_LAUNCHED();
+    k_fin_rr<<<g_.L, kThreads, 0, s>>>(partials_, red_ctas_, st_, g_.L, 1.0 / (double)g_.M, dlog,
+                                       log_rows, all_done_);
+    FHP_LAUNCHED();
+    k_update_all_done<<<1, 1, 0, s>>>(st_, g_.L, all_done_);
+    FHP_LAUNCHED();
+    return ST_OK;
+  }
+
+  R* x_cur_ = nullptr;  // the caller's solution buffer during cg_solve
+};
+
+}  // namespace fhp

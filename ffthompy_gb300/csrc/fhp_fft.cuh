@@ -1,0 +1,353 @@
+// Shared-memory line FFTs for the Fourier-Galerkin operator (sm_103a).
+//
+// A "line" is one 1D transform of logical length n held in shared memory.
+//  * direct lines: n factors into radices {2,3,4,5,8,16} and odd primes <= 31;
+//    forward = in-place decimation-in-frequency (natural in, digit-reversed
+//    out), inverse = in-place decimation-in-time (digit-reversed in, natural
+//    out).  No ping-pong buffer is needed: every butterfly reads and writes
+//    the same r slots.
+//  * Bluestein lines: n has a prime factor > 31 (89, 127, 509, 1021, 73 ...);
+//    the DFT is a chirp convolution of smooth length m >= 2n-1 done with the
+//    direct machinery (DIF, pointwise product with the filter spectrum stored
+//    in digit-reversed order, DIT).
+// Callers put/get values in *frequency* order through put_inv/get_fwd, so the
+// permutation never leaves shared memory and global spectra stay in natural
+// order (the layout of numpy's rfftn, ffthompy/tensors/fft.py:39-43).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace fhp {
+
+template <typename R> struct CplxT;
+template <> struct CplxT<float> { using T = float2; };
+template <> struct CplxT<double> { using T = double2; };
+template <typename R> using cplx = typename CplxT<R>::T;
+
+template <typename R>
+__host__ __device__ __forceinline__ cplx<R> mkc(R a, R b) { cplx<R> c; c.x = a; c.y = b; return c; }
+template <typename R>
+__device__ __forceinline__ cplx<R> cadd(cplx<R> a, cplx<R> b) { return mkc<R>(a.x + b.x, a.y + b.y); }
+template <typename R>
+__device__ __forceinline__ cplx<R> csub(cplx<R> a, cplx<R> b) { return mkc<R>(a.x - b.x, a.y - b.y); }
+template <typename R>
+__device__ __forceinline__ cplx<R> cmul(cplx<R> a, cplx<R> b) {
+  return mkc<R>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// a * conj(b)
+template <typename R>
+__device__ __forceinline__ cplx<R> cmulc(cplx<R> a, cplx<R> b) {
+  return mkc<R>(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+template <typename R>
+__device__ __forceinline__ cplx<R> cconj(cplx<R> a) { return mkc<R>(a.x, -a.y); }
+template <typename R>
+__device__ __forceinline__ cplx<R> cscale(cplx<R> a, R s) { return mkc<R>(a.x * s, a.y * s); }
+// -i * a
+template <typename R>
+__device__ __forceinline__ cplx<R> cmul_mi(cplx<R> a) { return mkc<R>(a.y, -a.x); }
+// +i * a
+template <typename R>
+__device__ __forceinline__ cplx<R> cmul_pi(cplx<R> a) { return mkc<R>(-a.y, a.x); }
+
+constexpr int kMaxStages = 24;
+
+// Device view of one line plan (passed by value in kernel parameters).
+template <typename R>
+struct LineDev {
+  int n;        // logical length
+  int nf;       // transform length of the core (n, or Bluestein m)
+  int blue;     // 1: Bluestein
+  int nst;      // number of radix stages of the core
+  int rad[kMaxStages];
+  const cplx<R>* tw;     // nf entries, W_nf^k = exp(-2 pi i k / nf)
+  const cplx<R>* chirp;  // n entries, exp(-i pi j^2 / n)      (Bluestein)
+  const cplx<R>* bhat;   // nf entries, filter spectrum / nf, digit-reversed (Bluestein)
+  const int* pos;        // n entries, frequency -> slot after the forward core (direct)
+};
+
+// ---------------------------------------------------------------------------
+// radix-r DFTs on registers (forward sign -; inverse = conj o forward o conj)
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ void dft2(cplx<R>* v) {
+  cplx<R> a = v[0], b = v[1];
+  v[0] = cadd<R>(a, b);
+  v[1] = csub<R>(a, b);
+}
+
+template <typename R>
+__device__ __forceinline__ void dft3(cplx<R>* v) {
+  const R h = R(0.86602540378443864676372317075294);  // sqrt(3)/2
+  cplx<R> s = cadd<R>(v[1], v[2]);
+  cplx<R> d = csub<R>(v[1], v[2]);
+  cplx<R> t1 = mkc<R>(v[0].x - R(0.5) * s.x, v[0].y - R(0.5) * s.y);
+  cplx<R> t2 = mkc<R>(h * d.x, h * d.y);
+  v[0] = cadd<R>(v[0], s);
+  v[1] = cadd<R>(t1, cmul_mi<R>(t2));
+  v[2] = cadd<R>(t1, cmul_pi<R>(t2));
+}
+
+template <typename R>
+__device__ __forceinline__ void dft4(cplx<R>* v) {
+  cplx<R> a = cadd<R>(v[0], v[2]), b = csub<R>(v[0], v[2]);
+  cplx<R> c = cadd<R>(v[1], v[3]), d = csub<R>(v[1], v[3]);
+  v[0] = cadd<R>(a, c);
+  v[2] = csub<R>(a, c);
+  v[1] = cadd<R>(b, cmul_mi<R>(d));
+  v[3] = cadd<R>(b, cmul_pi<R>(d));
+}
+
+template <typename R>
+__device__ __forceinline__ void dft5(cplx<R>* v) {
+  const R c1 = R(0.30901699437494742410229341718282);   // cos(2pi/5)
+  const R c2 = R(-0.80901699437494742410229341718282);  // cos(4pi/5)
+  const R s1 = R(0.95105651629515357211643933337938);   // sin(2pi/5)
+  const R s2 = R(0.58778525229247312916870595463907);   // sin(4pi/5)
+  cplx<R> t1 = cadd<R>(v[1], v[4]), t3 = csub<R>(v[1], v[4]);
+  cplx<R> t2 = cadd<R>(v[2], v[3]), t4 = csub<R>(v[2], v[3]);
+  cplx<R> x0 = v[0];
+  cplx<R> a1 = mkc<R>(x0.x + c1 * t1.x + c2 * t2.x, x0.y + c1 * t1.y + c2 * t2.y);
+  cplx<R> a2 = mkc<R>(x0.x + c2 * t1.x + c1 * t2.x, x0.y + c2 * t1.y + c1 * t2.y);
+  cplx<R> b1 = mkc<R>(s1 * t3.x + s2 * t4.x, s1 * t3.y + s2 * t4.y);
+  cplx<R> b2 = mkc<R>(s2 * t3.x - s1 * t4.x, s2 * t3.y - s1 * t4.y);
+  v[0] = mkc<R>(x0.x + t1.x + t2.x, x0.y + t1.y + t2.y);
+  v[1] = cadd<R>(a1, cmul_mi<R>(b1));
+  v[4] = cadd<R>(a1, cmul_pi<R>(b1));
+  v[2] = cadd<R>(a2, cmul_mi<R>(b2));
+  v[3] = cadd<R>(a2, cmul_pi<R>(b2));
+}
+
+template <typename R>
+__device__ __forceinline__ void dft8(cplx<R>* v) {
+  const R r = R(0.70710678118654752440084436210485);
+  cplx<R> e[4] = {v[0], v[2], v[4], v[6]};
+  cplx<R> o[4] = {v[1], v[3], v[5], v[7]};
+  dft4<R>(e);
+  dft4<R>(o);
+  // o[k] *= W8^k
+  o[1] = mkc<R>(r * (o[1].x + o[1].y), r * (o[1].y - o[1].x));
+  o[2] = cmul_mi<R>(o[2]);
+  o[3] = mkc<R>(r * (o[3].y - o[3].x), -r * (o[3].x + o[3].y));
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    v[k] = cadd<R>(e[k], o[k]);
+    v[k + 4] = csub<R>(e[k], o[k]);
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ void dft16(cplx<R>* v) {
+  // x[b + 4a]: u_b = DFT4_a, twiddle W16^(b k1), then DFT4 over b.
+  const R c1 = R(0.92387953251128675612818318939679);  // cos(pi/8)
+  const R s1 = R(0.38268343236508977172845998403040);  // sin(pi/8)
+  const R r = R(0.70710678118654752440084436210485);
+  cplx<R> u[4][4];
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    cplx<R> t[4] = {v[b], v[b + 4], v[b + 8], v[b + 12]};
+    dft4<R>(t);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) u[b][k] = t[k];
+  }
+  // W16^1 = (c1,-s1), W16^2 = (r,-r), W16^3 = (s1,-c1), W16^4 = -i,
+  // W16^6 = (-r,-r), W16^9 = (-c1,+s1)
+  u[1][1] = cmul<R>(u[1][1], mkc<R>(c1, -s1));
+  u[1][2] = cmul<R>(u[1][2], mkc<R>(r, -r));
+  u[1][3] = cmul<R>(u[1][3], mkc<R>(s1, -c1));
+  u[2][1] = cmul<R>(u[2][1], mkc<R>(r, -r));
+  u[2][2] = cmul_mi<R>(u[2][2]);
+  u[2][3] = cmul<R>(u[2][3], mkc<R>(-r, -r));
+  u[3][1] = cmul<R>(u[3][1], mkc<R>(s1, -c1));
+  u[3][2] = cmul<R>(u[3][2], mkc<R>(-r, -r));
+  u[3][3] = cmul<R>(u[3][3], mkc<R>(-c1, s1));
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) {
+    cplx<R> t[4] = {u[0][k1], u[1][k1], u[2][k1], u[3][k1]};
+    dft4<R>(t);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) v[k1 + 4 * k2] = t[k2];
+  }
+}
+
+// Odd prime radix, symmetric-pair form; roots W_r^m read from the line table
+// (W_r^m = tw[m * nf / r]).
+template <typename R, int RAD>
+__device__ __forceinline__ void dft_odd(cplx<R>* v, const cplx<R>* __restrict__ tw, int nf) {
+  constexpr int H = (RAD - 1) / 2;
+  const int step = nf / RAD;
+  cplx<R> sp[H], sm[H];
+#pragma unroll
+  for (int j = 1; j <= H; ++j) {
+    sp[j - 1] = cadd<R>(v[j], v[RAD - j]);
+    sm[j - 1] = csub<R>(v[j], v[RAD - j]);
+  }
+  cplx<R> y0 = v[0];
+#pragma unroll
+  for (int j = 0; j < H; ++j) y0 = cadd<R>(y0, sp[j]);
+  cplx<R> out[RAD];
+  out[0] = y0;
+#pragma unroll
+  for (int k = 1; k <= H; ++k) {
+    cplx<R> a = v[0];
+    cplx<R> b = mkc<R>(R(0), R(0));
+#pragma unroll
+    for (int j = 1; j <= H; ++j) {
+      const cplx<R> w = tw[((j * k) % RAD) * step];  // (cos, -sin)
+      a.x += w.x * sp[j - 1].x;
+      a.y += w.x * sp[j - 1].y;
+      // b = sum sin * sm  (sin = -w.y)
+      b.x -= w.y * sm[j - 1].x;
+      b.y -= w.y * sm[j - 1].y;
+    }
+    out[k] = cadd<R>(a, cmul_mi<R>(b));
+    out[RAD - k] = cadd<R>(a, cmul_pi<R>(b));
+  }
+#pragma unroll
+  for (int k = 0; k < RAD; ++k) v[k] = out[k];
+}
+
+template <typename R, int RAD>
+__device__ __forceinline__ void dft_fwd(cplx<R>* v, const cplx<R>* __restrict__ tw, int nf) {
+  if constexpr (RAD == 2) dft2<R>(v);
+  else if constexpr (RAD == 3) dft3<R>(v);
+  else if constexpr (RAD == 4) dft4<R>(v);
+  else if constexpr (RAD == 5) dft5<R>(v);
+  else if constexpr (RAD == 8) dft8<R>(v);
+  else if constexpr (RAD == 16) dft16<R>(v);
+  else dft_odd<R, RAD>(v, tw, nf);
+}
+
+// ---------------------------------------------------------------------------
+// radix stages over a batch of lines in shared memory
+// ---------------------------------------------------------------------------
+// Forward DIF stage on sub-arrays of length ns: butterfly (g, j1) reads
+// slots g*ns + j1 + q*ms, applies DFT_r, multiplies output p by W_ns^(j1 p).
+template <typename R, int RAD, bool INV>
+__device__ __forceinline__ void stage_run(cplx<R>* __restrict__ buf, int ld, int nlines, int nf,
+                                          int ns, const cplx<R>* __restrict__ tw, int tid,
+                                          int nthr) {
+  const int ms = ns / RAD;
+  const int nbl = nf / RAD;
+  const int total = nlines * nbl;
+  const int tws = nf / ns;
+  for (int b = tid; b < total; b += nthr) {
+    const int line = b / nbl;
+    const int bb = b - line * nbl;
+    const int g = bb / ms;
+    const int j1 = bb - g * ms;
+    cplx<R>* p = buf + line * ld + g * ns + j1;
+    cplx<R> v[RAD];
+    if constexpr (!INV) {
+#pragma unroll
+      for (int q = 0; q < RAD; ++q) v[q] = p[q * ms];
+      dft_fwd<R, RAD>(v, tw, nf);
+      p[0] = v[0];
+#pragma unroll
+      for (int q = 1; q < RAD; ++q) p[q * ms] = cmul<R>(v[q], tw[j1 * q * tws]);
+    } else {
+      v[0] = cconj<R>(p[0]);
+#pragma unroll
+      for (int q = 1; q < RAD; ++q) v[q] = cconj<R>(cmulc<R>(p[q * ms], tw[j1 * q * tws]));
+      dft_fwd<R, RAD>(v, tw, nf);
+#pragma unroll
+      for (int q = 0; q < RAD; ++q) p[q * ms] = cconj<R>(v[q]);
+    }
+  }
+}
+
+template <typename R, bool INV>
+__device__ __noinline__ void stage_dispatch(cplx<R>* buf, int ld, int nlines, int nf, int ns,
+                                            int rad, const cplx<R>* tw, int tid, int nthr) {
+  switch (rad) {
+    case 2: stage_run<R, 2, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
+    case 3: stage_run<R, 3, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
+    case 4: stage_run<R, 4, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
+    case 5: stage_run<R, 5, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
+    case 7: stage_run<R, 7, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
+    case 8: stage_run<R, 8, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
+    case 11: stage_run<R, 11, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
+    case 13: stage_run<R, 13, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
+    case 16: stage_run<R, 16, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
+    case 17: stage_run<R, 17, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
+    case 19: stage_run<R, 19, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
+    case 23: stage_run<R, 23, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
+    case 29: stage_run<R, 29, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
+    case 31: stage_run<R, 31, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
+    default: break;  // plans only contain the radices above
+  }
+}
+
+// Core transform of nlines lines (length L.nf each, stride ld) in place.
+//   direct, forward : DIF            (natural -> digit-reversed)
+//   direct, inverse : DIT^-1         (digit-reversed -> natural), unnormalised
+//   Bluestein (either direction, conjugations at put/get): DIF, * bhat, DIT^-1
+// Ends with __syncthreads().
+template <typename R>
+__device__ void line_core(cplx<R>* buf, int ld, int nlines, const LineDev<R>& L, bool inverse) {
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const bool do_fwd = L.blue || !inverse;
+  const bool do_inv = L.blue || inverse;
+  if (do_fwd) {
+    int ns = L.nf;
+    for (int s = 0; s < L.nst; ++s) {
+      stage_dispatch<R, false>(buf, ld, nlines, L.nf, ns, L.rad[s], L.tw, tid, nthr);
+      ns /= L.rad[s];
+      __syncthreads();
+    }
+  }
+  if (L.blue) {
+    const int tot = nlines * L.nf;
+    for (int e = tid; e < tot; e += nthr) {
+      const int line = e / L.nf, j = e - line * L.nf;
+      cplx<R>* p = buf + line * ld + j;
+      *p = cmul<R>(*p, L.bhat[j]);
+    }
+    __syncthreads();
+  }
+  if (do_inv) {
+    // stage sizes: ns_s = nf / (r_0 ... r_{s-1}); run s = nst-1 .. 0
+    int ns = 1;
+    for (int s = L.nst - 1; s >= 0; --s) {
+      ns *= L.rad[s];
+      stage_dispatch<R, true>(buf, ld, nlines, L.nf, ns, L.rad[s], L.tw, tid, nthr);
+      __syncthreads();
+    }
+  }
+}
+
+// --- value placement in frequency / space order -----------------------------
+// forward input x_j (natural, j < n)
+template <typename R>
+__device__ __forceinline__ void put_fwd(cplx<R>* line, const LineDev<R>& L, int j, cplx<R> v) {
+  line[j] = L.blue ? cmul<R>(v, L.chirp[j]) : v;
+}
+// forward output X_k (k < n)
+template <typename R>
+__device__ __forceinline__ cplx<R> get_fwd(const cplx<R>* line, const LineDev<R>& L, int k) {
+  return L.blue ? cmul<R>(line[k], L.chirp[k]) : line[L.pos[k]];
+}
+// inverse input X_k (k < n)
+template <typename R>
+__device__ __forceinline__ void put_inv(cplx<R>* line, const LineDev<R>& L, int k, cplx<R> v) {
+  if (L.blue) line[k] = cmul<R>(cconj<R>(v), L.chirp[k]);
+  else line[L.pos[k]] = v;
+}
+// inverse output x_j (j < n), unnormalised
+template <typename R>
+__device__ __forceinline__ cplx<R> get_inv(const cplx<R>* line, const LineDev<R>& L, int j) {
+  return L.blue ? cconj<R>(cmul<R>(line[j], L.chirp[j])) : line[j];
+}
+// Bluestein lines need zeros in slots [n, nf) before the core.
+template <typename R>
+__device__ __forceinline__ void zero_tail(cplx<R>* buf, int ld, int nlines, const LineDev<R>& L) {
+  if (!L.blue) return;
+  const int w = L.nf - L.n;
+  const int tot = nlines * w;
+  for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+    const int line = e / w, j = L.n + (e - line * w);
+    buf[line * ld + j] = mkc<R>(R(0), R(0));
+  }
+}
+
+}  // namespace fhp

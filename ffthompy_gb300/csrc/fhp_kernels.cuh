@@ -1,0 +1,785 @@
+// Kernels of the Fourier-Galerkin operator G o A, CG and postprocessing.
+//
+// Layouts (C order, all on one GPU):
+//   real field   x[comp][n0][n1][n2],  comp = load*dv + c, M = n0*n1*n2 voxels
+//   spectrum     S[comp][n0][n1][n2h], n2h = n2/2+1 (numpy rfftn half spectrum)
+//   coefficient  A[a][n0][n1][n2]: 1 (isotropic a*I), dv*(dv+1)/2 (symmetric,
+//                packed upper triangle) or dv*dv (full) values per voxel
+// 2D grids use n0 = 1.  The operator is FiGFA = iF o G o F o A
+// (ffthompy/applications.py:58 with Operator's reversed factor order,
+// ffthompy/tensors/operators.py:119-144).
+#pragma once
+#include "fhp_fft.cuh"
+
+namespace fhp {
+
+enum CoefKind { COEF_NONE = 0, COEF_ISO = 1, COEF_SYM = 2, COEF_FULL = 3 };
+
+struct LoadState {
+  double rr;        // <R,R>
+  double pap;       // <P,AP>
+  double alpha;
+  double beta;
+  double norm_res;  // sqrt(rr)
+  double tol;
+  int kit;
+  int maxiter;
+  int done;
+  int status;       // 0 ok, 2 breakdown (p.Ap <= 0), 3 non-finite
+};
+
+struct GridDims {
+  int dim;        // 2 or 3
+  int n0, n1, n2; // n0 = 1 for 2D
+  int n2h;
+  int dv;         // components per load
+  int L;          // loads
+  long long M;    // voxels
+};
+
+// Green projection parameters (ffthompy/projections.py:9-267)
+struct GreenParams {
+  int physics;    // 0 scalar, 1 elasticity (Mandel)
+  int proj;       // 1: G1 (compatible, primal), 2: G2 (equilibrated, dual)
+  int h[3];       // band half-widths |k_i| <= h_i, real axis order
+  double Y[3];    // cell size, real axis order
+  double scale;   // Ga scale prod(2N-1)/prod(N); 1 for GaNi
+};
+
+__device__ __forceinline__ int signed_freq(int k, int n) { return (2 * k <= n) ? k : k - n; }
+
+// Mandel index -> tensor pair and weight (3D order 0..5: 00 11 22 12 02 01;
+// 2D order 0..2: 00 11 01), ffthompy/projections.py:196-229.
+__device__ __forceinline__ void mandel_pair(int dim, int I, int& a, int& b) {
+  if (dim == 3) {
+    const int aa[6] = {0, 1, 2, 1, 0, 0};
+    const int bb[6] = {0, 1, 2, 2, 2, 1};
+    a = aa[I]; b = bb[I];
+  } else {
+    const int aa[3] = {0, 1, 0};
+    const int bb[3] = {0, 1, 1};
+    a = aa[I]; b = bb[I];
+  }
+}
+
+// y = G(xi) x for one frequency, G from the closed forms:
+//   scalar:     G1 = xi xi^T / |xi|^2,           G2 = I - G1
+//   elasticity: G1 e = sym(n (x) e n)*2 - n n (n.e.n), Mandel-weighted, G2 = I - G1
+// zero at k = 0 and outside the band; times scale.
+template <typename R>
+__device__ __forceinline__ void green_apply(const GreenParams& gp, int dim, const int* k,
+                                            cplx<R>* x /* in/out, dv values */) {
+  bool inband = true, zero = true;
+  R xi[3] = {R(0), R(0), R(0)};
+  for (int i = 0; i < dim; ++i) {
+    const int ki = k[i];
+    if (ki > gp.h[i] || -ki > gp.h[i]) inband = false;
+    if (ki != 0) zero = false;
+    xi[i] = R(ki) / R(gp.Y[i]);
+  }
+  const int dv = gp.physics == 0 ? dim : dim * (dim + 1) / 2;
+  if (!inband || zero) {
+    for (int c = 0; c < dv; ++c) x[c] = mkc<R>(R(0), R(0));
+    return;
+  }
+  const R s = R(gp.scale);
+  R nn = R(0);
+  for (int i = 0; i < dim; ++i) nn += xi[i] * xi[i];
+  if (gp.physics == 0) {
+    // (xi . x) / |xi|^2
+    cplx<R> t = mkc<R>(R(0), R(0));
+    for (int i = 0; i < dim; ++i) { t.x += xi[i] * x[i].x; t.y += xi[i] * x[i].y; }
+    t.x /= nn; t.y /= nn;
+    for (int i = 0; i < dim; ++i) {
+      cplx<R> g1 = mkc<R>(xi[i] * t.x, xi[i] * t.y);
+      x[i] = (gp.proj == 1) ? cscale<R>(g1, s) : cscale<R>(csub<R>(x[i], g1), s);
+    }
+    return;
+  }
+  // elasticity: unit normal, strain tensor from Mandel vector
+  const R inv = R(1) / sqrt(nn);
+  R n[3];
+  for (int i = 0; i < 3; ++i) n[i] = (i < dim) ? xi[i] * inv : R(0);
+  const R isq2 = R(0.70710678118654752440084436210485);
+  cplx<R> e[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) e[i][j] = mkc<R>(R(0), R(0));
+  for (int I = 0; I < dv; ++I) {
+    int a, b;
+    mandel_pair(dim, I, a, b);
+    if (a == b) e[a][a] = x[I];
+    else { e[a][b] = cscale<R>(x[I], isq2); e[b][a] = e[a][b]; }
+  }
+  cplx<R> en[3];
+  for (int i = 0; i < dim; ++i) {
+    en[i] = mkc<R>(R(0), R(0));
+    for (int j = 0; j < dim; ++j) { en[i].x += e[i][j].x * n[j]; en[i].y += e[i][j].y * n[j]; }
+  }
+  cplx<R> nen = mkc<R>(R(0), R(0));
+  for (int i = 0; i < dim; ++i) { nen.x += n[i] * en[i].x; nen.y += n[i] * en[i].y; }
+  const R sq2 = R(1.4142135623730950488016887242097);
+  for (int I = 0; I < dv; ++I) {
+    int a, b;
+    mandel_pair(dim, I, a, b);
+    // (G1 e)_ab = n_a (e n)_b + n_b (e n)_a - n_a n_b (n.e.n)
+    cplx<R> g = mkc<R>(n[a] * en[b].x + n[b] * en[a].x - n[a] * n[b] * nen.x,
+                       n[a] * en[b].y + n[b] * en[a].y - n[a] * n[b] * nen.y);
+    if (a != b) g = cscale<R>(g, sq2);
+    x[I] = (gp.proj == 1) ? cscale<R>(g, s) : cscale<R>(csub<R>(x[I], g), s);
+  }
+}
+
+// q = A(v) x for one voxel and one load; A component-major with stride M.
+template <typename R, int COEF>
+__device__ __forceinline__ void coef_apply(const R* __restrict__ A, long long M, long long v,
+                                           int dv, const R* x, R* q) {
+  if constexpr (COEF == COEF_NONE) {
+    for (int c = 0; c < dv; ++c) q[c] = x[c];
+  } else if constexpr (COEF == COEF_ISO) {
+    const R a = A[v];
+    for (int c = 0; c < dv; ++c) q[c] = a * x[c];
+  } else if constexpr (COEF == COEF_SYM) {
+    for (int a = 0; a < dv; ++a) {
+      R s = R(0);
+      for (int b = 0; b < dv; ++b) {
+        const int i = a < b ? a : b, j = a < b ? b : a;
+        const int t = i * dv - i * (i - 1) / 2 + (j - i);
+        s += A[(long long)t * M + v] * x[b];
+      }
+      q[a] = s;
+    }
+  } else {
+    for (int a = 0; a < dv; ++a) {
+      R s = R(0);
+      for (int b = 0; b < dv; ++b) s += A[(long long)(a * dv + b) * M + v] * x[b];
+      q[a] = s;
+    }
+  }
+}
+
+constexpr int kMaxDv = 6;
+constexpr int kMaxLoads = 6;
+
+// ---------------------------------------------------------------------------
+// block reductions (double)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Reduces acc[0..n) over the block; thread 0 writes out[0..n).  red must hold
+// (blockDim/32)*n doubles.
+__device__ __forceinline__ void block_sum_n(double* acc, int n, double* red, double* out) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int i = 0; i < n; ++i) {
+    double v = warp_sum(acc[i]);
+    if (lane == 0) red[w * n + i] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < n) {
+    double s = 0.;
+    for (int j = 0; j < nw; ++j) s += red[j * n + threadIdx.x];
+    out[threadIdx.x] = s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// pass 1: r2c along the last axis, with the coefficient multiply in the
+// prologue and (CG) the direction update P = R + beta P.
+// CTA: `rows` consecutive (i0,i1) rows, all comps; comps paired as z = a + i b.
+// ---------------------------------------------------------------------------
+template <typename R, int COEF, bool PUPD>
+__global__ void __launch_bounds__(256) k_r2c_last(
+    const R* xin, R* pio, const R* __restrict__ rvec,
+    const R* __restrict__ A, cplx<R>* __restrict__ S, GridDims g, LineDev<R> L, int rows,
+    const LoadState* __restrict__ st, const int* __restrict__ all_done) {
+  if (all_done && *all_done) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx<R>* buf = reinterpret_cast<cplx<R>*>(smem_raw);
+  const int C = g.L * g.dv;
+  const int np = (C + 1) / 2;
+  const int ld = L.nf;
+  const long long nrows = (long long)g.n0 * g.n1;
+  const long long row0 = (long long)blockIdx.x * rows;
+  const int n = g.n2;
+  const int tasks = rows * n;
+  for (int e = threadIdx.x; e < tasks; e += blockDim.x) {
+    const int rl = e / n, j = e - rl * n;
+    const long long row = row0 + rl;
+    cplx<R>* base = buf + (long long)rl * np * ld;
+    if (row >= nrows) {
+      for (int p = 0; p < np; ++p) base[p * ld + j] = mkc<R>(R(0), R(0));
+      continue;
+    }
+    const long long v = row * n + j;
+    for (int l = 0; l < g.L; ++l) {
+      R xv[kMaxDv], q[kMaxDv];
+      for (int c = 0; c < g.dv; ++c) {
+        const long long idx = (long long)(l * g.dv + c) * g.M + v;
+        R val = PUPD ? pio[idx] : xin[idx];
+        if constexpr (PUPD) {
+          const R bet = R(st[l].beta);
+          val = rvec[idx] + bet * val;
+          if (!st[l].done) pio[idx] = val;
+        }
+        xv[c] = val;
+      }
+      coef_apply<R, COEF>(A, g.M, v, g.dv, xv, q);
+      for (int c = 0; c < g.dv; ++c) {
+        const int comp = l * g.dv + c;
+        cplx<R>* line = base + (comp >> 1) * ld;
+        // slot j of the pair line: real part from even comp, imag from odd
+        R* slot = reinterpret_cast<R*>(line + j) + (comp & 1);
+        *slot = q[c];
+      }
+    }
+    if (C & 1) reinterpret_cast<R*>(base + (np - 1) * ld + j)[1] = R(0);
+  }
+  __syncthreads();
+  if (L.blue) {
+    // chirp pre-multiply of the stored values (put_fwd for Bluestein lines)
+    for (int e = threadIdx.x; e < rows * np * n; e += blockDim.x) {
+      const int line = e / n, j = e - line * n;
+      cplx<R>* p = buf + (long long)line * ld + j;
+      *p = cmul<R>(*p, L.chirp[j]);
+    }
+  }
+  zero_tail<R>(buf, ld, rows * np, L);
+  __syncthreads();
+  line_core<R>(buf, ld, rows * np, L, false);
+  // split the paired spectra: Xa = (Z_k + conj Z_{n-k})/2, Xb = (Z_k - conj Z_{n-k})/(2i)
+  const int n2h = g.n2h;
+  const int otasks = rows * np * n2h;
+  for (int e = threadIdx.x; e < otasks; e += blockDim.x) {
+    const int line = e / n2h, k = e - line * n2h;
+    const int rl = line / np, p = line - rl * np;
+    const long long row = row0 + rl;
+    if (row >= nrows) continue;
+    const cplx<R>* lp = buf + (long long)line * ld;
+    const cplx<R> zk = get_fwd<R>(lp, L, k);
+    const cplx<R> zm = get_fwd<R>(lp, L, k == 0 ? 0 : n - k);
+    const cplx<R> xa = mkc<R>(R(0.5) * (zk.x + zm.x), R(0.5) * (zk.y - zm.y));
+    const cplx<R> xb = mkc<R>(R(0.5) * (zk.y + zm.y), R(0.5) * (zm.x - zk.x));
+    const int ca = 2 * p, cb = 2 * p + 1;
+    S[((long long)ca * nrows + row) * n2h + k] = xa;
+    if (cb < C) S[((long long)cb * nrows + row) * n2h + k] = xb;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// strided c2c pass: lines of length na along an axis with `inner` contiguous
+// elements after it; CTA = tile of T inner columns of one outer index.
+// ---------------------------------------------------------------------------
+template <typename R, bool INV>
+__global__ void __launch_bounds__(256) k_c2c_axis(cplx<R>* __restrict__ S, int na, long long inner,
+                                                  LineDev<R> L, int T,
+                                                  const int* __restrict__ all_done,
+                                                  const LoadState* __restrict__ st,
+                                                  int outer_per_load) {
+  if (all_done && *all_done) return;
+  if (st && outer_per_load > 0 && st[blockIdx.y / outer_per_load].done) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx<R>* buf = reinterpret_cast<cplx<R>*>(smem_raw);
+  const int ld = L.nf;
+  const long long t0 = (long long)blockIdx.x * T;
+  cplx<R>* base = S + (long long)blockIdx.y * na * inner;
+  const int tasks = T * na;
+  for (int e = threadIdx.x; e < tasks; e += blockDim.x) {
+    const int i = e / T, t = e - i * T;
+    const long long col = t0 + t;
+    const cplx<R> v = (col < inner) ? base[(long long)i * inner + col] : mkc<R>(R(0), R(0));
+    if (INV) put_inv<R>(buf + t * ld, L, i, v);
+    else put_fwd<R>(buf + t * ld, L, i, v);
+  }
+  zero_tail<R>(buf, ld, T, L);
+  __syncthreads();
+  line_core<R>(buf, ld, T, L, INV);
+  for (int e = threadIdx.x; e < tasks; e += blockDim.x) {
+    const int i = e / T, t = e - i * T;
+    const long long col = t0 + t;
+    if (col >= inner) continue;
+    base[(long long)i * inner + col] = INV ? get_inv<R>(buf + t * ld, L, i)
+                                           : get_fwd<R>(buf + t * ld, L, i);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// projection pass on the first real axis: forward line DFT, y = G(xi) x over
+// the dv comps of each frequency, inverse line DFT.  CTA = T inner columns of
+// one load; lines (c, t) for c < dv.
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(256) k_proj_first(cplx<R>* __restrict__ S, GridDims g, int na,
+                                                    long long inner, LineDev<R> L, int T,
+                                                    GreenParams gp,
+                                                    const int* __restrict__ all_done,
+                                                    const LoadState* __restrict__ st) {
+  if (all_done && *all_done) return;
+  const int l = blockIdx.y;
+  if (st && st[l].done) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx<R>* buf = reinterpret_cast<cplx<R>*>(smem_raw);
+  const int ld = L.nf;
+  const int dv = g.dv;
+  const long long t0 = (long long)blockIdx.x * T;
+  const int nl = dv * T;
+  const int tasks = nl * na;
+  // coalesced load: consecutive threads take consecutive inner columns
+  for (int e = threadIdx.x; e < tasks; e += blockDim.x) {
+    const int t = e % T;
+    const int rest = e / T;
+    const int i = rest % na;
+    const int c = rest / na;
+    const long long col = t0 + t;
+    const cplx<R>* src = S + ((long long)(l * dv + c) * na) * inner;
+    const cplx<R> v = (col < inner) ? src[(long long)i * inner + col] : mkc<R>(R(0), R(0));
+    put_fwd<R>(buf + (c * T + t) * ld, L, i, v);
+  }
+  zero_tail<R>(buf, ld, nl, L);
+  __syncthreads();
+  line_core<R>(buf, ld, nl, L, false);
+  // Green projection per frequency
+  const int ftasks = T * na;
+  for (int e = threadIdx.x; e < ftasks; e += blockDim.x) {
+    const int t = e % T, k = e / T;
+    const long long col = t0 + t;
+    cplx<R> x[kMaxDv];
+    for (int c = 0; c < dv; ++c) x[c] = get_fwd<R>(buf + (c * T + t) * ld, L, k);
+    if (col < inner) {
+      int kv[3];
+      kv[0] = signed_freq(k, na);
+      if (g.dim == 3) {
+        const int k1 = (int)(col / g.n2h);
+        kv[1] = signed_freq(k1, g.n1);
+        kv[2] = (int)(col - (long long)k1 * g.n2h);
+      } else {
+        kv[1] = (int)col;
+      }
+      green_apply<R>(gp, g.dim, kv, x);
+    }
+    for (int c = 0; c < dv; ++c) put_inv<R>(buf + (c * T + t) * ld, L, k, x[c]);
+  }
+  __syncthreads();
+  zero_tail<R>(buf, ld, nl, L);
+  __syncthreads();
+  line_core<R>(buf, ld, nl, L, true);
+  for (int e = threadIdx.x; e < tasks; e += blockDim.x) {
+    const int t = e % T;
+    const int rest = e / T;
+    const int i = rest % na;
+    const int c = rest / na;
+    const long long col = t0 + t;
+    if (col >= inner) continue;
+    cplx<R>* dst = S + ((long long)(l * dv + c) * na) * inner;
+    dst[(long long)i * inner + col] = get_inv<R>(buf + (c * T + t) * ld, L, i);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// last pass: c2r along the last axis (pairs of comps), scale, store; optional
+// fused dot <p, y> per load (CG's <P, AP>).
+// ---------------------------------------------------------------------------
+template <typename R, bool DOT>
+__global__ void __launch_bounds__(256) k_c2r_last(const cplx<R>* __restrict__ S, R* __restrict__ y,
+                                                  const R* __restrict__ pdot,
+                                                  double* __restrict__ partials, GridDims g,
+                                                  LineDev<R> L, int rows, R scale,
+                                                  const int* __restrict__ all_done) {
+  if (all_done && *all_done) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx<R>* buf = reinterpret_cast<cplx<R>*>(smem_raw);
+  const int C = g.L * g.dv;
+  const int np = (C + 1) / 2;
+  const int ld = L.nf;
+  const long long nrows = (long long)g.n0 * g.n1;
+  const long long row0 = (long long)blockIdx.x * rows;
+  const int n = g.n2, n2h = g.n2h;
+  const int tasks = rows * np * n2h;
+  for (int e = threadIdx.x; e < tasks; e += blockDim.x) {
+    const int line = e / n2h, k = e - line * n2h;
+    const int rl = line / np, p = line - rl * np;
+    const long long row = row0 + rl;
+    cplx<R>* lp = buf + (long long)line * ld;
+    cplx<R> a = mkc<R>(R(0), R(0)), b = mkc<R>(R(0), R(0));
+    if (row < nrows) {
+      const int ca = 2 * p, cb = 2 * p + 1;
+      a = S[((long long)ca * nrows + row) * n2h + k];
+      if (cb < C) b = S[((long long)cb * nrows + row) * n2h + k];
+    }
+    const bool selfconj = (k == 0) || (2 * k == n);
+    if (selfconj) { a.y = R(0); b.y = R(0); }
+    // Z_k = A + iB ; Z_{n-k} = conj(A) + i conj(B)
+    put_inv<R>(lp, L, k, mkc<R>(a.x - b.y, a.y + b.x));
+    if (!selfconj) put_inv<R>(lp, L, n - k, mkc<R>(a.x + b.y, b.x - a.y));
+  }
+  zero_tail<R>(buf, ld, rows * np, L);
+  __syncthreads();
+  line_core<R>(buf, ld, rows * np, L, true);
+  double acc[kMaxLoads];
+  for (int i = 0; i < kMaxLoads; ++i) acc[i] = 0.;
+  const int otasks = rows * np * n;
+  for (int e = threadIdx.x; e < otasks; e += blockDim.x) {
+    const int line = e / n, j = e - line * n;
+    const int rl = line / np, p = line - rl * np;
+    const long long row = row0 + rl;
+    if (row >= nrows) continue;
+    const cplx<R> z = get_inv<R>(buf + (long long)line * ld, L, j);
+    const int ca = 2 * p, cb = 2 * p + 1;
+    const long long v = row * n + j;
+    const R ya = z.x * scale, yb = z.y * scale;
+    y[(long long)ca * g.M + v] = ya;
+    if (cb < C) y[(long long)cb * g.M + v] = yb;
+    if constexpr (DOT) {
+      acc[ca / g.dv] += (double)pdot[(long long)ca * g.M + v] * (double)ya;
+      if (cb < C) acc[cb / g.dv] += (double)pdot[(long long)cb * g.M + v] * (double)yb;
+    }
+  }
+  if constexpr (DOT) {
+    __syncthreads();
+    double* red = reinterpret_cast<double*>(smem_raw);
+    block_sum_n(acc, g.L, red, partials + (long long)blockIdx.x * g.L);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// CG helpers
+// ---------------------------------------------------------------------------
+// partial sums of <x, y> per load (grid-stride over voxels)
+template <typename R>
+__global__ void __launch_bounds__(256) k_dot(const R* __restrict__ x, const R* __restrict__ y,
+                                             double* __restrict__ partials, GridDims g) {
+  __shared__ double red[8 * kMaxLoads];
+  double acc[kMaxLoads];
+  for (int i = 0; i < kMaxLoads; ++i) acc[i] = 0.;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < g.M; v += stride) {
+    for (int l = 0; l < g.L; ++l)
+      for (int c = 0; c < g.dv; ++c) {
+        const long long i = (long long)(l * g.dv + c) * g.M + v;
+        acc[l] += (double)x[i] * (double)y[i];
+      }
+  }
+  block_sum_n(acc, g.L, red, partials + (long long)blockIdx.x * g.L);
+}
+
+// x += alpha P ; R -= alpha AP ; partial <R,R>   (ffthompy/general/solver.py:127-129)
+template <typename R>
+__global__ void __launch_bounds__(256) k_cg_update(R* __restrict__ x, R* __restrict__ r,
+                                                   const R* __restrict__ p,
+                                                   const R* __restrict__ ap,
+                                                   double* __restrict__ partials, GridDims g,
+                                                   const LoadState* __restrict__ st,
+                                                   const int* __restrict__ all_done) {
+  if (all_done && *all_done) return;
+  __shared__ double red[8 * kMaxLoads];
+  double acc[kMaxLoads];
+  double alpha[kMaxLoads];
+  bool act[kMaxLoads];
+  for (int l = 0; l < kMaxLoads; ++l) {
+    acc[l] = 0.;
+    act[l] = l < g.L && !st[l].done;
+    alpha[l] = act[l] ? st[l].alpha : 0.;
+  }
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < g.M; v += stride) {
+    for (int l = 0; l < g.L; ++l) {
+      if (!act[l]) continue;
+      for (int c = 0; c < g.dv; ++c) {
+        const long long i = (long long)(l * g.dv + c) * g.M + v;
+        const double pv = (double)p[i];
+        x[i] = (R)((double)x[i] + alpha[l] * pv);
+        const R rn = (R)((double)r[i] - alpha[l] * (double)ap[i]);
+        r[i] = rn;
+        acc[l] += (double)rn * (double)rn;
+      }
+    }
+  }
+  block_sum_n(acc, g.L, red, partials + (long long)blockIdx.x * g.L);
+}
+
+// Finalise <P,AP>: alpha = rr / pap  (solver.py:126)
+static __global__ void k_fin_pap(const double* __restrict__ partials, int nparts, LoadState* st, int L,
+                          double invM, const int* __restrict__ all_done) {
+  if (all_done && *all_done) return;
+  __shared__ double red[8];
+  const int l = blockIdx.x;
+  if (st[l].done) return;
+  double s = 0.;
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x) s += partials[(long long)i * L + l];
+  double t = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot = 0.;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
+    const double pap = tot * invM;
+    st[l].pap = pap;
+    if (!(pap > 0.) || !isfinite(pap)) {
+      st[l].status = isfinite(pap) ? 2 : 3;
+      st[l].alpha = 0.;
+      st[l].done = 1;
+    } else {
+      st[l].alpha = st[l].rr / pap;
+    }
+  }
+}
+
+// Finalise <R,R>: beta, norm, kit, stopping test (solver.py:129-134,123).
+// Also (first block) refreshes the all-done flag.
+static __global__ void k_fin_rr(const double* __restrict__ partials, int nparts, LoadState* st, int L,
+                         double invM, double* __restrict__ res_log, int log_cap, int* all_done) {
+  __shared__ double red[8];
+  const int l = blockIdx.x;
+  if (*all_done) return;
+  const bool was_done = st[l].done;
+  if (!was_done) {
+    double s = 0.;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) s += partials[(long long)i * L + l];
+    double t = warp_sum(s);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double tot = 0.;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
+      const double rrn = tot * invM;
+      LoadState& S = st[l];
+      S.kit += 1;
+      S.beta = rrn / S.rr;
+      S.rr = rrn;
+      S.norm_res = sqrt(rrn);
+      if (res_log && S.kit < log_cap) res_log[(long long)S.kit * L + l] = S.norm_res;
+      if (!isfinite(rrn)) { S.status = 3; S.done = 1; }
+      if (!(S.norm_res > S.tol && S.kit < S.maxiter)) S.done = 1;
+    }
+  }
+}
+
+// all_done = AND over loads (run after k_fin_rr, one thread)
+static __global__ void k_update_all_done(const LoadState* st, int L, int* all_done) {
+  int d = 1;
+  for (int l = 0; l < L; ++l) d &= st[l].done;
+  *all_done = d;
+}
+
+// initial residual norms: rr = sum/M, norm = sqrt(rr), done = !(norm > tol && 0 < maxiter)
+static __global__ void k_fin_init(const double* __restrict__ partials, int nparts, LoadState* st, int L,
+                           double invM, double* __restrict__ res_log, int log_cap) {
+  const int l = threadIdx.x;
+  if (l >= L) return;
+  double s = 0.;
+  for (int i = 0; i < nparts; ++i) s += partials[(long long)i * L + l];
+  LoadState& S = st[l];
+  S.rr = s * invM;
+  S.norm_res = sqrt(S.rr);
+  S.kit = 0;
+  S.beta = 0.;
+  S.alpha = 0.;
+  S.status = isfinite(S.rr) ? 0 : 3;
+  S.done = !(S.norm_res > S.tol && 0 < S.maxiter) || S.status != 0;
+  if (res_log && log_cap > 0) res_log[l] = S.norm_res;
+}
+
+// y = a*x + b*y elementwise over n values
+template <typename R>
+__global__ void k_axpby(long long n, double a, const R* __restrict__ x, double b, R* __restrict__ y) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    y[i] = (R)(a * (double)x[i] + b * (double)y[i]);
+}
+
+// x[l*dv + c] = val * delta(c, l)  (the constant macroscopic field E_N of load l,
+// ffthompy/applications.py:60-65, with val = -1 for the right-hand side)
+template <typename R>
+__global__ void k_fill_macro(R* __restrict__ x, GridDims g, double val) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long tot = (long long)g.L * g.dv * g.M;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += stride) {
+    const long long comp = i / g.M;
+    const int l = (int)(comp / g.dv), c = (int)(comp - (long long)l * g.dv);
+    x[i] = (c == l) ? (R)val : R(0);
+  }
+}
+
+// A_H partials: sum_v <A(v) u_i(v), u_j(v)>, u_i = X_i + e_i (postprocess.py:53-70,
+// add_macro2minimizer 73-86).  L <= 6 loads -> 36 accumulators.
+template <typename R, int COEF>
+__global__ void __launch_bounds__(128) k_energy(const R* __restrict__ X, const R* __restrict__ A,
+                                                double* __restrict__ partials, GridDims g,
+                                                int add_macro) {
+  __shared__ double red[4 * kMaxLoads * kMaxLoads];
+  const int L = g.L, dv = g.dv;
+  double acc[kMaxLoads * kMaxLoads];
+  for (int i = 0; i < kMaxLoads * kMaxLoads; ++i) acc[i] = 0.;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < g.M; v += stride) {
+    R u[kMaxLoads][kMaxDv];
+    for (int l = 0; l < L; ++l)
+      for (int c = 0; c < dv; ++c)
+        u[l][c] = X[(long long)(l * dv + c) * g.M + v] + ((add_macro && c == l) ? R(1) : R(0));
+    for (int i = 0; i < L; ++i) {
+      R q[kMaxDv];
+      coef_apply<R, COEF>(A, g.M, v, dv, u[i], q);
+      for (int j = 0; j < L; ++j) {
+        double s = 0.;
+        for (int c = 0; c < dv; ++c) s += (double)q[c] * (double)u[j][c];
+        acc[i * L + j] += s;
+      }
+    }
+  }
+  block_sum_n(acc, L * L, red, partials + (long long)blockIdx.x * L * L);
+}
+
+// sum partials[nparts][n] -> out[n] (one block)
+static __global__ void k_sum_partials(const double* __restrict__ partials, int nparts, int n,
+                               double scale, double* __restrict__ out) {
+  for (int j = 0; j < n; ++j) {
+    double s = 0.;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) s += partials[(long long)i * n + j];
+    __shared__ double red[32];
+    double t = warp_sum(s);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double tot = 0.;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
+      out[j] = tot * scale;
+    }
+    __syncthreads();
+  }
+}
+
+// Trigonometric interpolation N -> M on half spectra (Tensor.enlarge,
+// ffthompy/tensors/objects.py:428-467): target coefficient at signed
+// frequency q takes the source coefficient at q (weight 1) when |q| < N/2,
+// half of the Nyquist coefficient when N is even and |q| = N/2, else 0.
+template <typename R>
+__global__ void k_spectrum_pad(const cplx<R>* __restrict__ Sn, cplx<R>* __restrict__ Sm,
+                               int C, int dim, int N0, int N1, int N2, int M0, int M1, int M2) {
+  const int N2h = N2 / 2 + 1, M2h = M2 / 2 + 1;
+  const long long tot = (long long)C * M0 * M1 * M2h;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += stride) {
+    long long r = i;
+    const int k2 = (int)(r % M2h); r /= M2h;
+    const int k1 = (int)(r % M1); r /= M1;
+    const int k0 = (int)(r % M0); r /= M0;
+    const int c = (int)r;
+    double w = 1.;
+    int src[3];
+    const int Ms[2] = {M0, M1}, Ns[2] = {N0, N1}, ks[2] = {k0, k1};
+    bool ok = true;
+    for (int a = 0; a < 2; ++a) {
+      const int q = signed_freq(ks[a], Ms[a]);
+      const int Na = Ns[a];
+      const int aq = q < 0 ? -q : q;
+      if (2 * aq < Na) src[a] = q < 0 ? q + Na : q;
+      else if (2 * aq == Na) { src[a] = Na / 2; w *= 0.5; }
+      else { ok = false; break; }
+    }
+    if (ok) {
+      if (2 * k2 < N2) src[2] = k2;
+      else if (2 * k2 == N2) { src[2] = N2 / 2; w *= 0.5; }
+      else ok = false;
+    }
+    cplx<R> v = mkc<R>(R(0), R(0));
+    if (ok) {
+      const cplx<R> s = Sn[(((long long)c * N0 + src[0]) * N1 + src[1]) * N2h + src[2]];
+      v = mkc<R>((R)(w * (double)s.x), (R)(w * (double)s.y));
+    }
+    Sm[i] = v;
+  }
+}
+
+// Ga grid-based coefficient spectrum (ffthompy/materials.py:77-110): target
+// half-spectrum entry (t0,t1,t2) of the 2N-1 grid takes the source DFT
+// coefficient at (src0[t0], src1[t1], src2[t2]) of the P-grid image (the
+// reference's periodic tiling + central crop, as per-axis index tables) times
+// the separable cell-shape weights w0[t0] w1[t1] w2[t2].  Sources outside the
+// stored half spectrum are read through Hermitian symmetry.
+template <typename R>
+__global__ void k_ga_gather(const cplx<R>* __restrict__ Sp, cplx<R>* __restrict__ St, int C,
+                            int P0, int P1, int P2, int T0, int T1, int T2,
+                            const int* __restrict__ src, const double* __restrict__ w) {
+  const int P2h = P2 / 2 + 1, T2h = T2 / 2 + 1;
+  const int* s0 = src;
+  const int* s1 = src + T0;
+  const int* s2 = src + T0 + T1;
+  const double* w0 = w;
+  const double* w1 = w + T0;
+  const double* w2 = w + T0 + T1;
+  const long long tot = (long long)C * T0 * T1 * T2h;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += stride) {
+    long long r = i;
+    const int t2 = (int)(r % T2h); r /= T2h;
+    const int t1 = (int)(r % T1); r /= T1;
+    const int t0 = (int)(r % T0); r /= T0;
+    const int c = (int)r;
+    int a0 = s0[t0], a1 = s1[t1], a2 = s2[t2];
+    bool conj = false;
+    if (a2 >= P2h) {  // X[a] = conj(X[-a])
+      a2 = P2 - a2;
+      a0 = a0 ? P0 - a0 : 0;
+      a1 = a1 ? P1 - a1 : 0;
+      conj = true;
+    }
+    cplx<R> v = Sp[(((long long)c * P0 + a0) * P1 + a1) * P2h + a2];
+    if (conj) v.y = -v.y;
+    const double ww = w0[t0] * w1[t1] * w2[t2];
+    St[i] = mkc<R>((R)(ww * (double)v.x), (R)(ww * (double)v.y));
+  }
+}
+
+struct LoadScale { double v[kMaxLoads]; };
+
+// r = b - ax ; partial sum r^2 per load
+template <typename R>
+__global__ void __launch_bounds__(256) k_residual(const R* __restrict__ b, const R* __restrict__ ax,
+                                                  R* __restrict__ r, double* __restrict__ partials,
+                                                  GridDims g) {
+  __shared__ double red[8 * kMaxLoads];
+  double acc[kMaxLoads];
+  for (int i = 0; i < kMaxLoads; ++i) acc[i] = 0.;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < g.M; v += stride)
+    for (int l = 0; l < g.L; ++l)
+      for (int c = 0; c < g.dv; ++c) {
+        const long long i = (long long)(l * g.dv + c) * g.M + v;
+        const R rv = b[i] - ax[i];
+        r[i] = rv;
+        acc[l] += (double)rv * (double)rv;
+      }
+  block_sum_n(acc, g.L, red, partials + (long long)blockIdx.x * g.L);
+}
+
+// dst = s_l * src, src in FP64 (refinement: scaled residual into the working precision)
+template <typename RO>
+__global__ void k_scale_from64(const double* __restrict__ src, RO* __restrict__ dst, GridDims g,
+                               LoadScale s) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long tot = (long long)g.L * g.dv * g.M;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += stride)
+    dst[i] = (RO)(s.v[i / ((long long)g.dv * g.M)] * src[i]);
+}
+
+// x += s_l * d, x in FP64 (refinement: correction of the working precision)
+template <typename RI>
+__global__ void k_add_scaled_to64(const RI* __restrict__ d, double* __restrict__ x, GridDims g,
+                                  LoadScale s) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long tot = (long long)g.L * g.dv * g.M;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += stride)
+    x[i] += s.v[i / ((long long)g.dv * g.M)] * (double)d[i];
+}
+
+// precision conversion
+template <typename RO, typename RI>
+__global__ void k_convert(long long n, const RI* __restrict__ in, RO* __restrict__ out) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    out[i] = (RO)in[i];
+}
+
+}  // namespace fhp

@@ -1,0 +1,269 @@
+"""Python handle of one C-ABI plan (GPU Fourier-Galerkin operator + CG).
+
+Device memory for fields is allocated with torch (plumbing only); all
+arithmetic on the hot path runs in the library's own CUDA kernels.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+try:
+    import torch
+except ImportError:  # pragma: no cover - torch is a hard requirement on GPU hosts
+    torch = None
+
+
+def require_cuda():
+    if torch is None or not torch.cuda.is_available():
+        raise RuntimeError('ffthompy_gb300 needs a CUDA GPU; no CPU fallback exists')
+
+
+def coef_kind_of(A):
+    """Classify a coefficient array (dv, dv) + grid: ISO, SYM or FULL."""
+    dv = A.shape[0]
+    off = np.ones((dv, dv), dtype=bool)
+    np.fill_diagonal(off, False)
+    diag = np.stack([A[i, i] for i in range(dv)])
+    if not np.any(A[off]) and np.all(diag == diag[0:1]):
+        return _lib.FHP_COEF_ISO
+    if all(np.array_equal(A[i, j], A[j, i]) for i in range(dv) for j in range(i + 1, dv)):
+        return _lib.FHP_COEF_SYM
+    return _lib.FHP_COEF_FULL
+
+
+def pack_coefficient(A, kind):
+    """Component-major float64 values for fhp_set_coefficient."""
+    dv = A.shape[0]
+    if kind == _lib.FHP_COEF_ISO:
+        return np.ascontiguousarray(A[0, 0][None], dtype=np.float64)
+    if kind == _lib.FHP_COEF_SYM:
+        comps = [A[i, j] for i in range(dv) for j in range(i, dv)]
+        return np.ascontiguousarray(np.stack(comps), dtype=np.float64)
+    return np.ascontiguousarray(A.reshape((dv * dv,) + A.shape[2:]), dtype=np.float64)
+
+
+def coef_kind_of_torch(A):
+    dv = A.shape[0]
+    offdiag = any(bool(A[i, j].any()) for i in range(dv) for j in range(dv) if i != j)
+    if not offdiag and all(bool(torch.equal(A[i, i], A[0, 0])) for i in range(1, dv)):
+        return _lib.FHP_COEF_ISO
+    if all(bool(torch.equal(A[i, j], A[j, i])) for i in range(dv) for j in range(i + 1, dv)):
+        return _lib.FHP_COEF_SYM
+    return _lib.FHP_COEF_FULL
+
+
+def pack_coefficient_torch(A, kind):
+    dv = A.shape[0]
+    if kind == _lib.FHP_COEF_ISO:
+        return A[0, 0][None].contiguous()
+    if kind == _lib.FHP_COEF_SYM:
+        return torch.stack([A[i, j] for i in range(dv) for j in range(i, dv)]).contiguous()
+    return A.reshape((dv * dv,) + tuple(A.shape[2:])).contiguous()
+
+
+class GalerkinPlan:
+    """G o A on one solve grid for a batch of load cases.
+
+    N: solve grid; band: grid whose band carries the Green projection
+    (GaNi: band = N; Ga: N = 2*band - 1); scale: Ga scale prod(N)/prod(band)
+    by default; physics 'scalar' | 'elasticity'; precision 'f64' | 'f32' |
+    'mixed' (FP64 fields, FP32 inner CG with FP64 iterative refinement).
+    """
+
+    def __init__(self, N, Y, physics='scalar', nloads=None, band=None, scale=None,
+                 precision='f64'):
+        require_cuda()
+        self.lib = _lib.load()
+        self.N = tuple(int(n) for n in N)
+        self.dim = len(self.N)
+        self.band = tuple(int(n) for n in (band if band is not None else N))
+        self.Y = np.asarray(Y, dtype=np.float64)
+        self.physics = physics
+        self.dv = self.dim if physics == 'scalar' else self.dim * (self.dim + 1) // 2
+        self.nloads = int(nloads if nloads is not None else self.dv)
+        if scale is None:
+            scale = float(np.prod(self.N, dtype=np.float64) / np.prod(self.band, dtype=np.float64))
+        self.scale = float(scale)
+        self.precision = precision
+        if precision not in ('f64', 'f32', 'mixed'):
+            raise ValueError('precision must be f64, f32 or mixed')
+        self.dtype = torch.float32 if precision == 'f32' else torch.float64
+        self.device = torch.device('cuda', torch.cuda.current_device())
+        n = (ctypes.c_int * self.dim)(*self.N)
+        nb = (ctypes.c_int * self.dim)(*self.band)
+        y = (ctypes.c_double * self.dim)(*self.Y)
+        h = ctypes.c_void_p()
+        phys = _lib.FHP_SCALAR if physics == 'scalar' else _lib.FHP_ELASTICITY
+        prec = {'f64': _lib.FHP_F64, 'f32': _lib.FHP_F32, 'mixed': _lib.FHP_MIXED}[precision]
+        _lib.check(self.lib.fhp_plan_create(ctypes.byref(h), self.dim, n, nb, y, phys,
+                                            self.nloads, self.scale, prec), 'fhp_plan_create')
+        self.handle = h
+        self.coef_kind = None
+
+    def __del__(self):
+        h = getattr(self, 'handle', None)
+        if h is not None and h.value:
+            self.lib.fhp_plan_destroy(h)
+            self.handle = None
+
+    # -- helpers ---------------------------------------------------------------
+    @property
+    def field_shape(self):
+        return (self.nloads, self.dv) + self.N
+
+    def empty(self):
+        return torch.empty(self.field_shape, dtype=self.dtype, device=self.device)
+
+    def _stream(self):
+        return ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+
+    def _dev(self, x):
+        if not isinstance(x, torch.Tensor):
+            x = torch.as_tensor(np.asarray(x))
+        x = x.to(device=self.device, dtype=self.dtype).contiguous()
+        if tuple(x.shape) != self.field_shape:
+            x = x.reshape(self.field_shape)
+        return x
+
+    @staticmethod
+    def _ptr(x):
+        return ctypes.c_void_p(x.data_ptr())
+
+    def launches(self):
+        return int(self.lib.fhp_plan_launches(self.handle))
+
+    def profile(self, enable=True):
+        """Start (reset) or stop per-kernel CUDA-event timing."""
+        _lib.check(self.lib.fhp_profile_enable(self.handle, int(bool(enable))), 'profile')
+
+    def profile_read(self, max_kinds=32):
+        """{kernel: {'launches', 'ms', 'bytes_per_launch'}} of the recorded passes."""
+        names = ctypes.create_string_buffer(64 * max_kinds)
+        la = (ctypes.c_longlong * max_kinds)()
+        ms = (ctypes.c_double * max_kinds)()
+        by = (ctypes.c_double * max_kinds)()
+        nk = ctypes.c_int()
+        _lib.check(self.lib.fhp_profile_read(self.handle, max_kinds, names, la, ms, by,
+                                             ctypes.byref(nk)), 'profile_read')
+        out = {}
+        for i in range(min(nk.value, max_kinds)):
+            nm = names.raw[64 * i:64 * (i + 1)].split(b'\0')[0].decode()
+            out[nm] = {'launches': int(la[i]), 'ms': float(ms[i]),
+                       'bytes_per_launch': float(by[i])}
+        return out
+
+    # -- API -------------------------------------------------------------------
+    def set_coefficient(self, A, kind=None):
+        """A: (dv, dv) + N coefficient (numpy, or torch on the GPU), origin 0."""
+        shape = (self.dv, self.dv) + self.N
+        if tuple(A.shape) != shape:
+            raise ValueError('coefficient shape %s, expected %s' % (tuple(A.shape), shape))
+        if isinstance(A, torch.Tensor) and A.is_cuda:
+            A = A.detach().to(self.device, torch.float64)
+            kind = coef_kind_of_torch(A) if kind is None else kind
+            vals = pack_coefficient_torch(A, kind)
+            _lib.check(self.lib.fhp_set_coefficient(self.handle, kind, self._ptr(vals), 1,
+                                                    self._stream()), 'fhp_set_coefficient')
+        else:
+            if isinstance(A, torch.Tensor):
+                A = A.detach().cpu().numpy()
+            A = np.asarray(A, dtype=np.float64)
+            kind = coef_kind_of(A) if kind is None else kind
+            vals = pack_coefficient(A, kind)
+            _lib.check(self.lib.fhp_set_coefficient(self.handle, kind, vals.ctypes.data_as(
+                ctypes.c_void_p), 0, self._stream()), 'fhp_set_coefficient')
+        torch.cuda.current_stream(self.device).synchronize()
+        self.coef_kind = kind
+
+    def apply(self, x, proj=1):
+        x = self._dev(x)
+        y = self.empty()
+        _lib.check(self.lib.fhp_apply(self.handle, proj, self._ptr(x), self._ptr(y),
+                                      self._stream()), 'fhp_apply')
+        return y
+
+    def rhs_macro(self, proj=1):
+        b = self.empty()
+        _lib.check(self.lib.fhp_rhs_macro(self.handle, proj, self._ptr(b), self._stream()),
+                   'fhp_rhs_macro')
+        return b
+
+    def cg(self, b, x0=None, tol=1e-6, maxiter=1000, proj=1, log_rows=None):
+        """Batched CG; returns (x, info) with per-load kit / norm_res / res_log."""
+        b = self._dev(b)
+        x0p = ctypes.c_void_p(None)
+        if x0 is not None:
+            x0 = self._dev(x0)
+            x0p = self._ptr(x0)
+        x = self.empty()
+        L = self.nloads
+        kit = (ctypes.c_int * L)()
+        nres = (ctypes.c_double * L)()
+        stat = (ctypes.c_int * L)()
+        maxiter = int(maxiter)
+        rows = int(log_rows if log_rows is not None else min(maxiter + 1, 100001))
+        log = np.zeros((rows, L))
+        st = self.lib.fhp_cg_solve(self.handle, proj, self._ptr(b), x0p, float(tol), maxiter,
+                                   self._ptr(x), kit, nres, stat,
+                                   log.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), rows,
+                                   self._stream())
+        _lib.check(st, 'fhp_cg_solve')
+        kits = list(kit)
+        info = {'kit': kits, 'norm_res': list(nres), 'status': list(stat),
+                'res_log': [log[:k + 1, l].copy() for l, k in enumerate(kits)]}
+        return x, info
+
+    def energy(self, X, add_macro=True):
+        """A_H[i, j] = <A u_i, u_j> over the solve grid (u = X + E if add_macro)."""
+        X = self._dev(X)
+        L = self.nloads
+        AH = np.zeros((L, L))
+        _lib.check(self.lib.fhp_energy_matrix(self.handle, self._ptr(X), int(bool(add_macro)),
+                                              AH.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                              self._stream()), 'fhp_energy_matrix')
+        return AH
+
+    def interpolate_to(self, other, x):
+        """Trigonometric interpolation of fields x onto other's grid."""
+        x = self._dev(x)
+        y = other.empty()
+        _lib.check(self.lib.fhp_fourier_interp(self.handle, other.handle, self._ptr(x),
+                                               self._ptr(y), self._stream()),
+                   'fhp_fourier_interp')
+        return y
+
+    def homogenize_host(self, A=None, proj=1, tol=1e-6, maxiter=1000, return_solution=False,
+                        packed=None, kind=None):
+        """End to end with host buffers: coefficient in, A_H out (fhp_homogenize_host).
+
+        A: (dv, dv) + N host coefficient, or packed: host values already in the
+        layout of kind (e.g. a(x) for FHP_COEF_ISO, shape (1,) + N or N).
+        """
+        if packed is not None:
+            if kind is None:
+                raise ValueError('packed values need their kind')
+            vals = np.ascontiguousarray(packed, dtype=np.float64)
+        else:
+            A = np.asarray(A, dtype=np.float64)
+            kind = coef_kind_of(A)
+            vals = pack_coefficient(A, kind)
+        L = self.nloads
+        AH = np.zeros((L, L))
+        kit = (ctypes.c_int * L)()
+        nres = (ctypes.c_double * L)()
+        xh = None
+        xp = ctypes.c_void_p(None)
+        if return_solution:
+            xh = np.zeros(self.field_shape, dtype=np.float32 if self.precision == 'f32'
+                          else np.float64)
+            xp = xh.ctypes.data_as(ctypes.c_void_p)
+        st = self.lib.fhp_homogenize_host(self.handle, proj, kind,
+                                          vals.ctypes.data_as(ctypes.c_void_p), float(tol),
+                                          int(maxiter),
+                                          AH.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                          kit, nres, xp, self._stream())
+        _lib.check(st, 'fhp_homogenize_host')
+        self.coef_kind = kind
+        return AH, list(kit), list(nres), xh

@@ -1,0 +1,100 @@
+"""Linear solvers, mirroring ffthompy/general/solver.py.
+
+linear_solver(Afun, B, ATfun, x0, par, solver, callback) -> (x, info)
+(solver.py:8-60).  When Afun is a fused G o A Operator and solver is 'CG',
+the whole solve runs on the GPU in one library call (fhp_cg_solve: batched
+CG with FP64 reductions, absolute stopping test sqrt(<R,R>) <= tol,
+solver.py:80-139).  Other operators use the same CG recurrence written with
+Tensor arithmetic on the device.
+"""
+import time
+
+import numpy as np
+
+from ..tensors.objects import Tensor
+from ..tensors.operators import Operator
+from .solver_pp import CallBack
+
+
+def _defaults(par):
+    par = {} if par is None else par
+    par.setdefault('tol', 1e-6)
+    par.setdefault('maxiter', int(1e3))
+    return par
+
+
+def linear_solver(Afun, B, ATfun=None, x0=None, par=None, solver=None, callback=None):
+    t0 = (time.process_time(), time.perf_counter(), time.time())
+    if x0 is None:
+        x0 = B.zeros_like()
+    par = _defaults(par)
+    kind = (solver or 'CG').lower()
+    if kind == 'cg':
+        x, info = CG(Afun, B, x0=x0, par=par, callback=callback)
+    elif kind in ('iterative', 'richardson'):
+        x, info = richardson(Afun, B, x0, par=par, callback=callback)
+    else:
+        raise NotImplementedError('This kind (%s) of linear solver is not implemented' % solver)
+    t1 = (time.process_time(), time.perf_counter(), time.time())
+    info['time'] = [[t1[i] - t0[i] for i in range(3)]]
+    return x, info
+
+
+def CG(Afun, B, x0, par=None, callback=None):
+    par = _defaults(par)
+    if isinstance(Afun, Operator) and Afun.kind == 'GA' and isinstance(B, Tensor):
+        plan = Afun.plan()
+        zero_start = float(x0.data.abs().max()) == 0.0
+        xd, info = plan.cg(B.data[None], None if zero_start else x0.data[None],
+                           tol=par['tol'], maxiter=par['maxiter'], proj=Afun.projection.proj)
+        x = x0.copy(name='x', val=xd[0])
+        log = info['res_log'][0]
+        if isinstance(callback, CallBack):
+            callback.record_log(log)
+        elif callback is not None:
+            callback(x)
+        return x, {'kit': info['kit'][0], 'norm_res': info['norm_res'][0]}
+    return _cg_generic(Afun, B, x0, par, callback)
+
+
+def _cg_generic(Afun, B, x0, par, callback):
+    """solver.py:80-139 with device Tensor arithmetic."""
+    if callback is not None:
+        callback(x0)
+    scal = par.get('scal', lambda X, Y: X * Y)
+    x = x0
+    R = B - Afun(x0)
+    P = R
+    rr = scal(R, R)
+    res = {'kit': 0, 'norm_res': np.double(rr) ** 0.5}
+    while res['norm_res'] > par['tol'] and res['kit'] < par['maxiter']:
+        res['kit'] += 1
+        AP = Afun(P)
+        alp = float(rr / scal(P, AP))
+        x = x + alp * P
+        R = R - alp * AP
+        rrnext = scal(R, R)
+        bet = rrnext / rr
+        rr = rrnext
+        P = R + bet * P
+        res['norm_res'] = np.double(rr) ** 0.5
+        if callback is not None:
+            callback(x)
+    if res['kit'] == 0:
+        res['norm_res'] = 0
+    return x, res
+
+
+def richardson(Afun, B, x0, par=None, callback=None):
+    """solver.py:63-77."""
+    omega = 1. / par['alpha']
+    res = {'norm_res': 1e15, 'kit': 0}
+    x = x0
+    while res['norm_res'] > par['tol'] and res['kit'] < par['maxiter']:
+        res['kit'] += 1
+        residuum = B - Afun(x)
+        x = x + omega * residuum
+        res['norm_res'] = residuum.norm()
+        if callback is not None:
+            callback(x)
+    return x, res

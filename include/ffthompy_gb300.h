@@ -1,0 +1,175 @@
+/*
+ * ffthompy_gb300 -- C ABI of the GB300 Fourier-Galerkin homogenisation library.
+ *
+ * One plan = one solve grid (2D or 3D), one physics (scalar conductivity or
+ * small-strain elasticity in Mandel notation), a batch of nloads macroscopic
+ * load cases solved together, and one working precision.  All field pointers
+ * are DEVICE pointers of the plan's element type (double for FHP_F64, float
+ * for FHP_F32) with layout [load][component][n0][n1][n2] in C order, unless a
+ * function says "host".  `stream` is a cudaStream_t (NULL = legacy default
+ * stream).  Every function returns an FHP_* status code; no function aborts
+ * or traps.  Plans are not re-entrant: one thread and one stream per plan.
+ *
+ * The reference (vondrejc/FFTHomPy, pure Python/NumPy) has no C interface;
+ * each entry point below names the Python call it replaces.  The ctypes
+ * binding that the Python host layer uses is ffthompy_gb300/_lib.py.
+ */
+#ifndef FFTHOMPY_GB300_H
+#define FFTHOMPY_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct fhp_plan_s* fhp_plan;
+
+enum fhp_status {
+  FHP_OK = 0,
+  FHP_NONCONVERGED = 1, /* maxiter reached with norm_res > tol (per load) */
+  FHP_BREAKDOWN = 2,    /* <P, AP> <= 0 */
+  FHP_NONFINITE = 3,    /* NaN/Inf in a reduction */
+  FHP_TIMEOUT = 4,
+  FHP_BAD_ARG = 5,
+  FHP_OOM = 6,
+  FHP_CUDA = 7
+};
+
+/* FHP_MIXED: fields and the outer residual in FP64, inner CG with FP32
+   fields / FFTs and FP64 reductions (iterative refinement). */
+enum fhp_precision { FHP_F64 = 0, FHP_F32 = 1, FHP_MIXED = 2 };
+enum fhp_physics { FHP_SCALAR = 0, FHP_ELASTICITY = 1 };
+/* coefficient storage per voxel: a*I, packed upper triangle, full dv x dv */
+enum fhp_coef_kind { FHP_COEF_ISO = 1, FHP_COEF_SYM = 2, FHP_COEF_FULL = 3 };
+/* Green projection: 1 = G1 (compatible fields, primal), 2 = G2 (dual) */
+
+/* ABI version (major*100 + minor). */
+int fhp_version(void);
+const char* fhp_status_string(int status);
+/* Message of the last failure in this process (empty string if none). */
+const char* fhp_last_error(void);
+
+/*
+ * Create a plan.  n[dim]: solve grid.  n_band[dim]: grid N whose band
+ * |k_i| <= (Nodd_i-1)/2 carries the Green projection (n_band = n for GaNi,
+ * n_band = N with n = 2N-1 for Ga).  g_scale multiplies the projection
+ * (prod(2N-1)/prod(N) for Ga, 1 for GaNi).
+ * Replaces: ffthompy/projections.py:9-112 (scalar), :114-267 (elasticity),
+ * Tensor.enlarge for Ga (ffthompy/tensors/objects.py:428-467) and the DFT /
+ * Operator objects of ffthompy/applications.py:24-37,106-122.
+ */
+int fhp_plan_create(fhp_plan* out, int dim, const int* n, const int* n_band, const double* Y,
+                    int physics, int nloads, double g_scale, int precision);
+int fhp_plan_destroy(fhp_plan plan);
+/* FHP_MIXED plans: inner relative tolerance floor eta (default 1e-4) and the
+   maximum number of refinement steps (default 30). */
+int fhp_plan_set_refinement(fhp_plan plan, double eta, int max_outer);
+/* voxels = prod(n); components = dv per load; elem_bytes = 8 or 4. */
+int fhp_plan_query(fhp_plan plan, long long* voxels, int* components, int* loads,
+                   int* elem_bytes);
+
+/*
+ * Coefficient A on the solve grid, float64 values [c][n0][n1][n2] with
+ * c = 1 (ISO), dv(dv+1)/2 (SYM, packed upper triangle) or dv*dv (FULL);
+ * values on host (on_device = 0) or device.  Converted to the plan precision.
+ * Replaces: the Tensor produced by Material.get_A_GaNi / get_A_Ga
+ * (ffthompy/materials.py:54-123) as the A factor of FiGFA.
+ */
+int fhp_set_coefficient(fhp_plan plan, int kind, const double* values, int on_device,
+                        void* stream);
+
+/*
+ * y = iF( G . F( A . x ) ) for every load (x, y device, all loads).
+ * Replaces: Operator(name='FiGFA', mat=[[GN, A]]).__call__
+ * (ffthompy/applications.py:58, ffthompy/tensors/operators.py:136-144).
+ */
+int fhp_apply(fhp_plan plan, int proj, const void* x, void* y, void* stream);
+
+/*
+ * b_l = FiGFA(-E_l), E_l the constant unit field of load l.
+ * Replaces: B = Afun(-EN) (ffthompy/applications.py:64-69,150-155).
+ */
+int fhp_rhs_macro(fhp_plan plan, int proj, void* b, void* stream);
+
+/*
+ * Conjugate gradients on all loads at once, each load with its own scalars
+ * and stopping test sqrt(<R,R>) <= tol, <u,v> = sum(u*v)/prod(n).
+ * x0 may be NULL (zero start).  kit[loads], norm_res[loads], status[loads]
+ * (host) receive the per-load results (status FHP_OK, FHP_NONCONVERGED,
+ * FHP_BREAKDOWN or FHP_NONFINITE per load; the call itself returns FHP_OK
+ * unless an argument, memory or CUDA error occurred); res_log (host, may be
+ * NULL) receives log_rows x loads residual norms (row k = iteration k).
+ * FHP_MIXED plans run iterative refinement: FP64 residuals, FP32 inner CG.
+ * Replaces: linear_solver(..., solver='CG') / CG
+ * (ffthompy/general/solver.py:8-60, 80-139).
+ */
+int fhp_cg_solve(fhp_plan plan, int proj, const void* b, const void* x0, double tol,
+                 int maxiter, void* x, int* kit, double* norm_res, int* status,
+                 double* res_log, int log_rows, void* stream);
+
+/*
+ * AH[i*loads + j] = <A u_i, u_j>, u_i = X_i + E_i if add_macro else X_i
+ * (AH on host, float64, accumulated in FP64).
+ * Replaces: assembly_matrix (ffthompy/postprocess.py:53-70) with
+ * add_macro2minimizer (ffthompy/postprocess.py:73-86).
+ */
+int fhp_energy_matrix(fhp_plan plan, const void* X, int add_macro, double* AH, void* stream);
+
+/*
+ * Trigonometric interpolation of the fields of plan src onto the grid of
+ * plan dst (same physics, loads, precision; dst grid >= src grid).
+ * Replaces: Tensor.project / Tensor.enlarge (ffthompy/tensors/objects.py:
+ * 428-467, 488-511) as used by assembly_matrix for the Ga bounds.
+ */
+int fhp_fourier_interp(fhp_plan src, fhp_plan dst, const void* x_src, void* x_dst,
+                       void* stream);
+
+/*
+ * End to end with HOST buffers: upload the coefficient, build the right-hand
+ * sides, solve all loads by CG, assemble A_H (with the macroscopic field
+ * added) and copy AH / kit / norm_res (and the solution if x_host != NULL)
+ * back.  Replaces: the per-primal/dual body of applications.scalar /
+ * applications.elasticity with postprocess kind equal to the solve kind
+ * (ffthompy/applications.py:39-90, 124-176).
+ */
+int fhp_homogenize_host(fhp_plan plan, int proj, int coef_kind, const double* coef_host,
+                        double tol, int maxiter, double* AH_host, int* kit_host,
+                        double* norm_res_host, void* x_host, void* stream);
+
+/*
+ * Plain FFT plan of ncomp real fields on grid n (no physics): used for
+ * coefficient assembly.  Fields are [ncomp][n0][n1][n2].
+ */
+int fhp_fft_plan_create(fhp_plan* out, int dim, const int* n, int ncomp, int precision);
+
+/*
+ * Exact-integration coefficient of a voxel image on the 2N-1 grid:
+ * out = real( iDFT( W . H ) ) with H the DFT of the image on grid P read
+ * through the per-axis source index tables src_index (host, concatenated per
+ * axis, sum(n_out) ints; the reference's periodic tiling + central crop) and
+ * W the separable cell-shape weights (host, concatenated per axis, doubles).
+ * image (device, plan_img grid, origin 0) and out (device, plan_out grid,
+ * origin 0) hold ncomp fields each.
+ * Replaces: Material.get_A_Ga grid-based branch (ffthompy/materials.py:77-110).
+ */
+int fhp_ga_grid_coefficient(fhp_plan plan_img, fhp_plan plan_out, const void* image,
+                            const int* src_index, const double* weights, void* out,
+                            void* stream);
+
+/*
+ * Per-kernel timing with CUDA events recorded on the launch stream around each
+ * operator / CG pass (enable resets the counters).  fhp_profile_read returns
+ * up to max_kinds entries: names (64 chars each), launches, total ms and the
+ * algorithmic bytes per launch (each input read once, each output written
+ * once); *nkinds receives the number of kinds recorded.
+ */
+int fhp_profile_enable(fhp_plan plan, int enable);
+int fhp_profile_read(fhp_plan plan, int max_kinds, char* names, long long* launches,
+                     double* total_ms, double* bytes_per_launch, int* nkinds);
+
+/* Number of kernel launches issued by this plan since creation. */
+long long fhp_plan_launches(fhp_plan plan);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FFTHOMPY_GB300_H */

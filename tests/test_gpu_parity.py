@@ -1,0 +1,311 @@
+"""GPU parity of the CUDA Fourier-Galerkin path against the oracle and the
+reference's golden data (all calls go through the C ABI).
+
+Tolerances: FP64 operator 1e-12 relative (max-norm), FP64 A_H 1e-10
+relative; FP32 fields/FFT with FP64 reductions: operator 2e-5; mixed
+precision (FP32 inner CG refined with FP64 residuals to the problem's own
+tolerance): A_H 1e-9.  CG iteration counts equal those of the reference; on
+randomly generated, ill-conditioned problems (contrast 100, 50-80 iterations)
+a difference of one iteration is accepted only when the oracle's residual at
+that iteration lies within 25% of the tolerance: CG residual histories of
+such problems drift by several percent under different (equally accurate)
+FFT roundoff, so the two runs can straddle tol.
+"""
+import numpy as np
+import pytest
+
+import golden_io
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip('torch')
+
+
+@pytest.fixture(scope='module', autouse=True)
+def _built():
+    if not torch.cuda.is_available():
+        pytest.skip('needs a CUDA GPU')
+    import __graft_entry__
+    __graft_entry__.build()
+
+
+def _plan(N, Y, physics, kind, nloads=None, precision='f64'):
+    from ffthompy_gb300.engine import GalerkinPlan
+    N = np.asarray(N)
+    Ns = N if kind == 'GaNi' else 2 * N - 1
+    return GalerkinPlan(tuple(Ns), Y, physics=physics, nloads=nloads, band=tuple(N),
+                        precision=precision)
+
+
+def _relmax(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+@pytest.mark.parametrize('name', golden_io.names('op_'))
+@pytest.mark.parametrize('precision', ['f64', 'f32'])
+def test_operator_matches_reference(name, precision):
+    meta, arr = golden_io.load(name)
+    dv = arr['x'].shape[0]
+    plan = _plan(meta['N'], meta['Y'], meta['physics'], meta['kind'], nloads=1,
+                 precision=precision)
+    plan.set_coefficient(arr['A'])
+    tol = 1e-12 if precision == 'f64' else 2e-5
+    for proj in (1, 2):
+        y = plan.apply(arr['x'][None], proj=proj)[0].double().cpu().numpy()
+        assert y.shape == (dv,) + tuple(meta['Nbar'])
+        assert _relmax(y, arr['y%d' % proj]) < tol, (proj, _relmax(y, arr['y%d' % proj]))
+
+
+SIZES = [((5, 7), 'GaNi'), ((9, 8), 'GaNi'), ((45, 45), 'Ga'), ((64, 30), 'GaNi'),
+         ((89, 127), 'GaNi'), ((128, 255), 'GaNi'), ((253, 16), 'GaNi'), ((29, 31), 'GaNi'),
+         ((11, 13, 17), 'GaNi'), ((16, 9, 25), 'Ga'), ((7, 63, 10), 'GaNi'),
+         ((31, 45, 12), 'GaNi')]
+
+
+@pytest.mark.parametrize('N,kind', SIZES)
+@pytest.mark.parametrize('physics', ['scalar', 'elasticity'])
+def test_operator_random_sizes(N, kind, physics):
+    """Radix / Bluestein coverage: G o A vs the oracle on seeded random data."""
+    rng = np.random.default_rng(sum(N))
+    d = len(N)
+    Ns = np.asarray(N) if kind == 'GaNi' else 2 * np.asarray(N) - 1
+    dv = d if physics == 'scalar' else d * (d + 1) // 2
+    Y = 0.5 + rng.random(d)
+    B = rng.standard_normal((dv, dv) + tuple(Ns))
+    A = np.einsum('ik...,jk...->ij...', B, B) + np.einsum('ij,...->ij...', np.eye(dv),
+                                                          np.ones(tuple(Ns)))
+    x = rng.standard_normal((2, dv) + tuple(Ns))
+    plan = _plan(N, Y, physics, kind, nloads=2)
+    plan.set_coefficient(A)
+    for proj in (1, 2):
+        G, _ = oracle.green_operator(physics, np.asarray(N), Y, kind, proj)
+        y = plan.apply(x, proj=proj).cpu().numpy()
+        for l in range(2):
+            ref = oracle.apply_GA(G, A, x[l])
+            assert _relmax(y[l], ref) < 1e-12, (proj, l, _relmax(y[l], ref))
+
+
+@pytest.mark.parametrize('N', [(9, 9), (12, 10), (5, 7, 9), (6, 5, 8)])
+@pytest.mark.parametrize('physics', ['scalar', 'elasticity'])
+def test_projection_idempotent_orthogonal(N, physics):
+    """unittest_operators.py:177-203 on the GPU: G1 G1 = G1, G2 G2 = G2, G1 G2 = 0."""
+    rng = np.random.default_rng(3)
+    d = len(N)
+    dv = d if physics == 'scalar' else d * (d + 1) // 2
+    plan = _plan(N, np.ones(d), physics, 'GaNi', nloads=1)
+    eye = np.zeros((dv, dv) + N)
+    for i in range(dv):
+        eye[i, i] = 1.
+    plan.set_coefficient(eye)
+    x = rng.standard_normal((1, dv) + N)
+    g1 = plan.apply(x, 1)
+    g2 = plan.apply(x, 2)
+    scale = float(np.abs(x).max())
+    assert float((plan.apply(g1, 1) - g1).abs().max()) < 1e-13 * scale
+    assert float((plan.apply(g2, 2) - g2).abs().max()) < 1e-13 * scale
+    assert float(plan.apply(g1, 2).abs().max()) < 1e-13 * scale
+    # G1 + G2 = I - mean (odd N); for even N the Nyquist frequencies are zeroed
+    # by both projections (NyqNul, projections.py:37-42), so the remainder must
+    # lie in the kernel of both
+    xm = x - x.reshape(1, dv, -1).mean(-1).reshape((1, dv) + (1,) * d)
+    rest = torch.as_tensor(xm, device=g1.device) - g1 - g2
+    if all(n % 2 for n in N):
+        assert float(rest.abs().max()) < 1e-13 * scale
+    else:
+        assert float(plan.apply(rest, 1).abs().max()) < 1e-13 * scale
+        assert float(plan.apply(rest, 2).abs().max()) < 1e-13 * scale
+
+
+def _check_problem(name, precision='f64'):
+    from ffthompy_gb300.problem import Problem
+    prob, exp = golden_io.problem(name)
+    if precision != 'f64':
+        prob['solve'] = dict(prob['solve'], precision=precision)
+    pb = Problem(prob, None)
+    pb.calculate()
+    ref_run = oracle.solve_problem(golden_io.problem(name)[0]) if name.startswith('run_') \
+        else None
+    for pd, mats in exp['mat'].items():
+        got = pb.output['mat_' + pd]
+        assert set(got) == set(mats)
+        for key, ref in mats.items():
+            err = _relmax(got[key], ref)
+            lim = 1e-10 if precision == 'f64' else 1e-9
+            assert err < lim, (key, err)
+            assert np.abs(got[key] - ref).max() <= 1e-9 * max(1., np.abs(ref).max())
+        kits = [r['info']['kit'] for r in pb.output['res_' + pd]]
+        if precision != 'f64':
+            continue
+        for l, (k, kr) in enumerate(zip(kits, exp['kit'][pd])):
+            if k == kr:
+                continue
+            assert abs(k - kr) == 1 and ref_run is not None, (pd, l, kits, list(exp['kit'][pd]))
+            tol = prob['solver']['tol']
+            marg = ref_run['res_' + pd][l]['res_log'][min(k, kr)]
+            assert abs(marg - tol) < 0.25 * tol, (pd, l, marg, tol)
+        sols = np.stack([s.val for s in pb.output['sol_' + pd]])
+        if name.startswith('ref_'):
+            sols = np.fft.fftshift(sols, axes=tuple(range(2, sols.ndim)))
+        assert np.abs(sols - exp['sol'][pd]).max() < 1e-7
+
+
+@pytest.mark.parametrize('name', golden_io.names('ref_'))
+def test_golden_problems_fp64(name):
+    """The reference's own golden tests (run_unittests.py:36-66) on the GPU."""
+    _check_problem(name)
+
+
+@pytest.mark.parametrize('name', golden_io.names('run_'))
+def test_generated_problems_fp64(name):
+    _check_problem(name)
+
+
+@pytest.mark.parametrize('name', ['run_cfg1_square45', 'run_s3_ga_7', 'run_e3_gani_7',
+                                  'ref_scalar_3d_prob2', 'ref_linelas_3d_prob2',
+                                  'run_s2_ga_aniso'])
+def test_problems_mixed(name):
+    _check_problem(name, precision='mixed')
+
+
+def test_pure_fp32_cg_reports_floor():
+    """FP32 CG alone stops at its accuracy floor with a status, never a fault."""
+    from ffthompy_gb300.engine import GalerkinPlan
+    prob, exp = golden_io.problem('run_s3_ga_7')
+    N = np.asarray(prob['solve']['N'])
+    A = oracle.Material(dict(prob['material'])).get_A_Ga(2 * N - 1, 'primal')
+    plan = GalerkinPlan(tuple(2 * N - 1), np.ones(3), band=tuple(N), precision='f32')
+    plan.set_coefficient(A)
+    X, info = plan.cg(plan.rhs_macro(1), tol=1e-12, maxiter=400)
+    assert all(s in (1, 2) for s in info['status'])
+    AH = plan.energy(X)
+    ref = exp['mat']['primal']['AH_Ga_primal']
+    assert _relmax(AH, ref) < 1e-5
+
+
+def test_cfg1_bounds_and_iterations():
+    """Config 1 (2D GaNi 45^2 square, tol 1e-8): A_H, bounds and 25/22 iterations."""
+    from ffthompy_gb300.problem import Problem
+    prob, exp = golden_io.problem('run_cfg1_square45')
+    pb = Problem(prob, None)
+    pb.calculate()
+    m = pb.output
+    assert abs(m['mat_primal']['AH_GaNi_primal'][0, 0] - 1.901848083527682) < 2e-10
+    assert abs(m['mat_primal']['AH_Ga_primal'][0, 0] - 1.979683324453124) < 2e-10
+    assert abs(m['mat_dual']['AH_Ga_dual'][0, 0] - 1.8847530656481177) < 2e-10
+    assert [r['info']['kit'] for r in m['res_primal']] == [25, 25]
+    assert [r['info']['kit'] for r in m['res_dual']] == [22, 22]
+    lo = m['mat_dual']['AH_Ga_dual'][0, 0]
+    hi = m['mat_primal']['AH_Ga_primal'][0, 0]
+    assert lo <= m['mat_primal']['AH_GaNi_primal'][0, 0] <= hi
+
+
+def test_energy_and_interpolation_vs_oracle():
+    rng = np.random.default_rng(11)
+    from ffthompy_gb300.engine import GalerkinPlan
+    for N, M in (((5, 7), (9, 13)), ((6, 4), (11, 7)), ((5, 4, 3), (9, 7, 5))):
+        d = len(N)
+        src = GalerkinPlan(N, np.ones(d), nloads=d)
+        dst = GalerkinPlan(M, np.ones(d), nloads=d)
+        x = rng.standard_normal((d, d) + N)
+        y = src.interpolate_to(dst, x).cpu().numpy()
+        for l in range(d):
+            np.testing.assert_allclose(y[l], oracle.project(x[l], M), atol=1e-12)
+        A = np.einsum('ij,...->ij...', np.eye(d), 1 + rng.random(M))
+        dst.set_coefficient(A)
+        AH = dst.energy(y, add_macro=True)
+        sols = []
+        for l in range(d):
+            u = oracle.project(x[l], M).copy()
+            u[l] += 1.
+            sols.append(u)
+        np.testing.assert_allclose(AH, oracle.assembly_matrix(A, sols), rtol=1e-12)
+
+
+def test_status_codes_without_fault():
+    """Edge cases return statuses, never trap: maxiter=0, tol reached at start,
+    non-convergence, NaN coefficient."""
+    from ffthompy_gb300.engine import GalerkinPlan
+    N = (9, 9)
+    plan = GalerkinPlan(N, [1., 1.], nloads=2)
+    A = np.einsum('ij,...->ij...', np.eye(2), 1 + np.random.default_rng(0).random(N))
+    plan.set_coefficient(A)
+    B = plan.rhs_macro(1)
+    x, info = plan.cg(B, tol=1e-8, maxiter=0)
+    assert info['kit'] == [0, 0] and info['norm_res'] == [0.0, 0.0]
+    x, info = plan.cg(B, tol=1e3, maxiter=10)
+    assert info['kit'] == [0, 0]
+    x, info = plan.cg(B, tol=1e-30, maxiter=3)
+    assert info['kit'] == [3, 3] and info['status'] == [1, 1]
+    A2 = A.copy()
+    A2[0, 0, 3, 3] = np.nan
+    A2[1, 1, 3, 3] = np.nan
+    plan.set_coefficient(A2)
+    B = plan.rhs_macro(1)
+    x, info = plan.cg(B, tol=1e-8, maxiter=5)
+    assert all(s == 3 for s in info['status'])
+    # the context stays usable
+    plan.set_coefficient(A)
+    B = plan.rhs_macro(1)
+    x, info = plan.cg(B, tol=1e-8, maxiter=100)
+    assert info['status'] == [0, 0]
+
+
+def test_homogenize_host_matches_device_path():
+    """The host-buffer entry point (e2e) gives the same A_H as the device calls."""
+    from ffthompy_gb300.engine import GalerkinPlan
+    rng = np.random.default_rng(5)
+    N = (11, 9, 7)
+    A = np.einsum('ij,...->ij...', np.eye(3), 1 + 10 * rng.random(N))
+    p1 = GalerkinPlan(N, np.ones(3), nloads=3)
+    AH, kit, nres, xh = p1.homogenize_host(A, proj=1, tol=1e-9, maxiter=500,
+                                           return_solution=True)
+    p2 = GalerkinPlan(N, np.ones(3), nloads=3)
+    p2.set_coefficient(A)
+    X, info = p2.cg(p2.rhs_macro(1), tol=1e-9, maxiter=500)
+    np.testing.assert_allclose(AH, p2.energy(X), rtol=1e-13)
+    assert kit == info['kit']
+    np.testing.assert_allclose(xh, X.cpu().numpy(), atol=1e-13)
+
+
+def test_tensor_operator_api():
+    """The tutorial-04 style direct API (tutorials/04_exact_integration_fast.py:70-97)."""
+    import ffthompy_gb300.projections as proj
+    from ffthompy_gb300.general.solver import linear_solver
+    from ffthompy_gb300.materials import Material
+    from ffthompy_gb300.tensors import DFT, Operator, Tensor
+    dim = 2
+    N = np.array([15, 15])
+    mat_conf = {'Y': np.ones(dim), 'inclusions': ['square', 'otherwise'],
+                'positions': [np.zeros(dim), ''], 'params': [0.6 * np.ones(dim), ''],
+                'vals': [11 * np.eye(dim), np.eye(dim)], 'order': 1, 'P': 5 * np.ones(dim, int)}
+    mat = Material(dict(mat_conf))
+    Nbar = 2 * N - 1
+    A = mat.get_A_Ga(Nbar=Nbar, primaldual='primal')
+    _, hG1N, _ = proj.scalar(N, mat_conf['Y'], NyqNul=True, tensor=True)
+    hG1N = hG1N.enlarge(Nbar)
+    FN = DFT(name='FN', inverse=False, N=Nbar)
+    FiN = DFT(name='FiN', inverse=True, N=Nbar)
+    G1N = Operator(name='G1', mat=[[FiN, hG1N, FN]])
+    Afun = Operator(name='FiGFA', mat=[[G1N, A]])
+    E = np.zeros(dim)
+    E[0] = 1
+    EN = Tensor(name='EN', N=Nbar, shape=(dim,), Fourier=False)
+    EN.set_mean(E)
+    x0 = Tensor(N=Nbar, shape=(dim,), Fourier=False)
+    B = Afun(-EN)
+    X, info = linear_solver(solver='CG', Afun=Afun, B=B, x0=x0,
+                            par={'tol': 1e-8, 'maxiter': 1e3}, callback=None)
+    AH11 = A(X + EN) * (X + EN)
+    # oracle
+    om = oracle.Material(dict(mat_conf))
+    Ao = om.get_A_Ga(Nbar, 'primal')
+    G, _ = oracle.green_operator('scalar', N, np.ones(dim), 'Ga', 1)
+    Af = lambda v: oracle.apply_GA(G, Ao, v)
+    ENo = np.zeros((dim,) + tuple(Nbar))
+    ENo[0] = 1.
+    Xo, info_o = oracle.cg(Af, Af(-ENo), np.zeros_like(ENo), tol=1e-8, maxiter=1000)
+    u = Xo + ENo
+    ref = oracle.scal(np.einsum('ij...,j...->i...', Ao, u), u)
+    assert abs(AH11 - ref) < 1e-10 * abs(ref)
+    assert info['kit'] == info_o['kit']
