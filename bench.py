@@ -31,6 +31,7 @@ sys.path.insert(0, ROOT)
 WORKLOADS = {
     # name: (N (solve on 2N-1), P image, L loads, radius, vf, contrast, tol)
     'spheres509': dict(N=255, P=255, radius=0.08, vf=0.3, contrast=100., tol=1e-3, seed=2026),
+    'spheres255': dict(N=127, P=127, radius=0.08, vf=0.3, contrast=100., tol=1e-3, seed=2026),
     'spheres125': dict(N=63, P=63, radius=0.08, vf=0.3, contrast=100., tol=1e-3, seed=2026),
 }
 SAMPLE = dict(N=31, P=31, iters=4)    # CPU baseline sample (61^3 grid)
@@ -44,6 +45,9 @@ def parse():
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     ap.add_argument('--workload', default='spheres509', choices=sorted(WORKLOADS))
     ap.add_argument('--precision', default='f32', choices=['f32', 'mixed'])
+    ap.add_argument('--ga-mode', default='band', choices=['band', 'full'],
+                    help='band: CG fields on the N grid, coefficient on a smooth integration '
+                         'grid >= 2N-1; full: CG on the 2N-1 grid (the reference layout)')
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-fp64', action='store_true')
     return ap.parse_args()
@@ -86,13 +90,25 @@ def image_values(w):
                                contrast=w['contrast'], seed=w['seed'])
 
 
-def ga_coefficient(vals, w):
-    """Grid-based Ga coefficient (order 0) on 2N-1, assembled on the GPU."""
+def ga_coefficient(vals, w, grid=None):
+    """Grid-based Ga coefficient (order 0) of the 2N-1 grid, assembled on the
+    GPU, sampled on `grid` (default 2N-1)."""
     from ffthompy_gb300.materials import Material
     N = np.array([w['N']] * 3)
     mat = Material({'fun': lambda coord, _v=vals: _v, 'Y': np.ones(3), 'order': 0,
                     'P': np.array([w['P']] * 3)})
-    return mat.get_A_Ga(Nbar=2 * N - 1, primaldual='primal')
+    return mat.get_A_Ga(Nbar=2 * N - 1, primaldual='primal', grid=grid)
+
+
+def make_plan(w, precision, ga_mode):
+    from ffthompy_gb300.engine import GalerkinPlan, nice_size
+    N = w['N']
+    Ns = 2 * N - 1
+    if ga_mode == 'band':
+        return GalerkinPlan((N,) * 3, np.ones(3), physics='scalar', nloads=3,
+                            integ=(nice_size(Ns),) * 3, precision=precision)
+    return GalerkinPlan((Ns,) * 3, np.ones(3), physics='scalar', nloads=3, band=(N,) * 3,
+                        precision=precision)
 
 
 # ----------------------------------------------------------------------------
@@ -237,18 +253,19 @@ def run_gpu(args):
     __graft_entry__.build()
     from ffthompy_gb300.engine import GalerkinPlan
 
+    from ffthompy_gb300.engine import nice_size
     w = WORKLOADS[args.workload]
     N = w['N']
     Ns = 2 * N - 1
-    M = Ns ** 3
+    M = Ns ** 3                       # voxels of the reference's solve grid (2N-1)^3
     vals = image_values(w)
-    A = ga_coefficient(vals, w)                       # (3,3)+Nbar on the GPU, FP64
+    cgrid = (nice_size(Ns),) * 3 if args.ga_mode == 'band' else (Ns,) * 3
+    A = ga_coefficient(vals, w, grid=cgrid)           # (3,3)+grid on the GPU, FP64
     A_iso = A.data[0, 0].contiguous()
-    extras = {}
+    extras = {'coefficient_grid': list(cgrid)}
 
     # FP64-refined reference A_H (mixed plan, FP64 outer residual, tight tol)
-    ref = GalerkinPlan((Ns,) * 3, np.ones(3), physics='scalar', nloads=3, band=(N,) * 3,
-                       precision='mixed')
+    ref = make_plan(w, 'mixed', args.ga_mode)
     ref.set_coefficient(A.data)
     t0 = time.perf_counter()
     Xr, info_r = ref.cg(ref.rhs_macro(1), tol=w['tol'] * 1e-3, maxiter=2000)
@@ -259,8 +276,7 @@ def run_gpu(args):
     del Xr, ref
     torch.cuda.empty_cache()
 
-    plan = GalerkinPlan((Ns,) * 3, np.ones(3), physics='scalar', nloads=3, band=(N,) * 3,
-                        precision=args.precision)
+    plan = make_plan(w, args.precision, args.ga_mode)
     plan.set_coefficient(A.data)
     tol = w['tol']
 
@@ -331,8 +347,7 @@ def run_gpu(args):
 
     # FP64 GPU CG (plain form) for the mixed-vs-FP64 ratio: bounded iterations
     if not args.no_fp64:
-        p64 = GalerkinPlan((Ns,) * 3, np.ones(3), physics='scalar', nloads=3, band=(N,) * 3,
-                           precision='f64')
+        p64 = make_plan(w, 'f64', args.ga_mode)
         p64.set_coefficient(A.data)
         B64 = p64.rhs_macro(1)
         k64 = 3
@@ -351,11 +366,10 @@ def run_gpu(args):
         torch.cuda.empty_cache()
 
     # end to end through the host-buffer C-ABI entry point
-    host_A = torch.empty(A_iso.shape, dtype=torch.float64, pin_memory=True)
+    host_A = torch.empty(tuple(A_iso.shape), dtype=torch.float64, pin_memory=True)
     host_A.copy_(A_iso)
     A_host = host_A.numpy()
-    e2e_plan = GalerkinPlan((Ns,) * 3, np.ones(3), physics='scalar', nloads=3, band=(N,) * 3,
-                            precision=args.precision)
+    e2e_plan = make_plan(w, args.precision, args.ga_mode)
     from ffthompy_gb300 import _lib
     e2e_plan.homogenize_host(packed=A_host, kind=_lib.FHP_COEF_ISO, proj=1, tol=tol,
                              maxiter=2000)   # warm
@@ -388,8 +402,12 @@ def run_gpu(args):
                                % (args.workload, w['radius'], w['vf'], w['contrast'], w['P'],
                                   Ns, w['tol']),
                    'grid': [Ns] * 3, 'loads': 3, 'precision': args.precision,
-                   'l2': 'inputs larger than L2 (one field vector %.1f GB)'
-                         % (3 * 3 * M * (4 if args.precision == 'f32' else 8) / 1e9)},
+                   'ga_mode': args.ga_mode,
+                   'voxels_counted': 'prod(2N-1) per load and iteration (the reference grid)',
+                   'l2': 'inputs larger than L2 (coefficient %.2f GB, spectra %.1f GB)'
+                         % (np.prod(cgrid) * (4 if args.precision == 'f32' else 8) / 1e9,
+                            3 * 3 * np.prod(cgrid) * (4 if args.precision == 'f32' else 8)
+                            / 1e9)},
         'time_to_AH_s': round(ms / 1e3 / args.steps, 4),
         'cg_iterations': info['kit'],
         'AH': AH.tolist(), 'AH_rel_err_vs_fp64': AH_err,

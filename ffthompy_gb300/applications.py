@@ -9,13 +9,18 @@ postprocess.  Differences from the reference, by design:
   * all d (scalar) or d(d+1)/2 (elasticity) loads are solved together in one
     batched GPU CG (each load keeps its own CG scalars and stopping test);
   * the per-iteration CallBack residual (solver_pp.py:13-24) is taken from the
-    CG recursion instead of an extra operator application.
+    CG recursion instead of an extra operator application;
+  * Ga solves use the band representation by default: the CG fields are
+    stored on the N grid (they are band-limited trigonometric polynomials) and
+    the coefficient on a smooth integration grid >= 2N-1; the operator and
+    the inner products equal the reference's on the 2N-1 grid.
+    solve['ga_mode'] = 'full' runs CG on the 2N-1 grid as the reference does.
 """
 import time
 
 import numpy as np
 
-from .engine import GalerkinPlan
+from .engine import GalerkinPlan, nice_size
 from .general.solver_pp import CallBack
 from .materials import Material
 from .postprocess import Solutions, postprocess
@@ -35,16 +40,23 @@ def _solve(pb, physics):
     maxiter = int(pb.solver.get('maxiter', 1e3))
     if str(pb.solver.get('kind', 'CG')).lower() != 'cg':
         raise NotImplementedError('solver %s' % pb.solver.get('kind'))
+    ga_mode = pb.solve.get('ga_mode', 'band')
     for primaldual in pb.solve['primaldual']:
         t0 = time.time()
         mat = Material(pb.material)
+        proj = 1 if primaldual == 'primal' else 2
         if kind == 'GaNi':
             A = mat.get_A_GaNi(N, primaldual)
-        else:
+            plan = GalerkinPlan(tuple(N), pb.Y, physics=physics, precision=precision)
+        elif ga_mode == 'full':
             A = mat.get_A_Ga(Nbar=Nbar, primaldual=primaldual)
-        proj = 1 if primaldual == 'primal' else 2
-        plan = GalerkinPlan(tuple(Nbar), pb.Y, physics=physics, band=tuple(N),
-                            precision=precision)
+            plan = GalerkinPlan(tuple(Nbar), pb.Y, physics=physics, band=tuple(N),
+                                precision=precision)
+        else:
+            integ = tuple(nice_size(n) for n in Nbar)
+            A = mat.get_A_Ga(Nbar=Nbar, primaldual=primaldual, grid=integ)
+            plan = GalerkinPlan(tuple(N), pb.Y, physics=physics, integ=integ,
+                                precision=precision)
         plan.set_coefficient(A.data)
         plan._coef_tensor = A
         B = plan.rhs_macro(proj)
@@ -58,7 +70,8 @@ def _solve(pb, physics):
                                                'norm_res': info['norm_res'][l],
                                                'status': info['status'][l],
                                                'time': [[t_solve, t_solve, t_solve]]}})
-        postprocess(pb, A, mat, Solutions(plan, X, pb.Y), results, primaldual)
+        out_grid = tuple(N) if kind == 'GaNi' else tuple(Nbar)
+        postprocess(pb, A, mat, Solutions(plan, X, pb.Y, out_grid), results, primaldual)
 
 
 def scalar(problem):

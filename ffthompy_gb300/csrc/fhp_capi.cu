@@ -60,7 +60,7 @@ int cg_mixed(fhp_plan_s& p, int proj, const void* b, const void* x0, double tol,
   if (st == FHP_OK) {
     if (x0) {
       st = cuda_status(cudaMemcpyAsync(x, x0, n * 8, cudaMemcpyDeviceToDevice, s), "copy");
-      if (st == FHP_OK) st = hi.apply(proj, x, ax, s);
+      if (st == FHP_OK) st = hi.apply_ex(proj, x, ax, s, true);
     } else {
       st = cuda_status(cudaMemsetAsync(x, 0, n * 8, s), "memset");
       if (st == FHP_OK) st = cuda_status(cudaMemsetAsync(ax, 0, n * 8, s), "memset");
@@ -90,8 +90,9 @@ int cg_mixed(fhp_plan_s& p, int proj, const void* b, const void* x0, double tol,
     if ((st = lo.scale_from64(static_cast<const double*>(r), sc_in.data(), r32, s)) != FHP_OK) break;
     fhp::SolveResult in;
     if ((st = lo.cg_solve(proj, r32, nullptr, eta, room, d32, in, 1, s)) != FHP_OK) break;
-    if ((st = hi.add_scaled_to64(d32, sc_out.data(), x, s)) != FHP_OK) break;
-    if ((st = hi.apply(proj, x, ax, s)) != FHP_OK) break;
+    // d32 holds FP32 values: the FP32 engine owns the matching kernel instance
+    if ((st = lo.add_scaled_to64(d32, sc_out.data(), x, s)) != FHP_OK) break;
+    if ((st = hi.apply_ex(proj, x, ax, s, true)) != FHP_OK) break;
     if ((st = hi.residual(b, ax, r, sumsq.data(), s)) != FHP_OK) break;
     for (int l = 0; l < L; ++l) {
       if (!active[l]) continue;
@@ -107,6 +108,11 @@ int cg_mixed(fhp_plan_s& p, int proj, const void* b, const void* x0, double tol,
       }
     }
   }
+  // the FP32 corrections carry roundoff outside range(G), invisible to the
+  // G A G residual but first order in the energy: project x in FP64
+  if (st == FHP_OK) st = hi.project(proj, x, ax, s);
+  if (st == FHP_OK)
+    st = cuda_status(cudaMemcpyAsync(x, ax, n * 8, cudaMemcpyDeviceToDevice, s), "copy");
   for (void* q : {ax, r, r32, d32})
     if (q) cudaFreeAsync(q, s);
   if (st == FHP_OK) st = cuda_status(cudaStreamSynchronize(s), "sync");
@@ -159,6 +165,46 @@ int fhp_plan_create(fhp_plan* out, int dim, const int* n, const int* n_band, con
     if (n[i] > 4096) return bad("grid size per axis must be <= 4096");
     cfg.N[i] = n[i];
     cfg.band[i] = n_band[i];
+    cfg.Y[i] = Y[i];
+  }
+  cfg.physics = physics;
+  cfg.nloads = nloads;
+  cfg.scale = g_scale;
+  int st = FHP_OK;
+  std::unique_ptr<fhp::EngineBase> e, lo;
+  if (precision == FHP_F64 || precision == FHP_MIXED) e = fhp::make_engine_f64(cfg, &st);
+  else if (precision == FHP_F32) e = fhp::make_engine_f32(cfg, &st);
+  else return bad("unknown precision");
+  if (!e) return st == FHP_OK ? FHP_CUDA : st;
+  if (precision == FHP_MIXED) {
+    lo = fhp::make_engine_f32(cfg, &st);
+    if (!lo) return st == FHP_OK ? FHP_CUDA : st;
+  }
+  auto* p = new (std::nothrow) fhp_plan_s;
+  if (!p) return FHP_OOM;
+  p->eng = std::move(e);
+  p->lo = std::move(lo);
+  *out = p;
+  return FHP_OK;
+}
+
+int fhp_plan_create_band(fhp_plan* out, int dim, const int* n, const int* n_int,
+                         const double* Y, int physics, int nloads, double g_scale,
+                         int precision) {
+  if (!out) return bad("out is NULL");
+  *out = nullptr;
+  if (dim != 2 && dim != 3) return bad("dim must be 2 or 3");
+  if (!n || !n_int || !Y) return bad("n, n_int and Y are required");
+  if (physics != FHP_SCALAR && physics != FHP_ELASTICITY) return bad("unknown physics");
+  if (!(g_scale > 0) || !std::isfinite(g_scale)) return bad("g_scale must be positive");
+  fhp::PlanConfig cfg;
+  cfg.dim = dim;
+  for (int i = 0; i < dim; ++i) {
+    if (n[i] < 1 || n[i] > 4096 || n_int[i] > 4096) return bad("bad grid sizes");
+    if (n_int[i] < 2 * n[i] - 1) return bad("integration grid must be >= 2n-1");
+    cfg.N[i] = n[i];
+    cfg.band[i] = n[i];
+    cfg.integ[i] = n_int[i];
     cfg.Y[i] = Y[i];
   }
   cfg.physics = physics;
@@ -261,9 +307,9 @@ int fhp_fourier_interp(fhp_plan src, fhp_plan dst, const void* x_src, void* x_ds
   if (!src || !dst || !x_src || !x_dst) return bad("plans and fields are required");
   const fhp::PlanConfig& a = src->eng->config();
   const fhp::PlanConfig& b = dst->eng->config();
-  if (a.dim != b.dim || a.physics != b.physics || a.nloads != b.nloads ||
+  if (a.dim != b.dim || src->eng->dv() * src->eng->loads() != dst->eng->dv() * dst->eng->loads() ||
       src->eng->precision() != dst->eng->precision())
-    return bad("plans differ in dim, physics, loads or precision");
+    return bad("plans differ in dim, field count or precision");
   for (int i = 0; i < a.dim; ++i)
     if (b.N[i] < a.N[i]) return bad("destination grid must not be smaller");
   cudaStream_t s = as_stream(stream);

@@ -45,6 +45,7 @@ struct PlanConfig {
   int ncomp = 1;             // fields of a plain FFT plan
   int nloads = 1;
   double scale = 1.0;        // Ga: prod(2N-1)/prod(N)
+  int integ[3] = {0, 0, 0};  // band mode: integration grid (>= 2N-1); 0 = classic
 };
 
 struct SolveResult {
@@ -90,6 +91,10 @@ class EngineBase {
   virtual int set_coefficient(int kind, const double* values, bool on_device, cudaStream_t s) = 0;
   virtual int coef_kind() const = 0;
   virtual int apply(int proj, const void* x, void* y, cudaStream_t s) = 0;
+  // apply with the input projected first (G A G, band plans; same as apply otherwise)
+  virtual int apply_ex(int proj, const void* x, void* y, cudaStream_t s, bool inproj) = 0;
+  // y = G x, G the orthogonal Green projection (no coefficient)
+  virtual int project(int proj, const void* x, void* y, cudaStream_t s) = 0;
   virtual int rhs_macro(int proj, void* b, cudaStream_t s) = 0;
   virtual int cg_solve(int proj, const void* b, const void* x0, double tol, int maxiter, void* x,
                        SolveResult& res, int log_cap, cudaStream_t s) = 0;
@@ -106,7 +111,7 @@ class EngineBase {
   virtual int ga_gather(const void* spec_src, const PlanConfig& src, const int* d_index,
                         const double* d_weight, void* spec_dst, cudaStream_t s) = 0;
   // refinement helpers: r = b - ax with per-load sum r^2 (host); dst = s_l*src64;
-  // x64 += s_l*d
+  // x64 += s_l*d.  d and dst are fields of THIS engine's precision.
   virtual int residual(const void* b, const void* ax, void* r, double* sumsq,
                        cudaStream_t s) = 0;
   virtual int scale_from64(const double* src, const double* scale, void* dst,

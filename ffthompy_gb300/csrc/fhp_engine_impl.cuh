@@ -119,6 +119,9 @@ class Engine final : public EngineBase {
       return ST_BAD_ARG;
     }
     if (d == 3) T0_ = tile_cols(l0_.dev.nf, 1, (long long)g_.n1 * g_.n2h);
+    if (cfg_.integ[0] > 0) {
+      if ((st = init_band()) != ST_OK) return st;
+    }
     // reduction scratch
     int dev = 0;
     FHP_CHECK(cudaGetDevice(&dev));
@@ -134,6 +137,44 @@ class Engine final : public EngineBase {
     return set_attrs();
   }
 
+  int init_band() {
+    const int d = cfg_.dim;
+    band_ = true;
+    gi_ = g_;
+    gi_.n0 = d == 3 ? cfg_.integ[0] : 1;
+    gi_.n1 = cfg_.integ[d - 2];
+    gi_.n2 = cfg_.integ[d - 1];
+    gi_.n2h = gi_.n2 / 2 + 1;
+    gi_.M = (long long)gi_.n0 * gi_.n1 * gi_.n2;
+    if (gi_.n0 < g_.n0 || gi_.n1 < g_.n1 || gi_.n2 < g_.n2) {
+      set_error("integration grid must not be smaller than the solve grid");
+      return ST_BAD_ARG;
+    }
+    double pb = (double)gi_.M;
+    gp_.scale = cfg_.scale / pb;   // s / prod(B): normalised band coefficients
+    int st;
+    if ((st = make_line(gi_.n2, lb2_)) != ST_OK) return st;
+    if ((st = make_line(gi_.n1, lb1_)) != ST_OK) return st;
+    if (d == 3 && (st = make_line(gi_.n0, lb0_)) != ST_OK) return st;
+    const int C = g_.L * g_.dv;
+    const size_t n2h = (size_t)g_.n2h;
+    const size_t sa = std::max((size_t)C * g_.n0 * g_.n1 * n2h, (size_t)C * gi_.n0 * gi_.n1 * n2h);
+    const size_t sb = std::max((size_t)C * g_.n0 * gi_.n1 * n2h, (size_t)C * gi_.n0 * g_.n1 * n2h);
+    cudaFree(S_);
+    S_ = nullptr;
+    spec_elems_ = sa;
+    FHP_CHECK(cudaMalloc(&S_, sa * sizeof(cplx<R>)));
+    FHP_CHECK(cudaMalloc(&SB_, sb * sizeof(cplx<R>)));
+    const int np = (C + 1) / 2;
+    const size_t srow = (size_t)np * lb2_.dev.nf * sizeof(cplx<R>);
+    brows_ = std::max(1, kTargetElems / (np * lb2_.dev.nf));
+    brows_ = (int)std::min<size_t>(brows_, std::max<size_t>(1, kSmemBudget / srow));
+    bsmem_rows_ = (size_t)brows_ * srow;
+    if (bsmem_rows_ > kSmemMax) { set_error("integration line too long"); return ST_BAD_ARG; }
+    brow_ctas_ = (int)(((long long)gi_.n0 * gi_.n1 + brows_ - 1) / brows_);
+    return ST_OK;
+  }
+
   int precision() const override { return sizeof(R) == 8 ? 0 : 1; }
   long long voxels() const override { return g_.M; }
   int dv() const override { return g_.dv; }
@@ -147,7 +188,7 @@ class Engine final : public EngineBase {
     if (kind < COEF_ISO || kind > COEF_FULL) { set_error("bad coefficient kind"); return ST_BAD_ARG; }
     const int dv = g_.dv;
     const int c = kind == COEF_ISO ? 1 : kind == COEF_SYM ? dv * (dv + 1) / 2 : dv * dv;
-    const size_t n = (size_t)c * g_.M;
+    const size_t n = (size_t)c * (band_ ? gi_.M : g_.M);
     if (A_) { cudaFree(A_); A_ = nullptr; }
     FHP_CHECK(cudaMalloc(&A_, n * sizeof(R)));
     double* tmp = nullptr;
@@ -169,10 +210,32 @@ class Engine final : public EngineBase {
 
   // y = iF G F (A x) for all loads (ffthompy/tensors/operators.py:136-144)
   int apply(int proj, const void* x, void* y, cudaStream_t s) override {
+    return apply_ex(proj, x, y, s, false);
+  }
+
+  // inproj: G A G (band mode), see band_operator
+  int apply_ex(int proj, const void* x, void* y, cudaStream_t s, bool inproj) override {
     if (!A_) { set_error("coefficient not set"); return ST_BAD_ARG; }
     gp_.proj = proj;
     return run_operator(coef_kind_, false, static_cast<const R*>(x), nullptr, nullptr,
-                        static_cast<R*>(y), nullptr, s, false, false);
+                        static_cast<R*>(y), nullptr, s, false, false, inproj);
+  }
+
+  // y = G x (orthogonal projection onto the compatible / equilibrated fields
+  // of the solve grid band)
+  int project(int proj, const void* xv, void* yv, cudaStream_t s) override {
+    const int proj_saved = gp_.proj;
+    const double scale_saved = gp_.scale;
+    gp_.proj = proj;
+    gp_.scale = 1.0;
+    int st = fwd_passes(COEF_NONE, false, static_cast<const R*>(xv), nullptr, nullptr, S_, false,
+                        s);
+    if (st == ST_OK) st = proj_pass(S_, false, s);
+    if (st == ST_OK) st = inv_passes(S_, static_cast<R*>(yv), (R)(1.0 / (double)g_.M), false,
+                                     nullptr, false, s);
+    gp_.proj = proj_saved;
+    gp_.scale = scale_saved;
+    return st;
   }
 
   int rhs_macro(int proj, void* b, cudaStream_t s) override {
@@ -199,7 +262,7 @@ class Engine final : public EngineBase {
     // x = x0 ; R = B - A x0 ; P = R   (solver.py:114-117)
     if (x0) {
       FHP_CHECK(cudaMemcpyAsync(x, x0, n * sizeof(R), cudaMemcpyDeviceToDevice, s));
-      if ((st = apply(proj, x, ap_, s)) != ST_OK) return st;
+      if ((st = apply_ex(proj, x, ap_, s, true)) != ST_OK) return st;
       FHP_CHECK(cudaMemcpyAsync(r_, b, n * sizeof(R), cudaMemcpyDeviceToDevice, s));
       k_axpby<R><<<grid_for(n), kThreads, 0, s>>>((long long)n, -1.0, ap_, 1.0, r_);
       FHP_LAUNCHED();
@@ -215,6 +278,7 @@ class Engine final : public EngineBase {
       std::memset(&h, 0, sizeof(LoadState));
       h.tol = tol;
       h.maxiter = maxiter;
+      h.guard = sizeof(R) == 4 ? 32.0 : 0.0;
     }
     FHP_CHECK(cudaMemcpyAsync(st_, h_st_, g_.L * sizeof(LoadState), cudaMemcpyHostToDevice, s));
     FHP_CHECK(cudaMemsetAsync(all_done_, 0, sizeof(int), s));
@@ -273,6 +337,7 @@ class Engine final : public EngineBase {
     if (!A_) { set_error("coefficient not set"); return ST_BAD_ARG; }
     const R* X = static_cast<const R*>(Xv);
     const int L = g_.L;
+    if (band_) return band_energy(X, add_macro, AH, s);
     switch (coef_kind_) {
       case COEF_ISO: k_energy<R, COEF_ISO><<<red_ctas_, 128, 0, s>>>(X, A_, partials_, g_, add_macro); break;
       case COEF_SYM: k_energy<R, COEF_SYM><<<red_ctas_, 128, 0, s>>>(X, A_, partials_, g_, add_macro); break;
@@ -397,7 +462,7 @@ class Engine final : public EngineBase {
     const int dv = g_.dv;
     const int c = coef_kind_ == COEF_ISO ? 1 : coef_kind_ == COEF_SYM ? dv * (dv + 1) / 2
                 : coef_kind_ == COEF_FULL ? dv * dv : 0;
-    return (double)c * g_.M * sizeof(R);
+    return (double)c * (band_ ? gi_.M : g_.M) * sizeof(R);
   }
   int pbeg(const char* name, double bytes, cudaStream_t s) {
     if (!prof.on) return -1;
@@ -471,6 +536,15 @@ class Engine final : public EngineBase {
     FHP_ATTR((k_proj_first<R>));
     FHP_ATTR((k_c2r_last<R, false>));
     FHP_ATTR((k_c2r_last<R, true>));
+    FHP_ATTR((k_r2c_last<R, COEF_NONE, true>));
+    FHP_ATTR((k_band_axis<R, BAND_UP>));
+    FHP_ATTR((k_band_axis<R, BAND_DOWN>));
+    FHP_ATTR((k_band_axis<R, BAND_DOWN_PROJ>));
+    FHP_ATTR((k_band_axis<R, BAND_UP_PROJ>));
+    FHP_ATTR((k_band_axis<R, BAND_PAD>));
+    FHP_ATTR((k_band_last<R, COEF_ISO>));
+    FHP_ATTR((k_band_last<R, COEF_SYM>));
+    FHP_ATTR((k_band_last<R, COEF_FULL>));
 #undef FHP_ATTR
     return ST_OK;
   }
@@ -484,8 +558,9 @@ class Engine final : public EngineBase {
   }
 
   void release() {
-    for (DevLine<R>* l : {&l0_, &l1_, &l2_})
+    for (DevLine<R>* l : {&l0_, &l1_, &l2_, &lb0_, &lb1_, &lb2_})
       if (l->mem) { cudaFree(l->mem); l->mem = nullptr; }
+    if (SB_) { cudaFree(SB_); SB_ = nullptr; }
     if (S_) cudaFree(S_);
     if (A_) cudaFree(A_);
     if (r_) cudaFree(r_);
@@ -581,8 +656,186 @@ class Engine final : public EngineBase {
     return ST_OK;
   }
 
+  // ---- band representation (Ga on the solve grid, A on the integration grid) ----
+  int band_axis(int mode, const cplx<R>* in, cplx<R>* out, const BandAxis& ax,
+                const LineDev<R>& L1, const LineDev<R>& L2, bool cg, cudaStream_t s,
+                const char* name) {
+    const bool projm = mode == BAND_DOWN_PROJ || mode == BAND_UP_PROJ;
+    const int nlc = projm ? g_.dv : 1;
+    const int nf = (mode == BAND_PAD ? 0 : L1.nf) + (mode == BAND_DOWN ? 0 : L2.nf);
+    const int T = tile_cols(nf, nlc, ax.inner);
+    const size_t smem = (size_t)nlc * T * nf * sizeof(cplx<R>);
+    if (smem > kSmemMax) { set_error("band line too long for shared memory"); return ST_BAD_ARG; }
+    const int outer = projm ? g_.L : g_.L * g_.dv;
+    dim3 grid((unsigned)((ax.inner + T - 1) / T), (unsigned)(outer * ax.mid));
+    const int* ad = cg ? all_done_ : nullptr;
+    const LoadState* st = cg ? st_ : nullptr;
+    const double bytes = (double)(g_.L * g_.dv) * ax.mid * ax.inner *
+                         (ax.n_in + ax.n_out) * sizeof(cplx<R>);
+    const int pk = pbeg(name, bytes, s);
+    switch (mode) {
+      case BAND_UP:
+        k_band_axis<R, BAND_UP><<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st);
+        break;
+      case BAND_DOWN:
+        k_band_axis<R, BAND_DOWN><<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st);
+        break;
+      case BAND_UP_PROJ:
+        k_band_axis<R, BAND_UP_PROJ><<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st);
+        break;
+      case BAND_PAD:
+        k_band_axis<R, BAND_PAD><<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st);
+        break;
+      default:
+        k_band_axis<R, BAND_DOWN_PROJ><<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st);
+        break;
+    }
+    pend(pk, s);
+    FHP_LAUNCHED();
+    return ST_OK;
+  }
+
+  // inproj: apply G to the input first (G A G): identical on range(G), where
+  // the CG iterates live, and annihilates roundoff outside it
+  int band_operator(int coef, bool pupd, const R* x, R* pio, const R* rvec, R* y,
+                    const R* pdot, cudaStream_t s, bool cg, bool dot, bool inproj = false) {
+    int st;
+    const int d = g_.dim;
+    const int* ad = cg ? all_done_ : nullptr;
+    cplx<R>* SA = S_;
+    cplx<R>* SB = SB_;
+    const long long n2h = g_.n2h;
+    // K1: r2c on the solve grid (P update fused)
+    {
+      const dim3 grid1(row_ctas_);
+      const double b1 = (pupd ? 3.0 : 1.0) * field_bytes() + spec_bytes_n();
+      const int pk = pbeg(pupd ? "band_r2c_pupd" : "band_r2c", b1, s);
+      if (pupd)
+        k_r2c_last<R, COEF_NONE, true><<<grid1, kThreads, smem_rows_, s>>>(
+            x, pio, rvec, nullptr, SA, g_, l2_.dev, rows_, st_, ad);
+      else
+        k_r2c_last<R, COEF_NONE, false><<<grid1, kThreads, smem_rows_, s>>>(
+            x, pio, rvec, nullptr, SA, g_, l2_.dev, rows_, st_, ad);
+      pend(pk, s);
+      FHP_LAUNCHED();
+    }
+    cplx<R>* Sbig;
+    if (d == 3 && !inproj) {
+      BandAxis a1{g_.n1, gi_.n1, g_.n1, gi_.n1, gp_.h[1], n2h, g_.n0, g_.n0, 1, 0, 0};
+      if ((st = band_axis(BAND_UP, SA, SB, a1, l1_.dev, lb1_.dev, cg, s, "band_up_axis1")) != ST_OK) return st;
+      BandAxis a0{g_.n0, gi_.n0, g_.n0, gi_.n0, gp_.h[0], (long long)gi_.n1 * n2h, 1, 1, 2, 0, 0};
+      if ((st = band_axis(BAND_UP, SB, SA, a0, l0_.dev, lb0_.dev, cg, s, "band_up_axis0")) != ST_OK) return st;
+      Sbig = SA;
+    } else if (d == 3) {
+      // forward DFT_N along axis 1, then axis 0: DFT_N, G, pad, iDFT_B; then pad axis 1
+      dim3 grid((unsigned)((n2h + T1_ - 1) / T1_), (unsigned)(g_.L * g_.dv * g_.n0));
+      const int pk = pbeg("band_c2c_axis1_fwd", 2.0 * spec_bytes_n(), s);
+      k_c2c_axis<R, false><<<grid, kThreads, (size_t)T1_ * l1_.dev.nf * sizeof(cplx<R>), s>>>(
+          SA, g_.n1, n2h, l1_.dev, T1_, ad, cg ? st_ : nullptr, g_.dv * g_.n0);
+      pend(pk, s);
+      FHP_LAUNCHED();
+      BandAxis a0{g_.n0, gi_.n0, g_.n0, gi_.n0, gp_.h[0], (long long)g_.n1 * n2h, 1, 1, 2,
+                  (int)n2h, g_.n1};
+      if ((st = band_axis(BAND_UP_PROJ, SA, SB, a0, l0_.dev, lb0_.dev, cg, s, "band_upproj_axis0")) != ST_OK) return st;
+      BandAxis a1{g_.n1, gi_.n1, g_.n1, gi_.n1, gp_.h[1], n2h, gi_.n0, g_.n0, 1, 0, 0};
+      if ((st = band_axis(BAND_PAD, SB, SA, a1, lb1_.dev, lb1_.dev, cg, s, "band_pad_axis1")) != ST_OK) return st;
+      Sbig = SA;
+    } else {
+      BandAxis a1{g_.n1, gi_.n1, g_.n1, gi_.n1, gp_.h[0], n2h, 1, 1, 0, 0, 0};
+      if ((st = band_axis(inproj ? BAND_UP_PROJ : BAND_UP, SA, SB, a1, l1_.dev, lb1_.dev, cg, s,
+                          inproj ? "band_upproj_axis0" : "band_up_axis0")) != ST_OK) return st;
+      Sbig = SB;
+    }
+    // K4: last axis on the integration grid with the coefficient
+    {
+      const long long nrows = (long long)gi_.n0 * gi_.n1;
+      const R cs = (R)(1.0 / (double)g_.M);
+      const double b4 = 2.0 * (double)(g_.L * g_.dv) * nrows * n2h * sizeof(cplx<R>) + coef_bytes();
+      const int pk = pbeg("band_last_coef", b4, s);
+#define FHP_BL(C) k_band_last<R, C><<<brow_ctas_, kThreads, bsmem_rows_, s>>>(Sbig, A_, g_, nrows, (int)n2h, g_.n2, lb2_.dev, brows_, cs, ad)
+      switch (coef) {
+        case COEF_ISO: FHP_BL(COEF_ISO); break;
+        case COEF_SYM: FHP_BL(COEF_SYM); break;
+        default: FHP_BL(COEF_FULL); break;
+      }
+#undef FHP_BL
+      pend(pk, s);
+      FHP_LAUNCHED();
+    }
+    if (d == 3) {
+      BandAxis a0{gi_.n0, g_.n0, g_.n0, gi_.n0, gp_.h[0], (long long)gi_.n1 * n2h, 1, 1, 2, 0, 0};
+      if ((st = band_axis(BAND_DOWN, SA, SB, a0, lb0_.dev, l0_.dev, cg, s, "band_down_axis0")) != ST_OK) return st;
+      BandAxis a1{gi_.n1, g_.n1, g_.n1, gi_.n1, gp_.h[1], n2h, g_.n0, g_.n0, 1, 0, 0};
+      if ((st = band_axis(BAND_DOWN_PROJ, SB, SA, a1, lb1_.dev, l1_.dev, cg, s, "band_proj_axis1")) != ST_OK) return st;
+      // K7: inverse DFT_N along axis 0
+      dim3 grid((unsigned)((g_.n1 * n2h + T0_ - 1) / T0_), (unsigned)(g_.L * g_.dv));
+      const int pk = pbeg("band_c2c_axis0_inv", 2.0 * spec_bytes_n(), s);
+      k_c2c_axis<R, true><<<grid, kThreads, (size_t)T0_ * l0_.dev.nf * sizeof(cplx<R>), s>>>(
+          SA, g_.n0, (long long)g_.n1 * n2h, l0_.dev, T0_, ad, cg ? st_ : nullptr, g_.dv);
+      pend(pk, s);
+      FHP_LAUNCHED();
+    } else {
+      BandAxis a1{gi_.n1, g_.n1, g_.n1, gi_.n1, gp_.h[0], n2h, 1, 1, 0, 0, 0};
+      if ((st = band_axis(BAND_DOWN_PROJ, SB, SA, a1, lb1_.dev, l1_.dev, cg, s, "band_proj_axis0")) != ST_OK) return st;
+    }
+    // K8: c2r on the solve grid (+ <P, AP>)
+    const dim3 grid1(row_ctas_);
+    const int pk2 = pbeg(dot ? "band_c2r_dot" : "band_c2r",
+                         spec_bytes_n() + (dot ? 2.0 : 1.0) * field_bytes(), s);
+    if (dot)
+      k_c2r_last<R, true><<<grid1, kThreads, smem_rows_, s>>>(SA, y, pdot, partials_, g_, l2_.dev,
+                                                              rows_, (R)1, ad);
+    else
+      k_c2r_last<R, false><<<grid1, kThreads, smem_rows_, s>>>(SA, y, nullptr, nullptr, g_,
+                                                               l2_.dev, rows_, (R)1, ad);
+    pend(pk2, s);
+    FHP_LAUNCHED();
+    return ST_OK;
+  }
+
+  double spec_bytes_n() const {
+    return (double)g_.L * g_.dv * g_.n0 * g_.n1 * g_.n2h * 2 * sizeof(R);
+  }
+
+  // A_H via Parseval on the solve grid: W = band(A (X+E)) / prod(B), then
+  // A_H[i][j] = <W_i, X_j + E_j>  (exact: X + E is band limited)
+  int band_energy(const R* X, int add_macro, double* AH, cudaStream_t s) {
+    const size_t n = (size_t)g_.L * g_.dv * g_.M;
+    R* U = nullptr;
+    R* W = nullptr;
+    FHP_CHECK(cudaMallocAsync(&U, n * sizeof(R), s));
+    FHP_CHECK(cudaMallocAsync(&W, n * sizeof(R), s));
+    if (add_macro) {
+      k_add_macro<R><<<grid_for(n), kThreads, 0, s>>>(X, U, g_);
+      FHP_LAUNCHED();
+    } else {
+      FHP_CHECK(cudaMemcpyAsync(U, X, n * sizeof(R), cudaMemcpyDeviceToDevice, s));
+    }
+    const int proj_saved = gp_.proj;
+    const double scale_saved = gp_.scale;
+    gp_.proj = 0;
+    gp_.scale = 1.0 / (double)gi_.M;
+    int st = band_operator(coef_kind_, false, U, nullptr, nullptr, W, nullptr, s, false, false);
+    gp_.proj = proj_saved;
+    gp_.scale = scale_saved;
+    if (st == ST_OK) {
+      k_cross_dot<R><<<red_ctas_, 128, 0, s>>>(W, X, partials_, g_, add_macro);
+      FHP_LAUNCHED();
+      k_sum_partials<<<1, kThreads, 0, s>>>(partials_, red_ctas_, g_.L * g_.L,
+                                            1.0 / (double)g_.M, ad_);
+      FHP_LAUNCHED();
+      FHP_CHECK(cudaMemcpyAsync(AH, ad_, (size_t)g_.L * g_.L * sizeof(double),
+                                cudaMemcpyDeviceToHost, s));
+      FHP_CHECK(cudaStreamSynchronize(s));
+    }
+    cudaFreeAsync(U, s);
+    cudaFreeAsync(W, s);
+    return st;
+  }
+
   int run_operator(int coef, bool pupd, const R* x, R* pio, const R* rvec, R* y, const R* pdot,
-                   cudaStream_t s, bool cg, bool dot) {
+                   cudaStream_t s, bool cg, bool dot, bool inproj = false) {
+    if (band_) return band_operator(coef, pupd, x, pio, rvec, y, pdot, s, cg, dot, inproj);
     int st;
     if ((st = fwd_passes(coef, pupd, x, pio, rvec, S_, cg, s)) != ST_OK) return st;
     if ((st = proj_pass(S_, cg, s)) != ST_OK) return st;
@@ -591,7 +844,7 @@ class Engine final : public EngineBase {
 
   // one CG iteration on all loads (solver.py:124-134), P update fused into pass 1
   int cg_iteration(double* dlog, int log_rows, cudaStream_t s) {
-    int st = run_operator(coef_kind_, true, nullptr, p_, r_, ap_, p_, s, true, true);
+    int st = run_operator(coef_kind_, true, nullptr, p_, r_, ap_, p_, s, true, true, true);
     if (st != ST_OK) return st;
     k_fin_pap<<<g_.L, kThreads, 0, s>>>(partials_, row_ctas_, st_, g_.L, 1.0 / (double)g_.M,
                                         all_done_);
@@ -610,6 +863,13 @@ class Engine final : public EngineBase {
   }
 
   R* x_cur_ = nullptr;  // the caller's solution buffer during cg_solve
+  // band representation
+  bool band_ = false;
+  GridDims gi_{};
+  DevLine<R> lb0_, lb1_, lb2_;
+  cplx<R>* SB_ = nullptr;
+  int brows_ = 1, brow_ctas_ = 1;
+  size_t bsmem_rows_ = 0;
 };
 
 }  // namespace fhp

@@ -25,7 +25,9 @@ struct LoadState {
   int kit;
   int maxiter;
   int done;
-  int status;       // 0 ok, 2 breakdown (p.Ap <= 0), 3 non-finite
+  int status;       // 0 ok, 1 stagnated (FP32), 2 breakdown (p.Ap <= 0), 3 non-finite
+  double min_norm;  // smallest residual norm so far
+  double guard;     // stop when norm_res > guard * min_norm (0: off)
 };
 
 struct GridDims {
@@ -40,7 +42,7 @@ struct GridDims {
 // Green projection parameters (ffthompy/projections.py:9-267)
 struct GreenParams {
   int physics;    // 0 scalar, 1 elasticity (Mandel)
-  int proj;       // 1: G1 (compatible, primal), 2: G2 (equilibrated, dual)
+  int proj;       // 1: G1 (compatible, primal), 2: G2 (equilibrated, dual), 0: band only
   int h[3];       // band half-widths |k_i| <= h_i, real axis order
   double Y[3];    // cell size, real axis order
   double scale;   // Ga scale prod(2N-1)/prod(N); 1 for GaNi
@@ -78,11 +80,15 @@ __device__ __forceinline__ void green_apply(const GreenParams& gp, int dim, cons
     xi[i] = R(ki) / R(gp.Y[i]);
   }
   const int dv = gp.physics == 0 ? dim : dim * (dim + 1) / 2;
+  const R s = R(gp.scale);
+  if (gp.proj == 0) {  // no projection (energies): scale only
+    for (int c = 0; c < dv; ++c) x[c] = cscale<R>(x[c], s);
+    return;
+  }
   if (!inband || zero) {
     for (int c = 0; c < dv; ++c) x[c] = mkc<R>(R(0), R(0));
     return;
   }
-  const R s = R(gp.scale);
   R nn = R(0);
   for (int i = 0; i < dim; ++i) nn += xi[i] * xi[i];
   if (gp.physics == 0) {
@@ -552,6 +558,13 @@ static __global__ void k_fin_rr(const double* __restrict__ partials, int nparts,
       if (res_log && S.kit < log_cap) res_log[(long long)S.kit * L + l] = S.norm_res;
       if (!isfinite(rrn)) { S.status = 3; S.done = 1; }
       if (!(S.norm_res > S.tol && S.kit < S.maxiter)) S.done = 1;
+      if (S.norm_res < S.min_norm) S.min_norm = S.norm_res;
+      // FP32 fields: past the precision floor the recursion can diverge; stop
+      // while the iterate is still at the floor's accuracy
+      if (S.guard > 0. && S.kit >= 10 && S.norm_res > S.guard * S.min_norm) {
+        S.status = 1;
+        S.done = 1;
+      }
     }
   }
 }
@@ -573,6 +586,7 @@ static __global__ void k_fin_init(const double* __restrict__ partials, int npart
   LoadState& S = st[l];
   S.rr = s * invM;
   S.norm_res = sqrt(S.rr);
+  S.min_norm = S.norm_res;
   S.kit = 0;
   S.beta = 0.;
   S.alpha = 0.;
@@ -729,6 +743,347 @@ __global__ void k_ga_gather(const cplx<R>* __restrict__ Sp, cplx<R>* __restrict_
     if (conj) v.y = -v.y;
     const double ww = w0[t0] * w1[t1] * w2[t2];
     St[i] = mkc<R>((R)(ww * (double)v.x), (R)(ww * (double)v.y));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Band representation of the Ga operator (CG fields on the solve grid N, the
+// coefficient applied on an integration grid B >= 2N-1).  Along one axis:
+//   BAND_UP        : space N  -> DFT_N -> band |k| <= h -> iDFT_B -> space B
+//   BAND_DOWN      : space B  -> DFT_B -> band -> frequency (N layout)
+//   BAND_DOWN_PROJ : space B  -> DFT_B -> band -> G(xi) over the dv comps ->
+//                    iDFT_N -> space N
+// Arrays are [comp][mid][axis][inner]; CTA = T inner columns of one (comp, mid)
+// (of one (load, mid) with all dv comps for BAND_DOWN_PROJ).
+// ---------------------------------------------------------------------------
+//   BAND_UP_PROJ   : space N  -> DFT_N -> G(xi) -> iDFT_B (band pad) -> space B
+//   BAND_PAD       : frequency (N layout) -> band pad -> iDFT_B -> space B
+enum BandMode { BAND_UP = 0, BAND_DOWN = 1, BAND_DOWN_PROJ = 2, BAND_UP_PROJ = 3, BAND_PAD = 4 };
+
+struct BandAxis {
+  int n_in, n_out;     // line lengths in / out
+  int nN, nB;          // solve / integration length of this axis
+  int h;               // band half width
+  long long inner;     // contiguous elements after the axis
+  int mid;             // extent of the axis before this one (1 if none)
+  int mid_n;           // N extent of the mid axis (its frequency layout), PROJ only
+  int pmode;           // frequency decoding for G: 0 2D (line, inner); 1 3D (mid, line,
+                       // inner); 2 3D (line, inner = k1 * inner2 + k2)
+  int inner2;          // pmode 2: extent of the last axis (half spectrum)
+  int n1f;             // pmode 2: N extent of axis 1 (frequency layout)
+};
+
+__device__ __forceinline__ void band_freqs(const BandAxis& ax, int dim, int q, int m,
+                                           long long col, int* kv) {
+  if (dim == 2) { kv[0] = q; kv[1] = (int)col; return; }
+  if (ax.pmode == 1) { kv[0] = signed_freq(m, ax.mid_n); kv[1] = q; kv[2] = (int)col; return; }
+  const int k1 = (int)(col / ax.inner2);
+  kv[0] = q;
+  kv[1] = signed_freq(k1, ax.n1f);
+  kv[2] = (int)(col - (long long)k1 * ax.inner2);
+}
+
+// N-layout coefficient k (grid n) from the forward B-line (length nb)
+template <typename R>
+__device__ __forceinline__ cplx<R> band_down_value(const cplx<R>* line, const LineDev<R>& L, int k,
+                                                   int n, int nb) {
+  const int q = signed_freq(k, n);
+  if (2 * q == n) {  // Nyquist of an even N grid
+    const cplx<R> a = get_fwd<R>(line, L, q);
+    const cplx<R> b = get_fwd<R>(line, L, nb - q);
+    return mkc<R>(R(0.5) * (a.x + b.x), R(0.5) * (a.y + b.y));
+  }
+  return get_fwd<R>(line, L, q < 0 ? q + nb : q);
+}
+
+template <typename R, int MODE>
+__global__ void __launch_bounds__(256) k_band_axis(const cplx<R>* __restrict__ Sin,
+                                                   cplx<R>* __restrict__ Sout, GridDims g,
+                                                   BandAxis ax, LineDev<R> L1, LineDev<R> L2,
+                                                   int T, GreenParams gp,
+                                                   const int* __restrict__ all_done,
+                                                   const LoadState* __restrict__ st) {
+  if (all_done && *all_done) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr bool PROJ = (MODE == BAND_DOWN_PROJ || MODE == BAND_UP_PROJ);
+  const int nlc = PROJ ? g.dv : 1;   // comps per CTA
+  // blockIdx.y: (comp or load) * mid + m
+  const int m = blockIdx.y % ax.mid;
+  const int cl = blockIdx.y / ax.mid;
+  const int c0 = PROJ ? cl * g.dv : cl;
+  const int load = c0 / g.dv;
+  if (st && st[load].done) return;
+  const int ld1 = (MODE == BAND_PAD) ? 0 : L1.nf;
+  const int ld2 = (MODE == BAND_DOWN) ? 0 : L2.nf;
+  cplx<R>* buf1 = reinterpret_cast<cplx<R>*>(smem_raw);
+  cplx<R>* buf2 = buf1 + (size_t)nlc * T * ld1;
+  const long long t0 = (long long)blockIdx.x * T;
+  const int nl = nlc * T;
+  if constexpr (MODE == BAND_PAD) {
+    // input already in frequency (N layout): pad straight into the B line
+    for (int e = threadIdx.x; e < nl * ax.n_out; e += blockDim.x) {
+      const int t = e % T;
+      const int rest = e / T;
+      const int k = rest % ax.n_out;
+      const int c = rest / ax.n_out;
+      const long long col = t0 + t;
+      const int q = signed_freq(k, ax.n_out);
+      const int aq = q < 0 ? -q : q;
+      cplx<R> v = mkc<R>(R(0), R(0));
+      if (col < ax.inner && 2 * aq <= ax.n_in) {
+        const cplx<R>* src = Sin + (((long long)(c0 + c) * ax.mid + m) * ax.n_in) * ax.inner;
+        const int kin = 2 * aq == ax.n_in ? aq : (q < 0 ? q + ax.n_in : q);
+        v = src[(long long)kin * ax.inner + col];
+        if (2 * aq == ax.n_in) v = cscale<R>(v, R(0.5));
+      }
+      put_inv<R>(buf2 + (c * T + t) * ld2, L2, k, v);
+    }
+  } else {
+    // load: [comp][mid][n_in][inner]
+    for (int e = threadIdx.x; e < nl * ax.n_in; e += blockDim.x) {
+      const int t = e % T;
+      const int rest = e / T;
+      const int i = rest % ax.n_in;
+      const int c = rest / ax.n_in;
+      const long long col = t0 + t;
+      const cplx<R>* src = Sin + (((long long)(c0 + c) * ax.mid + m) * ax.n_in) * ax.inner;
+      const cplx<R> v = col < ax.inner ? src[(long long)i * ax.inner + col] : mkc<R>(R(0), R(0));
+      put_fwd<R>(buf1 + (c * T + t) * ld1, L1, i, v);
+    }
+    zero_tail<R>(buf1, ld1, nl, L1);
+    __syncthreads();
+    line_core<R>(buf1, ld1, nl, L1, false);
+  }
+  // Up: the B-grid coefficient at q is the N-grid one for 2|q| < N, half of the
+  // Nyquist one for 2|q| = N (the symmetric split of Tensor.enlarge,
+  // ffthompy/tensors/objects.py:441-453), else 0.  Down (the adjoint): the
+  // N-grid coefficient at k is the B-grid one for 2|k| < N and the mean of the
+  // B-grid coefficients at +-N/2 for the Nyquist index.
+  if constexpr (MODE == BAND_UP_PROJ) {
+    // G over the dv comps of each N frequency, then the padded B line
+    for (int e = threadIdx.x; e < T * ax.n_in; e += blockDim.x) {
+      const int t = e % T, k = e / T;
+      const long long col = t0 + t;
+      const int q = signed_freq(k, ax.n_in);
+      cplx<R> x[kMaxDv];
+      for (int c = 0; c < g.dv; ++c) x[c] = get_fwd<R>(buf1 + (c * T + t) * ld1, L1, k);
+      if (col < ax.inner) {
+        int kv[3];
+        band_freqs(ax, g.dim, q, m, col, kv);
+        green_apply<R>(gp, g.dim, kv, x);
+      }
+      for (int c = 0; c < g.dv; ++c) {
+        // the projected spectrum is band limited (Nyquist zeroed): place it
+        cplx<R>* l2 = buf2 + (c * T + t) * ld2;
+        if (2 * (q < 0 ? -q : q) < ax.n_in) put_inv<R>(l2, L2, q < 0 ? q + ax.n_out : q, x[c]);
+      }
+    }
+    // the remaining B frequencies are zero
+    for (int e = threadIdx.x; e < nl * ax.n_out; e += blockDim.x) {
+      const int line = e / ax.n_out, k = e - line * ax.n_out;
+      const int q = signed_freq(k, ax.n_out);
+      if (2 * (q < 0 ? -q : q) >= ax.n_in) put_inv<R>(buf2 + line * ld2, L2, k, mkc<R>(R(0), R(0)));
+    }
+  }
+  if constexpr (MODE == BAND_UP || MODE == BAND_UP_PROJ || MODE == BAND_PAD) {
+    if constexpr (MODE == BAND_UP) {
+    for (int e = threadIdx.x; e < nl * ax.n_out; e += blockDim.x) {
+      const int line = e / ax.n_out, k = e - line * ax.n_out;
+      const int q = signed_freq(k, ax.n_out);
+      const int aq = q < 0 ? -q : q;
+      cplx<R> v = mkc<R>(R(0), R(0));
+      if (2 * aq < ax.n_in) {
+        v = get_fwd<R>(buf1 + line * ld1, L1, q < 0 ? q + ax.n_in : q);
+      } else if (2 * aq == ax.n_in) {
+        v = cscale<R>(get_fwd<R>(buf1 + line * ld1, L1, aq), R(0.5));
+      }
+      put_inv<R>(buf2 + line * ld2, L2, k, v);
+    }
+    }
+    __syncthreads();
+    zero_tail<R>(buf2, ld2, nl, L2);
+    __syncthreads();
+    line_core<R>(buf2, ld2, nl, L2, true);
+    for (int e = threadIdx.x; e < nl * ax.n_out; e += blockDim.x) {
+      const int t = e % T;
+      const int rest = e / T;
+      const int i = rest % ax.n_out;
+      const int c = rest / ax.n_out;
+      const long long col = t0 + t;
+      if (col >= ax.inner) continue;
+      cplx<R>* dst = Sout + (((long long)(c0 + c) * ax.mid + m) * ax.n_out) * ax.inner;
+      dst[(long long)i * ax.inner + col] = get_inv<R>(buf2 + (c * T + t) * ld2, L2, i);
+    }
+  } else if constexpr (MODE == BAND_DOWN) {
+    for (int e = threadIdx.x; e < nl * ax.n_out; e += blockDim.x) {
+      const int t = e % T;
+      const int rest = e / T;
+      const int k = rest % ax.n_out;
+      const int c = rest / ax.n_out;
+      const long long col = t0 + t;
+      if (col >= ax.inner) continue;
+      const cplx<R> v = band_down_value<R>(buf1 + (c * T + t) * ld1, L1, k, ax.n_out, ax.n_in);
+      cplx<R>* dst = Sout + (((long long)(c0 + c) * ax.mid + m) * ax.n_out) * ax.inner;
+      dst[(long long)k * ax.inner + col] = v;
+    }
+  } else {
+    // G(xi) on the band, then inverse DFT_N along the line
+    for (int e = threadIdx.x; e < T * ax.n_out; e += blockDim.x) {
+      const int t = e % T, k = e / T;
+      const long long col = t0 + t;
+      const int q = signed_freq(k, ax.n_out);
+      cplx<R> x[kMaxDv];
+      for (int c = 0; c < g.dv; ++c)
+        x[c] = band_down_value<R>(buf1 + (c * T + t) * ld1, L1, k, ax.n_out, ax.n_in);
+      if (col < ax.inner) {
+        int kv[3];
+        band_freqs(ax, g.dim, q, m, col, kv);
+        green_apply<R>(gp, g.dim, kv, x);
+      }
+      for (int c = 0; c < g.dv; ++c) put_inv<R>(buf2 + (c * T + t) * ld2, L2, k, x[c]);
+    }
+    zero_tail<R>(buf2, ld2, nl, L2);
+    __syncthreads();
+    line_core<R>(buf2, ld2, nl, L2, true);
+    for (int e = threadIdx.x; e < nl * ax.n_out; e += blockDim.x) {
+      const int t = e % T;
+      const int rest = e / T;
+      const int i = rest % ax.n_out;
+      const int c = rest / ax.n_out;
+      const long long col = t0 + t;
+      if (col >= ax.inner) continue;
+      cplx<R>* dst = Sout + (((long long)(c0 + c) * ax.mid + m) * ax.n_out) * ax.inner;
+      dst[(long long)i * ax.inner + col] = get_inv<R>(buf2 + (c * T + t) * ld2, L2, i);
+    }
+  }
+}
+
+// Last axis on the integration grid, in place on band half spectra
+// S[comp][row][N2h] (row over the B grid's leading axes): c2r to the B2 points,
+// q = A x * cscale per voxel, r2c back and keep the band k2 <= h2.
+template <typename R, int COEF>
+__global__ void __launch_bounds__(256) k_band_last(cplx<R>* __restrict__ S,
+                                                   const R* __restrict__ A, GridDims g,
+                                                   long long nrows, int n2h_band, int n2_solve,
+                                                   LineDev<R> L, int rows, R coef_scale,
+                                                   const int* __restrict__ all_done) {
+  if (all_done && *all_done) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx<R>* buf = reinterpret_cast<cplx<R>*>(smem_raw);
+  const int C = g.L * g.dv;
+  const int np = (C + 1) / 2;
+  const int ld = L.nf;
+  const int n = L.n;                       // B2
+  const long long Mi = nrows * n;          // voxels of the integration grid
+  const long long row0 = (long long)blockIdx.x * rows;
+  // 1) Hermitian pair lines Z = A + iB over all B2 frequencies
+  for (int e = threadIdx.x; e < rows * np * n; e += blockDim.x) {
+    const int line = e / n, k = e - line * n;
+    const int rl = line / np, p = line - rl * np;
+    const long long row = row0 + rl;
+    const int q = signed_freq(k, n);
+    const int aq = q < 0 ? -q : q;
+    cplx<R> z = mkc<R>(R(0), R(0));
+    const R w = (2 * aq < n2_solve) ? R(1) : (2 * aq == n2_solve ? R(0.5) : R(0));
+    if (row < nrows && w != R(0)) {
+      const int ca = 2 * p, cb = 2 * p + 1;
+      cplx<R> a = cscale<R>(S[((long long)ca * nrows + row) * n2h_band + aq], w);
+      cplx<R> b = cb < C ? cscale<R>(S[((long long)cb * nrows + row) * n2h_band + aq], w)
+                         : mkc<R>(R(0), R(0));
+      if (aq == 0 || 2 * aq == n2_solve) { a.y = R(0); b.y = R(0); }
+      if (q < 0) { a.y = -a.y; b.y = -b.y; }     // X_{-k} = conj(X_k)
+      z = mkc<R>(a.x - b.y, a.y + b.x);
+    }
+    put_inv<R>(buf + (long long)line * ld, L, k, z);
+  }
+  zero_tail<R>(buf, ld, rows * np, L);
+  __syncthreads();
+  line_core<R>(buf, ld, rows * np, L, true);
+  // 2) coefficient per voxel (all loads), in place
+  for (int e = threadIdx.x; e < rows * n; e += blockDim.x) {
+    const int rl = e / n, j = e - rl * n;
+    const long long row = row0 + rl;
+    cplx<R>* base = buf + (long long)rl * np * ld;
+    if (row >= nrows) {
+      for (int p = 0; p < np; ++p) put_fwd<R>(base + p * ld, L, j, mkc<R>(R(0), R(0)));
+      continue;
+    }
+    const long long v = row * n + j;
+    R vals[2 * kMaxLoads * kMaxDv / 2 + 2];
+    for (int p = 0; p < np; ++p) {
+      const cplx<R> z = get_inv<R>(base + p * ld, L, j);
+      vals[2 * p] = z.x;
+      vals[2 * p + 1] = z.y;
+    }
+    for (int l = 0; l < g.L; ++l) {
+      R xv[kMaxDv], qv[kMaxDv];
+      for (int c = 0; c < g.dv; ++c) xv[c] = vals[l * g.dv + c];
+      coef_apply<R, COEF>(A, Mi, v, g.dv, xv, qv);
+      for (int c = 0; c < g.dv; ++c) vals[l * g.dv + c] = qv[c] * coef_scale;
+    }
+    if (C & 1) vals[C] = R(0);
+    for (int p = 0; p < np; ++p) put_fwd<R>(base + p * ld, L, j, mkc<R>(vals[2 * p], vals[2 * p + 1]));
+  }
+  __syncthreads();
+  zero_tail<R>(buf, ld, rows * np, L);
+  __syncthreads();
+  line_core<R>(buf, ld, rows * np, L, false);
+  // 3) split and keep the band
+  for (int e = threadIdx.x; e < rows * np * n2h_band; e += blockDim.x) {
+    const int line = e / n2h_band, k = e - line * n2h_band;
+    const int rl = line / np, p = line - rl * np;
+    const long long row = row0 + rl;
+    if (row >= nrows) continue;
+    cplx<R> xa = mkc<R>(R(0), R(0)), xb = mkc<R>(R(0), R(0));
+    if (2 * k <= n2_solve) {
+      const cplx<R>* lp = buf + (long long)line * ld;
+      const cplx<R> zk = get_fwd<R>(lp, L, k);
+      const cplx<R> zm = get_fwd<R>(lp, L, k == 0 ? 0 : n - k);
+      xa = mkc<R>(R(0.5) * (zk.x + zm.x), R(0.5) * (zk.y - zm.y));
+      xb = mkc<R>(R(0.5) * (zk.y + zm.y), R(0.5) * (zm.x - zk.x));
+      if (2 * k == n2_solve) { xa.y = R(0); xb.y = R(0); }  // mean of +-N/2 (real lines)
+    }
+    const int ca = 2 * p, cb = 2 * p + 1;
+    S[((long long)ca * nrows + row) * n2h_band + k] = xa;
+    if (cb < C) S[((long long)cb * nrows + row) * n2h_band + k] = xb;
+  }
+}
+
+// W_i . u_j cross products per load pair on the solve grid (band energy):
+// partial sums of sum_v sum_c W[i][c] (X[j][c] + delta_cj) (postprocess.py:53-70)
+template <typename R>
+__global__ void __launch_bounds__(128) k_cross_dot(const R* __restrict__ W, const R* __restrict__ X,
+                                                   double* __restrict__ partials, GridDims g,
+                                                   int add_macro) {
+  __shared__ double red[4 * kMaxLoads * kMaxLoads];
+  const int L = g.L, dv = g.dv;
+  double acc[kMaxLoads * kMaxLoads];
+  for (int i = 0; i < kMaxLoads * kMaxLoads; ++i) acc[i] = 0.;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < g.M; v += stride) {
+    for (int i = 0; i < L; ++i)
+      for (int j = 0; j < L; ++j) {
+        double s = 0.;
+        for (int c = 0; c < dv; ++c) {
+          const double u = (double)X[(long long)(j * dv + c) * g.M + v] +
+                           ((add_macro && c == j) ? 1.0 : 0.0);
+          s += (double)W[(long long)(i * dv + c) * g.M + v] * u;
+        }
+        acc[i * L + j] += s;
+      }
+  }
+  block_sum_n(acc, L * L, red, partials + (long long)blockIdx.x * L * L);
+}
+
+// x + E (macroscopic field added per load), for the band energy
+template <typename R>
+__global__ void k_add_macro(const R* __restrict__ X, R* __restrict__ U, GridDims g) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long tot = (long long)g.L * g.dv * g.M;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += stride) {
+    const long long comp = i / g.M;
+    const int l = (int)(comp / g.dv), c = (int)(comp - (long long)l * g.dv);
+    U[i] = X[i] + ((c == l) ? R(1) : R(0));
   }
 }
 

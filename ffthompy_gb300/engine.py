@@ -63,28 +63,50 @@ def pack_coefficient_torch(A, kind):
     return A.reshape((dv * dv,) + tuple(A.shape[2:])).contiguous()
 
 
+def nice_size(n):
+    """Smallest m >= n whose prime factors are all in {2, 3, 5, 7}."""
+    m = int(n)
+    while True:
+        r = m
+        for p in (2, 3, 5, 7):
+            while r % p == 0:
+                r //= p
+        if r == 1:
+            return m
+        m += 1
+
+
 class GalerkinPlan:
     """G o A on one solve grid for a batch of load cases.
 
     N: solve grid; band: grid whose band carries the Green projection
-    (GaNi: band = N; Ga: N = 2*band - 1); scale: Ga scale prod(N)/prod(band)
-    by default; physics 'scalar' | 'elasticity'; precision 'f64' | 'f32' |
-    'mixed' (FP64 fields, FP32 inner CG with FP64 iterative refinement).
+    (GaNi: band = N; Ga on the full double grid: N = 2*band - 1); scale: Ga
+    scale prod(N)/prod(band) by default; physics 'scalar' | 'elasticity';
+    precision 'f64' | 'f32' | 'mixed' (FP64 fields, FP32 inner CG with FP64
+    iterative refinement).
+    integ: band representation of Ga - fields on N, coefficient on the
+    integration grid integ >= 2N-1, projection scale prod(2N-1)/prod(N).
     """
 
     def __init__(self, N, Y, physics='scalar', nloads=None, band=None, scale=None,
-                 precision='f64'):
+                 precision='f64', integ=None):
         require_cuda()
         self.lib = _lib.load()
         self.N = tuple(int(n) for n in N)
         self.dim = len(self.N)
         self.band = tuple(int(n) for n in (band if band is not None else N))
+        self.integ = tuple(int(n) for n in integ) if integ is not None else None
         self.Y = np.asarray(Y, dtype=np.float64)
         self.physics = physics
         self.dv = self.dim if physics == 'scalar' else self.dim * (self.dim + 1) // 2
         self.nloads = int(nloads if nloads is not None else self.dv)
         if scale is None:
-            scale = float(np.prod(self.N, dtype=np.float64) / np.prod(self.band, dtype=np.float64))
+            if self.integ is not None:
+                scale = float(np.prod([2 * n - 1 for n in self.N], dtype=np.float64)
+                              / np.prod(self.N, dtype=np.float64))
+            else:
+                scale = float(np.prod(self.N, dtype=np.float64)
+                              / np.prod(self.band, dtype=np.float64))
         self.scale = float(scale)
         self.precision = precision
         if precision not in ('f64', 'f32', 'mixed'):
@@ -97,8 +119,15 @@ class GalerkinPlan:
         h = ctypes.c_void_p()
         phys = _lib.FHP_SCALAR if physics == 'scalar' else _lib.FHP_ELASTICITY
         prec = {'f64': _lib.FHP_F64, 'f32': _lib.FHP_F32, 'mixed': _lib.FHP_MIXED}[precision]
-        _lib.check(self.lib.fhp_plan_create(ctypes.byref(h), self.dim, n, nb, y, phys,
-                                            self.nloads, self.scale, prec), 'fhp_plan_create')
+        if self.integ is not None:
+            ni = (ctypes.c_int * self.dim)(*self.integ)
+            _lib.check(self.lib.fhp_plan_create_band(ctypes.byref(h), self.dim, n, ni, y, phys,
+                                                     self.nloads, self.scale, prec),
+                       'fhp_plan_create_band')
+        else:
+            _lib.check(self.lib.fhp_plan_create(ctypes.byref(h), self.dim, n, nb, y, phys,
+                                                self.nloads, self.scale, prec),
+                       'fhp_plan_create')
         self.handle = h
         self.coef_kind = None
 
@@ -112,6 +141,10 @@ class GalerkinPlan:
     @property
     def field_shape(self):
         return (self.nloads, self.dv) + self.N
+
+    @property
+    def coef_grid(self):
+        return self.integ if self.integ is not None else self.N
 
     def empty(self):
         return torch.empty(self.field_shape, dtype=self.dtype, device=self.device)
@@ -157,7 +190,7 @@ class GalerkinPlan:
     # -- API -------------------------------------------------------------------
     def set_coefficient(self, A, kind=None):
         """A: (dv, dv) + N coefficient (numpy, or torch on the GPU), origin 0."""
-        shape = (self.dv, self.dv) + self.N
+        shape = (self.dv, self.dv) + self.coef_grid
         if tuple(A.shape) != shape:
             raise ValueError('coefficient shape %s, expected %s' % (tuple(A.shape), shape))
         if isinstance(A, torch.Tensor) and A.is_cuda:
@@ -225,6 +258,13 @@ class GalerkinPlan:
                                               self._stream()), 'fhp_energy_matrix')
         return AH
 
+    def interpolate(self, x, grid):
+        """Trigonometric interpolation of this plan's fields onto grid (>= N)."""
+        grid = tuple(int(n) for n in grid)
+        if grid == self.N:
+            return self._dev(x)
+        return interpolate_fields(self._dev(x), self.N, grid)
+
     def interpolate_to(self, other, x):
         """Trigonometric interpolation of fields x onto other's grid."""
         x = self._dev(x)
@@ -267,3 +307,40 @@ class GalerkinPlan:
         _lib.check(st, 'fhp_homogenize_host')
         self.coef_kind = kind
         return AH, list(kit), list(nres), xh
+
+
+def _fft_plan(grid, ncomp, precision):
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    n = (ctypes.c_int * len(grid))(*grid)
+    prec = _lib.FHP_F32 if precision == torch.float32 else _lib.FHP_F64
+    _lib.check(lib.fhp_fft_plan_create(ctypes.byref(h), len(grid), n, ncomp, prec),
+               'fhp_fft_plan_create')
+    return h
+
+
+def interpolate_fields(x, src, dst):
+    """Trigonometric interpolation (Tensor.project, objects.py:488-511) of the
+    fields x[..., src] onto grid dst >= src on the GPU (fhp_fourier_interp)."""
+    lib = _lib.load()
+    src = tuple(int(n) for n in src)
+    dst = tuple(int(n) for n in dst)
+    lead = tuple(x.shape[:x.dim() - len(src)])
+    ncomp = int(np.prod(lead)) if lead else 1
+    xs = x.reshape((ncomp,) + src).contiguous()
+    out = torch.empty((ncomp,) + dst, dtype=x.dtype, device=x.device)
+    stream = ctypes.c_void_p(torch.cuda.current_stream(x.device).cuda_stream)
+    for k0 in range(0, ncomp, 6):
+        k1 = min(ncomp, k0 + 6)
+        hs = _fft_plan(src, k1 - k0, x.dtype)
+        try:
+            hd = _fft_plan(dst, k1 - k0, x.dtype)
+            try:
+                _lib.check(lib.fhp_fourier_interp(hs, hd, ctypes.c_void_p(xs[k0:k1].data_ptr()),
+                                                  ctypes.c_void_p(out[k0:k1].data_ptr()), stream),
+                           'fhp_fourier_interp')
+            finally:
+                lib.fhp_plan_destroy(hd)
+        finally:
+            lib.fhp_plan_destroy(hs)
+    return out.reshape(lead + dst)

@@ -118,7 +118,7 @@ def get_inverse(A):
     return inv
 
 
-def ga_axis_tables(P, Nbar, h, Y, order):
+def ga_axis_tables(P, Nbar, h, Y, order, target=None):
     """Per-axis source indices and weights of the grid-based Ga coefficient.
 
     For target frequency q of the Nbar grid (FFT order), src gives the FFT-order
@@ -126,6 +126,8 @@ def ga_axis_tables(P, Nbar, h, Y, order):
     crop of the centred spectrum places there (materials.py:94-106), and w the
     1D cell-shape weight h sinc(h q / Y) (order 0) or h sinc^2 (order 1)
     (materials.py:333-389).  The 1/|Y| factor is folded into axis 0.
+    target (>= Nbar, odd Nbar) re-indexes the tables onto a larger grid with
+    zero weight outside the Nbar band: the same trigonometric polynomial.
     """
     P = np.asarray(P, dtype=np.int64)
     Nbar = np.asarray(Nbar, dtype=np.int64)
@@ -160,6 +162,18 @@ def ga_axis_tables(P, Nbar, h, Y, order):
         srcs.append(src)
         ws.append(w)
     ws[0] = ws[0] / np.prod(Y)
+    if target is not None:
+        target = np.asarray(target, dtype=np.int64)
+        for i in range(Nbar.size):
+            n_, t_ = int(Nbar[i]), int(target[i])
+            hb = (n_ - 1) // 2
+            q = np.fft.fftfreq(t_, 1. / t_).astype(np.int64)
+            inb = np.abs(q) <= hb
+            s2 = np.zeros(t_, dtype=np.int32)
+            w2 = np.zeros(t_)
+            s2[inb] = srcs[i][q[inb] % n_]
+            w2[inb] = ws[i][q[inb] % n_]
+            srcs[i], ws[i] = s2, w2
     return np.concatenate(srcs).astype(np.int32), np.concatenate(ws)
 
 
@@ -171,12 +185,14 @@ def _gpu_available():
         return False
 
 
-def ga_grid_coefficient_gpu(vals, P, Nbar, Y, order):
+def ga_grid_coefficient_gpu(vals, P, Nbar, Y, order, target=None):
     """Grid-based Ga coefficient on the GPU (fhp_ga_grid_coefficient).
 
     vals: (dv, dv) + P nodal values, centred origin.  Distinct component fields
-    are transformed once; returns a torch tensor (dv, dv) + Nbar, origin 0.
+    are transformed once; returns a torch tensor (dv, dv) + grid, origin 0,
+    grid = Nbar or the larger target grid (same trigonometric polynomial).
     """
+    grid = Nbar if target is None else np.asarray(target, dtype=np.int64)
     import ctypes
     import torch
     from . import _lib
@@ -196,20 +212,21 @@ def ga_grid_coefficient_gpu(vals, P, Nbar, Y, order):
             else:
                 where[(m, n)] = len(comps)
                 comps.append(v)
-    out = torch.zeros((dv, dv) + tuple(int(n) for n in Nbar), dtype=torch.float64, device='cuda')
+    out = torch.zeros((dv, dv) + tuple(int(n) for n in grid), dtype=torch.float64, device='cuda')
     if not comps:
         return out
-    src, w = ga_axis_tables(P, Nbar, np.asarray(Y, dtype=np.float64) / np.asarray(P), Y, order)
+    src, w = ga_axis_tables(P, Nbar, np.asarray(Y, dtype=np.float64) / np.asarray(P), Y, order,
+                            target=target)
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     for k0 in range(0, len(comps), 6):
         chunk = comps[k0:k0 + 6]
         img = np.stack([np.fft.ifftshift(c) for c in chunk])
         dimg = torch.from_numpy(np.ascontiguousarray(img)).to('cuda')
-        dout = torch.empty((len(chunk),) + tuple(int(n) for n in Nbar), dtype=torch.float64,
+        dout = torch.empty((len(chunk),) + tuple(int(n) for n in grid), dtype=torch.float64,
                            device='cuda')
         hp, ho = ctypes.c_void_p(), ctypes.c_void_p()
         np_ = (ctypes.c_int * d)(*[int(x) for x in P])
-        no_ = (ctypes.c_int * d)(*[int(x) for x in Nbar])
+        no_ = (ctypes.c_int * d)(*[int(x) for x in grid])
         _lib.check(lib.fhp_fft_plan_create(ctypes.byref(hp), d, np_, len(chunk), _lib.FHP_F64),
                    'fhp_fft_plan_create')
         try:
@@ -354,8 +371,35 @@ class Material:
                 raise NotImplementedError('The inclusion (%s) is not supported!' % incl)
         return chars
 
-    def get_A_Ga(self, Nbar, primaldual='primal', order=-1, P=None):
+    def _get_A_Ga_on(self, Nbar, primaldual, order, P, grid):
+        grid = tuple(int(g) for g in grid)
+        if order == -1:
+            order = self.conf.get('order', -1)
+        if order in (0, 1, 'constant', 'bilinear') and _gpu_available() and \
+                np.all(Nbar % 2 == 1):
+            if P is None and 'P' in self.conf:
+                P = self.conf['P']
+            P = np.asarray(P, dtype=np.int64)
+            vals = self.evaluate(Grid.get_coordinates(P, self.Y))
+            if primaldual == 'dual':
+                vals = get_inverse(vals)
+            out = Tensor(name='A_Ga_o{0}_P{1}'.format(order, np.array(P).max()),
+                         val=ga_grid_coefficient_gpu(vals, P, Nbar, self.Y, order, target=grid),
+                         order=2, multype=21, origin=0)
+            out.Y = self.Y
+            return out
+        from .engine import interpolate_fields
+        A = self.get_A_Ga(Nbar, primaldual, order=order, P=P)
+        out = A.copy(val=interpolate_fields(A.data, tuple(int(n) for n in Nbar), grid))
+        out.Y = self.Y
+        return out
+
+    def get_A_Ga(self, Nbar, primaldual='primal', order=-1, P=None, grid=None):
+        """grid (optional, >= Nbar): return the same coefficient (the same
+        trigonometric polynomial) sampled on a larger integration grid."""
         Nbar = np.asarray(Nbar, dtype=np.int64)
+        if grid is not None and tuple(int(g) for g in grid) != tuple(Nbar):
+            return self._get_A_Ga_on(Nbar, primaldual, order, P, grid)
         if order == -1:
             if 'order' not in self.conf:
                 raise ValueError('The material order is undefined!')

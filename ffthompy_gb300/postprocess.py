@@ -13,49 +13,72 @@ import time
 
 import numpy as np
 
-from .engine import GalerkinPlan
+from .engine import GalerkinPlan, interpolate_fields
 from .tensors.objects import Tensor
 
 
 class Solutions:
     """The L zero-mean correctors of one primal/dual solve, kept on the GPU.
 
-    Indexing gives the reference's solution Tensors X_l + E_l
-    (add_macro2minimizer, postprocess.py:73-86).
+    Indexing gives the reference's solution Tensors X_l + E_l on the
+    reference's solution grid out_grid (N for GaNi, 2N-1 for Ga; band-mode
+    fields are interpolated there on access) (add_macro2minimizer,
+    postprocess.py:73-86).
     """
 
-    def __init__(self, plan, X, Y):
+    def __init__(self, plan, X, Y, out_grid=None):
         self.plan = plan
-        self.X = X          # (L, dv) + N, zero-mean fluctuations
+        self.X = X          # (L, dv) + plan.N, zero-mean fluctuations
         self.Y = Y
         self.N = plan.N
+        self.out_grid = tuple(out_grid) if out_grid is not None else plan.N
 
     def __len__(self):
         return self.plan.nloads
 
-    def __getitem__(self, l):
-        v = self.X[l].clone()
-        v[l] += 1.0
-        return Tensor(name='X+E', val=v, order=1, Y=self.Y)
+    def fields(self):
+        if self.out_grid == tuple(self.N):
+            return self.X
+        return interpolate_fields(self.X, self.N, self.out_grid)
 
     def tolist(self):
-        return [self[l] for l in range(len(self))]
+        X = self.fields()
+        out = []
+        for l in range(len(self)):
+            v = X[l].clone()
+            v[l] += 1.0
+            out.append(Tensor(name='X+E', val=v, order=1, Y=self.Y))
+        return out
+
+    def __getitem__(self, l):
+        return self.tolist()[l]
 
 
 def assembly_matrix(A, solutions):
-    """A_H from a coefficient Tensor A and a Solutions batch (postprocess.py:53-70)."""
+    """A_H from a coefficient Tensor A and a Solutions batch (postprocess.py:53-70).
+
+    The energy <A (X_i+E_i), X_j+E_j> on A's grid is exact for band-limited
+    solutions: on the solve grid by a direct sum, on a finer grid (the Ga
+    bounds) through a band plan whose integration grid is A's grid.
+    """
     plan = solutions.plan
-    if tuple(A.N) != tuple(plan.N):
-        tgt = GalerkinPlan(A.N, plan.Y, physics=plan.physics, nloads=plan.nloads,
-                           precision=plan.precision)
-        X = plan.interpolate_to(tgt, solutions.X)
-        tgt.set_coefficient(A.data)
-        return tgt.energy(X, add_macro=True)
-    plan_e = plan
-    if getattr(plan, '_coef_tensor', None) is not A:
-        plan_e = GalerkinPlan(plan.N, plan.Y, physics=plan.physics, nloads=plan.nloads,
+    G = tuple(int(n) for n in A.N)
+    N = tuple(plan.N)
+    if getattr(plan, '_coef_tensor', None) is A:
+        return plan.energy(solutions.X, add_macro=True)
+    if G == N and plan.integ is None:
+        plan_e = GalerkinPlan(N, plan.Y, physics=plan.physics, nloads=plan.nloads,
                               band=plan.band, scale=plan.scale, precision=plan.precision)
-        plan_e.set_coefficient(A.data)
+    elif all(g >= 2 * n - 1 for g, n in zip(G, N)):
+        plan_e = GalerkinPlan(N, plan.Y, physics=plan.physics, nloads=plan.nloads, integ=G,
+                              precision=plan.precision)
+    elif G == N:
+        plan_e = GalerkinPlan(N, plan.Y, physics=plan.physics, nloads=plan.nloads,
+                              precision=plan.precision)
+    else:
+        raise NotImplementedError('energy of solutions on %s with a coefficient on %s'
+                                  % (N, G))
+    plan_e.set_coefficient(A.data)
     return plan_e.energy(solutions.X, add_macro=True)
 
 

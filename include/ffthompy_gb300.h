@@ -59,6 +59,20 @@ const char* fhp_last_error(void);
  */
 int fhp_plan_create(fhp_plan* out, int dim, const int* n, const int* n_band, const double* Y,
                     int physics, int nloads, double g_scale, int precision);
+/*
+ * Band-representation plan for Galerkin with exact integration (Ga): the CG
+ * fields live on the solve grid n (they are trigonometric polynomials of the
+ * band |k_i| <= (Nodd_i-1)/2, so nothing is lost), the coefficient is given on
+ * an integration grid n_int >= 2n-1 (any such grid integrates exactly; a
+ * smooth size avoids prime-length FFTs) and g_scale is the reference's Ga
+ * scale prod(2n-1)/prod(n).  The operator equals the reference's FiGFA on the
+ * (2n-1)-grid restricted to band-limited fields, and inner products agree by
+ * Parseval.  Replaces: applications.scalar / elasticity with solve kind 'Ga'
+ * (ffthompy/applications.py:28-31,111-116) including the Ga bound energy.
+ */
+int fhp_plan_create_band(fhp_plan* out, int dim, const int* n, const int* n_int,
+                         const double* Y, int physics, int nloads, double g_scale,
+                         int precision);
 int fhp_plan_destroy(fhp_plan plan);
 /* FHP_MIXED plans: inner relative tolerance floor eta (default 1e-4) and the
    maximum number of refinement steps (default 30). */
@@ -116,7 +130,7 @@ int fhp_energy_matrix(fhp_plan plan, const void* X, int add_macro, double* AH, v
 
 /*
  * Trigonometric interpolation of the fields of plan src onto the grid of
- * plan dst (same physics, loads, precision; dst grid >= src grid).
+ * plan dst (same field count and precision; dst grid >= src grid).
  * Replaces: Tensor.project / Tensor.enlarge (ffthompy/tensors/objects.py:
  * 428-467, 488-511) as used by assembly_matrix for the Ga bounds.
  */
