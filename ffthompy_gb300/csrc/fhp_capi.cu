@@ -90,8 +90,14 @@ int cg_mixed(fhp_plan_s& p, int proj, const void* b, const void* x0, double tol,
     if ((st = lo.scale_from64(static_cast<const double*>(r), sc_in.data(), r32, s)) != FHP_OK) break;
     fhp::SolveResult in;
     if ((st = lo.cg_solve(proj, r32, nullptr, eta, room, d32, in, 1, s)) != FHP_OK) break;
-    // d32 holds FP32 values: the FP32 engine owns the matching kernel instance
-    if ((st = lo.add_scaled_to64(d32, sc_out.data(), x, s)) != FHP_OK) break;
+    // x += G (s d): the FP32 correction carries roundoff outside range(G),
+    // invisible to the residual but first order in the energy, so it is
+    // projected in FP64 before it is accumulated (d32 holds FP32 values: the
+    // FP32 engine owns the matching kernel instance)
+    if ((st = cuda_status(cudaMemsetAsync(ax, 0, n * 8, s), "memset")) != FHP_OK) break;
+    if ((st = lo.add_scaled_to64(d32, sc_out.data(), static_cast<double*>(ax), s)) != FHP_OK) break;
+    if ((st = hi.project(proj, ax, r, s)) != FHP_OK) break;
+    if ((st = hi.axpy(1.0, r, x, s)) != FHP_OK) break;
     if ((st = hi.apply_ex(proj, x, ax, s, true)) != FHP_OK) break;
     if ((st = hi.residual(b, ax, r, sumsq.data(), s)) != FHP_OK) break;
     for (int l = 0; l < L; ++l) {
@@ -108,11 +114,6 @@ int cg_mixed(fhp_plan_s& p, int proj, const void* b, const void* x0, double tol,
       }
     }
   }
-  // the FP32 corrections carry roundoff outside range(G), invisible to the
-  // G A G residual but first order in the energy: project x in FP64
-  if (st == FHP_OK) st = hi.project(proj, x, ax, s);
-  if (st == FHP_OK)
-    st = cuda_status(cudaMemcpyAsync(x, ax, n * 8, cudaMemcpyDeviceToDevice, s), "copy");
   for (void* q : {ax, r, r32, d32})
     if (q) cudaFreeAsync(q, s);
   if (st == FHP_OK) st = cuda_status(cudaStreamSynchronize(s), "sync");

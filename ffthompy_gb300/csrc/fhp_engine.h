@@ -93,6 +93,8 @@ class EngineBase {
   virtual int apply(int proj, const void* x, void* y, cudaStream_t s) = 0;
   // apply with the input projected first (G A G, band plans; same as apply otherwise)
   virtual int apply_ex(int proj, const void* x, void* y, cudaStream_t s, bool inproj) = 0;
+  // y += a x (fields of this engine's precision)
+  virtual int axpy(double a, const void* x, void* y, cudaStream_t s) = 0;
   // y = G x, G the orthogonal Green projection (no coefficient)
   virtual int project(int proj, const void* x, void* y, cudaStream_t s) = 0;
   virtual int rhs_macro(int proj, void* b, cudaStream_t s) = 0;

@@ -101,24 +101,24 @@ class Engine final : public EngineBase {
     FHP_CHECK(cudaMalloc(&S_, spec_elems_ * sizeof(cplx<R>)));
     // launch geometry
     const int np = (C + 1) / 2;
-    const size_t srow = (size_t)np * l2_.dev.nf * sizeof(cplx<R>);
-    rows_ = std::max(1, kTargetElems / (np * l2_.dev.nf));
+    const size_t srow = (size_t)np * l2_.dev.ld * sizeof(cplx<R>);
+    rows_ = std::max(1, kTargetElems / (np * l2_.dev.ld));
     rows_ = (int)std::min<size_t>(rows_, std::max<size_t>(1, kSmemBudget / srow));
     smem_rows_ = std::max<size_t>((size_t)rows_ * srow, 8 * kMaxLoads * sizeof(double));
     if (smem_rows_ > kSmemMax) { set_error("line too long for shared memory"); return ST_BAD_ARG; }
     row_ctas_ = (int)(((long long)g_.n0 * g_.n1 + rows_ - 1) / rows_);
     // strided c2c on axis 1 (3D) and projection on the first real axis
     if (d == 3) {
-      T1_ = tile_cols(l1_.dev.nf, 1, (long long)g_.n2h);
+      T1_ = tile_cols(l1_.dev.ld, 1, (long long)g_.n2h);
     }
     const LineDev<R>& lp = (d == 3) ? l0_.dev : l1_.dev;
     const long long pin = (d == 3) ? (long long)g_.n1 * g_.n2h : (long long)g_.n2h;
-    Tp_ = tile_cols(lp.nf, g_.dv, pin);
-    if ((size_t)Tp_ * g_.dv * lp.nf * sizeof(cplx<R>) > kSmemMax) {
+    Tp_ = tile_cols(lp.ld, g_.dv, pin);
+    if ((size_t)Tp_ * g_.dv * lp.ld * sizeof(cplx<R>) > kSmemMax) {
       set_error("projection line too long for shared memory");
       return ST_BAD_ARG;
     }
-    if (d == 3) T0_ = tile_cols(l0_.dev.nf, 1, (long long)g_.n1 * g_.n2h);
+    if (d == 3) T0_ = tile_cols(l0_.dev.ld, 1, (long long)g_.n1 * g_.n2h);
     if (cfg_.integ[0] > 0) {
       if ((st = init_band()) != ST_OK) return st;
     }
@@ -166,8 +166,8 @@ class Engine final : public EngineBase {
     FHP_CHECK(cudaMalloc(&S_, sa * sizeof(cplx<R>)));
     FHP_CHECK(cudaMalloc(&SB_, sb * sizeof(cplx<R>)));
     const int np = (C + 1) / 2;
-    const size_t srow = (size_t)np * lb2_.dev.nf * sizeof(cplx<R>);
-    brows_ = std::max(1, kTargetElems / (np * lb2_.dev.nf));
+    const size_t srow = (size_t)np * lb2_.dev.ld * sizeof(cplx<R>);
+    brows_ = std::max(1, kTargetElems / (np * lb2_.dev.ld));
     brows_ = (int)std::min<size_t>(brows_, std::max<size_t>(1, kSmemBudget / srow));
     bsmem_rows_ = (size_t)brows_ * srow;
     if (bsmem_rows_ > kSmemMax) { set_error("integration line too long"); return ST_BAD_ARG; }
@@ -219,6 +219,14 @@ class Engine final : public EngineBase {
     gp_.proj = proj;
     return run_operator(coef_kind_, false, static_cast<const R*>(x), nullptr, nullptr,
                         static_cast<R*>(y), nullptr, s, false, false, inproj);
+  }
+
+  int axpy(double a, const void* x, void* y, cudaStream_t s) override {
+    const size_t n = (size_t)g_.L * g_.dv * g_.M;
+    k_axpby<R><<<grid_for(n), kThreads, 0, s>>>((long long)n, a, static_cast<const R*>(x), 1.0,
+                                                static_cast<R*>(y));
+    FHP_LAUNCHED();
+    return ST_OK;
   }
 
   // y = G x (orthogonal projection onto the compatible / equilibrated fields
@@ -278,7 +286,7 @@ class Engine final : public EngineBase {
       std::memset(&h, 0, sizeof(LoadState));
       h.tol = tol;
       h.maxiter = maxiter;
-      h.guard = sizeof(R) == 4 ? 32.0 : 0.0;
+      h.guard = sizeof(R) == 4 ? 4.0 : 0.0;
     }
     FHP_CHECK(cudaMemcpyAsync(st_, h_st_, g_.L * sizeof(LoadState), cudaMemcpyHostToDevice, s));
     FHP_CHECK(cudaMemsetAsync(all_done_, 0, sizeof(int), s));
@@ -306,6 +314,14 @@ class Engine final : public EngineBase {
       }
       done_iters += nit;
       chunk = std::min(chunk * 2, 32);
+    }
+    // FP32 fields: the iterate drifts out of range(G) by roundoff accumulated
+    // over the iterations, and that component enters the energy to first
+    // order. One projection x <- G x (the identity in exact arithmetic) puts
+    // the drift back to a single rounding.
+    if (sizeof(R) == 4 && (st = project(proj, x, x, s)) != ST_OK) {
+      cudaFreeAsync(dlog, s);
+      return st;
     }
     FHP_CHECK(cudaMemcpyAsync(h_st_, st_, g_.L * sizeof(LoadState), cudaMemcpyDeviceToHost, s));
     res.res_log.assign((size_t)log_rows * g_.L, 0.0);
@@ -360,9 +376,9 @@ class Engine final : public EngineBase {
     const int d = g_.dim;
     const LineDev<R>& lf = d == 3 ? l0_.dev : l1_.dev;
     const long long inner = d == 3 ? (long long)g_.n1 * g_.n2h : (long long)g_.n2h;
-    const int T = d == 3 ? T0_ : tile_cols(lf.nf, 1, inner);
+    const int T = d == 3 ? T0_ : tile_cols(lf.ld, 1, inner);
     dim3 grid((unsigned)((inner + T - 1) / T), (unsigned)(g_.L * g_.dv));
-    k_c2c_axis<R, false><<<grid, kThreads, (size_t)T * lf.nf * sizeof(cplx<R>), s>>>(
+    k_c2c_axis<R, false><<<grid, kThreads, (size_t)T * lf.ld * sizeof(cplx<R>), s>>>(
         Sp, d == 3 ? g_.n0 : g_.n1, inner, lf, T, nullptr, nullptr, 0);
     FHP_LAUNCHED();
     return ST_OK;
@@ -373,9 +389,9 @@ class Engine final : public EngineBase {
     const int d = g_.dim;
     const LineDev<R>& lf = d == 3 ? l0_.dev : l1_.dev;
     const long long inner = d == 3 ? (long long)g_.n1 * g_.n2h : (long long)g_.n2h;
-    const int T = d == 3 ? T0_ : tile_cols(lf.nf, 1, inner);
+    const int T = d == 3 ? T0_ : tile_cols(lf.ld, 1, inner);
     dim3 grid((unsigned)((inner + T - 1) / T), (unsigned)(g_.L * g_.dv));
-    k_c2c_axis<R, true><<<grid, kThreads, (size_t)T * lf.nf * sizeof(cplx<R>), s>>>(
+    k_c2c_axis<R, true><<<grid, kThreads, (size_t)T * lf.ld * sizeof(cplx<R>), s>>>(
         Sp, d == 3 ? g_.n0 : g_.n1, inner, lf, T, nullptr, nullptr, 0);
     FHP_LAUNCHED();
     return inv_passes(Sp, static_cast<R*>(xv), (R)scale, false, nullptr, false, s);
@@ -511,6 +527,7 @@ class Engine final : public EngineBase {
     LineDev<R>& L = out.dev;
     L.n = h.n;
     L.nf = h.nf;
+    L.ld = padded_ld(h.nf);
     L.blue = h.blue;
     L.nst = h.nst;
     for (int i = 0; i < kMaxStages; ++i) L.rad[i] = i < h.nst ? h.rad[i] : 1;
@@ -608,7 +625,7 @@ class Engine final : public EngineBase {
     if (g_.dim == 3) {
       dim3 grid((unsigned)((g_.n2h + T1_ - 1) / T1_), (unsigned)(g_.L * g_.dv * g_.n0));
       const int pk = pbeg("c2c_axis1_fwd", 2.0 * spec_bytes(), s);
-      k_c2c_axis<R, false><<<grid, kThreads, (size_t)T1_ * l1_.dev.nf * sizeof(cplx<R>), s>>>(
+      k_c2c_axis<R, false><<<grid, kThreads, (size_t)T1_ * l1_.dev.ld * sizeof(cplx<R>), s>>>(
           Sp, g_.n1, (long long)g_.n2h, l1_.dev, T1_, ad, st, g_.dv * g_.n0);
       pend(pk, s);
       FHP_LAUNCHED();
@@ -623,7 +640,7 @@ class Engine final : public EngineBase {
     if (g_.dim == 3) {
       dim3 grid((unsigned)((g_.n2h + T1_ - 1) / T1_), (unsigned)(g_.L * g_.dv * g_.n0));
       const int pk = pbeg("c2c_axis1_inv", 2.0 * spec_bytes(), s);
-      k_c2c_axis<R, true><<<grid, kThreads, (size_t)T1_ * l1_.dev.nf * sizeof(cplx<R>), s>>>(
+      k_c2c_axis<R, true><<<grid, kThreads, (size_t)T1_ * l1_.dev.ld * sizeof(cplx<R>), s>>>(
           Sp, g_.n1, (long long)g_.n2h, l1_.dev, T1_, ad, st, g_.dv * g_.n0);
       pend(pk, s);
       FHP_LAUNCHED();
@@ -646,7 +663,7 @@ class Engine final : public EngineBase {
     const LineDev<R>& lp = d == 3 ? l0_.dev : l1_.dev;
     const long long inner = d == 3 ? (long long)g_.n1 * g_.n2h : (long long)g_.n2h;
     dim3 grid((unsigned)((inner + Tp_ - 1) / Tp_), (unsigned)g_.L);
-    const size_t smem = (size_t)Tp_ * g_.dv * lp.nf * sizeof(cplx<R>);
+    const size_t smem = (size_t)Tp_ * g_.dv * lp.ld * sizeof(cplx<R>);
     const int pk = pbeg("proj_axis0", 2.0 * spec_bytes(), s);
     k_proj_first<R><<<grid, kThreads, smem, s>>>(Sp, g_, d == 3 ? g_.n0 : g_.n1, inner, lp, Tp_,
                                                  gp_, cg ? all_done_ : nullptr,
@@ -662,7 +679,7 @@ class Engine final : public EngineBase {
                 const char* name) {
     const bool projm = mode == BAND_DOWN_PROJ || mode == BAND_UP_PROJ;
     const int nlc = projm ? g_.dv : 1;
-    const int nf = (mode == BAND_PAD ? 0 : L1.nf) + (mode == BAND_DOWN ? 0 : L2.nf);
+    const int nf = (mode == BAND_PAD ? 0 : L1.ld) + (mode == BAND_DOWN ? 0 : L2.ld);
     const int T = tile_cols(nf, nlc, ax.inner);
     const size_t smem = (size_t)nlc * T * nf * sizeof(cplx<R>);
     if (smem > kSmemMax) { set_error("band line too long for shared memory"); return ST_BAD_ARG; }
@@ -672,6 +689,10 @@ class Engine final : public EngineBase {
     const LoadState* st = cg ? st_ : nullptr;
     const double bytes = (double)(g_.L * g_.dv) * ax.mid * ax.inner *
                          (ax.n_in + ax.n_out) * sizeof(cplx<R>);
+    // the input projection of G A G is the plain orthogonal projection (scale 1);
+    // the output projection carries s / prod(B)
+    GreenParams gpin = gp_;
+    gpin.scale = 1.0;
     const int pk = pbeg(name, bytes, s);
     switch (mode) {
       case BAND_UP:
@@ -681,7 +702,7 @@ class Engine final : public EngineBase {
         k_band_axis<R, BAND_DOWN><<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st);
         break;
       case BAND_UP_PROJ:
-        k_band_axis<R, BAND_UP_PROJ><<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st);
+        k_band_axis<R, BAND_UP_PROJ><<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gpin, ad, st);
         break;
       case BAND_PAD:
         k_band_axis<R, BAND_PAD><<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st);
@@ -730,7 +751,7 @@ class Engine final : public EngineBase {
       // forward DFT_N along axis 1, then axis 0: DFT_N, G, pad, iDFT_B; then pad axis 1
       dim3 grid((unsigned)((n2h + T1_ - 1) / T1_), (unsigned)(g_.L * g_.dv * g_.n0));
       const int pk = pbeg("band_c2c_axis1_fwd", 2.0 * spec_bytes_n(), s);
-      k_c2c_axis<R, false><<<grid, kThreads, (size_t)T1_ * l1_.dev.nf * sizeof(cplx<R>), s>>>(
+      k_c2c_axis<R, false><<<grid, kThreads, (size_t)T1_ * l1_.dev.ld * sizeof(cplx<R>), s>>>(
           SA, g_.n1, n2h, l1_.dev, T1_, ad, cg ? st_ : nullptr, g_.dv * g_.n0);
       pend(pk, s);
       FHP_LAUNCHED();
@@ -770,7 +791,7 @@ class Engine final : public EngineBase {
       // K7: inverse DFT_N along axis 0
       dim3 grid((unsigned)((g_.n1 * n2h + T0_ - 1) / T0_), (unsigned)(g_.L * g_.dv));
       const int pk = pbeg("band_c2c_axis0_inv", 2.0 * spec_bytes_n(), s);
-      k_c2c_axis<R, true><<<grid, kThreads, (size_t)T0_ * l0_.dev.nf * sizeof(cplx<R>), s>>>(
+      k_c2c_axis<R, true><<<grid, kThreads, (size_t)T0_ * l0_.dev.ld * sizeof(cplx<R>), s>>>(
           SA, g_.n0, (long long)g_.n1 * n2h, l0_.dev, T0_, ad, cg ? st_ : nullptr, g_.dv);
       pend(pk, s);
       FHP_LAUNCHED();

@@ -52,11 +52,17 @@ __device__ __forceinline__ cplx<R> cmul_pi(cplx<R> a) { return mkc<R>(-a.y, a.x)
 
 constexpr int kMaxStages = 24;
 
+// Padded shared-memory slot of line element i: one spare slot per 32 elements
+// breaks the power-of-two strides of the late radix stages across banks.
+__device__ __forceinline__ int sp(int i) { return i + (i >> 5); }
+__host__ __device__ inline int padded_ld(int nf) { return nf + (nf >> 5) + 1; }
+
 // Device view of one line plan (passed by value in kernel parameters).
 template <typename R>
 struct LineDev {
   int n;        // logical length
   int nf;       // transform length of the core (n, or Bluestein m)
+  int ld;       // shared-memory stride of one line (padded, >= sp(nf - 1) + 1)
   int blue;     // 1: Bluestein
   int nst;      // number of radix stages of the core
   int rad[kMaxStages];
@@ -170,41 +176,49 @@ __device__ __forceinline__ void dft16(cplx<R>* v) {
   }
 }
 
-// Odd prime radix, symmetric-pair form; roots W_r^m read from the line table
-// (W_r^m = tw[m * nf / r]).
+// Odd prime radix, symmetric-pair form, in place: v[j] <- v[j] + v[r-j] and
+// v[r-j] <- v[j] - v[r-j] for j <= (r-1)/2, then the outputs pair up as
+// y_k = a_k - i b_k, y_{r-k} = a_k + i b_k with a_k = x0 + sum_j cos(2pi jk/r) s_j,
+// b_k = sum_j sin(2pi jk/r) d_j.  Roots W_r^m = tw[m * nf / r] (cos, -sin).
+// Only the r input registers and two accumulators stay live.
 template <typename R, int RAD>
 __device__ __forceinline__ void dft_odd(cplx<R>* v, const cplx<R>* __restrict__ tw, int nf) {
   constexpr int H = (RAD - 1) / 2;
   const int step = nf / RAD;
-  cplx<R> sp[H], sm[H];
 #pragma unroll
   for (int j = 1; j <= H; ++j) {
-    sp[j - 1] = cadd<R>(v[j], v[RAD - j]);
-    sm[j - 1] = csub<R>(v[j], v[RAD - j]);
+    const cplx<R> a = v[j], b = v[RAD - j];
+    v[j] = cadd<R>(a, b);
+    v[RAD - j] = csub<R>(a, b);
   }
-  cplx<R> y0 = v[0];
+  const cplx<R> x0 = v[0];
+  cplx<R> y0 = x0;
 #pragma unroll
-  for (int j = 0; j < H; ++j) y0 = cadd<R>(y0, sp[j]);
-  cplx<R> out[RAD];
-  out[0] = y0;
+  for (int j = 1; j <= H; ++j) y0 = cadd<R>(y0, v[j]);
+  // outputs are written back in place after all sums that need the inputs:
+  // compute pairs into a small rolling buffer of H values each
+  cplx<R> ak[H], bk[H];
 #pragma unroll
   for (int k = 1; k <= H; ++k) {
-    cplx<R> a = v[0];
+    cplx<R> a = x0;
     cplx<R> b = mkc<R>(R(0), R(0));
 #pragma unroll
     for (int j = 1; j <= H; ++j) {
-      const cplx<R> w = tw[((j * k) % RAD) * step];  // (cos, -sin)
-      a.x += w.x * sp[j - 1].x;
-      a.y += w.x * sp[j - 1].y;
-      // b = sum sin * sm  (sin = -w.y)
-      b.x -= w.y * sm[j - 1].x;
-      b.y -= w.y * sm[j - 1].y;
+      const cplx<R> w = tw[((j * k) % RAD) * step];
+      a.x += w.x * v[j].x;
+      a.y += w.x * v[j].y;
+      b.x -= w.y * v[RAD - j].x;
+      b.y -= w.y * v[RAD - j].y;
     }
-    out[k] = cadd<R>(a, cmul_mi<R>(b));
-    out[RAD - k] = cadd<R>(a, cmul_pi<R>(b));
+    ak[k - 1] = a;
+    bk[k - 1] = b;
   }
+  v[0] = y0;
 #pragma unroll
-  for (int k = 0; k < RAD; ++k) v[k] = out[k];
+  for (int k = 1; k <= H; ++k) {
+    v[k] = cadd<R>(ak[k - 1], cmul_mi<R>(bk[k - 1]));
+    v[RAD - k] = cadd<R>(ak[k - 1], cmul_pi<R>(bk[k - 1]));
+  }
 }
 
 template <typename R, int RAD>
@@ -236,45 +250,57 @@ __device__ __forceinline__ void stage_run(cplx<R>* __restrict__ buf, int ld, int
     const int bb = b - line * nbl;
     const int g = bb / ms;
     const int j1 = bb - g * ms;
-    cplx<R>* p = buf + line * ld + g * ns + j1;
+    cplx<R>* lp = buf + line * ld;
+    const int base = g * ns + j1;
     cplx<R> v[RAD];
     if constexpr (!INV) {
 #pragma unroll
-      for (int q = 0; q < RAD; ++q) v[q] = p[q * ms];
+      for (int q = 0; q < RAD; ++q) v[q] = lp[sp(base + q * ms)];
       dft_fwd<R, RAD>(v, tw, nf);
-      p[0] = v[0];
+      lp[sp(base)] = v[0];
 #pragma unroll
-      for (int q = 1; q < RAD; ++q) p[q * ms] = cmul<R>(v[q], tw[j1 * q * tws]);
+      for (int q = 1; q < RAD; ++q) lp[sp(base + q * ms)] = cmul<R>(v[q], tw[j1 * q * tws]);
     } else {
-      v[0] = cconj<R>(p[0]);
+      v[0] = cconj<R>(lp[sp(base)]);
 #pragma unroll
-      for (int q = 1; q < RAD; ++q) v[q] = cconj<R>(cmulc<R>(p[q * ms], tw[j1 * q * tws]));
+      for (int q = 1; q < RAD; ++q)
+        v[q] = cconj<R>(cmulc<R>(lp[sp(base + q * ms)], tw[j1 * q * tws]));
       dft_fwd<R, RAD>(v, tw, nf);
 #pragma unroll
-      for (int q = 0; q < RAD; ++q) p[q * ms] = cconj<R>(v[q]);
+      for (int q = 0; q < RAD; ++q) lp[sp(base + q * ms)] = cconj<R>(v[q]);
     }
   }
 }
 
+// Radix dispatch, split so that the large odd radices (register hungry, rare)
+// do not set the register budget of the common power-of-two / 3 / 5 stages.
 template <typename R, bool INV>
-__device__ __noinline__ void stage_dispatch(cplx<R>* buf, int ld, int nlines, int nf, int ns,
-                                            int rad, const cplx<R>* tw, int tid, int nthr) {
+__device__ __noinline__ void stage_dispatch_rare(cplx<R>* buf, int ld, int nlines, int nf, int ns,
+                                                 int rad, const cplx<R>* tw, int tid, int nthr) {
+  switch (rad) {
+    case 7: stage_run<R, 7, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
+    case 11: stage_run<R, 11, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
+    case 13: stage_run<R, 13, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
+    case 19: stage_run<R, 19, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
+    case 23: stage_run<R, 23, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
+    case 29: stage_run<R, 29, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
+    case 31: stage_run<R, 31, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
+    default: break;  // plans only contain the radices of factor_radices
+  }
+}
+
+template <typename R, bool INV>
+__device__ __forceinline__ void stage_dispatch(cplx<R>* buf, int ld, int nlines, int nf, int ns,
+                                               int rad, const cplx<R>* tw, int tid, int nthr) {
   switch (rad) {
     case 2: stage_run<R, 2, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
     case 3: stage_run<R, 3, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
     case 4: stage_run<R, 4, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
     case 5: stage_run<R, 5, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
-    case 7: stage_run<R, 7, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
     case 8: stage_run<R, 8, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
-    case 11: stage_run<R, 11, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
-    case 13: stage_run<R, 13, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
     case 16: stage_run<R, 16, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
     case 17: stage_run<R, 17, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
-    case 19: stage_run<R, 19, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
-    case 23: stage_run<R, 23, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
-    case 29: stage_run<R, 29, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
-    case 31: stage_run<R, 31, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
-    default: break;  // plans only contain the radices above
+    default: stage_dispatch_rare<R, INV>(buf, ld, nlines, nf, ns, rad, tw, tid, nthr); break;
   }
 }
 
@@ -300,7 +326,7 @@ __device__ void line_core(cplx<R>* buf, int ld, int nlines, const LineDev<R>& L,
     const int tot = nlines * L.nf;
     for (int e = tid; e < tot; e += nthr) {
       const int line = e / L.nf, j = e - line * L.nf;
-      cplx<R>* p = buf + line * ld + j;
+      cplx<R>* p = buf + line * ld + sp(j);
       *p = cmul<R>(*p, L.bhat[j]);
     }
     __syncthreads();
@@ -320,23 +346,23 @@ __device__ void line_core(cplx<R>* buf, int ld, int nlines, const LineDev<R>& L,
 // forward input x_j (natural, j < n)
 template <typename R>
 __device__ __forceinline__ void put_fwd(cplx<R>* line, const LineDev<R>& L, int j, cplx<R> v) {
-  line[j] = L.blue ? cmul<R>(v, L.chirp[j]) : v;
+  line[sp(j)] = L.blue ? cmul<R>(v, L.chirp[j]) : v;
 }
 // forward output X_k (k < n)
 template <typename R>
 __device__ __forceinline__ cplx<R> get_fwd(const cplx<R>* line, const LineDev<R>& L, int k) {
-  return L.blue ? cmul<R>(line[k], L.chirp[k]) : line[L.pos[k]];
+  return L.blue ? cmul<R>(line[sp(k)], L.chirp[k]) : line[sp(L.pos[k])];
 }
 // inverse input X_k (k < n)
 template <typename R>
 __device__ __forceinline__ void put_inv(cplx<R>* line, const LineDev<R>& L, int k, cplx<R> v) {
-  if (L.blue) line[k] = cmul<R>(cconj<R>(v), L.chirp[k]);
-  else line[L.pos[k]] = v;
+  if (L.blue) line[sp(k)] = cmul<R>(cconj<R>(v), L.chirp[k]);
+  else line[sp(L.pos[k])] = v;
 }
 // inverse output x_j (j < n), unnormalised
 template <typename R>
 __device__ __forceinline__ cplx<R> get_inv(const cplx<R>* line, const LineDev<R>& L, int j) {
-  return L.blue ? cconj<R>(cmul<R>(line[j], L.chirp[j])) : line[j];
+  return L.blue ? cconj<R>(cmul<R>(line[sp(j)], L.chirp[j])) : line[sp(j)];
 }
 // Bluestein lines need zeros in slots [n, nf) before the core.
 template <typename R>
@@ -346,7 +372,7 @@ __device__ __forceinline__ void zero_tail(cplx<R>* buf, int ld, int nlines, cons
   const int tot = nlines * w;
   for (int e = threadIdx.x; e < tot; e += blockDim.x) {
     const int line = e / w, j = L.n + (e - line * w);
-    buf[line * ld + j] = mkc<R>(R(0), R(0));
+    buf[line * ld + sp(j)] = mkc<R>(R(0), R(0));
   }
 }
 

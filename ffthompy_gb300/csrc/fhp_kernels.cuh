@@ -197,7 +197,7 @@ __device__ __forceinline__ void block_sum_n(double* acc, int n, double* red, dou
 // CTA: `rows` consecutive (i0,i1) rows, all comps; comps paired as z = a + i b.
 // ---------------------------------------------------------------------------
 template <typename R, int COEF, bool PUPD>
-__global__ void __launch_bounds__(256) k_r2c_last(
+__global__ void __launch_bounds__(256, 2) k_r2c_last(
     const R* xin, R* pio, const R* __restrict__ rvec,
     const R* __restrict__ A, cplx<R>* __restrict__ S, GridDims g, LineDev<R> L, int rows,
     const LoadState* __restrict__ st, const int* __restrict__ all_done) {
@@ -206,7 +206,7 @@ __global__ void __launch_bounds__(256) k_r2c_last(
   cplx<R>* buf = reinterpret_cast<cplx<R>*>(smem_raw);
   const int C = g.L * g.dv;
   const int np = (C + 1) / 2;
-  const int ld = L.nf;
+  const int ld = L.ld;
   const long long nrows = (long long)g.n0 * g.n1;
   const long long row0 = (long long)blockIdx.x * rows;
   const int n = g.n2;
@@ -216,7 +216,7 @@ __global__ void __launch_bounds__(256) k_r2c_last(
     const long long row = row0 + rl;
     cplx<R>* base = buf + (long long)rl * np * ld;
     if (row >= nrows) {
-      for (int p = 0; p < np; ++p) base[p * ld + j] = mkc<R>(R(0), R(0));
+      for (int p = 0; p < np; ++p) base[p * ld + sp(j)] = mkc<R>(R(0), R(0));
       continue;
     }
     const long long v = row * n + j;
@@ -237,18 +237,18 @@ __global__ void __launch_bounds__(256) k_r2c_last(
         const int comp = l * g.dv + c;
         cplx<R>* line = base + (comp >> 1) * ld;
         // slot j of the pair line: real part from even comp, imag from odd
-        R* slot = reinterpret_cast<R*>(line + j) + (comp & 1);
+        R* slot = reinterpret_cast<R*>(line + sp(j)) + (comp & 1);
         *slot = q[c];
       }
     }
-    if (C & 1) reinterpret_cast<R*>(base + (np - 1) * ld + j)[1] = R(0);
+    if (C & 1) reinterpret_cast<R*>(base + (np - 1) * ld + sp(j))[1] = R(0);
   }
   __syncthreads();
   if (L.blue) {
     // chirp pre-multiply of the stored values (put_fwd for Bluestein lines)
     for (int e = threadIdx.x; e < rows * np * n; e += blockDim.x) {
       const int line = e / n, j = e - line * n;
-      cplx<R>* p = buf + (long long)line * ld + j;
+      cplx<R>* p = buf + (long long)line * ld + sp(j);
       *p = cmul<R>(*p, L.chirp[j]);
     }
   }
@@ -279,7 +279,7 @@ __global__ void __launch_bounds__(256) k_r2c_last(
 // elements after it; CTA = tile of T inner columns of one outer index.
 // ---------------------------------------------------------------------------
 template <typename R, bool INV>
-__global__ void __launch_bounds__(256) k_c2c_axis(cplx<R>* __restrict__ S, int na, long long inner,
+__global__ void __launch_bounds__(256, 2) k_c2c_axis(cplx<R>* __restrict__ S, int na, long long inner,
                                                   LineDev<R> L, int T,
                                                   const int* __restrict__ all_done,
                                                   const LoadState* __restrict__ st,
@@ -288,7 +288,7 @@ __global__ void __launch_bounds__(256) k_c2c_axis(cplx<R>* __restrict__ S, int n
   if (st && outer_per_load > 0 && st[blockIdx.y / outer_per_load].done) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* buf = reinterpret_cast<cplx<R>*>(smem_raw);
-  const int ld = L.nf;
+  const int ld = L.ld;
   const long long t0 = (long long)blockIdx.x * T;
   cplx<R>* base = S + (long long)blockIdx.y * na * inner;
   const int tasks = T * na;
@@ -317,7 +317,7 @@ __global__ void __launch_bounds__(256) k_c2c_axis(cplx<R>* __restrict__ S, int n
 // one load; lines (c, t) for c < dv.
 // ---------------------------------------------------------------------------
 template <typename R>
-__global__ void __launch_bounds__(256) k_proj_first(cplx<R>* __restrict__ S, GridDims g, int na,
+__global__ void __launch_bounds__(256, 2) k_proj_first(cplx<R>* __restrict__ S, GridDims g, int na,
                                                     long long inner, LineDev<R> L, int T,
                                                     GreenParams gp,
                                                     const int* __restrict__ all_done,
@@ -327,7 +327,7 @@ __global__ void __launch_bounds__(256) k_proj_first(cplx<R>* __restrict__ S, Gri
   if (st && st[l].done) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* buf = reinterpret_cast<cplx<R>*>(smem_raw);
-  const int ld = L.nf;
+  const int ld = L.ld;
   const int dv = g.dv;
   const long long t0 = (long long)blockIdx.x * T;
   const int nl = dv * T;
@@ -388,7 +388,7 @@ __global__ void __launch_bounds__(256) k_proj_first(cplx<R>* __restrict__ S, Gri
 // fused dot <p, y> per load (CG's <P, AP>).
 // ---------------------------------------------------------------------------
 template <typename R, bool DOT>
-__global__ void __launch_bounds__(256) k_c2r_last(const cplx<R>* __restrict__ S, R* __restrict__ y,
+__global__ void __launch_bounds__(256, 2) k_c2r_last(const cplx<R>* __restrict__ S, R* __restrict__ y,
                                                   const R* __restrict__ pdot,
                                                   double* __restrict__ partials, GridDims g,
                                                   LineDev<R> L, int rows, R scale,
@@ -398,7 +398,7 @@ __global__ void __launch_bounds__(256) k_c2r_last(const cplx<R>* __restrict__ S,
   cplx<R>* buf = reinterpret_cast<cplx<R>*>(smem_raw);
   const int C = g.L * g.dv;
   const int np = (C + 1) / 2;
-  const int ld = L.nf;
+  const int ld = L.ld;
   const long long nrows = (long long)g.n0 * g.n1;
   const long long row0 = (long long)blockIdx.x * rows;
   const int n = g.n2, n2h = g.n2h;
@@ -492,13 +492,14 @@ __global__ void __launch_bounds__(256) k_cg_update(R* __restrict__ x, R* __restr
   for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < g.M; v += stride) {
     for (int l = 0; l < g.L; ++l) {
       if (!act[l]) continue;
+      // updates in the field precision, <R,R> accumulated in FP64
+      const R a = (R)alpha[l];
       for (int c = 0; c < g.dv; ++c) {
         const long long i = (long long)(l * g.dv + c) * g.M + v;
-        const double pv = (double)p[i];
-        x[i] = (R)((double)x[i] + alpha[l] * pv);
-        const R rn = (R)((double)r[i] - alpha[l] * (double)ap[i]);
+        x[i] = x[i] + a * p[i];
+        const R rn = r[i] - a * ap[i];
         r[i] = rn;
-        acc[l] += (double)rn * (double)rn;
+        acc[l] += (double)(rn * rn);
       }
     }
   }
@@ -797,7 +798,7 @@ __device__ __forceinline__ cplx<R> band_down_value(const cplx<R>* line, const Li
 }
 
 template <typename R, int MODE>
-__global__ void __launch_bounds__(256) k_band_axis(const cplx<R>* __restrict__ Sin,
+__global__ void __launch_bounds__(256, 2) k_band_axis(const cplx<R>* __restrict__ Sin,
                                                    cplx<R>* __restrict__ Sout, GridDims g,
                                                    BandAxis ax, LineDev<R> L1, LineDev<R> L2,
                                                    int T, GreenParams gp,
@@ -813,8 +814,8 @@ __global__ void __launch_bounds__(256) k_band_axis(const cplx<R>* __restrict__ S
   const int c0 = PROJ ? cl * g.dv : cl;
   const int load = c0 / g.dv;
   if (st && st[load].done) return;
-  const int ld1 = (MODE == BAND_PAD) ? 0 : L1.nf;
-  const int ld2 = (MODE == BAND_DOWN) ? 0 : L2.nf;
+  const int ld1 = (MODE == BAND_PAD) ? 0 : L1.ld;
+  const int ld2 = (MODE == BAND_DOWN) ? 0 : L2.ld;
   cplx<R>* buf1 = reinterpret_cast<cplx<R>*>(smem_raw);
   cplx<R>* buf2 = buf1 + (size_t)nlc * T * ld1;
   const long long t0 = (long long)blockIdx.x * T;
@@ -962,7 +963,7 @@ __global__ void __launch_bounds__(256) k_band_axis(const cplx<R>* __restrict__ S
 // S[comp][row][N2h] (row over the B grid's leading axes): c2r to the B2 points,
 // q = A x * cscale per voxel, r2c back and keep the band k2 <= h2.
 template <typename R, int COEF>
-__global__ void __launch_bounds__(256) k_band_last(cplx<R>* __restrict__ S,
+__global__ void __launch_bounds__(256, 2) k_band_last(cplx<R>* __restrict__ S,
                                                    const R* __restrict__ A, GridDims g,
                                                    long long nrows, int n2h_band, int n2_solve,
                                                    LineDev<R> L, int rows, R coef_scale,
@@ -972,7 +973,7 @@ __global__ void __launch_bounds__(256) k_band_last(cplx<R>* __restrict__ S,
   cplx<R>* buf = reinterpret_cast<cplx<R>*>(smem_raw);
   const int C = g.L * g.dv;
   const int np = (C + 1) / 2;
-  const int ld = L.nf;
+  const int ld = L.ld;
   const int n = L.n;                       // B2
   const long long Mi = nrows * n;          // voxels of the integration grid
   const long long row0 = (long long)blockIdx.x * rows;
@@ -1009,20 +1010,35 @@ __global__ void __launch_bounds__(256) k_band_last(cplx<R>* __restrict__ S,
       continue;
     }
     const long long v = row * n + j;
-    R vals[2 * kMaxLoads * kMaxDv / 2 + 2];
-    for (int p = 0; p < np; ++p) {
-      const cplx<R> z = get_inv<R>(base + p * ld, L, j);
-      vals[2 * p] = z.x;
-      vals[2 * p + 1] = z.y;
+    // slots of voxel j hold the inverse output; make them raw values first
+    // (Bluestein outputs carry conj and chirp), then one load at a time: comp c
+    // sits in pair line c/2 (real part for even c)
+    if (L.blue) {
+      for (int p = 0; p < np; ++p) {
+        const cplx<R> z = get_inv<R>(base + p * ld, L, j);
+        base[p * ld + sp(j)] = z;
+      }
     }
     for (int l = 0; l < g.L; ++l) {
       R xv[kMaxDv], qv[kMaxDv];
-      for (int c = 0; c < g.dv; ++c) xv[c] = vals[l * g.dv + c];
+      for (int c = 0; c < g.dv; ++c) {
+        const int comp = l * g.dv + c;
+        xv[c] = reinterpret_cast<const R*>(base + (comp >> 1) * ld + sp(j))[comp & 1];
+      }
       coef_apply<R, COEF>(A, Mi, v, g.dv, xv, qv);
-      for (int c = 0; c < g.dv; ++c) vals[l * g.dv + c] = qv[c] * coef_scale;
+      for (int c = 0; c < g.dv; ++c) {
+        const int comp = l * g.dv + c;
+        R* slot = reinterpret_cast<R*>(base + (comp >> 1) * ld + sp(j)) + (comp & 1);
+        *slot = qv[c] * coef_scale;
+      }
     }
-    if (C & 1) vals[C] = R(0);
-    for (int p = 0; p < np; ++p) put_fwd<R>(base + p * ld, L, j, mkc<R>(vals[2 * p], vals[2 * p + 1]));
+    if (C & 1) reinterpret_cast<R*>(base + (np - 1) * ld + sp(j))[1] = R(0);
+    if (L.blue) {  // forward Bluestein input carries the chirp
+      for (int p = 0; p < np; ++p) {
+        cplx<R>* slot = base + p * ld + sp(j);
+        *slot = cmul<R>(*slot, L.chirp[j]);
+      }
+    }
   }
   __syncthreads();
   zero_tail<R>(buf, ld, rows * np, L);
