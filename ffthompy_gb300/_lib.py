@@ -53,6 +53,9 @@ SIGNATURES = {
     'fhp_profile_read': (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_char_p, _c_ll_p,
                                         _c_double_p, _c_double_p, _c_int_p]),
     'fhp_plan_launches': (ctypes.c_longlong, [_vp]),
+    'fhp_energy_matrix_noalloc': (ctypes.c_int, [ctypes.c_int, _c_int_p, ctypes.c_int,
+                                                 ctypes.c_int, ctypes.c_int, _vp, _vp,
+                                                 ctypes.c_int, _vp, _vp]),
 }
 
 _lib = None

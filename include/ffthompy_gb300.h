@@ -183,6 +183,31 @@ int fhp_profile_read(fhp_plan plan, int max_kinds, char* names, long long* launc
 /* Number of kernel launches issued by this plan since creation. */
 long long fhp_plan_launches(fhp_plan plan);
 
+/*
+ * A_H[i*loads + j] = <A u_i, u_j> as fhp_energy_matrix computes it, for fields
+ * and a coefficient on one grid, without a plan and without allocating
+ * anything: one kernel launch whose block partial sums go to a fixed scratch
+ * array inside the library (36,896 doubles, 288.25 KiB per device).
+ * For callers that must not allocate while they run: code whose device memory
+ * is all owned by another allocator (a framework's caching allocator, or a pool
+ * reserved up front to the limit of HBM), where a cudaMalloc from inside a
+ * library fails or stalls the device, and loops that must not wait on the host.
+ * X [loads][dv][n...] and A [c][n...] (c as for fhp_set_coefficient) are
+ * float64 device arrays; AH is a float64 device array of loads*loads, written
+ * on `stream`; the call does not synchronise.
+ * Limits: loads <= 6 and dv <= 6 (the scratch holds 6 x 6 accumulators for at
+ * most 1024 blocks); larger sizes return FHP_BAD_ARG.
+ * Every call on a device uses the same scratch: calls that overlap in time on
+ * one device (several streams or host threads) race, so serialise them.
+ * The first call on each device does a one-time set-up (looks up the scratch
+ * address, loads the kernels); make that call before any stream capture.
+ * No counterpart in the reference: its assembly_matrix
+ * (ffthompy/postprocess.py:53-70) is the same sum, with no allocation contract.
+ */
+int fhp_energy_matrix_noalloc(int dim, const int* n, int dv, int loads, int kind,
+                              const double* A, const double* X, int add_macro, double* AH,
+                              void* stream);
+
 #ifdef __cplusplus
 }
 #endif
