@@ -338,7 +338,9 @@ def run_gpu(args):
     tf = os.path.join(ROOT, 'profiles', 'traffic.json')
     if os.path.exists(tf):
         try:
-            traffic = _json.load(open(tf)).get(tname, {}).get('bytes_per_launch')
+            # ncu DRAM bytes per launch of the dominant kernel, per workload
+            traffic = _json.load(open(tf)).get(args.workload, {}).get(tname, {}).get(
+                'bytes_per_launch')
         except (OSError, ValueError):
             traffic = None
     roofline = {'bound': 'hbm', 'achieved': round(achieved, 1), 'peak': peak, 'unit': 'GB/s',
