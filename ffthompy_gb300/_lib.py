@@ -43,6 +43,7 @@ SIGNATURES = {
                                     ctypes.c_int, _vp]),
     'fhp_energy_matrix': (ctypes.c_int, [_vp, _vp, ctypes.c_int, _c_double_p, _vp]),
     'fhp_fourier_interp': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    'fhp_energy_gradient': (ctypes.c_int, [_vp, _vp, ctypes.c_int, _c_double_p, _vp, _vp]),
     'fhp_homogenize_host': (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _vp, ctypes.c_double,
                                            ctypes.c_int, _c_double_p, _c_int_p, _c_double_p, _vp,
                                            _vp]),

@@ -1,0 +1,83 @@
+"""Many independent cells on one GPU (ensembles of microstructures).
+
+homogenize_many() solves the GaNi cell problems of a list of coefficient
+fields of possibly different grids - the reference would run
+applications.scalar / elasticity (ffthompy/applications.py:11-90, 93-176) once
+per instance - and returns one A_H per instance.
+
+Each worker thread owns a CUDA stream and one GalerkinPlan per grid size it
+meets (plans keep their buffers, so nothing is allocated per instance after
+the first of a size).  The library's C calls release the GIL (ctypes), so the
+instances of different workers run concurrently on the GPU: small grids,
+whose launches alone would leave most SMs idle, fill the GPU together.  Each
+instance is solved with its own CG scalars and stopping test, exactly as a
+separate run would be.
+"""
+import threading
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+import torch
+
+from .engine import GalerkinPlan, coef_kind_of_torch, pack_coefficient_torch, require_cuda
+
+
+def homogenize_many(coefs, Y=None, physics='scalar', tol=1e-6, maxiter=1000,
+                    precision='f64', workers=8, primaldual=('primal',)):
+    """coefs: sequence of (dv, dv) + N coefficient arrays (numpy or torch),
+    origin-0 grid values as Material.get_A_GaNi returns them.  Returns a list
+    of {'primal': A_H (L x L numpy), 'kit': [...], 'status': [...]} (and
+    'dual', the inverted dual energy matrix, if requested) in input order."""
+    require_cuda()
+    device = torch.device('cuda', torch.cuda.current_device())
+    order = sorted(range(len(coefs)), key=lambda i: -int(np.prod(coefs[i].shape[2:])))
+    out = [None] * len(coefs)
+    local = threading.local()
+
+    def state():
+        if not hasattr(local, 'stream'):
+            local.stream = torch.cuda.Stream(device=device)
+            local.plans = {}
+        return local
+
+    def run(i):
+        st = state()
+        A = coefs[i]
+        N = tuple(int(n) for n in A.shape[2:])
+        d = len(N)
+        Yi = np.ones(d) if Y is None else np.asarray(Y, dtype=np.float64)
+        with torch.cuda.stream(st.stream):
+            key = (N, tuple(Yi))
+            plan = st.plans.get(key)
+            if plan is None:
+                plan = GalerkinPlan(N, Yi, physics=physics, precision=precision)
+                st.plans[key] = plan
+            At = torch.as_tensor(np.asarray(A, dtype=np.float64) if not isinstance(A, torch.Tensor)
+                                 else A).to(device, torch.float64, non_blocking=False)
+            res = {}
+            for pd in primaldual:
+                proj = 1 if pd == 'primal' else 2
+                Ap = At if pd == 'primal' else _inverse_field(At)
+                kind = coef_kind_of_torch(Ap)
+                plan.set_coefficient_packed(pack_coefficient_torch(Ap, kind), kind)
+                X, info = plan.cg(plan.rhs_macro(proj), tol=tol, maxiter=maxiter, proj=proj)
+                AH = plan.energy(X)
+                res[pd] = AH if pd == 'primal' else np.linalg.inv(AH)
+                res['kit_' + pd] = info['kit']
+                res['status_' + pd] = info['status']
+            st.stream.synchronize()
+        out[i] = res
+
+    with ThreadPoolExecutor(max_workers=max(1, int(workers))) as ex:
+        for f in [ex.submit(run, i) for i in order]:
+            f.result()
+    return out
+
+
+def _inverse_field(A):
+    """Per-voxel inverse of a (dv, dv) + N field (the dual coefficient,
+    ffthompy/materials.py get_A_GaNi with primaldual='dual')."""
+    dv = A.shape[0]
+    N = A.shape[2:]
+    M = A.reshape(dv, dv, -1).permute(2, 0, 1)
+    return torch.linalg.inv(M).permute(1, 2, 0).reshape((dv, dv) + tuple(N)).contiguous()

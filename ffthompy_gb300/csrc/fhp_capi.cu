@@ -303,6 +303,12 @@ int fhp_energy_matrix(fhp_plan plan, const void* X, int add_macro, double* AH, v
   return plan->eng->energy(X, add_macro, AH, as_stream(stream));
 }
 
+int fhp_energy_gradient(fhp_plan plan, const void* X, int add_macro, const double* W,
+                        double* grad, void* stream) {
+  if (!plan || !X || !W || !grad) return bad("plan, X, W and grad are required");
+  return plan->eng->energy_gradient(X, add_macro, W, grad, as_stream(stream));
+}
+
 int fhp_fourier_interp(fhp_plan src, fhp_plan dst, const void* x_src, void* x_dst,
                        void* stream) {
   if (!src || !dst || !x_src || !x_dst) return bad("plans and fields are required");

@@ -101,6 +101,9 @@ class EngineBase {
   virtual int cg_solve(int proj, const void* b, const void* x0, double tol, int maxiter, void* x,
                        SolveResult& res, int log_cap, cudaStream_t s) = 0;
   virtual int energy(const void* X, int add_macro, double* AH, cudaStream_t s) = 0;
+  // grad[c][v] = sum_ij W[i*L+j] dA_H[i][j]/dA_c(v) (W on host, grad FP64 device)
+  virtual int energy_gradient(const void* X, int add_macro, const double* W, double* grad,
+                              cudaStream_t s) = 0;
   // forward r2c spectrum of X (all comps) into `spec` (natural order, half spectrum)
   virtual int forward_spectrum(const void* x, void* spec, cudaStream_t s) = 0;
   // inverse of a half spectrum into x with scale

@@ -78,6 +78,7 @@ class Engine final : public EngineBase {
     g_.n2h = g_.n2 / 2 + 1;
     g_.dv = cfg_.physics == 0 ? d : cfg_.physics == 1 ? d * (d + 1) / 2 : cfg_.ncomp;
     g_.L = cfg_.nloads;
+    set_grid_divs(g_);
     if (cfg_.physics < 0 && (g_.dv < 1 || g_.dv > kMaxDv)) {
       set_error("ncomp must be in 1..6");
       return ST_BAD_ARG;
@@ -146,6 +147,7 @@ class Engine final : public EngineBase {
     gi_.n2 = cfg_.integ[d - 1];
     gi_.n2h = gi_.n2 / 2 + 1;
     gi_.M = (long long)gi_.n0 * gi_.n1 * gi_.n2;
+    set_grid_divs(gi_);
     if (gi_.n0 < g_.n0 || gi_.n1 < g_.n1 || gi_.n2 < g_.n2) {
       set_error("integration grid must not be smaller than the solve grid");
       return ST_BAD_ARG;
@@ -189,8 +191,13 @@ class Engine final : public EngineBase {
     const int dv = g_.dv;
     const int c = kind == COEF_ISO ? 1 : kind == COEF_SYM ? dv * (dv + 1) / 2 : dv * dv;
     const size_t n = (size_t)c * (band_ ? gi_.M : g_.M);
-    if (A_) { cudaFree(A_); A_ = nullptr; }
-    FHP_CHECK(cudaMalloc(&A_, n * sizeof(R)));
+    // keep the buffer when it is large enough: cudaFree synchronises the device,
+    // which would serialise plans working on other streams
+    if (A_ && A_elems_ < n) { cudaFree(A_); A_ = nullptr; }
+    if (!A_) {
+      FHP_CHECK(cudaMalloc(&A_, n * sizeof(R)));
+      A_elems_ = n;
+    }
     double* tmp = nullptr;
     const double* src = values;
     if (!on_device) {
@@ -367,6 +374,33 @@ class Engine final : public EngineBase {
     return ST_OK;
   }
 
+  int energy_gradient(const void* Xv, int add_macro, const double* W, double* grad,
+                      cudaStream_t s) override {
+    if (!A_) { set_error("coefficient not set"); return ST_BAD_ARG; }
+    if (band_) {
+      set_error("coefficient gradient needs the coefficient on the solve grid "
+                "(GaNi or full-grid plan), not on a band integration grid");
+      return ST_BAD_ARG;
+    }
+    LoadMat lm{};
+    for (int i = 0; i < g_.L * g_.L; ++i) lm.w[i] = W[i];
+    const R* X = static_cast<const R*>(Xv);
+    const double invM = 1.0 / (double)g_.M;
+    switch (coef_kind_) {
+      case COEF_ISO:
+        k_energy_grad<R, COEF_ISO><<<red_ctas_, 128, 0, s>>>(X, grad, g_, add_macro, lm, invM);
+        break;
+      case COEF_SYM:
+        k_energy_grad<R, COEF_SYM><<<red_ctas_, 128, 0, s>>>(X, grad, g_, add_macro, lm, invM);
+        break;
+      default:
+        k_energy_grad<R, COEF_FULL><<<red_ctas_, 128, 0, s>>>(X, grad, g_, add_macro, lm, invM);
+        break;
+    }
+    FHP_LAUNCHED();
+    return ST_OK;
+  }
+
   int forward_spectrum(const void* xv, void* spec, cudaStream_t s) override {
     cplx<R>* Sp = static_cast<cplx<R>*>(spec);
     int st = fwd_passes(COEF_NONE, false, static_cast<const R*>(xv), nullptr, nullptr, Sp,
@@ -502,7 +536,9 @@ class Engine final : public EngineBase {
     T = std::min(T, 32);
     T = (int)std::min<size_t>(T, std::max<size_t>(1, kSmemBudget / per));
     T = (int)std::min<long long>(T, inner);
-    return std::max(T, 1);
+    T = std::max(T, 1);
+    while (T & (T - 1)) T &= T - 1;  // kernels index tiles with shifts: a power of two
+    return T;
   }
 
   int make_line(int n, DevLine<R>& out) {
@@ -530,7 +566,15 @@ class Engine final : public EngineBase {
     L.ld = padded_ld(h.nf);
     L.blue = h.blue;
     L.nst = h.nst;
-    for (int i = 0; i < kMaxStages; ++i) L.rad[i] = i < h.nst ? h.rad[i] : 1;
+    int ns = h.nf;
+    for (int i = 0; i < kMaxStages; ++i) {
+      L.rad[i] = i < h.nst ? h.rad[i] : 1;
+      L.dnbl[i] = make_fastdiv((unsigned)(h.nf / L.rad[i]));
+      L.dms[i] = make_fastdiv((unsigned)std::max(1, ns / L.rad[i]));
+      if (i < h.nst) ns /= h.rad[i];
+    }
+    L.dn = make_fastdiv((unsigned)h.n);
+    L.dnf = make_fastdiv((unsigned)h.nf);
     L.tw = dc;
     L.chirp = nch ? dc + ntw : nullptr;
     L.bhat = nbh ? dc + ntw + nch : nullptr;
@@ -550,15 +594,18 @@ class Engine final : public EngineBase {
     FHP_ATTR((k_r2c_last<R, COEF_FULL, true>));
     FHP_ATTR((k_c2c_axis<R, false>));
     FHP_ATTR((k_c2c_axis<R, true>));
-    FHP_ATTR((k_proj_first<R>));
+    FHP_ATTR((k_proj_first<R, 0>));
+    FHP_ATTR((k_proj_first<R, 1>));
     FHP_ATTR((k_c2r_last<R, false>));
     FHP_ATTR((k_c2r_last<R, true>));
     FHP_ATTR((k_r2c_last<R, COEF_NONE, true>));
-    FHP_ATTR((k_band_axis<R, BAND_UP>));
-    FHP_ATTR((k_band_axis<R, BAND_DOWN>));
-    FHP_ATTR((k_band_axis<R, BAND_DOWN_PROJ>));
-    FHP_ATTR((k_band_axis<R, BAND_UP_PROJ>));
-    FHP_ATTR((k_band_axis<R, BAND_PAD>));
+    FHP_ATTR((k_band_axis<R, BAND_UP, 0>));
+    FHP_ATTR((k_band_axis<R, BAND_DOWN, 0>));
+    FHP_ATTR((k_band_axis<R, BAND_DOWN_PROJ, 0>));
+    FHP_ATTR((k_band_axis<R, BAND_UP_PROJ, 0>));
+    FHP_ATTR((k_band_axis<R, BAND_DOWN_PROJ, 1>));
+    FHP_ATTR((k_band_axis<R, BAND_UP_PROJ, 1>));
+    FHP_ATTR((k_band_axis<R, BAND_PAD, 0>));
     FHP_ATTR((k_band_last<R, COEF_ISO>));
     FHP_ATTR((k_band_last<R, COEF_SYM>));
     FHP_ATTR((k_band_last<R, COEF_FULL>));
@@ -665,7 +712,8 @@ class Engine final : public EngineBase {
     dim3 grid((unsigned)((inner + Tp_ - 1) / Tp_), (unsigned)g_.L);
     const size_t smem = (size_t)Tp_ * g_.dv * lp.ld * sizeof(cplx<R>);
     const int pk = pbeg("proj_axis0", 2.0 * spec_bytes(), s);
-    k_proj_first<R><<<grid, kThreads, smem, s>>>(Sp, g_, d == 3 ? g_.n0 : g_.n1, inner, lp, Tp_,
+    auto kproj = gp_.physics == 0 ? k_proj_first<R, 0> : k_proj_first<R, 1>;
+    kproj<<<grid, kThreads, smem, s>>>(Sp, g_, d == 3 ? g_.n0 : g_.n1, inner, lp, Tp_,
                                                  gp_, cg ? all_done_ : nullptr,
                                                  cg ? st_ : nullptr);
     pend(pk, s);
@@ -674,9 +722,11 @@ class Engine final : public EngineBase {
   }
 
   // ---- band representation (Ga on the solve grid, A on the integration grid) ----
-  int band_axis(int mode, const cplx<R>* in, cplx<R>* out, const BandAxis& ax,
+  int band_axis(int mode, const cplx<R>* in, cplx<R>* out, const BandAxis& ax_in,
                 const LineDev<R>& L1, const LineDev<R>& L2, bool cg, cudaStream_t s,
                 const char* name) {
+    BandAxis ax = ax_in;
+    set_band_divs(ax);
     const bool projm = mode == BAND_DOWN_PROJ || mode == BAND_UP_PROJ;
     const int nlc = projm ? g_.dv : 1;
     const int nf = (mode == BAND_PAD ? 0 : L1.ld) + (mode == BAND_DOWN ? 0 : L2.ld);
@@ -693,23 +743,28 @@ class Engine final : public EngineBase {
     // the output projection carries s / prod(B)
     GreenParams gpin = gp_;
     gpin.scale = 1.0;
+    const bool scalar = gp_.physics == 0;
     const int pk = pbeg(name, bytes, s);
     switch (mode) {
       case BAND_UP:
-        k_band_axis<R, BAND_UP><<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st);
+        k_band_axis<R, BAND_UP, 0><<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st);
         break;
       case BAND_DOWN:
-        k_band_axis<R, BAND_DOWN><<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st);
+        k_band_axis<R, BAND_DOWN, 0><<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st);
         break;
-      case BAND_UP_PROJ:
-        k_band_axis<R, BAND_UP_PROJ><<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gpin, ad, st);
+      case BAND_UP_PROJ: {
+        auto k = scalar ? k_band_axis<R, BAND_UP_PROJ, 0> : k_band_axis<R, BAND_UP_PROJ, 1>;
+        k<<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gpin, ad, st);
         break;
+      }
       case BAND_PAD:
-        k_band_axis<R, BAND_PAD><<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st);
+        k_band_axis<R, BAND_PAD, 0><<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st);
         break;
-      default:
-        k_band_axis<R, BAND_DOWN_PROJ><<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st);
+      default: {
+        auto k = scalar ? k_band_axis<R, BAND_DOWN_PROJ, 0> : k_band_axis<R, BAND_DOWN_PROJ, 1>;
+        k<<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st);
         break;
+      }
     }
     pend(pk, s);
     FHP_LAUNCHED();
@@ -884,6 +939,7 @@ class Engine final : public EngineBase {
   }
 
   R* x_cur_ = nullptr;  // the caller's solution buffer during cg_solve
+  size_t A_elems_ = 0;   // capacity of A_ in elements
   // band representation
   bool band_ = false;
   GridDims gi_{};

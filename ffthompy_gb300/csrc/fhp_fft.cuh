@@ -1,12 +1,13 @@
 // Shared-memory line FFTs for the Fourier-Galerkin operator (sm_103a).
 //
 // A "line" is one 1D transform of logical length n held in shared memory.
-//  * direct lines: n factors into radices {2,3,4,5,8,16} and odd primes <= 31;
+//  * direct lines: n factors into radices {2,4,8,16} and the odd primes
+//    3, 5, 7, 11, 13, 17;
 //    forward = in-place decimation-in-frequency (natural in, digit-reversed
 //    out), inverse = in-place decimation-in-time (digit-reversed in, natural
 //    out).  No ping-pong buffer is needed: every butterfly reads and writes
 //    the same r slots.
-//  * Bluestein lines: n has a prime factor > 31 (89, 127, 509, 1021, 73 ...);
+//  * Bluestein lines: n has a prime factor > 17 (19, 89, 127, 509, 1021 ...);
 //    the DFT is a chirp convolution of smooth length m >= 2n-1 done with the
 //    direct machinery (DIF, pointwise product with the filter spectrum stored
 //    in digit-reversed order, DIT).
@@ -50,7 +51,33 @@ __device__ __forceinline__ cplx<R> cmul_mi(cplx<R> a) { return mkc<R>(a.y, -a.x)
 template <typename R>
 __device__ __forceinline__ cplx<R> cmul_pi(cplx<R> a) { return mkc<R>(-a.y, a.x); }
 
-constexpr int kMaxStages = 24;
+constexpr int kMaxStages = 16;
+
+// Division by a run-time invariant d as a multiply-high and two shifts
+// (Granlund & Montgomery, "Division by invariant integers using
+// multiplication", PLDI 1994, round-up variant): exact for every 32-bit x.
+struct FastDiv {
+  unsigned m;
+  unsigned char s1, s2;
+  unsigned short pad;
+};
+inline FastDiv make_fastdiv(unsigned d) {
+  FastDiv f{};
+  int l = 0;
+  while ((1ull << l) < d) ++l;
+  f.m = (unsigned)(((1ull << 32) * ((1ull << l) - d)) / d + 1);
+  f.s1 = (unsigned char)(l < 1 ? l : 1);
+  f.s2 = (unsigned char)(l > 1 ? l - 1 : 0);
+  return f;
+}
+__host__ __device__ __forceinline__ int fdiv(int x, FastDiv f) {
+#ifdef __CUDA_ARCH__
+  const unsigned t = __umulhi((unsigned)x, f.m);
+#else
+  const unsigned t = (unsigned)(((unsigned long long)(unsigned)x * f.m) >> 32);
+#endif
+  return (int)((t + (((unsigned)x - t) >> f.s1)) >> f.s2);
+}
 
 // Padded shared-memory slot of line element i: one spare slot per 32 elements
 // breaks the power-of-two strides of the late radix stages across banks.
@@ -66,6 +93,9 @@ struct LineDev {
   int blue;     // 1: Bluestein
   int nst;      // number of radix stages of the core
   int rad[kMaxStages];
+  FastDiv dnbl[kMaxStages];  // stage s: division by nf / rad[s] (butterflies per line)
+  FastDiv dms[kMaxStages];   // stage s: division by the butterfly span ms_s
+  FastDiv dn, dnf;           // division by n, nf
   const cplx<R>* tw;     // nf entries, W_nf^k = exp(-2 pi i k / nf)
   const cplx<R>* chirp;  // n entries, exp(-i pi j^2 / n)      (Bluestein)
   const cplx<R>* bhat;   // nf entries, filter spectrum / nf, digit-reversed (Bluestein)
@@ -240,67 +270,105 @@ __device__ __forceinline__ void dft_fwd(cplx<R>* v, const cplx<R>* __restrict__ 
 template <typename R, int RAD, bool INV>
 __device__ __forceinline__ void stage_run(cplx<R>* __restrict__ buf, int ld, int nlines, int nf,
                                           int ns, const cplx<R>* __restrict__ tw, int tid,
-                                          int nthr) {
+                                          int nthr, FastDiv dnbl, FastDiv dms) {
   const int ms = ns / RAD;
   const int nbl = nf / RAD;
-  const int total = nlines * nbl;
   const int tws = nf / ns;
-  for (int b = tid; b < total; b += nthr) {
-    const int line = b / nbl;
-    const int bb = b - line * nbl;
-    const int g = bb / ms;
+  if constexpr (RAD > 8 && RAD != 16) {
+    // odd radices above 8: one (line, butterfly) pair per step, nothing kept
+    // across lines (their slot offsets would not fit the register budget)
+    const int total = nlines * nbl;
+    for (int b = tid; b < total; b += nthr) {
+      const int line = fdiv(b, dnbl);
+      const int bb = b - line * nbl;
+      const int g = fdiv(bb, dms);
+      const int j1 = bb - g * ms;
+      cplx<R>* lp = buf + line * ld;
+      const int base = g * ns + j1;
+      cplx<R> v[RAD];
+      if constexpr (!INV) {
+#pragma unroll
+        for (int q = 0; q < RAD; ++q) v[q] = lp[sp(base + q * ms)];
+        dft_fwd<R, RAD>(v, tw, nf);
+        lp[sp(base)] = v[0];
+#pragma unroll
+        for (int q = 1; q < RAD; ++q) lp[sp(base + q * ms)] = cmul<R>(v[q], tw[j1 * q * tws]);
+      } else {
+        v[0] = cconj<R>(lp[sp(base)]);
+#pragma unroll
+        for (int q = 1; q < RAD; ++q)
+          v[q] = cconj<R>(cmulc<R>(lp[sp(base + q * ms)], tw[j1 * q * tws]));
+        dft_fwd<R, RAD>(v, tw, nf);
+#pragma unroll
+        for (int q = 0; q < RAD; ++q) lp[sp(base + q * ms)] = cconj<R>(v[q]);
+      }
+    }
+    return;
+  }
+  // Butterfly-stationary: a thread keeps one butterfly position (its slots
+  // and twiddles) and runs it over a strided subset of the lines, so the index
+  // arithmetic and twiddle loads are paid once per stage, not once per line.
+  int bb0 = tid, bstep = nthr, l0 = 0, lstep = 1;
+  if (nbl < nthr) {
+    lstep = fdiv(nthr, dnbl);  // groups of nbl threads
+    l0 = fdiv(tid, dnbl);
+    bb0 = tid - l0 * nbl;
+    bstep = nbl;
+    if (l0 >= lstep) return;
+  }
+  constexpr bool kCacheTw = RAD <= 8;  // registers: larger radices reload per line
+  for (int bb = bb0; bb < nbl; bb += bstep) {
+    const int g = fdiv(bb, dms);
     const int j1 = bb - g * ms;
-    cplx<R>* lp = buf + line * ld;
     const int base = g * ns + j1;
-    cplx<R> v[RAD];
-    if constexpr (!INV) {
+    cplx<R> w[RAD];
+    if constexpr (kCacheTw) {
 #pragma unroll
-      for (int q = 0; q < RAD; ++q) v[q] = lp[sp(base + q * ms)];
-      dft_fwd<R, RAD>(v, tw, nf);
-      lp[sp(base)] = v[0];
+      for (int q = 1; q < RAD; ++q) w[q] = tw[j1 * q * tws];
+    }
+    for (int line = l0; line < nlines; line += lstep) {
+      cplx<R>* lp = buf + line * ld;
+      cplx<R> v[RAD];
+      if constexpr (!INV) {
 #pragma unroll
-      for (int q = 1; q < RAD; ++q) lp[sp(base + q * ms)] = cmul<R>(v[q], tw[j1 * q * tws]);
-    } else {
-      v[0] = cconj<R>(lp[sp(base)]);
+        for (int q = 0; q < RAD; ++q) v[q] = lp[sp(base + q * ms)];
+        dft_fwd<R, RAD>(v, tw, nf);
+        lp[sp(base)] = v[0];
 #pragma unroll
-      for (int q = 1; q < RAD; ++q)
-        v[q] = cconj<R>(cmulc<R>(lp[sp(base + q * ms)], tw[j1 * q * tws]));
-      dft_fwd<R, RAD>(v, tw, nf);
+        for (int q = 1; q < RAD; ++q)
+          lp[sp(base + q * ms)] = cmul<R>(v[q], kCacheTw ? w[q] : tw[j1 * q * tws]);
+      } else {
+        v[0] = cconj<R>(lp[sp(base)]);
 #pragma unroll
-      for (int q = 0; q < RAD; ++q) lp[sp(base + q * ms)] = cconj<R>(v[q]);
+        for (int q = 1; q < RAD; ++q)
+          v[q] = cconj<R>(cmulc<R>(lp[sp(base + q * ms)], kCacheTw ? w[q] : tw[j1 * q * tws]));
+        dft_fwd<R, RAD>(v, tw, nf);
+#pragma unroll
+        for (int q = 0; q < RAD; ++q) lp[sp(base + q * ms)] = cconj<R>(v[q]);
+      }
     }
   }
 }
 
-// Radix dispatch, split so that the large odd radices (register hungry, rare)
-// do not set the register budget of the common power-of-two / 3 / 5 stages.
-template <typename R, bool INV>
-__device__ __noinline__ void stage_dispatch_rare(cplx<R>* buf, int ld, int nlines, int nf, int ns,
-                                                 int rad, const cplx<R>* tw, int tid, int nthr) {
-  switch (rad) {
-    case 7: stage_run<R, 7, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
-    case 11: stage_run<R, 11, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
-    case 13: stage_run<R, 13, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
-    case 19: stage_run<R, 19, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
-    case 23: stage_run<R, 23, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
-    case 29: stage_run<R, 29, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
-    case 31: stage_run<R, 31, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
-    default: break;  // plans only contain the radices of factor_radices
-  }
-}
-
+// Radix dispatch, inlined into every FFT kernel (no call, so no call-frame
+// registers or stack).  Lengths with a prime factor above 17 go through
+// Bluestein (build_line_plan), so these are all the radices a plan can hold.
 template <typename R, bool INV>
 __device__ __forceinline__ void stage_dispatch(cplx<R>* buf, int ld, int nlines, int nf, int ns,
-                                               int rad, const cplx<R>* tw, int tid, int nthr) {
+                                               int rad, const cplx<R>* tw, int tid, int nthr,
+                                               FastDiv dnbl, FastDiv dms) {
   switch (rad) {
-    case 2: stage_run<R, 2, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
-    case 3: stage_run<R, 3, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
-    case 4: stage_run<R, 4, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
-    case 5: stage_run<R, 5, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
-    case 8: stage_run<R, 8, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
-    case 16: stage_run<R, 16, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
-    case 17: stage_run<R, 17, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr); break;
-    default: stage_dispatch_rare<R, INV>(buf, ld, nlines, nf, ns, rad, tw, tid, nthr); break;
+    case 2: stage_run<R, 2, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr, dnbl, dms); break;
+    case 3: stage_run<R, 3, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr, dnbl, dms); break;
+    case 4: stage_run<R, 4, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr, dnbl, dms); break;
+    case 5: stage_run<R, 5, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr, dnbl, dms); break;
+    case 7: stage_run<R, 7, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr, dnbl, dms); break;
+    case 8: stage_run<R, 8, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr, dnbl, dms); break;
+    case 11: stage_run<R, 11, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr, dnbl, dms); break;
+    case 13: stage_run<R, 13, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr, dnbl, dms); break;
+    case 16: stage_run<R, 16, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr, dnbl, dms); break;
+    case 17: stage_run<R, 17, INV>(buf, ld, nlines, nf, ns, tw, tid, nthr, dnbl, dms); break;
+    default: break;  // plans only contain the radices of factor_radices
   }
 }
 
@@ -317,7 +385,8 @@ __device__ void line_core(cplx<R>* buf, int ld, int nlines, const LineDev<R>& L,
   if (do_fwd) {
     int ns = L.nf;
     for (int s = 0; s < L.nst; ++s) {
-      stage_dispatch<R, false>(buf, ld, nlines, L.nf, ns, L.rad[s], L.tw, tid, nthr);
+      stage_dispatch<R, false>(buf, ld, nlines, L.nf, ns, L.rad[s], L.tw, tid, nthr, L.dnbl[s],
+                               L.dms[s]);
       ns /= L.rad[s];
       __syncthreads();
     }
@@ -325,7 +394,7 @@ __device__ void line_core(cplx<R>* buf, int ld, int nlines, const LineDev<R>& L,
   if (L.blue) {
     const int tot = nlines * L.nf;
     for (int e = tid; e < tot; e += nthr) {
-      const int line = e / L.nf, j = e - line * L.nf;
+      const int line = fdiv(e, L.dnf), j = e - line * L.nf;
       cplx<R>* p = buf + line * ld + sp(j);
       *p = cmul<R>(*p, L.bhat[j]);
     }
@@ -336,7 +405,8 @@ __device__ void line_core(cplx<R>* buf, int ld, int nlines, const LineDev<R>& L,
     int ns = 1;
     for (int s = L.nst - 1; s >= 0; --s) {
       ns *= L.rad[s];
-      stage_dispatch<R, true>(buf, ld, nlines, L.nf, ns, L.rad[s], L.tw, tid, nthr);
+      stage_dispatch<R, true>(buf, ld, nlines, L.nf, ns, L.rad[s], L.tw, tid, nthr, L.dnbl[s],
+                              L.dms[s]);
       __syncthreads();
     }
   }
@@ -368,12 +438,9 @@ __device__ __forceinline__ cplx<R> get_inv(const cplx<R>* line, const LineDev<R>
 template <typename R>
 __device__ __forceinline__ void zero_tail(cplx<R>* buf, int ld, int nlines, const LineDev<R>& L) {
   if (!L.blue) return;
-  const int w = L.nf - L.n;
-  const int tot = nlines * w;
-  for (int e = threadIdx.x; e < tot; e += blockDim.x) {
-    const int line = e / w, j = L.n + (e - line * w);
-    buf[line * ld + sp(j)] = mkc<R>(R(0), R(0));
-  }
+  const int lane = threadIdx.x & 31;
+  for (int line = threadIdx.x >> 5; line < nlines; line += blockDim.x >> 5)
+    for (int j = L.n + lane; j < L.nf; j += 32) buf[line * ld + sp(j)] = mkc<R>(R(0), R(0));
 }
 
 }  // namespace fhp

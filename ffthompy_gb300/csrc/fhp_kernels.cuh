@@ -37,7 +37,22 @@ struct GridDims {
   int dv;         // components per load
   int L;          // loads
   long long M;    // voxels
+  FastDiv dn2, dn2h, dnp;  // division by n2, n2h and the pair-line count (L*dv+1)/2
 };
+
+inline void set_grid_divs(GridDims& g) {
+  g.dn2 = make_fastdiv((unsigned)g.n2);
+  g.dn2h = make_fastdiv((unsigned)g.n2h);
+  g.dnp = make_fastdiv((unsigned)((g.L * g.dv + 1) / 2));
+}
+
+// FFT pass kernels: two CTAs per SM (128 registers) for FP32; FP64 values take
+// two registers each, so the FP64 instantiations keep one CTA per SM and the
+// full register file instead of spilling.
+template <typename R> constexpr int kFftMinBlocks = sizeof(R) == 4 ? 2 : 1;
+
+constexpr int kMaxDv = 6;
+constexpr int kMaxLoads = 6;
 
 // Green projection parameters (ffthompy/projections.py:9-267)
 struct GreenParams {
@@ -67,87 +82,120 @@ __device__ __forceinline__ void mandel_pair(int dim, int I, int& a, int& b) {
 // y = G(xi) x for one frequency, G from the closed forms:
 //   scalar:     G1 = xi xi^T / |xi|^2,           G2 = I - G1
 //   elasticity: G1 e = sym(n (x) e n)*2 - n n (n.e.n), Mandel-weighted, G2 = I - G1
-// zero at k = 0 and outside the band; times scale.
-template <typename R>
-__device__ __forceinline__ void green_apply(const GreenParams& gp, int dim, const int* k,
-                                            cplx<R>* x /* in/out, dv values */) {
+// zero at k = 0 and outside the band; times scale.  DIM is a template
+// parameter so every small array is indexed by constants (registers).
+template <typename R, int DIM, int PHYS>
+__device__ __forceinline__ void green_apply_d(const GreenParams& gp, const int* k,
+                                              cplx<R>* x /* in/out, dv values */) {
+  constexpr int DVE = PHYS == 0 ? DIM : DIM * (DIM + 1) / 2;
   bool inband = true, zero = true;
-  R xi[3] = {R(0), R(0), R(0)};
-  for (int i = 0; i < dim; ++i) {
+  R xi[DIM];
+#pragma unroll
+  for (int i = 0; i < DIM; ++i) {
     const int ki = k[i];
     if (ki > gp.h[i] || -ki > gp.h[i]) inband = false;
     if (ki != 0) zero = false;
     xi[i] = R(ki) / R(gp.Y[i]);
   }
-  const int dv = gp.physics == 0 ? dim : dim * (dim + 1) / 2;
+  constexpr bool scalar = PHYS == 0;
   const R s = R(gp.scale);
   if (gp.proj == 0) {  // no projection (energies): scale only
-    for (int c = 0; c < dv; ++c) x[c] = cscale<R>(x[c], s);
+#pragma unroll
+    for (int c = 0; c < DVE; ++c)
+      if (!scalar || c < DIM) x[c] = cscale<R>(x[c], s);
     return;
   }
   if (!inband || zero) {
-    for (int c = 0; c < dv; ++c) x[c] = mkc<R>(R(0), R(0));
+#pragma unroll
+    for (int c = 0; c < DVE; ++c)
+      if (!scalar || c < DIM) x[c] = mkc<R>(R(0), R(0));
     return;
   }
   R nn = R(0);
-  for (int i = 0; i < dim; ++i) nn += xi[i] * xi[i];
-  if (gp.physics == 0) {
+#pragma unroll
+  for (int i = 0; i < DIM; ++i) nn += xi[i] * xi[i];
+  if constexpr (scalar) {
     // (xi . x) / |xi|^2
     cplx<R> t = mkc<R>(R(0), R(0));
-    for (int i = 0; i < dim; ++i) { t.x += xi[i] * x[i].x; t.y += xi[i] * x[i].y; }
+#pragma unroll
+    for (int i = 0; i < DIM; ++i) { t.x += xi[i] * x[i].x; t.y += xi[i] * x[i].y; }
     t.x /= nn; t.y /= nn;
-    for (int i = 0; i < dim; ++i) {
+#pragma unroll
+    for (int i = 0; i < DIM; ++i) {
       cplx<R> g1 = mkc<R>(xi[i] * t.x, xi[i] * t.y);
       x[i] = (gp.proj == 1) ? cscale<R>(g1, s) : cscale<R>(csub<R>(x[i], g1), s);
     }
     return;
-  }
+  } else {
   // elasticity: unit normal, strain tensor from Mandel vector
   const R inv = R(1) / sqrt(nn);
-  R n[3];
-  for (int i = 0; i < 3; ++i) n[i] = (i < dim) ? xi[i] * inv : R(0);
+  R n[DIM];
+#pragma unroll
+  for (int i = 0; i < DIM; ++i) n[i] = xi[i] * inv;
   const R isq2 = R(0.70710678118654752440084436210485);
-  cplx<R> e[3][3];
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) e[i][j] = mkc<R>(R(0), R(0));
-  for (int I = 0; I < dv; ++I) {
+  cplx<R> e[DIM][DIM];
+#pragma unroll
+  for (int I = 0; I < DVE; ++I) {
     int a, b;
-    mandel_pair(dim, I, a, b);
+    mandel_pair(DIM, I, a, b);
     if (a == b) e[a][a] = x[I];
     else { e[a][b] = cscale<R>(x[I], isq2); e[b][a] = e[a][b]; }
   }
-  cplx<R> en[3];
-  for (int i = 0; i < dim; ++i) {
+  cplx<R> en[DIM];
+#pragma unroll
+  for (int i = 0; i < DIM; ++i) {
     en[i] = mkc<R>(R(0), R(0));
-    for (int j = 0; j < dim; ++j) { en[i].x += e[i][j].x * n[j]; en[i].y += e[i][j].y * n[j]; }
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) { en[i].x += e[i][j].x * n[j]; en[i].y += e[i][j].y * n[j]; }
   }
   cplx<R> nen = mkc<R>(R(0), R(0));
-  for (int i = 0; i < dim; ++i) { nen.x += n[i] * en[i].x; nen.y += n[i] * en[i].y; }
+#pragma unroll
+  for (int i = 0; i < DIM; ++i) { nen.x += n[i] * en[i].x; nen.y += n[i] * en[i].y; }
   const R sq2 = R(1.4142135623730950488016887242097);
-  for (int I = 0; I < dv; ++I) {
+#pragma unroll
+  for (int I = 0; I < DVE; ++I) {
     int a, b;
-    mandel_pair(dim, I, a, b);
+    mandel_pair(DIM, I, a, b);
     // (G1 e)_ab = n_a (e n)_b + n_b (e n)_a - n_a n_b (n.e.n)
     cplx<R> g = mkc<R>(n[a] * en[b].x + n[b] * en[a].x - n[a] * n[b] * nen.x,
                        n[a] * en[b].y + n[b] * en[a].y - n[a] * n[b] * nen.y);
     if (a != b) g = cscale<R>(g, sq2);
     x[I] = (gp.proj == 1) ? cscale<R>(g, s) : cscale<R>(csub<R>(x[I], g), s);
   }
+  }
+}
+
+// PHYS is a template parameter of the kernels that call this, so a scalar
+// plan's kernels carry no elasticity code (and its register demand).
+template <typename R, int PHYS>
+__device__ __forceinline__ void green_apply(const GreenParams& gp, int dim, const int* k,
+                                            cplx<R>* x /* in/out, dv values */) {
+  if (dim == 3) green_apply_d<R, 3, PHYS>(gp, k, x);
+  else green_apply_d<R, 2, PHYS>(gp, k, x);
 }
 
 // q = A(v) x for one voxel and one load; A component-major with stride M.
+// Loops run to kMaxDv with a guard so x and q stay in registers.
 template <typename R, int COEF>
 __device__ __forceinline__ void coef_apply(const R* __restrict__ A, long long M, long long v,
                                            int dv, const R* x, R* q) {
   if constexpr (COEF == COEF_NONE) {
-    for (int c = 0; c < dv; ++c) q[c] = x[c];
+#pragma unroll
+    for (int c = 0; c < kMaxDv; ++c)
+      if (c < dv) q[c] = x[c];
   } else if constexpr (COEF == COEF_ISO) {
     const R a = A[v];
-    for (int c = 0; c < dv; ++c) q[c] = a * x[c];
+#pragma unroll
+    for (int c = 0; c < kMaxDv; ++c)
+      if (c < dv) q[c] = a * x[c];
   } else if constexpr (COEF == COEF_SYM) {
-    for (int a = 0; a < dv; ++a) {
+#pragma unroll
+    for (int a = 0; a < kMaxDv; ++a) {
+      if (a >= dv) break;
       R s = R(0);
-      for (int b = 0; b < dv; ++b) {
+#pragma unroll
+      for (int b = 0; b < kMaxDv; ++b) {
+        if (b >= dv) break;
         const int i = a < b ? a : b, j = a < b ? b : a;
         const int t = i * dv - i * (i - 1) / 2 + (j - i);
         s += A[(long long)t * M + v] * x[b];
@@ -155,16 +203,19 @@ __device__ __forceinline__ void coef_apply(const R* __restrict__ A, long long M,
       q[a] = s;
     }
   } else {
-    for (int a = 0; a < dv; ++a) {
+#pragma unroll
+    for (int a = 0; a < kMaxDv; ++a) {
+      if (a >= dv) break;
       R s = R(0);
-      for (int b = 0; b < dv; ++b) s += A[(long long)(a * dv + b) * M + v] * x[b];
+#pragma unroll
+      for (int b = 0; b < kMaxDv; ++b) {
+        if (b >= dv) break;
+        s += A[(long long)(a * dv + b) * M + v] * x[b];
+      }
       q[a] = s;
     }
   }
 }
-
-constexpr int kMaxDv = 6;
-constexpr int kMaxLoads = 6;
 
 // ---------------------------------------------------------------------------
 // block reductions (double)
@@ -175,11 +226,15 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-// Reduces acc[0..n) over the block; thread 0 writes out[0..n).  red must hold
-// (blockDim/32)*n doubles.
-__device__ __forceinline__ void block_sum_n(double* acc, int n, double* red, double* out) {
+// Reduces acc[0..n) over the block; threads i < n write out[i].  red must hold
+// (blockDim/32)*n doubles.  The loop runs to the array size with a guard so
+// acc stays in registers.
+template <int NMAX>
+__device__ __forceinline__ void block_sum_n(double (&acc)[NMAX], int n, double* red, double* out) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int i = 0; i < n; ++i) {
+#pragma unroll
+  for (int i = 0; i < NMAX; ++i) {
+    if (i >= n) break;
     double v = warp_sum(acc[i]);
     if (lane == 0) red[w * n + i] = v;
   }
@@ -197,9 +252,9 @@ __device__ __forceinline__ void block_sum_n(double* acc, int n, double* red, dou
 // CTA: `rows` consecutive (i0,i1) rows, all comps; comps paired as z = a + i b.
 // ---------------------------------------------------------------------------
 template <typename R, int COEF, bool PUPD>
-__global__ void __launch_bounds__(256, 2) k_r2c_last(
+__global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_r2c_last(
     const R* xin, R* pio, const R* __restrict__ rvec,
-    const R* __restrict__ A, cplx<R>* __restrict__ S, GridDims g, LineDev<R> L, int rows,
+    const R* __restrict__ A, cplx<R>* __restrict__ S, const __grid_constant__ GridDims g, const __grid_constant__ LineDev<R> L, int rows,
     const LoadState* __restrict__ st, const int* __restrict__ all_done) {
   if (all_done && *all_done) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -212,7 +267,7 @@ __global__ void __launch_bounds__(256, 2) k_r2c_last(
   const int n = g.n2;
   const int tasks = rows * n;
   for (int e = threadIdx.x; e < tasks; e += blockDim.x) {
-    const int rl = e / n, j = e - rl * n;
+    const int rl = fdiv(e, g.dn2), j = e - rl * n;
     const long long row = row0 + rl;
     cplx<R>* base = buf + (long long)rl * np * ld;
     if (row >= nrows) {
@@ -222,18 +277,23 @@ __global__ void __launch_bounds__(256, 2) k_r2c_last(
     const long long v = row * n + j;
     for (int l = 0; l < g.L; ++l) {
       R xv[kMaxDv], q[kMaxDv];
-      for (int c = 0; c < g.dv; ++c) {
+      const R bet = PUPD ? R(st[l].beta) : R(0);
+      const bool wr = PUPD && !st[l].done;
+#pragma unroll
+      for (int c = 0; c < kMaxDv; ++c) {
+        if (c >= g.dv) break;
         const long long idx = (long long)(l * g.dv + c) * g.M + v;
         R val = PUPD ? pio[idx] : xin[idx];
         if constexpr (PUPD) {
-          const R bet = R(st[l].beta);
           val = rvec[idx] + bet * val;
-          if (!st[l].done) pio[idx] = val;
+          if (wr) pio[idx] = val;
         }
         xv[c] = val;
       }
       coef_apply<R, COEF>(A, g.M, v, g.dv, xv, q);
-      for (int c = 0; c < g.dv; ++c) {
+#pragma unroll
+      for (int c = 0; c < kMaxDv; ++c) {
+        if (c >= g.dv) break;
         const int comp = l * g.dv + c;
         cplx<R>* line = base + (comp >> 1) * ld;
         // slot j of the pair line: real part from even comp, imag from odd
@@ -247,7 +307,7 @@ __global__ void __launch_bounds__(256, 2) k_r2c_last(
   if (L.blue) {
     // chirp pre-multiply of the stored values (put_fwd for Bluestein lines)
     for (int e = threadIdx.x; e < rows * np * n; e += blockDim.x) {
-      const int line = e / n, j = e - line * n;
+      const int line = fdiv(e, g.dn2), j = e - line * n;
       cplx<R>* p = buf + (long long)line * ld + sp(j);
       *p = cmul<R>(*p, L.chirp[j]);
     }
@@ -259,8 +319,8 @@ __global__ void __launch_bounds__(256, 2) k_r2c_last(
   const int n2h = g.n2h;
   const int otasks = rows * np * n2h;
   for (int e = threadIdx.x; e < otasks; e += blockDim.x) {
-    const int line = e / n2h, k = e - line * n2h;
-    const int rl = line / np, p = line - rl * np;
+    const int line = fdiv(e, g.dn2h), k = e - line * n2h;
+    const int rl = fdiv(line, g.dnp), p = line - rl * np;
     const long long row = row0 + rl;
     if (row >= nrows) continue;
     const cplx<R>* lp = buf + (long long)line * ld;
@@ -279,8 +339,8 @@ __global__ void __launch_bounds__(256, 2) k_r2c_last(
 // elements after it; CTA = tile of T inner columns of one outer index.
 // ---------------------------------------------------------------------------
 template <typename R, bool INV>
-__global__ void __launch_bounds__(256, 2) k_c2c_axis(cplx<R>* __restrict__ S, int na, long long inner,
-                                                  LineDev<R> L, int T,
+__global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_c2c_axis(cplx<R>* __restrict__ S, int na, long long inner,
+                                                  const __grid_constant__ LineDev<R> L, int T,
                                                   const int* __restrict__ all_done,
                                                   const LoadState* __restrict__ st,
                                                   int outer_per_load) {
@@ -292,8 +352,9 @@ __global__ void __launch_bounds__(256, 2) k_c2c_axis(cplx<R>* __restrict__ S, in
   const long long t0 = (long long)blockIdx.x * T;
   cplx<R>* base = S + (long long)blockIdx.y * na * inner;
   const int tasks = T * na;
+  const int lgT = __ffs(T) - 1;  // T is a power of two
   for (int e = threadIdx.x; e < tasks; e += blockDim.x) {
-    const int i = e / T, t = e - i * T;
+    const int i = e >> lgT, t = e & (T - 1);
     const long long col = t0 + t;
     const cplx<R> v = (col < inner) ? base[(long long)i * inner + col] : mkc<R>(R(0), R(0));
     if (INV) put_inv<R>(buf + t * ld, L, i, v);
@@ -303,7 +364,7 @@ __global__ void __launch_bounds__(256, 2) k_c2c_axis(cplx<R>* __restrict__ S, in
   __syncthreads();
   line_core<R>(buf, ld, T, L, INV);
   for (int e = threadIdx.x; e < tasks; e += blockDim.x) {
-    const int i = e / T, t = e - i * T;
+    const int i = e >> lgT, t = e & (T - 1);
     const long long col = t0 + t;
     if (col >= inner) continue;
     base[(long long)i * inner + col] = INV ? get_inv<R>(buf + t * ld, L, i)
@@ -316,10 +377,10 @@ __global__ void __launch_bounds__(256, 2) k_c2c_axis(cplx<R>* __restrict__ S, in
 // the dv comps of each frequency, inverse line DFT.  CTA = T inner columns of
 // one load; lines (c, t) for c < dv.
 // ---------------------------------------------------------------------------
-template <typename R>
-__global__ void __launch_bounds__(256, 2) k_proj_first(cplx<R>* __restrict__ S, GridDims g, int na,
-                                                    long long inner, LineDev<R> L, int T,
-                                                    GreenParams gp,
+template <typename R, int PHYS>
+__global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_proj_first(cplx<R>* __restrict__ S, const __grid_constant__ GridDims g, int na,
+                                                    long long inner, const __grid_constant__ LineDev<R> L, int T,
+                                                    const __grid_constant__ GreenParams gp,
                                                     const int* __restrict__ all_done,
                                                     const LoadState* __restrict__ st) {
   if (all_done && *all_done) return;
@@ -332,12 +393,13 @@ __global__ void __launch_bounds__(256, 2) k_proj_first(cplx<R>* __restrict__ S, 
   const long long t0 = (long long)blockIdx.x * T;
   const int nl = dv * T;
   const int tasks = nl * na;
+  const int lgT = __ffs(T) - 1;  // T is a power of two
   // coalesced load: consecutive threads take consecutive inner columns
   for (int e = threadIdx.x; e < tasks; e += blockDim.x) {
-    const int t = e % T;
-    const int rest = e / T;
-    const int i = rest % na;
-    const int c = rest / na;
+    const int t = e & (T - 1);
+    const int rest = e >> lgT;
+    const int c = fdiv(rest, L.dn);
+    const int i = rest - c * na;
     const long long col = t0 + t;
     const cplx<R>* src = S + ((long long)(l * dv + c) * na) * inner;
     const cplx<R> v = (col < inner) ? src[(long long)i * inner + col] : mkc<R>(R(0), R(0));
@@ -349,33 +411,38 @@ __global__ void __launch_bounds__(256, 2) k_proj_first(cplx<R>* __restrict__ S, 
   // Green projection per frequency
   const int ftasks = T * na;
   for (int e = threadIdx.x; e < ftasks; e += blockDim.x) {
-    const int t = e % T, k = e / T;
+    const int t = e & (T - 1), k = e >> lgT;
     const long long col = t0 + t;
     cplx<R> x[kMaxDv];
-    for (int c = 0; c < dv; ++c) x[c] = get_fwd<R>(buf + (c * T + t) * ld, L, k);
+#pragma unroll
+    for (int c = 0; c < kMaxDv; ++c)
+      if (c < dv) x[c] = get_fwd<R>(buf + (c * T + t) * ld, L, k);
     if (col < inner) {
       int kv[3];
       kv[0] = signed_freq(k, na);
       if (g.dim == 3) {
-        const int k1 = (int)(col / g.n2h);
+        const int k1 = fdiv((int)col, g.dn2h);
         kv[1] = signed_freq(k1, g.n1);
-        kv[2] = (int)(col - (long long)k1 * g.n2h);
+        kv[2] = (int)col - k1 * g.n2h;
       } else {
         kv[1] = (int)col;
+        kv[2] = 0;
       }
-      green_apply<R>(gp, g.dim, kv, x);
+      green_apply<R, PHYS>(gp, g.dim, kv, x);
     }
-    for (int c = 0; c < dv; ++c) put_inv<R>(buf + (c * T + t) * ld, L, k, x[c]);
+#pragma unroll
+    for (int c = 0; c < kMaxDv; ++c)
+      if (c < dv) put_inv<R>(buf + (c * T + t) * ld, L, k, x[c]);
   }
   __syncthreads();
   zero_tail<R>(buf, ld, nl, L);
   __syncthreads();
   line_core<R>(buf, ld, nl, L, true);
   for (int e = threadIdx.x; e < tasks; e += blockDim.x) {
-    const int t = e % T;
-    const int rest = e / T;
-    const int i = rest % na;
-    const int c = rest / na;
+    const int t = e & (T - 1);
+    const int rest = e >> lgT;
+    const int c = fdiv(rest, L.dn);
+    const int i = rest - c * na;
     const long long col = t0 + t;
     if (col >= inner) continue;
     cplx<R>* dst = S + ((long long)(l * dv + c) * na) * inner;
@@ -388,10 +455,10 @@ __global__ void __launch_bounds__(256, 2) k_proj_first(cplx<R>* __restrict__ S, 
 // fused dot <p, y> per load (CG's <P, AP>).
 // ---------------------------------------------------------------------------
 template <typename R, bool DOT>
-__global__ void __launch_bounds__(256, 2) k_c2r_last(const cplx<R>* __restrict__ S, R* __restrict__ y,
+__global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_c2r_last(const cplx<R>* __restrict__ S, R* __restrict__ y,
                                                   const R* __restrict__ pdot,
-                                                  double* __restrict__ partials, GridDims g,
-                                                  LineDev<R> L, int rows, R scale,
+                                                  double* __restrict__ partials, const __grid_constant__ GridDims g,
+                                                  const __grid_constant__ LineDev<R> L, int rows, R scale,
                                                   const int* __restrict__ all_done) {
   if (all_done && *all_done) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -404,8 +471,8 @@ __global__ void __launch_bounds__(256, 2) k_c2r_last(const cplx<R>* __restrict__
   const int n = g.n2, n2h = g.n2h;
   const int tasks = rows * np * n2h;
   for (int e = threadIdx.x; e < tasks; e += blockDim.x) {
-    const int line = e / n2h, k = e - line * n2h;
-    const int rl = line / np, p = line - rl * np;
+    const int line = fdiv(e, g.dn2h), k = e - line * n2h;
+    const int rl = fdiv(line, g.dnp), p = line - rl * np;
     const long long row = row0 + rl;
     cplx<R>* lp = buf + (long long)line * ld;
     cplx<R> a = mkc<R>(R(0), R(0)), b = mkc<R>(R(0), R(0));
@@ -424,22 +491,39 @@ __global__ void __launch_bounds__(256, 2) k_c2r_last(const cplx<R>* __restrict__
   __syncthreads();
   line_core<R>(buf, ld, rows * np, L, true);
   double acc[kMaxLoads];
+#pragma unroll
   for (int i = 0; i < kMaxLoads; ++i) acc[i] = 0.;
-  const int otasks = rows * np * n;
-  for (int e = threadIdx.x; e < otasks; e += blockDim.x) {
-    const int line = e / n, j = e - line * n;
-    const int rl = line / np, p = line - rl * np;
+  // one warp per pair line: the <p, y> terms of a line add up per lane in the
+  // field precision (at most n/32 terms) and reach the FP64 accumulators once
+  // per line (FP64 arithmetic per element would dominate on this part)
+  const int lane = threadIdx.x & 31;
+  for (int line = threadIdx.x >> 5; line < rows * np; line += blockDim.x >> 5) {
+    const int rl = fdiv(line, g.dnp), p = line - rl * np;
     const long long row = row0 + rl;
     if (row >= nrows) continue;
-    const cplx<R> z = get_inv<R>(buf + (long long)line * ld, L, j);
+    const cplx<R>* lp = buf + (long long)line * ld;
     const int ca = 2 * p, cb = 2 * p + 1;
-    const long long v = row * n + j;
-    const R ya = z.x * scale, yb = z.y * scale;
-    y[(long long)ca * g.M + v] = ya;
-    if (cb < C) y[(long long)cb * g.M + v] = yb;
+    R* ya_out = y + (long long)ca * g.M + row * n;
+    R* yb_out = y + (long long)cb * g.M + row * n;
+    R sa = R(0), sb = R(0);
+    for (int j = lane; j < n; j += 32) {
+      const cplx<R> z = get_inv<R>(lp, L, j);
+      const R ya = z.x * scale, yb = z.y * scale;
+      ya_out[j] = ya;
+      if (cb < C) yb_out[j] = yb;
+      if constexpr (DOT) {
+        sa += pdot[(long long)ca * g.M + row * n + j] * ya;
+        if (cb < C) sb += pdot[(long long)cb * g.M + row * n + j] * yb;
+      }
+    }
     if constexpr (DOT) {
-      acc[ca / g.dv] += (double)pdot[(long long)ca * g.M + v] * (double)ya;
-      if (cb < C) acc[cb / g.dv] += (double)pdot[(long long)cb * g.M + v] * (double)yb;
+      const int la = ca / g.dv, lb = cb < C ? cb / g.dv : -1;
+      // constant indices: acc stays in registers
+#pragma unroll
+      for (int l = 0; l < kMaxLoads; ++l) {
+        if (l == la) acc[l] += (double)sa;
+        if (l == lb) acc[l] += (double)sb;
+      }
     }
   }
   if constexpr (DOT) {
@@ -461,11 +545,14 @@ __global__ void __launch_bounds__(256) k_dot(const R* __restrict__ x, const R* _
   for (int i = 0; i < kMaxLoads; ++i) acc[i] = 0.;
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < g.M; v += stride) {
-    for (int l = 0; l < g.L; ++l)
+#pragma unroll
+    for (int l = 0; l < kMaxLoads; ++l) {
+      if (l >= g.L) break;
       for (int c = 0; c < g.dv; ++c) {
         const long long i = (long long)(l * g.dv + c) * g.M + v;
         acc[l] += (double)x[i] * (double)y[i];
       }
+    }
   }
   block_sum_n(acc, g.L, red, partials + (long long)blockIdx.x * g.L);
 }
@@ -483,6 +570,7 @@ __global__ void __launch_bounds__(256) k_cg_update(R* __restrict__ x, R* __restr
   double acc[kMaxLoads];
   double alpha[kMaxLoads];
   bool act[kMaxLoads];
+#pragma unroll
   for (int l = 0; l < kMaxLoads; ++l) {
     acc[l] = 0.;
     act[l] = l < g.L && !st[l].done;
@@ -490,17 +578,22 @@ __global__ void __launch_bounds__(256) k_cg_update(R* __restrict__ x, R* __restr
   }
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < g.M; v += stride) {
-    for (int l = 0; l < g.L; ++l) {
+#pragma unroll
+    for (int l = 0; l < kMaxLoads; ++l) {
+      if (l >= g.L) break;
       if (!act[l]) continue;
-      // updates in the field precision, <R,R> accumulated in FP64
+      // updates in the field precision; <R,R> summed over the comps of a voxel
+      // in the field precision, across voxels in FP64
       const R a = (R)alpha[l];
+      R sq = R(0);
       for (int c = 0; c < g.dv; ++c) {
         const long long i = (long long)(l * g.dv + c) * g.M + v;
         x[i] = x[i] + a * p[i];
         const R rn = r[i] - a * ap[i];
         r[i] = rn;
-        acc[l] += (double)(rn * rn);
+        sq += rn * rn;
       }
+      acc[l] += (double)sq;
     }
   }
   block_sum_n(acc, g.L, red, partials + (long long)blockIdx.x * g.L);
@@ -646,6 +739,80 @@ __global__ void __launch_bounds__(128) k_energy(const R* __restrict__ X, const R
   block_sum_n(acc, L * L, red, partials + (long long)blockIdx.x * L * L);
 }
 
+// Load-pair weights of a scalar function of A_H (the adjoint seed dF/dA_H).
+struct LoadMat {
+  double w[kMaxLoads * kMaxLoads];
+};
+
+// Coefficient gradient of sum_ij W[i][j] A_H[i][j], A_H[i][j] = <A u_i, u_j> =
+// (1/M) sum_v u_j(v) . A(v) u_i(v), u_i = X_i (+ E_i).  At the solution of
+// G A u_i = 0 the fields are stationary (Galerkin orthogonality), so the
+// derivative is the explicit one and needs no adjoint solve:
+//   S_ab(v) = sum_ij W_ij u_j[a] u_i[b] / M
+//   ISO: sum_a S_aa;  SYM (packed a <= b): S_aa, S_ab + S_ba;  FULL: S_ab.
+// FP64 throughout (a one-off per gradient).
+template <typename R, int COEF>
+__global__ void __launch_bounds__(128) k_energy_grad(const R* __restrict__ X,
+                                                     double* __restrict__ grad,
+                                                     const __grid_constant__ GridDims g,
+                                                     int add_macro,
+                                                     const __grid_constant__ LoadMat W,
+                                                     double invM) {
+  const int L = g.L, dv = g.dv;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < g.M; v += stride) {
+    double u[kMaxLoads][kMaxDv], T[kMaxLoads][kMaxDv];
+#pragma unroll
+    for (int l = 0; l < kMaxLoads; ++l)
+#pragma unroll
+      for (int c = 0; c < kMaxDv; ++c) {
+        u[l][c] = (l < L && c < dv) ? (double)X[(long long)(l * dv + c) * g.M + v] +
+                                          ((add_macro && c == l) ? 1. : 0.)
+                                    : 0.;
+      }
+    // T[j][b] = sum_i W_ij u_i[b]
+#pragma unroll
+    for (int j = 0; j < kMaxLoads; ++j)
+#pragma unroll
+      for (int b = 0; b < kMaxDv; ++b) {
+        double t = 0.;
+#pragma unroll
+        for (int i = 0; i < kMaxLoads; ++i)
+          if (i < L && j < L) t += W.w[i * L + j] * u[i][b];
+        T[j][b] = t;
+      }
+    auto S = [&](int a, int b) {
+      double s = 0.;
+#pragma unroll
+      for (int j = 0; j < kMaxLoads; ++j) s += u[j][a] * T[j][b];
+      return s * invM;
+    };
+    if constexpr (COEF == COEF_ISO) {
+      double s = 0.;
+#pragma unroll
+      for (int a = 0; a < kMaxDv; ++a)
+        if (a < dv) s += S(a, a);
+      grad[v] = s;
+    } else if constexpr (COEF == COEF_SYM) {
+#pragma unroll
+      for (int a = 0; a < kMaxDv; ++a)
+#pragma unroll
+        for (int b = 0; b < kMaxDv; ++b) {
+          if (a < dv && b < dv && a <= b) {
+            const int t = a * dv - a * (a - 1) / 2 + (b - a);
+            grad[(long long)t * g.M + v] = a == b ? S(a, a) : S(a, b) + S(b, a);
+          }
+        }
+    } else {
+#pragma unroll
+      for (int a = 0; a < kMaxDv; ++a)
+#pragma unroll
+        for (int b = 0; b < kMaxDv; ++b)
+          if (a < dv && b < dv) grad[(long long)(a * dv + b) * g.M + v] = S(a, b);
+    }
+  }
+}
+
 // sum partials[nparts][n] -> out[n] (one block)
 static __global__ void k_sum_partials(const double* __restrict__ partials, int nparts, int n,
                                double scale, double* __restrict__ out) {
@@ -772,16 +939,23 @@ struct BandAxis {
                        // inner); 2 3D (line, inner = k1 * inner2 + k2)
   int inner2;          // pmode 2: extent of the last axis (half spectrum)
   int n1f;             // pmode 2: N extent of axis 1 (frequency layout)
+  FastDiv dn_in, dn_out, dinner2;  // division by n_in, n_out, inner2
 };
+
+inline void set_band_divs(BandAxis& ax) {
+  ax.dn_in = make_fastdiv((unsigned)ax.n_in);
+  ax.dn_out = make_fastdiv((unsigned)ax.n_out);
+  ax.dinner2 = make_fastdiv((unsigned)(ax.inner2 > 0 ? ax.inner2 : 1));
+}
 
 __device__ __forceinline__ void band_freqs(const BandAxis& ax, int dim, int q, int m,
                                            long long col, int* kv) {
   if (dim == 2) { kv[0] = q; kv[1] = (int)col; return; }
   if (ax.pmode == 1) { kv[0] = signed_freq(m, ax.mid_n); kv[1] = q; kv[2] = (int)col; return; }
-  const int k1 = (int)(col / ax.inner2);
+  const int k1 = fdiv((int)col, ax.dinner2);
   kv[0] = q;
   kv[1] = signed_freq(k1, ax.n1f);
-  kv[2] = (int)(col - (long long)k1 * ax.inner2);
+  kv[2] = (int)col - k1 * ax.inner2;
 }
 
 // N-layout coefficient k (grid n) from the forward B-line (length nb)
@@ -797,11 +971,11 @@ __device__ __forceinline__ cplx<R> band_down_value(const cplx<R>* line, const Li
   return get_fwd<R>(line, L, q < 0 ? q + nb : q);
 }
 
-template <typename R, int MODE>
-__global__ void __launch_bounds__(256, 2) k_band_axis(const cplx<R>* __restrict__ Sin,
-                                                   cplx<R>* __restrict__ Sout, GridDims g,
-                                                   BandAxis ax, LineDev<R> L1, LineDev<R> L2,
-                                                   int T, GreenParams gp,
+template <typename R, int MODE, int PHYS>
+__global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_axis(const cplx<R>* __restrict__ Sin,
+                                                   cplx<R>* __restrict__ Sout, const __grid_constant__ GridDims g,
+                                                   const __grid_constant__ BandAxis ax, const __grid_constant__ LineDev<R> L1, const __grid_constant__ LineDev<R> L2,
+                                                   int T, const __grid_constant__ GreenParams gp,
                                                    const int* __restrict__ all_done,
                                                    const LoadState* __restrict__ st) {
   if (all_done && *all_done) return;
@@ -820,13 +994,14 @@ __global__ void __launch_bounds__(256, 2) k_band_axis(const cplx<R>* __restrict_
   cplx<R>* buf2 = buf1 + (size_t)nlc * T * ld1;
   const long long t0 = (long long)blockIdx.x * T;
   const int nl = nlc * T;
+  const int lgT = __ffs(T) - 1;  // T is a power of two
   if constexpr (MODE == BAND_PAD) {
     // input already in frequency (N layout): pad straight into the B line
     for (int e = threadIdx.x; e < nl * ax.n_out; e += blockDim.x) {
-      const int t = e % T;
-      const int rest = e / T;
-      const int k = rest % ax.n_out;
-      const int c = rest / ax.n_out;
+      const int t = e & (T - 1);
+      const int rest = e >> lgT;
+      const int c = fdiv(rest, ax.dn_out);
+      const int k = rest - c * ax.n_out;
       const long long col = t0 + t;
       const int q = signed_freq(k, ax.n_out);
       const int aq = q < 0 ? -q : q;
@@ -842,10 +1017,10 @@ __global__ void __launch_bounds__(256, 2) k_band_axis(const cplx<R>* __restrict_
   } else {
     // load: [comp][mid][n_in][inner]
     for (int e = threadIdx.x; e < nl * ax.n_in; e += blockDim.x) {
-      const int t = e % T;
-      const int rest = e / T;
-      const int i = rest % ax.n_in;
-      const int c = rest / ax.n_in;
+      const int t = e & (T - 1);
+      const int rest = e >> lgT;
+      const int c = fdiv(rest, ax.dn_in);
+      const int i = rest - c * ax.n_in;
       const long long col = t0 + t;
       const cplx<R>* src = Sin + (((long long)(c0 + c) * ax.mid + m) * ax.n_in) * ax.inner;
       const cplx<R> v = col < ax.inner ? src[(long long)i * ax.inner + col] : mkc<R>(R(0), R(0));
@@ -863,17 +1038,21 @@ __global__ void __launch_bounds__(256, 2) k_band_axis(const cplx<R>* __restrict_
   if constexpr (MODE == BAND_UP_PROJ) {
     // G over the dv comps of each N frequency, then the padded B line
     for (int e = threadIdx.x; e < T * ax.n_in; e += blockDim.x) {
-      const int t = e % T, k = e / T;
+      const int t = e & (T - 1), k = e >> lgT;
       const long long col = t0 + t;
       const int q = signed_freq(k, ax.n_in);
       cplx<R> x[kMaxDv];
-      for (int c = 0; c < g.dv; ++c) x[c] = get_fwd<R>(buf1 + (c * T + t) * ld1, L1, k);
+#pragma unroll
+      for (int c = 0; c < kMaxDv; ++c)
+        if (c < g.dv) x[c] = get_fwd<R>(buf1 + (c * T + t) * ld1, L1, k);
       if (col < ax.inner) {
         int kv[3];
         band_freqs(ax, g.dim, q, m, col, kv);
-        green_apply<R>(gp, g.dim, kv, x);
+        green_apply<R, PHYS>(gp, g.dim, kv, x);
       }
-      for (int c = 0; c < g.dv; ++c) {
+#pragma unroll
+      for (int c = 0; c < kMaxDv; ++c) {
+        if (c >= g.dv) break;
         // the projected spectrum is band limited (Nyquist zeroed): place it
         cplx<R>* l2 = buf2 + (c * T + t) * ld2;
         if (2 * (q < 0 ? -q : q) < ax.n_in) put_inv<R>(l2, L2, q < 0 ? q + ax.n_out : q, x[c]);
@@ -881,7 +1060,7 @@ __global__ void __launch_bounds__(256, 2) k_band_axis(const cplx<R>* __restrict_
     }
     // the remaining B frequencies are zero
     for (int e = threadIdx.x; e < nl * ax.n_out; e += blockDim.x) {
-      const int line = e / ax.n_out, k = e - line * ax.n_out;
+      const int line = fdiv(e, ax.dn_out), k = e - line * ax.n_out;
       const int q = signed_freq(k, ax.n_out);
       if (2 * (q < 0 ? -q : q) >= ax.n_in) put_inv<R>(buf2 + line * ld2, L2, k, mkc<R>(R(0), R(0)));
     }
@@ -889,7 +1068,7 @@ __global__ void __launch_bounds__(256, 2) k_band_axis(const cplx<R>* __restrict_
   if constexpr (MODE == BAND_UP || MODE == BAND_UP_PROJ || MODE == BAND_PAD) {
     if constexpr (MODE == BAND_UP) {
     for (int e = threadIdx.x; e < nl * ax.n_out; e += blockDim.x) {
-      const int line = e / ax.n_out, k = e - line * ax.n_out;
+      const int line = fdiv(e, ax.dn_out), k = e - line * ax.n_out;
       const int q = signed_freq(k, ax.n_out);
       const int aq = q < 0 ? -q : q;
       cplx<R> v = mkc<R>(R(0), R(0));
@@ -906,10 +1085,10 @@ __global__ void __launch_bounds__(256, 2) k_band_axis(const cplx<R>* __restrict_
     __syncthreads();
     line_core<R>(buf2, ld2, nl, L2, true);
     for (int e = threadIdx.x; e < nl * ax.n_out; e += blockDim.x) {
-      const int t = e % T;
-      const int rest = e / T;
-      const int i = rest % ax.n_out;
-      const int c = rest / ax.n_out;
+      const int t = e & (T - 1);
+      const int rest = e >> lgT;
+      const int c = fdiv(rest, ax.dn_out);
+      const int i = rest - c * ax.n_out;
       const long long col = t0 + t;
       if (col >= ax.inner) continue;
       cplx<R>* dst = Sout + (((long long)(c0 + c) * ax.mid + m) * ax.n_out) * ax.inner;
@@ -917,10 +1096,10 @@ __global__ void __launch_bounds__(256, 2) k_band_axis(const cplx<R>* __restrict_
     }
   } else if constexpr (MODE == BAND_DOWN) {
     for (int e = threadIdx.x; e < nl * ax.n_out; e += blockDim.x) {
-      const int t = e % T;
-      const int rest = e / T;
-      const int k = rest % ax.n_out;
-      const int c = rest / ax.n_out;
+      const int t = e & (T - 1);
+      const int rest = e >> lgT;
+      const int c = fdiv(rest, ax.dn_out);
+      const int k = rest - c * ax.n_out;
       const long long col = t0 + t;
       if (col >= ax.inner) continue;
       const cplx<R> v = band_down_value<R>(buf1 + (c * T + t) * ld1, L1, k, ax.n_out, ax.n_in);
@@ -930,27 +1109,30 @@ __global__ void __launch_bounds__(256, 2) k_band_axis(const cplx<R>* __restrict_
   } else {
     // G(xi) on the band, then inverse DFT_N along the line
     for (int e = threadIdx.x; e < T * ax.n_out; e += blockDim.x) {
-      const int t = e % T, k = e / T;
+      const int t = e & (T - 1), k = e >> lgT;
       const long long col = t0 + t;
       const int q = signed_freq(k, ax.n_out);
       cplx<R> x[kMaxDv];
-      for (int c = 0; c < g.dv; ++c)
-        x[c] = band_down_value<R>(buf1 + (c * T + t) * ld1, L1, k, ax.n_out, ax.n_in);
+#pragma unroll
+      for (int c = 0; c < kMaxDv; ++c)
+        if (c < g.dv) x[c] = band_down_value<R>(buf1 + (c * T + t) * ld1, L1, k, ax.n_out, ax.n_in);
       if (col < ax.inner) {
         int kv[3];
         band_freqs(ax, g.dim, q, m, col, kv);
-        green_apply<R>(gp, g.dim, kv, x);
+        green_apply<R, PHYS>(gp, g.dim, kv, x);
       }
-      for (int c = 0; c < g.dv; ++c) put_inv<R>(buf2 + (c * T + t) * ld2, L2, k, x[c]);
+#pragma unroll
+      for (int c = 0; c < kMaxDv; ++c)
+        if (c < g.dv) put_inv<R>(buf2 + (c * T + t) * ld2, L2, k, x[c]);
     }
     zero_tail<R>(buf2, ld2, nl, L2);
     __syncthreads();
     line_core<R>(buf2, ld2, nl, L2, true);
     for (int e = threadIdx.x; e < nl * ax.n_out; e += blockDim.x) {
-      const int t = e % T;
-      const int rest = e / T;
-      const int i = rest % ax.n_out;
-      const int c = rest / ax.n_out;
+      const int t = e & (T - 1);
+      const int rest = e >> lgT;
+      const int c = fdiv(rest, ax.dn_out);
+      const int i = rest - c * ax.n_out;
       const long long col = t0 + t;
       if (col >= ax.inner) continue;
       cplx<R>* dst = Sout + (((long long)(c0 + c) * ax.mid + m) * ax.n_out) * ax.inner;
@@ -963,10 +1145,10 @@ __global__ void __launch_bounds__(256, 2) k_band_axis(const cplx<R>* __restrict_
 // S[comp][row][N2h] (row over the B grid's leading axes): c2r to the B2 points,
 // q = A x * cscale per voxel, r2c back and keep the band k2 <= h2.
 template <typename R, int COEF>
-__global__ void __launch_bounds__(256, 2) k_band_last(cplx<R>* __restrict__ S,
-                                                   const R* __restrict__ A, GridDims g,
+__global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_last(cplx<R>* __restrict__ S,
+                                                   const R* __restrict__ A, const __grid_constant__ GridDims g,
                                                    long long nrows, int n2h_band, int n2_solve,
-                                                   LineDev<R> L, int rows, R coef_scale,
+                                                   const __grid_constant__ LineDev<R> L, int rows, R coef_scale,
                                                    const int* __restrict__ all_done) {
   if (all_done && *all_done) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -977,32 +1159,50 @@ __global__ void __launch_bounds__(256, 2) k_band_last(cplx<R>* __restrict__ S,
   const int n = L.n;                       // B2
   const long long Mi = nrows * n;          // voxels of the integration grid
   const long long row0 = (long long)blockIdx.x * rows;
-  // 1) Hermitian pair lines Z = A + iB over all B2 frequencies
-  for (int e = threadIdx.x; e < rows * np * n; e += blockDim.x) {
-    const int line = e / n, k = e - line * n;
-    const int rl = line / np, p = line - rl * np;
-    const long long row = row0 + rl;
-    const int q = signed_freq(k, n);
-    const int aq = q < 0 ? -q : q;
-    cplx<R> z = mkc<R>(R(0), R(0));
-    const R w = (2 * aq < n2_solve) ? R(1) : (2 * aq == n2_solve ? R(0.5) : R(0));
-    if (row < nrows && w != R(0)) {
-      const int ca = 2 * p, cb = 2 * p + 1;
-      cplx<R> a = cscale<R>(S[((long long)ca * nrows + row) * n2h_band + aq], w);
-      cplx<R> b = cb < C ? cscale<R>(S[((long long)cb * nrows + row) * n2h_band + aq], w)
-                         : mkc<R>(R(0), R(0));
-      if (aq == 0 || 2 * aq == n2_solve) { a.y = R(0); b.y = R(0); }
-      if (q < 0) { a.y = -a.y; b.y = -b.y; }     // X_{-k} = conj(X_k)
-      z = mkc<R>(a.x - b.y, a.y + b.x);
+  // 1) Hermitian pair lines Z = A + iB over all B2 frequencies.  Frequency-
+  // stationary: a thread decodes frequency k (weight, slot, chirp) once and
+  // fills it in its share of the lines.
+  const int nlines = rows * np;
+  {
+    int k0 = threadIdx.x, kstep = blockDim.x, l0 = 0, lstep = 1;
+    if (n < (int)blockDim.x) {
+      lstep = blockDim.x / n;
+      l0 = threadIdx.x / n;
+      k0 = threadIdx.x - l0 * n;
+      kstep = n;
     }
-    put_inv<R>(buf + (long long)line * ld, L, k, z);
+    if (l0 < lstep) {
+      for (int k = k0; k < n; k += kstep) {
+        const int q = signed_freq(k, n);
+        const int aq = q < 0 ? -q : q;
+        const R w = (2 * aq < n2_solve) ? R(1) : (2 * aq == n2_solve ? R(0.5) : R(0));
+        const bool real_only = aq == 0 || 2 * aq == n2_solve;
+        const int slot = L.blue ? sp(k) : sp(L.pos[k]);
+        const cplx<R> ch = L.blue ? L.chirp[k] : mkc<R>(R(1), R(0));
+        for (int line = l0; line < nlines; line += lstep) {
+          const int rl = fdiv(line, g.dnp), p = line - rl * np;
+          const long long row = row0 + rl;
+          cplx<R> z = mkc<R>(R(0), R(0));
+          if (row < nrows && w != R(0)) {
+            const int ca = 2 * p, cb = 2 * p + 1;
+            cplx<R> a = cscale<R>(S[((long long)ca * nrows + row) * n2h_band + aq], w);
+            cplx<R> bv = cb < C ? cscale<R>(S[((long long)cb * nrows + row) * n2h_band + aq], w)
+                                : mkc<R>(R(0), R(0));
+            if (real_only) { a.y = R(0); bv.y = R(0); }
+            if (q < 0) { a.y = -a.y; bv.y = -bv.y; }     // X_{-k} = conj(X_k)
+            z = mkc<R>(a.x - bv.y, a.y + bv.x);
+          }
+          buf[(long long)line * ld + slot] = L.blue ? cmul<R>(cconj<R>(z), ch) : z;
+        }
+      }
+    }
   }
   zero_tail<R>(buf, ld, rows * np, L);
   __syncthreads();
   line_core<R>(buf, ld, rows * np, L, true);
   // 2) coefficient per voxel (all loads), in place
   for (int e = threadIdx.x; e < rows * n; e += blockDim.x) {
-    const int rl = e / n, j = e - rl * n;
+    const int rl = fdiv(e, L.dn), j = e - rl * n;
     const long long row = row0 + rl;
     cplx<R>* base = buf + (long long)rl * np * ld;
     if (row >= nrows) {
@@ -1021,12 +1221,16 @@ __global__ void __launch_bounds__(256, 2) k_band_last(cplx<R>* __restrict__ S,
     }
     for (int l = 0; l < g.L; ++l) {
       R xv[kMaxDv], qv[kMaxDv];
-      for (int c = 0; c < g.dv; ++c) {
+#pragma unroll
+      for (int c = 0; c < kMaxDv; ++c) {
+        if (c >= g.dv) break;
         const int comp = l * g.dv + c;
         xv[c] = reinterpret_cast<const R*>(base + (comp >> 1) * ld + sp(j))[comp & 1];
       }
       coef_apply<R, COEF>(A, Mi, v, g.dv, xv, qv);
-      for (int c = 0; c < g.dv; ++c) {
+#pragma unroll
+      for (int c = 0; c < kMaxDv; ++c) {
+        if (c >= g.dv) break;
         const int comp = l * g.dv + c;
         R* slot = reinterpret_cast<R*>(base + (comp >> 1) * ld + sp(j)) + (comp & 1);
         *slot = qv[c] * coef_scale;
@@ -1044,24 +1248,42 @@ __global__ void __launch_bounds__(256, 2) k_band_last(cplx<R>* __restrict__ S,
   zero_tail<R>(buf, ld, rows * np, L);
   __syncthreads();
   line_core<R>(buf, ld, rows * np, L, false);
-  // 3) split and keep the band
-  for (int e = threadIdx.x; e < rows * np * n2h_band; e += blockDim.x) {
-    const int line = e / n2h_band, k = e - line * n2h_band;
-    const int rl = line / np, p = line - rl * np;
-    const long long row = row0 + rl;
-    if (row >= nrows) continue;
-    cplx<R> xa = mkc<R>(R(0), R(0)), xb = mkc<R>(R(0), R(0));
-    if (2 * k <= n2_solve) {
-      const cplx<R>* lp = buf + (long long)line * ld;
-      const cplx<R> zk = get_fwd<R>(lp, L, k);
-      const cplx<R> zm = get_fwd<R>(lp, L, k == 0 ? 0 : n - k);
-      xa = mkc<R>(R(0.5) * (zk.x + zm.x), R(0.5) * (zk.y - zm.y));
-      xb = mkc<R>(R(0.5) * (zk.y + zm.y), R(0.5) * (zm.x - zk.x));
-      if (2 * k == n2_solve) { xa.y = R(0); xb.y = R(0); }  // mean of +-N/2 (real lines)
+  // 3) split and keep the band (frequency-stationary as in 1)
+  {
+    int k0 = threadIdx.x, kstep = blockDim.x, l0 = 0, lstep = 1;
+    if (n2h_band < (int)blockDim.x) {
+      lstep = blockDim.x / n2h_band;
+      l0 = threadIdx.x / n2h_band;
+      k0 = threadIdx.x - l0 * n2h_band;
+      kstep = n2h_band;
     }
-    const int ca = 2 * p, cb = 2 * p + 1;
-    S[((long long)ca * nrows + row) * n2h_band + k] = xa;
-    if (cb < C) S[((long long)cb * nrows + row) * n2h_band + k] = xb;
+    if (l0 < lstep) {
+      for (int k = k0; k < n2h_band; k += kstep) {
+        const bool keep = 2 * k <= n2_solve;
+        const int km = k == 0 ? 0 : n - k;
+        const int sk = L.blue ? sp(k) : sp(L.pos[k]);
+        const int sm = L.blue ? sp(km) : sp(L.pos[km]);
+        const cplx<R> chk = L.blue ? L.chirp[k] : mkc<R>(R(1), R(0));
+        const cplx<R> chm = L.blue ? L.chirp[km] : mkc<R>(R(1), R(0));
+        for (int line = l0; line < nlines; line += lstep) {
+          const int rl = fdiv(line, g.dnp), p = line - rl * np;
+          const long long row = row0 + rl;
+          if (row >= nrows) continue;
+          cplx<R> xa = mkc<R>(R(0), R(0)), xb = mkc<R>(R(0), R(0));
+          if (keep) {
+            const cplx<R>* lp = buf + (long long)line * ld;
+            const cplx<R> zk = L.blue ? cmul<R>(lp[sk], chk) : lp[sk];
+            const cplx<R> zm = L.blue ? cmul<R>(lp[sm], chm) : lp[sm];
+            xa = mkc<R>(R(0.5) * (zk.x + zm.x), R(0.5) * (zk.y - zm.y));
+            xb = mkc<R>(R(0.5) * (zk.y + zm.y), R(0.5) * (zm.x - zk.x));
+            if (2 * k == n2_solve) { xa.y = R(0); xb.y = R(0); }  // mean of +-N/2 (real lines)
+          }
+          const int ca = 2 * p, cb = 2 * p + 1;
+          S[((long long)ca * nrows + row) * n2h_band + k] = xa;
+          if (cb < C) S[((long long)cb * nrows + row) * n2h_band + k] = xb;
+        }
+      }
+    }
   }
 }
 

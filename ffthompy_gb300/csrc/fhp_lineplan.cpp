@@ -93,11 +93,17 @@ bool factor_radices(int n, std::vector<int>& rad) {
   if (n < 1) return false;
   int m = n, p2 = 0;
   while (m % 2 == 0) { m /= 2; ++p2; }
-  while (p2 >= 4) { rad.push_back(16); p2 -= 4; }
-  if (p2 == 3) rad.push_back(8);
-  else if (p2 == 2) rad.push_back(4);
-  else if (p2 == 1) rad.push_back(2);
-  for (int p : {3, 5, 7, 11, 13, 17, 19, 23, 29, 31})
+  // 2^p2 in the fewest stages of radix <= 16, exponents as even as possible
+  // (512 = 8 * 8 * 8 rather than 16 * 16 * 2: no cheap radix-2 stage that costs
+  // a full pass over shared memory)
+  if (p2 > 0) {
+    const int nst2 = (p2 + 3) / 4;
+    for (int s = 0; s < nst2; ++s) {
+      const int e = p2 / nst2 + (s < p2 % nst2 ? 1 : 0);
+      rad.push_back(1 << e);
+    }
+  }
+  for (int p : {3, 5, 7, 11, 13, 17})
     while (m % p == 0) { rad.push_back(p); m /= p; }
   return m == 1;
 }

@@ -210,6 +210,27 @@ class GalerkinPlan:
         torch.cuda.current_stream(self.device).synchronize()
         self.coef_kind = kind
 
+    def set_coefficient_packed(self, vals, kind):
+        """vals: packed (c,) + coefficient grid float64 (numpy, or torch on the
+        GPU) of kind FHP_COEF_ISO / SYM / FULL (c = 1, dv(dv+1)/2, dv*dv)."""
+        c = {_lib.FHP_COEF_ISO: 1, _lib.FHP_COEF_SYM: self.dv * (self.dv + 1) // 2,
+             _lib.FHP_COEF_FULL: self.dv * self.dv}[kind]
+        shape = (c,) + self.coef_grid
+        if tuple(vals.shape) != shape:
+            vals = vals.reshape(shape)
+        if isinstance(vals, torch.Tensor) and vals.is_cuda:
+            vals = vals.detach().to(self.device, torch.float64).contiguous()
+            _lib.check(self.lib.fhp_set_coefficient(self.handle, kind, self._ptr(vals), 1,
+                                                    self._stream()), 'fhp_set_coefficient')
+        else:
+            if isinstance(vals, torch.Tensor):
+                vals = vals.detach().cpu().numpy()
+            vals = np.ascontiguousarray(vals, dtype=np.float64)
+            _lib.check(self.lib.fhp_set_coefficient(self.handle, kind, vals.ctypes.data_as(
+                ctypes.c_void_p), 0, self._stream()), 'fhp_set_coefficient')
+        torch.cuda.current_stream(self.device).synchronize()
+        self.coef_kind = kind
+
     def apply(self, x, proj=1):
         x = self._dev(x)
         y = self.empty()
@@ -257,6 +278,21 @@ class GalerkinPlan:
                                               AH.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                                               self._stream()), 'fhp_energy_matrix')
         return AH
+
+    def energy_gradient(self, X, W, add_macro=True):
+        """d(sum_ij W_ij A_H[i, j]) / dA_c(v) for the stored coefficient
+        components c of this plan's kind: a float64 torch tensor (c,) + N."""
+        X = self._dev(X)
+        L = self.nloads
+        W = np.ascontiguousarray(np.broadcast_to(np.asarray(W, dtype=np.float64), (L, L)))
+        c = {_lib.FHP_COEF_ISO: 1, _lib.FHP_COEF_SYM: self.dv * (self.dv + 1) // 2,
+             _lib.FHP_COEF_FULL: self.dv * self.dv}[self.coef_kind]
+        grad = torch.empty((c,) + self.N, dtype=torch.float64, device=self.device)
+        _lib.check(self.lib.fhp_energy_gradient(
+            self.handle, self._ptr(X), int(bool(add_macro)),
+            W.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), self._ptr(grad),
+            self._stream()), 'fhp_energy_gradient')
+        return grad
 
     def interpolate(self, x, grid):
         """Trigonometric interpolation of this plan's fields onto grid (>= N)."""

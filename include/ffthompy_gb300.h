@@ -129,6 +129,21 @@ int fhp_cg_solve(fhp_plan plan, int proj, const void* b, const void* x0, double 
 int fhp_energy_matrix(fhp_plan plan, const void* X, int add_macro, double* AH, void* stream);
 
 /*
+ * Coefficient gradient of a weighted energy matrix, for adjoint / sensitivity
+ * use: grad[c][v] = sum_ij W[i*loads + j] dA_H[i][j] / dA_c(v), where A_c(v)
+ * are the stored coefficient components of the plan's kind at voxel v
+ * (ISO: a(v); SYM: packed upper triangle; FULL: dv*dv) and A_H is as in
+ * fhp_energy_matrix.  At the CG solution the fields are stationary, so no
+ * adjoint solve is needed.  W on host (loads*loads), X and grad device
+ * (grad float64, components x voxels of the solve grid).  Plans with the
+ * coefficient on a band integration grid return FHP_BAD_ARG.
+ * No counterpart in the reference (it has no derivatives); the derivative of
+ * assembly_matrix (ffthompy/postprocess.py:53-70) at the solution.
+ */
+int fhp_energy_gradient(fhp_plan plan, const void* X, int add_macro, const double* W,
+                        double* grad, void* stream);
+
+/*
  * Trigonometric interpolation of the fields of plan src onto the grid of
  * plan dst (same field count and precision; dst grid >= src grid).
  * Replaces: Tensor.project / Tensor.enlarge (ffthompy/tensors/objects.py:
