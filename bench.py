@@ -8,11 +8,11 @@ time-to-A_H: right-hand sides, batched CG to the tolerance that gives A_H
 within 1e-6 of the FP64-refined value, and the A_H energy assembly, with the
 coefficient resident in HBM.  Fields (4.7 GB per vector) exceed L2.
 
---impl reference runs the NumPy restatement of the reference (the oracle: the
-reference itself is Python and cannot be installed on the GPU host) on a
-bounded sample of the same workload (Ga N=31 -> 61^3 grid, same sphere
-statistics, 3 loads, a few CG iterations per load), one worker process per
-host core.
+--impl reference runs the reference's algorithm on the host cores: its NumPy
+restatement (the oracle; the reference source tree is not present on the GPU
+host) on a bounded sample of the same workload (Ga N=31 -> 61^3 grid, same
+sphere statistics, 3 loads, a few CG iterations per load), one worker process
+per host core.
 """
 import argparse
 import json

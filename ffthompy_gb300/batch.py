@@ -19,6 +19,7 @@ from concurrent.futures import ThreadPoolExecutor
 import numpy as np
 import torch
 
+from . import _lib
 from .engine import GalerkinPlan, coef_kind_of_torch, pack_coefficient_torch, require_cuda
 
 
@@ -68,6 +69,10 @@ def homogenize_many(coefs, Y=None, physics='scalar', tol=1e-6, maxiter=1000,
             st.stream.synchronize()
         out[i] = res
 
+    if 'dual' in primaldual:
+        # torch initialises its linear-algebra backend lazily and not thread-safely:
+        # do it once here, before the workers start
+        torch.linalg.inv(torch.eye(2, dtype=torch.float64, device=device))
     with ThreadPoolExecutor(max_workers=max(1, int(workers))) as ex:
         for f in [ex.submit(run, i) for i in order]:
             f.result()
@@ -79,5 +84,8 @@ def _inverse_field(A):
     ffthompy/materials.py get_A_GaNi with primaldual='dual')."""
     dv = A.shape[0]
     N = A.shape[2:]
+    if coef_kind_of_torch(A) == _lib.FHP_COEF_ISO:
+        return torch.einsum('ij,...->ij...', torch.eye(dv, dtype=A.dtype, device=A.device),
+                            1.0 / A[0, 0])
     M = A.reshape(dv, dv, -1).permute(2, 0, 1)
     return torch.linalg.inv(M).permute(1, 2, 0).reshape((dv, dv) + tuple(N)).contiguous()

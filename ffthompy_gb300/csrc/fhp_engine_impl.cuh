@@ -38,6 +38,13 @@ constexpr int kThreads = 256;
 constexpr size_t kSmemBudget = 96 * 1024;   // two CTAs per SM
 constexpr size_t kSmemMax = 227 * 1024;
 constexpr int kTargetElems = 8192;          // complex elements per CTA
+// k_band_last per-CTA shared memory (lines + staged inputs): two CTAs per SM
+// for FP32, one for FP64 (whose kernels use the full register file)
+constexpr size_t kBandLastBudget32 = 110 * 1024;
+// r2c / c2r last-axis passes: pair lines + staged c2r input, same split
+constexpr size_t kRowBudget32 = 110 * 1024;
+constexpr size_t kRowBudget64 = 220 * 1024;
+constexpr size_t kBandLastBudget64 = 220 * 1024;
 
 template <typename T>
 static int set_smem_attr(T* kernel) {
@@ -103,9 +110,19 @@ class Engine final : public EngineBase {
     // launch geometry
     const int np = (C + 1) / 2;
     const size_t srow = (size_t)np * l2_.dev.ld * sizeof(cplx<R>);
-    rows_ = std::max(1, kTargetElems / (np * l2_.dev.ld));
-    rows_ = (int)std::min<size_t>(rows_, std::max<size_t>(1, kSmemBudget / srow));
-    smem_rows_ = std::max<size_t>((size_t)rows_ * srow, 8 * kMaxLoads * sizeof(double));
+    // rows per CTA for the last-axis passes: pair lines plus (when it fits
+    // the per-CTA budget) a staging area for the c2r input spectra
+    {
+      const size_t sraw_row = (size_t)C * g_.n2h * sizeof(cplx<R>);
+      const size_t budget = sizeof(R) == 4 ? kRowBudget32 : kRowBudget64;
+      auto smem_of = [&](int r, bool stg) {
+        return align16((size_t)r * srow) + (stg ? (size_t)r * sraw_row : 0);
+      };
+      rows_ = std::max(1, kTargetElems / (np * l2_.dev.ld));
+      c2r_stage_ = smem_of(1, true) <= budget;
+      while (rows_ > 1 && smem_of(rows_, c2r_stage_) > budget) --rows_;
+      smem_rows_ = std::max<size_t>(smem_of(rows_, c2r_stage_), 8 * kMaxLoads * sizeof(double));
+    }
     if (smem_rows_ > kSmemMax) { set_error("line too long for shared memory"); return ST_BAD_ARG; }
     row_ctas_ = (int)(((long long)g_.n0 * g_.n1 + rows_ - 1) / rows_);
     // strided c2c on axis 1 (3D) and projection on the first real axis
@@ -502,6 +519,7 @@ class Engine final : public EngineBase {
   int* all_done_ = nullptr;
   int* h_done_ = nullptr;
   int rows_ = 1, row_ctas_ = 1, T1_ = 1, Tp_ = 1, T0_ = 1;
+  bool c2r_stage_ = false;   // k_c2r_last stages its input spectra in shared memory
   size_t smem_rows_ = 0;
   int nsm_ = 1, red_ctas_ = 1, nparts_max_ = 1;
 
@@ -696,10 +714,11 @@ class Engine final : public EngineBase {
     const int pk2 = pbeg(dot ? "c2r_dot" : "c2r", spec_bytes() + (dot ? 2.0 : 1.0) * field_bytes(), s);
     if (dot)
       k_c2r_last<R, true><<<grid1, kThreads, smem_rows_, s>>>(Sp, y, pdot, partials_, g_, l2_.dev,
-                                                              rows_, scale, ad);
+                                                              rows_, scale, ad, (int)c2r_stage_);
     else
       k_c2r_last<R, false><<<grid1, kThreads, smem_rows_, s>>>(Sp, y, nullptr, nullptr, g_,
-                                                               l2_.dev, rows_, scale, ad);
+                                                               l2_.dev, rows_, scale, ad,
+                                                               (int)c2r_stage_);
     pend(pk2, s);
     FHP_LAUNCHED();
     return ST_OK;
@@ -828,7 +847,24 @@ class Engine final : public EngineBase {
       const R cs = (R)(1.0 / (double)g_.M);
       const double b4 = 2.0 * (double)(g_.L * g_.dv) * nrows * n2h * sizeof(cplx<R>) + coef_bytes();
       const int pk = pbeg("band_last_coef", b4, s);
-#define FHP_BL(C) k_band_last<R, C><<<brow_ctas_, kThreads, bsmem_rows_, s>>>(Sbig, A_, g_, nrows, (int)n2h, g_.n2, lb2_.dev, brows_, cs, ad)
+      // rows per CTA: the line target, reduced until lines + staged spectra +
+      // staged coefficient fit the per-CTA budget (2 CTAs/SM for FP32)
+      const int C = g_.L * g_.dv, np = (C + 1) / 2;
+      const int cA = coef == COEF_ISO ? 1 : coef == COEF_SYM ? g_.dv * (g_.dv + 1) / 2 : g_.dv * g_.dv;
+      const size_t budget = sizeof(R) == 4 ? kBandLastBudget32 : kBandLastBudget64;
+      // staging modes in order of preference: spectra and coefficient, spectra
+      // only, none (the lines alone always fit: checked at plan creation)
+      int rows = brows_, stage = 3;
+      auto smem_of = [&](int r, int stg) {
+        return band_last_smem_bytes<R>(r, np, lb2_.dev.ld, C, (int)n2h, cA, gi_.n2, stg);
+      };
+      for (stage = 3; stage > 0; stage = stage == 3 ? 1 : 0)
+        if (smem_of(1, stage) <= budget) break;
+      while (rows > 1 && smem_of(rows, stage) > budget) --rows;
+      const size_t smem = smem_of(rows, stage);
+      if (smem > kSmemMax) { set_error("integration line too long for shared memory"); return ST_BAD_ARG; }
+      const unsigned ctas = (unsigned)((nrows + rows - 1) / rows);
+#define FHP_BL(C) k_band_last<R, C><<<ctas, kThreads, smem, s>>>(Sbig, A_, g_, nrows, (int)n2h, g_.n2, lb2_.dev, rows, cs, ad, stage)
       switch (coef) {
         case COEF_ISO: FHP_BL(COEF_ISO); break;
         case COEF_SYM: FHP_BL(COEF_SYM); break;
@@ -860,10 +896,11 @@ class Engine final : public EngineBase {
                          spec_bytes_n() + (dot ? 2.0 : 1.0) * field_bytes(), s);
     if (dot)
       k_c2r_last<R, true><<<grid1, kThreads, smem_rows_, s>>>(SA, y, pdot, partials_, g_, l2_.dev,
-                                                              rows_, (R)1, ad);
+                                                              rows_, (R)1, ad, (int)c2r_stage_);
     else
       k_c2r_last<R, false><<<grid1, kThreads, smem_rows_, s>>>(SA, y, nullptr, nullptr, g_,
-                                                               l2_.dev, rows_, (R)1, ad);
+                                                               l2_.dev, rows_, (R)1, ad,
+                                                               (int)c2r_stage_);
     pend(pk2, s);
     FHP_LAUNCHED();
     return ST_OK;

@@ -83,6 +83,51 @@ __host__ __device__ __forceinline__ int fdiv(int x, FastDiv f) {
 // breaks the power-of-two strides of the late radix stages across banks.
 __device__ __forceinline__ int sp(int i) { return i + (i >> 5); }
 __host__ __device__ inline int padded_ld(int nf) { return nf + (nf >> 5) + 1; }
+__host__ __device__ inline size_t align16(size_t b) { return (b + 15) & ~(size_t)15; }
+
+// ---------------------------------------------------------------------------
+// Asynchronous global -> shared staging (cp.async, LDGSTS): copies go straight
+// to shared memory without registers, so a thread can keep many in flight
+// (the load phases are latency-bound otherwise).  Completion is waited for in
+// hardware (cp.async.wait_group), with no spin loop.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async_16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+template <int BYTES>
+__device__ __forceinline__ void cp_async_small(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s), "l"(gmem), "n"(BYTES)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// Block-cooperative copy of count elements of T (4, 8 or 16 bytes) from global
+// to shared memory: 16-byte copies when both ends are 16-byte aligned and the
+// length is a multiple of 16 bytes, element copies otherwise.
+template <typename T>
+__device__ __forceinline__ void stage_async(T* dst, const T* src, int count) {
+  static_assert(sizeof(T) == 4 || sizeof(T) == 8 || sizeof(T) == 16, "element size");
+  const size_t bytes = (size_t)count * sizeof(T);
+  const bool vec = (((size_t)__cvta_generic_to_shared(dst) | reinterpret_cast<size_t>(src) |
+                     bytes) & 15) == 0;
+  if (vec) {
+    const int n16 = (int)(bytes >> 4);
+    char* d = reinterpret_cast<char*>(dst);
+    const char* g = reinterpret_cast<const char*>(src);
+    for (int i = threadIdx.x; i < n16; i += blockDim.x) cp_async_16(d + 16 * i, g + 16 * i);
+  } else {
+    for (int i = threadIdx.x; i < count; i += blockDim.x)
+      cp_async_small<(int)sizeof(T)>(dst + i, src + i);
+  }
+}
 
 // Device view of one line plan (passed by value in kernel parameters).
 template <typename R>
@@ -434,6 +479,35 @@ template <typename R>
 __device__ __forceinline__ cplx<R> get_inv(const cplx<R>* line, const LineDev<R>& L, int j) {
   return L.blue ? cconj<R>(cmul<R>(line[sp(j)], L.chirp[j])) : line[sp(j)];
 }
+// Asynchronous placement of a line input element straight into its slot
+// (direct lines: a plain copy; Bluestein lines: the raw value, fixed up by
+// blue_fixup after the copies complete).  slot_fwd / slot_inv give the slot
+// of input element j of the forward / inverse core.
+template <typename R>
+__device__ __forceinline__ void cp_async_cplx(cplx<R>* smem, const cplx<R>* gmem) {
+  if constexpr (sizeof(cplx<R>) == 16) cp_async_16(smem, gmem);
+  else cp_async_small<8>(smem, gmem);
+}
+template <typename R>
+__device__ __forceinline__ int slot_fwd(const LineDev<R>& L, int j) { return sp(j); }
+template <typename R>
+__device__ __forceinline__ int slot_inv(const LineDev<R>& L, int k) {
+  return L.blue ? sp(k) : sp(L.pos[k]);
+}
+// Bluestein lines loaded raw into slots j < n: forward input x_j chirp_j,
+// inverse input conj(X_k) chirp_k (what put_fwd / put_inv store).
+template <typename R, bool INV>
+__device__ __forceinline__ void blue_fixup(cplx<R>* buf, int ld, int nlines, const LineDev<R>& L) {
+  if (!L.blue) return;
+  const int tot = nlines * L.n;
+  for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+    const int line = fdiv(e, L.dn), j = e - line * L.n;
+    cplx<R>* p = buf + line * ld + sp(j);
+    const cplx<R> v = *p;
+    *p = INV ? cmul<R>(cconj<R>(v), L.chirp[j]) : cmul<R>(v, L.chirp[j]);
+  }
+}
+
 // Bluestein lines need zeros in slots [n, nf) before the core.
 template <typename R>
 __device__ __forceinline__ void zero_tail(cplx<R>* buf, int ld, int nlines, const LineDev<R>& L) {

