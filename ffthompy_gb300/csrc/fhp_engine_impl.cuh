@@ -584,6 +584,17 @@ class Engine final : public EngineBase {
     L.ld = padded_ld(h.nf);
     L.blue = h.blue;
     L.nst = h.nst;
+    // compile-time power-of-two stages when the plan's radices are theirs
+    L.lg2 = 0;
+    {
+      int P = 0;
+      while ((1 << P) < h.nf) ++P;
+      if ((1 << P) == h.nf && P >= kP2Min && P <= kP2Max && h.nst == p2_nst(P)) {
+        bool same = true;
+        for (int s = 0; s < h.nst; ++s) same = same && h.rad[s] == (1 << p2_e(P, s));
+        if (same) L.lg2 = P;
+      }
+    }
     int ns = h.nf;
     for (int i = 0; i < kMaxStages; ++i) {
       L.rad[i] = i < h.nst ? h.rad[i] : 1;
@@ -627,6 +638,13 @@ class Engine final : public EngineBase {
     FHP_ATTR((k_band_last<R, COEF_ISO>));
     FHP_ATTR((k_band_last<R, COEF_SYM>));
     FHP_ATTR((k_band_last<R, COEF_FULL>));
+#define FHP_ATTR_P2(P)                              \
+    FHP_ATTR((k_band_last_p2<R, COEF_ISO, P>));     \
+    FHP_ATTR((k_band_last_p2<R, COEF_SYM, P>));     \
+    FHP_ATTR((k_band_last_p2<R, COEF_FULL, P>))
+    static_assert(kP2Min == 5 && kP2Max == 10, "k_band_last_p2 instances 2^5 .. 2^10");
+    FHP_ATTR_P2(5); FHP_ATTR_P2(6); FHP_ATTR_P2(7); FHP_ATTR_P2(8); FHP_ATTR_P2(9); FHP_ATTR_P2(10);
+#undef FHP_ATTR_P2
 #undef FHP_ATTR
     return ST_OK;
   }
@@ -864,13 +882,26 @@ class Engine final : public EngineBase {
       const size_t smem = smem_of(rows, stage);
       if (smem > kSmemMax) { set_error("integration line too long for shared memory"); return ST_BAD_ARG; }
       const unsigned ctas = (unsigned)((nrows + rows - 1) / rows);
-#define FHP_BL(C) k_band_last<R, C><<<ctas, kThreads, smem, s>>>(Sbig, A_, g_, nrows, (int)n2h, g_.n2, lb2_.dev, rows, cs, ad, stage)
+      // direct power-of-two integration lines: compile-time stages and phases
+      const int lgb = lb2_.dev.blue ? 0 : lb2_.dev.lg2;
+#define FHP_BLARGS <<<ctas, kThreads, smem, s>>>(Sbig, A_, g_, nrows, (int)n2h, g_.n2, lb2_.dev, rows, cs, ad, stage)
+#define FHP_BL(C)                                                  \
+      switch (lgb) {                                               \
+        case 5: k_band_last_p2<R, C, 5> FHP_BLARGS; break;          \
+        case 6: k_band_last_p2<R, C, 6> FHP_BLARGS; break;          \
+        case 7: k_band_last_p2<R, C, 7> FHP_BLARGS; break;          \
+        case 8: k_band_last_p2<R, C, 8> FHP_BLARGS; break;          \
+        case 9: k_band_last_p2<R, C, 9> FHP_BLARGS; break;          \
+        case 10: k_band_last_p2<R, C, 10> FHP_BLARGS; break;        \
+        default: k_band_last<R, C> FHP_BLARGS; break;               \
+      }
       switch (coef) {
         case COEF_ISO: FHP_BL(COEF_ISO); break;
         case COEF_SYM: FHP_BL(COEF_SYM); break;
         default: FHP_BL(COEF_FULL); break;
       }
 #undef FHP_BL
+#undef FHP_BLARGS
       pend(pk, s);
       FHP_LAUNCHED();
     }

@@ -52,6 +52,9 @@ template <typename R>
 __device__ __forceinline__ cplx<R> cmul_pi(cplx<R> a) { return mkc<R>(-a.y, a.x); }
 
 constexpr int kMaxStages = 16;
+// power-of-two core lengths 2^kP2Min .. 2^kP2Max run compile-time stages
+constexpr int kP2Min = 5;
+constexpr int kP2Max = 10;
 
 // Division by a run-time invariant d as a multiply-high and two shifts
 // (Granlund & Montgomery, "Division by invariant integers using
@@ -137,6 +140,8 @@ struct LineDev {
   int ld;       // shared-memory stride of one line (padded, >= sp(nf - 1) + 1)
   int blue;     // 1: Bluestein
   int nst;      // number of radix stages of the core
+  int lg2;      // log2(nf) when the core runs the compile-time power-of-two
+                // stages (kP2Min <= lg2 <= kP2Max), else 0
   int rad[kMaxStages];
   FastDiv dnbl[kMaxStages];  // stage s: division by nf / rad[s] (butterflies per line)
   FastDiv dms[kMaxStages];   // stage s: division by the butterfly span ms_s
@@ -417,6 +422,113 @@ __device__ __forceinline__ void stage_dispatch(cplx<R>* buf, int ld, int nlines,
   }
 }
 
+// ---------------------------------------------------------------------------
+// Power-of-two cores with a compile-time stage sequence.  The radices are
+// those of factor_radices (2^P in ceil(P/4) stages, exponents as even as
+// possible, the larger ones first: 512 = 8.8.8, 1024 = 16.8.8, 256 = 16.16),
+// and the slots and twiddles are the run-time path's, so the digit-reversed
+// positions (LineDev::pos) and the arithmetic are unchanged.  What changes is
+// the index work: butterfly coordinates are shifts and masks, and the r slots
+// of a butterfly sit at compile-time offsets from its first slot, because for
+// power-of-two spans sp(g*ns + j1 + q*ms) = sp(g*ns + j1) + sp(q*ms) (adding
+// q*ms never carries across a 32-slot boundary of the padding).
+// ---------------------------------------------------------------------------
+__host__ __device__ constexpr int p2_nst(int P) { return (P + 3) / 4; }
+__host__ __device__ constexpr int p2_e(int P, int s) {
+  return P / p2_nst(P) + (s < P % p2_nst(P) ? 1 : 0);
+}
+__host__ __device__ constexpr int p2_ebefore(int P, int s) {
+  int t = 0;
+  for (int i = 0; i < s; ++i) t += p2_e(P, i);
+  return t;
+}
+// slot of frequency k after the forward DIF of length 2^P (digit reversal)
+template <int P>
+__device__ __forceinline__ int p2_pos(int k) {
+  int pos = 0;
+#pragma unroll
+  for (int s = 0; s < p2_nst(P); ++s) {
+    const int e = p2_e(P, s), eb = p2_ebefore(P, s);
+    pos |= ((k >> eb) & ((1 << e) - 1)) << (P - eb - e);
+  }
+  return pos;
+}
+
+// Stage S of the in-place DIF (forward) or its inverse, on nlines lines.
+// A thread keeps one butterfly (its slots and twiddles) for all its lines;
+// requires blockDim.x to be a multiple of the butterflies per line (every
+// launch uses 256 threads; the largest count is 128).
+template <typename R, int P, int S, bool INV>
+__device__ __forceinline__ void p2_stage(cplx<R>* __restrict__ buf, int ld, int nlines,
+                                         const cplx<R>* __restrict__ tw) {
+  constexpr int E = p2_e(P, S), EB = p2_ebefore(P, S);
+  constexpr int RAD = 1 << E;
+  constexpr int LNS = P - EB, LMS = LNS - E, LNBL = P - E;
+  constexpr int NS = 1 << LNS, MS = 1 << LMS, NBL = 1 << LNBL;
+  static_assert(NBL <= 256, "butterflies per line exceed the CTA");
+  const int tid = threadIdx.x;
+  const int lstep = blockDim.x >> LNBL;
+  const int l0 = tid >> LNBL;
+  const int bb = tid & (NBL - 1);
+  const int g = bb >> LMS, j1 = bb & (MS - 1);
+  const int sbase = sp(g * NS + j1);
+  cplx<R> w[RAD];
+#pragma unroll
+  for (int q = 1; q < RAD; ++q) w[q] = tw[(j1 * q) << EB];
+  for (int line = l0; line < nlines; line += lstep) {
+    cplx<R>* lp = buf + line * ld + sbase;
+    cplx<R> v[RAD];
+    if constexpr (!INV) {
+#pragma unroll
+      for (int q = 0; q < RAD; ++q) v[q] = lp[sp(q * MS)];
+      dft_fwd<R, RAD>(v, tw, 1 << P);
+      lp[0] = v[0];
+#pragma unroll
+      for (int q = 1; q < RAD; ++q) lp[sp(q * MS)] = cmul<R>(v[q], w[q]);
+    } else {
+      v[0] = cconj<R>(lp[0]);
+#pragma unroll
+      for (int q = 1; q < RAD; ++q) v[q] = cconj<R>(cmulc<R>(lp[sp(q * MS)], w[q]));
+      dft_fwd<R, RAD>(v, tw, 1 << P);
+#pragma unroll
+      for (int q = 0; q < RAD; ++q) lp[sp(q * MS)] = cconj<R>(v[q]);
+    }
+  }
+}
+
+template <typename R, int P, bool INV>
+__device__ __forceinline__ void p2_run(cplx<R>* buf, int ld, int nlines, const cplx<R>* tw) {
+  constexpr int NST = p2_nst(P);
+  static_assert(NST <= 3, "power-of-two cores up to 2^12");
+  if constexpr (!INV) {
+    p2_stage<R, P, 0, false>(buf, ld, nlines, tw);
+    __syncthreads();
+    if constexpr (NST > 1) { p2_stage<R, P, 1, false>(buf, ld, nlines, tw); __syncthreads(); }
+    if constexpr (NST > 2) { p2_stage<R, P, 2, false>(buf, ld, nlines, tw); __syncthreads(); }
+  } else {
+    if constexpr (NST > 2) { p2_stage<R, P, 2, true>(buf, ld, nlines, tw); __syncthreads(); }
+    if constexpr (NST > 1) { p2_stage<R, P, 1, true>(buf, ld, nlines, tw); __syncthreads(); }
+    p2_stage<R, P, 0, true>(buf, ld, nlines, tw);
+    __syncthreads();
+  }
+}
+
+template <typename R, int P>
+__device__ __forceinline__ void line_core_p2(cplx<R>* buf, int ld, int nlines, const LineDev<R>& L,
+                                             bool inverse) {
+  if (L.blue || !inverse) p2_run<R, P, false>(buf, ld, nlines, L.tw);
+  if (L.blue) {
+    const int tot = nlines << P;
+    for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+      const int line = e >> P, j = e & ((1 << P) - 1);
+      cplx<R>* p = buf + line * ld + sp(j);
+      *p = cmul<R>(*p, L.bhat[j]);
+    }
+    __syncthreads();
+  }
+  if (L.blue || inverse) p2_run<R, P, true>(buf, ld, nlines, L.tw);
+}
+
 // Core transform of nlines lines (length L.nf each, stride ld) in place.
 //   direct, forward : DIF            (natural -> digit-reversed)
 //   direct, inverse : DIT^-1         (digit-reversed -> natural), unnormalised
@@ -424,6 +536,16 @@ __device__ __forceinline__ void stage_dispatch(cplx<R>* buf, int ld, int nlines,
 // Ends with __syncthreads().
 template <typename R>
 __device__ void line_core(cplx<R>* buf, int ld, int nlines, const LineDev<R>& L, bool inverse) {
+  static_assert(kP2Min == 5 && kP2Max == 10, "dispatch below lists 2^5 .. 2^10");
+  switch (L.lg2) {
+    case 5: line_core_p2<R, 5>(buf, ld, nlines, L, inverse); return;
+    case 6: line_core_p2<R, 6>(buf, ld, nlines, L, inverse); return;
+    case 7: line_core_p2<R, 7>(buf, ld, nlines, L, inverse); return;
+    case 8: line_core_p2<R, 8>(buf, ld, nlines, L, inverse); return;
+    case 9: line_core_p2<R, 9>(buf, ld, nlines, L, inverse); return;
+    case 10: line_core_p2<R, 10>(buf, ld, nlines, L, inverse); return;
+    default: break;
+  }
   const int tid = threadIdx.x, nthr = blockDim.x;
   const bool do_fwd = L.blue || !inverse;
   const bool do_inv = L.blue || inverse;

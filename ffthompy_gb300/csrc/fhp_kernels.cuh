@@ -1380,6 +1380,140 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_last(cplx<R>* __
   }
 }
 
+// k_band_last for a direct power-of-two integration line B2 = 2^P (the
+// smooth grids 2^k >= 2N-1 of the common solve sizes: 509 -> 512, 253 -> 256).
+// Same shared-memory layout, staging and results as k_band_last; the phases
+// around the transforms are organised per line instead of per element:
+//  1) a warp expands one pair line: lane aq reads the two staged band spectra
+//     once and writes frequency aq and its conjugate N-aq; the frequencies
+//     outside the band get zeros.  Digit-reversed slots are shifts (p2_pos).
+//  2) the coefficient per voxel; for isotropic coefficients both comps of a
+//     pair line scale together (one 8- or 16-byte access per pair line).
+//  3) a warp splits one pair line back into its two band half spectra with
+//     coalesced stores.
+template <typename R, int COEF, int P>
+__global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_last_p2(cplx<R>* __restrict__ S,
+                                                   const R* __restrict__ A, const __grid_constant__ GridDims g,
+                                                   long long nrows, int n2h_band, int n2_solve,
+                                                   const __grid_constant__ LineDev<R> L, int rows, R coef_scale,
+                                                   const int* __restrict__ all_done, int stage) {
+  constexpr int N = 1 << P;
+  if (all_done && *all_done) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx<R>* buf = reinterpret_cast<cplx<R>*>(smem_raw);
+  const int C = g.L * g.dv;
+  const int np = (C + 1) / 2;
+  const int ld = L.ld;
+  const long long Mi = nrows * N;
+  const long long row0 = (long long)blockIdx.x * rows;
+  const int cA = coef_comps<COEF>(g.dv);
+  const int vrows = (int)((nrows - row0) < rows ? (nrows - row0) : rows);
+  cplx<R>* sraw = reinterpret_cast<cplx<R>*>(
+      smem_raw + align16((size_t)rows * np * ld * sizeof(cplx<R>)));
+  R* acache = reinterpret_cast<R*>(
+      reinterpret_cast<unsigned char*>(sraw) +
+      ((stage & 1) ? align16((size_t)C * rows * n2h_band * sizeof(cplx<R>)) : 0));
+  const bool st_spec = stage & 1, st_coef = stage & 2;
+  if (st_spec)
+    for (int c = 0; c < C; ++c)
+      stage_async(sraw + (size_t)c * rows * n2h_band,
+                  S + ((long long)c * nrows + row0) * n2h_band, vrows * n2h_band);
+  cp_async_commit();
+  if (st_coef)
+    for (int t = 0; t < cA; ++t)
+      stage_async(acache + (size_t)t * rows * N, A + (long long)t * Mi + row0 * N, vrows * N);
+  cp_async_commit();
+  cp_async_wait<1>();
+  __syncthreads();
+  const int nlines = rows * np;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
+  // 1) Hermitian pair lines Z = A + iB
+  for (int line = warp; line < nlines; line += nwarp) {
+    const int rl = fdiv(line, g.dnp), p = line - rl * np;
+    cplx<R>* lp = buf + (long long)line * ld;
+    const bool valid = row0 + rl < nrows;
+    const int ca = 2 * p, cb = 2 * p + 1;
+    const cplx<R>* sa = st_spec ? sraw + ((size_t)ca * rows + rl) * n2h_band
+                                : S + ((long long)ca * nrows + row0 + rl) * n2h_band;
+    const cplx<R>* sb = st_spec ? sraw + ((size_t)cb * rows + rl) * n2h_band
+                                : S + ((long long)cb * nrows + row0 + rl) * n2h_band;
+    for (int aq = lane; aq < n2h_band; aq += 32) {
+      cplx<R> a = mkc<R>(R(0), R(0)), b = mkc<R>(R(0), R(0));
+      if (valid) {
+        const R w = (2 * aq < n2_solve) ? R(1) : R(0.5);
+        a = cscale<R>(sa[aq], w);
+        if (cb < C) b = cscale<R>(sb[aq], w);
+        if (aq == 0 || 2 * aq == n2_solve) { a.y = R(0); b.y = R(0); }
+      }
+      lp[sp(p2_pos<P>(aq))] = mkc<R>(a.x - b.y, a.y + b.x);
+      if (aq > 0) lp[sp(p2_pos<P>(N - aq))] = mkc<R>(a.x + b.y, b.x - a.y);  // X_{-k} = conj(X_k)
+    }
+    for (int k = n2h_band + lane; k <= N - n2h_band; k += 32)
+      lp[sp(p2_pos<P>(k))] = mkc<R>(R(0), R(0));
+  }
+  __syncthreads();
+  line_core_p2<R, P>(buf, ld, nlines, L, true);
+  // 2) coefficient per voxel (all loads), in place
+  cp_async_wait<0>();
+  __syncthreads();
+  for (int e = threadIdx.x; e < (rows << P); e += blockDim.x) {
+    const int rl = e >> P, j = e & (N - 1);
+    const long long row = row0 + rl;
+    cplx<R>* base = buf + (long long)rl * np * ld + sp(j);
+    if (row >= nrows) {
+      for (int p = 0; p < np; ++p) base[p * ld] = mkc<R>(R(0), R(0));
+      continue;
+    }
+    if constexpr (COEF == COEF_ISO) {
+      const R a = st_coef ? acache[(long long)rl * N + j] : A[row * N + j];
+      for (int p = 0; p < np; ++p) {
+        const cplx<R> z = base[p * ld];
+        base[p * ld] = mkc<R>((a * z.x) * coef_scale, (a * z.y) * coef_scale);
+      }
+    } else {
+      for (int l = 0; l < g.L; ++l) {
+        R xv[kMaxDv], qv[kMaxDv];
+#pragma unroll
+        for (int c = 0; c < kMaxDv; ++c) {
+          if (c >= g.dv) break;
+          const int comp = l * g.dv + c;
+          xv[c] = reinterpret_cast<const R*>(base + (comp >> 1) * ld)[comp & 1];
+        }
+        if (st_coef) coef_apply<R, COEF>(acache, (long long)rows * N, (long long)rl * N + j, g.dv, xv, qv);
+        else coef_apply<R, COEF>(A, Mi, row * N + j, g.dv, xv, qv);
+#pragma unroll
+        for (int c = 0; c < kMaxDv; ++c) {
+          if (c >= g.dv) break;
+          const int comp = l * g.dv + c;
+          reinterpret_cast<R*>(base + (comp >> 1) * ld)[comp & 1] = qv[c] * coef_scale;
+        }
+      }
+    }
+    if (C & 1) reinterpret_cast<R*>(base + (np - 1) * ld)[1] = R(0);
+  }
+  __syncthreads();
+  line_core_p2<R, P>(buf, ld, nlines, L, false);
+  // 3) split and keep the band
+  for (int line = warp; line < nlines; line += nwarp) {
+    const int rl = fdiv(line, g.dnp), p = line - rl * np;
+    const long long row = row0 + rl;
+    if (row >= nrows) continue;
+    const cplx<R>* lp = buf + (long long)line * ld;
+    const int ca = 2 * p, cb = 2 * p + 1;
+    cplx<R>* da = S + ((long long)ca * nrows + row) * n2h_band;
+    cplx<R>* db = S + ((long long)cb * nrows + row) * n2h_band;
+    for (int k = lane; k < n2h_band; k += 32) {
+      const cplx<R> zk = lp[sp(p2_pos<P>(k))];
+      const cplx<R> zm = lp[sp(p2_pos<P>(k == 0 ? 0 : N - k))];
+      cplx<R> xa = mkc<R>(R(0.5) * (zk.x + zm.x), R(0.5) * (zk.y - zm.y));
+      cplx<R> xb = mkc<R>(R(0.5) * (zk.y + zm.y), R(0.5) * (zm.x - zk.x));
+      if (2 * k == n2_solve) { xa.y = R(0); xb.y = R(0); }  // mean of +-N/2 (real lines)
+      da[k] = xa;
+      if (cb < C) db[k] = xb;
+    }
+  }
+}
+
 // W_i . u_j cross products per load pair on the solve grid (band energy):
 // partial sums of sum_v sum_c W[i][c] (X[j][c] + delta_cj) (postprocess.py:53-70)
 template <typename R>

@@ -364,12 +364,35 @@ def test_band_operator_equals_full_grid_operator(N, physics, precision):
     """Band representation of Ga: FiGFA on band-limited fields of the 2N-1 grid
     (the reference's operator, applications.py:28-58) equals the band plan
     applied on the N grid with the coefficient on a smooth integration grid."""
-    from ffthompy_gb300.engine import GalerkinPlan, nice_size
+    from ffthompy_gb300.engine import nice_size
+    _check_band_operator(N, physics, precision, tuple(nice_size(2 * n - 1) for n in N))
+
+
+def _pow2_at_least(n, lo=32):
+    m = lo
+    while m < n:
+        m *= 2
+    return m
+
+
+@pytest.mark.parametrize('N,physics', [((5, 20), 'scalar'), ((9, 60), 'scalar'),
+                                       ((7, 100), 'scalar'), ((5, 200), 'scalar'),
+                                       ((5, 300), 'scalar'), ((5, 7, 9), 'scalar'),
+                                       ((6, 5, 8), 'scalar'), ((5, 5, 5), 'elasticity'),
+                                       ((9, 60), 'elasticity')])
+@pytest.mark.parametrize('precision', ['f64', 'f32'])
+def test_band_operator_pow2_integration_grid(N, physics, precision):
+    """The band operator on power-of-two integration grids 32 .. 1024 (the
+    compile-time FFT stages) equals the reference's 2N-1 grid operator."""
+    _check_band_operator(N, physics, precision, tuple(_pow2_at_least(2 * n - 1) for n in N))
+
+
+def _check_band_operator(N, physics, precision, integ):
+    from ffthompy_gb300.engine import GalerkinPlan
     rng = np.random.default_rng(len(N) + sum(N))
     d = len(N)
     Nn = np.asarray(N)
     Nb = 2 * Nn - 1
-    integ = tuple(nice_size(n) for n in Nb)
     dv = d if physics == 'scalar' else d * (d + 1) // 2
     Y = 0.7 + rng.random(d)
     # a band-limited SPD coefficient on the 2N-1 grid (Ga coefficients are)
