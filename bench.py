@@ -33,7 +33,18 @@ WORKLOADS = {
     'spheres509': dict(N=255, P=255, radius=0.08, vf=0.3, contrast=100., tol=1e-3, seed=2026),
     'spheres255': dict(N=127, P=127, radius=0.08, vf=0.3, contrast=100., tol=1e-3, seed=2026),
     'spheres125': dict(N=63, P=63, radius=0.08, vf=0.3, contrast=100., tol=1e-3, seed=2026),
+    # small anisotropic cases with the line lengths of spheres509 (255 solve,
+    # 512 integration) on some axes, for profiling captures of a few GB:
+    # axes 0 and 1 (the axis passes), axis 2 (the last-axis integration pass)
+    'spheres255x255x127': dict(N=(255, 255, 127), P=(255, 255, 127), radius=0.08, vf=0.3,
+                               contrast=100., tol=1e-3, seed=2026),
+    'spheres63x127x255': dict(N=(63, 127, 255), P=(63, 127, 255), radius=0.08, vf=0.3,
+                              contrast=100., tol=1e-3, seed=2026),
 }
+
+
+def _dims(v):
+    return tuple(v) if isinstance(v, (tuple, list)) else (v,) * 3
 SAMPLE = dict(N=31, P=31, iters=4)    # CPU baseline sample (61^3 grid)
 
 
@@ -86,7 +97,7 @@ def reduce_max(dist, v):
 # ----------------------------------------------------------------------------
 def image_values(w):
     from ffthompy_gb300.workloads import spheres_coefficient
-    return spheres_coefficient((w['P'],) * 3, radius=w['radius'], vf=w['vf'],
+    return spheres_coefficient(_dims(w['P']), radius=w['radius'], vf=w['vf'],
                                contrast=w['contrast'], seed=w['seed'])
 
 
@@ -94,20 +105,20 @@ def ga_coefficient(vals, w, grid=None):
     """Grid-based Ga coefficient (order 0) of the 2N-1 grid, assembled on the
     GPU, sampled on `grid` (default 2N-1)."""
     from ffthompy_gb300.materials import Material
-    N = np.array([w['N']] * 3)
+    N = np.array(_dims(w['N']))
     mat = Material({'fun': lambda coord, _v=vals: _v, 'Y': np.ones(3), 'order': 0,
-                    'P': np.array([w['P']] * 3)})
+                    'P': np.array(_dims(w['P']))})
     return mat.get_A_Ga(Nbar=2 * N - 1, primaldual='primal', grid=grid)
 
 
 def make_plan(w, precision, ga_mode):
     from ffthompy_gb300.engine import GalerkinPlan, nice_size
-    N = w['N']
-    Ns = 2 * N - 1
+    N = _dims(w['N'])
+    Ns = tuple(2 * n - 1 for n in N)
     if ga_mode == 'band':
-        return GalerkinPlan((N,) * 3, np.ones(3), physics='scalar', nloads=3,
-                            integ=(nice_size(Ns),) * 3, precision=precision)
-    return GalerkinPlan((Ns,) * 3, np.ones(3), physics='scalar', nloads=3, band=(N,) * 3,
+        return GalerkinPlan(N, np.ones(3), physics='scalar', nloads=3,
+                            integ=tuple(nice_size(n) for n in Ns), precision=precision)
+    return GalerkinPlan(Ns, np.ones(3), physics='scalar', nloads=3, band=N,
                         precision=precision)
 
 
@@ -231,7 +242,7 @@ def run_reference(args):
         'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
         'config': {'workload': '%s (sample: Ga %d^3 -> %d^3, one sample per core)'
                                % (args.workload, SAMPLE['N'], 2 * SAMPLE['N'] - 1),
-                   'grid': [2 * w['N'] - 1] * 3, 'loads': 3},
+                   'grid': [2 * n - 1 for n in _dims(w['N'])], 'loads': 3},
         'cpu_baseline': {'value': value, 'unit': 'Mvoxel-iter/s', 'cores': cores, 'kind': 'port',
                          'sample': '%d processes x (Ga %d^3 -> %d^3 spheres, 3 loads x %d CG '
                                    'iterations), NumPy restatement of the reference'
@@ -255,11 +266,11 @@ def run_gpu(args):
 
     from ffthompy_gb300.engine import nice_size
     w = WORKLOADS[args.workload]
-    N = w['N']
-    Ns = 2 * N - 1
-    M = Ns ** 3                       # voxels of the reference's solve grid (2N-1)^3
+    N = _dims(w['N'])
+    Ns = tuple(2 * n - 1 for n in N)
+    M = int(np.prod(Ns))              # voxels of the reference's solve grid prod(2N-1)
     vals = image_values(w)
-    cgrid = (nice_size(Ns),) * 3 if args.ga_mode == 'band' else (Ns,) * 3
+    cgrid = tuple(nice_size(n) for n in Ns) if args.ga_mode == 'band' else Ns
     A = ga_coefficient(vals, w, grid=cgrid)           # (3,3)+grid on the GPU, FP64
     A_iso = A.data[0, 0].contiguous()
     extras = {'coefficient_grid': list(cgrid)}
@@ -400,10 +411,11 @@ def run_gpu(args):
         'vs_baseline': None, 'dtype': 'f32' if args.precision == 'f32' else 'f64+f32',
         'data': 'synthetic',
         'config': {'workload': '%s: 3D scalar Ga, spheres r=%.2f vf>=%.1f contrast %g, image '
-                               '%d^3 -> %d^3 grid, 3 loads batched, CG tol %g (A_H within 1e-6)'
-                               % (args.workload, w['radius'], w['vf'], w['contrast'], w['P'],
-                                  Ns, w['tol']),
-                   'grid': [Ns] * 3, 'loads': 3, 'precision': args.precision,
+                               '%s -> %s grid, 3 loads batched, CG tol %g (A_H within 1e-6)'
+                               % (args.workload, w['radius'], w['vf'], w['contrast'],
+                                  'x'.join(map(str, _dims(w['P']))), 'x'.join(map(str, Ns)),
+                                  w['tol']),
+                   'grid': list(Ns), 'loads': 3, 'precision': args.precision,
                    'ga_mode': args.ga_mode,
                    'voxels_counted': 'prod(2N-1) per load and iteration (the reference grid)',
                    'l2': 'inputs larger than L2 (coefficient %.2f GB, spectra %.1f GB)'

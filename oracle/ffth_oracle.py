@@ -23,6 +23,8 @@ __all__ = [
     'freq_ints', 'coordinates', 'projection_scalar', 'projection_elasticity',
     'green_operator', 'projection_elasticity_parts', 'apply_GA', 'scal', 'cg', 'get_inverse', 'Material',
     'project', 'assembly_matrix', 'solve_problem', 'mandel_isotropic',
+    'grad_symbol', 'potential_preconditioner', 'scal_fourier', 'cg_fourier',
+    'potential_operator', 'potential_rhs', 'potential_field', 'homog_potential',
 ]
 
 
@@ -701,3 +703,185 @@ def solve_problem(problem, as_shipped=False, verbose=False):
         out['sol_' + pd] = sols
         out['res_' + pd] = res
     return out
+
+
+# ----------------------------------------------------------------------------
+# potential formulation (ffthompy/tensorsLowRank/homogenisation.py:41-127)
+# ----------------------------------------------------------------------------
+# The unknown is the scalar potential u in the 'r' Fourier form of the N grid
+# (unnormalised half spectrum); the CG iterates are such spectra and the
+# inner product is the 'r' branch of scalar_product.
+def grad_symbol(N, Y):
+    """2 pi i xi on the 'r' half spectrum of grid N: grad_tensor
+    (tensors/operators.py:371-386) with frequencies Grid.get_xil (trigpol.py:
+    27-40; even N: the Nyquist index carries -N/2, also on the last axis)."""
+    N = np.asarray(N, dtype=np.int64)
+    Y = np.asarray(Y, dtype=np.float64)
+    d = N.size
+    xi = [freq_ints(int(n)) / Y[i] for i, n in enumerate(N)]
+    xi[-1] = xi[-1][:N[-1] // 2 + 1]
+    shape = tuple(len(x) for x in xi)
+    out = np.zeros((d,) + shape, dtype=np.complex128)
+    for i in range(d):
+        sh = [1] * d
+        sh[i] = shape[i]
+        out[i] = np.broadcast_to(xi[i].reshape(sh), shape)
+    return out * 2 * np.pi * 1j
+
+
+def potential_preconditioner(N, Y):
+    """P = 1/|2 pi xi| with 1 at the mean index (homogenisation.py:296-300)."""
+    h = grad_symbol(N, Y)
+    k2 = np.einsum('i...,i...', h, np.conj(h)).real
+    k2[(0,) * len(N)] = 1.
+    return 1. / k2 ** 0.5
+
+
+def scal_fourier(x, y, N):
+    """scalar_product of two 'r' form Fourier tensors (objects.py:618-631)."""
+    M2 = float(np.prod(N)) ** 2
+    if N[-1] % 2 == 1:
+        s = (np.sum(y[..., 0] * np.conj(x[..., 0])).real +
+             2 * np.sum(y[..., 1:] * np.conj(x[..., 1:])).real)
+    else:
+        s = (np.sum(y[..., 0] * np.conj(x[..., 0])).real +
+             np.sum(y[..., -1] * np.conj(x[..., -1])).real +
+             2 * np.sum(y[..., 1:-1] * np.conj(x[..., 1:-1])).real)
+    return float(s / M2)
+
+
+def cg_fourier(Afun, B, x0, N, tol=1e-6, maxiter=1000):
+    """CG (solver.py:80-139) with the 'r' Fourier inner product (get_scal picks
+    X*Y = scalar_product for Tensors, solver.py:287-298)."""
+    x = x0
+    R = B - Afun(x0)
+    P = R
+    rr = scal_fourier(R, R, N)
+    kit = 0
+    norm_res = np.double(rr) ** 0.5
+    log = [norm_res]
+    while norm_res > tol and kit < maxiter:
+        kit += 1
+        AP = Afun(P)
+        alp = float(rr / scal_fourier(P, AP, N))
+        x = x + alp * P
+        R = R - alp * AP
+        rrnext = scal_fourier(R, R, N)
+        bet = rrnext / rr
+        rr = rrnext
+        P = R + bet * P
+        norm_res = np.double(rr) ** 0.5
+        log.append(norm_res)
+    if kit == 0:
+        norm_res = 0
+    return x, {'kit': kit, 'norm_res': norm_res, 'res_log': log}
+
+
+def _r_axes(d, lead):
+    return tuple(range(lead, lead + d))
+
+
+def _enlarge_r(X, N, M):
+    """Tensor.enlarge of 'r' Fourier tensors (objects.py:428-467) for odd N:
+    centred zero padding with the 'r' <-> 'c' scalings 1/prod(N), prod(M).
+    For odd N the spectra here are Hermitian (rfftn of real fields), so the
+    padding equals the trigonometric interpolation of the real field."""
+    d = len(N)
+    ax = _r_axes(d, X.ndim - d)
+    x = np.fft.irfftn(X, s=tuple(N), axes=ax)
+    return np.fft.rfftn(project(x.reshape((-1,) + tuple(N)), M).reshape(
+        X.shape[:X.ndim - d] + tuple(M)), axes=ax)
+
+
+def _decrease_r(X, M, N):
+    """Tensor.decrease / project to a smaller grid (objects.py:469-511 with
+    trigpol.py:191-214) for odd N and M: the centred band of N, scaled by
+    prod(N)/prod(M)."""
+    d = len(N)
+    lead = X.shape[:X.ndim - d]
+    ax = _r_axes(d, len(lead))
+    full = np.fft.fftn(np.fft.irfftn(X, s=tuple(M), axes=ax), axes=ax)
+    idx = np.ix_(*[np.fft.ifftshift(np.arange(-(n // 2), n // 2 + 1)) % m
+                   for n, m in zip(N, M)])
+    out = full[(Ellipsis,) + idx] * (float(np.prod(N)) / float(np.prod(M)))
+    return out[..., :N[-1] // 2 + 1]
+
+
+def _grad(X, N, Y):
+    return grad_symbol(N, Y) * X[None]
+
+
+def _div(X, N, Y):
+    return np.einsum('i...,i...->...', grad_symbol(N, Y), X)
+
+
+def potential_operator(A, N, Y, Nbar=None):
+    """PDFAFGPfun (homogenisation.py:61-67, 97-103) as a function of the
+    preconditioned potential: P (-div F(A iF(grad(P x)))), with the Ga
+    enlargement to Nbar and projection back to N when Nbar is given."""
+    N = tuple(int(n) for n in N)
+    P = potential_preconditioner(N, Y)
+    d = len(N)
+    Ns = N if Nbar is None else tuple(int(n) for n in Nbar)
+    ax = _r_axes(d, 1)
+
+    def afun(x):
+        g = _grad(P * x, N, Y)
+        if Nbar is not None:
+            g = _enlarge_r(g, N, Ns)
+        e = np.fft.irfftn(g, s=Ns, axes=ax)
+        q = np.einsum('ij...,j...->i...', A, e)
+        Q = np.fft.rfftn(q, s=Ns, axes=ax)
+        if Nbar is not None:
+            Q = _decrease_r(Q, Ns, N)
+        return P * (-_div(Q, N, Y))
+    return afun
+
+
+def potential_rhs(A, N, Y, load=0, Nbar=None):
+    """P * B with B = div(F(A E)) (decreased to N for Ga), homogenisation.py:
+    58, 95 (E = e_load)."""
+    N = tuple(int(n) for n in N)
+    d = len(N)
+    Ns = N if Nbar is None else tuple(int(n) for n in Nbar)
+    E = np.zeros((d,) + Ns)
+    E[load] = 1.
+    Q = np.fft.rfftn(np.einsum('ij...,j...->i...', A, E), s=Ns, axes=_r_axes(d, 1))
+    if Nbar is not None:
+        Q = _decrease_r(Q, Ns, N)
+    return potential_preconditioner(N, Y) * _div(Q, N, Y)
+
+
+def potential_field(x, N, Y, Ns=None):
+    """X = iF(grad(P x)) on N, or iF2(grad(P x).project(Ns)) on the larger grid
+    Ns (homogenisation.py:74-77, 117-124)."""
+    N = tuple(int(n) for n in N)
+    d = len(N)
+    g = _grad(potential_preconditioner(N, Y) * x, N, Y)
+    if Ns is None or tuple(Ns) == N:
+        return np.fft.irfftn(g, s=N, axes=_r_axes(d, 1))
+    Ns = tuple(int(n) for n in Ns)
+    return np.fft.irfftn(_enlarge_r(g, N, Ns), s=Ns, axes=_r_axes(d, 1))
+
+
+def homog_potential(A, N, Y, tol, maxiter, Nbar=None, A_post=None, load=0):
+    """homog_GaNi_full_potential (homogenisation.py:83-127; Nbar None, A the
+    GaNi coefficient on N, A_post the optional Ga coefficient on 2N-1) and
+    homog_Ga_full_potential (homogenisation.py:41-81; A the Ga coefficient on
+    Nbar).  Returns dict AH, iPU (CG solution), Fu = P iPU, info."""
+    N = tuple(int(n) for n in N)
+    afun = potential_operator(A, N, Y, Nbar)
+    PB = potential_rhs(A, N, Y, load, Nbar)
+    x0 = np.zeros_like(PB)
+    iPU, info = cg_fourier(afun, PB, x0, N, tol=tol, maxiter=maxiter)
+    Fu = potential_preconditioner(N, Y) * iPU
+    if Nbar is not None:
+        Ap, Ns = A, tuple(int(n) for n in Nbar)
+    elif A_post is not None:
+        Ap, Ns = A_post, tuple(int(n) for n in A_post.shape[2:])
+    else:
+        Ap, Ns = A, N
+    X = potential_field(iPU, N, Y, Ns)
+    X[load] += 1.
+    AH = scal(np.einsum('ij...,j...->i...', Ap, X), X)
+    return {'AH': AH, 'iPU': iPU, 'Fu': Fu, 'info': info}

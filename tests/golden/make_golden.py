@@ -25,7 +25,13 @@ op_<name>.npz
     Green projection, the Ga scale factor of Tensor.enlarge and the r2c FFT
     conventions independently of CG.
 
-Usage:  python tests/golden/make_golden.py [REFERENCE_DIR]
+pot_<name>.npz
+    The potential formulation (ffthompy/tensorsLowRank/homogenisation.py:
+    41-127): A_H, CG iteration counts and the potential Fu of
+    homog_GaNi_full_potential / homog_Ga_full_potential, and one application
+    of their preconditioned operator.
+
+Usage:  python tests/golden/make_golden.py [REFERENCE_DIR [pickles|run|op|pot ...]]
 """
 import collections
 import collections.abc
@@ -267,10 +273,92 @@ def operator_cases():
         _save('op_' + name, meta, arrays)
 
 
+def _stub_ttpy():
+    """ffthompy.tensorsLowRank imports ttpy (absent here) at module level; the
+    full potential solvers used below never call it, so empty stand-in
+    modules satisfy the imports."""
+    import types
+
+    class _Absent(types.ModuleType):
+        def __getattr__(self, name):
+            if name.startswith('__'):
+                raise AttributeError(name)
+            return type(name, (), {})
+    for m in ('tt', 'tt.core', 'tt.core.vector', 'tt.core.tools', 'tt.core.matrix'):
+        sys.modules.setdefault(m, _Absent(m))
+
+
+def potential_cases():
+    """The potential formulation with the 1/|xi| preconditioner:
+    homog_GaNi_full_potential and homog_Ga_full_potential
+    (ffthompy/tensorsLowRank/homogenisation.py:41-127), run on reference
+    Material coefficients (E = e_0, as the reference does), plus single
+    applications of their preconditioned operator PDFAFGPfun built from the
+    same reference primitives (grad, div, DFT, enlarge, project)."""
+    _stub_ttpy()
+    import ffthompy.tensorsLowRank.homogenisation as H
+    from ffthompy import Struct
+    from ffthompy.materials import Material
+    from ffthompy.tensors import DFT, Tensor, grad, div
+    rng = np.random.default_rng(31)
+    cases = []
+    for dim in (2, 3):
+        mat = {'inclusions': ['square', 'otherwise'], 'positions': [np.zeros(dim), ''],
+               'params': [0.6 * np.ones(dim), ''], 'vals': [10 * np.eye(dim), np.eye(dim)],
+               'Y': np.ones(dim), 'P': dim * (5,), 'order': 0}
+        cases.append(('s%d_square5' % dim, mat, np.array(dim * [5])))
+    for name, Nl in [('s2_fun9', [9, 9]), ('s3_fun5', [5, 5, 5]), ('s3_fun_aniso', [5, 7, 9]),
+                     ('s2_fun_even8', [8, 8]), ('s2_fun_even6x7', [6, 7])]:
+        Nl = np.array(Nl)
+        a = 1. + 49. * (rng.random(tuple(Nl)) < 0.35) * rng.random(tuple(Nl))
+        cases.append((name, _fun_material(_iso_field(Nl.size, a), np.ones(Nl.size)), Nl))
+    for name, mconf, N in cases:
+        d = N.size
+        even = bool(np.any(N % 2 == 0))
+        pars = Struct(dim=d, N=tuple(int(n) for n in N), Y=np.ones(d),
+                      solver=dict(tol=1e-8, maxiter=200))
+        mat = Material(mconf)
+        Agani = mat.get_A_GaNi(N, primaldual='primal')
+        Aga = mat.get_A_Ga(2 * N - 1, primaldual='primal')
+        arrays = {'A_gani': Agani.val, 'A_ga': Aga.val}
+        runs = [('gani', lambda: H.homog_GaNi_full_potential(Agani, None, pars))]
+        if not even:
+            runs += [('gani_ga', lambda: H.homog_GaNi_full_potential(Agani, Aga, pars)),
+                     ('ga', lambda: H.homog_Ga_full_potential(Aga, pars))]
+        for key, fn in runs:
+            with contextlib.redirect_stdout(io.StringIO()):
+                r = fn()
+            arrays['AH__' + key] = np.array(float(r.AH))
+            arrays['kit__' + key] = np.array(int(r.info['kit']))
+            arrays['normres__' + key] = np.array(float(r.info['norm_res']))
+            arrays['Fu__' + key] = r.Fu.val
+        # one application of PDFAFGPfun to a seeded Hermitian spectrum
+        x = Tensor(name='x', val=np.fft.rfftn(rng.standard_normal(tuple(N))), order=0,
+                   N=N, Fourier=True)
+        P = H.get_preconditioner(N, pars)
+        F, iF = DFT(name='FN', inverse=False, N=N), DFT(name='FiN', inverse=True, N=N)
+        arrays['x'] = x.val
+        arrays['y__gani'] = (P * (-div(F(Agani * iF(grad(P * x)))))).val
+        if not even:
+            Nbar = 2 * N - 1
+            F2, iF2 = DFT(name='FN', inverse=False, N=Nbar), DFT(name='FiN', inverse=True, N=Nbar)
+            FAX = F2(Aga * iF2(grad(P * x).enlarge(Nbar))).project(N)
+            arrays['y__ga'] = (P * (-div(FAX))).val
+        meta = dict(N=[int(n) for n in N], Y=[1.] * d, tol=1e-8, maxiter=200, even=even,
+                    runs=[k for k, _ in runs])
+        _save('pot_' + name, meta, arrays)
+
+
 if __name__ == '__main__':
     _install_shim()
     import warnings
     warnings.simplefilter('ignore')
-    golden_pickles()
-    run_cases()
-    operator_cases()
+    only = sys.argv[2:] if len(sys.argv) > 2 else ['pickles', 'run', 'op', 'pot']
+    if 'pickles' in only:
+        golden_pickles()
+    if 'run' in only:
+        run_cases()
+    if 'op' in only:
+        operator_cases()
+    if 'pot' in only:
+        potential_cases()
