@@ -54,6 +54,11 @@ SIGNATURES = {
     'fhp_profile_read': (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_char_p, _c_ll_p,
                                         _c_double_p, _c_double_p, _c_int_p]),
     'fhp_plan_launches': (ctypes.c_longlong, [_vp]),
+    'fhp_potential_rhs': (ctypes.c_int, [_vp, _vp, _vp]),
+    'fhp_potential_apply': (ctypes.c_int, [_vp, _vp, _vp, _vp]),
+    'fhp_potential_cg': (ctypes.c_int, [_vp, _vp, ctypes.c_double, ctypes.c_int, _vp, _c_int_p,
+                                        _c_double_p, _c_int_p, _c_double_p, ctypes.c_int, _vp]),
+    'fhp_potential_field': (ctypes.c_int, [_vp, _vp, _vp, _vp]),
     'fhp_energy_matrix_noalloc': (ctypes.c_int, [ctypes.c_int, _c_int_p, ctypes.c_int,
                                                  ctypes.c_int, ctypes.c_int, _vp, _vp,
                                                  ctypes.c_int, _vp, _vp]),

@@ -273,6 +273,43 @@ int fhp_rhs_macro(fhp_plan plan, int proj, void* b, void* stream) {
   return plan->eng->rhs_macro(proj, b, as_stream(stream));
 }
 
+int fhp_potential_rhs(fhp_plan plan, void* bh, void* stream) {
+  if (!plan || !bh) return bad("plan and bh are required");
+  return plan->eng->pot_rhs(bh, as_stream(stream));
+}
+
+int fhp_potential_apply(fhp_plan plan, const void* xh, void* yh, void* stream) {
+  if (!plan || !xh || !yh) return bad("plan, xh and yh are required");
+  return plan->eng->pot_apply(xh, yh, as_stream(stream));
+}
+
+int fhp_potential_cg(fhp_plan plan, const void* bh, double tol, int maxiter, void* xh, int* kit,
+                     double* norm_res, int* status, double* res_log, int log_rows,
+                     void* stream) {
+  if (!plan || !bh || !xh) return bad("plan, bh and xh are required");
+  if (maxiter < 0) return bad("maxiter must be >= 0");
+  if (!(tol >= 0)) return bad("tol must be >= 0");
+  fhp::SolveResult r;
+  const int rows = res_log ? std::max(1, log_rows) : 1;
+  int st = plan->eng->pot_cg(bh, tol, maxiter, xh, r, rows, as_stream(stream));
+  if (st != FHP_OK) return st;
+  const int L = plan->eng->loads();
+  for (int l = 0; l < L && l < (int)r.kit.size(); ++l) {
+    if (kit) kit[l] = r.kit[l];
+    if (norm_res) norm_res[l] = r.norm_res[l];
+    if (status) status[l] = r.status[l];
+  }
+  if (res_log && !r.res_log.empty())
+    std::memcpy(res_log, r.res_log.data(),
+                std::min<size_t>((size_t)rows * L, r.res_log.size()) * sizeof(double));
+  return FHP_OK;
+}
+
+int fhp_potential_field(fhp_plan plan, const void* xh, void* X, void* stream) {
+  if (!plan || !xh || !X) return bad("plan, xh and X are required");
+  return plan->eng->pot_field(xh, X, as_stream(stream));
+}
+
 int fhp_cg_solve(fhp_plan plan, int proj, const void* b, const void* x0, double tol,
                  int maxiter, void* x, int* kit, double* norm_res, int* status,
                  double* res_log, int log_rows, void* stream) {

@@ -123,6 +123,20 @@ class EngineBase {
                            cudaStream_t s) = 0;
   virtual int add_scaled_to64(const void* d, const double* scale, double* x,
                               cudaStream_t s) = 0;
+  // potential formulation (scalar physics, plans without an integration
+  // grid; ffthompy/tensorsLowRank/homogenisation.py:41-127).  Potential
+  // spectra: 'r' form half spectra of the band grid N, [load][N0][N1][N2/2+1]
+  // complex of this engine's precision.
+  virtual long long pot_spectrum_elems() const = 0;
+  // bh = P B, B_l = div(decrease_N F(A E_l))
+  virtual int pot_rhs(void* bh, cudaStream_t s) = 0;
+  // yh = P (-div) decrease_N F(A iF(enlarge(grad(P xh))))
+  virtual int pot_apply(const void* xh, void* yh, cudaStream_t s) = 0;
+  // CG on the preconditioned system with the 'r' Fourier inner product
+  virtual int pot_cg(const void* bh, double tol, int maxiter, void* xh, SolveResult& res,
+                     int log_cap, cudaStream_t s) = 0;
+  // X = iF(enlarge(grad(P xh))): fields (load, comp) on this engine's grid
+  virtual int pot_field(const void* xh, void* X, cudaStream_t s) = 0;
   // kernel launch count of the last call (instrumentation)
   long long launches = 0;
 };

@@ -203,6 +203,232 @@ class Engine final : public EngineBase {
   const PlanConfig& config() const override { return cfg_; }
   int coef_kind() const override { return coef_kind_; }
 
+  // ---- potential formulation (homogenisation.py:41-127) --------------------
+  long long pot_spectrum_elems() const override {
+    const int d = g_.dim;
+    const long long b0 = d == 3 ? cfg_.band[0] : 1, b1 = cfg_.band[d - 2], b2 = cfg_.band[d - 1];
+    return (long long)g_.L * b0 * b1 * (b2 / 2 + 1);
+  }
+
+  int pot_check() {
+    if (cfg_.physics != 0) { set_error("the potential formulation is scalar"); return ST_BAD_ARG; }
+    if (band_) {
+      set_error("the potential formulation needs a plan without an integration grid");
+      return ST_BAD_ARG;
+    }
+    if (!A_) { set_error("coefficient not set"); return ST_BAD_ARG; }
+    const int d = g_.dim;
+    const int ns[3] = {g_.n0, g_.n1, g_.n2};
+    for (int a = 0; a < d; ++a) {
+      const int n = cfg_.band[a], gs = ns[3 - d + a];
+      if (gs != n && (n % 2 == 0 || gs < n)) {
+        set_error("potential formulation: a grid larger than the potential grid needs odd N");
+        return ST_BAD_ARG;
+      }
+    }
+    PotParams& pp = pp_;
+    pp.nb[0] = d == 3 ? cfg_.band[0] : 1;
+    pp.nb[1] = cfg_.band[d - 2];
+    pp.nb[2] = cfg_.band[d - 1];
+    pp.nbh = pp.nb[2] / 2 + 1;
+    pp.Yg[0] = d == 3 ? cfg_.Y[0] : 1.0;
+    pp.Yg[1] = cfg_.Y[d - 2];
+    pp.Yg[2] = cfg_.Y[d - 1];
+    pp.scale = (double)g_.M / ((double)pp.nb[0] * pp.nb[1] * pp.nb[2]);
+    pp.zs = 1.0 / ((double)pp.nb[0] * pp.nb[1] * pp.nb[2]);
+    if (!pe_) {
+      FHP_CHECK(cudaMalloc(&pe_, (size_t)g_.L * g_.dv * g_.M * sizeof(R)));
+      const int T = d == 3 ? T0_ : tile_cols(l1_.dev.ld, 1, (long long)g_.n2h);
+      Tfirst_ = T;
+    }
+    return ST_OK;
+  }
+
+  // full inverse transform of S_ into the fields y (1/M)
+  int pot_inv(R* y, bool cg, cudaStream_t s) {
+    const int* ad = cg ? all_done_ : nullptr;
+    const LoadState* st = cg ? st_ : nullptr;
+    const int d = g_.dim;
+    const DevLine<R>& lf = d == 3 ? l0_ : l1_;
+    const long long inner = d == 3 ? (long long)g_.n1 * g_.n2h : (long long)g_.n2h;
+    dim3 grid((unsigned)((inner + Tfirst_ - 1) / Tfirst_), (unsigned)(g_.L * g_.dv));
+    const int pk = pbeg("pot_c2c_first_inv", 2.0 * spec_bytes(), s);
+    k_c2c_axis<R, true><<<grid, kThreads, (size_t)Tfirst_ * lf.dev.ld * sizeof(cplx<R>), s>>>(
+        S_, d == 3 ? g_.n0 : g_.n1, inner, lf.dev, Tfirst_, ad, st, g_.dv);
+    pend(pk, s);
+    FHP_LAUNCHED();
+    return inv_passes(S_, y, (R)(1.0 / (double)g_.M), false, nullptr, cg, s);
+  }
+
+  // full forward transform of A x into S_
+  int pot_fwd(const R* x, bool cg, cudaStream_t s) {
+    const int* ad = cg ? all_done_ : nullptr;
+    const LoadState* st = cg ? st_ : nullptr;
+    int rc = fwd_passes(coef_kind_, false, x, nullptr, nullptr, S_, cg, s);
+    if (rc != ST_OK) return rc;
+    const int d = g_.dim;
+    const DevLine<R>& lf = d == 3 ? l0_ : l1_;
+    const long long inner = d == 3 ? (long long)g_.n1 * g_.n2h : (long long)g_.n2h;
+    dim3 grid((unsigned)((inner + Tfirst_ - 1) / Tfirst_), (unsigned)(g_.L * g_.dv));
+    const int pk = pbeg("pot_c2c_first_fwd", 2.0 * spec_bytes(), s);
+    k_c2c_axis<R, false><<<grid, kThreads, (size_t)Tfirst_ * lf.dev.ld * sizeof(cplx<R>), s>>>(
+        S_, d == 3 ? g_.n0 : g_.n1, inner, lf.dev, Tfirst_, ad, st, g_.dv);
+    pend(pk, s);
+    FHP_LAUNCHED();
+    return ST_OK;
+  }
+
+  // y = P (-div) decrease F A iF enlarge grad P x ; zio: x and y z-scaled
+  int pot_operator(const cplx<R>* x, cplx<R>* y, bool zio, bool cg, cudaStream_t s) {
+    const int* ad = cg ? all_done_ : nullptr;
+    const long long ns = (long long)g_.L * g_.n0 * g_.n1 * g_.n2h;
+    k_pot_expand<R><<<grid_for((size_t)ns), kThreads, 0, s>>>(x, S_, g_, pp_, zio ? 1 : 0, ad);
+    FHP_LAUNCHED();
+    int rc = pot_inv(pe_, cg, s);
+    if (rc == ST_OK) rc = pot_fwd(pe_, cg, s);
+    if (rc != ST_OK) return rc;
+    k_pot_contract<R><<<grid_for((size_t)pot_spectrum_elems()), kThreads, 0, s>>>(
+        S_, y, g_, pp_, -1.0, zio ? 1 : 0, ad);
+    FHP_LAUNCHED();
+    return ST_OK;
+  }
+
+  int pot_rhs(void* bh, cudaStream_t s) override {
+    int rc = pot_check();
+    if (rc != ST_OK) return rc;
+    const size_t n = (size_t)g_.L * g_.dv * g_.M;
+    k_fill_macro<R><<<grid_for(n), kThreads, 0, s>>>(pe_, g_, 1.0);
+    FHP_LAUNCHED();
+    if ((rc = pot_fwd(pe_, false, s)) != ST_OK) return rc;
+    k_pot_contract<R><<<grid_for((size_t)pot_spectrum_elems()), kThreads, 0, s>>>(
+        S_, static_cast<cplx<R>*>(bh), g_, pp_, 1.0, 0, nullptr);
+    FHP_LAUNCHED();
+    return ST_OK;
+  }
+
+  int pot_apply(const void* xh, void* yh, cudaStream_t s) override {
+    int rc = pot_check();
+    if (rc != ST_OK) return rc;
+    return pot_operator(static_cast<const cplx<R>*>(xh), static_cast<cplx<R>*>(yh), false,
+                        false, s);
+  }
+
+  int pot_field(const void* xh, void* X, cudaStream_t s) override {
+    int rc = pot_check();
+    if (rc != ST_OK) return rc;
+    const long long ns = (long long)g_.L * g_.n0 * g_.n1 * g_.n2h;
+    k_pot_expand<R><<<grid_for((size_t)ns), kThreads, 0, s>>>(
+        static_cast<const cplx<R>*>(xh), S_, g_, pp_, 0, nullptr);
+    FHP_LAUNCHED();
+    return pot_inv(static_cast<R*>(X), false, s);
+  }
+
+  // CG (solver.py:80-139) in z = sqrt(w) x / prod(N): the 'r' inner product
+  // (objects.py:618-631) is the Euclidean one of z, so the field CG kernels
+  // run on the z vectors (2 prod(N0 N1 (N2/2+1)) reals per load) with a
+  // unit mean factor.  x0 = 0 (homogenisation.py:59, 96).
+  int pot_cg(const void* bh, double tol, int maxiter, void* xh, SolveResult& res, int log_cap,
+             cudaStream_t s) override {
+    int rc = pot_check();
+    if (rc != ST_OK) return rc;
+    const long long mz = pot_spectrum_elems() / g_.L;  // complex entries per load
+    const size_t nz = (size_t)g_.L * mz;
+    if (!zx_) {
+      FHP_CHECK(cudaMalloc(&zx_, 4 * nz * sizeof(cplx<R>)));
+    }
+    cplx<R>* zx = zx_;
+    cplx<R>* zr = zx_ + nz;
+    cplx<R>* zp = zx_ + 2 * nz;
+    cplx<R>* zap = zx_ + 3 * nz;
+    GridDims gz = g_;
+    gz.dv = 1;
+    gz.M = 2 * mz;
+    R* rx = reinterpret_cast<R*>(zx);
+    R* rr = reinterpret_cast<R*>(zr);
+    R* rp = reinterpret_cast<R*>(zp);
+    R* rap = reinterpret_cast<R*>(zap);
+    FHP_CHECK(cudaMemsetAsync(zx, 0, nz * sizeof(cplx<R>), s));
+    k_pot_zscale<R><<<grid_for(nz), kThreads, 0, s>>>(static_cast<const cplx<R>*>(bh), zr,
+                                                       (long long)nz, pp_, 1);
+    FHP_LAUNCHED();
+    FHP_CHECK(cudaMemcpyAsync(zp, zr, nz * sizeof(cplx<R>), cudaMemcpyDeviceToDevice, s));
+    for (int l = 0; l < g_.L; ++l) {
+      LoadState& h = h_st_[l];
+      std::memset(&h, 0, sizeof(LoadState));
+      h.tol = tol;
+      h.maxiter = maxiter;
+      h.guard = sizeof(R) == 4 ? 4.0 : 0.0;
+    }
+    FHP_CHECK(cudaMemcpyAsync(st_, h_st_, g_.L * sizeof(LoadState), cudaMemcpyHostToDevice, s));
+    FHP_CHECK(cudaMemsetAsync(all_done_, 0, sizeof(int), s));
+    const int log_rows = std::max(1, std::min(log_cap, maxiter + 1));
+    double* dlog = nullptr;
+    FHP_CHECK(cudaMallocAsync(&dlog, (size_t)log_rows * g_.L * sizeof(double), s));
+    FHP_CHECK(cudaMemsetAsync(dlog, 0, (size_t)log_rows * g_.L * sizeof(double), s));
+    k_dot<R><<<red_ctas_, kThreads, 0, s>>>(rr, rr, partials_, gz);
+    FHP_LAUNCHED();
+    k_fin_init<<<1, 32, 0, s>>>(partials_, red_ctas_, st_, g_.L, 1.0, dlog, log_rows);
+    FHP_LAUNCHED();
+    k_update_all_done<<<1, 1, 0, s>>>(st_, g_.L, all_done_);
+    FHP_LAUNCHED();
+    int done_iters = 0, chunk = 2;
+    while (done_iters < maxiter) {
+      FHP_CHECK(cudaMemcpyAsync(h_done_, all_done_, sizeof(int), cudaMemcpyDeviceToHost, s));
+      FHP_CHECK(cudaStreamSynchronize(s));
+      if (*h_done_) break;
+      const int nit = std::min(chunk, maxiter - done_iters);
+      for (int it = 0; it < nit && rc == ST_OK; ++it) {
+        rc = pot_operator(zp, zap, true, true, s);
+        if (rc != ST_OK) break;
+        k_dot<R><<<red_ctas_, kThreads, 0, s>>>(rp, rap, partials_, gz);
+        FHP_LAUNCHED();
+        k_fin_pap<<<g_.L, kThreads, 0, s>>>(partials_, red_ctas_, st_, g_.L, 1.0, all_done_);
+        FHP_LAUNCHED();
+        k_cg_update<R><<<red_ctas_, kThreads, 0, s>>>(rx, rr, rp, rap, partials_, gz, st_,
+                                                      all_done_);
+        FHP_LAUNCHED();
+        k_fin_rr<<<g_.L, kThreads, 0, s>>>(partials_, red_ctas_, st_, g_.L, 1.0, dlog, log_rows,
+                                           all_done_);
+        FHP_LAUNCHED();
+        k_p_update<R><<<grid_for(2 * nz), kThreads, 0, s>>>(rr, rp, gz, st_, all_done_);
+        FHP_LAUNCHED();
+        k_update_all_done<<<1, 1, 0, s>>>(st_, g_.L, all_done_);
+        FHP_LAUNCHED();
+      }
+      if (rc != ST_OK) break;
+      done_iters += nit;
+      chunk = std::min(chunk * 2, 32);
+    }
+    if (rc == ST_OK) {
+      k_pot_zscale<R><<<grid_for(nz), kThreads, 0, s>>>(zx, static_cast<cplx<R>*>(xh),
+                                                         (long long)nz, pp_, 0);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); rc = ST_CUDA; }
+      ++launches;
+    }
+    if (rc != ST_OK) { cudaFreeAsync(dlog, s); return rc; }
+    FHP_CHECK(cudaMemcpyAsync(h_st_, st_, g_.L * sizeof(LoadState), cudaMemcpyDeviceToHost, s));
+    res.res_log.assign((size_t)log_rows * g_.L, 0.0);
+    FHP_CHECK(cudaMemcpyAsync(res.res_log.data(), dlog, (size_t)log_rows * g_.L * sizeof(double),
+                              cudaMemcpyDeviceToHost, s));
+    FHP_CHECK(cudaStreamSynchronize(s));
+    cudaFreeAsync(dlog, s);
+    res.kit.resize(g_.L);
+    res.norm_res.resize(g_.L);
+    res.status.resize(g_.L);
+    res.iterations_run = 0;
+    for (int l = 0; l < g_.L; ++l) {
+      const LoadState& h = h_st_[l];
+      res.kit[l] = h.kit;
+      res.norm_res[l] = h.kit == 0 ? 0.0 : h.norm_res;
+      int sl = h.status;
+      if (sl == 0 && h.norm_res > tol && h.kit > 0) sl = ST_NONCONVERGED;
+      res.status[l] = sl;
+      res.iterations_run = std::max(res.iterations_run, h.kit);
+    }
+    return ST_OK;
+  }
+
   int set_coefficient(int kind, const double* values, bool on_device, cudaStream_t s) override {
     if (kind < COEF_ISO || kind > COEF_FULL) { set_error("bad coefficient kind"); return ST_BAD_ARG; }
     const int dv = g_.dv;
@@ -670,6 +896,10 @@ class Engine final : public EngineBase {
     if (ad_) cudaFree(ad_);
     if (st_) cudaFree(st_);
     if (all_done_) cudaFree(all_done_);
+    if (pe_) cudaFree(pe_);
+    if (zx_) cudaFree(zx_);
+    pe_ = nullptr;
+    zx_ = nullptr;
     if (h_done_) cudaFreeHost(h_done_);
     if (h_st_) cudaFreeHost(h_st_);
     S_ = nullptr; A_ = nullptr; r_ = p_ = ap_ = nullptr;
@@ -1007,6 +1237,11 @@ class Engine final : public EngineBase {
   }
 
   R* x_cur_ = nullptr;  // the caller's solution buffer during cg_solve
+  // potential formulation
+  PotParams pp_{};
+  R* pe_ = nullptr;            // real fields (L, d) + grid
+  cplx<R>* zx_ = nullptr;      // z vectors x, r, p, Ap
+  int Tfirst_ = 1;             // column tile of the first-axis pass
   size_t A_elems_ = 0;   // capacity of A_ in elements
   // band representation
   bool band_ = false;

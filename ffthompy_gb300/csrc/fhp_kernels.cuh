@@ -1602,4 +1602,158 @@ __global__ void k_convert(long long n, const RI* __restrict__ in, RO* __restrict
     out[i] = (RO)in[i];
 }
 
+// ---------------------------------------------------------------------------
+// Potential formulation (ffthompy/tensorsLowRank/homogenisation.py:41-127).
+// The unknown is a scalar potential in the 'r' Fourier form of the grid N
+// (unnormalised half spectrum [load][n0][n1][n2/2+1]); the operator is
+//   P (-div) decrease_N F_Ns A iF_Ns enlarge_Ns grad P,
+// P = 1/|2 pi xi| (1 at the mean), Ns = N (GaNi) or 2N-1 (Ga; N odd).
+// Inside CG the iterates are held as z = sqrt(w) x / prod(N) with w the
+// weight of the 'r' inner product (objects.py:618-631: 1 on the k2 = 0 and
+// even-N Nyquist planes, 2 elsewhere), so that the reference's inner product
+// is the Euclidean one of z and the generic CG kernels apply.
+// ---------------------------------------------------------------------------
+struct PotParams {
+  int nb[3];       // potential grid N (GridDims axis order; nb[0] = 1 in 2D)
+  int nbh;         // nb[2] / 2 + 1
+  double Yg[3];    // cell size per GridDims axis
+  double scale;    // enlargement prod(Ns)/prod(N)
+  double zs;       // 1 / prod(N)
+};
+
+// frequency of index k on an n-point axis in the reference's 'r' form
+// (trigpol.py:27-40): 0..ceil(n/2)-1, then negative; the even-n Nyquist
+// index carries -n/2, also on the half axis
+__device__ __forceinline__ int ref_freq(int k, int n) { return k < (n + 1) / 2 ? k : k - n; }
+
+__device__ __forceinline__ double pot_weight(int k2, int n2) {
+  return (k2 == 0 || 2 * k2 == n2) ? 1.0 : 2.0;
+}
+
+// 2 pi xi per axis and P at frequency q (dim 2: q[0] = 0)
+__device__ __forceinline__ double pot_symbols(const PotParams& pp, int dim, const int* q,
+                                              double* tpx) {
+  const double tp = 6.283185307179586476925286766559;
+  double k2 = 0.;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    tpx[a] = (a == 0 && dim == 2) ? 0. : tp * (double)q[a] / pp.Yg[a];
+    k2 += tpx[a] * tpx[a];
+  }
+  return (q[0] == 0 && q[1] == 0 && q[2] == 0) ? 1.0 : 1.0 / sqrt(k2);
+}
+
+// S[l*d + a] (solve grid half spectrum) = scale * 2 pi i xi_a * P * x_l on the
+// band of N, 0 elsewhere; x natural (zin = 0) or z-scaled (zin = 1)
+template <typename R>
+__global__ void k_pot_expand(const cplx<R>* __restrict__ xin, cplx<R>* __restrict__ S,
+                             GridDims g, PotParams pp, int zin,
+                             const int* __restrict__ all_done) {
+  if (all_done && *all_done) return;
+  const long long Ms = (long long)g.n0 * g.n1 * g.n2h;
+  const long long Mn = (long long)pp.nb[0] * pp.nb[1] * pp.nbh;
+  const long long tot = (long long)g.L * Ms;
+  const int d = g.dim;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += stride) {
+    const int l = (int)(e / Ms);
+    const long long v = e - (long long)l * Ms;
+    const int i2 = (int)(v % g.n2h);
+    const long long r = v / g.n2h;
+    const int i1 = (int)(r % g.n1), i0 = (int)(r / g.n1);
+    const int q[3] = {ref_freq(i0, g.n0), ref_freq(i1, g.n1), ref_freq(i2, g.n2)};
+    const int ns[3] = {g.n0, g.n1, g.n2};
+    bool in = true;
+    int kn[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const int n = pp.nb[a];
+      if (ns[a] != n) in = in && (2 * (q[a] < 0 ? -q[a] : q[a]) < n);
+      kn[a] = q[a] >= 0 ? q[a] : q[a] + n;
+    }
+    cplx<R>* out = S + (long long)(l * d) * Ms + v;
+    if (!in) {
+      for (int a = 0; a < d; ++a) out[(long long)a * Ms] = mkc<R>(R(0), R(0));
+      continue;
+    }
+    const cplx<R> u0 = xin[(long long)l * Mn + ((long long)kn[0] * pp.nb[1] + kn[1]) * pp.nbh + kn[2]];
+    double tpx[3];
+    double f = pot_symbols(pp, d, q, tpx) * pp.scale;
+    if (zin) f /= pp.zs * sqrt(pot_weight(kn[2], pp.nb[2]));
+    const double ux = (double)u0.x * f, uy = (double)u0.y * f;
+    for (int a = 0; a < d; ++a) {
+      const double t = tpx[3 - d + a];
+      out[(long long)a * Ms] = mkc<R>((R)(-t * uy), (R)(t * ux));
+    }
+  }
+}
+
+// y_l (potential grid half spectrum) = sign * P / scale * sum_a 2 pi i xi_a
+// S[l*d + a] read at the band frequencies of the solve grid; y natural
+// (zout = 0) or z-scaled (zout = 1)
+template <typename R>
+__global__ void k_pot_contract(const cplx<R>* __restrict__ S, cplx<R>* __restrict__ y,
+                               GridDims g, PotParams pp, double sign, int zout,
+                               const int* __restrict__ all_done) {
+  if (all_done && *all_done) return;
+  const long long Ms = (long long)g.n0 * g.n1 * g.n2h;
+  const long long Mn = (long long)pp.nb[0] * pp.nb[1] * pp.nbh;
+  const long long tot = (long long)g.L * Mn;
+  const int d = g.dim;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += stride) {
+    const int l = (int)(e / Mn);
+    const long long v = e - (long long)l * Mn;
+    const int k2 = (int)(v % pp.nbh);
+    const long long r = v / pp.nbh;
+    const int k1 = (int)(r % pp.nb[1]), k0 = (int)(r / pp.nb[1]);
+    const int q[3] = {ref_freq(k0, pp.nb[0]), ref_freq(k1, pp.nb[1]), ref_freq(k2, pp.nb[2])};
+    const int ns[3] = {g.n0, g.n1, g.n2};
+    int ks[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) ks[a] = q[a] >= 0 ? q[a] : q[a] + ns[a];
+    const long long sv = ((long long)ks[0] * g.n1 + ks[1]) * g.n2h + ks[2];
+    double tpx[3];
+    double f = sign * pot_symbols(pp, d, q, tpx) / pp.scale;
+    if (zout) f *= pp.zs * sqrt(pot_weight(k2, pp.nb[2]));
+    double ax = 0., ay = 0.;
+    for (int a = 0; a < d; ++a) {
+      const cplx<R> s = S[(long long)(l * d + a) * Ms + sv];
+      const double t = tpx[3 - d + a];
+      ax -= t * (double)s.y;
+      ay += t * (double)s.x;
+    }
+    y[(long long)l * Mn + v] = mkc<R>((R)(f * ax), (R)(f * ay));
+  }
+}
+
+// natural <-> z scaling of potential spectra (to_z: z = zs sqrt(w) x)
+template <typename R>
+__global__ void k_pot_zscale(const cplx<R>* __restrict__ in, cplx<R>* __restrict__ out,
+                             long long tot, PotParams pp, int to_z) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += stride) {
+    const int k2 = (int)(e % pp.nbh);
+    const double w = pp.zs * sqrt(pot_weight(k2, pp.nb[2]));
+    const double f = to_z ? w : 1.0 / w;
+    const cplx<R> u = in[e];
+    out[e] = mkc<R>((R)(f * (double)u.x), (R)(f * (double)u.y));
+  }
+}
+
+// P = R + beta P for the active loads (solver.py:131)
+template <typename R>
+__global__ void k_p_update(const R* __restrict__ r, R* __restrict__ p, GridDims g,
+                           const LoadState* __restrict__ st, const int* __restrict__ all_done) {
+  if (all_done && *all_done) return;
+  const long long per = (long long)g.dv * g.M;
+  const long long tot = (long long)g.L * per;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += stride) {
+    const int l = (int)(i / per);
+    if (st[l].done) continue;
+    p[i] = r[i] + (R)st[l].beta * p[i];
+  }
+}
+
 }  // namespace fhp

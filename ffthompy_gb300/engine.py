@@ -310,6 +310,67 @@ class GalerkinPlan:
                    'fhp_fourier_interp')
         return y
 
+    # -- potential formulation (tensorsLowRank/homogenisation.py:41-127) -------
+    @property
+    def potential_shape(self):
+        """(loads,) + the 'r' half-spectrum shape of the band grid N."""
+        return (self.nloads,) + self.band[:-1] + (self.band[-1] // 2 + 1,)
+
+    def _cdev(self, x):
+        cdt = torch.complex64 if self.precision == 'f32' else torch.complex128
+        if not isinstance(x, torch.Tensor):
+            x = torch.as_tensor(np.asarray(x))
+        x = x.to(device=self.device, dtype=cdt).contiguous()
+        if tuple(x.shape) != self.potential_shape:
+            x = x.reshape(self.potential_shape)
+        return x
+
+    def _cempty(self):
+        cdt = torch.complex64 if self.precision == 'f32' else torch.complex128
+        return torch.empty(self.potential_shape, dtype=cdt, device=self.device)
+
+    def potential_rhs(self):
+        """P B per load, B_l = div(decrease_N F(A E_l)) (homogenisation.py:58, 95)."""
+        b = self._cempty()
+        _lib.check(self.lib.fhp_potential_rhs(self.handle, self._ptr(b), self._stream()),
+                   'fhp_potential_rhs')
+        return b
+
+    def potential_apply(self, x):
+        """PDFAFGPfun(x) per load (homogenisation.py:50-65, 88-101)."""
+        x = self._cdev(x)
+        y = self._cempty()
+        _lib.check(self.lib.fhp_potential_apply(self.handle, self._ptr(x), self._ptr(y),
+                                                self._stream()), 'fhp_potential_apply')
+        return y
+
+    def potential_cg(self, b, tol=1e-6, maxiter=1000, log_rows=None):
+        """CG from 0 with the 'r' Fourier inner product; returns (iPU, info)."""
+        b = self._cdev(b)
+        x = self._cempty()
+        L = self.nloads
+        kit = (ctypes.c_int * L)()
+        nres = (ctypes.c_double * L)()
+        stat = (ctypes.c_int * L)()
+        maxiter = int(maxiter)
+        rows = int(log_rows if log_rows is not None else min(maxiter + 1, 100001))
+        log = np.zeros((rows, L))
+        _lib.check(self.lib.fhp_potential_cg(self.handle, self._ptr(b), float(tol), maxiter,
+                                             self._ptr(x), kit, nres, stat,
+                                             log.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                             rows, self._stream()), 'fhp_potential_cg')
+        kits = list(kit)
+        return x, {'kit': kits, 'norm_res': list(nres), 'status': list(stat),
+                   'res_log': [log[:k + 1, l].copy() for l, k in enumerate(kits)]}
+
+    def potential_field(self, x):
+        """X = iF(enlarge(grad(P x))) as this plan's fields (loads, dim) + N."""
+        x = self._cdev(x)
+        X = self.empty()
+        _lib.check(self.lib.fhp_potential_field(self.handle, self._ptr(x), self._ptr(X),
+                                                self._stream()), 'fhp_potential_field')
+        return X
+
     def homogenize_host(self, A=None, proj=1, tol=1e-6, maxiter=1000, return_solution=False,
                         packed=None, kind=None):
         """End to end with host buffers: coefficient in, A_H out (fhp_homogenize_host).

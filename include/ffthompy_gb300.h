@@ -165,6 +165,38 @@ int fhp_homogenize_host(fhp_plan plan, int proj, int coef_kind, const double* co
                         double* norm_res_host, void* x_host, void* stream);
 
 /*
+ * Potential formulation with the 1/|xi| preconditioner (scalar physics; plans
+ * created by fhp_plan_create, not the band variant).  The unknown is a scalar
+ * potential per load in the 'r' Fourier form of the plan's band grid N
+ * (n_band): unnormalised half spectra [load][N0][N1][N2/2+1] of complex
+ * values (interleaved re/im) of the plan's element type, device pointers.
+ * The solve grid n is N (GaNi) or any larger grid with N odd (Ga: 2N-1), on
+ * which the coefficient lives.  P = 1/|2 pi xi| (1 at the mean).
+ *
+ * fhp_potential_rhs: bh_l = P div(decrease_N F(A E_l)), E_l = unit vector l.
+ *   Replaces: P*B of homog_GaNi_full_potential / homog_Ga_full_potential
+ *   (ffthompy/tensorsLowRank/homogenisation.py:58-65, 95-101, 296-300).
+ * fhp_potential_apply: yh = P (-div) decrease_N F(A iF(enlarge_n(grad(P xh)))).
+ *   Replaces: PDFAFGPfun (homogenisation.py:50-65, 88-101).
+ * fhp_potential_cg: CG from x0 = 0 on the preconditioned system with the
+ *   'r' Fourier inner product (ffthompy/tensors/objects.py:618-631); per-load
+ *   kit / norm_res / status and a residual log (log_rows x loads, host) as
+ *   fhp_cg_solve.  xh receives iPU; the potential is Fu = P iPU.
+ *   Replaces: linear_solver(solver='CG', Afun=PDFAFGPfun, B=PB, x0=0)
+ *   (homogenisation.py:66-69, 104-106; ffthompy/general/solver.py:80-139).
+ * fhp_potential_field: X = iF(enlarge_n(grad(P xh))) as plan fields
+ *   [load][dim][n...]; A_H then follows from fhp_energy_matrix(add_macro=1).
+ *   Replaces: X = iF2(grad(Fu).project(Nbar)) / iF(grad(Fu)) and
+ *   AH = A(X+E)*(X+E) (homogenisation.py:74-79, 114-125).
+ */
+int fhp_potential_rhs(fhp_plan plan, void* bh, void* stream);
+int fhp_potential_apply(fhp_plan plan, const void* xh, void* yh, void* stream);
+int fhp_potential_cg(fhp_plan plan, const void* bh, double tol, int maxiter, void* xh, int* kit,
+                     double* norm_res, int* status, double* res_log, int log_rows,
+                     void* stream);
+int fhp_potential_field(fhp_plan plan, const void* xh, void* X, void* stream);
+
+/*
  * Plain FFT plan of ncomp real fields on grid n (no physics): used for
  * coefficient assembly.  Fields are [ncomp][n0][n1][n2].
  */
