@@ -256,15 +256,60 @@ __device__ __forceinline__ void dft16(cplx<R>* v) {
   }
 }
 
+// cos(2 pi m / r) and sin(2 pi m / r), m = 1 .. (r-1)/2, of the odd prime
+// radices (evaluated in 50-digit decimal arithmetic from Machin's pi and
+// the Taylor series), so the DFT_r constants are immediates, not table loads.
+template <int RAD>
+__host__ __device__ constexpr double odd_root_cos(int m) {
+  if constexpr (RAD == 7) {
+    constexpr double t[3] = {6.234898018587335305250e-1, -2.225209339563144042889e-1, -9.009688679024191262361e-1};
+    return t[m - 1];
+  }
+  if constexpr (RAD == 11) {
+    constexpr double t[5] = {8.412535328311811688618e-1, 4.154150130018864255293e-1, -1.423148382732851404438e-1, -6.548607339452850640569e-1, -9.594929736144973898904e-1};
+    return t[m - 1];
+  }
+  if constexpr (RAD == 13) {
+    constexpr double t[6] = {8.854560256532098959004e-1, 5.680647467311558025118e-1, 1.205366802553230533491e-1, -3.546048870425356259696e-1, -7.485107481711010986346e-1, -9.709418174260520271570e-1};
+    return t[m - 1];
+  }
+  if constexpr (RAD == 17) {
+    constexpr double t[8] = {9.324722294043558045731e-1, 7.390089172206591159245e-1, 4.457383557765382673965e-1, 9.226835946330199523965e-2, -2.736629900720828635391e-1, -6.026346363792563891786e-1, -8.502171357296141521341e-1, -9.829730996839017782819e-1};
+    return t[m - 1];
+  }
+  return 0.0;
+}
+template <int RAD>
+__host__ __device__ constexpr double odd_root_sin(int m) {
+  if constexpr (RAD == 7) {
+    constexpr double t[3] = {7.818314824680298087084e-1, 9.749279121818236070181e-1, 4.338837391175581204758e-1};
+    return t[m - 1];
+  }
+  if constexpr (RAD == 11) {
+    constexpr double t[5] = {5.406408174555975821076e-1, 9.096319953545183714117e-1, 9.898214418809327323761e-1, 7.557495743542582837740e-1, 2.817325568414296977114e-1};
+    return t[m - 1];
+  }
+  if constexpr (RAD == 13) {
+    constexpr double t[6] = {4.647231720437685456560e-1, 8.229838658936563945796e-1, 9.927088740980539928008e-1, 9.350162426854148234398e-1, 6.631226582407952023768e-1, 2.393156642875577671488e-1};
+    return t[m - 1];
+  }
+  if constexpr (RAD == 17) {
+    constexpr double t[8] = {3.612416661871529487447e-1, 6.736956436465572117127e-1, 8.951632913550623220670e-1, 9.957341762950345218712e-1, 9.618256431728190704088e-1, 7.980172272802395033328e-1, 5.264321628773558002446e-1, 1.837495178165703315744e-1};
+    return t[m - 1];
+  }
+  return 0.0;
+}
+
 // Odd prime radix, symmetric-pair form, in place: v[j] <- v[j] + v[r-j] and
 // v[r-j] <- v[j] - v[r-j] for j <= (r-1)/2, then the outputs pair up as
 // y_k = a_k - i b_k, y_{r-k} = a_k + i b_k with a_k = x0 + sum_j cos(2pi jk/r) s_j,
-// b_k = sum_j sin(2pi jk/r) d_j.  Roots W_r^m = tw[m * nf / r] (cos, -sin).
+// b_k = sum_j sin(2pi jk/r) d_j, with the constants of odd_root_cos/sin.
 // Only the r input registers and two accumulators stay live.
 template <typename R, int RAD>
 __device__ __forceinline__ void dft_odd(cplx<R>* v, const cplx<R>* __restrict__ tw, int nf) {
   constexpr int H = (RAD - 1) / 2;
-  const int step = nf / RAD;
+  (void)tw;
+  (void)nf;
 #pragma unroll
   for (int j = 1; j <= H; ++j) {
     const cplx<R> a = v[j], b = v[RAD - j];
@@ -284,11 +329,14 @@ __device__ __forceinline__ void dft_odd(cplx<R>* v, const cplx<R>* __restrict__ 
     cplx<R> b = mkc<R>(R(0), R(0));
 #pragma unroll
     for (int j = 1; j <= H; ++j) {
-      const cplx<R> w = tw[((j * k) % RAD) * step];
-      a.x += w.x * v[j].x;
-      a.y += w.x * v[j].y;
-      b.x -= w.y * v[RAD - j].x;
-      b.y -= w.y * v[RAD - j].y;
+      // m = jk mod r folded into 1..H: cos is even, sin odd about r/2
+      const int m = (j * k) % RAD;
+      const R c = (R)odd_root_cos<RAD>(m <= H ? m : RAD - m);
+      const R sn = m <= H ? (R)odd_root_sin<RAD>(m) : -(R)odd_root_sin<RAD>(RAD - m);
+      a.x += c * v[j].x;
+      a.y += c * v[j].y;
+      b.x += sn * v[RAD - j].x;
+      b.y += sn * v[RAD - j].y;
     }
     ak[k - 1] = a;
     bk[k - 1] = b;

@@ -1006,6 +1006,27 @@ __device__ __forceinline__ cplx<R> band_down_value(const cplx<R>* line, const Li
   return get_fwd<R>(line, L, q < 0 ? q + nb : q);
 }
 
+// Visits every (tile line c < nlc, line index k < n, column t < T) of a
+// column tile once.  When T divides the block, a thread keeps one column t and
+// walks k with a fixed stride, so no index is divided per element and the
+// per-line bases are loop invariants; body(c, k, t).
+template <typename F>
+__device__ __forceinline__ void tile_loop(int nlc, int n, int T, int lgT, F&& body) {
+  if (T <= (int)blockDim.x) {
+    const int t = threadIdx.x & (T - 1);
+    const int kst = (int)blockDim.x >> lgT;
+    const int k0 = (int)threadIdx.x >> lgT;
+    for (int c = 0; c < nlc; ++c)
+      for (int k = k0; k < n; k += kst) body(c, k, t);
+  } else {
+    for (int e = threadIdx.x; e < nlc * n * T; e += blockDim.x) {
+      const int t = e & (T - 1), rest = e >> lgT;
+      const int c = rest / n, k = rest - c * n;
+      body(c, k, t);
+    }
+  }
+}
+
 template <typename R, int MODE, int PHYS>
 __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_axis(const cplx<R>* __restrict__ Sin,
                                                    cplx<R>* __restrict__ Sout, const __grid_constant__ GridDims g,
@@ -1032,41 +1053,33 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_axis(const cplx<
   const int lgT = __ffs(T) - 1;  // T is a power of two
   if constexpr (MODE == BAND_PAD) {
     // input already in frequency (N layout): pad straight into the B line
-    for (int e = threadIdx.x; e < nl * ax.n_out; e += blockDim.x) {
-      const int t = e & (T - 1);
-      const int rest = e >> lgT;
-      const int c = fdiv(rest, ax.dn_out);
-      const int k = rest - c * ax.n_out;
+    // raw values go straight to the inverse-input slots (plain async copies
+    // inside the band; the halved Nyquist entry and zeros by ordinary stores)
+    tile_loop(1, ax.n_out, T, lgT, [&](int, int k, int t) {
       const long long col = t0 + t;
       const int q = signed_freq(k, ax.n_out);
       const int aq = q < 0 ? -q : q;
-      // raw values go straight to the inverse-input slots (plain async copies
-      // inside the band; the halved Nyquist entry and zeros by ordinary stores)
-      cplx<R>* slot = buf2 + (c * T + t) * ld2 + slot_inv<R>(L2, k);
-      const cplx<R>* src = Sin + (((long long)(c0 + c) * ax.mid + m) * ax.n_in) * ax.inner;
+      cplx<R>* slot = buf2 + t * ld2 + slot_inv<R>(L2, k);
+      const cplx<R>* src = Sin + (((long long)c0 * ax.mid + m) * ax.n_in) * ax.inner + col;
       if (col < ax.inner && 2 * aq < ax.n_in) {
-        cp_async_cplx<R>(slot, src + (long long)(q < 0 ? q + ax.n_in : q) * ax.inner + col);
+        cp_async_cplx<R>(slot, src + (long long)(q < 0 ? q + ax.n_in : q) * ax.inner);
       } else if (col < ax.inner && 2 * aq == ax.n_in) {
-        *slot = cscale<R>(src[(long long)aq * ax.inner + col], R(0.5));
+        *slot = cscale<R>(src[(long long)aq * ax.inner], R(0.5));
       } else {
         *slot = mkc<R>(R(0), R(0));
       }
-    }
+    });
     cp_async_commit();
     cp_async_wait<0>();
   } else {
     // load: [comp][mid][n_in][inner]
-    for (int e = threadIdx.x; e < nl * ax.n_in; e += blockDim.x) {
-      const int t = e & (T - 1);
-      const int rest = e >> lgT;
-      const int c = fdiv(rest, ax.dn_in);
-      const int i = rest - c * ax.n_in;
+    tile_loop(nlc, ax.n_in, T, lgT, [&](int c, int i, int t) {
       const long long col = t0 + t;
-      const cplx<R>* src = Sin + (((long long)(c0 + c) * ax.mid + m) * ax.n_in) * ax.inner;
+      const cplx<R>* src = Sin + (((long long)(c0 + c) * ax.mid + m) * ax.n_in) * ax.inner + col;
       cplx<R>* slot = buf1 + (c * T + t) * ld1 + slot_fwd<R>(L1, i);
-      if (col < ax.inner) cp_async_cplx<R>(slot, src + (long long)i * ax.inner + col);
+      if (col < ax.inner) cp_async_cplx<R>(slot, src + (long long)i * ax.inner);
       else *slot = mkc<R>(R(0), R(0));
-    }
+    });
     cp_async_commit();
     zero_tail<R>(buf1, ld1, nl, L1);
     cp_async_wait<0>();
@@ -1106,16 +1119,18 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_axis(const cplx<
       }
     }
     // the remaining B frequencies are zero
-    for (int e = threadIdx.x; e < nl * ax.n_out; e += blockDim.x) {
-      const int line = fdiv(e, ax.dn_out), k = e - line * ax.n_out;
-      const int q = signed_freq(k, ax.n_out);
-      if (2 * (q < 0 ? -q : q) >= ax.n_in) put_inv<R>(buf2 + line * ld2, L2, k, mkc<R>(R(0), R(0)));
+    {
+      // out-of-band frequencies only (2|q| >= n_in): k in [kb, n_out - kb]
+      const int kb = (ax.n_in + 1) / 2, ke = ax.n_out - kb + 1;
+      tile_loop(nlc, ke - kb, T, lgT, [&](int c, int kk, int t) {
+        put_inv<R>(buf2 + (c * T + t) * ld2, L2, kb + kk, mkc<R>(R(0), R(0)));
+      });
     }
   }
   if constexpr (MODE == BAND_UP || MODE == BAND_UP_PROJ || MODE == BAND_PAD) {
     if constexpr (MODE == BAND_UP) {
-    for (int e = threadIdx.x; e < nl * ax.n_out; e += blockDim.x) {
-      const int line = fdiv(e, ax.dn_out), k = e - line * ax.n_out;
+    tile_loop(nlc, ax.n_out, T, lgT, [&](int c, int k, int t) {
+      const int line = c * T + t;
       const int q = signed_freq(k, ax.n_out);
       const int aq = q < 0 ? -q : q;
       cplx<R> v = mkc<R>(R(0), R(0));
@@ -1125,35 +1140,27 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_axis(const cplx<
         v = cscale<R>(get_fwd<R>(buf1 + line * ld1, L1, aq), R(0.5));
       }
       put_inv<R>(buf2 + line * ld2, L2, k, v);
-    }
+    });
     }
     __syncthreads();
     if constexpr (MODE == BAND_PAD) blue_fixup<R, true>(buf2, ld2, nl, L2);
     zero_tail<R>(buf2, ld2, nl, L2);
     __syncthreads();
     line_core<R>(buf2, ld2, nl, L2, true);
-    for (int e = threadIdx.x; e < nl * ax.n_out; e += blockDim.x) {
-      const int t = e & (T - 1);
-      const int rest = e >> lgT;
-      const int c = fdiv(rest, ax.dn_out);
-      const int i = rest - c * ax.n_out;
+    tile_loop(nlc, ax.n_out, T, lgT, [&](int c, int i, int t) {
       const long long col = t0 + t;
-      if (col >= ax.inner) continue;
-      cplx<R>* dst = Sout + (((long long)(c0 + c) * ax.mid + m) * ax.n_out) * ax.inner;
-      dst[(long long)i * ax.inner + col] = get_inv<R>(buf2 + (c * T + t) * ld2, L2, i);
-    }
+      if (col >= ax.inner) return;
+      cplx<R>* dst = Sout + (((long long)(c0 + c) * ax.mid + m) * ax.n_out) * ax.inner + col;
+      dst[(long long)i * ax.inner] = get_inv<R>(buf2 + (c * T + t) * ld2, L2, i);
+    });
   } else if constexpr (MODE == BAND_DOWN) {
-    for (int e = threadIdx.x; e < nl * ax.n_out; e += blockDim.x) {
-      const int t = e & (T - 1);
-      const int rest = e >> lgT;
-      const int c = fdiv(rest, ax.dn_out);
-      const int k = rest - c * ax.n_out;
+    tile_loop(nlc, ax.n_out, T, lgT, [&](int c, int k, int t) {
       const long long col = t0 + t;
-      if (col >= ax.inner) continue;
+      if (col >= ax.inner) return;
       const cplx<R> v = band_down_value<R>(buf1 + (c * T + t) * ld1, L1, k, ax.n_out, ax.n_in);
-      cplx<R>* dst = Sout + (((long long)(c0 + c) * ax.mid + m) * ax.n_out) * ax.inner;
-      dst[(long long)k * ax.inner + col] = v;
-    }
+      cplx<R>* dst = Sout + (((long long)(c0 + c) * ax.mid + m) * ax.n_out) * ax.inner + col;
+      dst[(long long)k * ax.inner] = v;
+    });
   } else {
     // G(xi) on the band, then inverse DFT_N along the line
     for (int e = threadIdx.x; e < T * ax.n_out; e += blockDim.x) {
@@ -1176,16 +1183,12 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_axis(const cplx<
     zero_tail<R>(buf2, ld2, nl, L2);
     __syncthreads();
     line_core<R>(buf2, ld2, nl, L2, true);
-    for (int e = threadIdx.x; e < nl * ax.n_out; e += blockDim.x) {
-      const int t = e & (T - 1);
-      const int rest = e >> lgT;
-      const int c = fdiv(rest, ax.dn_out);
-      const int i = rest - c * ax.n_out;
+    tile_loop(nlc, ax.n_out, T, lgT, [&](int c, int i, int t) {
       const long long col = t0 + t;
-      if (col >= ax.inner) continue;
-      cplx<R>* dst = Sout + (((long long)(c0 + c) * ax.mid + m) * ax.n_out) * ax.inner;
-      dst[(long long)i * ax.inner + col] = get_inv<R>(buf2 + (c * T + t) * ld2, L2, i);
-    }
+      if (col >= ax.inner) return;
+      cplx<R>* dst = Sout + (((long long)(c0 + c) * ax.mid + m) * ax.n_out) * ax.inner + col;
+      dst[(long long)i * ax.inner] = get_inv<R>(buf2 + (c * T + t) * ld2, L2, i);
+    });
   }
 }
 
