@@ -774,9 +774,10 @@ class Engine final : public EngineBase {
     return (unsigned)std::max<size_t>(1, std::min<size_t>(b, 65535 * 4));
   }
 
-  int tile_cols(int nf, int lines_per_col, long long inner) const {
+  int tile_cols(int nf, int lines_per_col, long long inner,
+                int target = kTargetElems) const {
     const size_t per = (size_t)lines_per_col * nf * sizeof(cplx<R>);
-    int T = std::max(1, kTargetElems / (lines_per_col * nf));
+    int T = std::max(1, target / (lines_per_col * nf));
     T = std::min(T, 32);
     T = (int)std::min<size_t>(T, std::max<size_t>(1, kSmemBudget / per));
     T = (int)std::min<long long>(T, inner);
@@ -997,7 +998,11 @@ class Engine final : public EngineBase {
     const bool projm = mode == BAND_DOWN_PROJ || mode == BAND_UP_PROJ;
     const int nlc = projm ? g_.dv : 1;
     const int nf = (mode == BAND_PAD ? 0 : L1.ld) + (mode == BAND_DOWN ? 0 : L2.ld);
-    const int T = tile_cols(nf, nlc, ax.inner);
+    // twice the usual line target: the axis passes are bound by instruction
+    // issue, and more columns per CTA fill the radix stages of every line
+    // length (and lengthen the contiguous rows); the register file still
+    // allows two CTAs per SM
+    const int T = tile_cols(nf, nlc, ax.inner, 2 * kTargetElems);
     const size_t smem = (size_t)nlc * T * nf * sizeof(cplx<R>);
     if (smem > kSmemMax) { set_error("band line too long for shared memory"); return ST_BAD_ARG; }
     const int outer = projm ? g_.L : g_.L * g_.dv;

@@ -318,21 +318,23 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_r2c_last(
   __syncthreads();
   line_core<R>(buf, ld, rows * np, L, false);
   // split the paired spectra: Xa = (Z_k + conj Z_{n-k})/2, Xb = (Z_k - conj Z_{n-k})/(2i)
+  // (one warp per pair line, lanes over k: coalesced stores, no division per element)
   const int n2h = g.n2h;
-  const int otasks = rows * np * n2h;
-  for (int e = threadIdx.x; e < otasks; e += blockDim.x) {
-    const int line = fdiv(e, g.dn2h), k = e - line * n2h;
+  const int lane = threadIdx.x & 31;
+  for (int line = threadIdx.x >> 5; line < rows * np; line += blockDim.x >> 5) {
     const int rl = fdiv(line, g.dnp), p = line - rl * np;
     const long long row = row0 + rl;
     if (row >= nrows) continue;
     const cplx<R>* lp = buf + (long long)line * ld;
-    const cplx<R> zk = get_fwd<R>(lp, L, k);
-    const cplx<R> zm = get_fwd<R>(lp, L, k == 0 ? 0 : n - k);
-    const cplx<R> xa = mkc<R>(R(0.5) * (zk.x + zm.x), R(0.5) * (zk.y - zm.y));
-    const cplx<R> xb = mkc<R>(R(0.5) * (zk.y + zm.y), R(0.5) * (zm.x - zk.x));
     const int ca = 2 * p, cb = 2 * p + 1;
-    S[((long long)ca * nrows + row) * n2h + k] = xa;
-    if (cb < C) S[((long long)cb * nrows + row) * n2h + k] = xb;
+    cplx<R>* da = S + ((long long)ca * nrows + row) * n2h;
+    cplx<R>* db = S + ((long long)cb * nrows + row) * n2h;
+    for (int k = lane; k < n2h; k += 32) {
+      const cplx<R> zk = get_fwd<R>(lp, L, k);
+      const cplx<R> zm = get_fwd<R>(lp, L, k == 0 ? 0 : n - k);
+      da[k] = mkc<R>(R(0.5) * (zk.x + zm.x), R(0.5) * (zk.y - zm.y));
+      if (cb < C) db[k] = mkc<R>(R(0.5) * (zk.y + zm.y), R(0.5) * (zm.x - zk.x));
+    }
   }
 }
 
@@ -497,28 +499,29 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_c2r_last(const cplx<R
     cp_async_wait<0>();
     __syncthreads();
   }
-  const int tasks = rows * np * n2h;
-  for (int e = threadIdx.x; e < tasks; e += blockDim.x) {
-    const int line = fdiv(e, g.dn2h), k = e - line * n2h;
+  // one warp per pair line, lanes over k (no division per element)
+  for (int line = threadIdx.x >> 5; line < rows * np; line += blockDim.x >> 5) {
     const int rl = fdiv(line, g.dnp), p = line - rl * np;
     const long long row = row0 + rl;
     cplx<R>* lp = buf + (long long)line * ld;
-    cplx<R> a = mkc<R>(R(0), R(0)), b = mkc<R>(R(0), R(0));
-    if (row < nrows) {
-      const int ca = 2 * p, cb = 2 * p + 1;
-      if (stage) {
-        a = sraw[((size_t)ca * rows + rl) * n2h + k];
-        if (cb < C) b = sraw[((size_t)cb * rows + rl) * n2h + k];
-      } else {
-        a = S[((long long)ca * nrows + row) * n2h + k];
-        if (cb < C) b = S[((long long)cb * nrows + row) * n2h + k];
+    const int ca = 2 * p, cb = 2 * p + 1;
+    const bool valid = row < nrows;
+    const cplx<R>* sa = stage ? sraw + ((size_t)ca * rows + rl) * n2h
+                              : S + ((long long)ca * nrows + row) * n2h;
+    const cplx<R>* sb = stage ? sraw + ((size_t)cb * rows + rl) * n2h
+                              : S + ((long long)cb * nrows + row) * n2h;
+    for (int k = (int)(threadIdx.x & 31); k < n2h; k += 32) {
+      cplx<R> a = mkc<R>(R(0), R(0)), b = mkc<R>(R(0), R(0));
+      if (valid) {
+        a = sa[k];
+        if (cb < C) b = sb[k];
       }
+      const bool selfconj = (k == 0) || (2 * k == n);
+      if (selfconj) { a.y = R(0); b.y = R(0); }
+      // Z_k = A + iB ; Z_{n-k} = conj(A) + i conj(B)
+      put_inv<R>(lp, L, k, mkc<R>(a.x - b.y, a.y + b.x));
+      if (!selfconj) put_inv<R>(lp, L, n - k, mkc<R>(a.x + b.y, b.x - a.y));
     }
-    const bool selfconj = (k == 0) || (2 * k == n);
-    if (selfconj) { a.y = R(0); b.y = R(0); }
-    // Z_k = A + iB ; Z_{n-k} = conj(A) + i conj(B)
-    put_inv<R>(lp, L, k, mkc<R>(a.x - b.y, a.y + b.x));
-    if (!selfconj) put_inv<R>(lp, L, n - k, mkc<R>(a.x + b.y, b.x - a.y));
   }
   zero_tail<R>(buf, ld, rows * np, L);
   __syncthreads();

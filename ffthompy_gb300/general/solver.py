@@ -5,7 +5,10 @@ linear_solver(Afun, B, ATfun, x0, par, solver, callback) -> (x, info)
 the whole solve runs on the GPU in one library call (fhp_cg_solve: batched
 CG with FP64 reductions, absolute stopping test sqrt(<R,R>) <= tol,
 solver.py:80-139).  Other operators use the same CG recurrence written with
-Tensor arithmetic on the device.
+Tensor arithmetic on the device.  'richardson' / 'iterative' (63-77),
+'bicg' (142-204) and 'chebyshev' (206-285) run their recurrences with device
+Tensor arithmetic around the fused operator, one library call per
+application.
 """
 import time
 
@@ -33,6 +36,11 @@ def linear_solver(Afun, B, ATfun=None, x0=None, par=None, solver=None, callback=
         x, info = CG(Afun, B, x0=x0, par=par, callback=callback)
     elif kind in ('iterative', 'richardson'):
         x, info = richardson(Afun, B, x0, par=par, callback=callback)
+    elif kind == 'bicg':
+        x, info = BiCG(Afun, ATfun if ATfun is not None else Afun, B, x0, par=par,
+                       callback=callback)
+    elif kind in ('chebyshev', 'cheby'):
+        x, info = cheby2TERM(Afun, B, x0, par=par, callback=callback)
     else:
         raise NotImplementedError('This kind (%s) of linear solver is not implemented' % solver)
     t1 = (time.process_time(), time.perf_counter(), time.time())
@@ -97,4 +105,84 @@ def richardson(Afun, B, x0, par=None, callback=None):
         res['norm_res'] = residuum.norm()
         if callback is not None:
             callback(x)
+    return x, res
+
+
+def BiCG(Afun, ATfun, B, x0, par=None, callback=None):
+    """BiConjugate gradients, solver.py:142-204 (shadow residual updated with
+    ATfun, stop on sqrt(<R, Rs>) <= tol).  The reference forms <R, Rs> as
+    R.T*Rs, which its Tensor class does not support; here it is the scalar
+    product.  Each Afun / ATfun application of a fused Operator is one call
+    into the CUDA library; the vector updates are device Tensor arithmetic."""
+    par = _defaults(par)
+    scal = par.get('scal', lambda X, Y: X * Y)
+    x = x0
+    R = B - Afun(x0)
+    Rs = R
+    rr = float(scal(R, Rs))
+    P, Ps = R, Rs
+    res = {'kit': 0, 'norm_res': rr ** 0.5}
+    while res['norm_res'] > par['tol'] and res['kit'] < par['maxiter']:
+        res['kit'] += 1
+        AP = Afun(P)
+        alp = rr / float(scal(AP, Ps))
+        x = x + alp * P
+        R = R - alp * AP
+        Rs = Rs - alp * ATfun(Ps)
+        rrnext = float(scal(R, Rs))
+        bet = rrnext / rr
+        rr = rrnext
+        P = R + bet * P
+        Ps = Rs + bet * Ps
+        res['norm_res'] = rr ** 0.5
+        if callback is not None:
+            callback(x)
+    if res['kit'] == 0:
+        res['norm_res'] = 0
+    return x, res
+
+
+def cheby2TERM(A, B, x0, M=None, par=None, callback=None):
+    """Chebyshev two-term iteration, solver.py:206-285: par['eigrange'] is
+    the eigenvalue interval, par['maxit'] the iteration limit (default 1e7),
+    norm_res the residual norm relative to the initial one."""
+    par = {} if par is None else par
+    par.setdefault('tol', 1e-06)
+    par.setdefault('maxit', 1e7)
+    if 'eigrange' not in par:
+        raise NotImplementedError('It is necessary to calculate eigenvalues.')
+    Egv = par['eigrange']
+    res = {'kit': 0}
+    bnrm2 = float(B * B) ** 0.5
+    Ib = 1.0 / bnrm2
+    x = x0
+    r = B - A(x)
+    r0 = np.double(r * r) ** 0.5
+    res['norm_res'] = Ib * r0
+    if res['norm_res'] < par['tol']:
+        return x, res
+    d = (Egv[1] + Egv[0]) / 2.0
+    c = (Egv[1] - Egv[0]) / 2.0
+    v = 0 * x0
+    w = 0.
+    while res['norm_res'] > par['tol'] and res['kit'] < par['maxit']:
+        res['kit'] += 1
+        x_prev = x
+        if res['kit'] == 1:
+            p = 0.
+            w = 1 / d
+        elif res['kit'] == 2:
+            p = -(1 / 2) * (c / d) * (c / d)
+            w = 1 / (d - c * c / 2 / d)
+        else:
+            p = -(c * c / 4) * w * w
+            w = 1 / (d - c * c * w / 4)
+        v = r - p * v
+        x = x_prev + w * v
+        r = B - A(x)
+        res['norm_res'] = (1.0 / r0) * r.norm()
+        if callback is not None:
+            callback(x)
+    if res['kit'] == 0:
+        res['norm_res'] = 0
     return x, res

@@ -23,7 +23,7 @@ __all__ = [
     'freq_ints', 'coordinates', 'projection_scalar', 'projection_elasticity',
     'green_operator', 'projection_elasticity_parts', 'apply_GA', 'scal', 'cg', 'get_inverse', 'Material',
     'project', 'assembly_matrix', 'solve_problem', 'mandel_isotropic',
-    'grad_symbol', 'potential_preconditioner', 'scal_fourier', 'cg_fourier',
+    'bicg', 'cheby2term', 'grad_symbol', 'potential_preconditioner', 'scal_fourier', 'cg_fourier',
     'potential_operator', 'potential_rhs', 'potential_field', 'homog_potential',
 ]
 
@@ -291,6 +291,73 @@ def cg(Afun, B, x0, tol=1e-6, maxiter=1000, callback=None):
     if kit == 0:
         norm_res = 0
     return x, {'kit': kit, 'norm_res': norm_res, 'res_log': log}
+
+
+def bicg(Afun, ATfun, B, x0, tol=1e-6, maxiter=1000):
+    """BiConjugate gradients (solver.py:142-204): shadow residual Rs with
+    ATfun, rr = <R, Rs>, stop on sqrt(rr) <= tol (absolute)."""
+    x = x0
+    R = B - Afun(x0)
+    Rs = R
+    rr = scal(R, Rs)
+    P, Ps = R, Rs
+    kit = 0
+    norm_res = rr ** 0.5
+    log = [norm_res]
+    while norm_res > tol and kit < maxiter:
+        kit += 1
+        AP = Afun(P)
+        alp = rr / scal(AP, Ps)
+        x = x + alp * P
+        R = R - alp * AP
+        Rs = Rs - alp * ATfun(Ps)
+        rrnext = scal(R, Rs)
+        bet = rrnext / rr
+        rr = rrnext
+        P = R + bet * P
+        Ps = Rs + bet * Ps
+        norm_res = rr ** 0.5
+        log.append(norm_res)
+    if kit == 0:
+        norm_res = 0
+    return x, {'kit': kit, 'norm_res': norm_res, 'res_log': log}
+
+
+def cheby2term(Afun, B, x0, eigrange, tol=1e-6, maxit=1e7):
+    """Chebyshev two-term iteration (solver.py:206-285) on the eigenvalue
+    interval eigrange; norm_res is |r| / |r0| in the grid-mean norm."""
+    kit = 0
+    bnrm2 = scal(B, B) ** 0.5
+    Ib = 1.0 / bnrm2
+    x = x0
+    r = B - Afun(x)
+    r0 = np.double(scal(r, r)) ** 0.5
+    norm_res = Ib * r0
+    if norm_res < tol:
+        return x, {'kit': kit, 'norm_res': norm_res}
+    d = (eigrange[1] + eigrange[0]) / 2.0
+    c = (eigrange[1] - eigrange[0]) / 2.0
+    v = 0 * x0
+    w = 0.
+    while norm_res > tol and kit < maxit:
+        kit += 1
+        x_prev = x
+        if kit == 1:
+            p = 0
+            w = 1 / d
+        elif kit == 2:
+            p = -(1 / 2) * (c / d) * (c / d)
+            w = 1 / (d - c * c / 2 / d)
+        else:
+            p = -(c * c / 4) * w * w
+            w = 1 / (d - c * c * w / 4)
+        v = r - p * v
+        x = x_prev + w * v
+        r = B - Afun(x)
+        norm_res = (1.0 / r0) * scal(r, r) ** 0.5
+    if kit == 0:
+        norm_res = 0
+    return x, {'kit': kit, 'norm_res': norm_res}
 
 
 def get_inverse(A):

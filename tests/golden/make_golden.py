@@ -31,7 +31,12 @@ pot_<name>.npz
     homog_GaNi_full_potential / homog_Ga_full_potential, and one application
     of their preconditioned operator.
 
-Usage:  python tests/golden/make_golden.py [REFERENCE_DIR [pickles|run|op|pot ...]]
+solv_<name>.npz
+    linear_solver with solver='chebyshev' (ffthompy/general/solver.py:
+    206-285) on a scalar FiGFA operator: solution, iteration count, final
+    relative residual.
+
+Usage:  python tests/golden/make_golden.py [REFERENCE_DIR [pickles|run|op|pot|solv ...]]
 """
 import collections
 import collections.abc
@@ -273,6 +278,55 @@ def operator_cases():
         _save('op_' + name, meta, arrays)
 
 
+def solver_cases():
+    """The two-term Chebyshev iteration of linear_solver (ffthompy/general/
+    solver.py:206-285, eigrange = the coefficient bounds) on the scalar
+    Galerkin operator of a seeded random material.  (BiCG, solver.py:142-204,
+    does not run on Tensor / Operator objects as shipped: it forms R.T*Rs,
+    and Tensor has no .T for vectors, and alp*ATfun*Ps multiplies an Operator
+    by a float first; the tests pin it by its oracle restatement.)"""
+    import ffthompy.projections as proj
+    from ffthompy.general.solver import linear_solver
+    from ffthompy.tensors import Tensor, DFT, Operator
+    rng = np.random.default_rng(11)
+    for name, Nl, kind in [('s2_gani_15', [15, 15], 'GaNi'), ('s2_ga_9', [9, 9], 'Ga'),
+                           ('s3_gani_7', [7, 7, 7], 'GaNi')]:
+        N = np.array(Nl)
+        d = N.size
+        Nbar = N if kind == 'GaNi' else 2 * N - 1
+        _, G1, _ = proj.scalar(N, np.ones(d), NyqNul=True, tensor=True)
+        if kind == 'Ga':
+            G1 = G1.enlarge(Nbar)
+        FN = DFT(name='FN', inverse=False, N=Nbar)
+        FiN = DFT(name='FiN', inverse=True, N=Nbar)
+        a = 1. + 9. * (rng.random(tuple(Nbar)) < 0.4)
+        Aval = np.einsum('ij,...->ij...', np.eye(d), a)
+        A = Tensor(name='A', val=Aval, order=2, N=Nbar, multype=21)
+        GN = Operator(name='G', mat=[[FiN, G1, FN]])
+        Afun = Operator(name='FiGFA', mat=[[GN, A]])
+        E = np.zeros(d)
+        E[0] = 1.
+        EN = Tensor(name='EN', N=Nbar, shape=(d,), Fourier=False)
+        EN.set_mean(E)
+        B = Afun(-EN)
+        arrays = {'A': Aval, 'B': B.val}
+        # the spectrum of FiGFA on its range: the coefficient bounds times the
+        # Ga scale prod(Nbar)/prod(N) of the enlarged projection
+        sc = float(np.prod(Nbar)) / float(np.prod(N))
+        eig = [sc * float(a.min()), sc * float(a.max())]
+        for solver, par in [('chebyshev', {'tol': 1e-6, 'maxit': 2000, 'eigrange': eig})]:
+            x0 = Tensor(N=Nbar, shape=(d,), Fourier=False)
+            with contextlib.redirect_stdout(io.StringIO()):
+                X, info = linear_solver(Afun, B, ATfun=Afun, x0=x0, par=dict(par),
+                                        solver=solver, callback=None)
+            arrays['x__' + solver] = X.val
+            arrays['kit__' + solver] = np.array(int(info['kit']))
+            arrays['normres__' + solver] = np.array(float(info['norm_res']))
+        meta = dict(N=Nl, kind=kind, Nbar=[int(v) for v in Nbar],
+                    chebyshev={'tol': 1e-6, 'maxit': 2000, 'eigrange': eig})
+        _save('solv_' + name, meta, arrays)
+
+
 def _stub_ttpy():
     """ffthompy.tensorsLowRank imports ttpy (absent here) at module level; the
     full potential solvers used below never call it, so empty stand-in
@@ -353,7 +407,7 @@ if __name__ == '__main__':
     _install_shim()
     import warnings
     warnings.simplefilter('ignore')
-    only = sys.argv[2:] if len(sys.argv) > 2 else ['pickles', 'run', 'op', 'pot']
+    only = sys.argv[2:] if len(sys.argv) > 2 else ['pickles', 'run', 'op', 'pot', 'solv']
     if 'pickles' in only:
         golden_pickles()
     if 'run' in only:
@@ -362,3 +416,5 @@ if __name__ == '__main__':
         operator_cases()
     if 'pot' in only:
         potential_cases()
+    if 'solv' in only:
+        solver_cases()
