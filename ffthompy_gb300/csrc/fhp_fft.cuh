@@ -374,12 +374,14 @@ __device__ __forceinline__ void stage_run(cplx<R>* __restrict__ buf, int ld, int
   const int tws = nf / ns;
   if constexpr (RAD > 8 && RAD != 16) {
     // odd radices above 8: one (line, butterfly) pair per step, nothing kept
-    // across lines (their slot offsets would not fit the register budget)
+    // across lines (their slot offsets would not fit the register budget).
+    // A span-1 stage (ms = 1, the last DIF stage) has only unit twiddles.
     const int total = nlines * nbl;
+    const bool tw1 = ms == 1;
     for (int b = tid; b < total; b += nthr) {
       const int line = fdiv(b, dnbl);
       const int bb = b - line * nbl;
-      const int g = fdiv(bb, dms);
+      const int g = tw1 ? bb : fdiv(bb, dms);
       const int j1 = bb - g * ms;
       cplx<R>* lp = buf + line * ld;
       const int base = g * ns + j1;
@@ -389,13 +391,23 @@ __device__ __forceinline__ void stage_run(cplx<R>* __restrict__ buf, int ld, int
         for (int q = 0; q < RAD; ++q) v[q] = lp[sp(base + q * ms)];
         dft_fwd<R, RAD>(v, tw, nf);
         lp[sp(base)] = v[0];
+        if (tw1) {
 #pragma unroll
-        for (int q = 1; q < RAD; ++q) lp[sp(base + q * ms)] = cmul<R>(v[q], tw[j1 * q * tws]);
+          for (int q = 1; q < RAD; ++q) lp[sp(base + q)] = v[q];
+        } else {
+#pragma unroll
+          for (int q = 1; q < RAD; ++q) lp[sp(base + q * ms)] = cmul<R>(v[q], tw[j1 * q * tws]);
+        }
       } else {
         v[0] = cconj<R>(lp[sp(base)]);
+        if (tw1) {
 #pragma unroll
-        for (int q = 1; q < RAD; ++q)
-          v[q] = cconj<R>(cmulc<R>(lp[sp(base + q * ms)], tw[j1 * q * tws]));
+          for (int q = 1; q < RAD; ++q) v[q] = cconj<R>(lp[sp(base + q)]);
+        } else {
+#pragma unroll
+          for (int q = 1; q < RAD; ++q)
+            v[q] = cconj<R>(cmulc<R>(lp[sp(base + q * ms)], tw[j1 * q * tws]));
+        }
         dft_fwd<R, RAD>(v, tw, nf);
 #pragma unroll
         for (int q = 0; q < RAD; ++q) lp[sp(base + q * ms)] = cconj<R>(v[q]);
@@ -505,15 +517,26 @@ __device__ __forceinline__ int p2_pos(int k) {
 // Stage S of the in-place DIF (forward) or its inverse, on nlines lines.
 // A thread keeps one butterfly (its slots and twiddles) for all its lines;
 // requires blockDim.x to be a multiple of the butterflies per line (every
-// launch uses 256 threads; the largest count is 128).
-template <typename R, int P, int S, bool INV>
+// launch uses 256 threads; the largest count is 128).  Stages of span 1 (the
+// last DIF / first DIT stage) have only the unit twiddle and skip the multiply.
+// PRUNE (span-1 stage of a line whose spectrum is zero for N/4 <= k <= 3N/4):
+// digits q in [RAD/4, 3 RAD/4) of such a butterfly are those frequencies, so
+// the inverse reads them as zeros and the forward does not store them.
+template <int RAD>
+__host__ __device__ constexpr bool p2_pruned_digit(int q) {
+  return q >= RAD / 4 && q < 3 * RAD / 4;
+}
+
+template <typename R, int P, int S, bool INV, bool PRUNE = false>
 __device__ __forceinline__ void p2_stage(cplx<R>* __restrict__ buf, int ld, int nlines,
                                          const cplx<R>* __restrict__ tw) {
   constexpr int E = p2_e(P, S), EB = p2_ebefore(P, S);
   constexpr int RAD = 1 << E;
   constexpr int LNS = P - EB, LMS = LNS - E, LNBL = P - E;
   constexpr int NS = 1 << LNS, MS = 1 << LMS, NBL = 1 << LNBL;
+  constexpr bool TW = MS > 1;
   static_assert(NBL <= 256, "butterflies per line exceed the CTA");
+  static_assert(!PRUNE || (!TW && RAD >= 4), "pruning applies to span-1 stages");
   const int tid = threadIdx.x;
   const int lstep = blockDim.x >> LNBL;
   const int l0 = tid >> LNBL;
@@ -521,8 +544,10 @@ __device__ __forceinline__ void p2_stage(cplx<R>* __restrict__ buf, int ld, int 
   const int g = bb >> LMS, j1 = bb & (MS - 1);
   const int sbase = sp(g * NS + j1);
   cplx<R> w[RAD];
+  if constexpr (TW) {
 #pragma unroll
-  for (int q = 1; q < RAD; ++q) w[q] = tw[(j1 * q) << EB];
+    for (int q = 1; q < RAD; ++q) w[q] = tw[(j1 * q) << EB];
+  }
   for (int line = l0; line < nlines; line += lstep) {
     cplx<R>* lp = buf + line * ld + sbase;
     cplx<R> v[RAD];
@@ -532,11 +557,17 @@ __device__ __forceinline__ void p2_stage(cplx<R>* __restrict__ buf, int ld, int 
       dft_fwd<R, RAD>(v, tw, 1 << P);
       lp[0] = v[0];
 #pragma unroll
-      for (int q = 1; q < RAD; ++q) lp[sp(q * MS)] = cmul<R>(v[q], w[q]);
+      for (int q = 1; q < RAD; ++q) {
+        if (PRUNE && p2_pruned_digit<RAD>(q)) continue;
+        lp[sp(q * MS)] = TW ? cmul<R>(v[q], w[q]) : v[q];
+      }
     } else {
       v[0] = cconj<R>(lp[0]);
 #pragma unroll
-      for (int q = 1; q < RAD; ++q) v[q] = cconj<R>(cmulc<R>(lp[sp(q * MS)], w[q]));
+      for (int q = 1; q < RAD; ++q) {
+        if (PRUNE && p2_pruned_digit<RAD>(q)) v[q] = mkc<R>(R(0), R(0));
+        else v[q] = TW ? cconj<R>(cmulc<R>(lp[sp(q * MS)], w[q])) : cconj<R>(lp[sp(q * MS)]);
+      }
       dft_fwd<R, RAD>(v, tw, 1 << P);
 #pragma unroll
       for (int q = 0; q < RAD; ++q) lp[sp(q * MS)] = cconj<R>(v[q]);

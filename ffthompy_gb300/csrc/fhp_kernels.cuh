@@ -1386,6 +1386,61 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_last(cplx<R>* __
   }
 }
 
+// The isotropic middle of k_band_last_p2 in one pass over shared memory: the
+// last inverse stage (S = 0, DIT), q = a(v) x / prod(N) per voxel, and the first
+// forward stage (S = 0, DIF).  Both stages use the same butterflies, slots
+// and twiddles, and after the inverse the slot j1 + q ms holds voxel j1 + q ms
+// of the line, so the coefficient is applied in registers between them.
+// Pair line p of row rl carries comps 2p, 2p+1, both scaled by a(v); the
+// unused imaginary half of the last line (odd comp count) is zeroed, rows past
+// the grid are zeroed, as in the unfused path.
+template <typename R, int P>
+__device__ __forceinline__ void p2_fused_iso_stage0(cplx<R>* __restrict__ buf, int ld, int nlines,
+                                                    const cplx<R>* __restrict__ tw, int np,
+                                                    FastDiv dnp, const R* acache,
+                                                    const R* __restrict__ A, long long row0,
+                                                    long long nrows, bool st_coef, R cs,
+                                                    bool codd) {
+  constexpr int E = p2_e(P, 0);
+  constexpr int RAD = 1 << E;
+  constexpr int LMS = P - E, MS = 1 << LMS, NBL = MS;
+  constexpr int N = 1 << P;
+  const int lstep = blockDim.x >> LMS;
+  const int l0 = threadIdx.x >> LMS;
+  const int j1 = threadIdx.x & (NBL - 1);
+  const int sbase = sp(j1);
+  cplx<R> w[RAD];
+#pragma unroll
+  for (int q = 1; q < RAD; ++q) w[q] = tw[j1 * q];
+  for (int line = l0; line < nlines; line += lstep) {
+    const int rl = fdiv(line, dnp), p = line - rl * np;
+    const long long row = row0 + rl;
+    const bool valid = row < nrows;
+    const R* arow = st_coef ? acache + (long long)rl * N : A + (valid ? row : 0) * N;
+    cplx<R>* lp = buf + line * ld + sbase;
+    cplx<R> v[RAD];
+    v[0] = cconj<R>(lp[0]);
+#pragma unroll
+    for (int q = 1; q < RAD; ++q) v[q] = cconj<R>(cmulc<R>(lp[sp(q * MS)], w[q]));
+    dft_fwd<R, RAD>(v, tw, N);
+    const bool zimag = codd && p == np - 1;
+#pragma unroll
+    for (int q = 0; q < RAD; ++q) {
+      const cplx<R> x = cconj<R>(v[q]);
+      if (valid) {
+        const R a = arow[j1 + q * MS];
+        v[q] = mkc<R>((a * x.x) * cs, zimag ? R(0) : (a * x.y) * cs);
+      } else {
+        v[q] = mkc<R>(R(0), R(0));
+      }
+    }
+    dft_fwd<R, RAD>(v, tw, N);
+    lp[0] = v[0];
+#pragma unroll
+    for (int q = 1; q < RAD; ++q) lp[sp(q * MS)] = cmul<R>(v[q], w[q]);
+  }
+}
+
 // k_band_last for a direct power-of-two integration line B2 = 2^P (the
 // smooth grids 2^k >= 2N-1 of the common solve sizes: 509 -> 512, 253 -> 256).
 // Same shared-memory layout, staging and results as k_band_last; the phases
@@ -1433,6 +1488,9 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_last_p2(cplx<R>*
   __syncthreads();
   const int nlines = rows * np;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
+  // the band |k| < n2h_band lies within N/4: the span-1 stages can skip the
+  // zero digits (p2_stage PRUNE)
+  const bool band4 = 4 * n2h_band <= N;
   // 1) Hermitian pair lines Z = A + iB
   for (int line = warp; line < nlines; line += nwarp) {
     const int rl = fdiv(line, g.dnp), p = line - rl * np;
@@ -1454,51 +1512,97 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_last_p2(cplx<R>*
       lp[sp(p2_pos<P>(aq))] = mkc<R>(a.x - b.y, a.y + b.x);
       if (aq > 0) lp[sp(p2_pos<P>(N - aq))] = mkc<R>(a.x + b.y, b.x - a.y);  // X_{-k} = conj(X_k)
     }
-    for (int k = n2h_band + lane; k <= N - n2h_band; k += 32)
-      lp[sp(p2_pos<P>(k))] = mkc<R>(R(0), R(0));
-  }
-  __syncthreads();
-  line_core_p2<R, P>(buf, ld, nlines, L, true);
-  // 2) coefficient per voxel (all loads), in place
-  cp_async_wait<0>();
-  __syncthreads();
-  for (int e = threadIdx.x; e < (rows << P); e += blockDim.x) {
-    const int rl = e >> P, j = e & (N - 1);
-    const long long row = row0 + rl;
-    cplx<R>* base = buf + (long long)rl * np * ld + sp(j);
-    if (row >= nrows) {
-      for (int p = 0; p < np; ++p) base[p * ld] = mkc<R>(R(0), R(0));
-      continue;
-    }
-    if constexpr (COEF == COEF_ISO) {
-      const R a = st_coef ? acache[(long long)rl * N + j] : A[row * N + j];
-      for (int p = 0; p < np; ++p) {
-        const cplx<R> z = base[p * ld];
-        base[p * ld] = mkc<R>((a * z.x) * coef_scale, (a * z.y) * coef_scale);
-      }
+    // zeros outside the band.  With the band within N/4 the first inverse
+    // stage reads the frequencies N/4 <= k < 3N/4 as zeros (pruned top
+    // digits), so only [n2h, N/4) and [3N/4, N - n2h] are written.
+    if (!band4) {
+      for (int k = n2h_band + lane; k <= N - n2h_band; k += 32)
+        lp[sp(p2_pos<P>(k))] = mkc<R>(R(0), R(0));
     } else {
-      for (int l = 0; l < g.L; ++l) {
-        R xv[kMaxDv], qv[kMaxDv];
-#pragma unroll
-        for (int c = 0; c < kMaxDv; ++c) {
-          if (c >= g.dv) break;
-          const int comp = l * g.dv + c;
-          xv[c] = reinterpret_cast<const R*>(base + (comp >> 1) * ld)[comp & 1];
-        }
-        if (st_coef) coef_apply<R, COEF>(acache, (long long)rows * N, (long long)rl * N + j, g.dv, xv, qv);
-        else coef_apply<R, COEF>(A, Mi, row * N + j, g.dv, xv, qv);
-#pragma unroll
-        for (int c = 0; c < kMaxDv; ++c) {
-          if (c >= g.dv) break;
-          const int comp = l * g.dv + c;
-          reinterpret_cast<R*>(base + (comp >> 1) * ld)[comp & 1] = qv[c] * coef_scale;
-        }
-      }
+      for (int k = n2h_band + lane; k < N / 4; k += 32)
+        lp[sp(p2_pos<P>(k))] = mkc<R>(R(0), R(0));
+      for (int k = 3 * (N / 4) + lane; k <= N - n2h_band; k += 32)
+        lp[sp(p2_pos<P>(k))] = mkc<R>(R(0), R(0));
     }
-    if (C & 1) reinterpret_cast<R*>(base + (np - 1) * ld)[1] = R(0);
   }
   __syncthreads();
-  line_core_p2<R, P>(buf, ld, nlines, L, false);
+  constexpr int NST = p2_nst(P);
+  if constexpr (COEF == COEF_ISO) {
+    // inverse stages NST-1 .. 1, fused stage 0 with the coefficient, forward
+    // stages 1 .. NST-1; the span-1 stages pruned to the band when it fits N/4
+    const bool codd = (C & 1) != 0;
+    if (band4) p2_stage<R, P, NST - 1, true, true>(buf, ld, nlines, L.tw);
+    else p2_stage<R, P, NST - 1, true, false>(buf, ld, nlines, L.tw);
+    __syncthreads();
+    if constexpr (NST > 2) { p2_stage<R, P, 1, true>(buf, ld, nlines, L.tw); __syncthreads(); }
+    cp_async_wait<0>();
+    __syncthreads();
+    p2_fused_iso_stage0<R, P>(buf, ld, nlines, L.tw, np, g.dnp, acache, A, row0, nrows, st_coef,
+                              coef_scale, codd);
+    __syncthreads();
+    if constexpr (NST > 2) { p2_stage<R, P, 1, false>(buf, ld, nlines, L.tw); __syncthreads(); }
+    if (band4) p2_stage<R, P, NST - 1, false, true>(buf, ld, nlines, L.tw);
+    else p2_stage<R, P, NST - 1, false, false>(buf, ld, nlines, L.tw);
+    __syncthreads();
+  } else {
+    if (band4) {
+      p2_stage<R, P, NST - 1, true, true>(buf, ld, nlines, L.tw);
+      __syncthreads();
+      if constexpr (NST > 2) { p2_stage<R, P, 1, true>(buf, ld, nlines, L.tw); __syncthreads(); }
+      p2_stage<R, P, 0, true>(buf, ld, nlines, L.tw);
+      __syncthreads();
+    } else {
+      line_core_p2<R, P>(buf, ld, nlines, L, true);
+    }
+    // 2) coefficient per voxel (all loads), in place
+    cp_async_wait<0>();
+    __syncthreads();
+    for (int e = threadIdx.x; e < (rows << P); e += blockDim.x) {
+      const int rl = e >> P, j = e & (N - 1);
+      const long long row = row0 + rl;
+      cplx<R>* base = buf + (long long)rl * np * ld + sp(j);
+      if (row >= nrows) {
+        for (int p = 0; p < np; ++p) base[p * ld] = mkc<R>(R(0), R(0));
+        continue;
+      }
+      if constexpr (COEF == COEF_ISO) {
+        const R a = st_coef ? acache[(long long)rl * N + j] : A[row * N + j];
+        for (int p = 0; p < np; ++p) {
+          const cplx<R> z = base[p * ld];
+          base[p * ld] = mkc<R>((a * z.x) * coef_scale, (a * z.y) * coef_scale);
+        }
+      } else {
+        for (int l = 0; l < g.L; ++l) {
+          R xv[kMaxDv], qv[kMaxDv];
+  #pragma unroll
+          for (int c = 0; c < kMaxDv; ++c) {
+            if (c >= g.dv) break;
+            const int comp = l * g.dv + c;
+            xv[c] = reinterpret_cast<const R*>(base + (comp >> 1) * ld)[comp & 1];
+          }
+          if (st_coef) coef_apply<R, COEF>(acache, (long long)rows * N, (long long)rl * N + j, g.dv, xv, qv);
+          else coef_apply<R, COEF>(A, Mi, row * N + j, g.dv, xv, qv);
+  #pragma unroll
+          for (int c = 0; c < kMaxDv; ++c) {
+            if (c >= g.dv) break;
+            const int comp = l * g.dv + c;
+            reinterpret_cast<R*>(base + (comp >> 1) * ld)[comp & 1] = qv[c] * coef_scale;
+          }
+        }
+      }
+      if (C & 1) reinterpret_cast<R*>(base + (np - 1) * ld)[1] = R(0);
+    }
+    __syncthreads();
+    if (band4) {
+      p2_stage<R, P, 0, false>(buf, ld, nlines, L.tw);
+      __syncthreads();
+      if constexpr (NST > 2) { p2_stage<R, P, 1, false>(buf, ld, nlines, L.tw); __syncthreads(); }
+      p2_stage<R, P, NST - 1, false, true>(buf, ld, nlines, L.tw);
+      __syncthreads();
+    } else {
+      line_core_p2<R, P>(buf, ld, nlines, L, false);
+    }
+  }
   // 3) split and keep the band
   for (int line = warp; line < nlines; line += nwarp) {
     const int rl = fdiv(line, g.dnp), p = line - rl * np;

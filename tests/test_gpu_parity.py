@@ -375,19 +375,26 @@ def _pow2_at_least(n, lo=32):
     return m
 
 
-@pytest.mark.parametrize('N,physics', [((5, 20), 'scalar'), ((9, 60), 'scalar'),
-                                       ((7, 100), 'scalar'), ((5, 200), 'scalar'),
-                                       ((5, 300), 'scalar'), ((5, 7, 9), 'scalar'),
-                                       ((6, 5, 8), 'scalar'), ((5, 5, 5), 'elasticity'),
-                                       ((9, 60), 'elasticity')])
+@pytest.mark.parametrize('N,physics,coef', [
+    ((5, 20), 'scalar', 'full'), ((9, 60), 'scalar', 'full'), ((7, 100), 'scalar', 'full'),
+    ((5, 200), 'scalar', 'full'), ((5, 300), 'scalar', 'full'), ((5, 7, 9), 'scalar', 'full'),
+    ((6, 5, 8), 'scalar', 'full'), ((5, 5, 5), 'elasticity', 'full'),
+    ((9, 60), 'elasticity', 'full'),
+    # isotropic a(x) I (the fused coefficient stage), band within / beyond N/4
+    ((5, 20), 'scalar', 'iso'), ((7, 100), 'scalar', 'iso'), ((5, 200), 'scalar', 'iso'),
+    ((5, 300), 'scalar', 'iso'), ((5, 7, 9), 'scalar', 'iso'), ((6, 5, 8), 'scalar', 'iso'),
+    ((7, 16), 'scalar', 'iso'), ((7, 16), 'scalar', 'full'), ((5, 5, 16), 'scalar', 'iso')])
 @pytest.mark.parametrize('precision', ['f64', 'f32'])
-def test_band_operator_pow2_integration_grid(N, physics, precision):
+def test_band_operator_pow2_integration_grid(N, physics, coef, precision):
     """The band operator on power-of-two integration grids 32 .. 1024 (the
-    compile-time FFT stages) equals the reference's 2N-1 grid operator."""
-    _check_band_operator(N, physics, precision, tuple(_pow2_at_least(2 * n - 1) for n in N))
+    compile-time FFT stages, the pruned span-1 stages when the band lies within
+    a quarter of the line, the fused stage of isotropic coefficients) equals
+    the reference's 2N-1 grid operator."""
+    _check_band_operator(N, physics, precision, tuple(_pow2_at_least(2 * n - 1) for n in N),
+                         iso=(coef == 'iso'))
 
 
-def _check_band_operator(N, physics, precision, integ):
+def _check_band_operator(N, physics, precision, integ, iso=False):
     from ffthompy_gb300.engine import GalerkinPlan
     rng = np.random.default_rng(len(N) + sum(N))
     d = len(N)
@@ -396,9 +403,13 @@ def _check_band_operator(N, physics, precision, integ):
     dv = d if physics == 'scalar' else d * (d + 1) // 2
     Y = 0.7 + rng.random(d)
     # a band-limited SPD coefficient on the 2N-1 grid (Ga coefficients are)
-    Bc = rng.standard_normal((dv, dv) + tuple(Nb))
-    A = np.einsum('ik...,jk...->ij...', Bc, Bc) + 3 * np.einsum('ij,...->ij...', np.eye(dv),
-                                                                np.ones(tuple(Nb)))
+    if iso:
+        a = rng.standard_normal(tuple(Nb)) ** 2 + 3.
+        A = np.einsum('ij,...->ij...', np.eye(dv), a)
+    else:
+        Bc = rng.standard_normal((dv, dv) + tuple(Nb))
+        A = np.einsum('ik...,jk...->ij...', Bc, Bc) + 3 * np.einsum('ij,...->ij...', np.eye(dv),
+                                                                    np.ones(tuple(Nb)))
     A_int = _project_comps(A, integ)
     xN = rng.standard_normal((2, dv) + tuple(N))
     plan = GalerkinPlan(tuple(N), Y, physics=physics, nloads=2, integ=integ,
