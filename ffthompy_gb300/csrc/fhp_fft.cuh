@@ -575,26 +575,37 @@ __device__ __forceinline__ void p2_stage(cplx<R>* __restrict__ buf, int ld, int 
   }
 }
 
-template <typename R, int P, bool INV>
+// PRUNE: the span-1 stage (S = NST-1) skips the digits of N/4 <= k < 3N/4
+// (inverse: zero inputs, forward: unused outputs); see p2_stage.
+template <typename R, int P, bool INV, bool PRUNE = false>
 __device__ __forceinline__ void p2_run(cplx<R>* buf, int ld, int nlines, const cplx<R>* tw) {
   constexpr int NST = p2_nst(P);
-  static_assert(NST <= 3, "power-of-two cores up to 2^12");
+  static_assert(NST >= 2 && NST <= 3, "power-of-two cores 2^5 .. 2^12");
   if constexpr (!INV) {
     p2_stage<R, P, 0, false>(buf, ld, nlines, tw);
     __syncthreads();
-    if constexpr (NST > 1) { p2_stage<R, P, 1, false>(buf, ld, nlines, tw); __syncthreads(); }
-    if constexpr (NST > 2) { p2_stage<R, P, 2, false>(buf, ld, nlines, tw); __syncthreads(); }
+    if constexpr (NST > 2) { p2_stage<R, P, 1, false>(buf, ld, nlines, tw); __syncthreads(); }
+    p2_stage<R, P, NST - 1, false, PRUNE>(buf, ld, nlines, tw);
+    __syncthreads();
   } else {
-    if constexpr (NST > 2) { p2_stage<R, P, 2, true>(buf, ld, nlines, tw); __syncthreads(); }
-    if constexpr (NST > 1) { p2_stage<R, P, 1, true>(buf, ld, nlines, tw); __syncthreads(); }
+    p2_stage<R, P, NST - 1, true, PRUNE>(buf, ld, nlines, tw);
+    __syncthreads();
+    if constexpr (NST > 2) { p2_stage<R, P, 1, true>(buf, ld, nlines, tw); __syncthreads(); }
     p2_stage<R, P, 0, true>(buf, ld, nlines, tw);
     __syncthreads();
   }
 }
 
+// prune: a direct line whose spectrum is zero (inverse) or not read (forward)
+// for N/4 <= k < 3N/4; ignored for Bluestein lines
 template <typename R, int P>
 __device__ __forceinline__ void line_core_p2(cplx<R>* buf, int ld, int nlines, const LineDev<R>& L,
-                                             bool inverse) {
+                                             bool inverse, bool prune = false) {
+  if (prune && !L.blue) {
+    if (inverse) p2_run<R, P, true, true>(buf, ld, nlines, L.tw);
+    else p2_run<R, P, false, true>(buf, ld, nlines, L.tw);
+    return;
+  }
   if (L.blue || !inverse) p2_run<R, P, false>(buf, ld, nlines, L.tw);
   if (L.blue) {
     const int tot = nlines << P;
@@ -608,21 +619,32 @@ __device__ __forceinline__ void line_core_p2(cplx<R>* buf, int ld, int nlines, c
   if (L.blue || inverse) p2_run<R, P, true>(buf, ld, nlines, L.tw);
 }
 
+// A line of length nf = 2^P (direct, compile-time core) whose nonzero or used
+// frequencies satisfy |q| <= hq can skip the digits of N/4 <= k < 3N/4 in its
+// span-1 stage: k = q <= hq < N/4 and k = N - q >= N - hq > 3N/4.
+template <typename R>
+__device__ __forceinline__ bool line_prunable(const LineDev<R>& L, int hq) {
+  return L.lg2 > 0 && !L.blue && 4 * hq < L.nf;
+}
+
 // Core transform of nlines lines (length L.nf each, stride ld) in place.
 //   direct, forward : DIF            (natural -> digit-reversed)
 //   direct, inverse : DIT^-1         (digit-reversed -> natural), unnormalised
 //   Bluestein (either direction, conjugations at put/get): DIF, * bhat, DIT^-1
 // Ends with __syncthreads().
+// prune (power-of-two direct lines only, see line_prunable): the caller's
+// spectrum is zero / unused for N/4 <= k < 3N/4.
 template <typename R>
-__device__ void line_core(cplx<R>* buf, int ld, int nlines, const LineDev<R>& L, bool inverse) {
+__device__ void line_core(cplx<R>* buf, int ld, int nlines, const LineDev<R>& L, bool inverse,
+                          bool prune = false) {
   static_assert(kP2Min == 5 && kP2Max == 10, "dispatch below lists 2^5 .. 2^10");
   switch (L.lg2) {
-    case 5: line_core_p2<R, 5>(buf, ld, nlines, L, inverse); return;
-    case 6: line_core_p2<R, 6>(buf, ld, nlines, L, inverse); return;
-    case 7: line_core_p2<R, 7>(buf, ld, nlines, L, inverse); return;
-    case 8: line_core_p2<R, 8>(buf, ld, nlines, L, inverse); return;
-    case 9: line_core_p2<R, 9>(buf, ld, nlines, L, inverse); return;
-    case 10: line_core_p2<R, 10>(buf, ld, nlines, L, inverse); return;
+    case 5: line_core_p2<R, 5>(buf, ld, nlines, L, inverse, prune); return;
+    case 6: line_core_p2<R, 6>(buf, ld, nlines, L, inverse, prune); return;
+    case 7: line_core_p2<R, 7>(buf, ld, nlines, L, inverse, prune); return;
+    case 8: line_core_p2<R, 8>(buf, ld, nlines, L, inverse, prune); return;
+    case 9: line_core_p2<R, 9>(buf, ld, nlines, L, inverse, prune); return;
+    case 10: line_core_p2<R, 10>(buf, ld, nlines, L, inverse, prune); return;
     default: break;
   }
   const int tid = threadIdx.x, nthr = blockDim.x;

@@ -1054,11 +1054,20 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_axis(const cplx<
   const long long t0 = (long long)blockIdx.x * T;
   const int nl = nlc * T;
   const int lgT = __ffs(T) - 1;  // T is a power of two
+  // band-pruned power-of-two B lines (line_prunable): the up / pad inverse
+  // transforms see at most |q| <= n_in/2 nonzero, the down forward transforms
+  // are read at |q| <= n_out/2 only; zeros on the pruned digits are not written
+  const bool pr2 = (MODE == BAND_UP || MODE == BAND_UP_PROJ || MODE == BAND_PAD) &&
+                   line_prunable<R>(L2, ax.n_in / 2);
+  const bool pr1 = (MODE == BAND_DOWN || MODE == BAND_DOWN_PROJ) &&
+                   line_prunable<R>(L1, ax.n_out / 2);
+  const int pq0 = L2.nf / 4, pq1 = 3 * (L2.nf / 4);  // pruned range of the B line (pr2)
   if constexpr (MODE == BAND_PAD) {
     // input already in frequency (N layout): pad straight into the B line
     // raw values go straight to the inverse-input slots (plain async copies
     // inside the band; the halved Nyquist entry and zeros by ordinary stores)
     tile_loop(1, ax.n_out, T, lgT, [&](int, int k, int t) {
+      if (pr2 && k >= pq0 && k < pq1) return;
       const long long col = t0 + t;
       const int q = signed_freq(k, ax.n_out);
       const int aq = q < 0 ? -q : q;
@@ -1091,7 +1100,7 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_axis(const cplx<
       blue_fixup<R, false>(buf1, ld1, nl, L1);
       __syncthreads();
     }
-    line_core<R>(buf1, ld1, nl, L1, false);
+    line_core<R>(buf1, ld1, nl, L1, false, pr1);
   }
   // Up: the B-grid coefficient at q is the N-grid one for 2|q| < N, half of the
   // Nyquist one for 2|q| = N (the symmetric split of Tensor.enlarge,
@@ -1126,6 +1135,7 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_axis(const cplx<
       // out-of-band frequencies only (2|q| >= n_in): k in [kb, n_out - kb]
       const int kb = (ax.n_in + 1) / 2, ke = ax.n_out - kb + 1;
       tile_loop(nlc, ke - kb, T, lgT, [&](int c, int kk, int t) {
+        if (pr2 && kb + kk >= pq0 && kb + kk < pq1) return;
         put_inv<R>(buf2 + (c * T + t) * ld2, L2, kb + kk, mkc<R>(R(0), R(0)));
       });
     }
@@ -1133,6 +1143,7 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_axis(const cplx<
   if constexpr (MODE == BAND_UP || MODE == BAND_UP_PROJ || MODE == BAND_PAD) {
     if constexpr (MODE == BAND_UP) {
     tile_loop(nlc, ax.n_out, T, lgT, [&](int c, int k, int t) {
+      if (pr2 && k >= pq0 && k < pq1) return;
       const int line = c * T + t;
       const int q = signed_freq(k, ax.n_out);
       const int aq = q < 0 ? -q : q;
@@ -1149,7 +1160,7 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_axis(const cplx<
     if constexpr (MODE == BAND_PAD) blue_fixup<R, true>(buf2, ld2, nl, L2);
     zero_tail<R>(buf2, ld2, nl, L2);
     __syncthreads();
-    line_core<R>(buf2, ld2, nl, L2, true);
+    line_core<R>(buf2, ld2, nl, L2, true, pr2);
     tile_loop(nlc, ax.n_out, T, lgT, [&](int c, int i, int t) {
       const long long col = t0 + t;
       if (col >= ax.inner) return;
