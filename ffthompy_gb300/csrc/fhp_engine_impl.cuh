@@ -822,6 +822,9 @@ class Engine final : public EngineBase {
         if (same) L.lg2 = P;
       }
     }
+    // compile-time mixed-radix core (its radix order is factor_radices')
+    L.mixed = (!h.blue && h.nf == 255 && h.nst == 3 && h.rad[0] == 3 && h.rad[1] == 5 &&
+               h.rad[2] == 17) ? 255 : 0;
     int ns = h.nf;
     for (int i = 0; i < kMaxStages; ++i) {
       L.rad[i] = i < h.nst ? h.rad[i] : 1;

@@ -142,6 +142,7 @@ struct LineDev {
   int nst;      // number of radix stages of the core
   int lg2;      // log2(nf) when the core runs the compile-time power-of-two
                 // stages (kP2Min <= lg2 <= kP2Max), else 0
+  int mixed;    // nf of a compile-time mixed-radix core (255 = 3.5.17), else 0
   int rad[kMaxStages];
   FastDiv dnbl[kMaxStages];  // stage s: division by nf / rad[s] (butterflies per line)
   FastDiv dms[kMaxStages];   // stage s: division by the butterfly span ms_s
@@ -619,6 +620,77 @@ __device__ __forceinline__ void line_core_p2(cplx<R>* buf, int ld, int nlines, c
   if (L.blue || inverse) p2_run<R, P, true>(buf, ld, nlines, L.tw);
 }
 
+// ---------------------------------------------------------------------------
+// Compile-time mixed-radix core for a direct line of length prod(RADS...) with
+// the radices in the order of factor_radices (so LineDev::pos stays valid):
+// 255 = 3.5.17, the solve-grid lines of the 255^3 image.  Butterfly
+// coordinates are divisions by compile-time constants; a thread computes its
+// butterfly's slots (and twiddles, for spans above 1) once per stage.
+// Requires blockDim.x >= N / RAD for every stage (at most 85 here).
+// ---------------------------------------------------------------------------
+template <typename R, int N, int RAD, int NS, bool INV>
+__device__ __forceinline__ void mixed_stage(cplx<R>* __restrict__ buf, int ld, int nlines,
+                                            const cplx<R>* __restrict__ tw) {
+  constexpr int MS = NS / RAD, NBL = N / RAD, TWS = N / NS;
+  constexpr bool TW = MS > 1;
+  const int tid = threadIdx.x;
+  const int lstep = (int)blockDim.x / NBL;
+  const int l0 = tid / NBL;
+  if (l0 >= lstep) return;
+  const int bb = tid - l0 * NBL;
+  const int g = bb / MS, j1 = bb - g * MS;
+  const int base = g * NS + j1;
+  int slot[RAD];
+#pragma unroll
+  for (int q = 0; q < RAD; ++q) slot[q] = sp(base + q * MS);
+  cplx<R> w[RAD];
+  if constexpr (TW) {
+#pragma unroll
+    for (int q = 1; q < RAD; ++q) w[q] = tw[j1 * q * TWS];
+  }
+  for (int line = l0; line < nlines; line += lstep) {
+    cplx<R>* lp = buf + line * ld;
+    cplx<R> v[RAD];
+    if constexpr (!INV) {
+#pragma unroll
+      for (int q = 0; q < RAD; ++q) v[q] = lp[slot[q]];
+      dft_fwd<R, RAD>(v, tw, N);
+      lp[slot[0]] = v[0];
+#pragma unroll
+      for (int q = 1; q < RAD; ++q) lp[slot[q]] = TW ? cmul<R>(v[q], w[q]) : v[q];
+    } else {
+      v[0] = cconj<R>(lp[slot[0]]);
+#pragma unroll
+      for (int q = 1; q < RAD; ++q)
+        v[q] = TW ? cconj<R>(cmulc<R>(lp[slot[q]], w[q])) : cconj<R>(lp[slot[q]]);
+      dft_fwd<R, RAD>(v, tw, N);
+#pragma unroll
+      for (int q = 0; q < RAD; ++q) lp[slot[q]] = cconj<R>(v[q]);
+    }
+  }
+}
+
+// 255 = 3.5.17: spans 255 / 85 / 17 with butterfly spans 85 / 17 / 1
+template <typename R>
+__device__ __forceinline__ void line_core_255(cplx<R>* buf, int ld, int nlines,
+                                              const cplx<R>* tw, bool inverse) {
+  if (!inverse) {
+    mixed_stage<R, 255, 3, 255, false>(buf, ld, nlines, tw);
+    __syncthreads();
+    mixed_stage<R, 255, 5, 85, false>(buf, ld, nlines, tw);
+    __syncthreads();
+    mixed_stage<R, 255, 17, 17, false>(buf, ld, nlines, tw);
+    __syncthreads();
+  } else {
+    mixed_stage<R, 255, 17, 17, true>(buf, ld, nlines, tw);
+    __syncthreads();
+    mixed_stage<R, 255, 5, 85, true>(buf, ld, nlines, tw);
+    __syncthreads();
+    mixed_stage<R, 255, 3, 255, true>(buf, ld, nlines, tw);
+    __syncthreads();
+  }
+}
+
 // A line of length nf = 2^P (direct, compile-time core) whose nonzero or used
 // frequencies satisfy |q| <= hq can skip the digits of N/4 <= k < 3N/4 in its
 // span-1 stage: k = q <= hq < N/4 and k = N - q >= N - hq > 3N/4.
@@ -646,6 +718,10 @@ __device__ void line_core(cplx<R>* buf, int ld, int nlines, const LineDev<R>& L,
     case 9: line_core_p2<R, 9>(buf, ld, nlines, L, inverse, prune); return;
     case 10: line_core_p2<R, 10>(buf, ld, nlines, L, inverse, prune); return;
     default: break;
+  }
+  if (L.mixed == 255) {
+    line_core_255<R>(buf, ld, nlines, L.tw, inverse);
+    return;
   }
   const int tid = threadIdx.x, nthr = blockDim.x;
   const bool do_fwd = L.blue || !inverse;

@@ -383,7 +383,10 @@ def _pow2_at_least(n, lo=32):
     # isotropic a(x) I (the fused coefficient stage), band within / beyond N/4
     ((5, 20), 'scalar', 'iso'), ((7, 100), 'scalar', 'iso'), ((5, 200), 'scalar', 'iso'),
     ((5, 300), 'scalar', 'iso'), ((5, 7, 9), 'scalar', 'iso'), ((6, 5, 8), 'scalar', 'iso'),
-    ((7, 16), 'scalar', 'iso'), ((7, 16), 'scalar', 'full'), ((5, 5, 16), 'scalar', 'iso')])
+    ((7, 16), 'scalar', 'iso'), ((7, 16), 'scalar', 'full'), ((5, 5, 16), 'scalar', 'iso'),
+    # 255-point solve lines (the compile-time 3.5.17 core) on each axis
+    ((255, 7), 'scalar', 'iso'), ((9, 255), 'scalar', 'full'), ((255, 5, 9), 'scalar', 'iso'),
+    ((5, 255, 7), 'elasticity', 'full')])
 @pytest.mark.parametrize('precision', ['f64', 'f32'])
 def test_band_operator_pow2_integration_grid(N, physics, coef, precision):
     """The band operator on power-of-two integration grids 32 .. 1024 (the
