@@ -145,7 +145,9 @@ class Engine final : public EngineBase {
     FHP_CHECK(cudaGetDevice(&dev));
     FHP_CHECK(cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, dev));
     red_ctas_ = (int)std::max<long long>(1, std::min<long long>(4LL * nsm_, (g_.M + kThreads - 1) / kThreads));
-    nparts_max_ = std::max(row_ctas_, red_ctas_);
+    // parts of the reductions: row passes, grid-stride kernels, and the
+    // component-split CG update (at least one part per component)
+    nparts_max_ = std::max(std::max(row_ctas_, red_ctas_), g_.L * g_.dv);
     FHP_CHECK(cudaMalloc(&partials_, (size_t)nparts_max_ * kMaxLoads * kMaxLoads * sizeof(double)));
     FHP_CHECK(cudaMalloc(&st_, kMaxLoads * sizeof(LoadState)));
     FHP_CHECK(cudaMalloc(&all_done_, sizeof(int)));
@@ -1232,11 +1234,14 @@ class Engine final : public EngineBase {
                                         all_done_);
     FHP_LAUNCHED();
     const int pk = pbeg("cg_update", 6.0 * field_bytes(), s);
-    k_cg_update<R><<<red_ctas_, kThreads, 0, s>>>(x_cur_, r_, p_, ap_, partials_, g_, st_,
-                                                  all_done_);
+    // one component per grid row; the parts fit the reduction buffer
+    const int C = g_.L * g_.dv;
+    const int ux = std::max(1, red_ctas_ / C);
+    k_cg_update_comp<R><<<dim3((unsigned)ux, (unsigned)C), kThreads, 0, s>>>(
+        x_cur_, r_, p_, ap_, partials_, g_, st_, all_done_);
     pend(pk, s);
     FHP_LAUNCHED();
-    k_fin_rr<<<g_.L, kThreads, 0, s>>>(partials_, red_ctas_, st_, g_.L, 1.0 / (double)g_.M, dlog,
+    k_fin_rr<<<g_.L, kThreads, 0, s>>>(partials_, ux * C, st_, g_.L, 1.0 / (double)g_.M, dlog,
                                        log_rows, all_done_);
     FHP_LAUNCHED();
     k_update_all_done<<<1, 1, 0, s>>>(st_, g_.L, all_done_);

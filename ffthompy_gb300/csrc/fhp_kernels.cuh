@@ -637,6 +637,71 @@ __global__ void __launch_bounds__(256) k_cg_update(R* __restrict__ x, R* __restr
   block_sum_n(acc, g.L, red, partials + (long long)blockIdx.x * g.L);
 }
 
+// The same update with the grid split by component (blockIdx.y = load * dv +
+// c): each CTA streams one component's four input and two output arrays
+// (instead of all components of a voxel at once) with four voxels in flight
+// per thread.  Partial <R,R> go to partials[(y * gridDim.x + x) * L + l] with
+// zeros for the other loads, so the finalisation over gridDim.x * gridDim.y
+// parts is unchanged.
+template <typename R>
+__global__ void __launch_bounds__(256) k_cg_update_comp(R* __restrict__ x, R* __restrict__ r,
+                                                        const R* __restrict__ p,
+                                                        const R* __restrict__ ap,
+                                                        double* __restrict__ partials, GridDims g,
+                                                        const LoadState* __restrict__ st,
+                                                        const int* __restrict__ all_done) {
+  if (all_done && *all_done) return;
+  __shared__ double red[8];
+  const int comp = blockIdx.y;
+  const int l = comp / g.dv;
+  const bool act = !st[l].done;
+  double acc = 0.;
+  if (act) {
+    const R a = (R)st[l].alpha;
+    const long long off = (long long)comp * g.M;
+    R* xc = x + off;
+    R* rc = r + off;
+    const R* pc = p + off;
+    const R* apc = ap + off;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    R sq = R(0);
+    for (; v + 3 * stride < g.M; v += 4 * stride) {
+      R pv[4], av[4], xv[4], rv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        pv[u] = pc[v + u * stride];
+        av[u] = apc[v + u * stride];
+        xv[u] = xc[v + u * stride];
+        rv[u] = rc[v + u * stride];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        xc[v + u * stride] = xv[u] + a * pv[u];
+        const R rn = rv[u] - a * av[u];
+        rc[v + u * stride] = rn;
+        sq += rn * rn;
+      }
+    }
+    for (; v < g.M; v += stride) {
+      xc[v] = xc[v] + a * pc[v];
+      const R rn = rc[v] - a * apc[v];
+      rc[v] = rn;
+      sq += rn * rn;
+    }
+    acc = (double)sq;
+  }
+  double t = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot = 0.;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
+    double* out = partials + ((long long)blockIdx.y * gridDim.x + blockIdx.x) * g.L;
+    for (int k = 0; k < g.L; ++k) out[k] = k == l ? tot : 0.;
+  }
+}
+
 // Finalise <P,AP>: alpha = rr / pap  (solver.py:126)
 static __global__ void k_fin_pap(const double* __restrict__ partials, int nparts, LoadState* st, int L,
                           double invM, const int* __restrict__ all_done) {
