@@ -253,7 +253,7 @@ __device__ __forceinline__ void block_sum_n(double (&acc)[NMAX], int n, double* 
 // ---------------------------------------------------------------------------
 template <typename R, int COEF, bool PUPD>
 __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_r2c_last(
-    const R* xin, R* pio, const R* __restrict__ rvec,
+    const R* __restrict__ xin, R* __restrict__ pio, const R* __restrict__ rvec,
     const R* __restrict__ A, cplx<R>* __restrict__ S, const __grid_constant__ GridDims g, const __grid_constant__ LineDev<R> L, int rows,
     const LoadState* __restrict__ st, const int* __restrict__ all_done) {
   if (all_done && *all_done) return;
@@ -266,6 +266,14 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_r2c_last(
   const long long row0 = (long long)blockIdx.x * rows;
   const int n = g.n2;
   const int tasks = rows * n;
+  // per-load beta and activity, read once (not per voxel)
+  R betl[kMaxLoads];
+  bool wrl[kMaxLoads];
+#pragma unroll
+  for (int l = 0; l < kMaxLoads; ++l) {
+    betl[l] = (PUPD && l < g.L) ? R(st[l].beta) : R(0);
+    wrl[l] = PUPD && l < g.L && !st[l].done;
+  }
   for (int e = threadIdx.x; e < tasks; e += blockDim.x) {
     const int rl = fdiv(e, g.dn2), j = e - rl * n;
     const long long row = row0 + rl;
@@ -278,19 +286,23 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_r2c_last(
 #pragma unroll
     for (int l = 0; l < kMaxLoads; ++l) {
       if (l >= g.L) break;
-      R xv[kMaxDv], q[kMaxDv];
-      const R bet = PUPD ? R(st[l].beta) : R(0);
-      const bool wr = PUPD && !st[l].done;
+      R xv[kMaxDv], q[kMaxDv], rv[kMaxDv];
+      // every global load of this load case before any store
 #pragma unroll
       for (int c = 0; c < kMaxDv; ++c) {
         if (c >= g.dv) break;
         const long long idx = (long long)(l * g.dv + c) * g.M + v;
-        R val = PUPD ? pio[idx] : xin[idx];
+        xv[c] = PUPD ? pio[idx] : xin[idx];
+        if constexpr (PUPD) rv[c] = rvec[idx];
+      }
+#pragma unroll
+      for (int c = 0; c < kMaxDv; ++c) {
+        if (c >= g.dv) break;
         if constexpr (PUPD) {
-          val = rvec[idx] + bet * val;
-          if (wr) pio[idx] = val;
+          const long long idx = (long long)(l * g.dv + c) * g.M + v;
+          xv[c] = rv[c] + betl[l] * xv[c];
+          if (wrl[l]) pio[idx] = xv[c];
         }
-        xv[c] = val;
       }
       coef_apply<R, COEF>(A, g.M, v, g.dv, xv, q);
 #pragma unroll
@@ -542,6 +554,8 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_c2r_last(const cplx<R
     R* ya_out = y + (long long)ca * g.M + row * n;
     R* yb_out = y + (long long)cb * g.M + row * n;
     R sa = R(0), sb = R(0);
+    // unrolled: the P loads of several j are in flight together
+#pragma unroll 4
     for (int j = lane; j < n; j += 32) {
       const cplx<R> z = get_inv<R>(lp, L, j);
       const R ya = z.x * scale, yb = z.y * scale;
