@@ -61,6 +61,8 @@ def parse():
                          'grid >= 2N-1; full: CG on the 2N-1 grid (the reference layout)')
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-fp64', action='store_true')
+    ap.add_argument('--no-ensemble', action='store_true',
+                    help='skip the 512-instance 2D ensemble measurement')
     ap.add_argument('--no-potential', action='store_true',
                     help='skip the potential-formulation measurement (GaNi on the image grid)')
     return ap.parse_args()
@@ -258,6 +260,35 @@ def run_reference(args):
 # ----------------------------------------------------------------------------
 # the GPU arm
 # ----------------------------------------------------------------------------
+def ensemble_measure(count=512, sizes=(63, 127, 255, 511), seed=12, tol=1e-6, workers=16):
+    """Many independent 2D GaNi cells (thresholded Gaussian random fields,
+    length 0.1, 0.4-quantile, contrast log-uniform in [2, 1000], n drawn from
+    sizes, 2 loads each) solved together by homogenize_many, FP64 to tol:
+    aggregate Mvoxel-iter/s over all instances."""
+    import torch
+    from ffthompy_gb300 import workloads
+    from ffthompy_gb300.batch import homogenize_many
+    rng = np.random.default_rng(seed)
+    coefs = []
+    for _ in range(count):
+        n = int(rng.choice(sizes))
+        contrast = float(np.exp(rng.uniform(np.log(2.), np.log(1000.))))
+        coefs.append(workloads.grf_phase_coefficient((n, n), ell=0.1, quantile=0.4,
+                                                     contrast=contrast,
+                                                     seed=int(rng.integers(1 << 30))))
+    homogenize_many(coefs[:workers], tol=tol, workers=workers)   # plans, first launches
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = homogenize_many(coefs, tol=tol, workers=workers)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    vox_it = sum(int(np.prod(A.shape[2:])) * sum(r['kit_primal']) for A, r in zip(coefs, res))
+    return {'instances': count, 'sizes': list(sizes), 'loads': 2, 'precision': 'f64',
+            'tol': tol, 'voxels': int(sum(np.prod(A.shape[2:]) for A in coefs)),
+            'seconds': dt, 'Mvoxel_iter_per_s': vox_it / dt / 1e6,
+            'all_converged': all(r['status_primal'] == [0, 0] for r in res)}
+
+
 def potential_measure(vals, w, tol, steps=2):
     """Time to A_H of the potential formulation (fhp_potential_*) for the
     GaNi discretisation on the image grid, 3 loads batched, FP32 with FP64
@@ -445,6 +476,8 @@ def run_gpu(args):
     # formulation's A_H on the same grid and tolerance
     if not args.no_potential:
         extras['potential'] = potential_measure(vals, w, tol)
+    if not args.no_ensemble:
+        extras['ensemble_grf2d'] = ensemble_measure()
 
     if rank != 0:
         return
