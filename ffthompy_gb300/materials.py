@@ -85,6 +85,44 @@ def get_weights_circ(r, Nbar, Y):
     return W / np.prod(Y)
 
 
+def _centered_ifft_real_separable(vecs, shape):
+    """_centered_ifft_real of the outer product of per-axis spectra vecs[i]:
+    the d-dimensional transform of a separable product is the product of the
+    1D transforms, so the cost is O(d N) transforms and one outer product
+    (the real part is formed from the complex partial products)."""
+    cs = [np.fft.fftshift(np.fft.ifft(np.fft.ifftshift(X))) * int(n)
+          for X, n in zip(vecs, shape)]
+    t = cs[0]
+    for c in cs[1:-1]:
+        t = np.multiply.outer(t, c)
+    if len(cs) == 1:
+        return t.real.copy()
+    last = cs[-1]
+    return np.multiply.outer(t.real, last.real) - np.multiply.outer(t.imag, last.imag)
+
+
+def _separable_char(kind, h, pos, N, Y):
+    """Characteristic function of a box ('cube') or bilinear pyramid on grid N
+    from its separable spectrum: per axis the phase of get_shift_inclusion
+    (integer frequencies in FFT order, as the reference pairs them) times the
+    centred 1D weight of get_weights_con / get_weights_lin; 1/|Y| once.
+    Equals _centered_ifft_real(SS * W, N) up to roundoff."""
+    N = np.asarray(N, dtype=np.int64)
+    Zr = Grid.get_ZNl(N)
+    Zc = Grid.get_ZNl(N, fft_form='c')
+    vecs = []
+    for i in range(N.size):
+        if kind == 'cube':
+            w = h[i] * np.sinc(h[i] * Zc[i] / Y[i])
+        else:
+            w = h[i] * np.sinc(h[i] * Zc[i] / Y[i]) ** 2
+        ph = np.ones(N[i], dtype=np.complex128) if pos is None else \
+            np.exp(-2j * np.pi * pos[i] * Zr[i] / Y[i])
+        vecs.append(ph * w)
+    vecs[0] = vecs[0] / np.prod(Y)
+    return _centered_ifft_real_separable(vecs, N)
+
+
 def get_shift_inclusion(N, h, Y):
     """Phase factor of an inclusion at position h (materials.py:317-330)."""
     N = np.asarray(N, dtype=np.int64)
@@ -273,24 +311,35 @@ class Material:
     # -- nodal evaluation -------------------------------------------------------
     def get_topologies(self, coord):
         """Characteristic functions at the nodes, summed over the 3^d periodic
-        images of each inclusion (materials.py:212-301)."""
+        images of each inclusion (materials.py:212-301).  coord are the
+        tensor-product nodes of Grid.get_coordinates."""
         incs = self.conf['inclusions']
         params, poss = self.conf['params'], self.conf['positions']
         d = coord.shape[0]
         grid = coord.shape[1:]
         images = list(itertools.product((-1, 0, 1), repeat=d))
+        # boxes and pyramids are products over the axes, so their sum over the
+        # 3^d periodic images is the product of per-axis sums over 3 images
+        axes = [coord[a][(0,) * a + (slice(None),) + (0,) * (d - a - 1)] for a in range(d)]
+
+        def outer(vs):
+            t = vs[0]
+            for v in vs[1:]:
+                t = np.multiply.outer(t, v)
+            return t.reshape(grid)
         topos = []
         for ii, kind in enumerate(incs):
             if kind in inclusion_keys['cube']:
                 p = np.asarray(params[ii], dtype=np.float64)
                 x0 = np.asarray(poss[ii], dtype=np.float64)
-                t = np.zeros(grid)
-                for im in images:
-                    loc = np.ones(grid, dtype=bool)
-                    for a in range(d):
-                        u = coord[a] - x0[a] + self.Y[a] * im[a]
-                        loc &= (u > -p[a] / 2) & (u <= p[a] / 2)
-                    t += loc
+                vs = []
+                for a in range(d):
+                    va = np.zeros(grid[a])
+                    for im in (-1, 0, 1):
+                        u = axes[a] - x0[a] + self.Y[a] * im
+                        va += (u > -p[a] / 2) & (u <= p[a] / 2)
+                    vs.append(va)
+                t = outer(vs)
             elif kind in inclusion_keys['ball']:
                 x0 = np.asarray(poss[ii], dtype=np.float64)
                 t = np.zeros(grid)
@@ -302,13 +351,14 @@ class Material:
             elif kind in inclusion_keys['pyramid']:
                 p = np.asarray(params[ii], dtype=np.float64)
                 x0 = np.asarray(poss[ii], dtype=np.float64)
-                t = np.zeros(grid)
-                for im in images:
-                    loc = np.ones(grid)
-                    for a in range(d):  # the reference shifts pyramids by 2*Y per image
-                        u = coord[a] - x0[a] + 2 * self.Y[a] * im[a]
-                        loc = loc * np.maximum(1 - np.abs(u) / (p[a] / 2.), 0.)
-                    t += loc
+                vs = []
+                for a in range(d):  # the reference shifts pyramids by 2*Y per image
+                    va = np.zeros(grid[a])
+                    for im in (-1, 0, 1):
+                        u = axes[a] - x0[a] + 2 * self.Y[a] * im
+                        va += np.maximum(1 - np.abs(u) / (p[a] / 2.), 0.)
+                    vs.append(va)
+                t = outer(vs)
             elif kind == 'otherwise':
                 t = np.ones(grid) - sum(topos) if topos else np.ones(grid)
                 if not (t >= 0).all():
@@ -351,18 +401,24 @@ class Material:
         params, poss = self.conf['params'], self.conf['positions']
         chars = []
         SS = None
+        shift_pos = None   # the phase of the last inclusion with a position (as SS)
         for ii, incl in enumerate(incs):
             if isinstance(poss[ii], np.ndarray):
-                SS = get_shift_inclusion(N2, poss[ii], self.Y)
+                shift_pos = np.asarray(poss[ii], dtype=np.float64)
+                SS = None
             if incl in inclusion_keys['cube']:
-                chars.append(_centered_ifft_real(SS * get_weights_con(params[ii], N2, self.Y), N2))
+                # separable spectrum: 1D transforms and an outer product
+                chars.append(_separable_char('cube', np.asarray(params[ii], dtype=np.float64),
+                                             shift_pos, N2, self.Y))
             elif incl in inclusion_keys['ball']:
+                if SS is None:
+                    SS = get_shift_inclusion(N2, shift_pos, self.Y)
                 r = params[ii] / 2
                 W = np.zeros(tuple(N2)) if r == 0 else get_weights_circ(r, N2, self.Y)
                 chars.append(_centered_ifft_real(SS * W, N2))
             elif incl in inclusion_keys['pyramid']:
-                W = get_weights_lin(np.asarray(params[ii]) / 2., N2, self.Y)
-                chars.append(_centered_ifft_real(SS * W, N2))
+                chars.append(_separable_char('pyramid', np.asarray(params[ii], dtype=np.float64) / 2.,
+                                             shift_pos, N2, self.Y))
             elif incl == 'all':
                 chars.append(np.ones(tuple(N2)))
             elif incl == 'otherwise':
