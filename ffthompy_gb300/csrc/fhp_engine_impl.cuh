@@ -99,6 +99,7 @@ class Engine final : public EngineBase {
       const int bodd = b - ((b + 1) % 2);
       gp_.h[i] = (bodd - 1) / 2;
       gp_.Y[i] = i < d ? cfg_.Y[i] : 1.0;
+      gp_.invY[i] = 1.0 / gp_.Y[i];
     }
     int st;
     if ((st = make_line(g_.n2, l2_)) != ST_OK) return st;

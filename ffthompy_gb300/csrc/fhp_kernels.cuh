@@ -60,6 +60,7 @@ struct GreenParams {
   int proj;       // 1: G1 (compatible, primal), 2: G2 (equilibrated, dual), 0: band only
   int h[3];       // band half-widths |k_i| <= h_i, real axis order
   double Y[3];    // cell size, real axis order
+  double invY[3]; // 1 / Y
   double scale;   // Ga scale prod(2N-1)/prod(N); 1 for GaNi
 };
 
@@ -95,7 +96,7 @@ __device__ __forceinline__ void green_apply_d(const GreenParams& gp, const int* 
     const int ki = k[i];
     if (ki > gp.h[i] || -ki > gp.h[i]) inband = false;
     if (ki != 0) zero = false;
-    xi[i] = R(ki) / R(gp.Y[i]);
+    xi[i] = R(ki) * R(gp.invY[i]);
   }
   constexpr bool scalar = PHYS == 0;
   const R s = R(gp.scale);
@@ -119,7 +120,9 @@ __device__ __forceinline__ void green_apply_d(const GreenParams& gp, const int* 
     cplx<R> t = mkc<R>(R(0), R(0));
 #pragma unroll
     for (int i = 0; i < DIM; ++i) { t.x += xi[i] * x[i].x; t.y += xi[i] * x[i].y; }
-    t.x /= nn; t.y /= nn;
+    const R inn = R(1) / nn;
+    t.x *= inn;
+    t.y *= inn;
 #pragma unroll
     for (int i = 0; i < DIM; ++i) {
       cplx<R> g1 = mkc<R>(xi[i] * t.x, xi[i] * t.y);
