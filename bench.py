@@ -260,11 +260,13 @@ def run_reference(args):
 # ----------------------------------------------------------------------------
 # the GPU arm
 # ----------------------------------------------------------------------------
-def ensemble_measure(count=512, sizes=(63, 127, 255, 511), seed=12, tol=1e-6, workers=16):
+def ensemble_measure(count=512, sizes=(63, 127, 255, 511), seed=12, tol=1e-6, workers=16,
+                     precision='f64'):
     """Many independent 2D GaNi cells (thresholded Gaussian random fields,
     length 0.1, 0.4-quantile, contrast log-uniform in [2, 1000], n drawn from
-    sizes, 2 loads each) solved together by homogenize_many, FP64 to tol:
-    aggregate Mvoxel-iter/s over all instances."""
+    sizes, 2 loads each) solved together by homogenize_many to tol (FP64, or
+    mixed: FP32 inner CG refined in FP64): aggregate Mvoxel-iter/s over all
+    instances."""
     import torch
     from ffthompy_gb300 import workloads
     from ffthompy_gb300.batch import homogenize_many
@@ -276,14 +278,14 @@ def ensemble_measure(count=512, sizes=(63, 127, 255, 511), seed=12, tol=1e-6, wo
         coefs.append(workloads.grf_phase_coefficient((n, n), ell=0.1, quantile=0.4,
                                                      contrast=contrast,
                                                      seed=int(rng.integers(1 << 30))))
-    homogenize_many(coefs[:workers], tol=tol, workers=workers)   # plans, first launches
+    homogenize_many(coefs[:workers], tol=tol, workers=workers, precision=precision)  # warm
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    res = homogenize_many(coefs, tol=tol, workers=workers)
+    res = homogenize_many(coefs, tol=tol, workers=workers, precision=precision)
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     vox_it = sum(int(np.prod(A.shape[2:])) * sum(r['kit_primal']) for A, r in zip(coefs, res))
-    return {'instances': count, 'sizes': list(sizes), 'loads': 2, 'precision': 'f64',
+    return {'instances': count, 'sizes': list(sizes), 'loads': 2, 'precision': precision,
             'tol': tol, 'voxels': int(sum(np.prod(A.shape[2:]) for A in coefs)),
             'seconds': dt, 'Mvoxel_iter_per_s': vox_it / dt / 1e6,
             'all_converged': all(r['status_primal'] == [0, 0] for r in res)}
@@ -478,6 +480,7 @@ def run_gpu(args):
         extras['potential'] = potential_measure(vals, w, tol)
     if not args.no_ensemble:
         extras['ensemble_grf2d'] = ensemble_measure()
+        extras['ensemble_grf2d_mixed'] = ensemble_measure(precision='mixed')
 
     if rank != 0:
         return

@@ -554,6 +554,32 @@ class Engine final : public EngineBase {
     FHP_LAUNCHED();
     k_update_all_done<<<1, 1, 0, s>>>(st_, g_.L, all_done_);
     FHP_LAUNCHED();
+    // One iteration's launches captured once per solve into a CUDA graph and
+    // replayed per iteration (one launch instead of about ten: small grids are
+    // launch-bound).  Direct launches when profiling (the per-kernel events)
+    // or when the stream cannot be captured (the legacy default stream).
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    long long per_iter = 0;
+    if (!prof.on && maxiter > 0 &&
+        cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      const long long l0 = launches;
+      const int cst = cg_iteration(dlog, log_rows, s);
+      const cudaError_t e = cudaStreamEndCapture(s, &graph);
+      per_iter = launches - l0;
+      launches = l0;
+      if (cst != ST_OK || e != cudaSuccess || !graph ||
+          cudaGraphInstantiate(&gexec, graph, 0) != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        graph = nullptr;
+        gexec = nullptr;
+      }
+    }
+    (void)cudaGetLastError();  // a refused capture leaves no error behind
+    auto release_graph = [&]() {
+      if (gexec) cudaGraphExecDestroy(gexec);
+      if (graph) cudaGraphDestroy(graph);
+    };
     // iterations, in chunks between host checks of all_done
     int done_iters = 0;
     int chunk = 2;
@@ -563,11 +589,25 @@ class Engine final : public EngineBase {
       if (*h_done_) break;
       const int nit = std::min(chunk, maxiter - done_iters);
       for (int it = 0; it < nit; ++it) {
-        if ((st = cg_iteration(dlog, log_rows, s)) != ST_OK) { cudaFreeAsync(dlog, s); return st; }
+        if (gexec) {
+          const cudaError_t e = cudaGraphLaunch(gexec, s);
+          if (e != cudaSuccess) {
+            set_error(std::string("cudaGraphLaunch: ") + cudaGetErrorString(e));
+            release_graph();
+            cudaFreeAsync(dlog, s);
+            return ST_CUDA;
+          }
+          launches += per_iter;
+        } else if ((st = cg_iteration(dlog, log_rows, s)) != ST_OK) {
+          release_graph();
+          cudaFreeAsync(dlog, s);
+          return st;
+        }
       }
       done_iters += nit;
       chunk = std::min(chunk * 2, 32);
     }
+    release_graph();
     // FP32 fields: the iterate drifts out of range(G) by roundoff accumulated
     // over the iterations, and that component enters the energy to first
     // order. One projection x <- G x (the identity in exact arithmetic) puts

@@ -525,3 +525,29 @@ def test_mixed_refinement_reaches_tol(name):
     AHm, AH64 = pm.energy(X), p64.energy(X64)
     print('AH mixed vs f64', _relmax(AHm, AH64), 'kits', i64['kit'])
     assert _relmax(AHm, AH64) < 1e-9
+
+
+@pytest.mark.parametrize('precision', ['f64', 'f32', 'mixed'])
+def test_cg_graph_replay_equals_direct_launches(precision):
+    """On a non-default stream each CG iteration is one CUDA-graph launch; on
+    the legacy default stream (not capturable) the kernels launch directly.
+    Both run the same kernels in the same order: identical iterates."""
+    from ffthompy_gb300.engine import GalerkinPlan
+    rng = np.random.default_rng(4)
+    N = (15, 17, 9)
+    a = 1. + 49. * (rng.random(N) < 0.3)
+    A = np.einsum('ij,...->ij...', np.eye(3), a)
+    out = {}
+    for name in ('default', 'side'):
+        plan = GalerkinPlan(N, np.ones(3), physics='scalar', nloads=3, precision=precision)
+        stream = torch.cuda.default_stream() if name == 'default' else torch.cuda.Stream()
+        with torch.cuda.stream(stream):
+            plan.set_coefficient(A)
+            X, info = plan.cg(plan.rhs_macro(1), tol=1e-6 if precision == 'f32' else 1e-9,
+                              maxiter=500)
+            AH = plan.energy(X)
+        torch.cuda.synchronize()
+        out[name] = (X.cpu().numpy(), info['kit'], AH)
+    assert out['default'][1] == out['side'][1]
+    np.testing.assert_array_equal(out['default'][0], out['side'][0])
+    np.testing.assert_array_equal(out['default'][2], out['side'][2])
