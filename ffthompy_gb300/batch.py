@@ -7,7 +7,9 @@ per instance - and returns one A_H per instance.
 
 Each worker thread owns a CUDA stream and one GalerkinPlan per grid size it
 meets (plans keep their buffers, so nothing is allocated per instance after
-the first of a size).  The library's C calls release the GIL (ctypes), so the
+the first of a size).  A host coefficient is solved by one library call
+(fhp_homogenize_host: upload, right-hand sides, CG, A_H) per primal / dual
+problem.  The library's C calls release the GIL (ctypes), so the
 instances of different workers run concurrently on the GPU: small grids,
 whose launches alone would leave most SMs idle, fill the GPU together.  Each
 instance is solved with its own CG scalars and stopping test, exactly as a
@@ -20,7 +22,9 @@ import numpy as np
 import torch
 
 from . import _lib
-from .engine import GalerkinPlan, coef_kind_of_torch, pack_coefficient_torch, require_cuda
+from .engine import (GalerkinPlan, coef_kind_of, coef_kind_of_torch, pack_coefficient,
+                     pack_coefficient_torch, require_cuda)
+from .materials import get_inverse
 
 
 def homogenize_many(coefs, Y=None, physics='scalar', tol=1e-6, maxiter=1000,
@@ -53,9 +57,25 @@ def homogenize_many(coefs, Y=None, physics='scalar', tol=1e-6, maxiter=1000,
             if plan is None:
                 plan = GalerkinPlan(N, Yi, physics=physics, precision=precision)
                 st.plans[key] = plan
-            At = torch.as_tensor(np.asarray(A, dtype=np.float64) if not isinstance(A, torch.Tensor)
-                                 else A).to(device, torch.float64, non_blocking=False)
             res = {}
+            if not isinstance(A, torch.Tensor):
+                # host coefficients: one library call per solve (upload, right-
+                # hand sides, CG, A_H) on this worker's stream, GIL released
+                Ah = np.asarray(A, dtype=np.float64)
+                for pd in primaldual:
+                    proj = 1 if pd == 'primal' else 2
+                    Ap = Ah if pd == 'primal' else get_inverse(Ah)
+                    kind = coef_kind_of(Ap)
+                    AH, kit, nres, _ = plan.homogenize_host(packed=pack_coefficient(Ap, kind),
+                                                            kind=kind, proj=proj, tol=tol,
+                                                            maxiter=maxiter)
+                    res[pd] = AH if pd == 'primal' else np.linalg.inv(AH)
+                    res['kit_' + pd] = kit
+                    res['status_' + pd] = [0 if (k == 0 or r <= tol) else _lib.FHP_NONCONVERGED
+                                           for k, r in zip(kit, nres)]
+                out[i] = res
+                return
+            At = A.to(device, torch.float64, non_blocking=False)
             for pd in primaldual:
                 proj = 1 if pd == 'primal' else 2
                 Ap = At if pd == 'primal' else _inverse_field(At)

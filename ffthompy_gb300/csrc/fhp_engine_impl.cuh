@@ -444,19 +444,19 @@ class Engine final : public EngineBase {
       FHP_CHECK(cudaMalloc(&A_, n * sizeof(R)));
       A_elems_ = n;
     }
+    // host values go through a stream-ordered staging buffer (cudaFree would
+    // synchronise the device and serialise plans on other streams); the copy
+    // from pageable memory has read the host buffer when the call returns
     double* tmp = nullptr;
     const double* src = values;
     if (!on_device) {
-      FHP_CHECK(cudaMalloc(&tmp, n * sizeof(double)));
+      FHP_CHECK(cudaMallocAsync(&tmp, n * sizeof(double), s));
       FHP_CHECK(cudaMemcpyAsync(tmp, values, n * sizeof(double), cudaMemcpyHostToDevice, s));
       src = tmp;
     }
     k_convert<R, double><<<grid_for(n), kThreads, 0, s>>>((long long)n, src, A_);
     FHP_LAUNCHED();
-    if (tmp) {
-      FHP_CHECK(cudaStreamSynchronize(s));
-      cudaFree(tmp);
-    }
+    if (tmp) FHP_CHECK(cudaFreeAsync(tmp, s));
     coef_kind_ = kind;
     return ST_OK;
   }
