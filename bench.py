@@ -61,6 +61,8 @@ def parse():
                          'grid >= 2N-1; full: CG on the 2N-1 grid (the reference layout)')
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-fp64', action='store_true')
+    ap.add_argument('--no-fibres', action='store_true',
+                    help='skip the 127^3 elasticity (fibres) time to A_H')
     ap.add_argument('--no-ensemble', action='store_true',
                     help='skip the 512-instance 2D ensemble measurement')
     ap.add_argument('--no-potential', action='store_true',
@@ -291,6 +293,38 @@ def ensemble_measure(count=512, sizes=(63, 127, 255, 511), seed=12, tol=1e-6, wo
             'all_converged': all(r['status_primal'] == [0, 0] for r in res)}
 
 
+def fibres_measure(n=127, tol=1e-6, seed=0):
+    """Linear elasticity with 8 parallel fibres on n^3 (Mandel 6x6 per voxel,
+    phases (E, nu) = (1, 0.3) and (10, 0.2)), GaNi solve of the 6 unit strains,
+    primal and dual, postprocessed with GaNi and Ga (order 0) bounds: the whole
+    Problem.calculate() through the drop-in API, FP64 and mixed precision."""
+    import torch
+    from ffthompy_gb300 import workloads
+    from ffthompy_gb300.problem import Problem
+    vals = workloads.fibres_coefficient((n, n, n), seed=seed)
+    N = np.array([n, n, n])
+    out = {'grid': [n] * 3, 'loads': 6, 'tol': tol}
+    mats = {}
+    for prec in ('f64', 'mixed'):
+        prob = {'name': 'fibres%d' % n, 'physics': 'elasticity',
+                'material': workloads.fun_material(vals),
+                'solve': {'kind': 'GaNi', 'N': N, 'primaldual': ['primal', 'dual'],
+                          'precision': prec},
+                'solver': {'kind': 'CG', 'tol': tol, 'maxiter': 1000},
+                'postprocess': [{'kind': 'GaNi'}, {'kind': 'Ga', 'order': 0, 'P': N}]}
+        pb = Problem(prob, None)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pb.calculate()
+        torch.cuda.synchronize()
+        out['seconds_' + prec] = time.perf_counter() - t0
+        out['kit_primal_' + prec] = [int(r['info']['kit']) for r in pb.output['res_primal']]
+        mats[prec] = pb.output['mat_primal']['AH_GaNi_primal']
+    out['AH_rel_diff_mixed_vs_f64'] = float(np.abs(mats['mixed'] - mats['f64']).max()
+                                            / np.abs(mats['f64']).max())
+    return out
+
+
 def potential_measure(vals, w, tol, steps=2):
     """Time to A_H of the potential formulation (fhp_potential_*) for the
     GaNi discretisation on the image grid, 3 loads batched, FP32 with FP64
@@ -478,6 +512,8 @@ def run_gpu(args):
     # formulation's A_H on the same grid and tolerance
     if not args.no_potential:
         extras['potential'] = potential_measure(vals, w, tol)
+    if not args.no_fibres:
+        extras['fibres127'] = fibres_measure()
     if not args.no_ensemble:
         extras['ensemble_grf2d'] = ensemble_measure()
         extras['ensemble_grf2d_mixed'] = ensemble_measure(precision='mixed')
