@@ -128,7 +128,9 @@ class Engine final : public EngineBase {
     row_ctas_ = (int)(((long long)g_.n0 * g_.n1 + rows_ - 1) / rows_);
     // strided c2c on axis 1 (3D) and projection on the first real axis
     if (d == 3) {
-      T1_ = tile_cols(l1_.dev.ld, 1, (long long)g_.n2h);
+      // column passes: twice the line target (as the band-axis passes) fills
+      // the radix stages of short lines and lengthens the contiguous rows
+      T1_ = tile_cols(l1_.dev.ld, 1, (long long)g_.n2h, 2 * kTargetElems);
     }
     const LineDev<R>& lp = (d == 3) ? l0_.dev : l1_.dev;
     const long long pin = (d == 3) ? (long long)g_.n1 * g_.n2h : (long long)g_.n2h;
@@ -137,7 +139,7 @@ class Engine final : public EngineBase {
       set_error("projection line too long for shared memory");
       return ST_BAD_ARG;
     }
-    if (d == 3) T0_ = tile_cols(l0_.dev.ld, 1, (long long)g_.n1 * g_.n2h);
+    if (d == 3) T0_ = tile_cols(l0_.dev.ld, 1, (long long)g_.n1 * g_.n2h, 2 * kTargetElems);
     if (cfg_.integ[0] > 0) {
       if ((st = init_band()) != ST_OK) return st;
     }
