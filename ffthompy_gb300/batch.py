@@ -7,9 +7,9 @@ per instance - and returns one A_H per instance.
 
 Each worker thread owns a CUDA stream and one GalerkinPlan per grid size it
 meets (plans keep their buffers, so nothing is allocated per instance after
-the first of a size).  A host coefficient is solved by one library call
-(fhp_homogenize_host: upload, right-hand sides, CG, A_H) per primal / dual
-problem.  The library's C calls release the GIL (ctypes), so the
+the first of a size).  A host coefficient's primal problem is solved by one
+library call (fhp_homogenize_host: upload, right-hand sides, CG, A_H); its
+dual coefficient is uploaded and inverted on the GPU (fhp_coefficient_inverse).  The library's C calls release the GIL (ctypes), so the
 instances of different workers run concurrently on the GPU: small grids,
 whose launches alone would leave most SMs idle, fill the GPU together.  Each
 instance is solved with its own CG scalars and stopping test, exactly as a
@@ -22,9 +22,8 @@ import numpy as np
 import torch
 
 from . import _lib
-from .engine import (GalerkinPlan, coef_kind_of, coef_kind_of_torch, pack_coefficient,
-                     pack_coefficient_torch, require_cuda)
-from .materials import get_inverse
+from .engine import (GalerkinPlan, coef_kind_of, coef_kind_of_torch, coefficient_inverse,
+                     pack_coefficient, pack_coefficient_torch, require_cuda)
 
 
 def homogenize_many(coefs, Y=None, physics='scalar', tol=1e-6, maxiter=1000,
@@ -58,25 +57,28 @@ def homogenize_many(coefs, Y=None, physics='scalar', tol=1e-6, maxiter=1000,
                 plan = GalerkinPlan(N, Yi, physics=physics, precision=precision)
                 st.plans[key] = plan
             res = {}
+            on_device = list(primaldual)
             if not isinstance(A, torch.Tensor):
-                # host coefficients: one library call per solve (upload, right-
-                # hand sides, CG, A_H) on this worker's stream, GIL released
                 Ah = np.asarray(A, dtype=np.float64)
-                for pd in primaldual:
-                    proj = 1 if pd == 'primal' else 2
-                    Ap = Ah if pd == 'primal' else get_inverse(Ah)
-                    kind = coef_kind_of(Ap)
-                    AH, kit, nres, _ = plan.homogenize_host(packed=pack_coefficient(Ap, kind),
-                                                            kind=kind, proj=proj, tol=tol,
+                if 'primal' in primaldual:
+                    # host coefficient: one library call (upload, right-hand
+                    # sides, CG, A_H) on this worker's stream, GIL released
+                    kind = coef_kind_of(Ah)
+                    AH, kit, nres, _ = plan.homogenize_host(packed=pack_coefficient(Ah, kind),
+                                                            kind=kind, proj=1, tol=tol,
                                                             maxiter=maxiter)
-                    res[pd] = AH if pd == 'primal' else np.linalg.inv(AH)
-                    res['kit_' + pd] = kit
-                    res['status_' + pd] = [0 if (k == 0 or r <= tol) else _lib.FHP_NONCONVERGED
-                                           for k, r in zip(kit, nres)]
-                out[i] = res
-                return
+                    res['primal'] = AH
+                    res['kit_primal'] = kit
+                    res['status_primal'] = [0 if (k == 0 or r <= tol) else _lib.FHP_NONCONVERGED
+                                            for k, r in zip(kit, nres)]
+                on_device = [pd for pd in primaldual if pd == 'dual']
+                if not on_device:
+                    out[i] = res
+                    return
+                # the dual coefficient is inverted on the GPU
+                A = torch.from_numpy(Ah)
             At = A.to(device, torch.float64, non_blocking=False)
-            for pd in primaldual:
+            for pd in on_device:
                 proj = 1 if pd == 'primal' else 2
                 Ap = At if pd == 'primal' else _inverse_field(At)
                 kind = coef_kind_of_torch(Ap)
@@ -89,10 +91,6 @@ def homogenize_many(coefs, Y=None, physics='scalar', tol=1e-6, maxiter=1000,
             st.stream.synchronize()
         out[i] = res
 
-    if 'dual' in primaldual:
-        # torch initialises its linear-algebra backend lazily and not thread-safely:
-        # do it once here, before the workers start
-        torch.linalg.inv(torch.eye(2, dtype=torch.float64, device=device))
     with ThreadPoolExecutor(max_workers=max(1, int(workers))) as ex:
         for f in [ex.submit(run, i) for i in order]:
             f.result()
@@ -101,11 +99,5 @@ def homogenize_many(coefs, Y=None, physics='scalar', tol=1e-6, maxiter=1000,
 
 def _inverse_field(A):
     """Per-voxel inverse of a (dv, dv) + N field (the dual coefficient,
-    ffthompy/materials.py get_A_GaNi with primaldual='dual')."""
-    dv = A.shape[0]
-    N = A.shape[2:]
-    if coef_kind_of_torch(A) == _lib.FHP_COEF_ISO:
-        return torch.einsum('ij,...->ij...', torch.eye(dv, dtype=A.dtype, device=A.device),
-                            1.0 / A[0, 0])
-    M = A.reshape(dv, dv, -1).permute(2, 0, 1)
-    return torch.linalg.inv(M).permute(1, 2, 0).reshape((dv, dv) + tuple(N)).contiguous()
+    ffthompy/materials.py get_A_GaNi with primaldual='dual'), on the GPU."""
+    return coefficient_inverse(A)

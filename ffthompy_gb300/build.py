@@ -18,7 +18,7 @@ OBJDIR = os.path.join(LIBDIR, 'obj')
 LIBNAME = 'libffthompy_gb300.so'
 LIBPATH = os.path.join(LIBDIR, LIBNAME)
 SOURCES = ['fhp_engine_f64.cu', 'fhp_engine_f32.cu', 'fhp_capi.cu', 'fhp_lineplan.cpp',
-           'fhp_noalloc.cu']
+           'fhp_noalloc.cu', 'fhp_coef.cu']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 
 

@@ -441,3 +441,29 @@ def interpolate_fields(x, src, dst):
         finally:
             lib.fhp_plan_destroy(hs)
     return out.reshape(lead + dst)
+
+
+def coefficient_inverse(A, shift=False):
+    """Per-voxel inverse of a (d, d) + grid coefficient on the GPU
+    (fhp_coefficient_inverse): the reference's Gauss-Jordan elimination
+    without pivoting (trigpol.py:120-159, Tensor.inv objects.py:247-251),
+    bit-identical to it for finite input.  A: NumPy array or torch tensor;
+    shift=True also moves a centred origin to 0 (the ifftshift of
+    Material.get_A_GaNi, materials.py:115-123).  Returns a float64 CUDA tensor.
+    """
+    require_cuda()
+    lib = _lib.load()
+    if isinstance(A, np.ndarray):
+        A = torch.from_numpy(np.ascontiguousarray(A, dtype=np.float64))
+    A = A.to('cuda' if not A.is_cuda else A.device, torch.float64).contiguous()
+    d = int(A.shape[0])
+    if A.dim() < 3 or A.shape[1] != d:
+        raise NotImplementedError('Non-square matrix!')
+    grid = tuple(int(n) for n in A.shape[2:])
+    out = torch.empty_like(A)
+    n = (ctypes.c_int * len(grid))(*grid)
+    stream = ctypes.c_void_p(torch.cuda.current_stream(A.device).cuda_stream)
+    _lib.check(lib.fhp_coefficient_inverse(len(grid), n, d, ctypes.c_void_p(A.data_ptr()),
+                                           ctypes.c_void_p(out.data_ptr()), int(bool(shift)),
+                                           stream), 'fhp_coefficient_inverse')
+    return out

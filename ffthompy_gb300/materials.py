@@ -226,9 +226,11 @@ def _gpu_available():
 def ga_grid_coefficient_gpu(vals, P, Nbar, Y, order, target=None):
     """Grid-based Ga coefficient on the GPU (fhp_ga_grid_coefficient).
 
-    vals: (dv, dv) + P nodal values, centred origin.  Distinct component fields
-    are transformed once; returns a torch tensor (dv, dv) + grid, origin 0,
-    grid = Nbar or the larger target grid (same trigonometric polynomial).
+    vals: (dv, dv) + P nodal values, a NumPy array with the centred origin or a
+    CUDA tensor with origin 0 (as coefficient_inverse(..., shift=True) returns
+    it).  Distinct component fields are transformed once; returns a torch
+    tensor (dv, dv) + grid, origin 0, grid = Nbar or the larger target grid
+    (same trigonometric polynomial).
     """
     grid = Nbar if target is None else np.asarray(target, dtype=np.int64)
     import ctypes
@@ -237,14 +239,16 @@ def ga_grid_coefficient_gpu(vals, P, Nbar, Y, order, target=None):
     lib = _lib.load()
     dv = vals.shape[0]
     d = len(P)
+    on_device = not isinstance(vals, np.ndarray)
+    same = torch.equal if on_device else np.array_equal
     comps, where = [], {}
     for m in range(dv):
         for n in range(dv):
             v = vals[m, n]
-            if not v.any():
+            if not bool(v.any()):
                 continue
             for k, c in enumerate(comps):
-                if np.array_equal(c, v):
+                if same(c, v):
                     where[(m, n)] = k
                     break
             else:
@@ -258,8 +262,11 @@ def ga_grid_coefficient_gpu(vals, P, Nbar, Y, order, target=None):
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     for k0 in range(0, len(comps), 6):
         chunk = comps[k0:k0 + 6]
-        img = np.stack([np.fft.ifftshift(c) for c in chunk])
-        dimg = torch.from_numpy(np.ascontiguousarray(img)).to('cuda')
+        if on_device:
+            dimg = torch.stack(chunk).contiguous()
+        else:
+            img = np.stack([np.fft.ifftshift(c) for c in chunk])
+            dimg = torch.from_numpy(np.ascontiguousarray(img)).to('cuda')
         dout = torch.empty((len(chunk),) + tuple(int(n) for n in grid), dtype=torch.float64,
                            device='cuda')
         hp, ho = ctypes.c_void_p(), ctypes.c_void_p()
@@ -389,8 +396,14 @@ class Material:
         A = self.evaluate(Grid.get_coordinates(N, self.Y))
         name = 'A_GaNi'
         if primaldual == 'dual':
-            A = get_inverse(A)
             name = 'inv(A_GaNi)'
+            if _gpu_available():
+                from .engine import coefficient_inverse
+                out = Tensor(name=name, val=coefficient_inverse(A, shift=True), order=2,
+                             multype=21, origin=0)
+                out.Y = self.Y
+                return out
+            A = get_inverse(A)
         out = self._origin0(A, name)
         out.Y = self.Y
         return out
@@ -438,7 +451,8 @@ class Material:
             P = np.asarray(P, dtype=np.int64)
             vals = self.evaluate(Grid.get_coordinates(P, self.Y))
             if primaldual == 'dual':
-                vals = get_inverse(vals)
+                from .engine import coefficient_inverse
+                vals = coefficient_inverse(vals, shift=True)
             out = Tensor(name='A_Ga_o{0}_P{1}'.format(order, np.array(P).max()),
                          val=ga_grid_coefficient_gpu(vals, P, Nbar, self.Y, order, target=grid),
                          order=2, multype=21, origin=0)
@@ -477,14 +491,17 @@ class Material:
                 P = self.conf['P']
             P = np.asarray(P, dtype=np.int64)
             vals = self.evaluate(Grid.get_coordinates(P, self.Y))
-            if primaldual == 'dual':
-                vals = get_inverse(vals)
             name = 'A_Ga_o{0}_P{1}'.format(order, np.array(P).max())
             if _gpu_available() and np.all(Nbar % 2 == 1) and Nbar.size == P.size:
+                if primaldual == 'dual':
+                    from .engine import coefficient_inverse
+                    vals = coefficient_inverse(vals, shift=True)
                 out = Tensor(name=name, val=ga_grid_coefficient_gpu(vals, P, Nbar, self.Y, order),
                              order=2, multype=21, origin=0)
                 out.Y = self.Y
                 return out
+            if primaldual == 'dual':
+                vals = get_inverse(vals)
             h = self.Y / P
             W = get_weights_con(h, Nbar, self.Y) if order in (0, 'constant') \
                 else get_weights_lin(h, Nbar, self.Y)

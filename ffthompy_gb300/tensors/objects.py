@@ -175,12 +175,11 @@ class Tensor:
         raise NotImplementedError('This type ({}) of norm is not implemented!'.format(ntype))
 
     def inv(self):
-        """Per-voxel matrix inverse (objects.py:247-251)."""
+        """Per-voxel matrix inverse (objects.py:247-251): the reference's
+        Gauss-Jordan elimination (trigpol.py:120-159) in the CUDA library."""
         assert self.order == 2 and self.shape[0] == self.shape[1]
-        d = self.shape[0]
-        m = self.data.reshape(d, d, -1).permute(2, 0, 1)
-        inv = torch.linalg.inv(m).permute(1, 2, 0).reshape(self.data.shape)
-        return self.copy(name='inv({})'.format(self.name), val=inv)
+        from ..engine import coefficient_inverse
+        return self.copy(name='inv({})'.format(self.name), val=coefficient_inverse(self.data))
 
     def shift(self, origin=None):
         """Move the origin between centred ('c') and 0 (objects.py:169-186)."""

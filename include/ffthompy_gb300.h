@@ -217,6 +217,24 @@ int fhp_ga_grid_coefficient(fhp_plan plan_img, fhp_plan plan_out, const void* im
                             void* stream);
 
 /*
+ * Per-voxel inverse of a field of d x d matrices (the dual coefficient):
+ * Ainv(x) = A(x)^-1 by Gauss-Jordan elimination without pivoting, in the
+ * reference's order, each product and difference rounded separately as NumPy
+ * evaluates them: bit-identical to the reference for finite input, and a zero
+ * pivot gives the reference's Inf / NaN.  A and Ainv are float64 device arrays
+ * [d][d][n0]...[n_{dim-1}] (C order) that must not overlap; shift = 1 writes the
+ * result ifftshift-ed over the grid axes (Ainv at j from A at (j + n/2) mod n,
+ * a centred origin moved to 0).  1 <= dim <= 3, 1 <= d <= 6, n[i] <= 65535.
+ * Written on `stream`; the call does not synchronise.
+ * Replaces: get_inverse (ffthompy/trigpol.py:120-159) behind Tensor.inv
+ * (ffthompy/tensors/objects.py:247-251), and with shift = 1 the inverse plus
+ * origin shift of Material.get_A_GaNi(primaldual='dual')
+ * (ffthompy/materials.py:115-123).
+ */
+int fhp_coefficient_inverse(int dim, const int* n, int d, const double* A, double* Ainv,
+                            int shift, void* stream);
+
+/*
  * Per-kernel timing with CUDA events recorded on the launch stream around each
  * operator / CG pass (enable resets the counters).  fhp_profile_read returns
  * up to max_kinds entries: names (64 chars each), launches, total ms and the

@@ -36,7 +36,11 @@ solv_<name>.npz
     206-285) on a scalar FiGFA operator: solution, iteration count, final
     relative residual.
 
-Usage:  python tests/golden/make_golden.py [REFERENCE_DIR [pickles|run|op|pot|solv ...]]
+inv_<name>.npz
+    Per-voxel inverses of get_inverse (ffthompy/trigpol.py:120-159) of
+    seeded matrix fields, one with zero pivots (Inf / NaN outputs).
+
+Usage:  python tests/golden/make_golden.py [REFERENCE_DIR [pickles|run|op|pot|solv|inv ...]]
 """
 import collections
 import collections.abc
@@ -403,11 +407,35 @@ def potential_cases():
         _save('pot_' + name, meta, arrays)
 
 
+def inverse_cases():
+    """Per-voxel inverses of the reference's get_inverse (ffthompy/trigpol.py:
+    120-159): seeded matrices a + d I (symmetric and not) for d = 1, 2, 3, 6 on
+    1D-3D grids, and a field with zero pivots at some voxels (Inf / NaN)."""
+    from ffthompy.trigpol import get_inverse
+    rng = np.random.default_rng(17)
+    cases = [('d1_1d_7', 1, (7,), 'full'), ('d2_2d_5x4', 2, (5, 4), 'sym'),
+             ('d3_3d_3x4x5', 3, (3, 4, 5), 'full'), ('d6_3d_4x3x5', 6, (4, 3, 5), 'sym'),
+             ('d3_2d_6x5_zero_pivot', 3, (6, 5), 'zero')]
+    for name, d, N, kind in cases:
+        A = rng.standard_normal((d, d) + N)
+        if kind == 'sym':
+            A = 0.5 * (A + A.transpose((1, 0) + tuple(range(2, 2 + len(N)))))
+        A = A + np.einsum('ij,...->ij...', d * np.eye(d), np.ones(N))
+        if kind == 'zero':
+            A[0, 0, 1, 2] = 0.
+            A[1, 1, 3, 0] = A[1, 0, 3, 0] * A[0, 1, 3, 0] / A[0, 0, 3, 0]
+            A[0, 0, 5, 4] = 0.
+            A[0, 1, 5, 4] = 0.
+        arrays = {'A': A, 'inv': np.asarray(get_inverse(A), dtype=np.float64)}
+        _save('inv_' + name, dict(d=d, N=list(N), kind=kind), arrays)
+
+
 if __name__ == '__main__':
     _install_shim()
     import warnings
     warnings.simplefilter('ignore')
-    only = sys.argv[2:] if len(sys.argv) > 2 else ['pickles', 'run', 'op', 'pot', 'solv']
+    only = sys.argv[2:] if len(sys.argv) > 2 else ['pickles', 'run', 'op', 'pot', 'solv',
+                                                   'inv']
     if 'pickles' in only:
         golden_pickles()
     if 'run' in only:
@@ -418,3 +446,5 @@ if __name__ == '__main__':
         potential_cases()
     if 'solv' in only:
         solver_cases()
+    if 'inv' in only:
+        inverse_cases()
