@@ -257,6 +257,48 @@ __device__ __forceinline__ void dft16(cplx<R>* v) {
   }
 }
 
+// 32 = 2 x 16: X[k] = E[k] + W32^k O[k], X[k+16] = E[k] - W32^k O[k] with E, O
+// the 16-point DFTs of the even and odd samples (natural order in and out).
+template <typename R>
+__device__ __forceinline__ void dft32(cplx<R>* v) {
+  const R c16 = R(0.98078528040323044912618223613424);   // cos(pi/16)
+  const R s16 = R(0.19509032201612826784828486847702);   // sin(pi/16)
+  const R c316 = R(0.83146961230254523707878837761791);  // cos(3pi/16)
+  const R s316 = R(0.55557023301960222474283081394853);  // sin(3pi/16)
+  const R c8 = R(0.92387953251128675612818318939679);    // cos(pi/8)
+  const R s8 = R(0.38268343236508977172845998403040);    // sin(pi/8)
+  const R r = R(0.70710678118654752440084436210485);
+  cplx<R> e[16], o[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    e[k] = v[2 * k];
+    o[k] = v[2 * k + 1];
+  }
+  dft16<R>(e);
+  dft16<R>(o);
+  // o[k] *= W32^k = (cos(pi k/16), -sin(pi k/16))
+  o[1] = cmul<R>(o[1], mkc<R>(c16, -s16));
+  o[2] = cmul<R>(o[2], mkc<R>(c8, -s8));
+  o[3] = cmul<R>(o[3], mkc<R>(c316, -s316));
+  o[4] = cmul<R>(o[4], mkc<R>(r, -r));
+  o[5] = cmul<R>(o[5], mkc<R>(s316, -c316));
+  o[6] = cmul<R>(o[6], mkc<R>(s8, -c8));
+  o[7] = cmul<R>(o[7], mkc<R>(s16, -c16));
+  o[8] = cmul_mi<R>(o[8]);
+  o[9] = cmul<R>(o[9], mkc<R>(-s16, -c16));
+  o[10] = cmul<R>(o[10], mkc<R>(-s8, -c8));
+  o[11] = cmul<R>(o[11], mkc<R>(-s316, -c316));
+  o[12] = cmul<R>(o[12], mkc<R>(-r, -r));
+  o[13] = cmul<R>(o[13], mkc<R>(-c316, -s316));
+  o[14] = cmul<R>(o[14], mkc<R>(-c8, -s8));
+  o[15] = cmul<R>(o[15], mkc<R>(-c16, -s16));
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    v[k] = cadd<R>(e[k], o[k]);
+    v[k + 16] = csub<R>(e[k], o[k]);
+  }
+}
+
 // cos(2 pi m / r) and sin(2 pi m / r), m = 1 .. (r-1)/2, of the odd prime
 // radices (evaluated in 50-digit decimal arithmetic from Machin's pi and
 // the Taylor series), so the DFT_r constants are immediates, not table loads.
@@ -358,6 +400,7 @@ __device__ __forceinline__ void dft_fwd(cplx<R>* v, const cplx<R>* __restrict__ 
   else if constexpr (RAD == 5) dft5<R>(v);
   else if constexpr (RAD == 8) dft8<R>(v);
   else if constexpr (RAD == 16) dft16<R>(v);
+  else if constexpr (RAD == 32) dft32<R>(v);
   else dft_odd<R, RAD>(v, tw, nf);
 }
 
@@ -494,22 +537,29 @@ __device__ __forceinline__ void stage_dispatch(cplx<R>* buf, int ld, int nlines,
 // power-of-two spans sp(g*ns + j1 + q*ms) = sp(g*ns + j1) + sp(q*ms) (adding
 // q*ms never carries across a 32-slot boundary of the padding).
 // ---------------------------------------------------------------------------
-__host__ __device__ constexpr int p2_nst(int P) { return (P + 3) / 4; }
-__host__ __device__ constexpr int p2_e(int P, int s) {
-  return P / p2_nst(P) + (s < P % p2_nst(P) ? 1 : 0);
+// Stage decomposition of a 2^P core, stage s taking e(s) bits of the index.
+// K = 0: ceil(P/4) stages of radix <= 16, larger radices first (the run-time
+// path's order, so LineDev::pos holds).  K = 2: two stages with the larger
+// radix last (512 = 16 . 32): the last DIF stage has span 1, so the radix-32
+// butterflies need no twiddles and carry the band pruning, and a line takes
+// three shared-memory passes (inverse, fused middle, forward) instead of five.
+__host__ __device__ constexpr int p2_nst(int P, int K = 0) { return K ? K : (P + 3) / 4; }
+__host__ __device__ constexpr int p2_e(int P, int s, int K = 0) {
+  return K ? P / K + (s >= K - P % K ? 1 : 0)
+           : P / p2_nst(P) + (s < P % p2_nst(P) ? 1 : 0);
 }
-__host__ __device__ constexpr int p2_ebefore(int P, int s) {
+__host__ __device__ constexpr int p2_ebefore(int P, int s, int K = 0) {
   int t = 0;
-  for (int i = 0; i < s; ++i) t += p2_e(P, i);
+  for (int i = 0; i < s; ++i) t += p2_e(P, i, K);
   return t;
 }
 // slot of frequency k after the forward DIF of length 2^P (digit reversal)
-template <int P>
+template <int P, int K = 0>
 __device__ __forceinline__ int p2_pos(int k) {
   int pos = 0;
 #pragma unroll
-  for (int s = 0; s < p2_nst(P); ++s) {
-    const int e = p2_e(P, s), eb = p2_ebefore(P, s);
+  for (int s = 0; s < p2_nst(P, K); ++s) {
+    const int e = p2_e(P, s, K), eb = p2_ebefore(P, s, K);
     pos |= ((k >> eb) & ((1 << e) - 1)) << (P - eb - e);
   }
   return pos;
@@ -528,10 +578,10 @@ __host__ __device__ constexpr bool p2_pruned_digit(int q) {
   return q >= RAD / 4 && q < 3 * RAD / 4;
 }
 
-template <typename R, int P, int S, bool INV, bool PRUNE = false>
+template <typename R, int P, int S, bool INV, bool PRUNE = false, int K = 0>
 __device__ __forceinline__ void p2_stage(cplx<R>* __restrict__ buf, int ld, int nlines,
                                          const cplx<R>* __restrict__ tw) {
-  constexpr int E = p2_e(P, S), EB = p2_ebefore(P, S);
+  constexpr int E = p2_e(P, S, K), EB = p2_ebefore(P, S, K);
   constexpr int RAD = 1 << E;
   constexpr int LNS = P - EB, LMS = LNS - E, LNBL = P - E;
   constexpr int NS = 1 << LNS, MS = 1 << LMS, NBL = 1 << LNBL;
@@ -578,21 +628,21 @@ __device__ __forceinline__ void p2_stage(cplx<R>* __restrict__ buf, int ld, int 
 
 // PRUNE: the span-1 stage (S = NST-1) skips the digits of N/4 <= k < 3N/4
 // (inverse: zero inputs, forward: unused outputs); see p2_stage.
-template <typename R, int P, bool INV, bool PRUNE = false>
+template <typename R, int P, bool INV, bool PRUNE = false, int K = 0>
 __device__ __forceinline__ void p2_run(cplx<R>* buf, int ld, int nlines, const cplx<R>* tw) {
-  constexpr int NST = p2_nst(P);
+  constexpr int NST = p2_nst(P, K);
   static_assert(NST >= 2 && NST <= 3, "power-of-two cores 2^5 .. 2^12");
   if constexpr (!INV) {
-    p2_stage<R, P, 0, false>(buf, ld, nlines, tw);
+    p2_stage<R, P, 0, false, false, K>(buf, ld, nlines, tw);
     __syncthreads();
-    if constexpr (NST > 2) { p2_stage<R, P, 1, false>(buf, ld, nlines, tw); __syncthreads(); }
-    p2_stage<R, P, NST - 1, false, PRUNE>(buf, ld, nlines, tw);
+    if constexpr (NST > 2) { p2_stage<R, P, 1, false, false, K>(buf, ld, nlines, tw); __syncthreads(); }
+    p2_stage<R, P, NST - 1, false, PRUNE, K>(buf, ld, nlines, tw);
     __syncthreads();
   } else {
-    p2_stage<R, P, NST - 1, true, PRUNE>(buf, ld, nlines, tw);
+    p2_stage<R, P, NST - 1, true, PRUNE, K>(buf, ld, nlines, tw);
     __syncthreads();
-    if constexpr (NST > 2) { p2_stage<R, P, 1, true>(buf, ld, nlines, tw); __syncthreads(); }
-    p2_stage<R, P, 0, true>(buf, ld, nlines, tw);
+    if constexpr (NST > 2) { p2_stage<R, P, 1, true, false, K>(buf, ld, nlines, tw); __syncthreads(); }
+    p2_stage<R, P, 0, true, false, K>(buf, ld, nlines, tw);
     __syncthreads();
   }
 }

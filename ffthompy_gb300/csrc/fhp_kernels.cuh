@@ -1487,14 +1487,14 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_last(cplx<R>* __
 // Pair line p of row rl carries comps 2p, 2p+1, both scaled by a(v); the
 // unused imaginary half of the last line (odd comp count) is zeroed, rows past
 // the grid are zeroed, as in the unfused path.
-template <typename R, int P>
+template <typename R, int P, int K = 0>
 __device__ __forceinline__ void p2_fused_iso_stage0(cplx<R>* __restrict__ buf, int ld, int nlines,
                                                     const cplx<R>* __restrict__ tw, int np,
                                                     FastDiv dnp, const R* acache,
                                                     const R* __restrict__ A, long long row0,
                                                     long long nrows, bool st_coef, R cs,
                                                     bool codd) {
-  constexpr int E = p2_e(P, 0);
+  constexpr int E = p2_e(P, 0, K);
   constexpr int RAD = 1 << E;
   constexpr int LMS = P - E, MS = 1 << LMS, NBL = MS;
   constexpr int N = 1 << P;
@@ -1552,6 +1552,9 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_last_p2(cplx<R>*
                                                    const __grid_constant__ LineDev<R> L, int rows, R coef_scale,
                                                    const int* __restrict__ all_done, int stage) {
   constexpr int N = 1 << P;
+  // FP32 512-point lines run as 16 . 32 (p2_e K = 2); the FP64 instance keeps
+  // 8 . 8 . 8, whose butterflies fit its registers
+  constexpr int K = (P == 9 && sizeof(R) == 4) ? 2 : 0;
   if (all_done && *all_done) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* buf = reinterpret_cast<cplx<R>*>(smem_raw);
@@ -1602,50 +1605,50 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_last_p2(cplx<R>*
         if (cb < C) b = cscale<R>(sb[aq], w);
         if (aq == 0 || 2 * aq == n2_solve) { a.y = R(0); b.y = R(0); }
       }
-      lp[sp(p2_pos<P>(aq))] = mkc<R>(a.x - b.y, a.y + b.x);
-      if (aq > 0) lp[sp(p2_pos<P>(N - aq))] = mkc<R>(a.x + b.y, b.x - a.y);  // X_{-k} = conj(X_k)
+      lp[sp(p2_pos<P, K>(aq))] = mkc<R>(a.x - b.y, a.y + b.x);
+      if (aq > 0) lp[sp(p2_pos<P, K>(N - aq))] = mkc<R>(a.x + b.y, b.x - a.y);  // X_{-k} = conj(X_k)
     }
     // zeros outside the band.  With the band within N/4 the first inverse
     // stage reads the frequencies N/4 <= k < 3N/4 as zeros (pruned top
     // digits), so only [n2h, N/4) and [3N/4, N - n2h] are written.
     if (!band4) {
       for (int k = n2h_band + lane; k <= N - n2h_band; k += 32)
-        lp[sp(p2_pos<P>(k))] = mkc<R>(R(0), R(0));
+        lp[sp(p2_pos<P, K>(k))] = mkc<R>(R(0), R(0));
     } else {
       for (int k = n2h_band + lane; k < N / 4; k += 32)
-        lp[sp(p2_pos<P>(k))] = mkc<R>(R(0), R(0));
+        lp[sp(p2_pos<P, K>(k))] = mkc<R>(R(0), R(0));
       for (int k = 3 * (N / 4) + lane; k <= N - n2h_band; k += 32)
-        lp[sp(p2_pos<P>(k))] = mkc<R>(R(0), R(0));
+        lp[sp(p2_pos<P, K>(k))] = mkc<R>(R(0), R(0));
     }
   }
   __syncthreads();
-  constexpr int NST = p2_nst(P);
+  constexpr int NST = p2_nst(P, K);
   if constexpr (COEF == COEF_ISO) {
     // inverse stages NST-1 .. 1, fused stage 0 with the coefficient, forward
     // stages 1 .. NST-1; the span-1 stages pruned to the band when it fits N/4
     const bool codd = (C & 1) != 0;
-    if (band4) p2_stage<R, P, NST - 1, true, true>(buf, ld, nlines, L.tw);
-    else p2_stage<R, P, NST - 1, true, false>(buf, ld, nlines, L.tw);
+    if (band4) p2_stage<R, P, NST - 1, true, true, K>(buf, ld, nlines, L.tw);
+    else p2_stage<R, P, NST - 1, true, false, K>(buf, ld, nlines, L.tw);
     __syncthreads();
-    if constexpr (NST > 2) { p2_stage<R, P, 1, true>(buf, ld, nlines, L.tw); __syncthreads(); }
+    if constexpr (NST > 2) { p2_stage<R, P, 1, true, false, K>(buf, ld, nlines, L.tw); __syncthreads(); }
     cp_async_wait<0>();
     __syncthreads();
-    p2_fused_iso_stage0<R, P>(buf, ld, nlines, L.tw, np, g.dnp, acache, A, row0, nrows, st_coef,
+    p2_fused_iso_stage0<R, P, K>(buf, ld, nlines, L.tw, np, g.dnp, acache, A, row0, nrows, st_coef,
                               coef_scale, codd);
     __syncthreads();
-    if constexpr (NST > 2) { p2_stage<R, P, 1, false>(buf, ld, nlines, L.tw); __syncthreads(); }
-    if (band4) p2_stage<R, P, NST - 1, false, true>(buf, ld, nlines, L.tw);
-    else p2_stage<R, P, NST - 1, false, false>(buf, ld, nlines, L.tw);
+    if constexpr (NST > 2) { p2_stage<R, P, 1, false, false, K>(buf, ld, nlines, L.tw); __syncthreads(); }
+    if (band4) p2_stage<R, P, NST - 1, false, true, K>(buf, ld, nlines, L.tw);
+    else p2_stage<R, P, NST - 1, false, false, K>(buf, ld, nlines, L.tw);
     __syncthreads();
   } else {
     if (band4) {
-      p2_stage<R, P, NST - 1, true, true>(buf, ld, nlines, L.tw);
+      p2_stage<R, P, NST - 1, true, true, K>(buf, ld, nlines, L.tw);
       __syncthreads();
-      if constexpr (NST > 2) { p2_stage<R, P, 1, true>(buf, ld, nlines, L.tw); __syncthreads(); }
-      p2_stage<R, P, 0, true>(buf, ld, nlines, L.tw);
+      if constexpr (NST > 2) { p2_stage<R, P, 1, true, false, K>(buf, ld, nlines, L.tw); __syncthreads(); }
+      p2_stage<R, P, 0, true, false, K>(buf, ld, nlines, L.tw);
       __syncthreads();
     } else {
-      line_core_p2<R, P>(buf, ld, nlines, L, true);
+      p2_run<R, P, true, false, K>(buf, ld, nlines, L.tw);
     }
     // 2) coefficient per voxel (all loads), in place
     cp_async_wait<0>();
@@ -1687,13 +1690,13 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_last_p2(cplx<R>*
     }
     __syncthreads();
     if (band4) {
-      p2_stage<R, P, 0, false>(buf, ld, nlines, L.tw);
+      p2_stage<R, P, 0, false, false, K>(buf, ld, nlines, L.tw);
       __syncthreads();
-      if constexpr (NST > 2) { p2_stage<R, P, 1, false>(buf, ld, nlines, L.tw); __syncthreads(); }
-      p2_stage<R, P, NST - 1, false, true>(buf, ld, nlines, L.tw);
+      if constexpr (NST > 2) { p2_stage<R, P, 1, false, false, K>(buf, ld, nlines, L.tw); __syncthreads(); }
+      p2_stage<R, P, NST - 1, false, true, K>(buf, ld, nlines, L.tw);
       __syncthreads();
     } else {
-      line_core_p2<R, P>(buf, ld, nlines, L, false);
+      p2_run<R, P, false, false, K>(buf, ld, nlines, L.tw);
     }
   }
   // 3) split and keep the band
@@ -1706,8 +1709,8 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_last_p2(cplx<R>*
     cplx<R>* da = S + ((long long)ca * nrows + row) * n2h_band;
     cplx<R>* db = S + ((long long)cb * nrows + row) * n2h_band;
     for (int k = lane; k < n2h_band; k += 32) {
-      const cplx<R> zk = lp[sp(p2_pos<P>(k))];
-      const cplx<R> zm = lp[sp(p2_pos<P>(k == 0 ? 0 : N - k))];
+      const cplx<R> zk = lp[sp(p2_pos<P, K>(k))];
+      const cplx<R> zm = lp[sp(p2_pos<P, K>(k == 0 ? 0 : N - k))];
       cplx<R> xa = mkc<R>(R(0.5) * (zk.x + zm.x), R(0.5) * (zk.y - zm.y));
       cplx<R> xb = mkc<R>(R(0.5) * (zk.y + zm.y), R(0.5) * (zm.x - zk.x));
       if (2 * k == n2_solve) { xa.y = R(0); xb.y = R(0); }  // mean of +-N/2 (real lines)

@@ -384,6 +384,8 @@ def _pow2_at_least(n, lo=32):
     ((5, 20), 'scalar', 'iso'), ((7, 100), 'scalar', 'iso'), ((5, 200), 'scalar', 'iso'),
     ((5, 300), 'scalar', 'iso'), ((5, 7, 9), 'scalar', 'iso'), ((6, 5, 8), 'scalar', 'iso'),
     ((7, 16), 'scalar', 'iso'), ((7, 16), 'scalar', 'full'), ((5, 5, 16), 'scalar', 'iso'),
+    # 512-point lines with the band beyond N/4 (no pruning; FP32 runs them as 16 . 32)
+    ((5, 256), 'scalar', 'iso'), ((6, 256), 'scalar', 'full'),
     # 255-point solve lines (the compile-time 3.5.17 core) on each axis
     ((255, 7), 'scalar', 'iso'), ((9, 255), 'scalar', 'full'), ((255, 5, 9), 'scalar', 'iso'),
     ((5, 255, 7), 'elasticity', 'full')])
