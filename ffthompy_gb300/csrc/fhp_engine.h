@@ -33,8 +33,11 @@ struct LinePlanHost {
   std::vector<std::complex<long double>> chirp;  // n   (Bluestein)
   std::vector<std::complex<long double>> bhat;   // nf  (Bluestein, digit-reversed, / nf)
 };
-bool build_line_plan(int n, LinePlanHost& out);
-bool factor_radices(int n, std::vector<int>& rad);
+// two_stage_len: a power-of-two core of exactly this length is factored into
+// two stages with the larger radix last (512 = 16 * 32) instead of the default
+// ceil(P/4) even stages; 0 = never.
+bool build_line_plan(int n, LinePlanHost& out, int two_stage_len = 0);
+bool factor_radices(int n, std::vector<int>& rad, int two_stage_len = 0);
 
 struct PlanConfig {
   int dim = 3;

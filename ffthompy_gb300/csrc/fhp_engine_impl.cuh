@@ -833,7 +833,10 @@ class Engine final : public EngineBase {
 
   int make_line(int n, DevLine<R>& out) {
     LinePlanHost h;
-    if (!build_line_plan(n, h)) { set_error("cannot plan FFT length " + std::to_string(n)); return ST_BAD_ARG; }
+    if (!build_line_plan(n, h, p2_two_stage_len<R>())) {
+      set_error("cannot plan FFT length " + std::to_string(n));
+      return ST_BAD_ARG;
+    }
     if (h.nst > kMaxStages) { set_error("too many FFT stages"); return ST_BAD_ARG; }
     const size_t ntw = h.tw.size(), nch = h.chirp.size(), nbh = h.bhat.size();
     const size_t bytes = (ntw + nch + nbh) * sizeof(cplx<R>) + h.pos.size() * sizeof(int) + 64;
@@ -861,11 +864,18 @@ class Engine final : public EngineBase {
     {
       int P = 0;
       while ((1 << P) < h.nf) ++P;
-      if ((1 << P) == h.nf && P >= kP2Min && P <= kP2Max && h.nst == p2_nst(P)) {
+      const int K = p2_k_for<R>(P);
+      if ((1 << P) == h.nf && P >= kP2Min && P <= kP2Max && h.nst == p2_nst(P, K)) {
         bool same = true;
-        for (int s = 0; s < h.nst; ++s) same = same && h.rad[s] == (1 << p2_e(P, s));
+        for (int s = 0; s < h.nst; ++s) same = same && h.rad[s] == (1 << p2_e(P, s, K));
         if (same) L.lg2 = P;
       }
+      // radix 32 exists only in the compile-time two-stage core
+      for (int s = 0; s < h.nst; ++s)
+        if (h.rad[s] > 17 && L.lg2 == 0) {
+          set_error("FFT length " + std::to_string(n) + ": radix without a core");
+          return ST_BAD_ARG;
+        }
     }
     // compile-time mixed-radix core (its radix order is factor_radices')
     L.mixed = (!h.blue && h.nf == 255 && h.nst == 3 && h.rad[0] == 3 && h.rad[1] == 5 &&

@@ -529,7 +529,8 @@ __device__ __forceinline__ void stage_dispatch(cplx<R>* buf, int ld, int nlines,
 // ---------------------------------------------------------------------------
 // Power-of-two cores with a compile-time stage sequence.  The radices are
 // those of factor_radices (2^P in ceil(P/4) stages, exponents as even as
-// possible, the larger ones first: 512 = 8.8.8, 1024 = 16.8.8, 256 = 16.16),
+// possible, the larger ones first: 512 = 8.8.8, 1024 = 16.8.8, 256 = 16.16;
+// FP32 512 = 16.32, see p2_k_for),
 // and the slots and twiddles are the run-time path's, so the digit-reversed
 // positions (LineDev::pos) and the arithmetic are unchanged.  What changes is
 // the index work: butterfly coordinates are shifts and masks, and the r slots
@@ -537,6 +538,20 @@ __device__ __forceinline__ void stage_dispatch(cplx<R>* buf, int ld, int nlines,
 // power-of-two spans sp(g*ns + j1 + q*ms) = sp(g*ns + j1) + sp(q*ms) (adding
 // q*ms never carries across a 32-slot boundary of the padding).
 // ---------------------------------------------------------------------------
+// FP32 cores of 2^kP2TwoStageLg points run as two stages (K = 2 below); the
+// host plans them with factor_radices(..., two_stage_len = 1 << kP2TwoStageLg)
+// so LineDev::pos and Bluestein's bhat follow the same digit order.  FP64
+// keeps the default stages, whose butterflies fit its registers.
+constexpr int kP2TwoStageLg = 9;
+template <typename R>
+__host__ __device__ constexpr int p2_k_for(int P) {
+  return (sizeof(R) == 4 && P == kP2TwoStageLg) ? 2 : 0;
+}
+template <typename R>
+constexpr int p2_two_stage_len() {
+  return sizeof(R) == 4 ? (1 << kP2TwoStageLg) : 0;
+}
+
 // Stage decomposition of a 2^P core, stage s taking e(s) bits of the index.
 // K = 0: ceil(P/4) stages of radix <= 16, larger radices first (the run-time
 // path's order, so LineDev::pos holds).  K = 2: two stages with the larger
@@ -652,12 +667,13 @@ __device__ __forceinline__ void p2_run(cplx<R>* buf, int ld, int nlines, const c
 template <typename R, int P>
 __device__ __forceinline__ void line_core_p2(cplx<R>* buf, int ld, int nlines, const LineDev<R>& L,
                                              bool inverse, bool prune = false) {
+  constexpr int K = p2_k_for<R>(P);
   if (prune && !L.blue) {
-    if (inverse) p2_run<R, P, true, true>(buf, ld, nlines, L.tw);
-    else p2_run<R, P, false, true>(buf, ld, nlines, L.tw);
+    if (inverse) p2_run<R, P, true, true, K>(buf, ld, nlines, L.tw);
+    else p2_run<R, P, false, true, K>(buf, ld, nlines, L.tw);
     return;
   }
-  if (L.blue || !inverse) p2_run<R, P, false>(buf, ld, nlines, L.tw);
+  if (L.blue || !inverse) p2_run<R, P, false, false, K>(buf, ld, nlines, L.tw);
   if (L.blue) {
     const int tot = nlines << P;
     for (int e = threadIdx.x; e < tot; e += blockDim.x) {
@@ -667,7 +683,7 @@ __device__ __forceinline__ void line_core_p2(cplx<R>* buf, int ld, int nlines, c
     }
     __syncthreads();
   }
-  if (L.blue || inverse) p2_run<R, P, true>(buf, ld, nlines, L.tw);
+  if (L.blue || inverse) p2_run<R, P, true, false, K>(buf, ld, nlines, L.tw);
 }
 
 // ---------------------------------------------------------------------------

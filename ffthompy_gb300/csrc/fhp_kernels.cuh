@@ -1552,9 +1552,8 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_last_p2(cplx<R>*
                                                    const __grid_constant__ LineDev<R> L, int rows, R coef_scale,
                                                    const int* __restrict__ all_done, int stage) {
   constexpr int N = 1 << P;
-  // FP32 512-point lines run as 16 . 32 (p2_e K = 2); the FP64 instance keeps
-  // 8 . 8 . 8, whose butterflies fit its registers
-  constexpr int K = (P == 9 && sizeof(R) == 4) ? 2 : 0;
+  // FP32 512-point lines run as 16 . 32 (p2_k_for), as the line plans do
+  constexpr int K = p2_k_for<R>(P);
   if (all_done && *all_done) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* buf = reinterpret_cast<cplx<R>*>(smem_raw);

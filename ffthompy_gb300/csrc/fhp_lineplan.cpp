@@ -88,11 +88,18 @@ Profiler::~Profiler() {
   for (cudaEvent_t e : pool) cudaEventDestroy(e);
 }
 
-bool factor_radices(int n, std::vector<int>& rad) {
+bool factor_radices(int n, std::vector<int>& rad, int two_stage_len) {
   rad.clear();
   if (n < 1) return false;
   int m = n, p2 = 0;
   while (m % 2 == 0) { m /= 2; ++p2; }
+  if (n == two_stage_len && m == 1 && p2 >= 2) {
+    // two stages, the larger radix last (512 = 16 * 32): the device's
+    // compile-time core for this length uses the same order
+    rad.push_back(1 << (p2 / 2));
+    rad.push_back(1 << (p2 - p2 / 2));
+    return true;
+  }
   // 2^p2 in the fewest stages of radix <= 16, exponents as even as possible
   // (512 = 8 * 8 * 8 rather than 16 * 16 * 2: no cheap radix-2 stage that costs
   // a full pass over shared memory)
@@ -125,7 +132,7 @@ static int dif_slot(int k, int n, const std::vector<int>& rad) {
   return P;
 }
 
-bool build_line_plan(int n, LinePlanHost& out) {
+bool build_line_plan(int n, LinePlanHost& out, int two_stage_len) {
   out = LinePlanHost();
   out.n = n;
   std::vector<int> rad;
@@ -135,7 +142,7 @@ bool build_line_plan(int n, LinePlanHost& out) {
     out.tw = {1.0L};
     return true;
   }
-  if (factor_radices(n, rad)) {
+  if (factor_radices(n, rad, two_stage_len)) {
     out.nf = n;
     out.blue = 0;
     out.rad = rad;
@@ -149,7 +156,7 @@ bool build_line_plan(int n, LinePlanHost& out) {
   // Bluestein: smallest 2^a 3^b 5^c >= 2n-1
   int m = 2 * n - 1;
   while (!smooth235(m)) ++m;
-  if (!factor_radices(m, rad)) return false;
+  if (!factor_radices(m, rad, two_stage_len)) return false;
   out.nf = m;
   out.blue = 1;
   out.rad = rad;
