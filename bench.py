@@ -325,6 +325,42 @@ def fibres_measure(n=127, tol=1e-6, seed=0):
     return out
 
 
+def inverse_measure(n=253, d=6, reps=5):
+    """The dual-coefficient inverse (fhp_coefficient_inverse) of a Mandel 6x6
+    field on the Ga grid of the fibres problem (2*127-1)^3, CUDA events on the
+    launching stream; algorithmic traffic 2 d^2 8 bytes per voxel, FP64
+    operations 4 d^2 (d-1) per voxel (the elimination's products and
+    differences) plus d^2 + d(d-1)/2 divisions."""
+    import torch
+    from ffthompy_gb300.engine import coefficient_inverse
+    g = torch.Generator(device='cuda').manual_seed(1)
+    R = torch.randn((d, d, n, n, n), dtype=torch.float64, device='cuda', generator=g)
+    A = (R + R.transpose(0, 1)).mul_(0.5)
+    A += d * torch.eye(d, dtype=torch.float64, device='cuda').reshape(d, d, 1, 1, 1)
+    del R
+    out = None
+    for _ in range(2):
+        out = coefficient_inverse(A, shift=True)
+    stream = torch.cuda.current_stream()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ms = []
+    for _ in range(reps):
+        del out
+        torch.cuda.synchronize()
+        ev[0].record(stream)
+        out = coefficient_inverse(A, shift=True)
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+        ms.append(ev[0].elapsed_time(ev[1]))
+    t = float(np.median(ms)) * 1e-3
+    vox = n ** 3
+    return {'grid': [n] * 3, 'd': d, 'ms': t * 1e3,
+            'GBps': 2 * d * d * 8 * vox / t / 1e9,
+            'fp64_gflops': 4 * d * d * (d - 1) * vox / t / 1e9,
+            'note': 'inputs (%.1f GB) larger than L2; median of %d launches'
+                    % (d * d * 8 * vox / 1e9, reps)}
+
+
 def potential_measure(vals, w, tol, steps=2):
     """Time to A_H of the potential formulation (fhp_potential_*) for the
     GaNi discretisation on the image grid, 3 loads batched, FP32 with FP64
@@ -514,6 +550,7 @@ def run_gpu(args):
         extras['potential'] = potential_measure(vals, w, tol)
     if not args.no_fibres:
         extras['fibres127'] = fibres_measure()
+        extras['coefficient_inverse'] = inverse_measure()
     if not args.no_ensemble:
         extras['ensemble_grf2d'] = ensemble_measure()
         extras['ensemble_grf2d_mixed'] = ensemble_measure(precision='mixed')
