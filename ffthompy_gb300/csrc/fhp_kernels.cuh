@@ -1190,9 +1190,12 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_axis(const cplx<
   // N-grid coefficient at k is the B-grid one for 2|k| < N and the mean of the
   // B-grid coefficients at +-N/2 for the Nyquist index.
   if constexpr (MODE == BAND_UP_PROJ) {
-    // G over the dv comps of each N frequency, then the padded B line
-    for (int e = threadIdx.x; e < T * ax.n_in; e += blockDim.x) {
-      const int t = e & (T - 1), k = e >> lgT;
+    // G over the dv comps of each N frequency, then the padded B line.  Lanes
+    // take consecutive frequencies of one column: the digit-reversed slots of
+    // consecutive k fall in distinct banks, those of one k in the T lines of a
+    // column tile do not.
+    for (int t = 0; t < T; ++t)
+    for (int k = threadIdx.x; k < ax.n_in; k += blockDim.x) {
       const long long col = t0 + t;
       const int q = signed_freq(k, ax.n_in);
       cplx<R> x[kMaxDv];
@@ -1258,9 +1261,10 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_axis(const cplx<
       dst[(long long)k * ax.inner] = v;
     });
   } else {
-    // G(xi) on the band, then inverse DFT_N along the line
-    for (int e = threadIdx.x; e < T * ax.n_out; e += blockDim.x) {
-      const int t = e & (T - 1), k = e >> lgT;
+    // G(xi) on the band, then inverse DFT_N along the line (lanes over the
+    // frequencies of one column, as in the up projection)
+    for (int t = 0; t < T; ++t)
+    for (int k = threadIdx.x; k < ax.n_out; k += blockDim.x) {
       const long long col = t0 + t;
       const int q = signed_freq(k, ax.n_out);
       cplx<R> x[kMaxDv];
