@@ -52,6 +52,10 @@ SIGNATURES = {
     'fhp_ga_grid_coefficient': (ctypes.c_int, [_vp, _vp, _vp, _c_int_p, _c_double_p, _vp, _vp]),
     'fhp_coefficient_inverse': (ctypes.c_int, [ctypes.c_int, _c_int_p, ctypes.c_int, _vp, _vp,
                                                ctypes.c_int, _vp]),
+    'fhp_ball_characteristic': (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_double,
+                                               _c_double_p, _c_double_p, _vp, _vp]),
+    'fhp_ball_topology': (ctypes.c_int, [ctypes.c_int, _c_int_p, _c_double_p, _c_double_p,
+                                         _c_double_p, ctypes.c_double, _vp, _vp]),
     'fhp_profile_enable': (ctypes.c_int, [_vp, ctypes.c_int]),
     'fhp_profile_read': (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_char_p, _c_ll_p,
                                         _c_double_p, _c_double_p, _c_int_p]),

@@ -486,6 +486,48 @@ int fhp_ga_grid_coefficient(fhp_plan plan_img, fhp_plan plan_out, const void* im
   return st;
 }
 
+int fhp_ball_characteristic(fhp_plan plan, double r, double volume, const double* sq,
+                            const double* phase, void* out, void* stream) {
+  if (!plan || !sq || !phase || !out) return bad("plan, tables and out are required");
+  if (!(r >= 0) || !(volume > 0)) return bad("r must be >= 0 and volume > 0");
+  const fhp::PlanConfig& c = plan->eng->config();
+  if (plan->eng->precision() != FHP_F64 || plan->eng->dv() * plan->eng->loads() != 1)
+    return bad("the plan must be an FP64 FFT plan of one component");
+  int g[3] = {1, 1, 1}, tot = 0;
+  for (int i = 0; i < c.dim; ++i) {
+    if (c.N[i] % 2 == 0) return bad("the grid must be odd on every axis");
+    g[3 - c.dim + i] = c.N[i];
+    tot += c.N[i];
+  }
+  // tables in the padded 3-axis order (a one-point axis 0 for 2D)
+  std::vector<double> hs, hp;
+  if (c.dim == 2) { hs.push_back(0.); hp.push_back(1.); hp.push_back(0.); }
+  hs.insert(hs.end(), sq, sq + tot);
+  hp.insert(hp.end(), phase, phase + 2 * tot);
+  cudaStream_t s = as_stream(stream);
+  void *dsq = nullptr, *dph = nullptr, *spec = nullptr;
+  int st = cuda_status(cudaMallocAsync(&dsq, hs.size() * sizeof(double), s), "alloc");
+  if (st == FHP_OK) st = cuda_status(cudaMallocAsync(&dph, hp.size() * sizeof(double), s), "alloc");
+  if (st == FHP_OK)
+    st = cuda_status(cudaMallocAsync(&spec, plan->eng->spectrum_elems() * 2 * sizeof(double), s),
+                     "alloc");
+  if (st == FHP_OK)
+    st = cuda_status(cudaMemcpyAsync(dsq, hs.data(), hs.size() * sizeof(double),
+                                     cudaMemcpyHostToDevice, s), "copy");
+  if (st == FHP_OK)
+    st = cuda_status(cudaMemcpyAsync(dph, hp.data(), hp.size() * sizeof(double),
+                                     cudaMemcpyHostToDevice, s), "copy");
+  if (st == FHP_OK)
+    st = fhp::ball_spectrum(static_cast<const double*>(dsq), static_cast<const double*>(dph),
+                            g[0], g[1], g[2], r, 1.0 / volume, spec, s);
+  if (st == FHP_OK) st = plan->eng->inverse_spectrum(spec, out, 1.0, s);
+  // the host tables are copied by the time the stream reaches this point
+  if (st == FHP_OK) st = cuda_status(cudaStreamSynchronize(s), "sync");
+  for (void* p : {dsq, dph, spec})
+    if (p) cudaFreeAsync(p, s);
+  return st;
+}
+
 int fhp_profile_enable(fhp_plan plan, int enable) {
   if (!plan) return bad("plan is NULL");
   for (fhp::EngineBase* e : {plan->eng.get(), plan->lo.get()}) {

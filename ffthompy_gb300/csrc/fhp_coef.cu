@@ -99,6 +99,84 @@ __global__ void __launch_bounds__(kInvThreads)
   }
 }
 
+// Nodal indicator of a ball summed over its 3^d periodic images (GaNi
+// topology): node x counts the images im in {-1,0,1}^d with
+// sqrt(sum_a ((x_a - x0_a) - Y_a im_a)^2) < radius, each difference, square
+// and sum rounded on its own as NumPy evaluates the reference's expression.
+__global__ void __launch_bounds__(kInvThreads)
+    k_ball_topology(const double* __restrict__ ax0, const double* __restrict__ ax1,
+                    const double* __restrict__ ax2, int dim, int n0, int n1, int n2, double x00,
+                    double x01, double x02, double Y0, double Y1, double Y2, double radius,
+                    double* __restrict__ out) {
+  const int i0 = blockIdx.z, i1 = blockIdx.y;
+  const long long row = ((long long)i0 * n1 + i1) * n2;
+  const double u0 = dim == 3 ? __dsub_rn(ax0[i0], x00) : 0.;
+  const double u1 = __dsub_rn(ax1[i1], x01);
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n2; j += gridDim.x * blockDim.x) {
+    const double u2 = __dsub_rn(ax2[j], x02);
+    double cnt = 0.;
+    for (int m0 = (dim == 3 ? -1 : 0); m0 <= (dim == 3 ? 1 : 0); ++m0)
+      for (int m1 = -1; m1 <= 1; ++m1)
+        for (int m2 = -1; m2 <= 1; ++m2) {
+          double r2 = 0.;
+          if (dim == 3) {
+            const double a = __dsub_rn(u0, Y0 * m0);
+            r2 = __dmul_rn(a, a);
+          }
+          const double b = __dsub_rn(u1, Y1 * m1);
+          r2 = __dadd_rn(r2, __dmul_rn(b, b));
+          const double c = __dsub_rn(u2, Y2 * m2);
+          r2 = __dadd_rn(r2, __dmul_rn(c, c));
+          if (__dsqrt_rn(r2) < radius) cnt += 1.;
+        }
+    out[row + j] = cnt;
+  }
+}
+
+// Half spectrum (FFT order, [n0][n1][n2/2+1]) of the Hermitian part of
+// X = W(|xi|) prod_a ph_a, the exact-integration spectrum of a ball
+// inclusion: W = r^2 J1(2 pi r rho) / (r rho) / |Y| with rho^2 = sum_a sq_a
+// (pi r^2 / |Y| at xi = 0), ph_a the per-axis phases.  Tables are indexed by
+// the centred position i_a = (k_a + n_a/2) mod n_a of frequency k_a; -k_a sits
+// at (n_a/2 - k_a) mod n_a with the same sq.  The real part of the full
+// inverse transform of X is the c2r transform of (X(k) + conj X(-k)) / 2.
+__global__ void __launch_bounds__(kInvThreads)
+    k_ball_spectrum(const double* __restrict__ sq, const double2* __restrict__ ph, int n0,
+                    int n1, int n2, double r, double inv_vol, double2* __restrict__ S) {
+  const int n2h = n2 / 2 + 1;
+  const int k0 = blockIdx.z, k1 = blockIdx.y;
+  const int c0 = n0 / 2, c1 = n1 / 2, c2 = n2 / 2;
+  const int i0 = (k0 + c0) % n0, m0 = (n0 - k0 + c0) % n0;
+  const int i1 = (k1 + c1) % n1, m1 = (n1 - k1 + c1) % n1;
+  const double* sq0 = sq;
+  const double* sq1 = sq + n0;
+  const double* sq2 = sq + n0 + n1;
+  const double2* ph0 = ph;
+  const double2* ph1 = ph + n0;
+  const double2* ph2 = ph + n0 + n1;
+  const double2 pa = ph0[i0], pb = ph0[m0];
+  const double2 qa = ph1[i1], qb = ph1[m1];
+  // ((1 ph0) ph1): the outer product in axis order
+  const double2 ea = make_double2(pa.x * qa.x - pa.y * qa.y, pa.x * qa.y + pa.y * qa.x);
+  const double2 eb = make_double2(pb.x * qb.x - pb.y * qb.y, pb.x * qb.y + pb.y * qb.x);
+  const double s01 = __dadd_rn(sq0[i0], sq1[i1]);
+  const long long row = ((long long)k0 * n1 + k1) * n2h;
+  for (int k2 = blockIdx.x * blockDim.x + threadIdx.x; k2 < n2h; k2 += gridDim.x * blockDim.x) {
+    const int i2 = (k2 + c2) % n2, m2 = (n2 - k2 + c2) % n2;
+    double w;
+    if (i0 == c0 && i1 == c1 && i2 == c2) {
+      w = M_PI * r * r * inv_vol;
+    } else {
+      const double rho = sqrt(__dadd_rn(s01, sq2[i2]));
+      w = (r * r * j1(2. * M_PI * rho * r)) / (rho * r) * inv_vol;
+    }
+    const double2 fa = ph2[i2], fb = ph2[m2];
+    const double2 xa = make_double2(ea.x * fa.x - ea.y * fa.y, ea.x * fa.y + ea.y * fa.x);
+    const double2 xb = make_double2(eb.x * fb.x - eb.y * fb.y, eb.x * fb.y + eb.y * fb.x);
+    S[row + k2] = make_double2(0.5 * w * (xa.x + xb.x), 0.5 * w * (xa.y - xb.y));
+  }
+}
+
 int fail(int status, const std::string& msg) {
   fhp::set_error(msg);
   return status;
@@ -139,5 +217,60 @@ extern "C" int fhp_coefficient_inverse(int dim, const int* n, int d, const doubl
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess)
     return fail(FHP_CUDA, std::string("k_coef_inverse launch: ") + cudaGetErrorString(e));
+  return FHP_OK;
+}
+
+namespace fhp {
+
+int ball_spectrum(const double* sq, const double* phase, int n0, int n1, int n2, double r,
+                  double inv_vol, void* spec, void* stream) {
+  const int n2h = n2 / 2 + 1;
+  const int gx = (n2h + kInvThreads - 1) / kInvThreads;
+  k_ball_spectrum<<<dim3(gx, n1, n0), kInvThreads, 0, static_cast<cudaStream_t>(stream)>>>(
+      sq, reinterpret_cast<const double2*>(phase), n0, n1, n2, r, inv_vol,
+      static_cast<double2*>(spec));
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess)
+    return fail(FHP_CUDA, std::string("k_ball_spectrum launch: ") + cudaGetErrorString(e));
+  return FHP_OK;
+}
+
+}  // namespace fhp
+
+extern "C" int fhp_ball_topology(int dim, const int* n, const double* axes, const double* x0,
+                                 const double* Y, double radius, double* out, void* stream) {
+  if (dim != 2 && dim != 3) return fail(FHP_BAD_ARG, "dim must be 2 or 3");
+  if (!n || !axes || !x0 || !Y || !out) return fail(FHP_BAD_ARG, "n, axes, x0, Y and out are required");
+  int g[3] = {1, 1, 1};
+  int tot = 0;
+  for (int i = 0; i < dim; ++i) {
+    if (n[i] < 1 || n[i] > kInvMaxAxis)
+      return fail(FHP_BAD_ARG, "grid size per axis must be between 1 and 65535");
+    g[3 - dim + i] = n[i];
+    tot += n[i];
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  double* dax = nullptr;
+  cudaError_t e = cudaMallocAsync(&dax, tot * sizeof(double), s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(dax, axes, tot * sizeof(double), cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) {
+    if (dax) cudaFreeAsync(dax, s);
+    return fail(e == cudaErrorMemoryAllocation ? FHP_OOM : FHP_CUDA,
+                std::string("ball topology set-up: ") + cudaGetErrorString(e));
+  }
+  // per-axis coordinate tables in the padded 3-axis order (axis 0 unused in 2D)
+  const double* a0 = dax;
+  const double* a1 = dim == 3 ? dax + n[0] : dax;
+  const double* a2 = dim == 3 ? dax + n[0] + n[1] : dax + n[0];
+  const double x00 = dim == 3 ? x0[0] : 0., Y0 = dim == 3 ? Y[0] : 0.;
+  const int gx = (g[2] + kInvThreads - 1) / kInvThreads;
+  k_ball_topology<<<dim3(gx, g[1], g[0]), kInvThreads, 0, s>>>(
+      a0, a1, a2, dim, g[0], g[1], g[2], x00, x0[dim - 2], x0[dim - 1], Y0, Y[dim - 2],
+      Y[dim - 1], radius, out);
+  e = cudaGetLastError();
+  cudaFreeAsync(dax, s);
+  if (e != cudaSuccess)
+    return fail(FHP_CUDA, std::string("k_ball_topology launch: ") + cudaGetErrorString(e));
   return FHP_OK;
 }

@@ -39,6 +39,12 @@ struct LinePlanHost {
 bool build_line_plan(int n, LinePlanHost& out, int two_stage_len = 0);
 bool factor_radices(int n, std::vector<int>& rad, int two_stage_len = 0);
 
+// Half spectrum [n0][n1][n2/2+1] (FFT order, FP64) of a ball inclusion's
+// exact-integration spectrum from device per-axis tables (fhp_coef.cu); the
+// caller transforms it with the plan's inverse_spectrum.
+int ball_spectrum(const double* sq, const double* phase, int n0, int n1, int n2, double r,
+                  double inv_vol, void* spec, void* stream);
+
 struct PlanConfig {
   int dim = 3;
   int N[3] = {1, 1, 1};      // solve grid (real axes)

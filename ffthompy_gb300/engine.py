@@ -467,3 +467,52 @@ def coefficient_inverse(A, shift=False):
                                            ctypes.c_void_p(out.data_ptr()), int(bool(shift)),
                                            stream), 'fhp_coefficient_inverse')
     return out
+
+
+def ball_characteristic(N, r, volume, sq, phase):
+    """Ga characteristic function of a ball on the odd grid N, origin 0, on
+    the GPU (fhp_ball_characteristic): the inverse transform of
+    W(|xi|) prod_a phase_a.  sq, phase: per-axis host tables in centred
+    position order (xi_a^2 and the complex phases), as the reference pairs
+    them in Material.get_shape_functions (materials.py:125-169, 317-330,
+    392-425).  Returns a float64 CUDA tensor of shape N."""
+    require_cuda()
+    lib = _lib.load()
+    N = tuple(int(n) for n in N)
+    h = _fft_plan(N, 1, torch.float64)
+    out = torch.empty(N, dtype=torch.float64, device='cuda')
+    sq = np.ascontiguousarray(np.concatenate([np.asarray(s, dtype=np.float64) for s in sq]))
+    ph = np.concatenate([np.asarray(p, dtype=np.complex128) for p in phase])
+    ph = np.ascontiguousarray(ph.view(np.float64))
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    try:
+        _lib.check(lib.fhp_ball_characteristic(
+            h, float(r), float(volume), sq.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+            ph.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.c_void_p(out.data_ptr()),
+            stream), 'fhp_ball_characteristic')
+    finally:
+        lib.fhp_plan_destroy(h)
+    return out
+
+
+def ball_topology(axes, x0, Y, radius):
+    """GaNi topology of a ball (fhp_ball_topology): at every node of the
+    tensor grid with per-axis coordinates axes, the number of the 3^d periodic
+    images within radius (materials.py:212-301), bit-identical to the NumPy
+    evaluation.  Returns a float64 CUDA tensor."""
+    require_cuda()
+    lib = _lib.load()
+    d = len(axes)
+    N = tuple(int(len(a)) for a in axes)
+    out = torch.empty(N, dtype=torch.float64, device='cuda')
+    ax = np.ascontiguousarray(np.concatenate([np.asarray(a, dtype=np.float64) for a in axes]))
+    x0 = np.ascontiguousarray(np.asarray(x0, dtype=np.float64))
+    Y = np.ascontiguousarray(np.asarray(Y, dtype=np.float64))
+    n = (ctypes.c_int * d)(*N)
+    dp = ctypes.POINTER(ctypes.c_double)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _lib.check(lib.fhp_ball_topology(d, n, ax.ctypes.data_as(dp), x0.ctypes.data_as(dp),
+                                     Y.ctypes.data_as(dp), float(radius),
+                                     ctypes.c_void_p(out.data_ptr()), stream),
+               'fhp_ball_topology')
+    return out

@@ -11,8 +11,13 @@ inclusions {'inclusions', 'positions', 'params', 'vals', 'Y', 'order', 'P'}.
   1: Fourier coefficients of a P-voxel image weighted by the cell shape
   function, materials.py:77-110).
 
-Coefficient assembly runs once per problem on the host (NumPy); the result is
-returned as a Tensor with origin 0 and uploaded to the GPU for the solve.
+Coefficient assembly runs once per problem. On a GPU the grid-based Ga
+coefficient (fhp_ga_grid_coefficient), the dual inverse
+(fhp_coefficient_inverse), the Ga characteristic function of balls
+(fhp_ball_characteristic) and their GaNi topologies (fhp_ball_topology) run
+in the CUDA library. Boxes and pyramids use separable host transforms; the
+rest runs on the host (NumPy). The result is a Tensor with origin 0 on the
+GPU.
 """
 import itertools
 
@@ -215,6 +220,25 @@ def ga_axis_tables(P, Nbar, h, Y, order, target=None):
     return np.concatenate(srcs).astype(np.int32), np.concatenate(ws)
 
 
+def _ball_char_gpu(r, pos, N, Y):
+    """get_shape_functions' ball characteristic function on the GPU
+    (fhp_ball_characteristic), centred like _centered_ifft_real(SS * W, N).
+    The tables pair what the reference pairs position by position: the
+    weight of centred frequency i - N/2 (get_weights_circ, materials.py:
+    392-425) with the phase of get_shift_inclusion at the same array position,
+    whose frequencies are in FFT order (materials.py:317-330)."""
+    from .engine import ball_characteristic
+    N = np.asarray(N, dtype=np.int64)
+    Y = np.asarray(Y, dtype=np.float64)
+    h = np.asarray(pos, dtype=np.float64)
+    Zc = Grid.get_ZNl(N, fft_form='c')
+    Zf = Grid.get_ZNl(N)
+    sq = [(Zc[i] / Y[i]) ** 2 for i in range(N.size)]
+    ph = [np.exp(-2j * np.pi * h[i] * Zf[i] / Y[i]) for i in range(N.size)]
+    out = ball_characteristic(N, r, float(np.prod(Y)), sq, ph)
+    return np.fft.fftshift(out.cpu().numpy())
+
+
 def _gpu_available():
     try:
         import torch
@@ -347,6 +371,10 @@ class Material:
                         va += (u > -p[a] / 2) & (u <= p[a] / 2)
                     vs.append(va)
                 t = outer(vs)
+            elif kind in inclusion_keys['ball'] and _gpu_available() and d in (2, 3):
+                from .engine import ball_topology
+                t = ball_topology(axes, np.asarray(poss[ii], dtype=np.float64), self.Y,
+                                  params[ii] / 2).cpu().numpy()
             elif kind in inclusion_keys['ball']:
                 x0 = np.asarray(poss[ii], dtype=np.float64)
                 t = np.zeros(grid)
@@ -424,9 +452,12 @@ class Material:
                 chars.append(_separable_char('cube', np.asarray(params[ii], dtype=np.float64),
                                              shift_pos, N2, self.Y))
             elif incl in inclusion_keys['ball']:
+                r = params[ii] / 2
+                if r != 0 and _gpu_available() and np.all(N2 % 2 == 1) and N2.size in (2, 3):
+                    chars.append(_ball_char_gpu(r, shift_pos, N2, self.Y))
+                    continue
                 if SS is None:
                     SS = get_shift_inclusion(N2, shift_pos, self.Y)
-                r = params[ii] / 2
                 W = np.zeros(tuple(N2)) if r == 0 else get_weights_circ(r, N2, self.Y)
                 chars.append(_centered_ifft_real(SS * W, N2))
             elif incl in inclusion_keys['pyramid']:

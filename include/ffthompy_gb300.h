@@ -217,6 +217,39 @@ int fhp_ga_grid_coefficient(fhp_plan plan_img, fhp_plan plan_out, const void* im
                             void* stream);
 
 /*
+ * Characteristic function of a ball inclusion for the exact-integration (Ga)
+ * coefficient: out = real(iDFT(X)) * prod(n), origin 0, with
+ * X = W(|xi|) prod_a phase_a, W = r^2 J1(2 pi r |xi|) / (r |xi|) / volume
+ * (pi r^2 / volume at xi = 0; J1 is CUDA's j1).  plan: an FP64
+ * fhp_fft_plan_create plan of one component on a grid odd on every axis.
+ * Host tables per axis, concatenated, indexed by the centred position i of
+ * the axis (i - n_a/2 the frequency): sq (sum n doubles) = xi_a^2 and phase
+ * (2 sum n doubles, interleaved re/im) = the phase the caller pairs with that
+ * position.  The real part is formed as the inverse c2r transform of the
+ * Hermitian part (X(k) + conj X(-k)) / 2, so a phase table that is not
+ * conjugate-symmetric is handled as the reference's .real handles it.
+ * out: float64 device array on the plan's grid.  Synchronises `stream`.
+ * Replaces, for balls: get_weights_circ (ffthompy/materials.py:392-425), the
+ * phase of get_shift_inclusion (materials.py:317-330) and the centred inverse
+ * DFT of Material.get_shape_functions (materials.py:125-169).
+ */
+int fhp_ball_characteristic(fhp_plan plan, double r, double volume, const double* sq,
+                            const double* phase, void* out, void* stream);
+
+/*
+ * Nodal indicator of a ball summed over its 3^dim periodic images (the
+ * topology of Material.get_A_GaNi): out[x] = number of images im in
+ * {-1,0,1}^dim with sqrt(sum_a ((x_a - x0_a) - Y_a im_a)^2) < radius, each
+ * difference, square and sum rounded as NumPy evaluates them (bit-identical).
+ * axes: host, concatenated per-axis node coordinates (sum n doubles); x0, Y:
+ * host, dim doubles; out: float64 device array [n0]..[n_{dim-1}].  dim 2 or 3.
+ * Replaces: the ball branch of Material.get_topologies
+ * (ffthompy/materials.py:212-301).
+ */
+int fhp_ball_topology(int dim, const int* n, const double* axes, const double* x0,
+                      const double* Y, double radius, double* out, void* stream);
+
+/*
  * Per-voxel inverse of a field of d x d matrices (the dual coefficient):
  * Ainv(x) = A(x)^-1 by Gauss-Jordan elimination without pivoting, in the
  * reference's order, each product and difference rounded separately as NumPy

@@ -113,3 +113,21 @@ def test_line_plans_factor_configured_sizes():
             while not factor(m) or any(m % p == 0 for p in (7, 11, 13, 17, 19, 23, 29, 31)):
                 m += 1
             assert m <= 4096
+
+
+def test_ball_entry_points_reject_bad_arguments(lib):
+    """fhp_ball_topology / fhp_ball_characteristic check their arguments
+    before any CUDA call."""
+    from ffthompy_gb300 import _lib
+    n = (ctypes.c_int * 3)(5, 5, 5)
+    t = (ctypes.c_double * 15)(*range(15))
+    x0 = (ctypes.c_double * 3)(0., 0., 0.)
+    Y = (ctypes.c_double * 3)(1., 1., 1.)
+    out = ctypes.c_void_p(1 << 20)
+    bad = _lib.FHP_BAD_ARG
+    assert lib.fhp_ball_topology(4, n, t, x0, Y, 0.2, out, None) == bad
+    assert lib.fhp_ball_topology(1, n, t, x0, Y, 0.2, out, None) == bad
+    assert lib.fhp_ball_topology(3, n, None, x0, Y, 0.2, out, None) == bad
+    z = (ctypes.c_int * 3)(5, 0, 5)
+    assert lib.fhp_ball_topology(3, z, t, x0, Y, 0.2, out, None) == bad
+    assert lib.fhp_ball_characteristic(None, 0.2, 1.0, t, t, out, None) == bad
