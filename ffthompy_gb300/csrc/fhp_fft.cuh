@@ -223,7 +223,9 @@ __device__ __forceinline__ void dft8(cplx<R>* v) {
   }
 }
 
-template <typename R>
+// ENDS: only x[0..3] and x[12..15] are nonzero (the band of a pruned
+// 32-point line), so the first DFT4 of each b sees (x_b, 0, 0, x_{b+12}).
+template <typename R, bool ENDS = false>
 __device__ __forceinline__ void dft16(cplx<R>* v) {
   // x[b + 4a]: u_b = DFT4_a, twiddle W16^(b k1), then DFT4 over b.
   const R c1 = R(0.92387953251128675612818318939679);  // cos(pi/8)
@@ -232,10 +234,18 @@ __device__ __forceinline__ void dft16(cplx<R>* v) {
   cplx<R> u[4][4];
 #pragma unroll
   for (int b = 0; b < 4; ++b) {
-    cplx<R> t[4] = {v[b], v[b + 4], v[b + 8], v[b + 12]};
-    dft4<R>(t);
+    if constexpr (ENDS) {
+      const cplx<R> x0 = v[b], x3 = v[b + 12];
+      u[b][0] = cadd<R>(x0, x3);
+      u[b][1] = cadd<R>(x0, cmul_pi<R>(x3));
+      u[b][2] = csub<R>(x0, x3);
+      u[b][3] = csub<R>(x0, cmul_pi<R>(x3));
+    } else {
+      cplx<R> t[4] = {v[b], v[b + 4], v[b + 8], v[b + 12]};
+      dft4<R>(t);
 #pragma unroll
-    for (int k = 0; k < 4; ++k) u[b][k] = t[k];
+      for (int k = 0; k < 4; ++k) u[b][k] = t[k];
+    }
   }
   // W16^1 = (c1,-s1), W16^2 = (r,-r), W16^3 = (s1,-c1), W16^4 = -i,
   // W16^6 = (-r,-r), W16^9 = (-c1,+s1)
@@ -259,7 +269,10 @@ __device__ __forceinline__ void dft16(cplx<R>* v) {
 
 // 32 = 2 x 16: X[k] = E[k] + W32^k O[k], X[k+16] = E[k] - W32^k O[k] with E, O
 // the 16-point DFTs of the even and odd samples (natural order in and out).
-template <typename R>
+// ZIN: inputs 8..23 are zero (inverse span-1 stage of a band-pruned line);
+// HALF: only outputs 0..7 and 24..31 are wanted (forward span-1 stage), the
+// others are left unspecified.
+template <typename R, bool ZIN = false, bool HALF = false>
 __device__ __forceinline__ void dft32(cplx<R>* v) {
   const R c16 = R(0.98078528040323044912618223613424);   // cos(pi/16)
   const R s16 = R(0.19509032201612826784828486847702);   // sin(pi/16)
@@ -274,8 +287,8 @@ __device__ __forceinline__ void dft32(cplx<R>* v) {
     e[k] = v[2 * k];
     o[k] = v[2 * k + 1];
   }
-  dft16<R>(e);
-  dft16<R>(o);
+  dft16<R, ZIN>(e);
+  dft16<R, ZIN>(o);
   // o[k] *= W32^k = (cos(pi k/16), -sin(pi k/16))
   o[1] = cmul<R>(o[1], mkc<R>(c16, -s16));
   o[2] = cmul<R>(o[2], mkc<R>(c8, -s8));
@@ -294,8 +307,8 @@ __device__ __forceinline__ void dft32(cplx<R>* v) {
   o[15] = cmul<R>(o[15], mkc<R>(-c16, -s16));
 #pragma unroll
   for (int k = 0; k < 16; ++k) {
-    v[k] = cadd<R>(e[k], o[k]);
-    v[k + 16] = csub<R>(e[k], o[k]);
+    if (!HALF || k < 8) v[k] = cadd<R>(e[k], o[k]);
+    if (!HALF || k >= 8) v[k + 16] = csub<R>(e[k], o[k]);
   }
 }
 
@@ -620,7 +633,8 @@ __device__ __forceinline__ void p2_stage(cplx<R>* __restrict__ buf, int ld, int 
     if constexpr (!INV) {
 #pragma unroll
       for (int q = 0; q < RAD; ++q) v[q] = lp[sp(q * MS)];
-      dft_fwd<R, RAD>(v, tw, 1 << P);
+      if constexpr (PRUNE && RAD == 32) dft32<R, false, true>(v);
+      else dft_fwd<R, RAD>(v, tw, 1 << P);
       lp[0] = v[0];
 #pragma unroll
       for (int q = 1; q < RAD; ++q) {
@@ -634,7 +648,8 @@ __device__ __forceinline__ void p2_stage(cplx<R>* __restrict__ buf, int ld, int 
         if (PRUNE && p2_pruned_digit<RAD>(q)) v[q] = mkc<R>(R(0), R(0));
         else v[q] = TW ? cconj<R>(cmulc<R>(lp[sp(q * MS)], w[q])) : cconj<R>(lp[sp(q * MS)]);
       }
-      dft_fwd<R, RAD>(v, tw, 1 << P);
+      if constexpr (PRUNE && RAD == 32) dft32<R, true, false>(v);
+      else dft_fwd<R, RAD>(v, tw, 1 << P);
 #pragma unroll
       for (int q = 0; q < RAD; ++q) lp[sp(q * MS)] = cconj<R>(v[q]);
     }
