@@ -49,11 +49,12 @@ int cg_mixed(fhp_plan_s& p, int proj, const void* b, const void* x0, double tol,
   const double M = (double)hi.voxels();
   const size_t n = (size_t)L * hi.dv() * hi.voxels();
   double* x = static_cast<double*>(xv);
-  void *ax = nullptr, *r = nullptr, *r32 = nullptr, *d32 = nullptr;
-  int st = cuda_status(cudaMallocAsync(&ax, n * 8, s), "alloc");
-  if (st == FHP_OK) st = cuda_status(cudaMallocAsync(&r, n * 8, s), "alloc");
-  if (st == FHP_OK) st = cuda_status(cudaMallocAsync(&r32, n * 4, s), "alloc");
-  if (st == FHP_OK) st = cuda_status(cudaMallocAsync(&d32, n * 4, s), "alloc");
+  // the plan's persistent scratch: nothing is allocated per solve
+  void* ax = hi.scratch(fhp::SCR_MIX_AX, n * 8);
+  void* r = hi.scratch(fhp::SCR_MIX_R, n * 8);
+  void* r32 = hi.scratch(fhp::SCR_MIX_R32, n * 4);
+  void* d32 = hi.scratch(fhp::SCR_MIX_D32, n * 4);
+  int st = (ax && r && r32 && d32) ? FHP_OK : FHP_OOM;
   std::vector<double> sumsq(L), norm(L), sc_in(L), sc_out(L);
   std::vector<int> kit(L, 0), status(L, 0), active(L, 1);
   res.res_log.assign((size_t)std::max(1, log_rows) * L, 0.0);
@@ -114,8 +115,6 @@ int cg_mixed(fhp_plan_s& p, int proj, const void* b, const void* x0, double tol,
       }
     }
   }
-  for (void* q : {ax, r, r32, d32})
-    if (q) cudaFreeAsync(q, s);
   if (st == FHP_OK) st = cuda_status(cudaStreamSynchronize(s), "sync");
   res.kit = kit;
   res.norm_res.resize(L);
@@ -382,10 +381,10 @@ int fhp_homogenize_host(fhp_plan plan, int proj, int coef_kind, const double* co
   int st = fhp_set_coefficient(plan, coef_kind, coef_host, 0, stream);
   if (st != FHP_OK) return st;
   const size_t bytes = (size_t)e.loads() * e.dv() * e.voxels() * e.elem_size();
-  void* b = nullptr;
-  void* x = nullptr;
-  st = cuda_status(cudaMallocAsync(&b, bytes, s), "alloc");
-  if (st == FHP_OK) st = cuda_status(cudaMallocAsync(&x, bytes, s), "alloc");
+  // the plan's persistent scratch: repeated calls allocate nothing
+  void* b = e.scratch(fhp::SCR_HOST_B, bytes);
+  void* x = e.scratch(fhp::SCR_HOST_X, bytes);
+  st = (b && x) ? FHP_OK : FHP_OOM;
   if (st == FHP_OK) st = e.rhs_macro(proj, b, s);
   fhp::SolveResult r;
   if (st == FHP_OK)
@@ -400,8 +399,6 @@ int fhp_homogenize_host(fhp_plan plan, int proj, int coef_kind, const double* co
     if (kit_host) kit_host[l] = r.kit[l];
     if (norm_res_host) norm_res_host[l] = r.norm_res[l];
   }
-  if (x) cudaFreeAsync(x, s);
-  if (b) cudaFreeAsync(b, s);
   return st;
 }
 

@@ -33,6 +33,23 @@ struct LinePlanHost {
   std::vector<std::complex<long double>> chirp;  // n   (Bluestein)
   std::vector<std::complex<long double>> bhat;   // nf  (Bluestein, digit-reversed, / nf)
 };
+// Scratch slots of EngineBase::scratch; no two users that can be active at
+// the same time on one plan share a slot.
+enum ScratchSlot {
+  SCR_COEF_STAGE = 0,  // host coefficient values staged for conversion
+  SCR_LOG,             // CG residual log
+  SCR_RHS_TMP,         // macroscopic field of rhs_macro
+  SCR_BAND_U,          // band energy: x + E
+  SCR_BAND_W,          // band energy: band(A (x + E))
+  SCR_HOST_B,          // fhp_homogenize_host: right-hand sides
+  SCR_HOST_X,          // fhp_homogenize_host: solution
+  SCR_MIX_AX,          // mixed refinement: A x (FP64)
+  SCR_MIX_R,           // mixed refinement: residual (FP64)
+  SCR_MIX_R32,         // mixed refinement: scaled residual (FP32)
+  SCR_MIX_D32,         // mixed refinement: correction (FP32)
+  kScratchSlots
+};
+
 // two_stage_len: a power-of-two core of exactly this length is factored into
 // two stages with the larger radix last (512 = 16 * 32) instead of the default
 // ceil(P/4) even stages; 0 = never.
@@ -137,6 +154,11 @@ class EngineBase {
   // spectra: 'r' form half spectra of the band grid N, [load][N0][N1][N2/2+1]
   // complex of this engine's precision.
   virtual long long pot_spectrum_elems() const = 0;
+  // Persistent per-plan device scratch: slot `slot` holds at least `bytes`
+  // (grown with cudaMalloc, never shrunk, freed with the plan), so repeated
+  // calls on a plan allocate nothing and plans on other streams share no
+  // memory.  nullptr if the allocation fails.
+  virtual void* scratch(int slot, size_t bytes) = 0;
   // bh = P B, B_l = div(decrease_N F(A E_l))
   virtual int pot_rhs(void* bh, cudaStream_t s) = 0;
   // yh = P (-div) decrease_N F(A iF(enlarge(grad(P xh))))

@@ -367,8 +367,9 @@ class Engine final : public EngineBase {
     FHP_CHECK(cudaMemcpyAsync(st_, h_st_, g_.L * sizeof(LoadState), cudaMemcpyHostToDevice, s));
     FHP_CHECK(cudaMemsetAsync(all_done_, 0, sizeof(int), s));
     const int log_rows = std::max(1, std::min(log_cap, maxiter + 1));
-    double* dlog = nullptr;
-    FHP_CHECK(cudaMallocAsync(&dlog, (size_t)log_rows * g_.L * sizeof(double), s));
+    double* dlog =
+        static_cast<double*>(scratch(SCR_LOG, (size_t)log_rows * g_.L * sizeof(double)));
+    if (!dlog) return ST_OOM;
     FHP_CHECK(cudaMemsetAsync(dlog, 0, (size_t)log_rows * g_.L * sizeof(double), s));
     k_dot<R><<<red_ctas_, kThreads, 0, s>>>(rr, rr, partials_, gz);
     FHP_LAUNCHED();
@@ -411,13 +412,12 @@ class Engine final : public EngineBase {
       if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); rc = ST_CUDA; }
       ++launches;
     }
-    if (rc != ST_OK) { cudaFreeAsync(dlog, s); return rc; }
+    if (rc != ST_OK) return rc;
     FHP_CHECK(cudaMemcpyAsync(h_st_, st_, g_.L * sizeof(LoadState), cudaMemcpyDeviceToHost, s));
     res.res_log.assign((size_t)log_rows * g_.L, 0.0);
     FHP_CHECK(cudaMemcpyAsync(res.res_log.data(), dlog, (size_t)log_rows * g_.L * sizeof(double),
                               cudaMemcpyDeviceToHost, s));
     FHP_CHECK(cudaStreamSynchronize(s));
-    cudaFreeAsync(dlog, s);
     res.kit.resize(g_.L);
     res.norm_res.resize(g_.L);
     res.status.resize(g_.L);
@@ -446,19 +446,19 @@ class Engine final : public EngineBase {
       FHP_CHECK(cudaMalloc(&A_, n * sizeof(R)));
       A_elems_ = n;
     }
-    // host values go through a stream-ordered staging buffer (cudaFree would
-    // synchronise the device and serialise plans on other streams); the copy
-    // from pageable memory has read the host buffer when the call returns
+    // host values go through the plan's persistent staging buffer (no
+    // allocation per call); the copy from pageable memory has read the host
+    // buffer when the call returns
     double* tmp = nullptr;
     const double* src = values;
     if (!on_device) {
-      FHP_CHECK(cudaMallocAsync(&tmp, n * sizeof(double), s));
+      tmp = static_cast<double*>(scratch(SCR_COEF_STAGE, n * sizeof(double)));
+      if (!tmp) return ST_OOM;
       FHP_CHECK(cudaMemcpyAsync(tmp, values, n * sizeof(double), cudaMemcpyHostToDevice, s));
       src = tmp;
     }
     k_convert<R, double><<<grid_for(n), kThreads, 0, s>>>((long long)n, src, A_);
     FHP_LAUNCHED();
-    if (tmp) FHP_CHECK(cudaFreeAsync(tmp, s));
     coef_kind_ = kind;
     return ST_OK;
   }
@@ -502,14 +502,12 @@ class Engine final : public EngineBase {
   }
 
   int rhs_macro(int proj, void* b, cudaStream_t s) override {
-    R* tmp = nullptr;
     const size_t n = (size_t)g_.L * g_.dv * g_.M;
-    FHP_CHECK(cudaMallocAsync(&tmp, n * sizeof(R), s));
+    R* tmp = static_cast<R*>(scratch(SCR_RHS_TMP, n * sizeof(R)));
+    if (!tmp) return ST_OOM;
     k_fill_macro<R><<<grid_for(n), kThreads, 0, s>>>(tmp, g_, -1.0);
     FHP_LAUNCHED();
-    int st = apply(proj, tmp, b, s);
-    cudaFreeAsync(tmp, s);
-    return st;
+    return apply(proj, tmp, b, s);
   }
 
   int cg_solve(int proj, const void* bv, const void* x0v, double tol, int maxiter, void* xv,
@@ -546,8 +544,9 @@ class Engine final : public EngineBase {
     FHP_CHECK(cudaMemcpyAsync(st_, h_st_, g_.L * sizeof(LoadState), cudaMemcpyHostToDevice, s));
     FHP_CHECK(cudaMemsetAsync(all_done_, 0, sizeof(int), s));
     const int log_rows = std::max(1, std::min(log_cap, maxiter + 1));
-    double* dlog = nullptr;
-    FHP_CHECK(cudaMallocAsync(&dlog, (size_t)log_rows * g_.L * sizeof(double), s));
+    double* dlog =
+        static_cast<double*>(scratch(SCR_LOG, (size_t)log_rows * g_.L * sizeof(double)));
+    if (!dlog) return ST_OOM;
     FHP_CHECK(cudaMemsetAsync(dlog, 0, (size_t)log_rows * g_.L * sizeof(double), s));
     k_dot<R><<<red_ctas_, kThreads, 0, s>>>(r_, r_, partials_, g_);
     FHP_LAUNCHED();
@@ -596,13 +595,11 @@ class Engine final : public EngineBase {
           if (e != cudaSuccess) {
             set_error(std::string("cudaGraphLaunch: ") + cudaGetErrorString(e));
             release_graph();
-            cudaFreeAsync(dlog, s);
             return ST_CUDA;
           }
           launches += per_iter;
         } else if ((st = cg_iteration(dlog, log_rows, s)) != ST_OK) {
           release_graph();
-          cudaFreeAsync(dlog, s);
           return st;
         }
       }
@@ -615,7 +612,6 @@ class Engine final : public EngineBase {
     // order. One projection x <- G x (the identity in exact arithmetic) puts
     // the drift back to a single rounding.
     if (sizeof(R) == 4 && (st = project(proj, x, x, s)) != ST_OK) {
-      cudaFreeAsync(dlog, s);
       return st;
     }
     FHP_CHECK(cudaMemcpyAsync(h_st_, st_, g_.L * sizeof(LoadState), cudaMemcpyDeviceToHost, s));
@@ -623,7 +619,6 @@ class Engine final : public EngineBase {
     FHP_CHECK(cudaMemcpyAsync(res.res_log.data(), dlog, (size_t)log_rows * g_.L * sizeof(double),
                               cudaMemcpyDeviceToHost, s));
     FHP_CHECK(cudaStreamSynchronize(s));
-    cudaFreeAsync(dlog, s);
     res.kit.resize(g_.L);
     res.norm_res.resize(g_.L);
     res.status.resize(g_.L);
@@ -784,6 +779,8 @@ class Engine final : public EngineBase {
   int coef_kind_ = 0;
   R *r_ = nullptr, *p_ = nullptr, *ap_ = nullptr;
   double* partials_ = nullptr;
+  void* scr_[kScratchSlots] = {};
+  size_t scr_bytes_[kScratchSlots] = {};
   double* ad_ = nullptr;
   LoadState* st_ = nullptr;
   LoadState* h_st_ = nullptr;
@@ -852,6 +849,11 @@ class Engine final : public EngineBase {
     int* ip = reinterpret_cast<int*>(c + ntw + nch + nbh);
     std::memcpy(ip, h.pos.data(), h.pos.size() * sizeof(int));
     FHP_CHECK(cudaMemcpy(out.mem, host.data(), bytes, cudaMemcpyHostToDevice));
+    // From pageable memory cudaMemcpy returns once the data is staged, and the
+    // DMA runs on the legacy default stream, which does not order work on
+    // non-blocking streams: a plan created in a worker thread could start its
+    // first solve on such a stream before its tables land.  Wait for it here.
+    FHP_CHECK(cudaStreamSynchronize(cudaStreamLegacy));
     cplx<R>* dc = reinterpret_cast<cplx<R>*>(out.mem);
     LineDev<R>& L = out.dev;
     L.n = h.n;
@@ -942,7 +944,26 @@ class Engine final : public EngineBase {
     return ST_OK;
   }
 
+  void* scratch(int slot, size_t bytes) override {
+    if (slot < 0 || slot >= kScratchSlots) return nullptr;
+    if (scr_bytes_[slot] < bytes) {
+      // growing frees the old buffer: cudaFree waits for work that still uses it
+      if (scr_[slot]) cudaFree(scr_[slot]);
+      scr_[slot] = nullptr;
+      scr_bytes_[slot] = 0;
+      if (cudaMalloc(&scr_[slot], bytes) != cudaSuccess) {
+        scr_[slot] = nullptr;
+        set_error("out of device memory for plan scratch");
+        return nullptr;
+      }
+      scr_bytes_[slot] = bytes;
+    }
+    return scr_[slot];
+  }
+
   void release() {
+    for (int i = 0; i < kScratchSlots; ++i)
+      if (scr_[i]) { cudaFree(scr_[i]); scr_[i] = nullptr; scr_bytes_[i] = 0; }
     for (DevLine<R>* l : {&l0_, &l1_, &l2_, &lb0_, &lb1_, &lb2_})
       if (l->mem) { cudaFree(l->mem); l->mem = nullptr; }
     if (SB_) { cudaFree(SB_); SB_ = nullptr; }
@@ -1238,10 +1259,9 @@ class Engine final : public EngineBase {
   // A_H[i][j] = <W_i, X_j + E_j>  (exact: X + E is band limited)
   int band_energy(const R* X, int add_macro, double* AH, cudaStream_t s) {
     const size_t n = (size_t)g_.L * g_.dv * g_.M;
-    R* U = nullptr;
-    R* W = nullptr;
-    FHP_CHECK(cudaMallocAsync(&U, n * sizeof(R), s));
-    FHP_CHECK(cudaMallocAsync(&W, n * sizeof(R), s));
+    R* U = static_cast<R*>(scratch(SCR_BAND_U, n * sizeof(R)));
+    R* W = static_cast<R*>(scratch(SCR_BAND_W, n * sizeof(R)));
+    if (!U || !W) return ST_OOM;
     if (add_macro) {
       k_add_macro<R><<<grid_for(n), kThreads, 0, s>>>(X, U, g_);
       FHP_LAUNCHED();
@@ -1265,8 +1285,6 @@ class Engine final : public EngineBase {
                                 cudaMemcpyDeviceToHost, s));
       FHP_CHECK(cudaStreamSynchronize(s));
     }
-    cudaFreeAsync(U, s);
-    cudaFreeAsync(W, s);
     return st;
   }
 
