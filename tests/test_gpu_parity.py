@@ -87,6 +87,29 @@ def test_operator_random_sizes(N, kind, physics):
             assert _relmax(y[l], ref) < 1e-12, (proj, l, _relmax(y[l], ref))
 
 
+@pytest.mark.parametrize('N', [(253, 20), (9, 251), (251, 7, 6), (5, 253, 9)])
+@pytest.mark.parametrize('physics', ['scalar', 'elasticity'])
+def test_operator_fp32_bluestein_512(N, physics):
+    """FP32 lines whose Bluestein core is 512 points (251, 253: 2n-1 -> 512)
+    run it as 16 . 32 with the filter spectrum in that digit order: G o A vs
+    the oracle at the FP32 operator tolerance, on every axis position."""
+    rng = np.random.default_rng(sum(N) + 7)
+    d = len(N)
+    dv = d if physics == 'scalar' else d * (d + 1) // 2
+    Y = 0.5 + rng.random(d)
+    B = rng.standard_normal((dv, dv) + tuple(N))
+    A = np.einsum('ik...,jk...->ij...', B, B) + np.einsum('ij,...->ij...', np.eye(dv),
+                                                          np.ones(tuple(N)))
+    x = rng.standard_normal((1, dv) + tuple(N))
+    plan = _plan(N, Y, physics, 'GaNi', nloads=1, precision='f32')
+    plan.set_coefficient(A)
+    for proj in (1, 2):
+        G, _ = oracle.green_operator(physics, np.asarray(N), Y, 'GaNi', proj)
+        y = plan.apply(x, proj=proj).double().cpu().numpy()
+        ref = oracle.apply_GA(G, A, x[0])
+        assert _relmax(y[0], ref) < 2e-5, (proj, _relmax(y[0], ref))
+
+
 @pytest.mark.parametrize('N', [(9, 9), (12, 10), (5, 7, 9), (6, 5, 8)])
 @pytest.mark.parametrize('physics', ['scalar', 'elasticity'])
 def test_projection_idempotent_orthogonal(N, physics):
