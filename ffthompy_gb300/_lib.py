@@ -54,6 +54,8 @@ SIGNATURES = {
                                                ctypes.c_int, _vp]),
     'fhp_ball_characteristic': (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_double,
                                                _c_double_p, _c_double_p, _vp, _vp]),
+    'fhp_outer_accumulate': (ctypes.c_int, [ctypes.c_int, _c_double_p, _vp, _vp,
+                                            ctypes.c_longlong, _vp]),
     'fhp_ball_topology': (ctypes.c_int, [ctypes.c_int, _c_int_p, _c_double_p, _c_double_p,
                                          _c_double_p, ctypes.c_double, _vp, _vp]),
     'fhp_profile_enable': (ctypes.c_int, [_vp, ctypes.c_int]),

@@ -516,3 +516,23 @@ def ball_topology(axes, x0, Y, radius):
                                      ctypes.c_void_p(out.data_ptr()), stream),
                'fhp_ball_topology')
     return out
+
+
+def outer_accumulate(out, v, c):
+    """out[k] += v[k] * c over a (nv,) + grid CUDA float64 field, on the GPU
+    (fhp_outer_accumulate): one inclusion's term of Material.get_A_Ga, order
+    None (materials.py:66-75), bit-identical to val += np.multiply.outer(v, c).
+    v: nv host values; c: CUDA float64 tensor of the grid's shape."""
+    require_cuda()
+    lib = _lib.load()
+    v = np.ascontiguousarray(np.asarray(v, dtype=np.float64).ravel())
+    M = int(c.numel())
+    if out.dtype != torch.float64 or c.dtype != torch.float64 or not out.is_contiguous() \
+            or not c.is_contiguous() or out.numel() != v.size * M:
+        raise ValueError('out must be a contiguous float64 field of len(v) x c.numel() values')
+    stream = ctypes.c_void_p(torch.cuda.current_stream(out.device).cuda_stream)
+    _lib.check(lib.fhp_outer_accumulate(int(v.size),
+                                        v.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                        ctypes.c_void_p(c.data_ptr()),
+                                        ctypes.c_void_p(out.data_ptr()), M, stream),
+               'fhp_outer_accumulate')

@@ -510,6 +510,25 @@ class Material:
         if order in (None, 'exact'):
             chars = self.get_shape_functions(Nbar)
             vals = self.conf['vals']
+            if _gpu_available():
+                # each characteristic function moved to origin 0 and uploaded
+                # once; the sum over inclusions runs on the GPU
+                # (fhp_outer_accumulate), bit-identical to the host sum
+                import torch
+                from .engine import outer_accumulate
+                shape = tuple(np.shape(vals[0]))
+                val_d = torch.zeros(shape + tuple(int(n) for n in Nbar), dtype=torch.float64,
+                                    device='cuda')
+                flat = val_d.view(int(np.prod(shape)), -1)
+                for v, c in zip(vals, chars):
+                    v = np.asarray(v, dtype=np.float64)
+                    if primaldual == 'dual':
+                        v = np.linalg.inv(v)
+                    c0 = torch.from_numpy(np.ascontiguousarray(np.fft.ifftshift(c))).to('cuda')
+                    outer_accumulate(flat, v, c0)
+                out = Tensor(name='A_Ga', val=val_d, order=2, multype=21, origin=0)
+                out.Y = self.Y
+                return out
             val = np.zeros(np.shape(vals[0]) + tuple(Nbar))
             for v, c in zip(vals, chars):
                 v = np.asarray(v, dtype=np.float64)

@@ -250,6 +250,18 @@ int fhp_ball_topology(int dim, const int* n, const double* axes, const double* x
                       const double* Y, double radius, double* out, void* stream);
 
 /*
+ * out[k][i] += v[k] * c[i] for k < nv, i < M: one inclusion's value matrix
+ * (nv = d_v^2 host doubles) times its characteristic function c (device,
+ * M doubles) added to the coefficient field out (device, [nv][M]), product and
+ * sum rounded as NumPy rounds val += np.multiply.outer(v, c) (bit-identical).
+ * c and out must not overlap.  1 <= nv <= 36.
+ * Replaces: the sum over inclusions of Material.get_A_Ga, order None
+ * (ffthompy/materials.py:66-75).
+ */
+int fhp_outer_accumulate(int nv, const double* v, const double* c, double* out, long long M,
+                         void* stream);
+
+/*
  * Per-voxel inverse of a field of d x d matrices (the dual coefficient):
  * Ainv(x) = A(x)^-1 by Gauss-Jordan elimination without pivoting, in the
  * reference's order, each product and difference rounded separately as NumPy

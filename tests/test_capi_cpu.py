@@ -131,3 +131,16 @@ def test_ball_entry_points_reject_bad_arguments(lib):
     z = (ctypes.c_int * 3)(5, 0, 5)
     assert lib.fhp_ball_topology(3, z, t, x0, Y, 0.2, out, None) == bad
     assert lib.fhp_ball_characteristic(None, 0.2, 1.0, t, t, out, None) == bad
+
+
+def test_outer_accumulate_rejects_bad_arguments(lib):
+    from ffthompy_gb300 import _lib
+    v = (ctypes.c_double * 40)(*range(40))
+    c = ctypes.c_void_p(1 << 20)
+    out = ctypes.c_void_p(1 << 30)
+    bad = _lib.FHP_BAD_ARG
+    assert lib.fhp_outer_accumulate(0, v, c, out, 100, None) == bad
+    assert lib.fhp_outer_accumulate(37, v, c, out, 100, None) == bad
+    assert lib.fhp_outer_accumulate(4, v, c, out, 0, None) == bad
+    assert lib.fhp_outer_accumulate(4, None, c, out, 100, None) == bad
+    assert lib.fhp_outer_accumulate(4, v, c, c, 100, None) == bad      # overlap

@@ -103,3 +103,22 @@ def test_reference_ball_problem_through_gpu_assembly():
         for key, val in mats.items():
             got = pb.output['mat_' + pd][key]
             assert np.abs(got - val).max() <= 1e-9 * np.abs(val).max(), (pd, key)
+
+
+def test_inclusion_sum_on_gpu_is_bit_identical(monkeypatch):
+    """Material.get_A_Ga (order None): the sum over inclusions on the GPU
+    (fhp_outer_accumulate) equals the host sum bit for bit when the
+    characteristic functions are the same (boxes, pyramids and 'otherwise',
+    whose transforms are host code), primal and dual, 2D and 3D."""
+    from ffthompy_gb300.materials import Material
+    for d, N in ((2, (31, 45)), (3, (15, 17, 13))):
+        conf = {'inclusions': ['cube', 'pyramid', 'otherwise'],
+                'positions': [np.full(d, -0.2), np.full(d, 0.25), ''],
+                'params': [np.full(d, 0.3), np.full(d, 0.35), ''],
+                'vals': [np.eye(d) * 7. + 1., np.diag(np.arange(1., d + 1.)) * 3., np.eye(d)],
+                'Y': np.ones(d), 'order': None}
+        for pd in ('primal', 'dual'):
+            gpu = Material(dict(conf)).get_A_Ga(np.array(N), pd, order=None).val
+            host = _host(monkeypatch,
+                         lambda: Material(dict(conf)).get_A_Ga(np.array(N), pd, order=None).val)
+            np.testing.assert_array_equal(gpu, host)
