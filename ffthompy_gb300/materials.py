@@ -14,8 +14,9 @@ inclusions {'inclusions', 'positions', 'params', 'vals', 'Y', 'order', 'P'}.
 Coefficient assembly runs once per problem. On a GPU the grid-based Ga
 coefficient (fhp_ga_grid_coefficient), the dual inverse
 (fhp_coefficient_inverse), the Ga characteristic function of balls
-(fhp_ball_characteristic) and their GaNi topologies (fhp_ball_topology) run
-in the CUDA library. Boxes and pyramids use separable host transforms; the
+(fhp_ball_characteristic), their GaNi topologies (fhp_ball_topology) and the
+sum over inclusions of the exact-integration coefficient
+(fhp_outer_accumulate) run in the CUDA library. Boxes and pyramids use separable host transforms; the
 rest runs on the host (NumPy). The result is a Tensor with origin 0 on the
 GPU.
 """
