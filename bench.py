@@ -10,9 +10,9 @@ coefficient resident in HBM.  Fields (4.7 GB per vector) exceed L2.
 
 --impl reference runs the reference's algorithm on the host cores: its NumPy
 restatement (the oracle; the reference source tree is not present on the GPU
-host) on a bounded sample of the same workload (Ga N=31 -> 61^3 grid, same
-sphere statistics, 3 loads, a few CG iterations per load), one worker process
-per host core.
+host) on a bounded sample of the same workload (Ga N=63 -> 125^3 grid, same
+sphere statistics, 3 loads, one CG iteration per load and step), one worker
+process per host core.
 """
 import argparse
 import json
@@ -45,7 +45,6 @@ WORKLOADS = {
 
 def _dims(v):
     return tuple(v) if isinstance(v, (tuple, list)) else (v,) * 3
-SAMPLE = dict(N=31, P=31, iters=4)    # CPU baseline sample (61^3 grid)
 
 
 def parse():
@@ -184,40 +183,113 @@ class ClockSampler:
 
 
 # ----------------------------------------------------------------------------
-# CPU baseline: the oracle (NumPy restatement of the reference) on a sample
+# CPU baseline: the oracle (NumPy restatement of the reference) on samples
 # ----------------------------------------------------------------------------
+_SAMPLE_CACHE = {}
+
+
+def _sample_operator(seed, N):
+    """Ga spheres sample on the (2N-1)^3 grid: the oracle's coefficient,
+    Green operator and the 3 right-hand sides (built once per process)."""
+    key = (seed, N)
+    if key not in _SAMPLE_CACHE:
+        sys.path.insert(0, ROOT)
+        import oracle
+        from ffthompy_gb300.workloads import spheres_coefficient
+        Nn = np.array([N] * 3)
+        vals = spheres_coefficient((N,) * 3, radius=0.08, vf=0.3, contrast=100., seed=seed)
+        mat = oracle.Material({'fun': lambda c, _v=vals: _v, 'Y': np.ones(3), 'order': 0,
+                               'P': Nn})
+        A = mat.get_A_Ga(2 * Nn - 1, 'primal')
+        G, Ns = oracle.green_operator('scalar', Nn, np.ones(3), 'Ga', 1)
+        Afun = lambda v, _G=G, _A=A: oracle.apply_GA(_G, _A, v)
+        Bs = []
+        for l in range(3):
+            E = np.zeros((3,) + tuple(Ns))
+            E[l] = 1.
+            Bs.append(Afun(-E))
+        _SAMPLE_CACHE.clear()
+        _SAMPLE_CACHE[key] = (Afun, Bs, int(np.prod(Ns)))
+    return _SAMPLE_CACHE[key]
+
+
 def _cpu_sample(args):
-    """One worker: Ga spheres sample, 3 loads x iters CG iterations (solver only)."""
-    seed, N, iters = args
-    sys.path.insert(0, ROOT)
+    """One worker: iters CG iterations of each of the 3 loads of a Ga spheres
+    sample; as_shipped adds the reference's CallBack matvec per iteration
+    (ffthompy/general/solver_pp.py:13-24, installed by
+    ffthompy/applications.py:71-72).  Returns (voxel-iterations, seconds)."""
+    seed, N, iters, as_shipped = args
     import oracle
-    from ffthompy_gb300.workloads import spheres_coefficient
-    Nn = np.array([N] * 3)
-    vals = spheres_coefficient((N,) * 3, radius=0.08, vf=0.3, contrast=100., seed=seed)
-    mat = oracle.Material({'fun': lambda c, _v=vals: _v, 'Y': np.ones(3), 'order': 0, 'P': Nn})
-    A = mat.get_A_Ga(2 * Nn - 1, 'primal')
-    G, Ns = oracle.green_operator('scalar', Nn, np.ones(3), 'Ga', 1)
-    Afun = lambda v: oracle.apply_GA(G, A, v)
-    M = int(np.prod(Ns))
+    Afun, Bs, M = _sample_operator(seed, N)
     t = 0.
     vox_it = 0
-    for l in range(3):
-        E = np.zeros((3,) + tuple(Ns))
-        E[l] = 1.
-        B = Afun(-E)
+    for B in Bs:
+        cb = None
+        if as_shipped:
+            log = []
+            # one operator application per call, as CallBack.__call__
+            cb = lambda x, _B=B, _log=log: _log.append(
+                float(np.sqrt(np.sum((_B - Afun(x)) ** 2) / M)))
         t0 = time.perf_counter()
-        _, info = oracle.cg(Afun, B, np.zeros_like(E), tol=0., maxiter=iters)
+        _, info = oracle.cg(Afun, B, np.zeros_like(B), tol=0., maxiter=iters, callback=cb)
         t += time.perf_counter() - t0
         vox_it += M * info['kit']
     return vox_it, t
 
 
+def _pinned_samples(jobs, core=0):
+    """Run the samples in a child process pinned to one host core."""
+    os.sched_setaffinity(0, {core})
+    return [_cpu_sample(j) for j in jobs]
+
+
+def host_cpu_model():
+    try:
+        out = subprocess.run(['lscpu'], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith('Model name:'):
+                return line.split(':', 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in open('/proc/cpuinfo'):
+            if line.lower().startswith(('model name', 'cpu part')):
+                return line.split(':', 1)[1].strip()
+    except OSError:
+        pass
+    return 'unknown'
+
+
 def cpu_baseline():
-    vox_it, t = _cpu_sample((7, SAMPLE['N'], SAMPLE['iters']))
-    return {'value': vox_it / t / 1e6, 'unit': 'Mvoxel-iter/s', 'cores': 1, 'kind': 'port',
-            'sample': 'NumPy restatement of the reference CG (rfftn G o A, solver only), '
-                      'Ga %d^3 -> %d^3 grid, spheres r=0.08 vf=0.3 contrast 100, 3 loads x %d '
-                      'iterations, 1 core' % (SAMPLE['N'], 2 * SAMPLE['N'] - 1, SAMPLE['iters'])}
+    """The oracle on one pinned host core: solver-only and as shipped (with the
+    CallBack matvec) on the 61^3 and 125^3 grids of the same configuration;
+    value = solver-only on 125^3 (the sample closest to the workload)."""
+    import multiprocessing as mp
+    jobs = [(7, 31, 4, False), (7, 31, 4, True), (7, 63, 2, False), (7, 63, 2, True)]
+    core = sorted(os.sched_getaffinity(0))[0]
+    with mp.get_context('spawn').Pool(1) as pool:
+        res = pool.apply(_pinned_samples, (jobs, core))
+    rates = {}
+    for (seed, N, iters, shipped), (vox, t) in zip(jobs, res):
+        rates['%s_%d^3' % ('as_shipped' if shipped else 'solver_only', 2 * N - 1)] = \
+            round(vox / t / 1e6, 4)
+    return {'value': rates['solver_only_125^3'], 'unit': 'Mvoxel-iter/s', 'cores': 1,
+            'kind': 'port', 'cpu_model': host_cpu_model(), 'pinned_core': core,
+            'variants': rates,
+            'sample': 'NumPy restatement of the reference CG (rfftn G o A) pinned to one '
+                      'host core: Ga spheres (r=0.08, vf=0.3, contrast 100, 3 loads) on the '
+                      '61^3 grid (4 iterations per load) and the 125^3 grid (2 iterations '
+                      'per load), solver-only and as shipped (the reference\'s CallBack '
+                      'adds one operator application per iteration); value = solver-only '
+                      'on 125^3'}
+
+
+REF_SAMPLE = dict(N=63, iters=1)    # reference arm: 125^3 grid, 1 iteration per load and step
+
+
+def _ref_worker(args):
+    wid, seed, N, iters = args
+    return _cpu_sample((seed, N, iters, False))
 
 
 def run_reference(args):
@@ -225,14 +297,17 @@ def run_reference(args):
     if rank != 0:
         return
     import multiprocessing as mp
-    cores = os.cpu_count() or 1
+    cores = sorted(os.sched_getaffinity(0))
+    ncores = len(cores)
     ctx = mp.get_context('spawn')
-    jobs = [(100 + i, SAMPLE['N'], SAMPLE['iters']) for i in range(cores)]
+    N, iters = REF_SAMPLE['N'], REF_SAMPLE['iters']
+    jobs = [(i, 100 + i, N, iters) for i in range(ncores)]
     times = []
-    with ctx.Pool(cores) as pool:
+    with ctx.Pool(ncores) as pool:
+        # one sample per worker process, built once (setup not timed)
+        pool.map(_ref_worker, [(i, s, n, 0) for i, s, n, _ in jobs], chunksize=1)
         for step in range(args.warmup + args.steps):
-            t0 = time.perf_counter()
-            res = pool.map(_cpu_sample, jobs)
+            res = pool.map(_ref_worker, jobs, chunksize=1)
             # the workers' CG phases run concurrently: aggregate over the slowest
             dt = max(r[1] for r in res)
             if step >= args.warmup:
@@ -246,13 +321,15 @@ def run_reference(args):
         'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
         'ms_per_step': 1e3 * tot / len(times), 'higher_is_better': True, 'scaling': 'weak',
         'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
-        'config': {'workload': '%s (sample: Ga %d^3 -> %d^3, one sample per core)'
-                               % (args.workload, SAMPLE['N'], 2 * SAMPLE['N'] - 1),
+        'config': {'workload': '%s (sample: Ga %d^3 -> %d^3, one sample per host core)'
+                               % (args.workload, N, 2 * N - 1),
                    'grid': [2 * n - 1 for n in _dims(w['N'])], 'loads': 3},
-        'cpu_baseline': {'value': value, 'unit': 'Mvoxel-iter/s', 'cores': cores, 'kind': 'port',
-                         'sample': '%d processes x (Ga %d^3 -> %d^3 spheres, 3 loads x %d CG '
-                                   'iterations), NumPy restatement of the reference'
-                                   % (cores, SAMPLE['N'], 2 * SAMPLE['N'] - 1, SAMPLE['iters'])},
+        'cpu_baseline': {'value': value, 'unit': 'Mvoxel-iter/s', 'cores': ncores, 'kind': 'port',
+                         'cpu_model': host_cpu_model(),
+                         'sample': '%d processes (one per host core) x (Ga %d^3 -> %d^3 spheres, '
+                                   'r=0.08 vf=0.3 contrast 100, 3 loads x %d CG iteration per '
+                                   'step, solver-only), NumPy restatement of the reference'
+                                   % (ncores, N, 2 * N - 1, iters)},
         'e2e': {'value': value, 'unit': 'Mvoxel-iter/s', 'h2d_bytes_per_step': 0,
                 'd2h_bytes_per_step': 0},
     }
@@ -319,6 +396,8 @@ def fibres_measure(n=127, tol=1e-6, seed=0):
         torch.cuda.synchronize()
         out['seconds_' + prec] = time.perf_counter() - t0
         out['kit_primal_' + prec] = [int(r['info']['kit']) for r in pb.output['res_primal']]
+        out['phases_' + prec] = {pd: {k: round(v, 4) for k, v in ph.items()}
+                                 for pd, ph in pb.output['time']['phases'].items()}
         mats[prec] = pb.output['mat_primal']['AH_GaNi_primal']
     out['AH_rel_diff_mixed_vs_f64'] = float(np.abs(mats['mixed'] - mats['f64']).max()
                                             / np.abs(mats['f64']).max())
@@ -431,18 +510,19 @@ def run_gpu(args):
     plan.set_coefficient(A.data)
     tol = w['tol']
 
-    def step():
-        B = plan.rhs_macro(1)
-        X, info = plan.cg(B, tol=tol, maxiter=2000, log_rows=1)
-        AH = plan.energy(X)
+    def step(p=plan, t=tol):
+        B = p.rhs_macro(1)
+        X, info = p.cg(B, tol=t, maxiter=2000, log_rows=1)
+        AH = p.energy(X)
         return AH, info
 
     for _ in range(args.warmup):
         AH, info = step()
     torch.cuda.synchronize()
     barrier(dist)
+    # the timed region runs the shipped path: each CG iteration is one CUDA
+    # graph replay, no per-kernel events
     launches0 = plan.launches()
-    plan.profile(True)
     clk = ClockSampler(torch.cuda.current_device())
     clk.start()
     stream = torch.cuda.current_stream()
@@ -461,13 +541,26 @@ def run_gpu(args):
     ms = ev0.elapsed_time(ev1)
     ms = reduce_max(dist, ms)
     launches = plan.launches() - launches0
-    prof = plan.profile_read()
-    plan.profile(False)
     vox_it = M * sum(kits) * world
     value = vox_it / (ms / 1e3) / 1e6
     AH_err = float(np.abs(AH - AH_ref).max() / np.abs(AH_ref).max())
 
-    # roofline of the dominant kernel (largest total time in the timed region)
+    # per-kernel CUDA events: one more step of the same workload with the
+    # profiler on (direct launches instead of graph replay, same kernels)
+    plan.profile(True)
+    torch.cuda.synchronize()
+    ev2 = torch.cuda.Event(enable_timing=True)
+    ev3 = torch.cuda.Event(enable_timing=True)
+    ev2.record(stream)
+    AHp, infop = step()
+    ev3.record(stream)
+    torch.cuda.synchronize()
+    prof = plan.profile_read()
+    plan.profile(False)
+    extras['profiled_step_ms'] = ev2.elapsed_time(ev3)
+    extras['profiled_step_cg_iterations'] = infop['kit']
+
+    # roofline of the dominant kernel (largest total time in the profiled step)
     import json as _json
     peaks = {}
     try:
@@ -480,11 +573,22 @@ def run_gpu(args):
     tname, t = top
     per_launch_s = t['ms'] / 1e3 / max(1, t['launches'])
     achieved = t['bytes_per_launch'] / per_launch_s / 1e9
-    kernels = {k: {'launches': v['launches'], 'ms_total': round(v['ms'], 3),
-                   'share': round(v['ms'] / max(1e-9, sum(x['ms'] for x in prof.values())), 4),
-                   'GBps': round(v['bytes_per_launch'] / (v['ms'] / 1e3 / max(1, v['launches']))
-                                 / 1e9, 1)}
-               for k, v in sorted(prof.items(), key=lambda kv: -kv[1]['ms'])}
+    tot_ms = sum(x['ms'] for x in prof.values())
+    it_max = max(infop['kit'])
+    kernels = {}
+    for k, v in sorted(prof.items(), key=lambda kv: -kv[1]['ms']):
+        row = {'launches': v['launches'], 'ms_total': round(v['ms'], 3),
+               'share': round(v['ms'] / max(1e-9, tot_ms), 4),
+               'MB_per_launch': round(v['bytes_per_launch'] / 1e6, 1)}
+        gbps = v['bytes_per_launch'] / (v['ms'] / 1e3 / max(1, v['launches'])) / 1e9
+        # kernels launched a few times per step (set-up, final projection)
+        # may run from L2: their rate is not evidence of HBM bandwidth
+        if v['launches'] >= it_max:
+            row['GBps'] = round(gbps, 1)
+        else:
+            row['GBps_not_hbm'] = round(gbps, 1)
+            row['note'] = 'launched %d times per step (outside the CG loop)' % v['launches']
+        kernels[k] = row
     traffic = None
     tf = os.path.join(ROOT, 'profiles', 'traffic.json')
     if os.path.exists(tf):
@@ -496,26 +600,30 @@ def run_gpu(args):
             traffic = None
     roofline = {'bound': 'hbm', 'achieved': round(achieved, 1), 'peak': peak, 'unit': 'GB/s',
                 'frac': round(achieved / peak, 4), 'traffic': traffic, 'kernel': tname,
-                'peak_source': peak_src + ' hbm_gbs'}
+                'peak_source': peak_src + ' hbm_gbs',
+                'timing': 'CUDA events around each launch in a profiled step of the same '
+                          'workload after the timed region'}
 
-    # FP64 GPU CG (plain form) for the mixed-vs-FP64 ratio: bounded iterations
+    # the plain form: FP64 fields and FFTs, the same band operator and
+    # tolerance, timed to A_H (right-hand sides, CG, energy) with CUDA events
     if not args.no_fp64:
         p64 = make_plan(w, 'f64', args.ga_mode)
         p64.set_coefficient(A.data)
-        B64 = p64.rhs_macro(1)
-        k64 = 3
-        p64.cg(B64, tol=0., maxiter=1)
+        p64.cg(p64.rhs_macro(1), tol=0., maxiter=1)     # warm: graph, scratch
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        p64.cg(B64, tol=0., maxiter=k64)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        AH64, info64 = step(p64, tol)
+        e1.record(stream)
         torch.cuda.synchronize()
-        it64 = (time.perf_counter() - t0) / k64
-        per_it = ms / 1e3 / args.steps / max(1, max(info['kit']))
-        extras['fp64_seconds_per_iteration'] = it64
-        extras['fp64_time_to_AH_s_extrapolated'] = it64 * max(info['kit'])
-        extras['mixed_seconds_per_iteration'] = per_it
-        extras['speedup_vs_fp64_gpu'] = it64 / per_it
-        del p64, B64
+        t64 = e0.elapsed_time(e1) / 1e3
+        extras['fp64_time_to_AH_s'] = t64
+        extras['fp64_cg_iterations'] = info64['kit']
+        extras['fp64_AH_rel_err_vs_fp64_refined'] = float(np.abs(AH64 - AH_ref).max()
+                                                          / np.abs(AH_ref).max())
+        extras['speedup_vs_fp64_gpu'] = t64 / (ms / 1e3 / args.steps)
+        del p64
         torch.cuda.empty_cache()
 
     # end to end through the host-buffer C-ABI entry point
@@ -528,7 +636,7 @@ def run_gpu(args):
                              maxiter=2000)   # warm
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    e2e_steps = max(1, min(args.steps, 2))
+    e2e_steps = max(1, min(args.steps, 3))
     kit_e = 0
     for _ in range(e2e_steps):
         AHe, kit, _, _ = e2e_plan.homogenize_host(packed=A_host, kind=_lib.FHP_COEF_ISO, proj=1,
@@ -540,7 +648,27 @@ def run_gpu(args):
            'h2d_bytes_per_step': int(A_host.nbytes), 'd2h_bytes_per_step': 9 * 8,
            'seconds_per_step': e2e_s / e2e_steps}
     extras['AH_e2e_rel_diff'] = float(np.abs(AHe - AH).max() / np.abs(AH).max())
-    del e2e_plan
+    # the same phases through the package API, each bracketed by CUDA events
+    ph = {}
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    evs[0].record(stream)
+    e2e_plan.set_coefficient_packed(A_host, _lib.FHP_COEF_ISO)
+    evs[1].record(stream)
+    Be = e2e_plan.rhs_macro(1)
+    evs[2].record(stream)
+    Xe, _ = e2e_plan.cg(Be, tol=tol, maxiter=2000, log_rows=1)
+    evs[3].record(stream)
+    e2e_plan.energy(Xe)
+    evs[4].record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    for i, name in enumerate(['coefficient_upload_ms', 'rhs_ms', 'cg_ms', 'energy_ms']):
+        ph[name] = round(evs[i].elapsed_time(evs[i + 1]), 3)
+    ph['wall_ms'] = round(wall * 1e3, 3)
+    extras['e2e_phases'] = ph
+    del e2e_plan, Xe, Be
     torch.cuda.empty_cache()
 
     # potential formulation with the 1/|xi| preconditioner (homog_GaNi_full_

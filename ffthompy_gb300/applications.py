@@ -19,6 +19,7 @@ postprocess.  Differences from the reference, by design:
 import time
 
 import numpy as np
+import torch
 
 from .engine import GalerkinPlan, nice_size
 from .general.solver_pp import CallBack
@@ -41,8 +42,10 @@ def _solve(pb, physics):
     if str(pb.solver.get('kind', 'CG')).lower() != 'cg':
         raise NotImplementedError('solver %s' % pb.solver.get('kind'))
     ga_mode = pb.solve.get('ga_mode', 'band')
+    phases = pb.output.setdefault('time', {}).setdefault('phases', {})
     for primaldual in pb.solve['primaldual']:
         t0 = time.time()
+        tp = _phase_clock()
         mat = Material(pb.material)
         proj = 1 if primaldual == 'primal' else 2
         if kind == 'GaNi':
@@ -57,10 +60,13 @@ def _solve(pb, physics):
             A = mat.get_A_Ga(Nbar=Nbar, primaldual=primaldual, grid=integ)
             plan = GalerkinPlan(tuple(N), pb.Y, physics=physics, integ=integ,
                                 precision=precision)
+        ph = phases.setdefault(primaldual, {})
+        ph['coefficient_s'] = tp()
         plan.set_coefficient(A.data)
         plan._coef_tensor = A
         B = plan.rhs_macro(proj)
         X, info = plan.cg(B, None, tol=tol, maxiter=maxiter, proj=proj)
+        ph['solve_s'] = tp()
         results = []
         t_solve = time.time() - t0
         for l in range(plan.nloads):
@@ -72,6 +78,20 @@ def _solve(pb, physics):
                                                'time': [[t_solve, t_solve, t_solve]]}})
         out_grid = tuple(N) if kind == 'GaNi' else tuple(Nbar)
         postprocess(pb, A, mat, Solutions(plan, X, pb.Y, out_grid), results, primaldual)
+        ph['postprocess_s'] = tp()
+
+
+def _phase_clock():
+    """Seconds since the previous call, with the device synchronised at each
+    call so that a phase's GPU work is charged to it."""
+    last = [time.perf_counter()]
+
+    def lap():
+        torch.cuda.synchronize()
+        now = time.perf_counter()
+        dt, last[0] = now - last[0], now
+        return dt
+    return lap
 
 
 def scalar(problem):

@@ -277,20 +277,20 @@ extern "C" int fhp_ball_topology(int dim, const int* n, const double* axes, cons
 
 namespace {
 
+// One inclusion's values, passed by value (288 bytes of kernel parameters).
+struct OuterValues { double v[36]; };
+
 // out[k][i] += v[k] * c[i] for k < nv: the product and the sum rounded on
 // their own, as NumPy's val += np.multiply.outer(v, c) rounds them.
 __global__ void __launch_bounds__(256)
     k_outer_accumulate(const double* __restrict__ c, double* __restrict__ out, int nv,
-                       double v0, double v1, double v2, double v3, double v4, double v5,
-                       const double* __restrict__ vrest, long long M) {
+                       const __grid_constant__ OuterValues vals, long long M) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += stride) {
     const double ci = c[i];
     for (int k = 0; k < nv; ++k) {
-      const double vk = k == 0 ? v0 : k == 1 ? v1 : k == 2 ? v2 : k == 3 ? v3 : k == 4 ? v4
-                        : k == 5 ? v5 : vrest[k - 6];
       double* o = out + (long long)k * M + i;
-      *o = __dadd_rn(*o, __dmul_rn(vk, ci));
+      *o = __dadd_rn(*o, __dmul_rn(vals.v[k], ci));
     }
   }
 }
@@ -306,27 +306,15 @@ extern "C" int fhp_outer_accumulate(int nv, const double* v, const double* c, do
   if (c0 < o0 + ob && o0 < c0 + (unsigned long long)M * sizeof(double))
     return fail(FHP_BAD_ARG, "c and out overlap");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  double* rest = nullptr;
-  if (nv > 6) {
-    cudaError_t e = cudaMallocAsync(&rest, (nv - 6) * sizeof(double), s);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(rest, v + 6, (nv - 6) * sizeof(double), cudaMemcpyHostToDevice, s);
-    if (e != cudaSuccess) {
-      if (rest) cudaFreeAsync(rest, s);
-      return fail(FHP_CUDA, std::string("outer accumulate set-up: ") + cudaGetErrorString(e));
-    }
-  }
-  double vv[6] = {0., 0., 0., 0., 0., 0.};
-  for (int k = 0; k < nv && k < 6; ++k) vv[k] = v[k];
+  OuterValues vals{};
+  for (int k = 0; k < nv; ++k) vals.v[k] = v[k];
   int nsm = 152, dev = 0;
   if (cudaGetDevice(&dev) == cudaSuccess)
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   const long long need = (M + 255) / 256;
   const int grid = (int)(need < 8LL * nsm ? need : 8LL * nsm);
-  k_outer_accumulate<<<grid, 256, 0, s>>>(c, out, nv, vv[0], vv[1], vv[2], vv[3], vv[4], vv[5],
-                                          rest, M);
+  k_outer_accumulate<<<grid, 256, 0, s>>>(c, out, nv, vals, M);
   const cudaError_t e = cudaGetLastError();
-  if (rest) cudaFreeAsync(rest, s);
   if (e != cudaSuccess)
     return fail(FHP_CUDA, std::string("k_outer_accumulate launch: ") + cudaGetErrorString(e));
   return FHP_OK;

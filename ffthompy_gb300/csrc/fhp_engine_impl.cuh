@@ -793,7 +793,11 @@ class Engine final : public EngineBase {
 
   // algorithmic bytes of the passes (each input read once, each output written once)
   double field_bytes() const { return (double)g_.L * g_.dv * g_.M * sizeof(R); }
-  double spec_bytes() const { return (double)spec_elems_ * 2 * sizeof(R); }
+  // the solve grid's half spectrum (the buffer of band plans is larger: it
+  // also holds the integration grid's spectra)
+  double spec_bytes() const {
+    return (double)g_.L * g_.dv * g_.n0 * g_.n1 * g_.n2h * 2 * sizeof(R);
+  }
   double coef_bytes() const {
     const int dv = g_.dv;
     const int c = coef_kind_ == COEF_ISO ? 1 : coef_kind_ == COEF_SYM ? dv * (dv + 1) / 2

@@ -12,8 +12,9 @@
 // Limits: loads <= 6 and dv <= 6 (36 accumulators per block), at most
 // kNoAllocMaxBlocks blocks; the scratch is shared by every call on a device, so
 // calls that overlap in time on one device race and must be serialised by the
-// caller.  The first call on a device looks up the scratch address and loads
-// the kernels; it should come before any stream capture.
+// caller.  Every call looks up the scratch's device address (no allocation);
+// the first call on a device also loads the kernels and should come before
+// any stream capture.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -106,23 +107,25 @@ int fail(int status, const char* msg) {
   return status;
 }
 
-// Once per device, with that device current: the scratch's device address, the
-// SM count, and the kernels loaded.
+// Once per device, with that device current: the SM count and the kernels
+// loaded.  The scratch's device address is looked up on every call (no
+// allocation, and a cached address would go stale if the device's primary
+// context were reset and created again).
 int scratch_for_current_device(DeviceScratch& out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return fail(FHP_CUDA, "cudaGetDevice failed");
   if (dev < 0 || dev >= kMaxDevices) return fail(FHP_BAD_ARG, "device index beyond 63");
+  double* p = nullptr;
+  cudaError_t ea = cudaGetSymbolAddress((void**)&p, fhp_noalloc_scratch);
+  if (ea != cudaSuccess) {
+    fhp::set_error(std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(ea));
+    return FHP_CUDA;
+  }
   std::lock_guard<std::mutex> g(g_setup_mu);
   DeviceScratch& d = g_setup[dev];
   if (!d.ready) {
-    double* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress((void**)&p, fhp_noalloc_scratch);
-    if (e != cudaSuccess) {
-      fhp::set_error(std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
-      return FHP_CUDA;
-    }
     int nsm = 0;
-    e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaError_t e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     cudaFuncAttributes fa;
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_energy_oneshot<fhp::COEF_ISO>);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_energy_oneshot<fhp::COEF_SYM>);
@@ -131,10 +134,10 @@ int scratch_for_current_device(DeviceScratch& out) {
       fhp::set_error(std::string("no-alloc energy set-up: ") + cudaGetErrorString(e));
       return FHP_CUDA;
     }
-    d.ptr = p;
     d.nsm = nsm > 0 ? nsm : 1;
     d.ready = true;
   }
+  d.ptr = p;
   out = d;
   return FHP_OK;
 }

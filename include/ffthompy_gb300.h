@@ -309,8 +309,9 @@ long long fhp_plan_launches(fhp_plan plan);
  * most 1024 blocks); larger sizes return FHP_BAD_ARG.
  * Every call on a device uses the same scratch: calls that overlap in time on
  * one device (several streams or host threads) race, so serialise them.
- * The first call on each device does a one-time set-up (looks up the scratch
- * address, loads the kernels); make that call before any stream capture.
+ * Every call looks up the scratch's device address (no allocation); the first
+ * call on each device also loads the kernels: make that call before any stream
+ * capture.
  * No counterpart in the reference: its assembly_matrix
  * (ffthompy/postprocess.py:53-70) is the same sum, with no allocation contract.
  */

@@ -1,7 +1,8 @@
 """Generate the golden fixtures under tests/golden/ from the FFTHomPy reference.
 
 This script is the only place that runs the reference.  It imports the
-unmodified reference package from REFERENCE_DIR (default /root/reference),
+unmodified reference package from the directory given as its first argument
+(or, with no argument, from the environment variable FFTHOMPY_REFERENCE),
 with a small runtime shim for the NumPy/SciPy/Python names it still uses
 (np.int/np.float/np.complex, time.clock, collections.Callable,
 scipy.setdiff1d).  It writes plain .npz files (arrays + a JSON metadata
@@ -40,7 +41,8 @@ inv_<name>.npz
     Per-voxel inverses of get_inverse (ffthompy/trigpol.py:120-159) of
     seeded matrix fields, one with zero pivots (Inf / NaN outputs).
 
-Usage:  python tests/golden/make_golden.py [REFERENCE_DIR [pickles|run|op|pot|solv|inv ...]]
+Usage:  python tests/golden/make_golden.py REFERENCE_DIR [pickles|run|op|pot|solv|inv ...]
+        FFTHOMPY_REFERENCE=REFERENCE_DIR python tests/golden/make_golden.py
 """
 import collections
 import collections.abc
@@ -57,7 +59,7 @@ import numpy as np
 import scipy
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE_DIR = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
+REFERENCE_DIR = sys.argv[1] if len(sys.argv) > 1 else os.environ.get('FFTHOMPY_REFERENCE')
 
 
 def _install_shim():
@@ -431,6 +433,9 @@ def inverse_cases():
 
 
 if __name__ == '__main__':
+    if not REFERENCE_DIR or not os.path.isdir(REFERENCE_DIR):
+        sys.exit('make_golden.py: give the FFTHomPy source directory as the first argument '
+                 'or in FFTHOMPY_REFERENCE')
     _install_shim()
     import warnings
     warnings.simplefilter('ignore')
