@@ -66,6 +66,10 @@ def parse():
                     help='skip the 512-instance 2D ensemble measurement')
     ap.add_argument('--no-potential', action='store_true',
                     help='skip the potential-formulation measurement (GaNi on the image grid)')
+    ap.add_argument('--kernels-only', action='store_true',
+                    help='only the warm-up and timed steps of the workload (for profiler '
+                         'captures): no FP64-refined reference, FP64 run, end-to-end run, '
+                         'extra workloads or CPU baseline')
     return ap.parse_args()
 
 
@@ -340,15 +344,16 @@ def run_reference(args):
 # the GPU arm
 # ----------------------------------------------------------------------------
 def ensemble_measure(count=512, sizes=(63, 127, 255, 511), seed=12, tol=1e-6, workers=16,
-                     precision='f64'):
+                     precision='f64', dist=None):
     """Many independent 2D GaNi cells (thresholded Gaussian random fields,
     length 0.1, 0.4-quantile, contrast log-uniform in [2, 1000], n drawn from
     sizes, 2 loads each) solved together by homogenize_many to tol (FP64, or
     mixed: FP32 inner CG refined in FP64): aggregate Mvoxel-iter/s over all
-    instances."""
+    instances.  Under torchrun the cells are split across the ranks
+    (homogenize_many_ranks) and the time is the slowest rank's."""
     import torch
     from ffthompy_gb300 import workloads
-    from ffthompy_gb300.batch import homogenize_many
+    from ffthompy_gb300.batch import homogenize_many, homogenize_many_ranks
     rng = np.random.default_rng(seed)
     coefs = []
     for _ in range(count):
@@ -359,13 +364,17 @@ def ensemble_measure(count=512, sizes=(63, 127, 255, 511), seed=12, tol=1e-6, wo
                                                      seed=int(rng.integers(1 << 30))))
     homogenize_many(coefs[:workers], tol=tol, workers=workers, precision=precision)  # warm
     torch.cuda.synchronize()
+    barrier(dist)
     t0 = time.perf_counter()
-    res = homogenize_many(coefs, tol=tol, workers=workers, precision=precision)
+    res = homogenize_many_ranks(coefs, tol=tol, workers=workers, precision=precision)
     torch.cuda.synchronize()
-    dt = time.perf_counter() - t0
+    dt = reduce_max(dist, time.perf_counter() - t0)
+    if res is None:     # not rank 0
+        return None
     vox_it = sum(int(np.prod(A.shape[2:])) * sum(r['kit_primal']) for A, r in zip(coefs, res))
     return {'instances': count, 'sizes': list(sizes), 'loads': 2, 'precision': precision,
             'tol': tol, 'voxels': int(sum(np.prod(A.shape[2:]) for A in coefs)),
+            'ranks': 1 if dist is None else dist.get_world_size(),
             'seconds': dt, 'Mvoxel_iter_per_s': vox_it / dt / 1e6,
             'all_converged': all(r['status_primal'] == [0, 0] for r in res)}
 
@@ -475,6 +484,32 @@ def potential_measure(vals, w, tol, steps=2):
                                                          / np.abs(AHg).max())}
 
 
+def run_kernels_only(args, w, A, M, dist, world, rank):
+    """The workload's steps alone (warm-up, then timed): the command line
+    for profiler captures of the CG kernels."""
+    import torch
+    plan = make_plan(w, args.precision, args.ga_mode)
+    plan.set_coefficient(A.data)
+    kits = []
+    torch.cuda.synchronize()
+    t0 = None
+    for i in range(args.warmup + args.steps):
+        if i == args.warmup:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+        X, info = plan.cg(plan.rhs_macro(1), tol=w['tol'], maxiter=2000, log_rows=1)
+        plan.energy(X)
+        if i >= args.warmup:
+            kits.append(sum(info['kit']))
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - (t0 if t0 is not None else time.perf_counter())
+    if rank == 0:
+        print(json.dumps({'workload': args.workload, 'kernels_only': True,
+                          'cg_iterations': info['kit'], 'seconds': dt,
+                          'Mvoxel_iter_per_s': M * sum(kits) / max(dt, 1e-9) / 1e6}),
+              flush=True)
+
+
 def run_gpu(args):
     import torch
     rank, world, dist = dist_init()
@@ -494,6 +529,10 @@ def run_gpu(args):
     A_iso = A.data[0, 0].contiguous()
     extras = {'coefficient_grid': list(cgrid)}
 
+    if args.kernels_only:
+        args.no_fp64 = args.no_fibres = args.no_ensemble = args.no_potential = True
+        args.no_cpu_baseline = True
+        return run_kernels_only(args, w, A, M, dist, world, rank)
     # FP64-refined reference A_H (mixed plan, FP64 outer residual, tight tol)
     ref = make_plan(w, 'mixed', args.ga_mode)
     ref.set_coefficient(A.data)
@@ -667,6 +706,15 @@ def run_gpu(args):
     for i, name in enumerate(['coefficient_upload_ms', 'rhs_ms', 'cg_ms', 'energy_ms']):
         ph[name] = round(evs[i].elapsed_time(evs[i + 1]), 3)
     ph['wall_ms'] = round(wall * 1e3, 3)
+    # the same host buffer copied by torch, for comparison with the upload
+    dev_A = torch.empty(tuple(A_iso.shape), dtype=torch.float64, device='cuda')
+    torch.cuda.synchronize()
+    evs[0].record(stream)
+    dev_A.copy_(host_A, non_blocking=True)
+    evs[1].record(stream)
+    torch.cuda.synchronize()
+    ph['torch_h2d_same_buffer_ms'] = round(evs[0].elapsed_time(evs[1]), 3)
+    del dev_A
     extras['e2e_phases'] = ph
     del e2e_plan, Xe, Be
     torch.cuda.empty_cache()
@@ -680,8 +728,8 @@ def run_gpu(args):
         extras['fibres127'] = fibres_measure()
         extras['coefficient_inverse'] = inverse_measure()
     if not args.no_ensemble:
-        extras['ensemble_grf2d'] = ensemble_measure()
-        extras['ensemble_grf2d_mixed'] = ensemble_measure(precision='mixed')
+        extras['ensemble_grf2d'] = ensemble_measure(dist=dist)
+        extras['ensemble_grf2d_mixed'] = ensemble_measure(precision='mixed', dist=dist)
 
     if rank != 0:
         return

@@ -34,6 +34,7 @@ SIGNATURES = {
                                             ctypes.c_double, ctypes.c_int]),
     'fhp_plan_destroy': (ctypes.c_int, [_vp]),
     'fhp_plan_set_refinement': (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_int]),
+    'fhp_plan_set_band_cg': (ctypes.c_int, [_vp, ctypes.c_int]),
     'fhp_plan_query': (ctypes.c_int, [_vp, _c_ll_p, _c_int_p, _c_int_p, _c_int_p]),
     'fhp_set_coefficient': (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_int, _vp]),
     'fhp_apply': (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp]),

@@ -101,3 +101,18 @@ def _inverse_field(A):
     """Per-voxel inverse of a (dv, dv) + N field (the dual coefficient,
     ffthompy/materials.py get_A_GaNi with primaldual='dual'), on the GPU."""
     return coefficient_inverse(A)
+
+
+def homogenize_many_ranks(coefs, group=None, **kw):
+    """homogenize_many with the cells split across the ranks of an initialised
+    torch.distributed process group (one process per GPU, each on its own
+    device): every rank solves its share (partition.partition_costs by voxel
+    count) and rank 0 receives all results in input order (None on the other
+    ranks).  Without an initialised group this is homogenize_many."""
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()):
+        return homogenize_many(coefs, **kw)
+    from .partition import homogenize_partitioned, torch_gather
+    return homogenize_partitioned(coefs, dist.get_rank(group), dist.get_world_size(group),
+                                  lambda cs: homogenize_many(cs, **kw),
+                                  gather=torch_gather(group))

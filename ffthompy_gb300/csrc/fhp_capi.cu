@@ -236,6 +236,14 @@ int fhp_plan_set_refinement(fhp_plan plan, double eta, int max_outer) {
   return FHP_OK;
 }
 
+int fhp_plan_set_band_cg(fhp_plan plan, int spectral) {
+  if (!plan) return bad("plan is NULL");
+  if (spectral != 0 && spectral != 1) return bad("spectral must be 0 or 1");
+  plan->eng->set_spectral_cg(spectral != 0);
+  if (plan->lo) plan->lo->set_spectral_cg(spectral != 0);
+  return FHP_OK;
+}
+
 int fhp_plan_destroy(fhp_plan plan) {
   delete plan;
   return FHP_OK;

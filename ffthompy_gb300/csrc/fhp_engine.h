@@ -168,6 +168,9 @@ class EngineBase {
                      int log_cap, cudaStream_t s) = 0;
   // X = iF(enlarge(grad(P xh))): fields (load, comp) on this engine's grid
   virtual int pot_field(const void* xh, void* X, cudaStream_t s) = 0;
+  // band plans: CG on the half spectra of the iterates (default) or on the
+  // real fields of the solve grid; other plans ignore it
+  virtual void set_spectral_cg(bool on) { (void)on; }
   // kernel launch count of the last call (instrumentation)
   long long launches = 0;
 };

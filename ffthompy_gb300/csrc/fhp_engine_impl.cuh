@@ -517,6 +517,7 @@ class Engine final : public EngineBase {
     const R* b = static_cast<const R*>(bv);
     const R* x0 = static_cast<const R*>(x0v);
     R* x = static_cast<R*>(xv);
+    if (band_ && spectral_cg_) return spectral_cg_solve(proj, b, x0, tol, maxiter, x, res, log_cap, s);
     const size_t n = (size_t)g_.L * g_.dv * g_.M;
     int st = ensure_cg_buffers();
     if (st != ST_OK) return st;
@@ -555,17 +556,33 @@ class Engine final : public EngineBase {
     FHP_LAUNCHED();
     k_update_all_done<<<1, 1, 0, s>>>(st_, g_.L, all_done_);
     FHP_LAUNCHED();
-    // One iteration's launches captured once per solve into a CUDA graph and
-    // replayed per iteration (one launch instead of about ten: small grids are
-    // launch-bound).  Direct launches when profiling (the per-kernel events)
-    // or when the stream cannot be captured (the legacy default stream).
+    st = iterate(maxiter, s, [&]() { return cg_iteration(dlog, log_rows, s); });
+    if (st != ST_OK) return st;
+    // FP32 fields: the iterate drifts out of range(G) by roundoff accumulated
+    // over the iterations, and that component enters the energy to first
+    // order. One projection x <- G x (the identity in exact arithmetic) puts
+    // the drift back to a single rounding.
+    if (sizeof(R) == 4 && (st = project(proj, x, x, s)) != ST_OK) {
+      return st;
+    }
+    return collect(tol, log_rows, dlog, res, s);
+  }
+
+  // The iterations of a solve, in chunks between host checks of all_done.
+  // One iteration's launches are captured once per solve into a CUDA graph
+  // and replayed per iteration (one launch instead of about ten: small grids
+  // are launch-bound).  Direct launches when profiling (the per-kernel events)
+  // or when the stream cannot be captured (the legacy default stream).
+  template <typename F>
+  int iterate(int maxiter, cudaStream_t s, F&& one_iteration) {
+    int st = ST_OK;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
     long long per_iter = 0;
     if (!prof.on && maxiter > 0 &&
         cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
       const long long l0 = launches;
-      const int cst = cg_iteration(dlog, log_rows, s);
+      const int cst = one_iteration();
       const cudaError_t e = cudaStreamEndCapture(s, &graph);
       per_iter = launches - l0;
       launches = l0;
@@ -581,7 +598,6 @@ class Engine final : public EngineBase {
       if (gexec) cudaGraphExecDestroy(gexec);
       if (graph) cudaGraphDestroy(graph);
     };
-    // iterations, in chunks between host checks of all_done
     int done_iters = 0;
     int chunk = 2;
     while (done_iters < maxiter) {
@@ -598,7 +614,7 @@ class Engine final : public EngineBase {
             return ST_CUDA;
           }
           launches += per_iter;
-        } else if ((st = cg_iteration(dlog, log_rows, s)) != ST_OK) {
+        } else if ((st = one_iteration()) != ST_OK) {
           release_graph();
           return st;
         }
@@ -607,13 +623,11 @@ class Engine final : public EngineBase {
       chunk = std::min(chunk * 2, 32);
     }
     release_graph();
-    // FP32 fields: the iterate drifts out of range(G) by roundoff accumulated
-    // over the iterations, and that component enters the energy to first
-    // order. One projection x <- G x (the identity in exact arithmetic) puts
-    // the drift back to a single rounding.
-    if (sizeof(R) == 4 && (st = project(proj, x, x, s)) != ST_OK) {
-      return st;
-    }
+    return ST_OK;
+  }
+
+  // per-load results of a solve (solver.py:137-138) from the device state
+  int collect(double tol, int log_rows, const double* dlog, SolveResult& res, cudaStream_t s) {
     FHP_CHECK(cudaMemcpyAsync(h_st_, st_, g_.L * sizeof(LoadState), cudaMemcpyDeviceToHost, s));
     res.res_log.assign((size_t)log_rows * g_.L, 0.0);
     FHP_CHECK(cudaMemcpyAsync(res.res_log.data(), dlog, (size_t)log_rows * g_.L * sizeof(double),
@@ -622,7 +636,6 @@ class Engine final : public EngineBase {
     res.kit.resize(g_.L);
     res.norm_res.resize(g_.L);
     res.status.resize(g_.L);
-    int worst = ST_OK;
     res.iterations_run = 0;
     for (int l = 0; l < g_.L; ++l) {
       const LoadState& h = h_st_[l];
@@ -631,11 +644,192 @@ class Engine final : public EngineBase {
       int sl = h.status;
       if (sl == 0 && h.norm_res > tol && h.kit > 0) sl = ST_NONCONVERGED;
       res.status[l] = sl;
-      worst = std::max(worst, sl);
       res.iterations_run = std::max(res.iterations_run, h.kit);
     }
-    (void)worst;
     return ST_OK;  // per-load statuses are reported in res.status
+  }
+
+  // ---- spectral CG of band plans ---------------------------------------------
+  // The iterates x, r, p, Ap are kept as half spectra of the N grid in z form
+  // (k_half_weight): the band operator then starts at the pad to the
+  // integration grid and ends at the band projection, with no transform on
+  // the N grid inside the iteration, and the grid-mean inner products are
+  // Euclidean sums over z (fin kernels with a unit mean factor).  CG is the
+  // same recursion on the same operator in an orthogonal basis (Parseval), so
+  // iterates, residual norms and stopping tests are the reference's up to
+  // roundoff.  The initial residual is projected onto range(G).
+  void set_spectral_cg(bool on) override { spectral_cg_ = on; }
+
+  int ensure_spectral() {
+    const size_t nz = (size_t)g_.L * g_.dv * g_.n0 * g_.n1 * g_.n2h;
+    if (!zb_) FHP_CHECK(cudaMalloc(&zb_, 4 * nz * sizeof(cplx<R>)));
+    gz_ = g_;
+    gz_.M = 2LL * g_.n0 * g_.n1 * g_.n2h;
+    // partial sums of the spectral projection pass: one per CTA (the buffer
+    // grows once per plan; cudaFree waits for work that still uses it)
+    projf_parts_ = band_axis_ctas(BAND_DOWN_PROJ_F, spectral_proj_axis(), lb1_.dev, l1_.dev);
+    if (projf_parts_ > nparts_max_) {
+      double* np = nullptr;
+      FHP_CHECK(cudaMalloc(&np, (size_t)projf_parts_ * kMaxLoads * kMaxLoads * sizeof(double)));
+      cudaFree(partials_);
+      partials_ = np;
+      nparts_max_ = (int)projf_parts_;
+    }
+    return ST_OK;
+  }
+
+  // the last band pass of the spectral operator: axis 1 (3D) or the line axis (2D)
+  BandAxis spectral_proj_axis() const {
+    const long long n2h = g_.n2h;
+    if (g_.dim == 3) return BandAxis{gi_.n1, g_.n1, g_.n1, gi_.n1, gp_.h[1], n2h, g_.n0, g_.n0, 1, 0, 0};
+    return BandAxis{gi_.n1, g_.n1, g_.n1, gi_.n1, gp_.h[0], n2h, 1, 1, 0, 0, 0};
+  }
+
+  // field (plan precision, real) -> z form of its half spectrum
+  int to_z(const R* field, cplx<R>* z, cudaStream_t s) {
+    int st = forward_spectrum(field, S_, s);
+    if (st != ST_OK) return st;
+    const size_t nz = (size_t)g_.L * g_.dv * g_.n0 * g_.n1 * g_.n2h;
+    k_half_weight<R><<<grid_for(nz), kThreads, 0, s>>>(S_, z, (long long)nz, g_.n2h, g_.n2,
+                                                       1.0 / (double)g_.M, 1);
+    FHP_LAUNCHED();
+    return ST_OK;
+  }
+
+  // z form -> real field
+  int from_z(const cplx<R>* z, R* field, cudaStream_t s) {
+    const size_t nz = (size_t)g_.L * g_.dv * g_.n0 * g_.n1 * g_.n2h;
+    k_half_weight<R><<<grid_for(nz), kThreads, 0, s>>>(z, S_, (long long)nz, g_.n2h, g_.n2, 1.0,
+                                                       0);
+    FHP_LAUNCHED();
+    return inverse_spectrum(S_, field, 1.0, s);
+  }
+
+  // z <- G z (orthogonal projection onto range(G), unit scale)
+  int spec_green(cplx<R>* z, cudaStream_t s) {
+    GreenParams gpo = gp_;
+    gpo.scale = 1.0;
+    const size_t nf = (size_t)g_.L * g_.n0 * g_.n1 * g_.n2h;
+    if (gp_.physics == 0) k_spec_green<R, 0><<<grid_for(nf), kThreads, 0, s>>>(z, g_, gpo);
+    else k_spec_green<R, 1><<<grid_for(nf), kThreads, 0, s>>>(z, g_, gpo);
+    FHP_LAUNCHED();
+    return ST_OK;
+  }
+
+  // zap = G A p in z form, p = r + beta p first (all in the spectral buffers),
+  // partial <p, Ap> per CTA of the last pass
+  int spectral_operator(const cplx<R>* zr, cplx<R>* zp, cplx<R>* zap, cudaStream_t s) {
+    int st;
+    const long long n2h = g_.n2h;
+    cplx<R>* SA = S_;
+    cplx<R>* SB = SB_;
+    cplx<R>* Sbig;
+    if (g_.dim == 3) {
+      BandAxis a0{g_.n0, gi_.n0, g_.n0, gi_.n0, gp_.h[0], (long long)g_.n1 * n2h, 1, 1, 2,
+                  (int)n2h, g_.n1};
+      if ((st = band_axis(BAND_PAD_PUPD, zr, SB, a0, lb0_.dev, lb0_.dev, true, s,
+                          "band_pad_pupd_axis0", zp)) != ST_OK) return st;
+      BandAxis a1{g_.n1, gi_.n1, g_.n1, gi_.n1, gp_.h[1], n2h, gi_.n0, g_.n0, 1, 0, 0};
+      if ((st = band_axis(BAND_PAD, SB, SA, a1, lb1_.dev, lb1_.dev, true, s,
+                          "band_pad_axis1")) != ST_OK) return st;
+      Sbig = SA;
+    } else {
+      BandAxis a1{g_.n1, gi_.n1, g_.n1, gi_.n1, gp_.h[0], n2h, 1, 1, 0, 0, 0};
+      if ((st = band_axis(BAND_PAD_PUPD, zr, SB, a1, lb1_.dev, lb1_.dev, true, s,
+                          "band_pad_pupd_axis0", zp)) != ST_OK) return st;
+      Sbig = SB;
+    }
+    // the z-form input carries 1 / prod(N) already: unit coefficient scale
+    if ((st = band_last_pass(coef_kind_, Sbig, (R)1, true, s)) != ST_OK) return st;
+    if (g_.dim == 3) {
+      BandAxis a0{gi_.n0, g_.n0, g_.n0, gi_.n0, gp_.h[0], (long long)gi_.n1 * n2h, 1, 1, 2, 0, 0};
+      if ((st = band_axis(BAND_DOWN, SA, SB, a0, lb0_.dev, l0_.dev, true, s,
+                          "band_down_axis0")) != ST_OK) return st;
+    }
+    return band_axis(BAND_DOWN_PROJ_F, SB, zap, spectral_proj_axis(), lb1_.dev, l1_.dev, true, s,
+                     "band_projf_axis1", zp, partials_);
+  }
+
+  int spectral_iteration(cplx<R>* zx, cplx<R>* zr, cplx<R>* zp, cplx<R>* zap, double* dlog,
+                         int log_rows, cudaStream_t s) {
+    int st = spectral_operator(zr, zp, zap, s);
+    if (st != ST_OK) return st;
+    k_fin_pap<<<g_.L, kThreads, 0, s>>>(partials_, (int)projf_parts_, st_, g_.L, 1.0, all_done_);
+    FHP_LAUNCHED();
+    const int C = g_.L * g_.dv;
+    const int ux = std::max(1, red_ctas_ / C);
+    const int pk = pbeg("cg_update_spectral", 6.0 * (double)C * gz_.M * sizeof(R), s);
+    k_cg_update_comp<R><<<dim3((unsigned)ux, (unsigned)C), kThreads, 0, s>>>(
+        reinterpret_cast<R*>(zx), reinterpret_cast<R*>(zr), reinterpret_cast<const R*>(zp),
+        reinterpret_cast<const R*>(zap), partials_, gz_, st_, all_done_);
+    pend(pk, s);
+    FHP_LAUNCHED();
+    k_fin_rr<<<g_.L, kThreads, 0, s>>>(partials_, ux * C, st_, g_.L, 1.0, dlog, log_rows,
+                                       all_done_);
+    FHP_LAUNCHED();
+    k_update_all_done<<<1, 1, 0, s>>>(st_, g_.L, all_done_);
+    FHP_LAUNCHED();
+    return ST_OK;
+  }
+
+  int spectral_cg_solve(int proj, const R* b, const R* x0, double tol, int maxiter, R* x,
+                        SolveResult& res, int log_cap, cudaStream_t s) {
+    int st = ensure_spectral();
+    if (st != ST_OK) return st;
+    const size_t n = (size_t)g_.L * g_.dv * g_.M;
+    const size_t nz = (size_t)g_.L * g_.dv * g_.n0 * g_.n1 * g_.n2h;
+    cplx<R>* zx = zb_;
+    cplx<R>* zr = zb_ + nz;
+    cplx<R>* zp = zb_ + 2 * nz;
+    cplx<R>* zap = zb_ + 3 * nz;
+    // x = x0 ; R = B - A x0 (solver.py:114-117), then both in z form, R
+    // projected onto range(G)
+    const R* rsrc = b;
+    if (x0) {
+      if ((st = ensure_cg_buffers()) != ST_OK) return st;
+      if ((st = apply_ex(proj, x0, ap_, s, true)) != ST_OK) return st;
+      FHP_CHECK(cudaMemcpyAsync(r_, b, n * sizeof(R), cudaMemcpyDeviceToDevice, s));
+      k_axpby<R><<<grid_for(n), kThreads, 0, s>>>((long long)n, -1.0, ap_, 1.0, r_);
+      FHP_LAUNCHED();
+      rsrc = r_;
+      if ((st = to_z(x0, zx, s)) != ST_OK) return st;
+      if ((st = spec_green(zx, s)) != ST_OK) return st;
+    } else {
+      FHP_CHECK(cudaMemsetAsync(zx, 0, nz * sizeof(cplx<R>), s));
+    }
+    if ((st = to_z(rsrc, zr, s)) != ST_OK) return st;
+    if ((st = spec_green(zr, s)) != ST_OK) return st;
+    FHP_CHECK(cudaMemcpyAsync(zp, zr, nz * sizeof(cplx<R>), cudaMemcpyDeviceToDevice, s));
+    for (int l = 0; l < g_.L; ++l) {
+      LoadState& h = h_st_[l];
+      std::memset(&h, 0, sizeof(LoadState));
+      h.tol = tol;
+      h.maxiter = maxiter;
+      h.guard = sizeof(R) == 4 ? 4.0 : 0.0;
+    }
+    FHP_CHECK(cudaMemcpyAsync(st_, h_st_, g_.L * sizeof(LoadState), cudaMemcpyHostToDevice, s));
+    FHP_CHECK(cudaMemsetAsync(all_done_, 0, sizeof(int), s));
+    const int log_rows = std::max(1, std::min(log_cap, maxiter + 1));
+    double* dlog =
+        static_cast<double*>(scratch(SCR_LOG, (size_t)log_rows * g_.L * sizeof(double)));
+    if (!dlog) return ST_OOM;
+    FHP_CHECK(cudaMemsetAsync(dlog, 0, (size_t)log_rows * g_.L * sizeof(double), s));
+    k_dot<R><<<red_ctas_, kThreads, 0, s>>>(reinterpret_cast<const R*>(zr),
+                                            reinterpret_cast<const R*>(zr), partials_, gz_);
+    FHP_LAUNCHED();
+    k_fin_init<<<1, 32, 0, s>>>(partials_, red_ctas_, st_, g_.L, 1.0, dlog, log_rows);
+    FHP_LAUNCHED();
+    k_update_all_done<<<1, 1, 0, s>>>(st_, g_.L, all_done_);
+    FHP_LAUNCHED();
+    st = iterate(maxiter, s, [&]() {
+      return spectral_iteration(zx, zr, zp, zap, dlog, log_rows, s);
+    });
+    if (st != ST_OK) return st;
+    // back to the caller's real field; FP32 iterates are projected first
+    // (roundoff of the updates outside range(G), see cg_solve)
+    if (sizeof(R) == 4 && (st = spec_green(zx, s)) != ST_OK) return st;
+    if ((st = from_z(zx, x, s)) != ST_OK) return st;
+    return collect(tol, log_rows, dlog, res, s);
   }
 
   // A_H[i][j] = <A u_i, u_j>, u_i = X_i (+ E_i)  (postprocess.py:53-70)
@@ -821,11 +1015,11 @@ class Engine final : public EngineBase {
   }
 
   int tile_cols(int nf, int lines_per_col, long long inner,
-                int target = kTargetElems) const {
+                int target = kTargetElems, size_t budget = kSmemBudget) const {
     const size_t per = (size_t)lines_per_col * nf * sizeof(cplx<R>);
     int T = std::max(1, target / (lines_per_col * nf));
     T = std::min(T, 32);
-    T = (int)std::min<size_t>(T, std::max<size_t>(1, kSmemBudget / per));
+    T = (int)std::min<size_t>(T, std::max<size_t>(1, budget / per));
     T = (int)std::min<long long>(T, inner);
     T = std::max(T, 1);
     while (T & (T - 1)) T &= T - 1;  // kernels index tiles with shifts: a power of two
@@ -926,6 +1120,9 @@ class Engine final : public EngineBase {
     FHP_ATTR((k_band_axis<R, BAND_DOWN_PROJ, 1>));
     FHP_ATTR((k_band_axis<R, BAND_UP_PROJ, 1>));
     FHP_ATTR((k_band_axis<R, BAND_PAD, 0>));
+    FHP_ATTR((k_band_axis<R, BAND_PAD_PUPD, 0>));
+    FHP_ATTR((k_band_axis<R, BAND_DOWN_PROJ_F, 0>));
+    FHP_ATTR((k_band_axis<R, BAND_DOWN_PROJ_F, 1>));
     FHP_ATTR((k_band_last<R, COEF_ISO>));
     FHP_ATTR((k_band_last<R, COEF_SYM>));
     FHP_ATTR((k_band_last<R, COEF_FULL>));
@@ -982,6 +1179,8 @@ class Engine final : public EngineBase {
     if (all_done_) cudaFree(all_done_);
     if (pe_) cudaFree(pe_);
     if (zx_) cudaFree(zx_);
+    if (zb_) cudaFree(zb_);
+    zb_ = nullptr;
     pe_ = nullptr;
     zx_ = nullptr;
     if (h_done_) cudaFreeHost(h_done_);
@@ -1073,27 +1272,55 @@ class Engine final : public EngineBase {
   }
 
   // ---- band representation (Ga on the solve grid, A on the integration grid) ----
-  int band_axis(int mode, const cplx<R>* in, cplx<R>* out, const BandAxis& ax_in,
-                const LineDev<R>& L1, const LineDev<R>& L2, bool cg, cudaStream_t s,
-                const char* name) {
-    BandAxis ax = ax_in;
-    set_band_divs(ax);
-    const bool projm = mode == BAND_DOWN_PROJ || mode == BAND_UP_PROJ;
+  // CTAs of a band pass (the partial-sum count of BAND_DOWN_PROJ_F)
+  long long band_axis_ctas(int mode, const BandAxis& ax, const LineDev<R>& L1,
+                           const LineDev<R>& L2) const {
+    const int T = band_axis_tile(mode, ax, L1, L2);
+    const bool projm = mode == BAND_DOWN_PROJ || mode == BAND_UP_PROJ || mode == BAND_DOWN_PROJ_F;
+    return ((ax.inner + T - 1) / T) * (long long)((projm ? g_.L : g_.L * g_.dv) * ax.mid);
+  }
+
+  int band_axis_tile(int mode, const BandAxis& ax, const LineDev<R>& L1,
+                     const LineDev<R>& L2) const {
+    const bool projm = mode == BAND_DOWN_PROJ || mode == BAND_UP_PROJ || mode == BAND_DOWN_PROJ_F;
+    const bool padin = mode == BAND_PAD || mode == BAND_PAD_PUPD;
     const int nlc = projm ? g_.dv : 1;
-    const int nf = (mode == BAND_PAD ? 0 : L1.ld) + (mode == BAND_DOWN ? 0 : L2.ld);
+    const int nf = (padin ? 0 : L1.ld) + ((mode == BAND_DOWN || mode == BAND_DOWN_PROJ_F) ? 0 : L2.ld);
     // twice the usual line target: the axis passes are bound by instruction
     // issue, and more columns per CTA fill the radix stages of every line
     // length (and lengthen the contiguous rows); the register file still
-    // allows two CTAs per SM
-    const int T = tile_cols(nf, nlc, ax.inner, 2 * kTargetElems);
+    // allows two CTAs per SM.  The spectral projection pass holds one line
+    // buffer per column, so its tile may use the integration pass's budget.
+    const size_t budget = (mode == BAND_DOWN_PROJ_F && sizeof(R) == 4) ? kBandLastBudget32
+                                                                        : kSmemBudget;
+    return tile_cols(nf, nlc, ax.inner, 2 * kTargetElems, budget);
+  }
+
+  int band_axis(int mode, const cplx<R>* in, cplx<R>* out, const BandAxis& ax_in,
+                const LineDev<R>& L1, const LineDev<R>& L2, bool cg, cudaStream_t s,
+                const char* name, cplx<R>* aux = nullptr, double* parts = nullptr) {
+    BandAxis ax = ax_in;
+    set_band_divs(ax);
+    const bool projm = mode == BAND_DOWN_PROJ || mode == BAND_UP_PROJ || mode == BAND_DOWN_PROJ_F;
+    const bool padin = mode == BAND_PAD || mode == BAND_PAD_PUPD;
+    const int nlc = projm ? g_.dv : 1;
+    const int nf = (padin ? 0 : L1.ld) + ((mode == BAND_DOWN || mode == BAND_DOWN_PROJ_F) ? 0 : L2.ld);
+    const int T = band_axis_tile(mode, ax, L1, L2);
     const size_t smem = (size_t)nlc * T * nf * sizeof(cplx<R>);
     if (smem > kSmemMax) { set_error("band line too long for shared memory"); return ST_BAD_ARG; }
     const int outer = projm ? g_.L : g_.L * g_.dv;
     dim3 grid((unsigned)((ax.inner + T - 1) / T), (unsigned)(outer * ax.mid));
     const int* ad = cg ? all_done_ : nullptr;
     const LoadState* st = cg ? st_ : nullptr;
-    const double bytes = (double)(g_.L * g_.dv) * ax.mid * ax.inner *
-                         (ax.n_in + ax.n_out) * sizeof(cplx<R>);
+    // algorithmic bytes: each input read once, each output written once; the
+    // direction update also reads r and rewrites p, the spectral projection
+    // reads p for <p, Ap>
+    double bytes = (double)(g_.L * g_.dv) * ax.mid * ax.inner *
+                   (ax.n_in + ax.n_out) * sizeof(cplx<R>);
+    if (mode == BAND_PAD_PUPD)
+      bytes += 2.0 * (g_.L * g_.dv) * ax.mid * ax.inner * ax.n_in * sizeof(cplx<R>);
+    if (mode == BAND_DOWN_PROJ_F && parts)
+      bytes += (double)(g_.L * g_.dv) * ax.mid * ax.inner * ax.n_out * sizeof(cplx<R>);
     // the input projection of G A G is the plain orthogonal projection (scale 1);
     // the output projection carries s / prod(B)
     GreenParams gpin = gp_;
@@ -1102,25 +1329,83 @@ class Engine final : public EngineBase {
     const int pk = pbeg(name, bytes, s);
     switch (mode) {
       case BAND_UP:
-        k_band_axis<R, BAND_UP, 0><<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st);
+        k_band_axis<R, BAND_UP, 0><<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st, nullptr, nullptr);
         break;
       case BAND_DOWN:
-        k_band_axis<R, BAND_DOWN, 0><<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st);
+        k_band_axis<R, BAND_DOWN, 0><<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st, nullptr, nullptr);
         break;
       case BAND_UP_PROJ: {
         auto k = scalar ? k_band_axis<R, BAND_UP_PROJ, 0> : k_band_axis<R, BAND_UP_PROJ, 1>;
-        k<<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gpin, ad, st);
+        k<<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gpin, ad, st, nullptr, nullptr);
         break;
       }
       case BAND_PAD:
-        k_band_axis<R, BAND_PAD, 0><<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st);
+        k_band_axis<R, BAND_PAD, 0><<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st, nullptr, nullptr);
         break;
+      case BAND_PAD_PUPD:
+        k_band_axis<R, BAND_PAD_PUPD, 0><<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st, aux, nullptr);
+        break;
+      case BAND_DOWN_PROJ_F: {
+        auto k = scalar ? k_band_axis<R, BAND_DOWN_PROJ_F, 0> : k_band_axis<R, BAND_DOWN_PROJ_F, 1>;
+        k<<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st, aux, parts);
+        break;
+      }
       default: {
         auto k = scalar ? k_band_axis<R, BAND_DOWN_PROJ, 0> : k_band_axis<R, BAND_DOWN_PROJ, 1>;
-        k<<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st);
+        k<<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st, nullptr, nullptr);
         break;
       }
     }
+    pend(pk, s);
+    FHP_LAUNCHED();
+    return ST_OK;
+  }
+
+  // last axis on the integration grid: c2r, q = a x cs, r2c, keep the band
+  // (in place in Sbig, all loads and comps)
+  int band_last_pass(int coef, cplx<R>* Sbig, R cs, bool cg, cudaStream_t s) {
+    const int* ad = cg ? all_done_ : nullptr;
+    const long long n2h = g_.n2h;
+    const long long nrows = (long long)gi_.n0 * gi_.n1;
+    const double b4 = 2.0 * (double)(g_.L * g_.dv) * nrows * n2h * sizeof(cplx<R>) + coef_bytes();
+    const int pk = pbeg("band_last_coef", b4, s);
+    // rows per CTA: the line target, reduced until lines + staged spectra +
+    // staged coefficient fit the per-CTA budget (2 CTAs/SM for FP32)
+    const int C = g_.L * g_.dv, np = (C + 1) / 2;
+    const int cA = coef == COEF_ISO ? 1 : coef == COEF_SYM ? g_.dv * (g_.dv + 1) / 2 : g_.dv * g_.dv;
+    const size_t budget = sizeof(R) == 4 ? kBandLastBudget32 : kBandLastBudget64;
+    // staging modes in order of preference: spectra and coefficient, spectra
+    // only, none (the lines alone always fit: checked at plan creation)
+    int rows = brows_, stage = 3;
+    auto smem_of = [&](int r, int stg) {
+      return band_last_smem_bytes<R>(r, np, lb2_.dev.ld, C, (int)n2h, cA, gi_.n2, stg);
+    };
+    for (stage = 3; stage > 0; stage = stage == 3 ? 1 : 0)
+      if (smem_of(1, stage) <= budget) break;
+    while (rows > 1 && smem_of(rows, stage) > budget) --rows;
+    const size_t smem = smem_of(rows, stage);
+    if (smem > kSmemMax) { set_error("integration line too long for shared memory"); return ST_BAD_ARG; }
+    const unsigned ctas = (unsigned)((nrows + rows - 1) / rows);
+    // direct power-of-two integration lines: compile-time stages and phases
+    const int lgb = lb2_.dev.blue ? 0 : lb2_.dev.lg2;
+#define FHP_BLARGS <<<ctas, kThreads, smem, s>>>(Sbig, A_, g_, nrows, (int)n2h, g_.n2, lb2_.dev, rows, cs, ad, stage)
+#define FHP_BL(C)                                                  \
+    switch (lgb) {                                               \
+      case 5: k_band_last_p2<R, C, 5> FHP_BLARGS; break;          \
+      case 6: k_band_last_p2<R, C, 6> FHP_BLARGS; break;          \
+      case 7: k_band_last_p2<R, C, 7> FHP_BLARGS; break;          \
+      case 8: k_band_last_p2<R, C, 8> FHP_BLARGS; break;          \
+      case 9: k_band_last_p2<R, C, 9> FHP_BLARGS; break;          \
+      case 10: k_band_last_p2<R, C, 10> FHP_BLARGS; break;        \
+      default: k_band_last<R, C> FHP_BLARGS; break;               \
+    }
+    switch (coef) {
+      case COEF_ISO: FHP_BL(COEF_ISO); break;
+      case COEF_SYM: FHP_BL(COEF_SYM); break;
+      default: FHP_BL(COEF_FULL); break;
+    }
+#undef FHP_BL
+#undef FHP_BLARGS
     pend(pk, s);
     FHP_LAUNCHED();
     return ST_OK;
@@ -1178,51 +1463,7 @@ class Engine final : public EngineBase {
       Sbig = SB;
     }
     // K4: last axis on the integration grid with the coefficient
-    {
-      const long long nrows = (long long)gi_.n0 * gi_.n1;
-      const R cs = (R)(1.0 / (double)g_.M);
-      const double b4 = 2.0 * (double)(g_.L * g_.dv) * nrows * n2h * sizeof(cplx<R>) + coef_bytes();
-      const int pk = pbeg("band_last_coef", b4, s);
-      // rows per CTA: the line target, reduced until lines + staged spectra +
-      // staged coefficient fit the per-CTA budget (2 CTAs/SM for FP32)
-      const int C = g_.L * g_.dv, np = (C + 1) / 2;
-      const int cA = coef == COEF_ISO ? 1 : coef == COEF_SYM ? g_.dv * (g_.dv + 1) / 2 : g_.dv * g_.dv;
-      const size_t budget = sizeof(R) == 4 ? kBandLastBudget32 : kBandLastBudget64;
-      // staging modes in order of preference: spectra and coefficient, spectra
-      // only, none (the lines alone always fit: checked at plan creation)
-      int rows = brows_, stage = 3;
-      auto smem_of = [&](int r, int stg) {
-        return band_last_smem_bytes<R>(r, np, lb2_.dev.ld, C, (int)n2h, cA, gi_.n2, stg);
-      };
-      for (stage = 3; stage > 0; stage = stage == 3 ? 1 : 0)
-        if (smem_of(1, stage) <= budget) break;
-      while (rows > 1 && smem_of(rows, stage) > budget) --rows;
-      const size_t smem = smem_of(rows, stage);
-      if (smem > kSmemMax) { set_error("integration line too long for shared memory"); return ST_BAD_ARG; }
-      const unsigned ctas = (unsigned)((nrows + rows - 1) / rows);
-      // direct power-of-two integration lines: compile-time stages and phases
-      const int lgb = lb2_.dev.blue ? 0 : lb2_.dev.lg2;
-#define FHP_BLARGS <<<ctas, kThreads, smem, s>>>(Sbig, A_, g_, nrows, (int)n2h, g_.n2, lb2_.dev, rows, cs, ad, stage)
-#define FHP_BL(C)                                                  \
-      switch (lgb) {                                               \
-        case 5: k_band_last_p2<R, C, 5> FHP_BLARGS; break;          \
-        case 6: k_band_last_p2<R, C, 6> FHP_BLARGS; break;          \
-        case 7: k_band_last_p2<R, C, 7> FHP_BLARGS; break;          \
-        case 8: k_band_last_p2<R, C, 8> FHP_BLARGS; break;          \
-        case 9: k_band_last_p2<R, C, 9> FHP_BLARGS; break;          \
-        case 10: k_band_last_p2<R, C, 10> FHP_BLARGS; break;        \
-        default: k_band_last<R, C> FHP_BLARGS; break;               \
-      }
-      switch (coef) {
-        case COEF_ISO: FHP_BL(COEF_ISO); break;
-        case COEF_SYM: FHP_BL(COEF_SYM); break;
-        default: FHP_BL(COEF_FULL); break;
-      }
-#undef FHP_BL
-#undef FHP_BLARGS
-      pend(pk, s);
-      FHP_LAUNCHED();
-    }
+    if ((st = band_last_pass(coef, Sbig, (R)(1.0 / (double)g_.M), cg, s)) != ST_OK) return st;
     if (d == 3) {
       BandAxis a0{gi_.n0, g_.n0, g_.n0, gi_.n0, gp_.h[0], (long long)gi_.n1 * n2h, 1, 1, 2, 0, 0};
       if ((st = band_axis(BAND_DOWN, SA, SB, a0, lb0_.dev, l0_.dev, cg, s, "band_down_axis0")) != ST_OK) return st;
@@ -1338,6 +1579,11 @@ class Engine final : public EngineBase {
   cplx<R>* SB_ = nullptr;
   int brows_ = 1, brow_ctas_ = 1;
   size_t bsmem_rows_ = 0;
+  // spectral CG of band plans
+  bool spectral_cg_ = true;
+  cplx<R>* zb_ = nullptr;      // z vectors x, r, p, Ap (half spectra of the N grid)
+  GridDims gz_{};              // the z vectors as real arrays: M = 2 n0 n1 n2h per comp
+  long long projf_parts_ = 0;  // partial sums of the spectral projection pass
 };
 
 }  // namespace fhp

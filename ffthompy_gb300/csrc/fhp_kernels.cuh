@@ -1046,7 +1046,12 @@ __global__ void k_ga_gather(const cplx<R>* __restrict__ Sp, cplx<R>* __restrict_
 // ---------------------------------------------------------------------------
 //   BAND_UP_PROJ   : space N  -> DFT_N -> G(xi) -> iDFT_B (band pad) -> space B
 //   BAND_PAD       : frequency (N layout) -> band pad -> iDFT_B -> space B
-enum BandMode { BAND_UP = 0, BAND_DOWN = 1, BAND_DOWN_PROJ = 2, BAND_UP_PROJ = 3, BAND_PAD = 4 };
+//   BAND_PAD_PUPD  : as BAND_PAD, the input being the CG direction of the
+//                    spectral iterates, updated first (p = r + beta p)
+//   BAND_DOWN_PROJ_F : space B -> DFT_B -> band -> G(xi) -> frequency (N
+//                    layout) of the spectral iterates, with the partial <p, Ap>
+enum BandMode { BAND_UP = 0, BAND_DOWN = 1, BAND_DOWN_PROJ = 2, BAND_UP_PROJ = 3, BAND_PAD = 4,
+                BAND_PAD_PUPD = 5, BAND_DOWN_PROJ_F = 6 };
 
 struct BandAxis {
   int n_in, n_out;     // line lengths in / out
@@ -1091,6 +1096,27 @@ __device__ __forceinline__ cplx<R> band_down_value(const cplx<R>* line, const Li
   return get_fwd<R>(line, L, q < 0 ? q + nb : q);
 }
 
+// Spectral CG iterates are half spectra scaled to z = sqrt(w) V / prod(N), w
+// the weight of the half-spectrum inner product (1 on the k2 = 0 plane and on
+// the Nyquist plane of an even n2, 2 elsewhere), so that the grid-mean inner
+// product of the fields is the Euclidean one of z.  Column col of a band pass
+// holds last-axis frequency k2 = col mod inner2 (inner2 = n2h; 0: k2 = col).
+template <typename R>
+__device__ __forceinline__ R half_weight_root(const BandAxis& ax, const GridDims& g, long long col,
+                                              bool inverse) {
+  int k2 = (int)col;
+  if (ax.inner2 > 0) k2 = (int)col - fdiv((int)col, ax.dinner2) * ax.inner2;
+  if (k2 == 0 || 2 * k2 == g.n2) return R(1);
+  return inverse ? R(0.70710678118654752440084436210485) : R(1.4142135623730950488016887242097);
+}
+
+// forward output slot of frequency k written so that get_fwd returns v
+template <typename R>
+__device__ __forceinline__ void set_fwd(cplx<R>* line, const LineDev<R>& L, int k, cplx<R> v) {
+  if (L.blue) line[sp(k)] = cmulc<R>(v, L.chirp[k]);
+  else line[sp(L.pos[k])] = v;
+}
+
 // Visits every (tile line c < nlc, line index k < n, column t < T) of a
 // column tile once.  When T divides the block, a thread keeps one column t and
 // walks k with a fixed stride, so no index is divided per element and the
@@ -1112,25 +1138,37 @@ __device__ __forceinline__ void tile_loop(int nlc, int n, int T, int lgT, F&& bo
   }
 }
 
+// aux: BAND_PAD_PUPD the CG direction p (read and updated in place, Sin = r);
+// BAND_DOWN_PROJ_F the direction p read for the partial <p, Ap>, written to
+// partials[(blockIdx.y * gridDim.x + blockIdx.x) * L + l] (zero for l other
+// than the CTA's load) when partials is not null.
 template <typename R, int MODE, int PHYS>
 __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_axis(const cplx<R>* __restrict__ Sin,
                                                    cplx<R>* __restrict__ Sout, const __grid_constant__ GridDims g,
                                                    const __grid_constant__ BandAxis ax, const __grid_constant__ LineDev<R> L1, const __grid_constant__ LineDev<R> L2,
                                                    int T, const __grid_constant__ GreenParams gp,
                                                    const int* __restrict__ all_done,
-                                                   const LoadState* __restrict__ st) {
+                                                   const LoadState* __restrict__ st,
+                                                   cplx<R>* __restrict__ aux,
+                                                   double* __restrict__ partials) {
   if (all_done && *all_done) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr bool PROJ = (MODE == BAND_DOWN_PROJ || MODE == BAND_UP_PROJ);
+  constexpr bool PROJ = (MODE == BAND_DOWN_PROJ || MODE == BAND_UP_PROJ ||
+                         MODE == BAND_DOWN_PROJ_F);
+  constexpr bool PADIN = (MODE == BAND_PAD || MODE == BAND_PAD_PUPD);
   const int nlc = PROJ ? g.dv : 1;   // comps per CTA
   // blockIdx.y: (comp or load) * mid + m
   const int m = blockIdx.y % ax.mid;
   const int cl = blockIdx.y / ax.mid;
   const int c0 = PROJ ? cl * g.dv : cl;
   const int load = c0 / g.dv;
-  if (st && st[load].done) return;
-  const int ld1 = (MODE == BAND_PAD) ? 0 : L1.ld;
-  const int ld2 = (MODE == BAND_DOWN) ? 0 : L2.ld;
+  if (st && st[load].done) {
+    if (MODE == BAND_DOWN_PROJ_F && partials && threadIdx.x < g.L)
+      partials[((long long)blockIdx.y * gridDim.x + blockIdx.x) * g.L + threadIdx.x] = 0.;
+    return;
+  }
+  const int ld1 = PADIN ? 0 : L1.ld;
+  const int ld2 = (MODE == BAND_DOWN || MODE == BAND_DOWN_PROJ_F) ? 0 : L2.ld;
   cplx<R>* buf1 = reinterpret_cast<cplx<R>*>(smem_raw);
   cplx<R>* buf2 = buf1 + (size_t)nlc * T * ld1;
   const long long t0 = (long long)blockIdx.x * T;
@@ -1139,9 +1177,9 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_axis(const cplx<
   // band-pruned power-of-two B lines (line_prunable): the up / pad inverse
   // transforms see at most |q| <= n_in/2 nonzero, the down forward transforms
   // are read at |q| <= n_out/2 only; zeros on the pruned digits are not written
-  const bool pr2 = (MODE == BAND_UP || MODE == BAND_UP_PROJ || MODE == BAND_PAD) &&
+  const bool pr2 = (MODE == BAND_UP || MODE == BAND_UP_PROJ || PADIN) &&
                    line_prunable<R>(L2, ax.n_in / 2);
-  const bool pr1 = (MODE == BAND_DOWN || MODE == BAND_DOWN_PROJ) &&
+  const bool pr1 = (MODE == BAND_DOWN || MODE == BAND_DOWN_PROJ || MODE == BAND_DOWN_PROJ_F) &&
                    line_prunable<R>(L1, ax.n_out / 2);
   const int pq0 = L2.nf / 4, pq1 = 3 * (L2.nf / 4);  // pruned range of the B line (pr2)
   if constexpr (MODE == BAND_PAD) {
@@ -1165,6 +1203,29 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_axis(const cplx<
     });
     cp_async_commit();
     cp_async_wait<0>();
+  } else if constexpr (MODE == BAND_PAD_PUPD) {
+    // p = r + beta p on the spectral iterates (Sin = r, aux = p, N layout,
+    // updated in place), then p / sqrt(w) padded into the B line.  Entries
+    // with 2|q| = n_in (the Nyquist index of an even n_in) are zero on
+    // range(G), where the iterates live, and stay untouched.
+    const R bet = R(st[load].beta);
+    tile_loop(1, ax.n_out, T, lgT, [&](int, int k, int t) {
+      if (pr2 && k >= pq0 && k < pq1) return;
+      const long long col = t0 + t;
+      const int q = signed_freq(k, ax.n_out);
+      const int aq = q < 0 ? -q : q;
+      cplx<R> v = mkc<R>(R(0), R(0));
+      if (col < ax.inner && 2 * aq < ax.n_in) {
+        const long long idx = (((long long)c0 * ax.mid + m) * ax.n_in +
+                               (q < 0 ? q + ax.n_in : q)) * ax.inner + col;
+        const cplx<R> r = Sin[idx];
+        cplx<R> p = aux[idx];
+        p = mkc<R>(r.x + bet * p.x, r.y + bet * p.y);
+        aux[idx] = p;
+        v = cscale<R>(p, half_weight_root<R>(ax, g, col, true));
+      }
+      buf2[t * ld2 + slot_inv<R>(L2, k)] = v;
+    });
   } else {
     // load: [comp][mid][n_in][inner]
     tile_loop(nlc, ax.n_in, T, lgT, [&](int c, int i, int t) {
@@ -1225,7 +1286,7 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_axis(const cplx<
       });
     }
   }
-  if constexpr (MODE == BAND_UP || MODE == BAND_UP_PROJ || MODE == BAND_PAD) {
+  if constexpr (MODE == BAND_UP || MODE == BAND_UP_PROJ || PADIN) {
     if constexpr (MODE == BAND_UP) {
     tile_loop(nlc, ax.n_out, T, lgT, [&](int c, int k, int t) {
       if (pr2 && k >= pq0 && k < pq1) return;
@@ -1242,7 +1303,7 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_axis(const cplx<
     });
     }
     __syncthreads();
-    if constexpr (MODE == BAND_PAD) blue_fixup<R, true>(buf2, ld2, nl, L2);
+    if constexpr (PADIN) blue_fixup<R, true>(buf2, ld2, nl, L2);
     zero_tail<R>(buf2, ld2, nl, L2);
     __syncthreads();
     line_core<R>(buf2, ld2, nl, L2, true, pr2);
@@ -1260,6 +1321,58 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_axis(const cplx<
       cplx<R>* dst = Sout + (((long long)(c0 + c) * ax.mid + m) * ax.n_out) * ax.inner + col;
       dst[(long long)k * ax.inner] = v;
     });
+  } else if constexpr (MODE == BAND_DOWN_PROJ_F) {
+    // G(xi) on the band, written back in place into the B-line slot of each
+    // N frequency (lanes over the frequencies of one column)
+    for (int t = 0; t < T; ++t)
+    for (int k = threadIdx.x; k < ax.n_out; k += blockDim.x) {
+      const long long col = t0 + t;
+      const int q = signed_freq(k, ax.n_out);
+      cplx<R> x[kMaxDv];
+#pragma unroll
+      for (int c = 0; c < kMaxDv; ++c)
+        if (c < g.dv) x[c] = band_down_value<R>(buf1 + (c * T + t) * ld1, L1, k, ax.n_out, ax.n_in);
+      if (col < ax.inner) {
+        int kv[3];
+        band_freqs(ax, g.dim, q, m, col, kv);
+        green_apply<R, PHYS>(gp, g.dim, kv, x);
+      }
+      const int kb = q < 0 ? q + ax.n_in : q;
+#pragma unroll
+      for (int c = 0; c < kMaxDv; ++c)
+        if (c < g.dv) set_fwd<R>(buf1 + (c * T + t) * ld1, L1, kb, x[c]);
+    }
+    __syncthreads();
+    // rows of T columns to global (z form: times sqrt(w)), with <p, Ap>
+    R dot = R(0);
+    tile_loop(nlc, ax.n_out, T, lgT, [&](int c, int k, int t) {
+      const long long col = t0 + t;
+      if (col >= ax.inner) return;
+      const int q = signed_freq(k, ax.n_out);
+      cplx<R> v = get_fwd<R>(buf1 + (c * T + t) * ld1, L1, q < 0 ? q + ax.n_in : q);
+      v = cscale<R>(v, half_weight_root<R>(ax, g, col, false));
+      const long long idx = (((long long)(c0 + c) * ax.mid + m) * ax.n_out + k) * ax.inner + col;
+      Sout[idx] = v;
+      if (partials) {
+        const cplx<R> p = aux[idx];
+        dot += p.x * v.x + p.y * v.y;
+      }
+    });
+    if (partials) {
+      // the line buffers are read: their first bytes take the warp sums (no
+      // static shared memory, so the whole dynamic allowance stays usable)
+      __syncthreads();
+      double* red = reinterpret_cast<double*>(smem_raw);
+      const double tsum = warp_sum((double)dot);
+      if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = tsum;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double tot = 0.;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
+        double* out = partials + ((long long)blockIdx.y * gridDim.x + blockIdx.x) * g.L;
+        for (int l = 0; l < g.L; ++l) out[l] = l == load ? tot : 0.;
+      }
+    }
   } else {
     // G(xi) on the band, then inverse DFT_N along the line (lanes over the
     // frequencies of one column, as in the up projection)
@@ -1962,6 +2075,57 @@ __global__ void k_p_update(const R* __restrict__ r, R* __restrict__ p, GridDims 
     const int l = (int)(i / per);
     if (st[l].done) continue;
     p[i] = r[i] + (R)st[l].beta * p[i];
+  }
+}
+
+// Spectral CG iterates of band plans: half spectra V (N layout
+// [C][n0][n1][n2h]) and their z form z = sqrt(w) V f (to_z) or V = z f /
+// sqrt(w) (from z), w the half-spectrum weight of the last-axis frequency.
+template <typename R>
+__global__ void k_half_weight(const cplx<R>* __restrict__ in, cplx<R>* __restrict__ out,
+                              long long tot, int n2h, int n2, double f, int to_z) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += stride) {
+    const int k2 = (int)(e % n2h);
+    const bool single = k2 == 0 || 2 * k2 == n2;
+    const double w = single ? 1.0 : (to_z ? 1.4142135623730950488016887242097
+                                          : 0.70710678118654752440084436210485);
+    const double fw = f * w;
+    const cplx<R> u = in[e];
+    out[e] = mkc<R>((R)(fw * (double)u.x), (R)(fw * (double)u.y));
+  }
+}
+
+// z <- G(xi) z at every frequency of half spectra in the N layout, all loads
+// (the orthogonal projection: gp.scale 1; zero outside the band)
+template <typename R, int PHYS>
+__global__ void k_spec_green(cplx<R>* __restrict__ z, GridDims g, GreenParams gp) {
+  const long long F = (long long)g.n0 * g.n1 * g.n2h;
+  const long long tot = (long long)g.L * F;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += stride) {
+    const int l = (int)(e / F);
+    const long long f = e - (long long)l * F;
+    const int k2 = (int)(f % g.n2h);
+    const long long r = f / g.n2h;
+    const int i1 = (int)(r % g.n1), i0 = (int)(r / g.n1);
+    int kv[3];
+    if (g.dim == 3) {
+      kv[0] = signed_freq(i0, g.n0);
+      kv[1] = signed_freq(i1, g.n1);
+      kv[2] = k2;
+    } else {
+      kv[0] = signed_freq(i1, g.n1);
+      kv[1] = k2;
+    }
+    cplx<R> x[kMaxDv];
+#pragma unroll
+    for (int c = 0; c < kMaxDv; ++c)
+      if (c < g.dv) x[c] = z[((long long)l * g.dv + c) * F + f];
+    green_apply<R, PHYS>(gp, g.dim, kv, x);
+#pragma unroll
+    for (int c = 0; c < kMaxDv; ++c)
+      if (c < g.dv) z[((long long)l * g.dv + c) * F + f] = x[c];
   }
 }
 

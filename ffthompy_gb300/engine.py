@@ -86,10 +86,12 @@ class GalerkinPlan:
     iterative refinement).
     integ: band representation of Ga - fields on N, coefficient on the
     integration grid integ >= 2N-1, projection scale prod(2N-1)/prod(N).
+    band_cg (band plans): 'spectral' keeps the CG iterates as half spectra of
+    N (no transform of the N grid inside an iteration), 'real' as real fields.
     """
 
     def __init__(self, N, Y, physics='scalar', nloads=None, band=None, scale=None,
-                 precision='f64', integ=None):
+                 precision='f64', integ=None, band_cg='spectral'):
         require_cuda()
         self.lib = _lib.load()
         self.N = tuple(int(n) for n in N)
@@ -130,6 +132,11 @@ class GalerkinPlan:
                        'fhp_plan_create')
         self.handle = h
         self.coef_kind = None
+        if band_cg not in ('spectral', 'real'):
+            raise ValueError("band_cg must be 'spectral' or 'real'")
+        self.band_cg = band_cg
+        _lib.check(self.lib.fhp_plan_set_band_cg(h, 1 if band_cg == 'spectral' else 0),
+                   'fhp_plan_set_band_cg')
 
     def __del__(self):
         h = getattr(self, 'handle', None)

@@ -73,6 +73,18 @@ int fhp_plan_create(fhp_plan* out, int dim, const int* n, const int* n_band, con
 int fhp_plan_create_band(fhp_plan* out, int dim, const int* n, const int* n_int,
                          const double* Y, int physics, int nloads, double g_scale,
                          int precision);
+/*
+ * Band plans: how CG stores its iterates.  spectral = 1 (default): as half
+ * spectra of the solve grid, so an iteration runs the operator from the pad
+ * to the integration grid to the band projection with no transform on the
+ * solve grid; spectral = 0: as real fields of the solve grid, with forward
+ * and inverse transforms of the solve grid in every iteration.  The same CG
+ * recursion on the same operator (inner products by Parseval), so iterates
+ * and stopping tests agree up to roundoff.  Other plans ignore the setting.
+ * No counterpart in the reference (its CG iterates are real fields,
+ * ffthompy/general/solver.py:80-139).
+ */
+int fhp_plan_set_band_cg(fhp_plan plan, int spectral);
 int fhp_plan_destroy(fhp_plan plan);
 /* FHP_MIXED plans: inner relative tolerance floor eta (default 1e-4) and the
    maximum number of refinement steps (default 30). */

@@ -576,3 +576,58 @@ def test_cg_graph_replay_equals_direct_launches(precision):
     assert out['default'][1] == out['side'][1]
     np.testing.assert_array_equal(out['default'][0], out['side'][0])
     np.testing.assert_array_equal(out['default'][2], out['side'][2])
+
+
+@pytest.mark.parametrize('N,physics', [((7, 7, 7), 'scalar'), ((6, 5, 8), 'scalar'),
+                                       ((15, 15), 'scalar'), ((8, 9), 'scalar'),
+                                       ((5, 5, 5), 'elasticity'), ((9, 7), 'elasticity')])
+@pytest.mark.parametrize('precision', ['f64', 'f32', 'mixed'])
+def test_band_spectral_cg_equals_real_cg(N, physics, precision):
+    """Band plans keep the CG iterates as half spectra of the solve grid
+    (band_cg='spectral', the default) or as real fields ('real'): the same
+    recursion on the same operator with inner products equal by Parseval, so
+    the iteration counts agree (band rule: within 3 % or 1) and so do the
+    solutions and A_H (FP64 1e-10; FP32 / mixed at their precision).  Covers
+    odd and even grids, 2D and 3D, scalar and elasticity, and a start x0."""
+    from ffthompy_gb300.engine import GalerkinPlan, nice_size
+    N = np.asarray(N)
+    d = N.size
+    rng = np.random.default_rng(int(np.prod(N)) + d)
+    dv = d if physics == 'scalar' else d * (d + 1) // 2
+    Ns = 2 * N - 1
+    if physics == 'scalar':
+        a = 1. + 20. * (rng.random(tuple(Ns)) < 0.4)
+        A = np.einsum('ij,...->ij...', np.eye(dv), a)
+    else:
+        C1 = oracle.mandel_isotropic(1., 0.5, d)
+        C2 = oracle.mandel_isotropic(10., 3., d)
+        m = rng.random(tuple(Ns)) < 0.4
+        A = np.einsum('ij,...->ij...', C1, ~m) + np.einsum('ij,...->ij...', C2, m)
+    integ = tuple(nice_size(n) for n in Ns)
+    A = _project_comps(A, integ)
+    out = {}
+    for mode in ('spectral', 'real'):
+        plan = GalerkinPlan(tuple(N), np.ones(d), physics=physics, integ=integ,
+                            precision=precision, band_cg=mode)
+        plan.set_coefficient(A)
+        B = plan.rhs_macro(1)
+        # FP32 fields: a tolerance above the precision floor of the real-field
+        # iterates (whose FFT roundoff stagnates CG near 1e-6 here)
+        tol = 1e-4 if precision == 'f32' else 1e-9
+        X, info = plan.cg(B, tol=tol, maxiter=500)
+        X0 = 0.5 * X
+        X2, info2 = plan.cg(B, x0=X0, tol=tol, maxiter=500)
+        out[mode] = (info, plan.energy(X), X.double().cpu().numpy(), info2,
+                     plan.energy(X2))
+        print(mode, precision, info['kit'], info['status'], info2['kit'])
+    (i_s, AH_s, X_s, i2_s, AH2_s), (i_r, AH_r, X_r, i2_r, AH2_r) = out['spectral'], out['real']
+    close = lambda a, b: all(abs(p - q) <= max(1, int(np.ceil(0.03 * q))) for p, q in zip(a, b))
+    assert all(s == 0 for s in i_s['status']), i_s['status']
+    assert all(s == 0 for s in i_r['status']), i_r['status']
+    assert close(i_s['kit'], i_r['kit']), (i_s['kit'], i_r['kit'])
+    assert close(i2_s['kit'], i2_r['kit']), (i2_s['kit'], i2_r['kit'])
+    tolAH = 1e-10 if precision != 'f32' else 1e-5
+    assert _relmax(AH_s, AH_r) < tolAH, _relmax(AH_s, AH_r)
+    assert _relmax(AH2_s, AH2_r) < tolAH, _relmax(AH2_s, AH2_r)
+    tolX = 1e-7 if precision != 'f32' else 1e-2
+    assert _relmax(X_s, X_r) < tolX, _relmax(X_s, X_r)
