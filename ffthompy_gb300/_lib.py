@@ -35,6 +35,22 @@ SIGNATURES = {
     'fhp_plan_destroy': (ctypes.c_int, [_vp]),
     'fhp_plan_set_refinement': (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_int]),
     'fhp_plan_set_band_cg': (ctypes.c_int, [_vp, ctypes.c_int]),
+    'fhp_cg_solve_many': (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_vp), ctypes.c_int,
+                                          ctypes.POINTER(_vp), ctypes.c_double, ctypes.c_int,
+                                          ctypes.POINTER(_vp), _c_int_p, _c_double_p, _c_int_p,
+                                          _vp]),
+    'fhp_plan_set_integration_kernel': (ctypes.c_int, [_vp, ctypes.c_int]),
+    'fhp_separable_char': (ctypes.c_int, [ctypes.c_int, _c_int_p, _c_double_p, _c_double_p, _vp,
+                                          _vp]),
+    'fhp_plan_autotune': (ctypes.c_int, [_vp, _c_int_p, ctypes.POINTER(ctypes.c_float), _vp]),
+    'fhp_richardson_solve': (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, ctypes.c_double,
+                                            ctypes.c_double, ctypes.c_int, _vp, _c_int_p,
+                                            _c_double_p, _c_int_p, _vp]),
+    'fhp_chebyshev_solve': (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, ctypes.c_double,
+                                           ctypes.c_double, ctypes.c_double, ctypes.c_int, _vp,
+                                           _c_int_p, _c_double_p, _c_int_p, _vp]),
+    'fhp_bicg_solve': (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, ctypes.c_double, ctypes.c_int,
+                                      _vp, _c_int_p, _c_double_p, _c_int_p, _vp]),
     'fhp_plan_query': (ctypes.c_int, [_vp, _c_ll_p, _c_int_p, _c_int_p, _c_int_p]),
     'fhp_set_coefficient': (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_int, _vp]),
     'fhp_apply': (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp]),

@@ -128,6 +128,304 @@ int cg_mixed(fhp_plan_s& p, int proj, const void* b, const void* x0, double tol,
   return st;
 }
 
+// done[i] = *flags[i] for the plans of the current graph, all_done = AND
+__global__ void k_gather_done(const int* const* __restrict__ flags, const int* __restrict__ idx,
+                              int n, int* __restrict__ done, int* all_done) {
+  int d = 1;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int v = *flags[idx[i]];
+    done[i] = v;
+    d &= v;
+  }
+  d = __syncthreads_and(d);
+  if (threadIdx.x == 0) *all_done = d;
+}
+
+// Several plans' CG solves advanced together (fhp_cg_solve_many).  Each plan
+// keeps its own loads, scalars and stopping tests (cg_begin / cg_end).  One
+// iteration of each plan is captured once as its own graph; the iteration of
+// the ensemble is a graph whose nodes are these child graphs of the plans
+// still running, all independent (the GPU runs them side by side), followed
+// by one kernel that gathers the plans' done flags.  The host reads them every
+// few iterations and, once a quarter of the graph's plans have stopped,
+// assembles a new graph of the running ones (a stopped plan's kernels would
+// still be launched, only to return).  Without graph capture (profiling on,
+// or a refused capture) the running plans' iterations are launched directly.
+int cg_many(const std::vector<fhp::EngineBase*>& engs, int proj, const std::vector<const void*>& b,
+            const std::vector<double>& tol, int maxiter, const std::vector<void*>& x,
+            std::vector<fhp::SolveResult>& res, cudaStream_t s) {
+  const int n = (int)engs.size();
+  res.assign(n, fhp::SolveResult());
+  if (n == 0) return FHP_OK;
+  int st = FHP_OK;
+  for (int i = 0; i < n && st == FHP_OK; ++i)
+    st = engs[i]->cg_begin(proj, b[i], nullptr, tol[i], maxiter, x[i], 1, s);
+  if (st != FHP_OK) return st;
+  std::vector<const int*> hflags(n);
+  bool prof = false;
+  for (int i = 0; i < n; ++i) {
+    hflags[i] = engs[i]->cg_done_flag();
+    prof = prof || engs[i]->prof.on;
+  }
+  const int** dflags = nullptr;
+  int *didx = nullptr, *ddone = nullptr, *hdone = nullptr;
+  std::vector<cudaGraph_t> child(n, nullptr);
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  std::vector<long long> per_iter(n, 0);
+  auto drop_graph = [&]() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (graph) cudaGraphDestroy(graph);
+    gexec = nullptr;
+    graph = nullptr;
+  };
+  auto cleanup = [&]() {
+    drop_graph();
+    for (cudaGraph_t c : child)
+      if (c) cudaGraphDestroy(c);
+    if (dflags) cudaFreeAsync(dflags, s);
+    if (didx) cudaFreeAsync(didx, s);
+    if (ddone) cudaFreeAsync(ddone, s);
+    if (hdone) cudaFreeHost(hdone);
+  };
+  // running plans (indices into engs); ddone[0..m) their flags, ddone[n] the AND
+  std::vector<int> run(n);
+  for (int i = 0; i < n; ++i) run[i] = i;
+  st = cuda_status(cudaMallocAsync((void**)&dflags, n * sizeof(int*), s), "alloc");
+  if (st == FHP_OK) st = cuda_status(cudaMallocAsync((void**)&didx, n * sizeof(int), s), "alloc");
+  if (st == FHP_OK)
+    st = cuda_status(cudaMallocAsync((void**)&ddone, (n + 1) * sizeof(int), s), "alloc");
+  if (st == FHP_OK) st = cuda_status(cudaMallocHost((void**)&hdone, (n + 1) * sizeof(int)), "alloc");
+  if (st == FHP_OK)
+    st = cuda_status(cudaMemcpyAsync(dflags, hflags.data(), n * sizeof(int*),
+                                     cudaMemcpyHostToDevice, s), "copy");
+  // the host vector must outlive the copy from pageable memory
+  if (st == FHP_OK) st = cuda_status(cudaStreamSynchronize(s), "sync");
+  if (st != FHP_OK) { cleanup(); return st; }
+  // one iteration of every plan as its own graph
+  bool use_graph = !prof && maxiter > 0;
+  for (int i = 0; i < n && use_graph && st == FHP_OK; ++i) {
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      use_graph = false;
+      break;
+    }
+    const long long l0 = engs[i]->launches;
+    const int cst = engs[i]->cg_step(s);
+    per_iter[i] = engs[i]->launches - l0;
+    engs[i]->launches = l0;
+    const cudaError_t e = cudaStreamEndCapture(s, &child[i]);
+    if (cst != FHP_OK) st = cst;
+    if (e != cudaSuccess || !child[i]) use_graph = false;
+  }
+  (void)cudaGetLastError();  // a refused capture leaves no error behind
+  if (st != FHP_OK) { cleanup(); return st; }
+  // the ensemble's iteration: the running plans' graphs, then the gather
+  int gm = 0;
+  auto build_graph = [&]() {
+    drop_graph();
+    if (!use_graph) return;
+    bool ok = cudaGraphCreate(&graph, 0) == cudaSuccess;
+    std::vector<cudaGraphNode_t> nodes(run.size());
+    for (size_t j = 0; j < run.size() && ok; ++j)
+      ok = cudaGraphAddChildGraphNode(&nodes[j], graph, nullptr, 0, child[run[j]]) == cudaSuccess;
+    gm = (int)run.size();
+    int* dall = ddone + n;
+    void* args[] = {(void*)&dflags, (void*)&didx, (void*)&gm, (void*)&ddone, (void*)&dall};
+    cudaKernelNodeParams kp = {};
+    kp.func = (void*)k_gather_done;
+    kp.gridDim = dim3(1);
+    kp.blockDim = dim3(256);
+    kp.sharedMemBytes = 0;
+    kp.kernelParams = args;
+    cudaGraphNode_t kn;
+    if (ok) ok = cudaGraphAddKernelNode(&kn, graph, nodes.data(), nodes.size(), &kp) == cudaSuccess;
+    if (ok) ok = cudaGraphInstantiate(&gexec, graph, 0) == cudaSuccess;
+    if (!ok) {
+      drop_graph();
+      use_graph = false;
+    }
+    (void)cudaGetLastError();
+  };
+  auto upload_run = [&]() {
+    int r = cuda_status(cudaMemcpyAsync(didx, run.data(), run.size() * sizeof(int),
+                                        cudaMemcpyHostToDevice, s), "copy");
+    if (r == FHP_OK) r = cuda_status(cudaStreamSynchronize(s), "sync");
+    return r;
+  };
+  st = upload_run();
+  if (st == FHP_OK) build_graph();
+  std::vector<int> gset = run;   // the plans of the graph, in the order of its done flags
+  int done_iters = 0, chunk = 2;
+  bool first = true;
+  while (st == FHP_OK && done_iters < maxiter) {
+    // the done flags of the graph's plans (refreshed by its last node), or
+    // gathered here for direct launches and before the first iteration
+    const bool gathered_here = first || !gexec;
+    const std::vector<int>& order = gathered_here ? run : gset;
+    if (gathered_here) {
+      if (!first && (st = upload_run()) != FHP_OK) break;
+      k_gather_done<<<1, 256, 0, s>>>(dflags, didx, (int)run.size(), ddone, ddone + n);
+      st = cuda_status(cudaGetLastError(), "k_gather_done");
+      if (st != FHP_OK) break;
+    }
+    st = cuda_status(cudaMemcpyAsync(hdone, ddone, (n + 1) * sizeof(int), cudaMemcpyDeviceToHost,
+                                     s), "copy");
+    if (st == FHP_OK) st = cuda_status(cudaStreamSynchronize(s), "sync");
+    if (st != FHP_OK) break;
+    first = false;
+    if (hdone[n]) break;
+    std::vector<int> still;
+    for (size_t j = 0; j < order.size(); ++j)
+      if (!hdone[j]) still.push_back(order[j]);
+    if (still.empty()) break;
+    run.swap(still);
+    if (gexec && 4 * run.size() <= 3 * gset.size()) {
+      // a quarter of the graph's plans have stopped: a graph of the running ones
+      if ((st = upload_run()) != FHP_OK) break;
+      build_graph();
+      gset = run;
+    }
+    const int nit = std::min(chunk, maxiter - done_iters);
+    for (int it = 0; it < nit && st == FHP_OK; ++it) {
+      if (gexec) {
+        st = cuda_status(cudaGraphLaunch(gexec, s), "cudaGraphLaunch");
+        for (int j : gset) engs[j]->launches += per_iter[j];
+      } else {
+        for (size_t j = 0; j < run.size() && st == FHP_OK; ++j) st = engs[run[j]]->cg_step(s);
+      }
+    }
+    done_iters += nit;
+    chunk = std::min(chunk * 2, 16);
+  }
+  for (int i = 0; i < n && st == FHP_OK; ++i) st = engs[i]->cg_end(res[i], s);
+  cleanup();
+  return st;
+}
+
+// Mixed precision over several plans: the refinement of cg_mixed per plan,
+// with each outer step's FP32 inner solves of all plans advanced together.
+int cg_mixed_many(const std::vector<fhp_plan_s*>& plans, int proj,
+                  const std::vector<const void*>& b, double tol, int maxiter,
+                  const std::vector<void*>& xv, std::vector<fhp::SolveResult>& out,
+                  cudaStream_t s) {
+  const int n = (int)plans.size();
+  out.assign(n, fhp::SolveResult());
+  struct P {
+    void *ax, *r, *r32, *d32;
+    std::vector<double> sumsq, norm, sc_in, sc_out;
+    std::vector<int> kit, status, active;
+  };
+  std::vector<P> ps(n);
+  int st = FHP_OK;
+  for (int i = 0; i < n && st == FHP_OK; ++i) {
+    fhp::EngineBase& hi = *plans[i]->eng;
+    const int L = hi.loads();
+    const size_t nv = (size_t)L * hi.dv() * hi.voxels();
+    P& q = ps[i];
+    q.ax = hi.scratch(fhp::SCR_MIX_AX, nv * 8);
+    q.r = hi.scratch(fhp::SCR_MIX_R, nv * 8);
+    q.r32 = hi.scratch(fhp::SCR_MIX_R32, nv * 4);
+    q.d32 = hi.scratch(fhp::SCR_MIX_D32, nv * 4);
+    if (!(q.ax && q.r && q.r32 && q.d32)) { st = FHP_OOM; break; }
+    q.sumsq.assign(L, 0.);
+    q.norm.assign(L, 0.);
+    q.sc_in.assign(L, 0.);
+    q.sc_out.assign(L, 0.);
+    q.kit.assign(L, 0);
+    q.status.assign(L, 0);
+    q.active.assign(L, 1);
+    st = cuda_status(cudaMemsetAsync(xv[i], 0, nv * 8, s), "memset");
+    if (st == FHP_OK) st = cuda_status(cudaMemsetAsync(q.ax, 0, nv * 8, s), "memset");
+    if (st == FHP_OK) st = hi.residual(b[i], q.ax, q.r, q.sumsq.data(), s);
+    const double M = (double)hi.voxels();
+    for (int l = 0; l < L; ++l) {
+      q.norm[l] = std::sqrt(q.sumsq[l] / M);
+      if (!std::isfinite(q.norm[l])) { q.status[l] = FHP_NONFINITE; q.active[l] = 0; }
+      if (!(q.norm[l] > tol && maxiter > 0)) q.active[l] = 0;
+    }
+  }
+  const int max_outer = n ? plans[0]->max_outer : 0;
+  for (int outer = 0; st == FHP_OK && outer < max_outer; ++outer) {
+    std::vector<fhp::EngineBase*> lo;
+    std::vector<const void*> rb;
+    std::vector<void*> dx;
+    std::vector<double> eta;
+    std::vector<int> idx;
+    int room = maxiter;
+    for (int i = 0; i < n; ++i) {
+      P& q = ps[i];
+      const int L = (int)q.kit.size();
+      int any = 0;
+      double e = 0.5;
+      for (int l = 0; l < L; ++l) {
+        if (!q.active[l]) continue;
+        any = 1;
+        room = std::min(room, maxiter - q.kit[l]);
+        e = std::min(e, std::max(plans[i]->eta, 0.5 * tol / q.norm[l]));
+      }
+      if (!any) continue;
+      for (int l = 0; l < L; ++l) {
+        q.sc_in[l] = q.active[l] ? 1.0 / q.norm[l] : 0.0;
+        q.sc_out[l] = q.active[l] ? q.norm[l] : 0.0;
+      }
+      if ((st = plans[i]->lo->scale_from64(static_cast<const double*>(q.r), q.sc_in.data(), q.r32,
+                                           s)) != FHP_OK) break;
+      lo.push_back(plans[i]->lo.get());
+      rb.push_back(q.r32);
+      dx.push_back(q.d32);
+      eta.push_back(e);
+      idx.push_back(i);
+    }
+    if (st != FHP_OK || idx.empty() || room <= 0) break;
+    std::vector<fhp::SolveResult> in;
+    if ((st = cg_many(lo, proj, rb, eta, room, dx, in, s)) != FHP_OK) break;
+    for (size_t j = 0; j < idx.size() && st == FHP_OK; ++j) {
+      const int i = idx[j];
+      fhp::EngineBase& hi = *plans[i]->eng;
+      P& q = ps[i];
+      double* x = static_cast<double*>(xv[i]);
+      const size_t nv = (size_t)hi.loads() * hi.dv() * hi.voxels();
+      const double M = (double)hi.voxels();
+      // x += G (s d), as cg_mixed
+      if ((st = cuda_status(cudaMemsetAsync(q.ax, 0, nv * 8, s), "memset")) != FHP_OK) break;
+      if ((st = plans[i]->lo->add_scaled_to64(q.d32, q.sc_out.data(), static_cast<double*>(q.ax),
+                                              s)) != FHP_OK) break;
+      if ((st = hi.project(proj, q.ax, q.r, s)) != FHP_OK) break;
+      if ((st = hi.axpy(1.0, q.r, x, s)) != FHP_OK) break;
+      if ((st = hi.apply_ex(proj, x, q.ax, s, true)) != FHP_OK) break;
+      if ((st = hi.residual(b[i], q.ax, q.r, q.sumsq.data(), s)) != FHP_OK) break;
+      for (int l = 0; l < (int)q.kit.size(); ++l) {
+        if (!q.active[l]) continue;
+        const double prev = q.norm[l];
+        q.kit[l] += in[j].kit[l];
+        q.norm[l] = std::sqrt(q.sumsq[l] / M);
+        if (!std::isfinite(q.norm[l])) { q.status[l] = FHP_NONFINITE; q.active[l] = 0; continue; }
+        if (q.norm[l] <= tol) { q.active[l] = 0; continue; }
+        if (q.kit[l] >= maxiter || in[j].kit[l] == 0 || q.norm[l] > 0.5 * prev) {
+          q.status[l] = FHP_NONCONVERGED;
+          q.active[l] = 0;
+        }
+      }
+    }
+  }
+  if (st == FHP_OK) st = cuda_status(cudaStreamSynchronize(s), "sync");
+  for (int i = 0; i < n; ++i) {
+    P& q = ps[i];
+    fhp::SolveResult& r = out[i];
+    const int L = (int)q.kit.size();
+    r.kit = q.kit;
+    r.status = q.status;
+    r.norm_res.assign(L, 0.);
+    r.res_log.assign(L, 0.);
+    for (int l = 0; l < L; ++l) {
+      r.norm_res[l] = q.kit[l] == 0 ? 0.0 : q.norm[l];
+      if (r.status[l] == 0 && q.norm[l] > tol && q.kit[l] > 0) r.status[l] = FHP_NONCONVERGED;
+      r.iterations_run = std::max(r.iterations_run, q.kit[l]);
+    }
+  }
+  return st;
+}
+
 }  // namespace
 
 extern "C" {
@@ -244,6 +542,22 @@ int fhp_plan_set_band_cg(fhp_plan plan, int spectral) {
   return FHP_OK;
 }
 
+int fhp_plan_set_integration_kernel(fhp_plan plan, int kind) {
+  if (!plan) return bad("plan is NULL");
+  if (kind != 0 && kind != 1) return bad("kind must be 0 or 1");
+  plan->eng->set_integration_kernel(kind);
+  if (plan->lo) plan->lo->set_integration_kernel(kind);
+  return FHP_OK;
+}
+
+int fhp_plan_autotune(fhp_plan plan, int* chosen, float* ms_per_apply, void* stream) {
+  if (!plan) return bad("plan is NULL");
+  cudaStream_t s = as_stream(stream);
+  int st = plan->eng->autotune(s, chosen, ms_per_apply);
+  if (st == FHP_OK && plan->lo) st = plan->lo->autotune(s, nullptr, nullptr);
+  return st;
+}
+
 int fhp_plan_destroy(fhp_plan plan) {
   delete plan;
   return FHP_OK;
@@ -340,6 +654,90 @@ int fhp_cg_solve(fhp_plan plan, int proj, const void* b, const void* x0, double 
     std::memcpy(res_log, r.res_log.data(),
                 std::min<size_t>((size_t)rows * L, r.res_log.size()) * sizeof(double));
   return st;
+}
+
+int fhp_cg_solve_many(int count, const fhp_plan* plans, int proj, const void* const* b,
+                      double tol, int maxiter, void* const* x, int* kit, double* norm_res,
+                      int* status, void* stream) {
+  if (count < 0 || (count > 0 && (!plans || !b || !x))) return bad("plans, b and x are required");
+  if (proj != 1 && proj != 2) return bad("proj must be 1 or 2");
+  if (maxiter < 0) return bad("maxiter must be >= 0");
+  if (!(tol >= 0)) return bad("tol must be >= 0");
+  if (count == 0) return FHP_OK;
+  const bool mixed = plans[0] && plans[0]->lo;
+  for (int i = 0; i < count; ++i) {
+    if (!plans[i] || !b[i] || !x[i]) return bad("every plan needs a plan, b and x");
+    if ((plans[i]->lo != nullptr) != mixed) return bad("plans mix FHP_MIXED and other precisions");
+    for (int j = 0; j < i; ++j)
+      if (plans[j] == plans[i]) return bad("a plan appears twice");
+  }
+  cudaStream_t s = as_stream(stream);
+  std::vector<fhp::SolveResult> r;
+  std::vector<const void*> bv(b, b + count);
+  std::vector<void*> xv(x, x + count);
+  int st;
+  if (mixed) {
+    std::vector<fhp_plan_s*> ps(plans, plans + count);
+    st = cg_mixed_many(ps, proj, bv, tol, maxiter, xv, r, s);
+  } else {
+    std::vector<fhp::EngineBase*> engs(count);
+    for (int i = 0; i < count; ++i) engs[i] = plans[i]->eng.get();
+    st = cg_many(engs, proj, bv, std::vector<double>(count, tol), maxiter, xv, r, s);
+  }
+  int off = 0;
+  for (int i = 0; i < count; ++i) {
+    const int L = plans[i]->eng->loads();
+    for (int l = 0; l < L && i < (int)r.size() && l < (int)r[i].kit.size(); ++l) {
+      if (kit) kit[off + l] = r[i].kit[l];
+      if (norm_res) norm_res[off + l] = r[i].norm_res[l];
+      if (status) status[off + l] = r[i].status[l];
+    }
+    off += L;
+  }
+  return st;
+}
+
+namespace {
+int solve_other_c(int kind, fhp_plan plan, int proj, const void* b, const void* x0, double p0,
+                  double p1, double tol, int maxiter, void* x, int* kit, double* norm_res,
+                  int* status, void* stream) {
+  if (!plan || !b || !x) return bad("plan, b and x are required");
+  if (proj != 1 && proj != 2) return bad("proj must be 1 or 2");
+  if (maxiter < 0) return bad("maxiter must be >= 0");
+  if (!(tol >= 0)) return bad("tol must be >= 0");
+  fhp::SolveResult r;
+  const int st = plan->eng->solve_other(kind, proj, b, x0, p0, p1, tol, maxiter, x, r, 1,
+                                        as_stream(stream));
+  const int L = plan->eng->loads();
+  for (int l = 0; l < L && l < (int)r.kit.size(); ++l) {
+    if (kit) kit[l] = r.kit[l];
+    if (norm_res) norm_res[l] = r.norm_res[l];
+    if (status) status[l] = r.status[l];
+  }
+  return st;
+}
+}  // namespace
+
+int fhp_richardson_solve(fhp_plan plan, int proj, const void* b, const void* x0, double omega,
+                         double tol, int maxiter, void* x, int* kit, double* norm_res,
+                         int* status, void* stream) {
+  if (!(omega > 0)) return bad("omega must be > 0");
+  return solve_other_c(0, plan, proj, b, x0, omega, 0., tol, maxiter, x, kit, norm_res, status,
+                       stream);
+}
+
+int fhp_chebyshev_solve(fhp_plan plan, int proj, const void* b, const void* x0, double eig_min,
+                        double eig_max, double tol, int maxiter, void* x, int* kit,
+                        double* norm_res, int* status, void* stream) {
+  if (!(eig_max > eig_min && eig_min > 0)) return bad("need 0 < eig_min < eig_max");
+  return solve_other_c(1, plan, proj, b, x0, eig_min, eig_max, tol, maxiter, x, kit, norm_res,
+                       status, stream);
+}
+
+int fhp_bicg_solve(fhp_plan plan, int proj, const void* b, const void* x0, double tol,
+                   int maxiter, void* x, int* kit, double* norm_res, int* status, void* stream) {
+  return solve_other_c(2, plan, proj, b, x0, 0., 0., tol, maxiter, x, kit, norm_res, status,
+                       stream);
 }
 
 int fhp_energy_matrix(fhp_plan plan, const void* X, int add_macro, double* AH, void* stream) {

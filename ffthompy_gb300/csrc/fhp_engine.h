@@ -47,6 +47,9 @@ enum ScratchSlot {
   SCR_MIX_R,           // mixed refinement: residual (FP64)
   SCR_MIX_R32,         // mixed refinement: scaled residual (FP32)
   SCR_MIX_D32,         // mixed refinement: correction (FP32)
+  SCR_SOLV_A,          // Richardson / Chebyshev / BiCG vectors
+  SCR_SOLV_B,
+  SCR_SOLV_C,
   kScratchSlots
 };
 
@@ -126,6 +129,22 @@ class EngineBase {
   virtual int rhs_macro(int proj, void* b, cudaStream_t s) = 0;
   virtual int cg_solve(int proj, const void* b, const void* x0, double tol, int maxiter, void* x,
                        SolveResult& res, int log_cap, cudaStream_t s) = 0;
+  // the same solve in phases: cg_begin sets up the state and the first
+  // residual, cg_step enqueues one iteration (no host synchronisation; it can
+  // be captured into a CUDA graph), cg_done_flag is the device flag that is
+  // nonzero once every load has stopped, cg_end finishes and collects the results
+  virtual int cg_begin(int proj, const void* b, const void* x0, double tol, int maxiter, void* x,
+                       int log_cap, cudaStream_t s) = 0;
+  virtual int cg_step(cudaStream_t s) = 0;
+  virtual const int* cg_done_flag() const = 0;
+  virtual int cg_end(SolveResult& res, cudaStream_t s) = 0;
+  // Richardson (kind 0: omega = p0), two-term Chebyshev (kind 1: eigenvalue
+  // interval [p0, p1]) and BiCG (kind 2, the transpose operator equal to the
+  // operator) over the fused operator, all loads at once with per-load state
+  // (ffthompy/general/solver.py:63-77, 142-285)
+  virtual int solve_other(int kind, int proj, const void* b, const void* x0, double p0, double p1,
+                          double tol, int maxiter, void* x, SolveResult& res, int log_cap,
+                          cudaStream_t s) = 0;
   virtual int energy(const void* X, int add_macro, double* AH, cudaStream_t s) = 0;
   // grad[c][v] = sum_ij W[i*L+j] dA_H[i][j]/dA_c(v) (W on host, grad FP64 device)
   virtual int energy_gradient(const void* X, int add_macro, const double* W, double* grad,
@@ -171,6 +190,13 @@ class EngineBase {
   // band plans: CG on the half spectra of the iterates (default) or on the
   // real fields of the solve grid; other plans ignore it
   virtual void set_spectral_cg(bool on) { (void)on; }
+  // band plans: integration pass with register-resident lines where they
+  // apply (1, default) or the shared-memory line cores (0)
+  virtual void set_integration_kernel(int kind) { (void)kind; }
+  // time candidate launch shapes of the operator on this plan's buffers and
+  // keep the fastest (cached per plan geometry); chosen[3] and best_ms (per
+  // application) may be null
+  virtual int autotune(cudaStream_t s, int* chosen, float* best_ms) = 0;
   // kernel launch count of the last call (instrumentation)
   long long launches = 0;
 };

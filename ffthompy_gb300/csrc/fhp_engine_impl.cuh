@@ -5,6 +5,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <functional>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -113,19 +116,9 @@ class Engine final : public EngineBase {
     const size_t srow = (size_t)np * l2_.dev.ld * sizeof(cplx<R>);
     // rows per CTA for the last-axis passes: pair lines plus (when it fits
     // the per-CTA budget) a staging area for the c2r input spectra
-    {
-      const size_t sraw_row = (size_t)C * g_.n2h * sizeof(cplx<R>);
-      const size_t budget = sizeof(R) == 4 ? kRowBudget32 : kRowBudget64;
-      auto smem_of = [&](int r, bool stg) {
-        return align16((size_t)r * srow) + (stg ? (size_t)r * sraw_row : 0);
-      };
-      rows_ = std::max(1, kTargetElems / (np * l2_.dev.ld));
-      c2r_stage_ = smem_of(1, true) <= budget;
-      while (rows_ > 1 && smem_of(rows_, c2r_stage_) > budget) --rows_;
-      smem_rows_ = std::max<size_t>(smem_of(rows_, c2r_stage_), 8 * kMaxLoads * sizeof(double));
-    }
+    (void)srow;
+    rows_ = set_row_geometry(std::max(1, kTargetElems / (np * l2_.dev.ld)));
     if (smem_rows_ > kSmemMax) { set_error("line too long for shared memory"); return ST_BAD_ARG; }
-    row_ctas_ = (int)(((long long)g_.n0 * g_.n1 + rows_ - 1) / rows_);
     // strided c2c on axis 1 (3D) and projection on the first real axis
     if (d == 3) {
       // column passes: twice the line target (as the band-axis passes) fills
@@ -196,6 +189,150 @@ class Engine final : public EngineBase {
     bsmem_rows_ = (size_t)brows_ * srow;
     if (bsmem_rows_ > kSmemMax) { set_error("integration line too long"); return ST_BAD_ARG; }
     brow_ctas_ = (int)(((long long)gi_.n0 * gi_.n1 + brows_ - 1) / brows_);
+    return ST_OK;
+  }
+
+  // rows per CTA of the last-axis passes: pair lines plus (when it fits the
+  // per-CTA budget) a staging area for the c2r input spectra; the request is
+  // reduced until it fits.  Sets rows_, c2r_stage_, smem_rows_, row_ctas_.
+  int set_row_geometry(int want) {
+    const int C = g_.L * g_.dv, np = (C + 1) / 2;
+    const size_t srow = (size_t)np * l2_.dev.ld * sizeof(cplx<R>);
+    const size_t sraw_row = (size_t)C * g_.n2h * sizeof(cplx<R>);
+    const size_t budget = sizeof(R) == 4 ? kRowBudget32 : kRowBudget64;
+    auto smem_of = [&](int r, bool stg) {
+      return align16((size_t)r * srow) + (stg ? (size_t)r * sraw_row : 0);
+    };
+    int r = std::max(1, want);
+    c2r_stage_ = smem_of(1, true) <= budget;
+    while (r > 1 && smem_of(r, c2r_stage_) > budget) --r;
+    rows_ = r;
+    smem_rows_ = std::max<size_t>(smem_of(r, c2r_stage_), 8 * kMaxLoads * sizeof(double));
+    row_ctas_ = (int)(((long long)g_.n0 * g_.n1 + r - 1) / r);
+    return r;
+  }
+
+  // ---- autotuning: launch shapes timed on this plan's own buffers ----------
+  // Candidates: band plans - the integration kernel (register lines with 1 or
+  // 2 CTAs per SM where they apply, or the shared-memory cores) and the
+  // column-tile target of the axis passes (1x, 2x, 4x the line target);
+  // other plans - rows per CTA of the last-axis passes and the column tile of
+  // the first-axis projection pass.  Each candidate is timed over three
+  // operator applications (CUDA events, after one warm-up) and the fastest
+  // is kept; the choice is cached per plan geometry, precision, coefficient
+  // kind and device, so plans of the same shape reuse it.
+  struct TuneChoice { int a = 0, b = 0, c = 0; float ms = 0.f; };
+  static std::mutex& tune_mu() { static std::mutex m; return m; }
+  static std::map<std::string, TuneChoice>& tune_cache() {
+    static std::map<std::string, TuneChoice> c;
+    return c;
+  }
+  std::string tune_key() const {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::string k = std::to_string(dev) + (sizeof(R) == 8 ? ":f64" : ":f32") + ":d" +
+                    std::to_string(g_.dim) + ":p" + std::to_string(cfg_.physics) + ":L" +
+                    std::to_string(g_.L) + ":k" + std::to_string(coef_kind_);
+    for (int i = 0; i < 3; ++i) k += ":" + std::to_string(cfg_.N[i]) + "/" + std::to_string(cfg_.integ[i]);
+    return k;
+  }
+  void tune_apply(const TuneChoice& c) {
+    if (band_) {
+      integ_kernel_ = c.a;
+      if (c.a == 1) reg512_ctas_per_sm_ = c.b;
+      axis_target_mult_ = c.c;
+    } else {
+      set_row_geometry(c.a);
+      Tp_ = c.b;
+    }
+  }
+  int autotune(cudaStream_t s, int* chosen, float* best_ms) override {
+    if (!A_) { set_error("coefficient not set"); return ST_BAD_ARG; }
+    const std::string key = tune_key();
+    {
+      std::lock_guard<std::mutex> g(tune_mu());
+      auto it = tune_cache().find(key);
+      if (it != tune_cache().end()) {
+        tune_apply(it->second);
+        if (chosen) { chosen[0] = it->second.a; chosen[1] = it->second.b; chosen[2] = it->second.c; }
+        if (best_ms) *best_ms = it->second.ms;
+        return ST_OK;
+      }
+    }
+    std::vector<TuneChoice> cand;
+    if (band_) {
+      for (int m : {1, 2, 4}) {
+        if (reg512_applies(coef_kind_)) {
+          cand.push_back({1, 1, m});
+          cand.push_back({1, 2, m});
+        }
+        cand.push_back({0, 0, m});
+      }
+    } else {
+      const int d = g_.dim;
+      const LineDev<R>& lp = d == 3 ? l0_.dev : l1_.dev;
+      const long long pin = d == 3 ? (long long)g_.n1 * g_.n2h : (long long)g_.n2h;
+      for (int r : {1, 2, 4, 8, 16, 32}) {
+        if (r > 1 && r > g_.n0 * g_.n1) break;
+        for (int T = 1; T <= 32 && T <= pin; T *= 2) {
+          if ((size_t)T * g_.dv * lp.ld * sizeof(cplx<R>) > kSmemMax) break;
+          cand.push_back({r, T, 0});
+        }
+      }
+    }
+    // partial sums must hold the most CTAs any candidate launches
+    const int save_rows = rows_, save_Tp = Tp_, save_ik = integ_kernel_,
+              save_rc = reg512_ctas_per_sm_, save_m = axis_target_mult_;
+    int st = ensure_cg_buffers();
+    if (st != ST_OK) return st;
+    {
+      const long long worst = ((long long)g_.n0 * g_.n1);
+      if (worst > nparts_max_) {
+        double* np = nullptr;
+        FHP_CHECK(cudaMalloc(&np, (size_t)worst * kMaxLoads * kMaxLoads * sizeof(double)));
+        cudaFree(partials_);
+        partials_ = np;
+        nparts_max_ = (int)worst;
+      }
+    }
+    const size_t n = (size_t)g_.L * g_.dv * g_.M;
+    k_fill_macro<R><<<grid_for(n), kThreads, 0, s>>>(r_, g_, 1.0);
+    FHP_LAUNCHED();
+    cudaEvent_t e0, e1;
+    FHP_CHECK(cudaEventCreate(&e0));
+    FHP_CHECK(cudaEventCreate(&e1));
+    TuneChoice best;
+    best.ms = 1e30f;
+    for (const TuneChoice& c : cand) {
+      tune_apply(c);
+      if ((st = apply_ex(1, r_, ap_, s, false)) != ST_OK) break;
+      cudaEventRecord(e0, s);
+      for (int rep = 0; rep < 3 && st == ST_OK; ++rep) st = apply_ex(1, r_, ap_, s, false);
+      cudaEventRecord(e1, s);
+      if (st != ST_OK || cudaEventSynchronize(e1) != cudaSuccess) { st = st ? st : ST_CUDA; break; }
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < best.ms) { best = c; best.ms = ms; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st != ST_OK || cand.empty()) {
+      rows_ = save_rows;
+      set_row_geometry(save_rows);
+      Tp_ = save_Tp;
+      integ_kernel_ = save_ik;
+      reg512_ctas_per_sm_ = save_rc;
+      axis_target_mult_ = save_m;
+      return st;
+    }
+    best.ms /= 3.f;
+    tune_apply(best);
+    {
+      std::lock_guard<std::mutex> g(tune_mu());
+      tune_cache()[key] = best;
+    }
+    if (chosen) { chosen[0] = best.a; chosen[1] = best.b; chosen[2] = best.c; }
+    if (best_ms) *best_ms = best.ms;
     return ST_OK;
   }
 
@@ -512,12 +649,161 @@ class Engine final : public EngineBase {
 
   int cg_solve(int proj, const void* bv, const void* x0v, double tol, int maxiter, void* xv,
                SolveResult& res, int log_cap, cudaStream_t s) override {
+    int st = cg_begin(proj, bv, x0v, tol, maxiter, xv, log_cap, s);
+    if (st != ST_OK) return st;
+    st = iterate(maxiter, s, [&]() { return cg_step(s); });
+    if (st != ST_OK) return st;
+    return cg_end(res, s);
+  }
+
+  // ---- Richardson / Chebyshev / BiCG (solver.py:63-77, 142-285) -----------
+  // The operator runs with the per-load done flags (done loads skipped), the
+  // recurrences in fused component-row kernels with per-load scalars on the
+  // device, one iteration per CUDA-graph replay, and the host reads the
+  // all-done flag between chunks of iterations, as in cg_solve.
+  int solve_other(int kind, int proj, const void* bv, const void* x0v, double p0, double p1,
+                  double tol, int maxiter, void* xv, SolveResult& res, int log_cap,
+                  cudaStream_t s) override {
+    if (!A_) { set_error("coefficient not set"); return ST_BAD_ARG; }
+    if (kind < 0 || kind > 2) { set_error("unknown solver"); return ST_BAD_ARG; }
+    gp_.proj = proj;
+    const R* b = static_cast<const R*>(bv);
+    const R* x0 = static_cast<const R*>(x0v);
+    R* x = static_cast<R*>(xv);
+    const size_t n = (size_t)g_.L * g_.dv * g_.M;
+    int st = ensure_cg_buffers();
+    if (st != ST_OK) return st;
+    R* va = static_cast<R*>(scratch(SCR_SOLV_A, n * sizeof(R)));
+    R* vb = static_cast<R*>(scratch(SCR_SOLV_B, n * sizeof(R)));
+    R* vc = static_cast<R*>(scratch(SCR_SOLV_C, n * sizeof(R)));
+    if (!va || !vb || !vc) return ST_OOM;
+    if (x0) FHP_CHECK(cudaMemcpyAsync(x, x0, n * sizeof(R), cudaMemcpyDeviceToDevice, s));
+    else FHP_CHECK(cudaMemsetAsync(x, 0, n * sizeof(R), s));
+    if ((st = init_state(tol, maxiter, log_cap, s)) != ST_OK) return st;
+    const double invM = 1.0 / (double)g_.M;
+    const int C = g_.L * g_.dv;
+    const int ux = std::max(1, red_ctas_ / C);
+    const dim3 cgrid((unsigned)ux, (unsigned)C);
+    auto op = [&](const R* in, R* out) {
+      return run_operator(coef_kind_, false, in, nullptr, nullptr, out, nullptr, s, true, false);
+    };
+    auto sum_into = [&](double* dst_rr, bool relative) {
+      // partials of a component-row kernel -> per-load norm (relative to r0)
+      k_fin_norm<<<g_.L, kThreads, 0, s>>>(partials_, ux * C, st_, g_.L, invM,
+                                           relative ? 1 : 0, cg_log_, cg_log_rows_, all_done_);
+      (void)dst_rr;
+    };
+    std::function<int()> step;
+    if (kind == 0) {
+      // norm_res starts at 1e15 (solver.py:65-66): the first iteration runs
+      k_set_norm<<<1, 32, 0, s>>>(st_, g_.L, 1e15);
+      FHP_LAUNCHED();
+      step = [&, b, x]() -> int {
+        int r = op(x, ap_);
+        if (r != ST_OK) return r;
+        k_resid_comp<R, 0><<<cgrid, kThreads, 0, s>>>(b, ap_, x, p0, partials_, g_, st_,
+                                                     all_done_);
+        FHP_LAUNCHED();
+        sum_into(nullptr, false);
+        FHP_LAUNCHED();
+        k_update_all_done<<<1, 1, 0, s>>>(st_, g_.L, all_done_);
+        FHP_LAUNCHED();
+        return ST_OK;
+      };
+    } else if (kind == 1) {
+      // r = B - A x0, r0 = |r| (pap), norm_res = r0 / |B| (solver.py:226-236)
+      if ((st = op(x, ap_)) != ST_OK) return st;
+      k_resid_comp<R, 1><<<cgrid, kThreads, 0, s>>>(b, ap_, r_, 0., partials_, g_, st_, nullptr);
+      FHP_LAUNCHED();
+      k_dot<R><<<red_ctas_, kThreads, 0, s>>>(b, b, partials_ + (size_t)ux * C * g_.L, g_);
+      FHP_LAUNCHED();
+      k_cheb_init<<<1, 32, 0, s>>>(partials_, ux * C, partials_ + (size_t)ux * C * g_.L,
+                                   red_ctas_, st_, g_.L, invM, cg_log_, cg_log_rows_);
+      FHP_LAUNCHED();
+      k_update_all_done<<<1, 1, 0, s>>>(st_, g_.L, all_done_);
+      FHP_LAUNCHED();
+      FHP_CHECK(cudaMemsetAsync(va, 0, n * sizeof(R), s));  // v = 0
+      const double d = (p1 + p0) / 2.0, c = (p1 - p0) / 2.0;
+      step = [&, b, x, va, d, c]() -> int {
+        k_cheb_coef<<<1, 32, 0, s>>>(st_, g_.L, d, c, all_done_);
+        FHP_LAUNCHED();
+        k_cheb_update<R><<<cgrid, kThreads, 0, s>>>(r_, va, x, g_, st_, all_done_);
+        FHP_LAUNCHED();
+        int r = op(x, ap_);
+        if (r != ST_OK) return r;
+        k_resid_comp<R, 1><<<cgrid, kThreads, 0, s>>>(b, ap_, r_, 0., partials_, g_, st_,
+                                                     all_done_);
+        FHP_LAUNCHED();
+        sum_into(nullptr, true);
+        FHP_LAUNCHED();
+        k_update_all_done<<<1, 1, 0, s>>>(st_, g_.L, all_done_);
+        FHP_LAUNCHED();
+        return ST_OK;
+      };
+    } else {
+      // R = B - A x0, Rs = R, P = R, Ps = Rs, rr = <R, Rs> (solver.py:158-166)
+      R* rs = va;
+      R* ps = vb;
+      R* atps = vc;
+      if ((st = op(x, ap_)) != ST_OK) return st;
+      FHP_CHECK(cudaMemcpyAsync(r_, b, n * sizeof(R), cudaMemcpyDeviceToDevice, s));
+      k_axpby<R><<<grid_for(n), kThreads, 0, s>>>((long long)n, -1.0, ap_, 1.0, r_);
+      FHP_LAUNCHED();
+      FHP_CHECK(cudaMemcpyAsync(rs, r_, n * sizeof(R), cudaMemcpyDeviceToDevice, s));
+      FHP_CHECK(cudaMemcpyAsync(p_, r_, n * sizeof(R), cudaMemcpyDeviceToDevice, s));
+      FHP_CHECK(cudaMemcpyAsync(ps, r_, n * sizeof(R), cudaMemcpyDeviceToDevice, s));
+      k_dot<R><<<red_ctas_, kThreads, 0, s>>>(r_, rs, partials_, g_);
+      FHP_LAUNCHED();
+      k_fin_init<<<1, 32, 0, s>>>(partials_, red_ctas_, st_, g_.L, invM, cg_log_, cg_log_rows_);
+      FHP_LAUNCHED();
+      k_update_all_done<<<1, 1, 0, s>>>(st_, g_.L, all_done_);
+      FHP_LAUNCHED();
+      step = [&, x, rs, ps, atps]() -> int {
+        int r = op(p_, ap_);
+        if (r == ST_OK) r = op(ps, atps);
+        if (r != ST_OK) return r;
+        k_dot<R><<<red_ctas_, kThreads, 0, s>>>(ap_, ps, partials_, g_);
+        FHP_LAUNCHED();
+        k_fin_pap<<<g_.L, kThreads, 0, s>>>(partials_, red_ctas_, st_, g_.L, invM, all_done_);
+        FHP_LAUNCHED();
+        k_bicg_update<R><<<cgrid, kThreads, 0, s>>>(x, r_, rs, p_, ap_, atps, partials_, g_, st_,
+                                                    all_done_);
+        FHP_LAUNCHED();
+        k_fin_rr<<<g_.L, kThreads, 0, s>>>(partials_, ux * C, st_, g_.L, invM, cg_log_,
+                                           cg_log_rows_, all_done_);
+        FHP_LAUNCHED();
+        k_bicg_dirs<R><<<cgrid, kThreads, 0, s>>>(r_, rs, p_, ps, g_, st_, all_done_);
+        FHP_LAUNCHED();
+        k_update_all_done<<<1, 1, 0, s>>>(st_, g_.L, all_done_);
+        FHP_LAUNCHED();
+        return ST_OK;
+      };
+    }
+    if ((st = iterate(maxiter, s, step)) != ST_OK) return st;
+    if ((st = collect(tol, cg_log_rows_, cg_log_, res, s)) != ST_OK) return st;
+    // Chebyshev returns at once with norm_res = r0 / |B| when that is below
+    // tol (solver.py:234-236)
+    if (kind == 1)
+      for (int l = 0; l < g_.L; ++l)
+        if (res.kit[l] == 0 && h_st_[l].norm_res < tol) res.norm_res[l] = h_st_[l].norm_res;
+    return ST_OK;
+  }
+
+  // ---- CG in phases: begin (state, first residual), step (one iteration's
+  // launches, capturable), end (final projection, results).  cg_solve runs
+  // them for one plan; fhp_cg_solve_many advances several plans together.
+  int cg_begin(int proj, const void* bv, const void* x0v, double tol, int maxiter, void* xv,
+               int log_cap, cudaStream_t s) override {
     if (!A_) { set_error("coefficient not set"); return ST_BAD_ARG; }
     gp_.proj = proj;
     const R* b = static_cast<const R*>(bv);
     const R* x0 = static_cast<const R*>(x0v);
     R* x = static_cast<R*>(xv);
-    if (band_ && spectral_cg_) return spectral_cg_solve(proj, b, x0, tol, maxiter, x, res, log_cap, s);
+    cg_spectral_ = band_ && spectral_cg_;
+    cg_proj_ = proj;
+    cg_tol_ = tol;
+    cg_x_ = x;
+    if (cg_spectral_) return spectral_cg_begin(proj, b, x0, tol, maxiter, log_cap, s);
     const size_t n = (size_t)g_.L * g_.dv * g_.M;
     int st = ensure_cg_buffers();
     if (st != ST_OK) return st;
@@ -534,7 +820,47 @@ class Engine final : public EngineBase {
     }
     FHP_CHECK(cudaMemcpyAsync(p_, r_, n * sizeof(R), cudaMemcpyDeviceToDevice, s));
     x_cur_ = x;
-    // state
+    if ((st = init_state(tol, maxiter, log_cap, s)) != ST_OK) return st;
+    k_dot<R><<<red_ctas_, kThreads, 0, s>>>(r_, r_, partials_, g_);
+    FHP_LAUNCHED();
+    k_fin_init<<<1, 32, 0, s>>>(partials_, red_ctas_, st_, g_.L, 1.0 / (double)g_.M, cg_log_,
+                                cg_log_rows_);
+    FHP_LAUNCHED();
+    k_update_all_done<<<1, 1, 0, s>>>(st_, g_.L, all_done_);
+    FHP_LAUNCHED();
+    return ST_OK;
+  }
+
+  int cg_step(cudaStream_t s) override {
+    if (cg_spectral_) {
+      const size_t nz = (size_t)g_.L * g_.dv * g_.n0 * g_.n1 * g_.n2h;
+      return spectral_iteration(zb_, zb_ + nz, zb_ + 2 * nz, zb_ + 3 * nz, cg_log_, cg_log_rows_,
+                                s);
+    }
+    return cg_iteration(cg_log_, cg_log_rows_, s);
+  }
+
+  const int* cg_done_flag() const override { return all_done_; }
+
+  int cg_end(SolveResult& res, cudaStream_t s) override {
+    int st;
+    if (cg_spectral_) {
+      // back to the caller's real field; FP32 iterates are projected first
+      // (roundoff of the updates outside range(G))
+      if (sizeof(R) == 4 && (st = spec_green(zb_, s)) != ST_OK) return st;
+      if ((st = from_z(zb_, cg_x_, s)) != ST_OK) return st;
+    } else if (sizeof(R) == 4 && (st = project(cg_proj_, cg_x_, cg_x_, s)) != ST_OK) {
+      // FP32 fields: the iterate drifts out of range(G) by roundoff accumulated
+      // over the iterations, and that component enters the energy to first
+      // order. One projection x <- G x (the identity in exact arithmetic) puts
+      // the drift back to a single rounding.
+      return st;
+    }
+    return collect(cg_tol_, cg_log_rows_, cg_log_, res, s);
+  }
+
+  // per-load CG state, all_done and the residual log of a new solve
+  int init_state(double tol, int maxiter, int log_cap, cudaStream_t s) {
     for (int l = 0; l < g_.L; ++l) {
       LoadState& h = h_st_[l];
       std::memset(&h, 0, sizeof(LoadState));
@@ -544,28 +870,11 @@ class Engine final : public EngineBase {
     }
     FHP_CHECK(cudaMemcpyAsync(st_, h_st_, g_.L * sizeof(LoadState), cudaMemcpyHostToDevice, s));
     FHP_CHECK(cudaMemsetAsync(all_done_, 0, sizeof(int), s));
-    const int log_rows = std::max(1, std::min(log_cap, maxiter + 1));
-    double* dlog =
-        static_cast<double*>(scratch(SCR_LOG, (size_t)log_rows * g_.L * sizeof(double)));
-    if (!dlog) return ST_OOM;
-    FHP_CHECK(cudaMemsetAsync(dlog, 0, (size_t)log_rows * g_.L * sizeof(double), s));
-    k_dot<R><<<red_ctas_, kThreads, 0, s>>>(r_, r_, partials_, g_);
-    FHP_LAUNCHED();
-    k_fin_init<<<1, 32, 0, s>>>(partials_, red_ctas_, st_, g_.L, 1.0 / (double)g_.M, dlog,
-                                log_rows);
-    FHP_LAUNCHED();
-    k_update_all_done<<<1, 1, 0, s>>>(st_, g_.L, all_done_);
-    FHP_LAUNCHED();
-    st = iterate(maxiter, s, [&]() { return cg_iteration(dlog, log_rows, s); });
-    if (st != ST_OK) return st;
-    // FP32 fields: the iterate drifts out of range(G) by roundoff accumulated
-    // over the iterations, and that component enters the energy to first
-    // order. One projection x <- G x (the identity in exact arithmetic) puts
-    // the drift back to a single rounding.
-    if (sizeof(R) == 4 && (st = project(proj, x, x, s)) != ST_OK) {
-      return st;
-    }
-    return collect(tol, log_rows, dlog, res, s);
+    cg_log_rows_ = std::max(1, std::min(log_cap, maxiter + 1));
+    cg_log_ = static_cast<double*>(scratch(SCR_LOG, (size_t)cg_log_rows_ * g_.L * sizeof(double)));
+    if (!cg_log_) return ST_OOM;
+    FHP_CHECK(cudaMemsetAsync(cg_log_, 0, (size_t)cg_log_rows_ * g_.L * sizeof(double), s));
+    return ST_OK;
   }
 
   // The iterations of a solve, in chunks between host checks of all_done.
@@ -659,6 +968,7 @@ class Engine final : public EngineBase {
   // iterates, residual norms and stopping tests are the reference's up to
   // roundoff.  The initial residual is projected onto range(G).
   void set_spectral_cg(bool on) override { spectral_cg_ = on; }
+  void set_integration_kernel(int kind) override { integ_kernel_ = kind; }
 
   int ensure_spectral() {
     const size_t nz = (size_t)g_.L * g_.dv * g_.n0 * g_.n1 * g_.n2h;
@@ -772,8 +1082,8 @@ class Engine final : public EngineBase {
     return ST_OK;
   }
 
-  int spectral_cg_solve(int proj, const R* b, const R* x0, double tol, int maxiter, R* x,
-                        SolveResult& res, int log_cap, cudaStream_t s) {
+  int spectral_cg_begin(int proj, const R* b, const R* x0, double tol, int maxiter,
+                        int log_cap, cudaStream_t s) {
     int st = ensure_spectral();
     if (st != ST_OK) return st;
     const size_t n = (size_t)g_.L * g_.dv * g_.M;
@@ -781,7 +1091,6 @@ class Engine final : public EngineBase {
     cplx<R>* zx = zb_;
     cplx<R>* zr = zb_ + nz;
     cplx<R>* zp = zb_ + 2 * nz;
-    cplx<R>* zap = zb_ + 3 * nz;
     // x = x0 ; R = B - A x0 (solver.py:114-117), then both in z form, R
     // projected onto range(G)
     const R* rsrc = b;
@@ -800,36 +1109,15 @@ class Engine final : public EngineBase {
     if ((st = to_z(rsrc, zr, s)) != ST_OK) return st;
     if ((st = spec_green(zr, s)) != ST_OK) return st;
     FHP_CHECK(cudaMemcpyAsync(zp, zr, nz * sizeof(cplx<R>), cudaMemcpyDeviceToDevice, s));
-    for (int l = 0; l < g_.L; ++l) {
-      LoadState& h = h_st_[l];
-      std::memset(&h, 0, sizeof(LoadState));
-      h.tol = tol;
-      h.maxiter = maxiter;
-      h.guard = sizeof(R) == 4 ? 4.0 : 0.0;
-    }
-    FHP_CHECK(cudaMemcpyAsync(st_, h_st_, g_.L * sizeof(LoadState), cudaMemcpyHostToDevice, s));
-    FHP_CHECK(cudaMemsetAsync(all_done_, 0, sizeof(int), s));
-    const int log_rows = std::max(1, std::min(log_cap, maxiter + 1));
-    double* dlog =
-        static_cast<double*>(scratch(SCR_LOG, (size_t)log_rows * g_.L * sizeof(double)));
-    if (!dlog) return ST_OOM;
-    FHP_CHECK(cudaMemsetAsync(dlog, 0, (size_t)log_rows * g_.L * sizeof(double), s));
+    if ((st = init_state(tol, maxiter, log_cap, s)) != ST_OK) return st;
     k_dot<R><<<red_ctas_, kThreads, 0, s>>>(reinterpret_cast<const R*>(zr),
                                             reinterpret_cast<const R*>(zr), partials_, gz_);
     FHP_LAUNCHED();
-    k_fin_init<<<1, 32, 0, s>>>(partials_, red_ctas_, st_, g_.L, 1.0, dlog, log_rows);
+    k_fin_init<<<1, 32, 0, s>>>(partials_, red_ctas_, st_, g_.L, 1.0, cg_log_, cg_log_rows_);
     FHP_LAUNCHED();
     k_update_all_done<<<1, 1, 0, s>>>(st_, g_.L, all_done_);
     FHP_LAUNCHED();
-    st = iterate(maxiter, s, [&]() {
-      return spectral_iteration(zx, zr, zp, zap, dlog, log_rows, s);
-    });
-    if (st != ST_OK) return st;
-    // back to the caller's real field; FP32 iterates are projected first
-    // (roundoff of the updates outside range(G), see cg_solve)
-    if (sizeof(R) == 4 && (st = spec_green(zx, s)) != ST_OK) return st;
-    if ((st = from_z(zx, x, s)) != ST_OK) return st;
-    return collect(tol, log_rows, dlog, res, s);
+    return ST_OK;
   }
 
   // A_H[i][j] = <A u_i, u_j>, u_i = X_i (+ E_i)  (postprocess.py:53-70)
@@ -1126,6 +1414,7 @@ class Engine final : public EngineBase {
     FHP_ATTR((k_band_last<R, COEF_ISO>));
     FHP_ATTR((k_band_last<R, COEF_SYM>));
     FHP_ATTR((k_band_last<R, COEF_FULL>));
+    if constexpr (sizeof(R) == 4) FHP_ATTR((k_band_last_r512<R>));
 #define FHP_ATTR_P2(P)                              \
     FHP_ATTR((k_band_last_p2<R, COEF_ISO, P>));     \
     FHP_ATTR((k_band_last_p2<R, COEF_SYM, P>));     \
@@ -1293,7 +1582,7 @@ class Engine final : public EngineBase {
     // buffer per column, so its tile may use the integration pass's budget.
     const size_t budget = (mode == BAND_DOWN_PROJ_F && sizeof(R) == 4) ? kBandLastBudget32
                                                                         : kSmemBudget;
-    return tile_cols(nf, nlc, ax.inner, 2 * kTargetElems, budget);
+    return tile_cols(nf, nlc, ax.inner, 2 * kTargetElems * axis_target_mult_, budget);
   }
 
   int band_axis(int mode, const cplx<R>* in, cplx<R>* out, const BandAxis& ax_in,
@@ -1363,9 +1652,33 @@ class Engine final : public EngineBase {
 
   // last axis on the integration grid: c2r, q = a x cs, r2c, keep the band
   // (in place in Sbig, all loads and comps)
+  // the register-resident 512-point integration kernel applies: FP32, an
+  // isotropic coefficient, a direct 512-point line, the band within N/4
+  bool reg512_applies(int coef) const {
+    return sizeof(R) == 4 && coef == COEF_ISO && !lb2_.dev.blue && lb2_.dev.nf == 512 &&
+           4 * g_.n2h <= 512 && 2 * g_.n2h - 1 <= g_.n2 + 1;
+  }
+
   int band_last_pass(int coef, cplx<R>* Sbig, R cs, bool cg, cudaStream_t s) {
     const int* ad = cg ? all_done_ : nullptr;
     const long long n2h = g_.n2h;
+    if constexpr (sizeof(R) == 4) {
+      if (integ_kernel_ == 1 && reg512_applies(coef)) {
+        const long long nrows = (long long)gi_.n0 * gi_.n1;
+        const double b4 = 2.0 * (double)(g_.L * g_.dv) * nrows * n2h * sizeof(cplx<R>) +
+                          coef_bytes();
+        const int pk = pbeg("band_last_coef", b4, s);
+        const long long need = (nrows + kR512Warps - 1) / kR512Warps;
+        const unsigned ctas =
+            (unsigned)std::min<long long>(need, (long long)reg512_ctas_per_sm_ * nsm_);
+        k_band_last_r512<R><<<ctas, 32 * kR512Warps, r512_smem_bytes(), s>>>(
+            reinterpret_cast<float2*>(Sbig), reinterpret_cast<const float*>(A_), g_, nrows,
+            (int)n2h, g_.n2, reinterpret_cast<const float2*>(lb2_.dev.tw), (float)cs, ad);
+        pend(pk, s);
+        FHP_LAUNCHED();
+        return ST_OK;
+      }
+    }
     const long long nrows = (long long)gi_.n0 * gi_.n1;
     const double b4 = 2.0 * (double)(g_.L * g_.dv) * nrows * n2h * sizeof(cplx<R>) + coef_bytes();
     const int pk = pbeg("band_last_coef", b4, s);
@@ -1579,6 +1892,18 @@ class Engine final : public EngineBase {
   cplx<R>* SB_ = nullptr;
   int brows_ = 1, brow_ctas_ = 1;
   size_t bsmem_rows_ = 0;
+  // integration pass kernel: 1 register-resident 512-point lines where they
+  // apply, 0 the shared-memory line cores
+  int integ_kernel_ = 1;
+  int reg512_ctas_per_sm_ = 2;
+  int axis_target_mult_ = 1;   // band axis passes: column-tile target x this
+  // the solve in progress (cg_begin .. cg_end)
+  bool cg_spectral_ = false;
+  int cg_proj_ = 1;
+  double cg_tol_ = 0.0;
+  R* cg_x_ = nullptr;
+  double* cg_log_ = nullptr;
+  int cg_log_rows_ = 1;
   // spectral CG of band plans
   bool spectral_cg_ = true;
   cplx<R>* zb_ = nullptr;      // z vectors x, r, p, Ap (half spectra of the N grid)

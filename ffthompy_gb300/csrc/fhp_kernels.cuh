@@ -1209,23 +1209,62 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_axis(const cplx<
     // with 2|q| = n_in (the Nyquist index of an even n_in) are zero on
     // range(G), where the iterates live, and stay untouched.
     const R bet = R(st[load].beta);
-    tile_loop(1, ax.n_out, T, lgT, [&](int, int k, int t) {
-      if (pr2 && k >= pq0 && k < pq1) return;
-      const long long col = t0 + t;
-      const int q = signed_freq(k, ax.n_out);
-      const int aq = q < 0 ? -q : q;
-      cplx<R> v = mkc<R>(R(0), R(0));
-      if (col < ax.inner && 2 * aq < ax.n_in) {
-        const long long idx = (((long long)c0 * ax.mid + m) * ax.n_in +
-                               (q < 0 ? q + ax.n_in : q)) * ax.inner + col;
-        const cplx<R> r = Sin[idx];
-        cplx<R> p = aux[idx];
-        p = mkc<R>(r.x + bet * p.x, r.y + bet * p.y);
-        aux[idx] = p;
-        v = cscale<R>(p, half_weight_root<R>(ax, g, col, true));
-      }
-      buf2[t * ld2 + slot_inv<R>(L2, k)] = v;
-    });
+    const cplx<R>* rbase = Sin + (((long long)c0 * ax.mid + m) * ax.n_in) * ax.inner + t0;
+    cplx<R>* pbase = aux + (((long long)c0 * ax.mid + m) * ax.n_in) * ax.inner + t0;
+    if (pr2 && !L2.blue) {
+      // pruned direct B lines: the slots of the pruned frequencies
+      // [nf/4, 3nf/4) are never read by the inverse core, so they hold r
+      // while p sits in its own slot; both arrive by cp.async (all loads in
+      // flight at once), then p is updated, written back and scaled in place
+      const int sh = L2.nf / 4;
+      tile_loop(1, ax.n_out, T, lgT, [&](int, int k, int t) {
+        if (k >= pq0 && k < pq1) return;
+        const int q = signed_freq(k, ax.n_out);
+        const int aq = q < 0 ? -q : q;
+        cplx<R>* slot = buf2 + t * ld2 + slot_inv<R>(L2, k);
+        if (t0 + t < ax.inner && 2 * aq < ax.n_in) {
+          const long long off = (long long)(q < 0 ? q + ax.n_in : q) * ax.inner + t;
+          cp_async_cplx<R>(slot, pbase + off);
+          cp_async_cplx<R>(buf2 + t * ld2 + slot_inv<R>(L2, q < 0 ? k - sh : k + sh), rbase + off);
+        } else {
+          *slot = mkc<R>(R(0), R(0));
+        }
+      });
+      cp_async_commit();
+      cp_async_wait<0>();
+      __syncthreads();
+      tile_loop(1, ax.n_out, T, lgT, [&](int, int k, int t) {
+        if (k >= pq0 && k < pq1) return;
+        const int q = signed_freq(k, ax.n_out);
+        const int aq = q < 0 ? -q : q;
+        const long long col = t0 + t;
+        if (col < ax.inner && 2 * aq < ax.n_in) {
+          cplx<R>* slot = buf2 + t * ld2 + slot_inv<R>(L2, k);
+          const cplx<R> r = buf2[t * ld2 + slot_inv<R>(L2, q < 0 ? k - sh : k + sh)];
+          cplx<R> p = *slot;
+          p = mkc<R>(r.x + bet * p.x, r.y + bet * p.y);
+          pbase[(long long)(q < 0 ? q + ax.n_in : q) * ax.inner + t] = p;
+          *slot = cscale<R>(p, half_weight_root<R>(ax, g, col, true));
+        }
+      });
+    } else {
+      tile_loop(1, ax.n_out, T, lgT, [&](int, int k, int t) {
+        if (pr2 && k >= pq0 && k < pq1) return;
+        const long long col = t0 + t;
+        const int q = signed_freq(k, ax.n_out);
+        const int aq = q < 0 ? -q : q;
+        cplx<R> v = mkc<R>(R(0), R(0));
+        if (col < ax.inner && 2 * aq < ax.n_in) {
+          const long long off = (long long)(q < 0 ? q + ax.n_in : q) * ax.inner + t;
+          const cplx<R> r = rbase[off];
+          cplx<R> p = pbase[off];
+          p = mkc<R>(r.x + bet * p.x, r.y + bet * p.y);
+          pbase[off] = p;
+          v = cscale<R>(p, half_weight_root<R>(ax, g, col, true));
+        }
+        buf2[t * ld2 + slot_inv<R>(L2, k)] = v;
+      });
+    }
   } else {
     // load: [comp][mid][n_in][inner]
     tile_loop(nlc, ax.n_in, T, lgT, [&](int c, int i, int t) {
@@ -1343,21 +1382,54 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_axis(const cplx<
         if (c < g.dv) set_fwd<R>(buf1 + (c * T + t) * ld1, L1, kb, x[c]);
     }
     __syncthreads();
-    // rows of T columns to global (z form: times sqrt(w)), with <p, Ap>
+    // rows of T columns to global (z form: times sqrt(w)), with <p, Ap>: a
+    // thread keeps one column and takes its frequencies four at a time, the
+    // four loads of p issued before their products
     R dot = R(0);
-    tile_loop(nlc, ax.n_out, T, lgT, [&](int c, int k, int t) {
+    if (T <= (int)blockDim.x) {
+      const int t = threadIdx.x & (T - 1);
+      const int kst = (int)blockDim.x >> lgT;
       const long long col = t0 + t;
-      if (col >= ax.inner) return;
-      const int q = signed_freq(k, ax.n_out);
-      cplx<R> v = get_fwd<R>(buf1 + (c * T + t) * ld1, L1, q < 0 ? q + ax.n_in : q);
-      v = cscale<R>(v, half_weight_root<R>(ax, g, col, false));
-      const long long idx = (((long long)(c0 + c) * ax.mid + m) * ax.n_out + k) * ax.inner + col;
-      Sout[idx] = v;
-      if (partials) {
-        const cplx<R> p = aux[idx];
-        dot += p.x * v.x + p.y * v.y;
+      if (col < ax.inner) {
+        const R fo = half_weight_root<R>(ax, g, col, false);
+        for (int c = 0; c < nlc; ++c) {
+          const long long base = (((long long)(c0 + c) * ax.mid + m) * ax.n_out) * ax.inner + col;
+          const cplx<R>* line = buf1 + (c * T + t) * ld1;
+          for (int k = (int)threadIdx.x >> lgT; k < ax.n_out; k += 4 * kst) {
+            cplx<R> pv[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              const int ku = k + u * kst;
+              pv[u] = (partials && ku < ax.n_out) ? aux[base + (long long)ku * ax.inner]
+                                                  : mkc<R>(R(0), R(0));
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              const int ku = k + u * kst;
+              if (ku >= ax.n_out) break;
+              const int q = signed_freq(ku, ax.n_out);
+              const cplx<R> v = cscale<R>(get_fwd<R>(line, L1, q < 0 ? q + ax.n_in : q), fo);
+              Sout[base + (long long)ku * ax.inner] = v;
+              dot += pv[u].x * v.x + pv[u].y * v.y;
+            }
+          }
+        }
       }
-    });
+    } else {
+      tile_loop(nlc, ax.n_out, T, lgT, [&](int c, int k, int t) {
+        const long long col = t0 + t;
+        if (col >= ax.inner) return;
+        const int q = signed_freq(k, ax.n_out);
+        cplx<R> v = get_fwd<R>(buf1 + (c * T + t) * ld1, L1, q < 0 ? q + ax.n_in : q);
+        v = cscale<R>(v, half_weight_root<R>(ax, g, col, false));
+        const long long idx = (((long long)(c0 + c) * ax.mid + m) * ax.n_out + k) * ax.inner + col;
+        Sout[idx] = v;
+        if (partials) {
+          const cplx<R> p = aux[idx];
+          dot += p.x * v.x + p.y * v.y;
+        }
+      });
+    }
     if (partials) {
       // the line buffers are read: their first bytes take the warp sums (no
       // static shared memory, so the whole dynamic allowance stays usable)
@@ -1836,6 +1908,251 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_last_p2(cplx<R>*
   }
 }
 
+// ---------------------------------------------------------------------------
+// Integration pass with register-resident 512-point lines (FP32, isotropic
+// coefficient, band within a quarter of the line: the spheres configuration).
+//
+// One warp owns one pair line Z = X_a + i X_b at a time and keeps it in
+// registers, 16 complex values per lane:
+//  * frequency distribution: lane 2 k1 + h, register r holds Z[k1 + 16 h + 32 r]
+//    (k1 < 16, h < 2, r < 16); the band |q| < n2h <= 128 lives in registers
+//    0..3 and 12..15, the others are zero;
+//  * space distribution: lane l, register j holds z[32 j + l].
+// 512 = 16 x 32: a 16-point DFT in registers, the twiddles W512^(l k1), a
+// transpose through a padded per-warp tile in shared memory, a radix-2 step
+// between lane pairs (shuffles) and a second 16-point DFT in registers.
+// Against the shared-memory cores each value crosses shared memory once per
+// transform and no block barrier is needed.  The coefficient row lives in
+// registers (lane l, register j: a[32 j + l]).
+// ---------------------------------------------------------------------------
+constexpr int kR512Warps = 8;            // warps per CTA
+constexpr int kR512Tile = 16 * 34;       // transpose tile per warp (complex)
+
+// tile slot of element (k1, l): rows of 34, the two lane halves 17 apart, so
+// both transpose directions are free of bank conflicts
+__device__ __forceinline__ int r512_slot(int k1, int l) { return 34 * k1 + 17 * (l >> 4) + (l & 15); }
+
+// W32^r for r < 16 (compile-time after unrolling)
+__device__ __forceinline__ float2 w32f(int r) {
+  const float c[16] = {1.f, 0.98078528040323044912f, 0.92387953251128675613f, 0.83146961230254523708f,
+                       0.70710678118654752440f, 0.55557023301960222474f, 0.38268343236508977173f,
+                       0.19509032201612826785f, 0.f, -0.19509032201612826785f, -0.38268343236508977173f,
+                       -0.55557023301960222474f, -0.70710678118654752440f, -0.83146961230254523708f,
+                       -0.92387953251128675613f, -0.98078528040323044912f};
+  const float sn[16] = {0.f, 0.19509032201612826785f, 0.38268343236508977173f, 0.55557023301960222474f,
+                        0.70710678118654752440f, 0.83146961230254523708f, 0.92387953251128675613f,
+                        0.98078528040323044912f, 1.f, 0.98078528040323044912f, 0.92387953251128675613f,
+                        0.83146961230254523708f, 0.70710678118654752440f, 0.55557023301960222474f,
+                        0.38268343236508977173f, 0.19509032201612826785f};
+  return make_float2(c[r], -sn[r]);
+}
+
+// inverse transform of one pair line: frequency distribution in v, space
+// distribution out (unnormalised)
+__device__ __forceinline__ void r512_inverse(float2 (&v)[16], float2* tile, const float2* twt,
+                                             int lane) {
+  // 16-point inverse DFT over the registers (band: inputs 0..3, 12..15)
+#pragma unroll
+  for (int r = 0; r < 16; ++r) v[r].y = -v[r].y;
+  dft16<float, true>(v);
+#pragma unroll
+  for (int r = 0; r < 16; ++r) v[r].y = -v[r].y;
+  // odd lanes: times W32^(-l'), then the radix-2 step between lane pairs
+  const bool odd = lane & 1;
+  if (odd) {
+#pragma unroll
+    for (int r = 1; r < 16; ++r) v[r] = cmulc<float>(v[r], w32f(r));
+  }
+  const float sg = odd ? -1.f : 1.f;
+#pragma unroll
+  for (int r = 0; r < 16; ++r) {
+    const float px = __shfl_xor_sync(0xffffffffu, v[r].x, 1);
+    const float py = __shfl_xor_sync(0xffffffffu, v[r].y, 1);
+    v[r] = make_float2(fmaf(sg, v[r].x, px), fmaf(sg, v[r].y, py));
+  }
+  // transpose: lane 2 k1 + g register l' holds Y[l' + 16 g][k1]
+  const int k1 = lane >> 1, g = lane & 1;
+#pragma unroll
+  for (int r = 0; r < 16; ++r) tile[r512_slot(k1, r + 16 * g)] = v[r];
+  __syncwarp();
+#pragma unroll
+  for (int r = 0; r < 16; ++r) v[r] = tile[r512_slot(r, lane)];
+  __syncwarp();
+  // W512^(-l k1), then the 16-point inverse DFT over k1
+#pragma unroll
+  for (int r = 1; r < 16; ++r) v[r] = cmulc<float>(v[r], twt[r * 32 + lane]);
+#pragma unroll
+  for (int r = 0; r < 16; ++r) v[r].y = -v[r].y;
+  dft16<float>(v);
+#pragma unroll
+  for (int r = 0; r < 16; ++r) v[r].y = -v[r].y;
+}
+
+// forward transform: space distribution in v, frequency distribution out
+__device__ __forceinline__ void r512_forward(float2 (&v)[16], float2* tile, const float2* twt,
+                                             int lane) {
+  dft16<float>(v);
+#pragma unroll
+  for (int r = 1; r < 16; ++r) v[r] = cmul<float>(v[r], twt[r * 32 + lane]);
+#pragma unroll
+  for (int r = 0; r < 16; ++r) tile[r512_slot(r, lane)] = v[r];
+  __syncwarp();
+  const int k1 = lane >> 1, g = lane & 1;
+#pragma unroll
+  for (int r = 0; r < 16; ++r) v[r] = tile[r512_slot(k1, r + 16 * g)];
+  __syncwarp();
+  const bool odd = lane & 1;
+  const float sg = odd ? -1.f : 1.f;
+#pragma unroll
+  for (int r = 0; r < 16; ++r) {
+    const float px = __shfl_xor_sync(0xffffffffu, v[r].x, 1);
+    const float py = __shfl_xor_sync(0xffffffffu, v[r].y, 1);
+    v[r] = make_float2(fmaf(sg, v[r].x, px), fmaf(sg, v[r].y, py));
+  }
+  if (odd) {
+#pragma unroll
+    for (int r = 1; r < 16; ++r) v[r] = cmul<float>(v[r], w32f(r));
+  }
+  dft16<float>(v);
+}
+
+// Per-warp shared memory of k_band_last_r512 (float2 units): the transpose
+// tile, two staging buffers for a pair line's band spectra (2 x 128 complex
+// each) and two for coefficient rows (512 floats each).
+constexpr int kR512Stage = 2 * 128;
+constexpr int kR512WarpSmem = kR512Tile + 2 * kR512Stage + 2 * 256;
+__host__ __device__ constexpr size_t r512_smem_bytes() {
+  return (size_t)(16 * 32 + kR512Warps * kR512WarpSmem) * sizeof(float2);
+}
+
+// S: band spectra [C][nrows][n2h] (in place); A: isotropic coefficient
+// [nrows][512]; tw: W512^k, k < 512.  Requires n2h <= 128 and 2 n2h - 1 <=
+// n2_solve + 1 (the band of the solve grid).  Each warp walks its pair lines
+// (row by row, the np pair lines of a row in turn) and copies the next pair
+// line's spectra (and, at a new row, the next coefficient row) into shared
+// memory with cp.async while it transforms the current one.  A template
+// instantiated for float only, so the FP64 translation unit compiles none of it.
+template <typename R>
+__global__ void __launch_bounds__(32 * kR512Warps, 2) k_band_last_r512(
+    float2* __restrict__ S, const float* __restrict__ A, const __grid_constant__ GridDims g,
+    long long nrows, int n2h, int n2_solve, const float2* __restrict__ tw, float cs,
+    const int* __restrict__ all_done) {
+  static_assert(sizeof(R) == 4, "FP32 lines");
+  if (all_done && *all_done) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* twt = reinterpret_cast<float2*>(smem_raw);   // W512^(l k1) at [k1][l]
+  for (int e = threadIdx.x; e < 16 * 32; e += blockDim.x) twt[e] = tw[(e & 31) * (e >> 5)];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float2* wsm = twt + 16 * 32 + warp * kR512WarpSmem;
+  float2* tile = wsm;
+  float2* stg = wsm + kR512Tile;                                            // [2][2][128]
+  float* cst = reinterpret_cast<float*>(wsm + kR512Tile + 2 * kR512Stage);  // [2][512]
+  const int C = g.L * g.dv;
+  const int np = (C + 1) / 2;
+  const int k1 = lane >> 1, h = lane & 1;
+  const int kl = k1 + 16 * h;
+  const int plane = lane >= 2 ? 33 - lane : lane;   // lane of the frequency -k
+  const long long gw = (long long)blockIdx.x * kR512Warps + warp;
+  const long long nw = (long long)gridDim.x * kR512Warps;
+  const long long nrow_w = gw < nrows ? (nrows - gw + nw - 1) / nw : 0;   // rows of this warp
+  const long long ntask = nrow_w * np;
+  // copy task t (row gw + (t / np) nw, pair line t % np) into buffer t & 1
+  auto prefetch = [&](long long t) {
+    if (t < ntask) {
+      const long long row = gw + (t / np) * nw;
+      const int p = (int)(t % np);
+      const int b = (int)(t & 1);
+      for (int half = 0; half < 2; ++half) {
+        const int c = 2 * p + half;
+        if (c >= C) break;
+        const float2* src = S + ((long long)c * nrows + row) * n2h;
+        float2* dst = stg + (b * 2 + half) * 128;
+        for (int k = lane; k < n2h; k += 32) cp_async_small<8>(dst + k, src + k);
+      }
+      if (p == 0) {
+        const float* src = A + row * 512;
+        float* dst = cst + ((t / np) & 1) * 512;
+        for (int j = lane; j < 128; j += 32) cp_async_16(dst + 4 * j, src + 4 * j);
+      }
+    }
+    cp_async_commit();
+  };
+  prefetch(0);
+  float a[16];
+  for (long long t = 0; t < ntask; ++t) {
+    const long long row = gw + (t / np) * nw;
+    const int p = (int)(t % np);
+    const int b = (int)(t & 1);
+    __syncwarp();       // every lane is done with the buffers of task t - 1
+    prefetch(t + 1);
+    cp_async_wait<1>();
+    __syncwarp();       // task t's copies of every lane are visible
+    if (p == 0) {
+      const float* ar = cst + ((t / np) & 1) * 512;
+#pragma unroll
+      for (int j = 0; j < 16; ++j) a[j] = ar[32 * j + lane] * cs;
+    }
+    const int ca = 2 * p, cb = 2 * p + 1;
+    const bool hb = cb < C;
+    const float2* sa = stg + (b * 2) * 128;
+    const float2* sb = stg + (b * 2 + 1) * 128;
+    float2 v[16];
+#pragma unroll
+    for (int r = 4; r < 12; ++r) v[r] = make_float2(0.f, 0.f);
+    // expand: Z_k = A_k + i B_k, Z_{-q} = conj(A_q) + i conj(B_q)
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int k = kl + 32 * r;
+      float2 za = make_float2(0.f, 0.f), zb = make_float2(0.f, 0.f);
+      if (k < n2h) {
+        const float w = (2 * k < n2_solve) ? 1.f : 0.5f;
+        za = sa[k];
+        zb = hb ? sb[k] : make_float2(0.f, 0.f);
+        za.x *= w; za.y *= w; zb.x *= w; zb.y *= w;
+        if (k == 0 || 2 * k == n2_solve) { za.y = 0.f; zb.y = 0.f; }
+      }
+      v[r] = make_float2(za.x - zb.y, za.y + zb.x);
+      const int q = 512 - (kl + 32 * (15 - r));     // register 15 - r holds -q
+      float2 ma = make_float2(0.f, 0.f), mb = make_float2(0.f, 0.f);
+      if (q < n2h) {
+        const float w = (2 * q < n2_solve) ? 1.f : 0.5f;
+        ma = sa[q];
+        mb = hb ? sb[q] : make_float2(0.f, 0.f);
+        ma.x *= w; ma.y *= w; mb.x *= w; mb.y *= w;
+        if (2 * q == n2_solve) { ma.y = 0.f; mb.y = 0.f; }
+      }
+      v[15 - r] = make_float2(ma.x + mb.y, mb.x - ma.y);
+    }
+    r512_inverse(v, tile, twt, lane);
+    // q = a x cs on both real fields of the pair (the imaginary part is zero
+    // when the line has no second field)
+#pragma unroll
+    for (int j = 0; j < 16; ++j) v[j] = make_float2(a[j] * v[j].x, hb ? a[j] * v[j].y : 0.f);
+    r512_forward(v, tile, twt, lane);
+    // split: X_a = (Z_k + conj Z_-k) / 2, X_b = (Z_k - conj Z_-k) / 2i
+    float2* da = S + ((long long)ca * nrows + row) * n2h;
+    float2* db = S + ((long long)cb * nrows + row) * n2h;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const float mx = __shfl_sync(0xffffffffu, v[15 - r].x, plane);
+      const float my = __shfl_sync(0xffffffffu, v[15 - r].y, plane);
+      float2 zm = make_float2(mx, my);
+      if (lane == 0) zm = v[(16 - r) & 15];   // k = 32 r: -k = 32 (16 - r)
+      const int k = kl + 32 * r;
+      if (k < n2h) {
+        const float2 zk = v[r];
+        float2 xa = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+        float2 xb = make_float2(0.5f * (zk.y + zm.y), 0.5f * (zm.x - zk.x));
+        if (2 * k == n2_solve) { xa.y = 0.f; xb.y = 0.f; }
+        da[k] = xa;
+        if (hb) db[k] = xb;
+      }
+    }
+  }
+  cp_async_wait<0>();
+}
+
 // W_i . u_j cross products per load pair on the solve grid (band energy):
 // partial sums of sum_v sum_c W[i][c] (X[j][c] + delta_cj) (postprocess.py:53-70)
 template <typename R>
@@ -2075,6 +2392,214 @@ __global__ void k_p_update(const R* __restrict__ r, R* __restrict__ p, GridDims 
     const int l = (int)(i / per);
     if (st[l].done) continue;
     p[i] = r[i] + (R)st[l].beta * p[i];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Richardson, Chebyshev and BiCG recurrences over the fused operator
+// (ffthompy/general/solver.py:63-77, 142-285), one component row per CTA row
+// (grid (x, L*dv)) with partial sums in the layout of k_cg_update_comp.
+// Loads whose state is done are left untouched.
+// ---------------------------------------------------------------------------
+// MODE 0 (Richardson): x += omega (b - ax), partial |b - ax|^2;
+// MODE 1 (Chebyshev residual): r = b - ax, partial |r|^2.
+template <typename R, int MODE>
+__global__ void __launch_bounds__(256) k_resid_comp(const R* __restrict__ b,
+                                                    const R* __restrict__ ax,
+                                                    R* __restrict__ out, double omega,
+                                                    double* __restrict__ partials, GridDims g,
+                                                    const LoadState* __restrict__ st,
+                                                    const int* __restrict__ all_done) {
+  if (all_done && *all_done) return;
+  __shared__ double red[8];
+  const int comp = blockIdx.y;
+  const int l = comp / g.dv;
+  double acc = 0.;
+  if (!st[l].done) {
+    const long long off = (long long)comp * g.M;
+    const R w = (R)omega;
+    R sq = R(0);
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < g.M;
+         v += (long long)gridDim.x * blockDim.x) {
+      const R r = b[off + v] - ax[off + v];
+      if (MODE == 0) out[off + v] = out[off + v] + w * r;
+      else out[off + v] = r;
+      sq += r * r;
+    }
+    acc = (double)sq;
+  }
+  double t = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot = 0.;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
+    double* o = partials + ((long long)blockIdx.y * gridDim.x + blockIdx.x) * g.L;
+    for (int k = 0; k < g.L; ++k) o[k] = k == l ? tot : 0.;
+  }
+}
+
+// Chebyshev two-term coefficients of the iteration about to run (its number
+// k = kit + 1), per active load: k = 1: p = 0, w = 1/d; k = 2: p = -(c/d)^2/2,
+// w = 1/(d - c^2/(2d)); then p = -(c^2/4) w^2, w = 1/(d - c^2 w/4) with the
+// previous w (solver.py:250-262).  p -> beta, w -> alpha.
+static __global__ void k_cheb_coef(LoadState* st, int L, double d, double c,
+                                   const int* __restrict__ all_done) {
+  if (all_done && *all_done) return;
+  const int l = threadIdx.x;
+  if (l >= L || st[l].done) return;
+  const int k = st[l].kit + 1;
+  double p, w;
+  if (k == 1) {
+    p = 0.;
+    w = 1. / d;
+  } else if (k == 2) {
+    p = -(1. / 2.) * (c / d) * (c / d);
+    w = 1. / (d - c * c / 2. / d);
+  } else {
+    const double wp = st[l].alpha;
+    p = -(c * c / 4.) * wp * wp;
+    w = 1. / (d - c * c * wp / 4.);
+  }
+  st[l].beta = p;
+  st[l].alpha = w;
+}
+
+// norm_res of every load set to v (Richardson starts from 1e15, solver.py:65-66)
+static __global__ void k_set_norm(LoadState* st, int L, double v) {
+  const int l = threadIdx.x;
+  if (l < L) st[l].norm_res = v;
+}
+
+// Chebyshev start (solver.py:226-236): r0 = sqrt(<r,r>), kept in pap; norm_res
+// = r0 / sqrt(<B,B>); stop at once if norm_res < tol.  rpart: partials of
+// k_resid_comp (nr parts), bpart: of k_dot (nb parts).
+static __global__ void k_cheb_init(const double* __restrict__ rpart, int nr,
+                                   const double* __restrict__ bpart, int nb, LoadState* st, int L,
+                                   double invM, double* __restrict__ res_log, int log_cap) {
+  const int l = threadIdx.x;
+  if (l >= L) return;
+  double sr = 0., sb = 0.;
+  for (int i = 0; i < nr; ++i) sr += rpart[(long long)i * L + l];
+  for (int i = 0; i < nb; ++i) sb += bpart[(long long)i * L + l];
+  LoadState& S = st[l];
+  const double r0 = sqrt(sr * invM);
+  S.pap = r0;
+  S.norm_res = (1.0 / sqrt(sb * invM)) * r0;
+  S.kit = 0;
+  S.alpha = 0.;
+  S.beta = 0.;
+  S.status = isfinite(S.norm_res) ? 0 : 3;
+  S.done = !(S.norm_res > S.tol && S.maxiter > 0) || S.status != 0;
+  if (res_log && log_cap > 0) res_log[l] = S.norm_res;
+}
+
+// Chebyshev update: v = r - p v, x += w v
+template <typename R>
+__global__ void __launch_bounds__(256) k_cheb_update(const R* __restrict__ r, R* __restrict__ v,
+                                                     R* __restrict__ x, GridDims g,
+                                                     const LoadState* __restrict__ st,
+                                                     const int* __restrict__ all_done) {
+  if (all_done && *all_done) return;
+  const int comp = blockIdx.y;
+  const int l = comp / g.dv;
+  if (st[l].done) return;
+  const R p = (R)st[l].beta, w = (R)st[l].alpha;
+  const long long off = (long long)comp * g.M;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < g.M;
+       i += (long long)gridDim.x * blockDim.x) {
+    const R vn = r[off + i] - p * v[off + i];
+    v[off + i] = vn;
+    x[off + i] = x[off + i] + w * vn;
+  }
+}
+
+// Residual norms of Richardson / Chebyshev: norm = sqrt(sum / M) * scale_l
+// (scale: 1, or 1 / r0 held in pap for Chebyshev), kit + 1, the residual log
+// and the stopping test norm > tol && kit < maxiter (solver.py:70-76, 263-281).
+static __global__ void k_fin_norm(const double* __restrict__ partials, int nparts, LoadState* st,
+                                  int L, double invM, int relative, double* __restrict__ res_log,
+                                  int log_cap, int* all_done) {
+  __shared__ double red[8];
+  const int l = blockIdx.x;
+  if (*all_done || st[l].done) return;
+  double s = 0.;
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x) s += partials[(long long)i * L + l];
+  double t = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot = 0.;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
+    LoadState& S = st[l];
+    S.kit += 1;
+    double nrm = sqrt(tot * invM);
+    if (relative) nrm = (1.0 / S.pap) * nrm;
+    S.norm_res = nrm;
+    if (res_log && S.kit < log_cap) res_log[(long long)S.kit * L + l] = nrm;
+    if (!isfinite(nrm)) { S.status = 3; S.done = 1; }
+    if (!(nrm > S.tol && S.kit < S.maxiter)) S.done = 1;
+  }
+}
+
+// BiCG update: x += alpha P, R -= alpha AP, Rs -= alpha AT Ps, partial <R, Rs>
+template <typename R>
+__global__ void __launch_bounds__(256) k_bicg_update(R* __restrict__ x, R* __restrict__ r,
+                                                     R* __restrict__ rs, const R* __restrict__ p,
+                                                     const R* __restrict__ ap,
+                                                     const R* __restrict__ atps,
+                                                     double* __restrict__ partials, GridDims g,
+                                                     const LoadState* __restrict__ st,
+                                                     const int* __restrict__ all_done) {
+  if (all_done && *all_done) return;
+  __shared__ double red[8];
+  const int comp = blockIdx.y;
+  const int l = comp / g.dv;
+  double acc = 0.;
+  if (!st[l].done) {
+    const R a = (R)st[l].alpha;
+    const long long off = (long long)comp * g.M;
+    R sq = R(0);
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < g.M;
+         v += (long long)gridDim.x * blockDim.x) {
+      const long long i = off + v;
+      x[i] = x[i] + a * p[i];
+      const R rn = r[i] - a * ap[i];
+      const R sn = rs[i] - a * atps[i];
+      r[i] = rn;
+      rs[i] = sn;
+      sq += rn * sn;
+    }
+    acc = (double)sq;
+  }
+  double t = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot = 0.;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
+    double* o = partials + ((long long)blockIdx.y * gridDim.x + blockIdx.x) * g.L;
+    for (int k = 0; k < g.L; ++k) o[k] = k == l ? tot : 0.;
+  }
+}
+
+// BiCG directions: P = R + beta P, Ps = Rs + beta Ps
+template <typename R>
+__global__ void __launch_bounds__(256) k_bicg_dirs(const R* __restrict__ r,
+                                                   const R* __restrict__ rs, R* __restrict__ p,
+                                                   R* __restrict__ ps, GridDims g,
+                                                   const LoadState* __restrict__ st,
+                                                   const int* __restrict__ all_done) {
+  if (all_done && *all_done) return;
+  const int comp = blockIdx.y;
+  const int l = comp / g.dv;
+  if (st[l].done) return;
+  const R be = (R)st[l].beta;
+  const long long off = (long long)comp * g.M;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < g.M;
+       i += (long long)gridDim.x * blockDim.x) {
+    p[off + i] = r[off + i] + be * p[off + i];
+    ps[off + i] = rs[off + i] + be * ps[off + i];
   }
 }
 

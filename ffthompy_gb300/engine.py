@@ -88,10 +88,13 @@ class GalerkinPlan:
     integration grid integ >= 2N-1, projection scale prod(2N-1)/prod(N).
     band_cg (band plans): 'spectral' keeps the CG iterates as half spectra of
     N (no transform of the N grid inside an iteration), 'real' as real fields.
+    integ_kernel (band plans): 'register' runs the integration pass with
+    lines held in registers where that kernel applies, 'shared' with the
+    shared-memory line cores.
     """
 
     def __init__(self, N, Y, physics='scalar', nloads=None, band=None, scale=None,
-                 precision='f64', integ=None, band_cg='spectral'):
+                 precision='f64', integ=None, band_cg='spectral', integ_kernel='register'):
         require_cuda()
         self.lib = _lib.load()
         self.N = tuple(int(n) for n in N)
@@ -137,6 +140,11 @@ class GalerkinPlan:
         self.band_cg = band_cg
         _lib.check(self.lib.fhp_plan_set_band_cg(h, 1 if band_cg == 'spectral' else 0),
                    'fhp_plan_set_band_cg')
+        if integ_kernel not in ('register', 'shared'):
+            raise ValueError("integ_kernel must be 'register' or 'shared'")
+        self.integ_kernel = integ_kernel
+        _lib.check(self.lib.fhp_plan_set_integration_kernel(
+            h, 1 if integ_kernel == 'register' else 0), 'fhp_plan_set_integration_kernel')
 
     def __del__(self):
         h = getattr(self, 'handle', None)
@@ -276,6 +284,48 @@ class GalerkinPlan:
                 'res_log': [log[:k + 1, l].copy() for l, k in enumerate(kits)]}
         return x, info
 
+    def solve_other(self, kind, b, x0=None, tol=1e-6, maxiter=1000, proj=1, p0=0., p1=0.):
+        """Richardson ('richardson', p0 = omega), two-term Chebyshev
+        ('chebyshev', eigenvalues in [p0, p1]) or BiCG ('bicg') on the GPU,
+        all loads at once (fhp_richardson_solve / fhp_chebyshev_solve /
+        fhp_bicg_solve).  Returns (x, info) with per-load kit / norm_res /
+        status."""
+        b = self._dev(b)
+        x0p = ctypes.c_void_p(None)
+        if x0 is not None:
+            x0 = self._dev(x0)
+            x0p = self._ptr(x0)
+        x = self.empty()
+        L = self.nloads
+        kit = (ctypes.c_int * L)()
+        nres = (ctypes.c_double * L)()
+        stat = (ctypes.c_int * L)()
+        args = (kit, nres, stat, self._stream())
+        if kind == 'richardson':
+            st = self.lib.fhp_richardson_solve(self.handle, proj, self._ptr(b), x0p, float(p0),
+                                               float(tol), int(maxiter), self._ptr(x), *args)
+        elif kind == 'chebyshev':
+            st = self.lib.fhp_chebyshev_solve(self.handle, proj, self._ptr(b), x0p, float(p0),
+                                              float(p1), float(tol), int(maxiter), self._ptr(x),
+                                              *args)
+        elif kind == 'bicg':
+            st = self.lib.fhp_bicg_solve(self.handle, proj, self._ptr(b), x0p, float(tol),
+                                         int(maxiter), self._ptr(x), *args)
+        else:
+            raise ValueError('unknown solver %s' % kind)
+        _lib.check(st, 'fhp_%s_solve' % kind)
+        return x, {'kit': list(kit), 'norm_res': list(nres), 'status': list(stat)}
+
+    def autotune(self):
+        """Time candidate launch shapes of the operator on this plan and keep
+        the fastest (fhp_plan_autotune; cached per plan geometry).  Returns
+        (choice triple, ms per operator application)."""
+        ch = (ctypes.c_int * 3)()
+        ms = ctypes.c_float()
+        _lib.check(self.lib.fhp_plan_autotune(self.handle, ch, ctypes.byref(ms), self._stream()),
+                   'fhp_plan_autotune')
+        return tuple(ch), float(ms.value)
+
     def energy(self, X, add_macro=True):
         """A_H[i, j] = <A u_i, u_j> over the solve grid (u = X + E if add_macro)."""
         X = self._dev(X)
@@ -413,6 +463,38 @@ class GalerkinPlan:
         return AH, list(kit), list(nres), xh
 
 
+def cg_many(plans, bs, tol=1e-6, maxiter=1000, proj=1):
+    """CG on several plans at once (fhp_cg_solve_many): plan i solves its own
+    loads from bs[i], zero start, with its own scalars and stopping tests; all
+    plans advance together, one CUDA graph per iteration.  Returns
+    [(x_i, info_i)] with info as GalerkinPlan.cg (without residual logs)."""
+    require_cuda()
+    plans = list(plans)
+    if not plans:
+        return []
+    lib = plans[0].lib
+    n = len(plans)
+    bs = [p._dev(b) for p, b in zip(plans, bs)]
+    xs = [p.empty() for p in plans]
+    hs = (ctypes.c_void_p * n)(*[p.handle.value for p in plans])
+    bp = (ctypes.c_void_p * n)(*[b.data_ptr() for b in bs])
+    xp = (ctypes.c_void_p * n)(*[x.data_ptr() for x in xs])
+    tot = sum(p.nloads for p in plans)
+    kit = (ctypes.c_int * tot)()
+    nres = (ctypes.c_double * tot)()
+    stat = (ctypes.c_int * tot)()
+    st = lib.fhp_cg_solve_many(n, hs, int(proj), bp, float(tol), int(maxiter), xp, kit, nres,
+                               stat, plans[0]._stream())
+    _lib.check(st, 'fhp_cg_solve_many')
+    out, off = [], 0
+    for p, x in zip(plans, xs):
+        L = p.nloads
+        out.append((x, {'kit': list(kit[off:off + L]), 'norm_res': list(nres[off:off + L]),
+                        'status': list(stat[off:off + L])}))
+        off += L
+    return out
+
+
 def _fft_plan(grid, ncomp, precision):
     lib = _lib.load()
     h = ctypes.c_void_p()
@@ -499,6 +581,29 @@ def ball_characteristic(N, r, volume, sq, phase):
             stream), 'fhp_ball_characteristic')
     finally:
         lib.fhp_plan_destroy(h)
+    return out
+
+
+def separable_char(N, re, im=None):
+    """Product of per-axis factors on grid N on the GPU (fhp_separable_char):
+    prod_a re_a[x_a], or with im the real part of prod_a (re_a + i im_a)[x_a],
+    rounded as NumPy's outer products round them.  re, im: sequences of
+    per-axis host vectors.  Returns a float64 CUDA tensor of shape N."""
+    require_cuda()
+    lib = _lib.load()
+    N = tuple(int(n) for n in N)
+    out = torch.empty(N, dtype=torch.float64, device='cuda')
+    r = np.ascontiguousarray(np.concatenate([np.asarray(v, dtype=np.float64) for v in re]))
+    dp = ctypes.POINTER(ctypes.c_double)
+    ip = None
+    if im is not None:
+        i_ = np.ascontiguousarray(np.concatenate([np.asarray(v, dtype=np.float64) for v in im]))
+        ip = i_.ctypes.data_as(dp)
+    n = (ctypes.c_int * len(N))(*N)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _lib.check(lib.fhp_separable_char(len(N), n, r.ctypes.data_as(dp), ip,
+                                      ctypes.c_void_p(out.data_ptr()), stream),
+               'fhp_separable_char')
     return out
 
 

@@ -6,9 +6,11 @@ the whole solve runs on the GPU in one library call (fhp_cg_solve: batched
 CG with FP64 reductions, absolute stopping test sqrt(<R,R>) <= tol,
 solver.py:80-139).  Other operators use the same CG recurrence written with
 Tensor arithmetic on the device.  'richardson' / 'iterative' (63-77),
-'bicg' (142-204) and 'chebyshev' (206-285) run their recurrences with device
-Tensor arithmetic around the fused operator, one library call per
-application.
+'bicg' (142-204) and 'chebyshev' (206-285) over a fused Operator run in one
+library call each (fhp_richardson_solve, fhp_bicg_solve,
+fhp_chebyshev_solve): the recurrences in fused kernels with per-load scalars
+on the device and one CUDA-graph replay per iteration, no host
+synchronisation per scalar.  Other operators use Tensor arithmetic.
 """
 import time
 
@@ -93,8 +95,28 @@ def _cg_generic(Afun, B, x0, par, callback):
     return x, res
 
 
+def _fused(Afun, B):
+    return isinstance(Afun, Operator) and Afun.kind == 'GA' and isinstance(B, Tensor)
+
+
+def _device_solve(kind, Afun, B, x0, par, callback, p0=0., p1=0., maxiter=None):
+    plan = Afun.plan()
+    zero_start = float(x0.data.abs().max()) == 0.0
+    xd, info = plan.solve_other(kind, B.data[None], None if zero_start else x0.data[None],
+                                tol=par['tol'],
+                                maxiter=par['maxiter'] if maxiter is None else maxiter,
+                                proj=Afun.projection.proj, p0=p0, p1=p1)
+    x = x0.copy(name='x', val=xd[0])
+    if callback is not None and not isinstance(callback, CallBack):
+        callback(x)
+    return x, {'kit': info['kit'][0], 'norm_res': info['norm_res'][0]}
+
+
 def richardson(Afun, B, x0, par=None, callback=None):
     """solver.py:63-77."""
+    if _fused(Afun, B) and par.get('norm', 'L2') in ('L2', 2):
+        par = _defaults(par)
+        return _device_solve('richardson', Afun, B, x0, par, callback, p0=1. / par['alpha'])
     omega = 1. / par['alpha']
     res = {'norm_res': 1e15, 'kit': 0}
     x = x0
@@ -112,9 +134,12 @@ def BiCG(Afun, ATfun, B, x0, par=None, callback=None):
     """BiConjugate gradients, solver.py:142-204 (shadow residual updated with
     ATfun, stop on sqrt(<R, Rs>) <= tol).  The reference forms <R, Rs> as
     R.T*Rs, which its Tensor class does not support; here it is the scalar
-    product.  Each Afun / ATfun application of a fused Operator is one call
-    into the CUDA library; the vector updates are device Tensor arithmetic."""
+    product.  With a fused Operator as its own transpose (the symmetric
+    G o A) the whole recurrence runs in the CUDA library (fhp_bicg_solve);
+    otherwise with Tensor arithmetic."""
     par = _defaults(par)
+    if _fused(Afun, B) and ATfun is Afun and 'scal' not in par:
+        return _device_solve('bicg', Afun, B, x0, par, callback)
     scal = par.get('scal', lambda X, Y: X * Y)
     x = x0
     R = B - Afun(x0)
@@ -152,6 +177,9 @@ def cheby2TERM(A, B, x0, M=None, par=None, callback=None):
     if 'eigrange' not in par:
         raise NotImplementedError('It is necessary to calculate eigenvalues.')
     Egv = par['eigrange']
+    if _fused(A, B) and M is None:
+        return _device_solve('chebyshev', A, B, x0, par, callback, p0=Egv[0], p1=Egv[1],
+                             maxiter=int(min(par['maxit'], 2 ** 31 - 1)))
     res = {'kit': 0}
     bnrm2 = float(B * B) ** 0.5
     Ib = 1.0 / bnrm2

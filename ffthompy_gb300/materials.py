@@ -11,17 +11,19 @@ inclusions {'inclusions', 'positions', 'params', 'vals', 'Y', 'order', 'P'}.
   1: Fourier coefficients of a P-voxel image weighted by the cell shape
   function, materials.py:77-110).
 
-Coefficient assembly runs once per problem. On a GPU the grid-based Ga
-coefficient (fhp_ga_grid_coefficient), the dual inverse
-(fhp_coefficient_inverse), the Ga characteristic function of balls
-(fhp_ball_characteristic), their GaNi topologies (fhp_ball_topology) and the
-sum over inclusions of the exact-integration coefficient
-(fhp_outer_accumulate) run in the CUDA library. Boxes and pyramids use separable host transforms; the
-rest runs on the host (NumPy). The result is a Tensor with origin 0 on the
-GPU.
+Coefficient assembly runs once per problem, on the GPU (it needs CUDA, as
+the solve does; there is no host fallback).  Topologies and characteristic
+functions are built at origin 0 on the device: boxes and pyramids from
+their per-axis factors (fhp_separable_char; the per-axis factors are 1D
+sums and 1D transforms formed on the host), balls by fhp_ball_topology /
+fhp_ball_characteristic; sums over inclusions (fhp_outer_accumulate), the
+dual inverse (fhp_coefficient_inverse) and the grid-based Ga coefficient
+(fhp_ga_grid_coefficient) run in the CUDA library.  Results are
+bit-identical to the NumPy evaluation of the reference's expressions except
+the transforms (ball characteristic functions, grid-based Ga), which agree to
+roundoff.  A 'fun' material's values come from the user's host function and
+are uploaded.  The result is a Tensor with origin 0 on the GPU.
 """
-import itertools
-
 import numpy as np
 import scipy.special as sps
 
@@ -40,20 +42,6 @@ def _outer_axes(N, vecs):
     for i, v in enumerate(vecs):
         out = out * v.reshape([N[i] if j == i else 1 for j in range(d)])
     return out
-
-
-def _centered_fft(x, shape):
-    """Centred, 1/prod(N)-normalised DFT of a real grid image (fft.py:4-9)."""
-    ax = tuple(range(x.ndim - len(shape), x.ndim))
-    X = np.fft.fftn(np.fft.ifftshift(x, axes=ax), s=tuple(shape), axes=ax)
-    return np.fft.fftshift(X, axes=ax) / np.prod(shape)
-
-
-def _centered_ifft_real(X, shape):
-    """Real part of the centred inverse DFT times prod(N) (fft.py:11-16)."""
-    ax = tuple(range(X.ndim - len(shape), X.ndim))
-    x = np.fft.ifftn(np.fft.ifftshift(X, axes=ax), s=tuple(shape), axes=ax)
-    return np.fft.fftshift(x, axes=ax).real * np.prod(shape)
 
 
 def get_weights_con(h, Nbar, Y):
@@ -91,28 +79,15 @@ def get_weights_circ(r, Nbar, Y):
     return W / np.prod(Y)
 
 
-def _centered_ifft_real_separable(vecs, shape):
-    """_centered_ifft_real of the outer product of per-axis spectra vecs[i]:
-    the d-dimensional transform of a separable product is the product of the
-    1D transforms, so the cost is O(d N) transforms and one outer product
-    (the real part is formed from the complex partial products)."""
-    cs = [np.fft.fftshift(np.fft.ifft(np.fft.ifftshift(X))) * int(n)
-          for X, n in zip(vecs, shape)]
-    t = cs[0]
-    for c in cs[1:-1]:
-        t = np.multiply.outer(t, c)
-    if len(cs) == 1:
-        return t.real.copy()
-    last = cs[-1]
-    return np.multiply.outer(t.real, last.real) - np.multiply.outer(t.imag, last.imag)
-
-
-def _separable_char(kind, h, pos, N, Y):
-    """Characteristic function of a box ('cube') or bilinear pyramid on grid N
-    from its separable spectrum: per axis the phase of get_shift_inclusion
-    (integer frequencies in FFT order, as the reference pairs them) times the
-    centred 1D weight of get_weights_con / get_weights_lin; 1/|Y| once.
-    Equals _centered_ifft_real(SS * W, N) up to roundoff."""
+def _separable_axis_values(kind, h, pos, N, Y):
+    """Per-axis factors of the characteristic function of a box ('cube') or
+    bilinear pyramid on grid N (centred order, complex): per axis the phase
+    of get_shift_inclusion (integer frequencies in FFT order, as the
+    reference pairs them) times the centred 1D weight of get_weights_con /
+    get_weights_lin, 1/|Y| on axis 0, transformed by the centred 1D inverse
+    DFT.  The d-dimensional function is the real part of their product
+    (the transform of a separable spectrum is the product of the 1D
+    transforms), as the reference's centred inverse DFT of SS * W forms it."""
     N = np.asarray(N, dtype=np.int64)
     Zr = Grid.get_ZNl(N)
     Zc = Grid.get_ZNl(N, fft_form='c')
@@ -126,7 +101,22 @@ def _separable_char(kind, h, pos, N, Y):
             np.exp(-2j * np.pi * pos[i] * Zr[i] / Y[i])
         vecs.append(ph * w)
     vecs[0] = vecs[0] / np.prod(Y)
-    return _centered_ifft_real_separable(vecs, N)
+    return [np.fft.fftshift(np.fft.ifft(np.fft.ifftshift(X))) * int(n)
+            for X, n in zip(vecs, N)]
+
+
+def _separable_dev(N, vecs):
+    """Product of per-axis factors on the GPU (fhp_separable_char), origin 0:
+    real tables give prod_a v_a[x_a], complex ones the real part of the
+    product, each as NumPy's outer products round them."""
+    from .engine import separable_char
+    N = np.asarray(N, dtype=np.int64)
+    if N.size not in (2, 3):
+        raise NotImplementedError('grids of 2 or 3 dimensions')
+    vecs = [np.asarray(v)[_o0(n)] for v, n in zip(vecs, N)]
+    if np.iscomplexobj(vecs[0]):
+        return separable_char(N, [v.real for v in vecs], [v.imag for v in vecs])
+    return separable_char(N, vecs, None)
 
 
 def get_shift_inclusion(N, h, Y):
@@ -221,13 +211,19 @@ def ga_axis_tables(P, Nbar, h, Y, order, target=None):
     return np.concatenate(srcs).astype(np.int32), np.concatenate(ws)
 
 
-def _ball_char_gpu(r, pos, N, Y):
-    """get_shape_functions' ball characteristic function on the GPU
-    (fhp_ball_characteristic), centred like _centered_ifft_real(SS * W, N).
-    The tables pair what the reference pairs position by position: the
-    weight of centred frequency i - N/2 (get_weights_circ, materials.py:
-    392-425) with the phase of get_shift_inclusion at the same array position,
-    whose frequencies are in FFT order (materials.py:317-330)."""
+def _o0(n):
+    """Gather indices of np.fft.ifftshift on an axis of n points: the
+    origin-0 array's entry j is the centred array's entry _o0(n)[j]."""
+    return np.fft.ifftshift(np.arange(int(n)))
+
+
+def _ball_char_dev(r, pos, N, Y):
+    """Ga characteristic function of a ball on the GPU
+    (fhp_ball_characteristic), origin 0.  The tables pair what the reference
+    pairs position by position: the weight of centred frequency i - N/2
+    (get_weights_circ, materials.py:392-425) with the phase of
+    get_shift_inclusion at the same array position, whose frequencies are in
+    FFT order (materials.py:317-330)."""
     from .engine import ball_characteristic
     N = np.asarray(N, dtype=np.int64)
     Y = np.asarray(Y, dtype=np.float64)
@@ -236,16 +232,7 @@ def _ball_char_gpu(r, pos, N, Y):
     Zf = Grid.get_ZNl(N)
     sq = [(Zc[i] / Y[i]) ** 2 for i in range(N.size)]
     ph = [np.exp(-2j * np.pi * h[i] * Zf[i] / Y[i]) for i in range(N.size)]
-    out = ball_characteristic(N, r, float(np.prod(Y)), sq, ph)
-    return np.fft.fftshift(out.cpu().numpy())
-
-
-def _gpu_available():
-    try:
-        import torch
-        return torch.cuda.is_available()
-    except ImportError:
-        return False
+    return ball_characteristic(N, r, float(np.prod(Y)), sq, ph)
 
 
 def ga_grid_coefficient_gpu(vals, P, Nbar, Y, order, target=None):
@@ -341,80 +328,100 @@ class Material:
             self.conf['positions'][ii] = np.asarray(self.conf['positions'][ii]) % self.Y
 
     # -- nodal evaluation -------------------------------------------------------
-    def get_topologies(self, coord):
-        """Characteristic functions at the nodes, summed over the 3^d periodic
-        images of each inclusion (materials.py:212-301).  coord are the
-        tensor-product nodes of Grid.get_coordinates."""
+    @staticmethod
+    def _grid_axes(coord):
+        """Per-axis node coordinates of tensor-product nodes (Grid.get_coordinates)."""
+        d = coord.shape[0]
+        return [np.asarray(coord[a][(0,) * a + (slice(None),) + (0,) * (d - a - 1)],
+                           dtype=np.float64) for a in range(d)]
+
+    def _topologies_dev(self, axes, origin0=True):
+        """Characteristic functions at the nodes (per-axis coordinates axes,
+        centred order), summed over the 3^d periodic images of each inclusion
+        (materials.py:212-301), on the GPU; origin0 returns them ifftshift-ed.
+        Boxes and pyramids are products over the axes, so their sum over the
+        images is the product of per-axis sums over 3 images."""
+        import torch
+        from .engine import ball_topology, outer_accumulate, require_cuda
+        require_cuda()
         incs = self.conf['inclusions']
         params, poss = self.conf['params'], self.conf['positions']
-        d = coord.shape[0]
-        grid = coord.shape[1:]
-        images = list(itertools.product((-1, 0, 1), repeat=d))
-        # boxes and pyramids are products over the axes, so their sum over the
-        # 3^d periodic images is the product of per-axis sums over 3 images
-        axes = [coord[a][(0,) * a + (slice(None),) + (0,) * (d - a - 1)] for a in range(d)]
-
-        def outer(vs):
-            t = vs[0]
-            for v in vs[1:]:
-                t = np.multiply.outer(t, v)
-            return t.reshape(grid)
+        d = len(axes)
+        grid = tuple(len(a) for a in axes)
+        perm = [_o0(n) if origin0 else np.arange(n) for n in grid]
         topos = []
         for ii, kind in enumerate(incs):
-            if kind in inclusion_keys['cube']:
+            if kind in inclusion_keys['cube'] or kind in inclusion_keys['pyramid']:
                 p = np.asarray(params[ii], dtype=np.float64)
                 x0 = np.asarray(poss[ii], dtype=np.float64)
+                cube = kind in inclusion_keys['cube']
                 vs = []
                 for a in range(d):
                     va = np.zeros(grid[a])
                     for im in (-1, 0, 1):
-                        u = axes[a] - x0[a] + self.Y[a] * im
-                        va += (u > -p[a] / 2) & (u <= p[a] / 2)
-                    vs.append(va)
-                t = outer(vs)
-            elif kind in inclusion_keys['ball'] and _gpu_available() and d in (2, 3):
-                from .engine import ball_topology
-                t = ball_topology(axes, np.asarray(poss[ii], dtype=np.float64), self.Y,
-                                  params[ii] / 2).cpu().numpy()
+                        if cube:
+                            u = axes[a] - x0[a] + self.Y[a] * im
+                            va += (u > -p[a] / 2) & (u <= p[a] / 2)
+                        else:  # the reference shifts pyramids by 2*Y per image
+                            u = axes[a] - x0[a] + 2 * self.Y[a] * im
+                            va += np.maximum(1 - np.abs(u) / (p[a] / 2.), 0.)
+                    vs.append(va[perm[a]])
+                from .engine import separable_char
+                t = separable_char(grid, vs, None)
             elif kind in inclusion_keys['ball']:
-                x0 = np.asarray(poss[ii], dtype=np.float64)
-                t = np.zeros(grid)
-                for im in images:
-                    r2 = np.zeros(grid)
-                    for a in range(d):
-                        r2 += (coord[a] - x0[a] - self.Y[a] * im[a]) ** 2
-                    t += np.sqrt(r2) < params[ii] / 2
-            elif kind in inclusion_keys['pyramid']:
-                p = np.asarray(params[ii], dtype=np.float64)
-                x0 = np.asarray(poss[ii], dtype=np.float64)
-                vs = []
-                for a in range(d):  # the reference shifts pyramids by 2*Y per image
-                    va = np.zeros(grid[a])
-                    for im in (-1, 0, 1):
-                        u = axes[a] - x0[a] + 2 * self.Y[a] * im
-                        va += np.maximum(1 - np.abs(u) / (p[a] / 2.), 0.)
-                    vs.append(va)
-                t = outer(vs)
+                t = ball_topology([ax[pm] for ax, pm in zip(axes, perm)],
+                                  np.asarray(poss[ii], dtype=np.float64), self.Y, params[ii] / 2)
             elif kind == 'otherwise':
-                t = np.ones(grid) - sum(topos) if topos else np.ones(grid)
-                if not (t >= 0).all():
+                # np.ones(grid) - sum(topos), with Python's left-to-right sum
+                t = torch.ones(grid, dtype=torch.float64, device='cuda')
+                if topos:
+                    acc = torch.zeros(grid, dtype=torch.float64, device='cuda')
+                    for prev in topos:
+                        outer_accumulate(acc.view(1, -1), [1.], prev)
+                    outer_accumulate(t.view(1, -1), [-1.], acc)
+                if bool((t < 0).any()):
                     raise NotImplementedError('Overlapping inclusions!')
             elif kind == 'all':
-                t = np.ones(grid)
+                t = torch.ones(grid, dtype=torch.float64, device='cuda')
             else:
                 raise NotImplementedError('Inclusion (%s) is not implemented.' % kind)
-            topos.append(t)
+            topos.append(t.contiguous())
         return topos
 
+    def _nodal_dev(self, axes, origin0=True):
+        """Nodal coefficient (d_v, d_v) + grid of an inclusion material on the
+        GPU: sum over inclusions of vals (x) topology, as evaluate."""
+        import torch
+        from .engine import outer_accumulate
+        vals = self.conf['vals']
+        shape = tuple(np.shape(vals[0]))
+        grid = tuple(len(a) for a in axes)
+        A = torch.zeros(shape + grid, dtype=torch.float64, device='cuda')
+        flat = A.view(int(np.prod(shape)), -1)
+        for v, t in zip(vals, self._topologies_dev(axes, origin0)):
+            outer_accumulate(flat, np.asarray(v, dtype=np.float64), t)
+        return A
+
+    def get_topologies(self, coord):
+        """Characteristic functions at the nodes coord (tensor-product nodes of
+        Grid.get_coordinates), centred, as host arrays (materials.py:212-301);
+        computed on the GPU."""
+        return [t.cpu().numpy() for t in self._topologies_dev(self._grid_axes(coord), False)]
+
     def evaluate(self, coord):
-        """Coefficient values (d_v, d_v) + grid at the nodes, centred origin."""
+        """Coefficient values (d_v, d_v) + grid at the nodes, centred origin
+        (host array; inclusion materials are evaluated on the GPU)."""
         if 'fun' in self.conf:
             return np.asarray(self.conf['fun'](coord), dtype=np.float64)
-        vals = self.conf['vals']
-        A = np.zeros(np.shape(vals[0]) + coord.shape[1:])
-        for v, t in zip(vals, self.get_topologies(coord)):
-            A += np.multiply.outer(np.asarray(v, dtype=np.float64), t)
-        return A
+        return self._nodal_dev(self._grid_axes(coord), False).cpu().numpy()
+
+    def _nodal_origin0(self, N):
+        """Nodal values on grid N with origin 0 as a CUDA tensor, and whether
+        they are already shifted (inclusions: built shifted on the GPU; 'fun':
+        the user's host values, centred)."""
+        if 'fun' in self.conf:
+            return self.evaluate(Grid.get_coordinates(N, self.Y)), False
+        return self._nodal_dev(Grid.get_axes(N, self.Y), True), True
 
     @staticmethod
     def _origin0(val, name):
@@ -422,69 +429,83 @@ class Material:
         return Tensor(name=name, val=val, order=2, multype=21, origin=0)
 
     def get_A_GaNi(self, N, primaldual='primal'):
-        A = self.evaluate(Grid.get_coordinates(N, self.Y))
+        from .engine import coefficient_inverse, require_cuda
+        require_cuda()
+        N = np.asarray(N, dtype=np.int64)
+        A, shifted = self._nodal_origin0(N)
         name = 'A_GaNi'
         if primaldual == 'dual':
             name = 'inv(A_GaNi)'
-            if _gpu_available():
-                from .engine import coefficient_inverse
-                out = Tensor(name=name, val=coefficient_inverse(A, shift=True), order=2,
-                             multype=21, origin=0)
-                out.Y = self.Y
-                return out
-            A = get_inverse(A)
-        out = self._origin0(A, name)
+            out = Tensor(name=name, val=coefficient_inverse(A, shift=not shifted), order=2,
+                         multype=21, origin=0)
+        elif shifted:
+            out = Tensor(name=name, val=A, order=2, multype=21, origin=0)
+        else:
+            out = self._origin0(A, name)
         out.Y = self.Y
         return out
 
-    def get_shape_functions(self, N2):
+    def _shape_functions_dev(self, N2, origin0=True):
+        """Ga characteristic functions of the inclusions on grid N2
+        (materials.py:125-169) as CUDA tensors (origin 0, or centred)."""
+        import torch
+        from .engine import outer_accumulate, require_cuda
+        require_cuda()
         N2 = np.asarray(N2, dtype=np.int64)
         incs = self.conf['inclusions']
         params, poss = self.conf['params'], self.conf['positions']
+        grid = tuple(int(n) for n in N2)
         chars = []
-        SS = None
-        shift_pos = None   # the phase of the last inclusion with a position (as SS)
+        shift_pos = None   # the position of the last inclusion that has one
         for ii, incl in enumerate(incs):
             if isinstance(poss[ii], np.ndarray):
                 shift_pos = np.asarray(poss[ii], dtype=np.float64)
-                SS = None
-            if incl in inclusion_keys['cube']:
-                # separable spectrum: 1D transforms and an outer product
-                chars.append(_separable_char('cube', np.asarray(params[ii], dtype=np.float64),
-                                             shift_pos, N2, self.Y))
+            if incl in inclusion_keys['cube'] or incl in inclusion_keys['pyramid']:
+                cube = incl in inclusion_keys['cube']
+                h = np.asarray(params[ii], dtype=np.float64) / (1. if cube else 2.)
+                vecs = _separable_axis_values('cube' if cube else 'pyramid', h, shift_pos, N2,
+                                              self.Y)
+                c = _separable_dev(N2, vecs)
             elif incl in inclusion_keys['ball']:
                 r = params[ii] / 2
-                if r != 0 and _gpu_available() and np.all(N2 % 2 == 1) and N2.size in (2, 3):
-                    chars.append(_ball_char_gpu(r, shift_pos, N2, self.Y))
-                    continue
-                if SS is None:
-                    SS = get_shift_inclusion(N2, shift_pos, self.Y)
-                W = np.zeros(tuple(N2)) if r == 0 else get_weights_circ(r, N2, self.Y)
-                chars.append(_centered_ifft_real(SS * W, N2))
-            elif incl in inclusion_keys['pyramid']:
-                chars.append(_separable_char('pyramid', np.asarray(params[ii], dtype=np.float64) / 2.,
-                                             shift_pos, N2, self.Y))
+                if r == 0:
+                    c = torch.zeros(grid, dtype=torch.float64, device='cuda')
+                elif np.all(N2 % 2 == 1) and N2.size in (2, 3):
+                    c = _ball_char_dev(r, shift_pos, N2, self.Y)
+                else:
+                    raise NotImplementedError('ball inclusions need an odd grid of 2 or 3 '
+                                              'dimensions (exact integration grids 2N-1 are)')
             elif incl == 'all':
-                chars.append(np.ones(tuple(N2)))
+                c = torch.ones(grid, dtype=torch.float64, device='cuda')
             elif incl == 'otherwise':
-                chars.append(np.ones(tuple(N2)) - sum(chars) if chars else np.ones(tuple(N2)))
+                c = torch.ones(grid, dtype=torch.float64, device='cuda')
+                if chars:
+                    acc = torch.zeros(grid, dtype=torch.float64, device='cuda')
+                    for prev in chars:
+                        outer_accumulate(acc.view(1, -1), [1.], prev)
+                    outer_accumulate(c.view(1, -1), [-1.], acc)
             else:
                 raise NotImplementedError('The inclusion (%s) is not supported!' % incl)
+            chars.append(c.contiguous())
+        if not origin0:
+            # the centred order of the public get_shape_functions
+            chars = [torch.fft.fftshift(c) for c in chars]
         return chars
+
+    def get_shape_functions(self, N2):
+        """Characteristic functions on grid N2, centred (host arrays), as the
+        reference returns them (materials.py:125-169); computed on the GPU."""
+        return [c.cpu().numpy() for c in self._shape_functions_dev(N2, origin0=False)]
 
     def _get_A_Ga_on(self, Nbar, primaldual, order, P, grid):
         grid = tuple(int(g) for g in grid)
         if order == -1:
             order = self.conf.get('order', -1)
-        if order in (0, 1, 'constant', 'bilinear') and _gpu_available() and \
-                np.all(Nbar % 2 == 1):
+        if order in (0, 1, 'constant', 'bilinear') and np.all(Nbar % 2 == 1):
             if P is None and 'P' in self.conf:
                 P = self.conf['P']
             P = np.asarray(P, dtype=np.int64)
-            vals = self.evaluate(Grid.get_coordinates(P, self.Y))
-            if primaldual == 'dual':
-                from .engine import coefficient_inverse
-                vals = coefficient_inverse(vals, shift=True)
+            vals = self._grid_image(P, primaldual)
             out = Tensor(name='A_Ga_o{0}_P{1}'.format(order, np.array(P).max()),
                          val=ga_grid_coefficient_gpu(vals, P, Nbar, self.Y, order, target=grid),
                          order=2, multype=21, origin=0)
@@ -496,9 +517,21 @@ class Material:
         out.Y = self.Y
         return out
 
+    def _grid_image(self, P, primaldual):
+        """The P-voxel image of a grid-based Ga coefficient for
+        ga_grid_coefficient_gpu: origin-0 CUDA values (inverted per voxel for
+        the dual), or the centred host values of a 'fun' material's primal."""
+        from .engine import coefficient_inverse
+        vals, shifted = self._nodal_origin0(P)
+        if primaldual == 'dual':
+            return coefficient_inverse(vals, shift=not shifted)
+        return vals
+
     def get_A_Ga(self, Nbar, primaldual='primal', order=-1, P=None, grid=None):
         """grid (optional, >= Nbar): return the same coefficient (the same
         trigonometric polynomial) sampled on a larger integration grid."""
+        from .engine import require_cuda
+        require_cuda()
         Nbar = np.asarray(Nbar, dtype=np.int64)
         if grid is not None and tuple(int(g) for g in grid) != tuple(Nbar):
             return self._get_A_Ga_on(Nbar, primaldual, order, P, grid)
@@ -509,68 +542,35 @@ class Material:
         elif order not in (None, 'exact', 0, 1):
             raise ValueError('Wrong material order (%s)!' % str(order))
         if order in (None, 'exact'):
-            chars = self.get_shape_functions(Nbar)
+            # each characteristic function at origin 0 on the GPU; the sum over
+            # inclusions runs there too (fhp_outer_accumulate), bit-identical
+            # to the host sum of the same functions
+            import torch
+            from .engine import outer_accumulate
+            chars = self._shape_functions_dev(Nbar)
             vals = self.conf['vals']
-            if _gpu_available():
-                # each characteristic function moved to origin 0 and uploaded
-                # once; the sum over inclusions runs on the GPU
-                # (fhp_outer_accumulate), bit-identical to the host sum
-                import torch
-                from .engine import outer_accumulate
-                shape = tuple(np.shape(vals[0]))
-                val_d = torch.zeros(shape + tuple(int(n) for n in Nbar), dtype=torch.float64,
-                                    device='cuda')
-                flat = val_d.view(int(np.prod(shape)), -1)
-                for v, c in zip(vals, chars):
-                    v = np.asarray(v, dtype=np.float64)
-                    if primaldual == 'dual':
-                        v = np.linalg.inv(v)
-                    c0 = torch.from_numpy(np.ascontiguousarray(np.fft.ifftshift(c))).to('cuda')
-                    outer_accumulate(flat, v, c0)
-                out = Tensor(name='A_Ga', val=val_d, order=2, multype=21, origin=0)
-                out.Y = self.Y
-                return out
-            val = np.zeros(np.shape(vals[0]) + tuple(Nbar))
+            shape = tuple(np.shape(vals[0]))
+            val_d = torch.zeros(shape + tuple(int(n) for n in Nbar), dtype=torch.float64,
+                                device='cuda')
+            flat = val_d.view(int(np.prod(shape)), -1)
             for v, c in zip(vals, chars):
                 v = np.asarray(v, dtype=np.float64)
                 if primaldual == 'dual':
                     v = np.linalg.inv(v)
-                val += np.multiply.outer(v, c)
-            name = 'A_Ga'
-        else:
-            if P is None and 'P' in self.conf:
-                P = self.conf['P']
-            P = np.asarray(P, dtype=np.int64)
-            vals = self.evaluate(Grid.get_coordinates(P, self.Y))
-            name = 'A_Ga_o{0}_P{1}'.format(order, np.array(P).max())
-            if _gpu_available() and np.all(Nbar % 2 == 1) and Nbar.size == P.size:
-                if primaldual == 'dual':
-                    from .engine import coefficient_inverse
-                    vals = coefficient_inverse(vals, shift=True)
-                out = Tensor(name=name, val=ga_grid_coefficient_gpu(vals, P, Nbar, self.Y, order),
-                             order=2, multype=21, origin=0)
-                out.Y = self.Y
-                return out
-            if primaldual == 'dual':
-                vals = get_inverse(vals)
-            h = self.Y / P
-            W = get_weights_con(h, Nbar, self.Y) if order in (0, 'constant') \
-                else get_weights_lin(h, Nbar, self.Y)
-            val = np.zeros(vals.shape[:2] + tuple(Nbar))
-            for m, n in itertools.product(range(vals.shape[0]), range(vals.shape[1])):
-                hA = np.prod(P) * _centered_fft(vals[m, n], P)
-                if np.all(P == Nbar):
-                    hAN = hA
-                elif np.all(P >= Nbar):
-                    hAN = decrease(hA, Nbar)
-                elif np.all(P < Nbar):
-                    reps = 2 * np.ceil(Nbar / 2. / P).astype(np.int64) + 1
-                    hAN = decrease(np.tile(hA, reps), Nbar)
-                else:
-                    raise NotImplementedError('This combination of double N (%s) and P (%s)'
-                                              % (Nbar, P))
-                val[m, n] = _centered_ifft_real(W * hAN, Nbar)
-            name = 'A_Ga_o{0}_P{1}'.format(order, np.array(P).max())
-        out = self._origin0(val, name)
+                outer_accumulate(flat, v, c)
+            out = Tensor(name='A_Ga', val=val_d, order=2, multype=21, origin=0)
+            out.Y = self.Y
+            return out
+        if P is None and 'P' in self.conf:
+            P = self.conf['P']
+        P = np.asarray(P, dtype=np.int64)
+        if not (np.all(Nbar % 2 == 1) and Nbar.size == P.size):
+            raise NotImplementedError('grid-based Ga coefficients need an odd double grid '
+                                      '(2N-1 is) of the image dimension')
+        name = 'A_Ga_o{0}_P{1}'.format(order, np.array(P).max())
+        out = Tensor(name=name, val=ga_grid_coefficient_gpu(self._grid_image(P, primaldual), P,
+                                                            Nbar, self.Y, order),
+                     order=2, multype=21, origin=0)
         out.Y = self.Y
         return out
+

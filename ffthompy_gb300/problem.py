@@ -64,15 +64,22 @@ class Problem:
                     print(key)
                     print(val)
         if hasattr(self, 'save'):
+            # the reference's layout (problem.py:98-126): self.output with the
+            # problem's definition added - mat_<pd> dicts of arrays, sol_<pd>
+            # lists of Tensors (values pickled as host arrays), res_<pd> lists
+            # of {'cb': CallBack, 'info': {...}}
             self.save.setdefault('data', 'all')
             data = dict(self.output)
+            material = {}
+            for k, v in self.material.items():
+                try:
+                    pickle.dumps(v, protocol=3)
+                except Exception:       # e.g. a 'fun' defined in a closure
+                    continue
+                material[k] = v
             data.update({'physics': self.physics, 'solve': self.solve, 'solver': self.solver,
                          'postprocess': self.postprocess, 'save': self.save,
-                         'material': {k: v for k, v in self.material.items() if k != 'fun'}})
-            for pd in self.solve['primaldual']:
-                data['sol_' + pd] = [s.val for s in data.get('sol_' + pd, [])]
-                data['res_' + pd] = [{'info': r['info'], 'res_norm': r['cb'].res_norm}
-                                     for r in data.get('res_' + pd, [])]
+                         'material': material})
             filename = self.save['filename']
             dirs = os.path.dirname(filename)
             if dirs and not os.path.exists(dirs):

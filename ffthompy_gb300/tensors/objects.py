@@ -60,6 +60,20 @@ class Tensor:
         self.dim = len(self.N)
         self.Y = np.ones(self.dim) if Y is None else np.asarray(Y, dtype=np.float64)
 
+    # pickling (Problem.postprocessing saves Tensors, as the reference does,
+    # ffthompy/problem.py:98-126): the values travel as a host NumPy array
+    # and return to the GPU on loading when one is present
+    def __getstate__(self):
+        st = {k: v for k, v in self.__dict__.items() if k != 'data'}
+        st['val_host'] = self.data.detach().cpu().numpy()
+        return st
+
+    def __setstate__(self, st):
+        st = dict(st)
+        v = st.pop('val_host')
+        self.__dict__.update(st)
+        self.data = _to_device(v)
+
     # -- values -----------------------------------------------------------------
     @property
     def val(self):

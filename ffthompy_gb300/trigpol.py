@@ -33,9 +33,13 @@ class Grid:
     @staticmethod
     def get_coordinates(N, Y):
         """Nodes Y_i * k_i / N_i, centred origin, shape (d,) + N."""
+        return np.stack(np.meshgrid(*Grid.get_axes(N, Y), indexing='ij'))
+
+    @staticmethod
+    def get_axes(N, Y):
+        """The per-axis node coordinates of get_coordinates."""
         N = np.asarray(N, dtype=np.int64)
-        axes = [Y[i] * _ints(N[i], True) / N[i] for i in range(N.size)]
-        return np.stack(np.meshgrid(*axes, indexing='ij'))
+        return [Y[i] * _ints(N[i], True) / N[i] for i in range(N.size)]
 
 
 def get_Nodd(N):

@@ -85,6 +85,30 @@ int fhp_plan_create_band(fhp_plan* out, int dim, const int* n, const int* n_int,
  * ffthompy/general/solver.py:80-139).
  */
 int fhp_plan_set_band_cg(fhp_plan plan, int spectral);
+/*
+ * Band plans: kernel of the integration pass (inverse transform of the last
+ * axis, coefficient, forward transform).  kind = 1 (default): lines held in
+ * registers, one warp per line, where that kernel applies (FP32 fields, an
+ * isotropic coefficient, a 512-point integration line with the band within a
+ * quarter of it); kind = 0: the shared-memory line cores, for every plan.
+ * Both compute the same transforms.  No counterpart in the reference (its
+ * transforms are numpy.fft.rfftn / irfftn, ffthompy/tensors/fft.py:39-43).
+ */
+int fhp_plan_set_integration_kernel(fhp_plan plan, int kind);
+/*
+ * Autotuner: times candidate launch shapes of the plan's operator on the
+ * plan's own buffers (three applications each, CUDA events) and keeps the
+ * fastest.  Band plans: the integration kernel (register lines at 1 or 2 CTAs
+ * per SM, or the shared-memory cores) and the column-tile target of the axis
+ * passes; other plans: rows per CTA of the last-axis passes and the column
+ * tile of the projection pass.  Choices are cached per plan geometry,
+ * precision, coefficient kind and device for the life of the process, so a
+ * second plan of the same shape is tuned without timing.  The coefficient
+ * must be set.  chosen[3] (host, may be NULL) receives the choice, and
+ * ms_per_apply (may be NULL) the time of one application.  Synchronises
+ * `stream`.  No counterpart in the reference.
+ */
+int fhp_plan_autotune(fhp_plan plan, int* chosen, float* ms_per_apply, void* stream);
 int fhp_plan_destroy(fhp_plan plan);
 /* FHP_MIXED plans: inner relative tolerance floor eta (default 1e-4) and the
    maximum number of refinement steps (default 30). */
@@ -131,6 +155,50 @@ int fhp_rhs_macro(fhp_plan plan, int proj, void* b, void* stream);
 int fhp_cg_solve(fhp_plan plan, int proj, const void* b, const void* x0, double tol,
                  int maxiter, void* x, int* kit, double* norm_res, int* status,
                  double* res_log, int log_rows, void* stream);
+
+/*
+ * CG on several plans at once: an ensemble of independent cells (grids may
+ * differ), each solving its own loads from its own right-hand sides b[i] into
+ * x[i] from a zero start, with its own scalars and stopping tests, exactly as
+ * fhp_cg_solve would.  The plans advance together: every iteration of all of
+ * them is one CUDA graph (the plans' kernels forked over a pool of streams),
+ * and the host checks one combined done flag.  kit, norm_res and status
+ * (host, may be NULL) receive the per-load results concatenated over the
+ * plans in order.  The plans must all be FHP_MIXED (refinement, each outer
+ * step's FP32 solves advanced together) or all not, and no plan may appear
+ * twice.  Replaces: one applications.scalar / elasticity run per cell
+ * (ffthompy/applications.py:11-90, 93-176), i.e. linear_solver(..., 'CG')
+ * called once per cell and load (ffthompy/general/solver.py:80-139).
+ */
+int fhp_cg_solve_many(int count, const fhp_plan* plans, int proj, const void* const* b,
+                      double tol, int maxiter, void* const* x, int* kit, double* norm_res,
+                      int* status, void* stream);
+
+/*
+ * The reference's other linear solvers over the fused operator, all loads at
+ * once with per-load scalars and stopping tests kept on the device (one
+ * CUDA-graph replay per iteration, the host reads only an all-done flag):
+ * fhp_richardson_solve: x += omega (b - A x) while the norm of the residual
+ *   of the previous iterate exceeds tol (norm_res starts at 1e15).
+ *   Replaces: richardson / 'iterative' (ffthompy/general/solver.py:63-77).
+ * fhp_chebyshev_solve: the two-term Chebyshev iteration for eigenvalues in
+ *   [eig_min, eig_max]; norm_res relative to the first residual (r0 / |b| at
+ *   the start).  Replaces: cheby2TERM (solver.py:206-285).
+ * fhp_bicg_solve: biconjugate gradients with the operator as its own
+ *   transpose, shadow residual and directions updated with it, stopping test
+ *   sqrt(<R, Rs>) <= tol.  Replaces: BiCG (solver.py:142-204; see the
+ *   package's general/solver.py for the scalar product it uses).
+ * x0 may be NULL (zero start); kit, norm_res, status as fhp_cg_solve.
+ * FHP_MIXED plans run these in FP64.
+ */
+int fhp_richardson_solve(fhp_plan plan, int proj, const void* b, const void* x0, double omega,
+                         double tol, int maxiter, void* x, int* kit, double* norm_res,
+                         int* status, void* stream);
+int fhp_chebyshev_solve(fhp_plan plan, int proj, const void* b, const void* x0, double eig_min,
+                        double eig_max, double tol, int maxiter, void* x, int* kit,
+                        double* norm_res, int* status, void* stream);
+int fhp_bicg_solve(fhp_plan plan, int proj, const void* b, const void* x0, double tol,
+                   int maxiter, void* x, int* kit, double* norm_res, int* status, void* stream);
 
 /*
  * AH[i*loads + j] = <A u_i, u_j>, u_i = X_i + E_i if add_macro else X_i
@@ -260,6 +328,21 @@ int fhp_ball_characteristic(fhp_plan plan, double r, double volume, const double
  */
 int fhp_ball_topology(int dim, const int* n, const double* axes, const double* x0,
                       const double* Y, double radius, double* out, void* stream);
+
+/*
+ * Characteristic function of a separable inclusion (a box or a bilinear
+ * pyramid): out[x] = prod_a re_a[x_a] when im is NULL, else the real part of
+ * prod_a (re_a + i im_a)[x_a] - the per-axis factors of its GaNi topology
+ * (sums over the periodic images) or of its Ga spectrum transformed per axis.
+ * re, im: host, concatenated per axis (sum n doubles each); out: float64
+ * device array [n0]..[n_{dim-1}].  Products are formed left to right and the
+ * complex ones as NumPy forms them (bit-identical to its outer products).
+ * dim 2 or 3.  Replaces, for boxes and pyramids: the topologies of
+ * Material.get_topologies (ffthompy/materials.py:212-301) and the centred
+ * inverse DFT of Material.get_shape_functions (materials.py:125-169).
+ */
+int fhp_separable_char(int dim, const int* n, const double* re, const double* im, double* out,
+                       void* stream);
 
 /*
  * out[k][i] += v[k] * c[i] for k < nv, i < M: one inclusion's value matrix

