@@ -414,6 +414,28 @@ def fibres_measure(n=127, tol=1e-6, seed=0):
     return out
 
 
+def adjoint_measure(n=127, tol=1e-10):
+    """dA_H/da(x) of the scalar GaNi problem with a(x) = exp(g(x)) on n^3
+    (g a seeded Gaussian random field, length 0.15), 3 loads, mixed
+    precision: forward solve and gradient through torch.autograd, timed
+    end to end (CUDA synchronised)."""
+    import torch
+    from ffthompy_gb300 import workloads
+    from ffthompy_gb300.adjoint import homogenized_matrix
+    a_np = np.exp(workloads.gaussian_field((n,) * 3, 0.15, seed=11))
+    out = {'grid': [n] * 3, 'loads': 3, 'precision': 'mixed', 'tol': tol}
+    for rep in range(2):
+        a = torch.tensor(a_np, device='cuda', requires_grad=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        AH = homogenized_matrix(a, tol=tol, precision='mixed')
+        AH[0, 0].backward()
+        torch.cuda.synchronize()
+        out['seconds_forward_and_gradient'] = time.perf_counter() - t0
+    out['AH00'] = float(AH[0, 0])
+    return out
+
+
 def inverse_measure(n=253, d=6, reps=5):
     """The dual-coefficient inverse (fhp_coefficient_inverse) of a Mandel 6x6
     field on the Ga grid of the fibres problem (2*127-1)^3, CUDA events on the
@@ -689,9 +711,14 @@ def run_gpu(args):
         torch.cuda.empty_cache()
 
     # end to end through the host-buffer C-ABI entry point
+    # the coefficient as a user holds it: a pinned host array written by the
+    # CPU (a pinned buffer filled by a device-to-host copy uploaded at a tenth
+    # of the link rate on this machine, see e2e_phases)
+    A_np = A_iso.cpu().numpy()
     host_A = torch.empty(tuple(A_iso.shape), dtype=torch.float64, pin_memory=True)
-    host_A.copy_(A_iso)
     A_host = host_A.numpy()
+    np.copyto(A_host, A_np)
+    del A_np
     e2e_plan = make_plan(w, args.precision, args.ga_mode)
     e2e_plan.set_coefficient(A.data)
     e2e_plan.autotune()     # the cached choice of the timed plan
@@ -731,8 +758,18 @@ def run_gpu(args):
     for i, name in enumerate(['coefficient_upload_ms', 'rhs_ms', 'cg_ms', 'energy_ms']):
         ph[name] = round(evs[i].elapsed_time(evs[i + 1]), 3)
     ph['wall_ms'] = round(wall * 1e3, 3)
-    # the same host buffer copied by torch, for comparison with the upload
+    # the same host buffer copied by torch, for comparison with the upload,
+    # and a pinned buffer filled by a device-to-host copy
     dev_A = torch.empty(tuple(A_iso.shape), dtype=torch.float64, device='cuda')
+    d2h_filled = torch.empty(tuple(A_iso.shape), dtype=torch.float64, pin_memory=True)
+    d2h_filled.copy_(A_iso)
+    torch.cuda.synchronize()
+    evs[0].record(stream)
+    dev_A.copy_(d2h_filled, non_blocking=True)
+    evs[1].record(stream)
+    torch.cuda.synchronize()
+    ph['torch_h2d_d2h_filled_buffer_ms'] = round(evs[0].elapsed_time(evs[1]), 3)
+    del d2h_filled
     torch.cuda.synchronize()
     evs[0].record(stream)
     dev_A.copy_(host_A, non_blocking=True)
@@ -752,6 +789,7 @@ def run_gpu(args):
     if not args.no_potential:
         extras['potential'] = potential_measure(vals, w, tol)
     if not args.no_fibres:
+        extras['adjoint127'] = adjoint_measure()
         extras['fibres127'] = fibres_measure()
         extras['coefficient_inverse'] = inverse_measure()
     if not args.no_ensemble:

@@ -1142,8 +1142,17 @@ __device__ __forceinline__ void tile_loop(int nlc, int n, int T, int lgT, F&& bo
 // BAND_DOWN_PROJ_F the direction p read for the partial <p, Ap>, written to
 // partials[(blockIdx.y * gridDim.x + blockIdx.x) * L + l] (zero for l other
 // than the CTA's load) when partials is not null.
+// FP32 pad passes hold one line buffer per column and no per-frequency
+// projection: three CTAs per SM fit their registers (80) and shared memory,
+// which hides more of their global-memory latency (measured: 1.13 -> 1.06 ms
+// and 0.99 -> 0.85 ms at the 509^3 workload; the down pass was not faster).
+template <typename R, int MODE>
+constexpr int band_axis_min_blocks() {
+  return (sizeof(R) == 4 && (MODE == 4 || MODE == 5)) ? 3 : kFftMinBlocks<R>;
+}
+
 template <typename R, int MODE, int PHYS>
-__global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_band_axis(const cplx<R>* __restrict__ Sin,
+__global__ void __launch_bounds__(256, band_axis_min_blocks<R, MODE>()) k_band_axis(const cplx<R>* __restrict__ Sin,
                                                    cplx<R>* __restrict__ Sout, const __grid_constant__ GridDims g,
                                                    const __grid_constant__ BandAxis ax, const __grid_constant__ LineDev<R> L1, const __grid_constant__ LineDev<R> L2,
                                                    int T, const __grid_constant__ GreenParams gp,

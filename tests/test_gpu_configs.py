@@ -178,6 +178,53 @@ def test_gradient_127_matches_gpu_central_differences():
           % (t_grad, time.perf_counter() - t0))
 
 
+def test_gradient_127_mixed_64_voxels_within_1e4():
+    """The adjoint configuration as specified: a(x) = exp(g(x)) on 127^3
+    (g a seeded Gaussian random field, length 0.15), dA_H[0,0]/da(x) from
+    the mixed-precision solve (FP32 inner CG, FP64 refinement) through
+    torch.autograd, against central differences of the mixed-precision
+    A_H[0,0] (one-load plan, same tolerance) on 64 seeded voxels with step
+    1e-3 a(x): truncation ~1e-6 relative, so the bar is 1e-4."""
+    from ffthompy_gb300 import _lib
+    from ffthompy_gb300.adjoint import homogenized_matrix
+    from ffthompy_gb300.engine import GalerkinPlan
+    N = (127, 127, 127)
+    a_np = np.exp(workloads.gaussian_field(N, 0.15, seed=11))
+    a = torch.tensor(a_np, device='cuda', requires_grad=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    AH = homogenized_matrix(a, tol=1e-10, precision='mixed')
+    AH[0, 0].backward()
+    torch.cuda.synchronize()
+    t_grad = time.perf_counter() - t0
+    grad = a.grad.cpu().numpy()
+    plan = GalerkinPlan(N, np.ones(3), physics='scalar', nloads=1, precision='mixed')
+    base = torch.tensor(a_np, device='cuda').reshape((1,) + N)
+
+    def ah00(vals):
+        plan.set_coefficient_packed(vals, _lib.FHP_COEF_ISO)
+        X, info = plan.cg(plan.rhs_macro(1), tol=1e-10, maxiter=2000)
+        assert info['status'] == [0]
+        return plan.energy(X)[0, 0]
+
+    assert abs(ah00(base) - float(AH[0, 0])) < 1e-10 * abs(float(AH[0, 0]))
+    rng = np.random.default_rng(64)
+    worst = 0.
+    for _ in range(64):
+        v = tuple(int(rng.integers(n)) for n in N)
+        h = 1e-3 * a_np[v]
+        vp = base.clone()
+        vp[(0,) + v] += h
+        vm = base.clone()
+        vm[(0,) + v] -= h
+        fd = (ah00(vp) - ah00(vm)) / (2 * h)
+        err = abs(fd - grad[v]) / abs(grad[v])
+        worst = max(worst, err)
+        assert err < 1e-4, (v, fd, grad[v])
+    print('127^3 mixed gradient %.2f s (forward + backward); worst FD error %.2e'
+          % (t_grad, worst))
+
+
 def test_gradient_elasticity_packed_matches_central_differences():
     """Mandel 6x6 packed (SYM) coefficient, 6 loads, general adjoint seed W."""
     from ffthompy_gb300 import _lib
