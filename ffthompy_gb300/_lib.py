@@ -32,6 +32,10 @@ SIGNATURES = {
     'fhp_plan_create_band': (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.c_int, _c_int_p,
                                             _c_int_p, _c_double_p, ctypes.c_int, ctypes.c_int,
                                             ctypes.c_double, ctypes.c_int]),
+    'fhp_plan_create_cells': (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.c_int, _c_int_p,
+                                             _c_int_p, _c_double_p, ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_double, ctypes.c_int, ctypes.c_int]),
+    'fhp_plan_cells': (ctypes.c_int, [_vp]),
     'fhp_plan_destroy': (ctypes.c_int, [_vp]),
     'fhp_plan_set_refinement': (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_int]),
     'fhp_plan_set_band_cg': (ctypes.c_int, [_vp, ctypes.c_int]),

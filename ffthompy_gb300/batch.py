@@ -5,12 +5,16 @@ fields of possibly different grids - the reference would run
 applications.scalar / elasticity (ffthompy/applications.py:11-90, 93-176) once
 per instance - and returns one A_H per instance.
 
-mode='threads' (the default) and mode='batched' give the same per-cell
-results.  On the 512-cell 2D ensemble (n in 63..511, 2 loads, tol 1e-6) the
-threads take 9.8 s in FP64 and 2.7 s mixed on a GB300, the batched solve
-13.2 s and 4.5 s: the cells' kernels are small, and the thread pool overlaps
-cells at different iterations while one graph per ensemble iteration waits
-for its slowest cell.
+mode='threads' (the default), mode='cells' and mode='batched' give the same
+per-cell results.
+
+mode='cells': the cells of one grid size share one plan of several cells
+(GalerkinPlan(ncells=K), fhp_plan_create_cells): every pass of an iteration is
+one launch for all K cells, each load of each cell keeps its own CG scalars
+and stopping test, and the passes skip the cells whose loads have all
+stopped.  The plans of the different sizes advance together in one
+fhp_cg_solve_many call (one CUDA graph per iteration).  Plans are kept in a
+process-wide pool per size, cell count and precision.
 
 mode='batched': every cell gets a plan from a pool kept across
 calls (one plan per cell and grid size, created once, each with its own
@@ -64,8 +68,10 @@ def homogenize_many(coefs, Y=None, physics='scalar', tol=1e-6, maxiter=1000,
     workers: threads of mode='threads'."""
     if mode == 'batched':
         return _homogenize_batched(coefs, Y, physics, tol, maxiter, precision, primaldual)
+    if mode == 'cells':
+        return _homogenize_cells(coefs, Y, physics, tol, maxiter, precision, primaldual)
     if mode != 'threads':
-        raise ValueError("mode must be 'batched' or 'threads'")
+        raise ValueError("mode must be 'threads', 'cells' or 'batched'")
     require_cuda()
     device = torch.device('cuda', torch.cuda.current_device())
     order = sorted(range(len(coefs)), key=lambda i: -int(np.prod(coefs[i].shape[2:])))
@@ -180,6 +186,70 @@ def _homogenize_batched(coefs, Y, physics, tol, maxiter, precision, primaldual):
             out[i][pd] = AH if pd == 'primal' else np.linalg.inv(AH)
             out[i]['kit_' + pd] = info['kit']
             out[i]['status_' + pd] = info['status']
+    return out
+
+
+def _cell_groups(coefs, Y, physics, field_cap=4e9):
+    """{(N, Y, part): [cell indices]}: the cells of each grid size, in parts
+    whose fields stay below field_cap bytes (FP64) each."""
+    groups = {}
+    for i, A in enumerate(coefs):
+        N = tuple(int(n) for n in A.shape[2:])
+        Yi = np.ones(len(N)) if Y is None else np.asarray(Y, dtype=np.float64)
+        groups.setdefault((N, tuple(Yi)), []).append(i)
+    out = {}
+    for (N, Yi), idx in groups.items():
+        d = len(N)
+        dv = d if physics == 'scalar' else d * (d + 1) // 2
+        per = float(np.prod(N)) * dv * dv * 8.0      # one cell's field: dv loads x dv comps
+        cap = max(1, int(field_cap // per))
+        for k in range(0, len(idx), cap):
+            out[(N, Yi, k // cap)] = idx[k:k + cap]
+    return out
+
+
+def _homogenize_cells(coefs, Y, physics, tol, maxiter, precision, primaldual):
+    require_cuda()
+    from .engine import cg_many
+    device = torch.device('cuda', torch.cuda.current_device())
+    groups = _cell_groups(coefs, Y, physics)
+    plans = {}
+    for (N, Yi, part), idx in groups.items():
+        key = ('cells', device.index, N, Yi, physics, precision, len(idx), part)
+        plans[(N, Yi, part)] = _pooled_plans(
+            key, 1, lambda: GalerkinPlan(N, np.asarray(Yi), physics=physics,
+                                         precision=precision, ncells=len(idx)))[0]
+    out = [dict() for _ in coefs]
+    for pd in primaldual:
+        proj = 1 if pd == 'primal' else 2
+        bs = []
+        for gk, idx in groups.items():
+            plan = plans[gk]
+            host = pd == 'primal' and not any(isinstance(coefs[i], torch.Tensor) for i in idx)
+            if host:
+                As = [np.asarray(coefs[i], dtype=np.float64) for i in idx]
+                kind = max(coef_kind_of(A) for A in As)
+                vals = np.stack([pack_coefficient(A, kind) for A in As])
+            else:
+                As = []
+                for i in idx:
+                    At = torch.as_tensor(coefs[i]).to(device, torch.float64)
+                    As.append(At if pd == 'primal' else _inverse_field(At))
+                kind = max(coef_kind_of_torch(A) for A in As)
+                vals = torch.stack([pack_coefficient_torch(A, kind) for A in As])
+            # every cell's coefficient, packed with the most general kind
+            plan.set_coefficient_packed(vals, kind)
+            plan.autotune()
+            bs.append(plan.rhs_macro(proj))
+        sols = cg_many([plans[gk] for gk in groups], bs, tol=tol, maxiter=maxiter, proj=proj)
+        for (gk, idx), (X, info) in zip(groups.items(), sols):
+            plan = plans[gk]
+            AH = plan.energy(X)
+            L = plan.nloads
+            for j, i in enumerate(idx):
+                out[i][pd] = AH[j] if pd == 'primal' else np.linalg.inv(AH[j])
+                out[i]['kit_' + pd] = info['kit'][j * L:(j + 1) * L]
+                out[i]['status_' + pd] = info['status'][j * L:(j + 1) * L]
     return out
 
 

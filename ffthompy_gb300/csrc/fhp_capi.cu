@@ -27,12 +27,39 @@ int bad(const char* msg) {
 
 cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// per-load results of a plan: loads x cells (cell-major) for a batched plan
+int loads_all(const fhp::EngineBase& e) { return e.loads() * e.instances(); }
+
+// entry points that work on one cell only
+int one_cell(fhp_plan p) {
+  return p && p->eng->instances() != 1 ? bad("the plan is batched over cells; this entry "
+                                             "point takes single-cell plans")
+                                       : FHP_OK;
+}
+
 int cuda_status(cudaError_t e, const char* what) {
   if (e == cudaSuccess) return FHP_OK;
   fhp::set_error(std::string(what) + ": " + cudaGetErrorString(e));
   return e == cudaErrorMemoryAllocation ? FHP_OOM : FHP_CUDA;
 }
 
+
+// The inner tolerance of each cell of a plan of several cells: the cell's own
+// min over its active loads, as a plan of that cell alone takes it (the
+// FP32 engine's next solve stops each load on its cell's value).
+void cell_inner_tols(fhp_plan_s& p, const std::vector<double>& norm,
+                     const std::vector<int>& active, double tol) {
+  const int K = p.eng->instances(), Lc = p.eng->loads();
+  if (K == 1) return;
+  std::vector<double> t((size_t)K * Lc, 0.5);
+  for (int c = 0; c < K; ++c) {
+    double e = 0.5;
+    for (int l = c * Lc; l < (c + 1) * Lc; ++l)
+      if (active[l]) e = std::min(e, std::max(p.eta, 0.5 * tol / norm[l]));
+    for (int l = c * Lc; l < (c + 1) * Lc; ++l) t[l] = e;
+  }
+  p.lo->set_load_tols(t.data(), K * Lc);
+}
 
 // Mixed-precision CG by iterative refinement: the residual r = b - A x is
 // formed with the FP64 operator, each load's residual is normalised and solved
@@ -45,7 +72,7 @@ int cg_mixed(fhp_plan_s& p, int proj, const void* b, const void* x0, double tol,
              void* xv, fhp::SolveResult& res, int log_rows, cudaStream_t s) {
   fhp::EngineBase& hi = *p.eng;
   fhp::EngineBase& lo = *p.lo;
-  const int L = hi.loads();
+  const int L = loads_all(hi);
   const double M = (double)hi.voxels();
   const size_t n = (size_t)L * hi.dv() * hi.voxels();
   double* x = static_cast<double*>(xv);
@@ -89,6 +116,7 @@ int cg_mixed(fhp_plan_s& p, int proj, const void* b, const void* x0, double tol,
       sc_out[l] = active[l] ? norm[l] : 0.0;
     }
     if ((st = lo.scale_from64(static_cast<const double*>(r), sc_in.data(), r32, s)) != FHP_OK) break;
+    cell_inner_tols(p, norm, active, tol);
     fhp::SolveResult in;
     if ((st = lo.cg_solve(proj, r32, nullptr, eta, room, d32, in, 1, s)) != FHP_OK) break;
     // x += G (s d): the FP32 correction carries roundoff outside range(G),
@@ -319,7 +347,7 @@ int cg_mixed_many(const std::vector<fhp_plan_s*>& plans, int proj,
   int st = FHP_OK;
   for (int i = 0; i < n && st == FHP_OK; ++i) {
     fhp::EngineBase& hi = *plans[i]->eng;
-    const int L = hi.loads();
+    const int L = loads_all(hi);
     const size_t nv = (size_t)L * hi.dv() * hi.voxels();
     P& q = ps[i];
     q.ax = hi.scratch(fhp::SCR_MIX_AX, nv * 8);
@@ -370,6 +398,7 @@ int cg_mixed_many(const std::vector<fhp_plan_s*>& plans, int proj,
       }
       if ((st = plans[i]->lo->scale_from64(static_cast<const double*>(q.r), q.sc_in.data(), q.r32,
                                            s)) != FHP_OK) break;
+      cell_inner_tols(*plans[i], q.norm, q.active, tol);
       lo.push_back(plans[i]->lo.get());
       rb.push_back(q.r32);
       dx.push_back(q.d32);
@@ -384,7 +413,7 @@ int cg_mixed_many(const std::vector<fhp_plan_s*>& plans, int proj,
       fhp::EngineBase& hi = *plans[i]->eng;
       P& q = ps[i];
       double* x = static_cast<double*>(xv[i]);
-      const size_t nv = (size_t)hi.loads() * hi.dv() * hi.voxels();
+      const size_t nv = (size_t)loads_all(hi) * hi.dv() * hi.voxels();
       const double M = (double)hi.voxels();
       // x += G (s d), as cg_mixed
       if ((st = cuda_status(cudaMemsetAsync(q.ax, 0, nv * 8, s), "memset")) != FHP_OK) break;
@@ -448,8 +477,9 @@ const char* fhp_status_string(int status) {
 
 const char* fhp_last_error(void) { return fhp::last_error(); }
 
-int fhp_plan_create(fhp_plan* out, int dim, const int* n, const int* n_band, const double* Y,
-                    int physics, int nloads, double g_scale, int precision) {
+namespace {
+int plan_create(fhp_plan* out, int dim, const int* n, const int* n_band, const double* Y,
+                int physics, int nloads, double g_scale, int precision, int ncells) {
   if (!out) return bad("out is NULL");
   *out = nullptr;
   if (dim != 2 && dim != 3) return bad("dim must be 2 or 3");
@@ -468,6 +498,7 @@ int fhp_plan_create(fhp_plan* out, int dim, const int* n, const int* n_band, con
   cfg.physics = physics;
   cfg.nloads = nloads;
   cfg.scale = g_scale;
+  cfg.ninst = ncells;
   int st = FHP_OK;
   std::unique_ptr<fhp::EngineBase> e, lo;
   if (precision == FHP_F64 || precision == FHP_MIXED) e = fhp::make_engine_f64(cfg, &st);
@@ -485,6 +516,21 @@ int fhp_plan_create(fhp_plan* out, int dim, const int* n, const int* n_band, con
   *out = p;
   return FHP_OK;
 }
+}  // namespace
+
+int fhp_plan_create(fhp_plan* out, int dim, const int* n, const int* n_band, const double* Y,
+                    int physics, int nloads, double g_scale, int precision) {
+  return plan_create(out, dim, n, n_band, Y, physics, nloads, g_scale, precision, 1);
+}
+
+int fhp_plan_create_cells(fhp_plan* out, int dim, const int* n, const int* n_band,
+                          const double* Y, int physics, int nloads, double g_scale,
+                          int precision, int ncells) {
+  if (ncells < 1 || ncells > 65535) return bad("ncells must be in 1..65535");
+  return plan_create(out, dim, n, n_band, Y, physics, nloads, g_scale, precision, ncells);
+}
+
+int fhp_plan_cells(fhp_plan plan) { return plan ? plan->eng->instances() : 0; }
 
 int fhp_plan_create_band(fhp_plan* out, int dim, const int* n, const int* n_int,
                          const double* Y, int physics, int nloads, double g_scale,
@@ -596,11 +642,13 @@ int fhp_rhs_macro(fhp_plan plan, int proj, void* b, void* stream) {
 
 int fhp_potential_rhs(fhp_plan plan, void* bh, void* stream) {
   if (!plan || !bh) return bad("plan and bh are required");
+  if (one_cell(plan)) return FHP_BAD_ARG;
   return plan->eng->pot_rhs(bh, as_stream(stream));
 }
 
 int fhp_potential_apply(fhp_plan plan, const void* xh, void* yh, void* stream) {
   if (!plan || !xh || !yh) return bad("plan, xh and yh are required");
+  if (one_cell(plan)) return FHP_BAD_ARG;
   return plan->eng->pot_apply(xh, yh, as_stream(stream));
 }
 
@@ -608,6 +656,7 @@ int fhp_potential_cg(fhp_plan plan, const void* bh, double tol, int maxiter, voi
                      double* norm_res, int* status, double* res_log, int log_rows,
                      void* stream) {
   if (!plan || !bh || !xh) return bad("plan, bh and xh are required");
+  if (one_cell(plan)) return FHP_BAD_ARG;
   if (maxiter < 0) return bad("maxiter must be >= 0");
   if (!(tol >= 0)) return bad("tol must be >= 0");
   fhp::SolveResult r;
@@ -628,6 +677,7 @@ int fhp_potential_cg(fhp_plan plan, const void* bh, double tol, int maxiter, voi
 
 int fhp_potential_field(fhp_plan plan, const void* xh, void* X, void* stream) {
   if (!plan || !xh || !X) return bad("plan, xh and X are required");
+  if (one_cell(plan)) return FHP_BAD_ARG;
   return plan->eng->pot_field(xh, X, as_stream(stream));
 }
 
@@ -644,7 +694,7 @@ int fhp_cg_solve(fhp_plan plan, int proj, const void* b, const void* x0, double 
                     : plan->eng->cg_solve(proj, b, x0, tol, maxiter, x, r, rows,
                                           as_stream(stream));
   if (st != FHP_OK && r.kit.empty()) return st;
-  const int L = plan->eng->loads();
+  const int L = loads_all(*plan->eng);
   for (int l = 0; l < L && l < (int)r.kit.size(); ++l) {
     if (kit) kit[l] = r.kit[l];
     if (norm_res) norm_res[l] = r.norm_res[l];
@@ -686,7 +736,7 @@ int fhp_cg_solve_many(int count, const fhp_plan* plans, int proj, const void* co
   }
   int off = 0;
   for (int i = 0; i < count; ++i) {
-    const int L = plans[i]->eng->loads();
+    const int L = loads_all(*plans[i]->eng);
     for (int l = 0; l < L && i < (int)r.size() && l < (int)r[i].kit.size(); ++l) {
       if (kit) kit[off + l] = r[i].kit[l];
       if (norm_res) norm_res[off + l] = r[i].norm_res[l];
@@ -702,6 +752,7 @@ int solve_other_c(int kind, fhp_plan plan, int proj, const void* b, const void* 
                   double p1, double tol, int maxiter, void* x, int* kit, double* norm_res,
                   int* status, void* stream) {
   if (!plan || !b || !x) return bad("plan, b and x are required");
+  if (one_cell(plan)) return FHP_BAD_ARG;
   if (proj != 1 && proj != 2) return bad("proj must be 1 or 2");
   if (maxiter < 0) return bad("maxiter must be >= 0");
   if (!(tol >= 0)) return bad("tol must be >= 0");
@@ -748,12 +799,14 @@ int fhp_energy_matrix(fhp_plan plan, const void* X, int add_macro, double* AH, v
 int fhp_energy_gradient(fhp_plan plan, const void* X, int add_macro, const double* W,
                         double* grad, void* stream) {
   if (!plan || !X || !W || !grad) return bad("plan, X, W and grad are required");
+  if (one_cell(plan)) return FHP_BAD_ARG;
   return plan->eng->energy_gradient(X, add_macro, W, grad, as_stream(stream));
 }
 
 int fhp_fourier_interp(fhp_plan src, fhp_plan dst, const void* x_src, void* x_dst,
                        void* stream) {
   if (!src || !dst || !x_src || !x_dst) return bad("plans and fields are required");
+  if (one_cell(src) || one_cell(dst)) return FHP_BAD_ARG;
   const fhp::PlanConfig& a = src->eng->config();
   const fhp::PlanConfig& b = dst->eng->config();
   if (a.dim != b.dim || src->eng->dv() * src->eng->loads() != dst->eng->dv() * dst->eng->loads() ||
@@ -786,7 +839,7 @@ int fhp_homogenize_host(fhp_plan plan, int proj, int coef_kind, const double* co
   fhp::EngineBase& e = *plan->eng;
   int st = fhp_set_coefficient(plan, coef_kind, coef_host, 0, stream);
   if (st != FHP_OK) return st;
-  const size_t bytes = (size_t)e.loads() * e.dv() * e.voxels() * e.elem_size();
+  const size_t bytes = (size_t)loads_all(e) * e.dv() * e.voxels() * e.elem_size();
   // the plan's persistent scratch: repeated calls allocate nothing
   void* b = e.scratch(fhp::SCR_HOST_B, bytes);
   void* x = e.scratch(fhp::SCR_HOST_X, bytes);
@@ -800,7 +853,7 @@ int fhp_homogenize_host(fhp_plan plan, int proj, int coef_kind, const double* co
   if (st == FHP_OK && x_host)
     st = cuda_status(cudaMemcpyAsync(x_host, x, bytes, cudaMemcpyDeviceToHost, s), "copy");
   if (st == FHP_OK) st = cuda_status(cudaStreamSynchronize(s), "sync");
-  const int L = e.loads();
+  const int L = loads_all(e);
   for (int l = 0; l < L && l < (int)r.kit.size(); ++l) {
     if (kit_host) kit_host[l] = r.kit[l];
     if (norm_res_host) norm_res_host[l] = r.norm_res[l];
@@ -843,6 +896,7 @@ int fhp_ga_grid_coefficient(fhp_plan plan_img, fhp_plan plan_out, const void* im
                             void* stream) {
   if (!plan_img || !plan_out || !image || !src_index || !weights || !out)
     return bad("plans, image, tables and out are required");
+  if (one_cell(plan_img) || one_cell(plan_out)) return FHP_BAD_ARG;
   const fhp::PlanConfig& a = plan_img->eng->config();
   const fhp::PlanConfig& b = plan_out->eng->config();
   if (a.dim != b.dim || plan_img->eng->dv() * plan_img->eng->loads() !=
@@ -892,6 +946,7 @@ int fhp_ga_grid_coefficient(fhp_plan plan_img, fhp_plan plan_out, const void* im
 int fhp_ball_characteristic(fhp_plan plan, double r, double volume, const double* sq,
                             const double* phase, void* out, void* stream) {
   if (!plan || !sq || !phase || !out) return bad("plan, tables and out are required");
+  if (one_cell(plan)) return FHP_BAD_ARG;
   if (!(r >= 0) || !(volume > 0)) return bad("r must be >= 0 and volume > 0");
   const fhp::PlanConfig& c = plan->eng->config();
   if (plan->eng->precision() != FHP_F64 || plan->eng->dv() * plan->eng->loads() != 1)

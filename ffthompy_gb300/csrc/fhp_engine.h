@@ -75,6 +75,7 @@ struct PlanConfig {
   int nloads = 1;
   double scale = 1.0;        // Ga: prod(2N-1)/prod(N)
   int integ[3] = {0, 0, 0};  // band mode: integration grid (>= 2N-1); 0 = classic
+  int ninst = 1;             // cells of the same grid solved together by one plan
 };
 
 struct SolveResult {
@@ -115,6 +116,12 @@ class EngineBase {
   virtual long long voxels() const = 0;
   virtual int dv() const = 0;
   virtual int loads() const = 0;
+  // cells of a batched plan: fields [cell][load][component][grid], per-load
+  // results cell-major (cell * loads + load)
+  virtual int instances() const = 0;
+  // per-load stopping tolerances (cells x loads) for the next CG solve only,
+  // in place of its single tol (inner solves of a refinement over cells)
+  virtual void set_load_tols(const double* tols, int n) = 0;
   virtual size_t elem_size() const = 0;
   // coefficient (c values per voxel, component-major, f64 on host or device)
   virtual int set_coefficient(int kind, const double* values, bool on_device, cudaStream_t s) = 0;

@@ -95,6 +95,14 @@ class Engine final : public EngineBase {
     }
     if (g_.L < 1 || g_.L > kMaxLoads) { set_error("nloads must be in 1..6"); return ST_BAD_ARG; }
     g_.M = (long long)g_.n0 * g_.n1 * g_.n2;
+    // cells of a batched plan: the grid's instance dimension (y or z, at most
+    // 65535); band plans hold one cell
+    g_.K = cfg_.ninst;
+    if (g_.K < 1 || g_.K > 65535) { set_error("cells must be in 1..65535"); return ST_BAD_ARG; }
+    if (g_.K > 1 && (cfg_.integ[0] > 0 || cfg_.physics < 0)) {
+      set_error("batched plans hold GaNi or full-grid Ga cells");
+      return ST_BAD_ARG;
+    }
     gp_.physics = cfg_.physics;
     gp_.scale = cfg_.scale;
     for (int i = 0; i < 3; ++i) {
@@ -109,7 +117,9 @@ class Engine final : public EngineBase {
     if ((st = make_line(g_.n1, l1_)) != ST_OK) return st;
     if (d == 3 && (st = make_line(g_.n0, l0_)) != ST_OK) return st;
     const int C = g_.L * g_.dv;
-    spec_elems_ = (size_t)C * g_.n0 * g_.n1 * g_.n2h;
+    g_.sf = (long long)C * g_.M;
+    g_.ss = (long long)C * g_.n0 * g_.n1 * g_.n2h;
+    spec_elems_ = (size_t)g_.K * g_.ss;
     FHP_CHECK(cudaMalloc(&S_, spec_elems_ * sizeof(cplx<R>)));
     // launch geometry
     const int np = (C + 1) / 2;
@@ -144,12 +154,16 @@ class Engine final : public EngineBase {
     // parts of the reductions: row passes, grid-stride kernels, and the
     // component-split CG update (at least one part per component)
     nparts_max_ = std::max(std::max(row_ctas_, red_ctas_), g_.L * g_.dv);
-    FHP_CHECK(cudaMalloc(&partials_, (size_t)nparts_max_ * kMaxLoads * kMaxLoads * sizeof(double)));
-    FHP_CHECK(cudaMalloc(&st_, kMaxLoads * sizeof(LoadState)));
+    // per cell: partial sums, load states, reduced sums and per-load scales
+    const size_t K = (size_t)g_.K;
+    FHP_CHECK(cudaMalloc(&partials_,
+                         K * nparts_max_ * kMaxLoads * kMaxLoads * sizeof(double)));
+    FHP_CHECK(cudaMalloc(&st_, K * kMaxLoads * sizeof(LoadState)));
     FHP_CHECK(cudaMalloc(&all_done_, sizeof(int)));
     FHP_CHECK(cudaMallocHost(&h_done_, sizeof(int)));
-    FHP_CHECK(cudaMallocHost(&h_st_, kMaxLoads * sizeof(LoadState)));
-    FHP_CHECK(cudaMalloc(&ad_, 2 * kMaxLoads * kMaxLoads * sizeof(double)));
+    FHP_CHECK(cudaMallocHost(&h_st_, K * kMaxLoads * sizeof(LoadState)));
+    FHP_CHECK(cudaMalloc(&ad_, K * 2 * kMaxLoads * kMaxLoads * sizeof(double)));
+    FHP_CHECK(cudaMalloc(&dscale_, K * 2 * kMaxLoads * sizeof(double)));
     return set_attrs();
   }
 
@@ -232,7 +246,8 @@ class Engine final : public EngineBase {
     cudaGetDevice(&dev);
     std::string k = std::to_string(dev) + (sizeof(R) == 8 ? ":f64" : ":f32") + ":d" +
                     std::to_string(g_.dim) + ":p" + std::to_string(cfg_.physics) + ":L" +
-                    std::to_string(g_.L) + ":k" + std::to_string(coef_kind_);
+                    std::to_string(g_.L) + ":k" + std::to_string(coef_kind_) + ":K" +
+                    std::to_string(g_.K);
     for (int i = 0; i < 3; ++i) k += ":" + std::to_string(cfg_.N[i]) + "/" + std::to_string(cfg_.integ[i]);
     return k;
   }
@@ -289,13 +304,13 @@ class Engine final : public EngineBase {
       const long long worst = ((long long)g_.n0 * g_.n1);
       if (worst > nparts_max_) {
         double* np = nullptr;
-        FHP_CHECK(cudaMalloc(&np, (size_t)worst * kMaxLoads * kMaxLoads * sizeof(double)));
+        FHP_CHECK(cudaMalloc(&np, (size_t)g_.K * worst * kMaxLoads * kMaxLoads * sizeof(double)));
         cudaFree(partials_);
         partials_ = np;
         nparts_max_ = (int)worst;
       }
     }
-    const size_t n = (size_t)g_.L * g_.dv * g_.M;
+    const size_t n = (size_t)g_.K * g_.L * g_.dv * g_.M;
     k_fill_macro<R><<<grid_for(n), kThreads, 0, s>>>(r_, g_, 1.0);
     FHP_LAUNCHED();
     cudaEvent_t e0, e1;
@@ -340,6 +355,8 @@ class Engine final : public EngineBase {
   long long voxels() const override { return g_.M; }
   int dv() const override { return g_.dv; }
   int loads() const override { return g_.L; }
+  int instances() const override { return g_.K; }
+  void set_load_tols(const double* tols, int n) override { load_tol_.assign(tols, tols + n); }
   size_t elem_size() const override { return sizeof(R); }
   size_t spectrum_elems() const override { return spec_elems_; }
   const PlanConfig& config() const override { return cfg_; }
@@ -379,7 +396,7 @@ class Engine final : public EngineBase {
     pp.scale = (double)g_.M / ((double)pp.nb[0] * pp.nb[1] * pp.nb[2]);
     pp.zs = 1.0 / ((double)pp.nb[0] * pp.nb[1] * pp.nb[2]);
     if (!pe_) {
-      FHP_CHECK(cudaMalloc(&pe_, (size_t)g_.L * g_.dv * g_.M * sizeof(R)));
+      FHP_CHECK(cudaMalloc(&pe_, (size_t)g_.K * g_.L * g_.dv * g_.M * sizeof(R)));
       const int T = d == 3 ? T0_ : tile_cols(l1_.dev.ld, 1, (long long)g_.n2h);
       Tfirst_ = T;
     }
@@ -396,7 +413,7 @@ class Engine final : public EngineBase {
     dim3 grid((unsigned)((inner + Tfirst_ - 1) / Tfirst_), (unsigned)(g_.L * g_.dv));
     const int pk = pbeg("pot_c2c_first_inv", 2.0 * spec_bytes(), s);
     k_c2c_axis<R, true><<<grid, kThreads, (size_t)Tfirst_ * lf.dev.ld * sizeof(cplx<R>), s>>>(
-        S_, d == 3 ? g_.n0 : g_.n1, inner, lf.dev, Tfirst_, ad, st, g_.dv);
+        S_, d == 3 ? g_.n0 : g_.n1, inner, lf.dev, Tfirst_, ad, st, g_.dv, g_.ss, g_.L);
     pend(pk, s);
     FHP_LAUNCHED();
     return inv_passes(S_, y, (R)(1.0 / (double)g_.M), false, nullptr, cg, s);
@@ -414,7 +431,7 @@ class Engine final : public EngineBase {
     dim3 grid((unsigned)((inner + Tfirst_ - 1) / Tfirst_), (unsigned)(g_.L * g_.dv));
     const int pk = pbeg("pot_c2c_first_fwd", 2.0 * spec_bytes(), s);
     k_c2c_axis<R, false><<<grid, kThreads, (size_t)Tfirst_ * lf.dev.ld * sizeof(cplx<R>), s>>>(
-        S_, d == 3 ? g_.n0 : g_.n1, inner, lf.dev, Tfirst_, ad, st, g_.dv);
+        S_, d == 3 ? g_.n0 : g_.n1, inner, lf.dev, Tfirst_, ad, st, g_.dv, g_.ss, g_.L);
     pend(pk, s);
     FHP_LAUNCHED();
     return ST_OK;
@@ -438,7 +455,7 @@ class Engine final : public EngineBase {
   int pot_rhs(void* bh, cudaStream_t s) override {
     int rc = pot_check();
     if (rc != ST_OK) return rc;
-    const size_t n = (size_t)g_.L * g_.dv * g_.M;
+    const size_t n = (size_t)g_.K * g_.L * g_.dv * g_.M;
     k_fill_macro<R><<<grid_for(n), kThreads, 0, s>>>(pe_, g_, 1.0);
     FHP_LAUNCHED();
     if ((rc = pot_fwd(pe_, false, s)) != ST_OK) return rc;
@@ -575,7 +592,9 @@ class Engine final : public EngineBase {
     if (kind < COEF_ISO || kind > COEF_FULL) { set_error("bad coefficient kind"); return ST_BAD_ARG; }
     const int dv = g_.dv;
     const int c = kind == COEF_ISO ? 1 : kind == COEF_SYM ? dv * (dv + 1) / 2 : dv * dv;
-    const size_t n = (size_t)c * (band_ ? gi_.M : g_.M);
+    // [cell][c][grid]: every cell of a batched plan has its own coefficient
+    const size_t n = (size_t)g_.K * c * (band_ ? gi_.M : g_.M);
+    g_.sa = (long long)c * (band_ ? gi_.M : g_.M);
     // keep the buffer when it is large enough: cudaFree synchronises the device,
     // which would serialise plans working on other streams
     if (A_ && A_elems_ < n) { cudaFree(A_); A_ = nullptr; }
@@ -614,7 +633,7 @@ class Engine final : public EngineBase {
   }
 
   int axpy(double a, const void* x, void* y, cudaStream_t s) override {
-    const size_t n = (size_t)g_.L * g_.dv * g_.M;
+    const size_t n = (size_t)g_.K * g_.L * g_.dv * g_.M;
     k_axpby<R><<<grid_for(n), kThreads, 0, s>>>((long long)n, a, static_cast<const R*>(x), 1.0,
                                                 static_cast<R*>(y));
     FHP_LAUNCHED();
@@ -639,7 +658,7 @@ class Engine final : public EngineBase {
   }
 
   int rhs_macro(int proj, void* b, cudaStream_t s) override {
-    const size_t n = (size_t)g_.L * g_.dv * g_.M;
+    const size_t n = (size_t)g_.K * g_.L * g_.dv * g_.M;
     R* tmp = static_cast<R*>(scratch(SCR_RHS_TMP, n * sizeof(R)));
     if (!tmp) return ST_OOM;
     k_fill_macro<R><<<grid_for(n), kThreads, 0, s>>>(tmp, g_, -1.0);
@@ -670,7 +689,7 @@ class Engine final : public EngineBase {
     const R* b = static_cast<const R*>(bv);
     const R* x0 = static_cast<const R*>(x0v);
     R* x = static_cast<R*>(xv);
-    const size_t n = (size_t)g_.L * g_.dv * g_.M;
+    const size_t n = (size_t)g_.K * g_.L * g_.dv * g_.M;
     int st = ensure_cg_buffers();
     if (st != ST_OK) return st;
     R* va = static_cast<R*>(scratch(SCR_SOLV_A, n * sizeof(R)));
@@ -804,7 +823,7 @@ class Engine final : public EngineBase {
     cg_tol_ = tol;
     cg_x_ = x;
     if (cg_spectral_) return spectral_cg_begin(proj, b, x0, tol, maxiter, log_cap, s);
-    const size_t n = (size_t)g_.L * g_.dv * g_.M;
+    const size_t n = (size_t)g_.K * g_.L * g_.dv * g_.M;
     int st = ensure_cg_buffers();
     if (st != ST_OK) return st;
     // x = x0 ; R = B - A x0 ; P = R   (solver.py:114-117)
@@ -821,12 +840,12 @@ class Engine final : public EngineBase {
     FHP_CHECK(cudaMemcpyAsync(p_, r_, n * sizeof(R), cudaMemcpyDeviceToDevice, s));
     x_cur_ = x;
     if ((st = init_state(tol, maxiter, log_cap, s)) != ST_OK) return st;
-    k_dot<R><<<red_ctas_, kThreads, 0, s>>>(r_, r_, partials_, g_);
+    k_dot<R><<<dim3(red_ctas_, g_.K), kThreads, 0, s>>>(r_, r_, partials_, g_);
     FHP_LAUNCHED();
-    k_fin_init<<<1, 32, 0, s>>>(partials_, red_ctas_, st_, g_.L, 1.0 / (double)g_.M, cg_log_,
-                                cg_log_rows_);
+    k_fin_init<<<g_.K, 32, 0, s>>>(partials_, red_ctas_, st_, g_.L, 1.0 / (double)g_.M, cg_log_,
+                                   cg_log_rows_);
     FHP_LAUNCHED();
-    k_update_all_done<<<1, 1, 0, s>>>(st_, g_.L, all_done_);
+    k_update_all_done<<<1, 1, 0, s>>>(st_, g_.L * g_.K, all_done_);
     FHP_LAUNCHED();
     return ST_OK;
   }
@@ -861,19 +880,22 @@ class Engine final : public EngineBase {
 
   // per-load CG state, all_done and the residual log of a new solve
   int init_state(double tol, int maxiter, int log_cap, cudaStream_t s) {
-    for (int l = 0; l < g_.L; ++l) {
+    const int LK = g_.L * g_.K;
+    const bool per_load = (int)load_tol_.size() == LK;
+    for (int l = 0; l < LK; ++l) {
       LoadState& h = h_st_[l];
       std::memset(&h, 0, sizeof(LoadState));
-      h.tol = tol;
+      h.tol = per_load ? load_tol_[l] : tol;
       h.maxiter = maxiter;
       h.guard = sizeof(R) == 4 ? 4.0 : 0.0;
     }
-    FHP_CHECK(cudaMemcpyAsync(st_, h_st_, g_.L * sizeof(LoadState), cudaMemcpyHostToDevice, s));
+    load_tol_.clear();
+    FHP_CHECK(cudaMemcpyAsync(st_, h_st_, LK * sizeof(LoadState), cudaMemcpyHostToDevice, s));
     FHP_CHECK(cudaMemsetAsync(all_done_, 0, sizeof(int), s));
     cg_log_rows_ = std::max(1, std::min(log_cap, maxiter + 1));
-    cg_log_ = static_cast<double*>(scratch(SCR_LOG, (size_t)cg_log_rows_ * g_.L * sizeof(double)));
+    cg_log_ = static_cast<double*>(scratch(SCR_LOG, (size_t)cg_log_rows_ * LK * sizeof(double)));
     if (!cg_log_) return ST_OOM;
-    FHP_CHECK(cudaMemsetAsync(cg_log_, 0, (size_t)cg_log_rows_ * g_.L * sizeof(double), s));
+    FHP_CHECK(cudaMemsetAsync(cg_log_, 0, (size_t)cg_log_rows_ * LK * sizeof(double), s));
     return ST_OK;
   }
 
@@ -937,16 +959,17 @@ class Engine final : public EngineBase {
 
   // per-load results of a solve (solver.py:137-138) from the device state
   int collect(double tol, int log_rows, const double* dlog, SolveResult& res, cudaStream_t s) {
-    FHP_CHECK(cudaMemcpyAsync(h_st_, st_, g_.L * sizeof(LoadState), cudaMemcpyDeviceToHost, s));
-    res.res_log.assign((size_t)log_rows * g_.L, 0.0);
-    FHP_CHECK(cudaMemcpyAsync(res.res_log.data(), dlog, (size_t)log_rows * g_.L * sizeof(double),
+    const int LK = g_.L * g_.K;   // every cell's loads, cell-major
+    FHP_CHECK(cudaMemcpyAsync(h_st_, st_, LK * sizeof(LoadState), cudaMemcpyDeviceToHost, s));
+    res.res_log.assign((size_t)log_rows * LK, 0.0);
+    FHP_CHECK(cudaMemcpyAsync(res.res_log.data(), dlog, (size_t)log_rows * LK * sizeof(double),
                               cudaMemcpyDeviceToHost, s));
     FHP_CHECK(cudaStreamSynchronize(s));
-    res.kit.resize(g_.L);
-    res.norm_res.resize(g_.L);
-    res.status.resize(g_.L);
+    res.kit.resize(LK);
+    res.norm_res.resize(LK);
+    res.status.resize(LK);
     res.iterations_run = 0;
-    for (int l = 0; l < g_.L; ++l) {
+    for (int l = 0; l < LK; ++l) {
       const LoadState& h = h_st_[l];
       res.kit[l] = h.kit;
       res.norm_res[l] = h.kit == 0 ? 0.0 : h.norm_res;  // solver.py:137-138
@@ -1086,7 +1109,7 @@ class Engine final : public EngineBase {
                         int log_cap, cudaStream_t s) {
     int st = ensure_spectral();
     if (st != ST_OK) return st;
-    const size_t n = (size_t)g_.L * g_.dv * g_.M;
+    const size_t n = (size_t)g_.K * g_.L * g_.dv * g_.M;
     const size_t nz = (size_t)g_.L * g_.dv * g_.n0 * g_.n1 * g_.n2h;
     cplx<R>* zx = zb_;
     cplx<R>* zr = zb_ + nz;
@@ -1127,14 +1150,15 @@ class Engine final : public EngineBase {
     const int L = g_.L;
     if (band_) return band_energy(X, add_macro, AH, s);
     switch (coef_kind_) {
-      case COEF_ISO: k_energy<R, COEF_ISO><<<red_ctas_, 128, 0, s>>>(X, A_, partials_, g_, add_macro); break;
-      case COEF_SYM: k_energy<R, COEF_SYM><<<red_ctas_, 128, 0, s>>>(X, A_, partials_, g_, add_macro); break;
-      default: k_energy<R, COEF_FULL><<<red_ctas_, 128, 0, s>>>(X, A_, partials_, g_, add_macro); break;
+      case COEF_ISO: k_energy<R, COEF_ISO><<<dim3(red_ctas_, g_.K), 128, 0, s>>>(X, A_, partials_, g_, add_macro); break;
+      case COEF_SYM: k_energy<R, COEF_SYM><<<dim3(red_ctas_, g_.K), 128, 0, s>>>(X, A_, partials_, g_, add_macro); break;
+      default: k_energy<R, COEF_FULL><<<dim3(red_ctas_, g_.K), 128, 0, s>>>(X, A_, partials_, g_, add_macro); break;
     }
     FHP_LAUNCHED();
-    k_sum_partials<<<1, kThreads, 0, s>>>(partials_, red_ctas_, L * L, 1.0 / (double)g_.M, ad_);
+    k_sum_partials<<<g_.K, kThreads, 0, s>>>(partials_, red_ctas_, L * L, 1.0 / (double)g_.M, ad_);
     FHP_LAUNCHED();
-    FHP_CHECK(cudaMemcpyAsync(AH, ad_, (size_t)L * L * sizeof(double), cudaMemcpyDeviceToHost, s));
+    FHP_CHECK(cudaMemcpyAsync(AH, ad_, (size_t)g_.K * L * L * sizeof(double),
+                              cudaMemcpyDeviceToHost, s));
     FHP_CHECK(cudaStreamSynchronize(s));
     return ST_OK;
   }
@@ -1176,9 +1200,9 @@ class Engine final : public EngineBase {
     const LineDev<R>& lf = d == 3 ? l0_.dev : l1_.dev;
     const long long inner = d == 3 ? (long long)g_.n1 * g_.n2h : (long long)g_.n2h;
     const int T = d == 3 ? T0_ : tile_cols(lf.ld, 1, inner);
-    dim3 grid((unsigned)((inner + T - 1) / T), (unsigned)(g_.L * g_.dv));
+    dim3 grid((unsigned)((inner + T - 1) / T), (unsigned)(g_.L * g_.dv), (unsigned)g_.K);
     k_c2c_axis<R, false><<<grid, kThreads, (size_t)T * lf.ld * sizeof(cplx<R>), s>>>(
-        Sp, d == 3 ? g_.n0 : g_.n1, inner, lf, T, nullptr, nullptr, 0);
+        Sp, d == 3 ? g_.n0 : g_.n1, inner, lf, T, nullptr, nullptr, 0, g_.ss, g_.L);
     FHP_LAUNCHED();
     return ST_OK;
   }
@@ -1189,40 +1213,48 @@ class Engine final : public EngineBase {
     const LineDev<R>& lf = d == 3 ? l0_.dev : l1_.dev;
     const long long inner = d == 3 ? (long long)g_.n1 * g_.n2h : (long long)g_.n2h;
     const int T = d == 3 ? T0_ : tile_cols(lf.ld, 1, inner);
-    dim3 grid((unsigned)((inner + T - 1) / T), (unsigned)(g_.L * g_.dv));
+    dim3 grid((unsigned)((inner + T - 1) / T), (unsigned)(g_.L * g_.dv), (unsigned)g_.K);
     k_c2c_axis<R, true><<<grid, kThreads, (size_t)T * lf.ld * sizeof(cplx<R>), s>>>(
-        Sp, d == 3 ? g_.n0 : g_.n1, inner, lf, T, nullptr, nullptr, 0);
+        Sp, d == 3 ? g_.n0 : g_.n1, inner, lf, T, nullptr, nullptr, 0, g_.ss, g_.L);
     FHP_LAUNCHED();
     return inv_passes(Sp, static_cast<R*>(xv), (R)scale, false, nullptr, false, s);
   }
 
   int residual(const void* b, const void* ax, void* r, double* sumsq,
                cudaStream_t s) override {
-    k_residual<R><<<red_ctas_, kThreads, 0, s>>>(static_cast<const R*>(b),
+    k_residual<R><<<dim3(red_ctas_, g_.K), kThreads, 0, s>>>(static_cast<const R*>(b),
                                                  static_cast<const R*>(ax), static_cast<R*>(r),
                                                  partials_, g_);
     FHP_LAUNCHED();
-    k_sum_partials<<<1, kThreads, 0, s>>>(partials_, red_ctas_, g_.L, 1.0, ad_);
+    k_sum_partials<<<g_.K, kThreads, 0, s>>>(partials_, red_ctas_, g_.L, 1.0, ad_);
     FHP_LAUNCHED();
-    FHP_CHECK(cudaMemcpyAsync(sumsq, ad_, g_.L * sizeof(double), cudaMemcpyDeviceToHost, s));
+    FHP_CHECK(cudaMemcpyAsync(sumsq, ad_, (size_t)g_.K * g_.L * sizeof(double),
+                              cudaMemcpyDeviceToHost, s));
     FHP_CHECK(cudaStreamSynchronize(s));
     return ST_OK;
   }
 
+  // scale[] holds one value per load of every cell (host); the values go to
+  // the plan's device scale slots (the copy from pageable memory has read
+  // them when it returns)
   int scale_from64(const double* src, const double* scale, void* dst, cudaStream_t s) override {
-    LoadScale ls{};
-    for (int l = 0; l < g_.L; ++l) ls.v[l] = scale[l];
-    const size_t n = (size_t)g_.L * g_.dv * g_.M;
-    k_scale_from64<R><<<grid_for(n), kThreads, 0, s>>>(src, static_cast<R*>(dst), g_, ls);
+    const size_t LK = (size_t)g_.L * g_.K;
+    FHP_CHECK(cudaMemcpyAsync(dscale_, scale, LK * sizeof(double), cudaMemcpyHostToDevice, s));
+    const size_t n = (size_t)g_.K * g_.L * g_.dv * g_.M;
+    k_scale_from64<R><<<grid_for(n), kThreads, 0, s>>>(src, static_cast<R*>(dst), (long long)n,
+                                                        (long long)g_.dv * g_.M, dscale_);
     FHP_LAUNCHED();
     return ST_OK;
   }
 
   int add_scaled_to64(const void* d, const double* scale, double* x, cudaStream_t s) override {
-    LoadScale ls{};
-    for (int l = 0; l < g_.L; ++l) ls.v[l] = scale[l];
-    const size_t n = (size_t)g_.L * g_.dv * g_.M;
-    k_add_scaled_to64<R><<<grid_for(n), kThreads, 0, s>>>(static_cast<const R*>(d), x, g_, ls);
+    const size_t LK = (size_t)g_.L * g_.K;
+    double* ds = dscale_ + (size_t)g_.K * kMaxLoads;
+    FHP_CHECK(cudaMemcpyAsync(ds, scale, LK * sizeof(double), cudaMemcpyHostToDevice, s));
+    const size_t n = (size_t)g_.K * g_.L * g_.dv * g_.M;
+    k_add_scaled_to64<R><<<grid_for(n), kThreads, 0, s>>>(static_cast<const R*>(d), x,
+                                                           (long long)n, (long long)g_.dv * g_.M,
+                                                           ds);
     FHP_LAUNCHED();
     return ST_OK;
   }
@@ -1264,6 +1296,8 @@ class Engine final : public EngineBase {
   void* scr_[kScratchSlots] = {};
   size_t scr_bytes_[kScratchSlots] = {};
   double* ad_ = nullptr;
+  double* dscale_ = nullptr;   // per-load scales of the refinement (2 x cells x loads)
+  std::vector<double> load_tol_;   // per-load tolerances of the next solve (set_load_tols)
   LoadState* st_ = nullptr;
   LoadState* h_st_ = nullptr;
   int* all_done_ = nullptr;
@@ -1274,17 +1308,17 @@ class Engine final : public EngineBase {
   int nsm_ = 1, red_ctas_ = 1, nparts_max_ = 1;
 
   // algorithmic bytes of the passes (each input read once, each output written once)
-  double field_bytes() const { return (double)g_.L * g_.dv * g_.M * sizeof(R); }
+  double field_bytes() const { return (double)g_.K * g_.L * g_.dv * g_.M * sizeof(R); }
   // the solve grid's half spectrum (the buffer of band plans is larger: it
   // also holds the integration grid's spectra)
   double spec_bytes() const {
-    return (double)g_.L * g_.dv * g_.n0 * g_.n1 * g_.n2h * 2 * sizeof(R);
+    return (double)g_.K * g_.L * g_.dv * g_.n0 * g_.n1 * g_.n2h * 2 * sizeof(R);
   }
   double coef_bytes() const {
     const int dv = g_.dv;
     const int c = coef_kind_ == COEF_ISO ? 1 : coef_kind_ == COEF_SYM ? dv * (dv + 1) / 2
                 : coef_kind_ == COEF_FULL ? dv * dv : 0;
-    return (double)c * (band_ ? gi_.M : g_.M) * sizeof(R);
+    return (double)g_.K * c * (band_ ? gi_.M : g_.M) * sizeof(R);
   }
   int pbeg(const char* name, double bytes, cudaStream_t s) {
     if (!prof.on) return -1;
@@ -1427,7 +1461,7 @@ class Engine final : public EngineBase {
   }
 
   int ensure_cg_buffers() {
-    const size_t n = (size_t)g_.L * g_.dv * g_.M * sizeof(R);
+    const size_t n = (size_t)g_.K * g_.L * g_.dv * g_.M * sizeof(R);
     if (!r_) FHP_CHECK(cudaMalloc(&r_, n));
     if (!p_) FHP_CHECK(cudaMalloc(&p_, n));
     if (!ap_) FHP_CHECK(cudaMalloc(&ap_, n));
@@ -1464,6 +1498,7 @@ class Engine final : public EngineBase {
     if (ap_) cudaFree(ap_);
     if (partials_) cudaFree(partials_);
     if (ad_) cudaFree(ad_);
+    if (dscale_) cudaFree(dscale_);
     if (st_) cudaFree(st_);
     if (all_done_) cudaFree(all_done_);
     if (pe_) cudaFree(pe_);
@@ -1475,6 +1510,7 @@ class Engine final : public EngineBase {
     if (h_done_) cudaFreeHost(h_done_);
     if (h_st_) cudaFreeHost(h_st_);
     S_ = nullptr; A_ = nullptr; r_ = p_ = ap_ = nullptr;
+    ad_ = dscale_ = nullptr;
   }
 
   // pass 1 (+ axis-1 forward for 3D); leaves the spectrum ready for the
@@ -1483,7 +1519,7 @@ class Engine final : public EngineBase {
                  bool cg, cudaStream_t s) {
     const int* ad = cg ? all_done_ : nullptr;
     const LoadState* st = cg ? st_ : nullptr;
-    const dim3 grid1(row_ctas_);
+    const dim3 grid1(row_ctas_, g_.K);
     const double b1 = (pupd ? 3.0 : 1.0) * field_bytes() + (coef ? coef_bytes() : 0.0) +
                       spec_bytes();
     const int pk1 = pbeg(pupd ? "r2c_coef_pupd" : (coef ? "r2c_coef" : "r2c"), b1, s);
@@ -1508,10 +1544,11 @@ class Engine final : public EngineBase {
     pend(pk1, s);
     FHP_LAUNCHED();
     if (g_.dim == 3) {
-      dim3 grid((unsigned)((g_.n2h + T1_ - 1) / T1_), (unsigned)(g_.L * g_.dv * g_.n0));
+      dim3 grid((unsigned)((g_.n2h + T1_ - 1) / T1_), (unsigned)(g_.L * g_.dv * g_.n0),
+                (unsigned)g_.K);
       const int pk = pbeg("c2c_axis1_fwd", 2.0 * spec_bytes(), s);
       k_c2c_axis<R, false><<<grid, kThreads, (size_t)T1_ * l1_.dev.ld * sizeof(cplx<R>), s>>>(
-          Sp, g_.n1, (long long)g_.n2h, l1_.dev, T1_, ad, st, g_.dv * g_.n0);
+          Sp, g_.n1, (long long)g_.n2h, l1_.dev, T1_, ad, st, g_.dv * g_.n0, g_.ss, g_.L);
       pend(pk, s);
       FHP_LAUNCHED();
     }
@@ -1523,22 +1560,24 @@ class Engine final : public EngineBase {
     const int* ad = cg ? all_done_ : nullptr;
     const LoadState* st = cg ? st_ : nullptr;
     if (g_.dim == 3) {
-      dim3 grid((unsigned)((g_.n2h + T1_ - 1) / T1_), (unsigned)(g_.L * g_.dv * g_.n0));
+      dim3 grid((unsigned)((g_.n2h + T1_ - 1) / T1_), (unsigned)(g_.L * g_.dv * g_.n0),
+                (unsigned)g_.K);
       const int pk = pbeg("c2c_axis1_inv", 2.0 * spec_bytes(), s);
       k_c2c_axis<R, true><<<grid, kThreads, (size_t)T1_ * l1_.dev.ld * sizeof(cplx<R>), s>>>(
-          Sp, g_.n1, (long long)g_.n2h, l1_.dev, T1_, ad, st, g_.dv * g_.n0);
+          Sp, g_.n1, (long long)g_.n2h, l1_.dev, T1_, ad, st, g_.dv * g_.n0, g_.ss, g_.L);
       pend(pk, s);
       FHP_LAUNCHED();
     }
-    const dim3 grid1(row_ctas_);
+    const dim3 grid1(row_ctas_, g_.K);
     const int pk2 = pbeg(dot ? "c2r_dot" : "c2r", spec_bytes() + (dot ? 2.0 : 1.0) * field_bytes(), s);
     if (dot)
       k_c2r_last<R, true><<<grid1, kThreads, smem_rows_, s>>>(Sp, y, pdot, partials_, g_, l2_.dev,
-                                                              rows_, scale, ad, (int)c2r_stage_);
+                                                              rows_, scale, ad, (int)c2r_stage_,
+                                                              st);
     else
       k_c2r_last<R, false><<<grid1, kThreads, smem_rows_, s>>>(Sp, y, nullptr, nullptr, g_,
                                                                l2_.dev, rows_, scale, ad,
-                                                               (int)c2r_stage_);
+                                                               (int)c2r_stage_, st);
     pend(pk2, s);
     FHP_LAUNCHED();
     return ST_OK;
@@ -1548,7 +1587,7 @@ class Engine final : public EngineBase {
     const int d = g_.dim;
     const LineDev<R>& lp = d == 3 ? l0_.dev : l1_.dev;
     const long long inner = d == 3 ? (long long)g_.n1 * g_.n2h : (long long)g_.n2h;
-    dim3 grid((unsigned)((inner + Tp_ - 1) / Tp_), (unsigned)g_.L);
+    dim3 grid((unsigned)((inner + Tp_ - 1) / Tp_), (unsigned)g_.L, (unsigned)g_.K);
     const size_t smem = (size_t)Tp_ * g_.dv * lp.ld * sizeof(cplx<R>);
     const int pk = pbeg("proj_axis0", 2.0 * spec_bytes(), s);
     auto kproj = gp_.physics == 0 ? k_proj_first<R, 0> : k_proj_first<R, 1>;
@@ -1760,7 +1799,7 @@ class Engine final : public EngineBase {
       dim3 grid((unsigned)((n2h + T1_ - 1) / T1_), (unsigned)(g_.L * g_.dv * g_.n0));
       const int pk = pbeg("band_c2c_axis1_fwd", 2.0 * spec_bytes_n(), s);
       k_c2c_axis<R, false><<<grid, kThreads, (size_t)T1_ * l1_.dev.ld * sizeof(cplx<R>), s>>>(
-          SA, g_.n1, n2h, l1_.dev, T1_, ad, cg ? st_ : nullptr, g_.dv * g_.n0);
+          SA, g_.n1, n2h, l1_.dev, T1_, ad, cg ? st_ : nullptr, g_.dv * g_.n0, g_.ss, g_.L);
       pend(pk, s);
       FHP_LAUNCHED();
       BandAxis a0{g_.n0, gi_.n0, g_.n0, gi_.n0, gp_.h[0], (long long)g_.n1 * n2h, 1, 1, 2,
@@ -1786,7 +1825,7 @@ class Engine final : public EngineBase {
       dim3 grid((unsigned)((g_.n1 * n2h + T0_ - 1) / T0_), (unsigned)(g_.L * g_.dv));
       const int pk = pbeg("band_c2c_axis0_inv", 2.0 * spec_bytes_n(), s);
       k_c2c_axis<R, true><<<grid, kThreads, (size_t)T0_ * l0_.dev.ld * sizeof(cplx<R>), s>>>(
-          SA, g_.n0, (long long)g_.n1 * n2h, l0_.dev, T0_, ad, cg ? st_ : nullptr, g_.dv);
+          SA, g_.n0, (long long)g_.n1 * n2h, l0_.dev, T0_, ad, cg ? st_ : nullptr, g_.dv, g_.ss, g_.L);
       pend(pk, s);
       FHP_LAUNCHED();
     } else {
@@ -1799,11 +1838,12 @@ class Engine final : public EngineBase {
                          spec_bytes_n() + (dot ? 2.0 : 1.0) * field_bytes(), s);
     if (dot)
       k_c2r_last<R, true><<<grid1, kThreads, smem_rows_, s>>>(SA, y, pdot, partials_, g_, l2_.dev,
-                                                              rows_, (R)1, ad, (int)c2r_stage_);
+                                                              rows_, (R)1, ad, (int)c2r_stage_,
+                                                              nullptr);
     else
       k_c2r_last<R, false><<<grid1, kThreads, smem_rows_, s>>>(SA, y, nullptr, nullptr, g_,
                                                                l2_.dev, rows_, (R)1, ad,
-                                                               (int)c2r_stage_);
+                                                               (int)c2r_stage_, nullptr);
     pend(pk2, s);
     FHP_LAUNCHED();
     return ST_OK;
@@ -1816,7 +1856,7 @@ class Engine final : public EngineBase {
   // A_H via Parseval on the solve grid: W = band(A (X+E)) / prod(B), then
   // A_H[i][j] = <W_i, X_j + E_j>  (exact: X + E is band limited)
   int band_energy(const R* X, int add_macro, double* AH, cudaStream_t s) {
-    const size_t n = (size_t)g_.L * g_.dv * g_.M;
+    const size_t n = (size_t)g_.K * g_.L * g_.dv * g_.M;
     R* U = static_cast<R*>(scratch(SCR_BAND_U, n * sizeof(R)));
     R* W = static_cast<R*>(scratch(SCR_BAND_W, n * sizeof(R)));
     if (!U || !W) return ST_OOM;
@@ -1859,21 +1899,21 @@ class Engine final : public EngineBase {
   int cg_iteration(double* dlog, int log_rows, cudaStream_t s) {
     int st = run_operator(coef_kind_, true, nullptr, p_, r_, ap_, p_, s, true, true, true);
     if (st != ST_OK) return st;
-    k_fin_pap<<<g_.L, kThreads, 0, s>>>(partials_, row_ctas_, st_, g_.L, 1.0 / (double)g_.M,
-                                        all_done_);
+    k_fin_pap<<<dim3(g_.L, g_.K), kThreads, 0, s>>>(partials_, row_ctas_, st_, g_.L,
+                                                    1.0 / (double)g_.M, all_done_);
     FHP_LAUNCHED();
     const int pk = pbeg("cg_update", 6.0 * field_bytes(), s);
     // one component per grid row; the parts fit the reduction buffer
     const int C = g_.L * g_.dv;
     const int ux = std::max(1, red_ctas_ / C);
-    k_cg_update_comp<R><<<dim3((unsigned)ux, (unsigned)C), kThreads, 0, s>>>(
+    k_cg_update_comp<R><<<dim3((unsigned)ux, (unsigned)C, (unsigned)g_.K), kThreads, 0, s>>>(
         x_cur_, r_, p_, ap_, partials_, g_, st_, all_done_);
     pend(pk, s);
     FHP_LAUNCHED();
-    k_fin_rr<<<g_.L, kThreads, 0, s>>>(partials_, ux * C, st_, g_.L, 1.0 / (double)g_.M, dlog,
-                                       log_rows, all_done_);
+    k_fin_rr<<<dim3(g_.L, g_.K), kThreads, 0, s>>>(partials_, ux * C, st_, g_.L,
+                                                   1.0 / (double)g_.M, dlog, log_rows, all_done_);
     FHP_LAUNCHED();
-    k_update_all_done<<<1, 1, 0, s>>>(st_, g_.L, all_done_);
+    k_update_all_done<<<1, 1, 0, s>>>(st_, g_.L * g_.K, all_done_);
     FHP_LAUNCHED();
     return ST_OK;
   }

@@ -38,6 +38,12 @@ struct GridDims {
   int L;          // loads
   long long M;    // voxels
   FastDiv dn2, dn2h, dnp;  // division by n2, n2h and the pair-line count (L*dv+1)/2
+  // a plan batched over K cells of the same grid: cell k's fields, spectra and
+  // coefficient start k * sf, k * ss, k * sa elements further, its loads'
+  // states k * L entries further; the passes take the cell from the grid's
+  // instance dimension (K = 1: one cell)
+  int K = 1;
+  long long sf = 0, ss = 0, sa = 0;
 };
 
 inline void set_grid_divs(GridDims& g) {
@@ -253,6 +259,13 @@ __device__ __forceinline__ void block_sum_n(double (&acc)[NMAX], int n, double* 
 // pass 1: r2c along the last axis, with the coefficient multiply in the
 // prologue and (CG) the direction update P = R + beta P.
 // CTA: `rows` consecutive (i0,i1) rows, all comps; comps paired as z = a + i b.
+// every load of a cell has stopped (the CG passes skip the cell)
+__device__ __forceinline__ bool cell_done(const LoadState* __restrict__ st, int L) {
+  for (int l = 0; l < L; ++l)
+    if (!st[l].done) return false;
+  return true;
+}
+
 // ---------------------------------------------------------------------------
 template <typename R, int COEF, bool PUPD>
 __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_r2c_last(
@@ -260,6 +273,16 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_r2c_last(
     const R* __restrict__ A, cplx<R>* __restrict__ S, const __grid_constant__ GridDims g, const __grid_constant__ LineDev<R> L, int rows,
     const LoadState* __restrict__ st, const int* __restrict__ all_done) {
   if (all_done && *all_done) return;
+  {  // the cell of a batched plan (grid y)
+    const long long k = blockIdx.y;
+    if (xin) xin += k * g.sf;
+    if (pio) pio += k * g.sf;
+    if (rvec) rvec += k * g.sf;
+    if (A) A += k * g.sa;
+    S += k * g.ss;
+    if (st) st += k * g.L;
+  }
+  if (all_done && st && cell_done(st, g.L)) return;   // CG only (all_done given)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* buf = reinterpret_cast<cplx<R>*>(smem_raw);
   const int C = g.L * g.dv;
@@ -362,8 +385,13 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_c2c_axis(cplx<R>* __r
                                                   const __grid_constant__ LineDev<R> L, int T,
                                                   const int* __restrict__ all_done,
                                                   const LoadState* __restrict__ st,
-                                                  int outer_per_load) {
+                                                  int outer_per_load, long long cell_stride,
+                                                  int cell_loads) {
   if (all_done && *all_done) return;
+  // the cell of a batched plan (grid z): spectra cell_stride further, states
+  // cell_loads further
+  S += (long long)blockIdx.z * cell_stride;
+  if (st) st += (long long)blockIdx.z * cell_loads;
   if (st && outer_per_load > 0 && st[blockIdx.y / outer_per_load].done) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* buf = reinterpret_cast<cplx<R>*>(smem_raw);
@@ -411,6 +439,8 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_proj_first(cplx<R>* _
                                                     const LoadState* __restrict__ st) {
   if (all_done && *all_done) return;
   const int l = blockIdx.y;
+  S += (long long)blockIdx.z * g.ss;          // the cell of a batched plan
+  if (st) st += (long long)blockIdx.z * g.L;
   if (st && st[l].done) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* buf = reinterpret_cast<cplx<R>*>(smem_raw);
@@ -492,8 +522,18 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_c2r_last(const cplx<R
                                                   const R* __restrict__ pdot,
                                                   double* __restrict__ partials, const __grid_constant__ GridDims g,
                                                   const __grid_constant__ LineDev<R> L, int rows, R scale,
-                                                  const int* __restrict__ all_done, int stage) {
+                                                  const int* __restrict__ all_done, int stage,
+                                                  const LoadState* __restrict__ st) {
   if (all_done && *all_done) return;
+  {  // the cell of a batched plan (grid y); partial sums [cell][CTA][load]
+    const long long k = blockIdx.y;
+    S += k * g.ss;
+    y += k * g.sf;
+    if (pdot) pdot += k * g.sf;
+    if (partials) partials += k * gridDim.x * g.L;
+    if (st) st += k * g.L;
+  }
+  if (st && cell_done(st, g.L)) return;   // CG only: a cell whose loads have all stopped
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* buf = reinterpret_cast<cplx<R>*>(smem_raw);
   const int C = g.L * g.dv;
@@ -593,6 +633,9 @@ __global__ void __launch_bounds__(256, kFftMinBlocks<R>) k_c2r_last(const cplx<R
 template <typename R>
 __global__ void __launch_bounds__(256) k_dot(const R* __restrict__ x, const R* __restrict__ y,
                                              double* __restrict__ partials, GridDims g) {
+  x += (long long)blockIdx.y * g.sf;        // the cell of a batched plan (grid y)
+  y += (long long)blockIdx.y * g.sf;
+  partials += (long long)blockIdx.y * gridDim.x * g.L;
   __shared__ double red[8 * kMaxLoads];
   double acc[kMaxLoads];
   for (int i = 0; i < kMaxLoads; ++i) acc[i] = 0.;
@@ -669,6 +712,15 @@ __global__ void __launch_bounds__(256) k_cg_update_comp(R* __restrict__ x, R* __
                                                         const int* __restrict__ all_done) {
   if (all_done && *all_done) return;
   __shared__ double red[8];
+  {  // the cell of a batched plan (grid z); partial sums [cell][y][x][load]
+    const long long k = blockIdx.z;
+    x += k * g.sf;
+    r += k * g.sf;
+    p += k * g.sf;
+    ap += k * g.sf;
+    st += k * g.L;
+    partials += k * gridDim.x * gridDim.y * g.L;
+  }
   const int comp = blockIdx.y;
   const int l = comp / g.dv;
   const bool act = !st[l].done;
@@ -724,6 +776,8 @@ static __global__ void k_fin_pap(const double* __restrict__ partials, int nparts
                           double invM, const int* __restrict__ all_done) {
   if (all_done && *all_done) return;
   __shared__ double red[8];
+  partials += (long long)blockIdx.y * nparts * L;   // the cell of a batched plan (grid y)
+  st += (long long)blockIdx.y * L;
   const int l = blockIdx.x;
   if (st[l].done) return;
   double s = 0.;
@@ -753,6 +807,10 @@ static __global__ void k_fin_rr(const double* __restrict__ partials, int nparts,
   __shared__ double red[8];
   const int l = blockIdx.x;
   if (*all_done) return;
+  // the cell of a batched plan (grid y); residual log rows of gridDim.y * L
+  const int cell = blockIdx.y;
+  partials += (long long)cell * nparts * L;
+  st += (long long)cell * L;
   const bool was_done = st[l].done;
   if (!was_done) {
     double s = 0.;
@@ -769,7 +827,8 @@ static __global__ void k_fin_rr(const double* __restrict__ partials, int nparts,
       S.beta = rrn / S.rr;
       S.rr = rrn;
       S.norm_res = sqrt(rrn);
-      if (res_log && S.kit < log_cap) res_log[(long long)S.kit * L + l] = S.norm_res;
+      if (res_log && S.kit < log_cap)
+        res_log[(long long)S.kit * L * gridDim.y + (long long)cell * L + l] = S.norm_res;
       if (!isfinite(rrn)) { S.status = 3; S.done = 1; }
       if (!(S.norm_res > S.tol && S.kit < S.maxiter)) S.done = 1;
       if (S.norm_res < S.min_norm) S.min_norm = S.norm_res;
@@ -795,6 +854,11 @@ static __global__ void k_fin_init(const double* __restrict__ partials, int npart
                            double invM, double* __restrict__ res_log, int log_cap) {
   const int l = threadIdx.x;
   if (l >= L) return;
+  // the cell of a batched plan (grid x); residual log rows of gridDim.x * L
+  const int cell = blockIdx.x;
+  partials += (long long)cell * nparts * L;
+  st += (long long)cell * L;
+  if (res_log) res_log += (long long)cell * L;
   double s = 0.;
   for (int i = 0; i < nparts; ++i) s += partials[(long long)i * L + l];
   LoadState& S = st[l];
@@ -822,10 +886,11 @@ __global__ void k_axpby(long long n, double a, const R* __restrict__ x, double b
 template <typename R>
 __global__ void k_fill_macro(R* __restrict__ x, GridDims g, double val) {
   const long long stride = (long long)gridDim.x * blockDim.x;
-  const long long tot = (long long)g.L * g.dv * g.M;
+  const long long tot = (long long)g.K * g.L * g.dv * g.M;   // every cell of a batched plan
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += stride) {
     const long long comp = i / g.M;
-    const int l = (int)(comp / g.dv), c = (int)(comp - (long long)l * g.dv);
+    const long long j = comp / g.dv;
+    const int c = (int)(comp - j * g.dv), l = (int)(j % g.L);
     x[i] = (c == l) ? (R)val : R(0);
   }
 }
@@ -836,6 +901,12 @@ template <typename R, int COEF>
 __global__ void __launch_bounds__(128) k_energy(const R* __restrict__ X, const R* __restrict__ A,
                                                 double* __restrict__ partials, GridDims g,
                                                 int add_macro) {
+  {  // the cell of a batched plan (grid y); partial sums [cell][CTA][L * L]
+    const long long k = blockIdx.y;
+    X += k * g.sf;
+    A += k * g.sa;
+    partials += k * gridDim.x * g.L * g.L;
+  }
   __shared__ double red[4 * kMaxLoads * kMaxLoads];
   const int L = g.L, dv = g.dv;
   double acc[kMaxLoads * kMaxLoads];
@@ -936,6 +1007,8 @@ __global__ void __launch_bounds__(128) k_energy_grad(const R* __restrict__ X,
 // sum partials[nparts][n] -> out[n] (one block)
 static __global__ void k_sum_partials(const double* __restrict__ partials, int nparts, int n,
                                double scale, double* __restrict__ out) {
+  partials += (long long)blockIdx.x * nparts * n;   // the cell of a batched plan (grid x)
+  out += (long long)blockIdx.x * n;
   for (int j = 0; j < n; ++j) {
     double s = 0.;
     for (int i = threadIdx.x; i < nparts; i += blockDim.x) s += partials[(long long)i * n + j];
@@ -2200,13 +2273,19 @@ __global__ void k_add_macro(const R* __restrict__ X, R* __restrict__ U, GridDims
   }
 }
 
-struct LoadScale { double v[kMaxLoads]; };
 
 // r = b - ax ; partial sum r^2 per load
 template <typename R>
 __global__ void __launch_bounds__(256) k_residual(const R* __restrict__ b, const R* __restrict__ ax,
                                                   R* __restrict__ r, double* __restrict__ partials,
                                                   GridDims g) {
+  {  // the cell of a batched plan (grid y)
+    const long long k = blockIdx.y;
+    b += k * g.sf;
+    ax += k * g.sf;
+    r += k * g.sf;
+    partials += k * gridDim.x * g.L;
+  }
   __shared__ double red[8 * kMaxLoads];
   double acc[kMaxLoads];
   for (int i = 0; i < kMaxLoads; ++i) acc[i] = 0.;
@@ -2222,24 +2301,23 @@ __global__ void __launch_bounds__(256) k_residual(const R* __restrict__ b, const
   block_sum_n(acc, g.L, red, partials + (long long)blockIdx.x * g.L);
 }
 
-// dst = s_l * src, src in FP64 (refinement: scaled residual into the working precision)
+// dst = s_j * src, src in FP64, s one scale per load of every cell (device,
+// cells x loads; refinement: scaled residual into the working precision)
 template <typename RO>
-__global__ void k_scale_from64(const double* __restrict__ src, RO* __restrict__ dst, GridDims g,
-                               LoadScale s) {
+__global__ void k_scale_from64(const double* __restrict__ src, RO* __restrict__ dst, long long tot,
+                               long long per, const double* __restrict__ s) {
   const long long stride = (long long)gridDim.x * blockDim.x;
-  const long long tot = (long long)g.L * g.dv * g.M;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += stride)
-    dst[i] = (RO)(s.v[i / ((long long)g.dv * g.M)] * src[i]);
+    dst[i] = (RO)(s[i / per] * src[i]);
 }
 
-// x += s_l * d, x in FP64 (refinement: correction of the working precision)
+// x += s_j * d, x in FP64 (refinement: correction of the working precision)
 template <typename RI>
-__global__ void k_add_scaled_to64(const RI* __restrict__ d, double* __restrict__ x, GridDims g,
-                                  LoadScale s) {
+__global__ void k_add_scaled_to64(const RI* __restrict__ d, double* __restrict__ x, long long tot,
+                                  long long per, const double* __restrict__ s) {
   const long long stride = (long long)gridDim.x * blockDim.x;
-  const long long tot = (long long)g.L * g.dv * g.M;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += stride)
-    x[i] += s.v[i / ((long long)g.dv * g.M)] * (double)d[i];
+    x[i] += s[i / per] * (double)d[i];
 }
 
 // precision conversion

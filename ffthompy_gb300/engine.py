@@ -91,11 +91,21 @@ class GalerkinPlan:
     integ_kernel (band plans): 'register' runs the integration pass with
     lines held in registers where that kernel applies, 'shared' with the
     shared-memory line cores.
+    ncells (GaNi / full-grid Ga): cells of the same grid solved together
+    (fhp_plan_create_cells): fields (cells, loads, dv) + N, packed
+    coefficients (cells, c) + N, per-load results cell-major, A_H
+    (cells, L, L); each load of each cell keeps its own CG state.
     """
 
     def __init__(self, N, Y, physics='scalar', nloads=None, band=None, scale=None,
-                 precision='f64', integ=None, band_cg='spectral', integ_kernel='register'):
+                 precision='f64', integ=None, band_cg='spectral', integ_kernel='register',
+                 ncells=1):
         require_cuda()
+        self.ncells = int(ncells)
+        if self.ncells < 1:
+            raise ValueError('ncells must be >= 1')
+        if self.ncells > 1 and integ is not None:
+            raise ValueError('band plans hold one cell')
         self.lib = _lib.load()
         self.N = tuple(int(n) for n in N)
         self.dim = len(self.N)
@@ -129,6 +139,10 @@ class GalerkinPlan:
             _lib.check(self.lib.fhp_plan_create_band(ctypes.byref(h), self.dim, n, ni, y, phys,
                                                      self.nloads, self.scale, prec),
                        'fhp_plan_create_band')
+        elif self.ncells > 1:
+            _lib.check(self.lib.fhp_plan_create_cells(ctypes.byref(h), self.dim, n, nb, y, phys,
+                                                      self.nloads, self.scale, prec,
+                                                      self.ncells), 'fhp_plan_create_cells')
         else:
             _lib.check(self.lib.fhp_plan_create(ctypes.byref(h), self.dim, n, nb, y, phys,
                                                 self.nloads, self.scale, prec),
@@ -155,7 +169,14 @@ class GalerkinPlan:
     # -- helpers ---------------------------------------------------------------
     @property
     def field_shape(self):
-        return (self.nloads, self.dv) + self.N
+        """(loads, dv) + N; (cells, loads, dv) + N for a plan of several cells."""
+        lead = (self.ncells,) if self.ncells > 1 else ()
+        return lead + (self.nloads, self.dv) + self.N
+
+    @property
+    def _lk(self):
+        # per-load results: every load of every cell, cell-major
+        return self.nloads * self.ncells
 
     @property
     def coef_grid(self):
@@ -204,7 +225,10 @@ class GalerkinPlan:
 
     # -- API -------------------------------------------------------------------
     def set_coefficient(self, A, kind=None):
-        """A: (dv, dv) + N coefficient (numpy, or torch on the GPU), origin 0."""
+        """A: (dv, dv) + N coefficient (numpy, or torch on the GPU), origin 0.
+        Plans of several cells take packed values (set_coefficient_packed)."""
+        if self.ncells > 1:
+            raise ValueError('a plan of several cells takes set_coefficient_packed')
         shape = (self.dv, self.dv) + self.coef_grid
         if tuple(A.shape) != shape:
             raise ValueError('coefficient shape %s, expected %s' % (tuple(A.shape), shape))
@@ -230,7 +254,7 @@ class GalerkinPlan:
         GPU) of kind FHP_COEF_ISO / SYM / FULL (c = 1, dv(dv+1)/2, dv*dv)."""
         c = {_lib.FHP_COEF_ISO: 1, _lib.FHP_COEF_SYM: self.dv * (self.dv + 1) // 2,
              _lib.FHP_COEF_FULL: self.dv * self.dv}[kind]
-        shape = (c,) + self.coef_grid
+        shape = ((self.ncells,) if self.ncells > 1 else ()) + (c,) + self.coef_grid
         if tuple(vals.shape) != shape:
             vals = vals.reshape(shape)
         if isinstance(vals, torch.Tensor) and vals.is_cuda:
@@ -260,14 +284,15 @@ class GalerkinPlan:
         return b
 
     def cg(self, b, x0=None, tol=1e-6, maxiter=1000, proj=1, log_rows=None):
-        """Batched CG; returns (x, info) with per-load kit / norm_res / res_log."""
+        """Batched CG; returns (x, info) with per-load kit / norm_res / res_log
+        (every load of every cell, cell-major, for a plan of several cells)."""
         b = self._dev(b)
         x0p = ctypes.c_void_p(None)
         if x0 is not None:
             x0 = self._dev(x0)
             x0p = self._ptr(x0)
         x = self.empty()
-        L = self.nloads
+        L = self._lk
         kit = (ctypes.c_int * L)()
         nres = (ctypes.c_double * L)()
         stat = (ctypes.c_int * L)()
@@ -327,10 +352,11 @@ class GalerkinPlan:
         return tuple(ch), float(ms.value)
 
     def energy(self, X, add_macro=True):
-        """A_H[i, j] = <A u_i, u_j> over the solve grid (u = X + E if add_macro)."""
+        """A_H[i, j] = <A u_i, u_j> over the solve grid (u = X + E if add_macro);
+        (cells, L, L) for a plan of several cells."""
         X = self._dev(X)
         L = self.nloads
-        AH = np.zeros((L, L))
+        AH = np.zeros(((self.ncells,) if self.ncells > 1 else ()) + (L, L))
         _lib.check(self.lib.fhp_energy_matrix(self.handle, self._ptr(X), int(bool(add_macro)),
                                               AH.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                                               self._stream()), 'fhp_energy_matrix')
@@ -444,9 +470,9 @@ class GalerkinPlan:
             kind = coef_kind_of(A)
             vals = pack_coefficient(A, kind)
         L = self.nloads
-        AH = np.zeros((L, L))
-        kit = (ctypes.c_int * L)()
-        nres = (ctypes.c_double * L)()
+        AH = np.zeros(((self.ncells,) if self.ncells > 1 else ()) + (L, L))
+        kit = (ctypes.c_int * self._lk)()
+        nres = (ctypes.c_double * self._lk)()
         xh = None
         xp = ctypes.c_void_p(None)
         if return_solution:
@@ -479,7 +505,7 @@ def cg_many(plans, bs, tol=1e-6, maxiter=1000, proj=1):
     hs = (ctypes.c_void_p * n)(*[p.handle.value for p in plans])
     bp = (ctypes.c_void_p * n)(*[b.data_ptr() for b in bs])
     xp = (ctypes.c_void_p * n)(*[x.data_ptr() for x in xs])
-    tot = sum(p.nloads for p in plans)
+    tot = sum(p._lk for p in plans)
     kit = (ctypes.c_int * tot)()
     nres = (ctypes.c_double * tot)()
     stat = (ctypes.c_int * tot)()
@@ -488,7 +514,7 @@ def cg_many(plans, bs, tol=1e-6, maxiter=1000, proj=1):
     _lib.check(st, 'fhp_cg_solve_many')
     out, off = [], 0
     for p, x in zip(plans, xs):
-        L = p.nloads
+        L = p._lk
         out.append((x, {'kit': list(kit[off:off + L]), 'norm_res': list(nres[off:off + L]),
                         'status': list(stat[off:off + L])}))
         off += L

@@ -60,6 +60,24 @@ const char* fhp_last_error(void);
 int fhp_plan_create(fhp_plan* out, int dim, const int* n, const int* n_band, const double* Y,
                     int physics, int nloads, double g_scale, int precision);
 /*
+ * A plan of ncells cells of the same grid (1..65535), solved together: every
+ * pass launches once for all cells.  Device fields are [cell][load][component]
+ * [grid], the coefficient of fhp_set_coefficient is [cell][c][grid], and the
+ * per-load arrays of fhp_cg_solve / fhp_cg_solve_many / fhp_homogenize_host
+ * and the A_H of fhp_energy_matrix hold every cell, cell-major
+ * (ncells * nloads entries, ncells * nloads * nloads for A_H).  Each load of
+ * each cell keeps its own CG state and stops on its own test; passes skip the
+ * cells whose loads have all stopped.  The potential formulation, the other
+ * solvers, fhp_energy_gradient and fhp_fourier_interp take single-cell plans.
+ * Replaces: the per-cell loop over applications.scalar
+ * (ffthompy/applications.py:24-82) for an ensemble of cells of one size.
+ */
+int fhp_plan_create_cells(fhp_plan* out, int dim, const int* n, const int* n_band,
+                          const double* Y, int physics, int nloads, double g_scale,
+                          int precision, int ncells);
+/* Cells of a plan (1 unless created by fhp_plan_create_cells; 0 for NULL). */
+int fhp_plan_cells(fhp_plan plan);
+/*
  * Band-representation plan for Galerkin with exact integration (Ga): the CG
  * fields live on the solve grid n (they are trigonometric polynomials of the
  * band |k_i| <= (Nodd_i-1)/2, so nothing is lost), the coefficient is given on

@@ -44,6 +44,10 @@ def test_status_strings_and_bad_args(lib):
     assert lib.fhp_plan_create(ctypes.byref(h), 2, n, n, y, 7, 2, 1.0, 0) == 5
     assert lib.fhp_plan_create(ctypes.byref(h), 2, n, n, y, 0, 2, -1.0, 0) == 5
     assert lib.fhp_plan_create(None, 2, n, n, y, 0, 2, 1.0, 0) == 5
+    # plans of several cells: 1..65535 cells
+    assert lib.fhp_plan_create_cells(ctypes.byref(h), 2, n, n, y, 0, 2, 1.0, 0, 0) == 5
+    assert lib.fhp_plan_create_cells(ctypes.byref(h), 2, n, n, y, 0, 2, 1.0, 0, 65536) == 5
+    assert lib.fhp_plan_cells(None) == 0
     assert lib.fhp_apply(None, 1, None, None, None) == 5
     assert b'required' in lib.fhp_last_error()
 

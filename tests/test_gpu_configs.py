@@ -353,3 +353,87 @@ def test_batched_and_threaded_ensembles_agree():
         for pd in ('primal', 'dual'):
             assert ra['kit_' + pd] == rb['kit_' + pd]
             assert np.abs(ra[pd] - rb[pd]).max() < 1e-12 * np.abs(rb[pd]).max()
+
+
+def _spd_field(dv, N, rng):
+    """A symmetric positive definite (dv, dv) + N coefficient with varying
+    eigenvalues (full-kind packing for dv > 1)."""
+    B = 0.3 * rng.standard_normal((dv, dv) + N)
+    A = np.einsum('ik...,jk...->ij...', B, B)
+    for i in range(dv):
+        A[i, i] += 1.0 + 9.0 * rng.random(N)
+    return A
+
+
+def _cell_cases(case, rng):
+    if case == '2d':       # same size, contrasts 2..1000: different iteration counts
+        return 'scalar', _grf_instances(5, [33], seed=4)
+    if case == '3d':
+        return 'scalar', [_spd_field(3, (15, 15, 15), rng) for _ in range(3)]
+    return 'elasticity', [_spd_field(6, (9, 9, 9), rng) for _ in range(2)]
+
+
+@pytest.mark.parametrize('precision', ['f64', 'f32', 'mixed'])
+@pytest.mark.parametrize('case', ['2d', '3d', 'elast'])
+def test_cell_plan_equals_single_cell_plans(case, precision):
+    """A plan of several cells of one grid (fhp_plan_create_cells: every pass
+    one launch for all cells) runs each cell's own CG: per cell the same
+    iteration counts, statuses, solutions and A_H as a plan of that cell
+    alone, for both projections; 2D and 3D scalar, 3D elasticity."""
+    from ffthompy_gb300.engine import GalerkinPlan, coef_kind_of, pack_coefficient
+    rng = np.random.default_rng(7)
+    physics, coefs = _cell_cases(case, rng)
+    N = coefs[0].shape[2:]
+    K = len(coefs)
+    Y = np.ones(len(N))
+    kind = max(coef_kind_of(A) for A in coefs)
+    vals = np.stack([pack_coefficient(A, kind) for A in coefs])
+    tol = 1e-5 if precision == 'f32' else 1e-9
+    cells = GalerkinPlan(N, Y, physics=physics, precision=precision, ncells=K)
+    assert int(cells.lib.fhp_plan_cells(cells.handle)) == K
+    cells.set_coefficient_packed(vals, kind)
+    singles = [GalerkinPlan(N, Y, physics=physics, precision=precision) for _ in coefs]
+    for p, v in zip(singles, vals):
+        p.set_coefficient_packed(v, kind)
+    L = cells.nloads
+    for proj in (1, 2):
+        b = cells.rhs_macro(proj)
+        assert tuple(b.shape) == (K, L, cells.dv) + tuple(N)
+        X, info = cells.cg(b, tol=tol, maxiter=600, proj=proj)
+        AH = cells.energy(X)
+        assert AH.shape == (K, L, L)
+        for k, p in enumerate(singles):
+            bk = p.rhs_macro(proj)
+            assert float((b[k] - bk).abs().max()) <= 1e-12 * float(bk.abs().max())
+            Xk, ik = p.cg(bk, tol=tol, maxiter=600, proj=proj)
+            assert info['kit'][k * L:(k + 1) * L] == ik['kit'], (k, info['kit'], ik['kit'])
+            assert info['status'][k * L:(k + 1) * L] == ik['status']
+            d = float((X[k] - Xk).abs().max()) / max(float(Xk.abs().max()), 1e-300)
+            assert d < (1e-6 if precision == 'f32' else 1e-12), (k, d)
+            AHk = p.energy(Xk)
+            assert np.abs(AH[k] - AHk).max() <= (1e-6 if precision == 'f32' else 1e-12) * \
+                np.abs(AHk).max()
+    if case == '2d':
+        kits = [info['kit'][k * L] for k in range(K)]
+        assert len(set(kits)) > 1, kits      # the cells stopped at different iterations
+
+
+def test_cells_mode_matches_threads():
+    """homogenize_many(mode='cells') - one plan of several cells per grid size,
+    the sizes advanced together - gives each cell the A_H and iteration counts
+    of the thread-pool mode, primal and dual."""
+    from ffthompy_gb300.batch import homogenize_many
+    coefs = _grf_instances(14, [31, 63, 127], seed=21)
+    a = homogenize_many(coefs, tol=1e-8, primaldual=('primal', 'dual'), mode='cells')
+    b = homogenize_many(coefs, tol=1e-8, primaldual=('primal', 'dual'), mode='threads',
+                        workers=4)
+    # the launch shapes are tuned per plan (cells or single), so reductions
+    # may group differently: equally accurate roundoff, a few % of the
+    # iteration count at contrast 1000
+    for ra, rb in zip(a, b):
+        for pd in ('primal', 'dual'):
+            assert all(abs(x - y) <= max(1, int(0.02 * y))
+                       for x, y in zip(ra['kit_' + pd], rb['kit_' + pd])), \
+                (ra['kit_' + pd], rb['kit_' + pd])
+            assert ra['status_' + pd] == [0, 0]
+            assert np.abs(ra[pd] - rb[pd]).max() < 1e-10 * np.abs(rb[pd]).max()
