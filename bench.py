@@ -349,7 +349,9 @@ def ensemble_measure(count=512, sizes=(63, 127, 255, 511), seed=12, tol=1e-6, wo
     length 0.1, 0.4-quantile, contrast log-uniform in [2, 1000], n drawn from
     sizes, 2 loads each) solved together by homogenize_many to tol (FP64, or
     mixed: FP32 inner CG refined in FP64): aggregate Mvoxel-iter/s over all
-    instances.  Under torchrun the cells are split across the ranks
+    instances.  The cells of one size share one plan of several cells (every
+    pass one launch for all of them), and the four sizes advance together in
+    one graph per iteration.  Under torchrun the cells are split across the ranks
     (homogenize_many_ranks) and the time is the slowest rank's."""
     import torch
     from ffthompy_gb300 import workloads
@@ -363,17 +365,19 @@ def ensemble_measure(count=512, sizes=(63, 127, 255, 511), seed=12, tol=1e-6, wo
                                                      contrast=contrast,
                                                      seed=int(rng.integers(1 << 30))))
     # warm: the plan pool (one plan per cell), the autotuned launch shapes
-    homogenize_many(coefs, tol=tol, workers=workers, precision=precision)
+    homogenize_many(coefs, tol=tol, workers=workers, precision=precision, mode='cells')
     torch.cuda.synchronize()
     barrier(dist)
     t0 = time.perf_counter()
-    res = homogenize_many_ranks(coefs, tol=tol, workers=workers, precision=precision)
+    res = homogenize_many_ranks(coefs, tol=tol, workers=workers, precision=precision,
+                                mode='cells')
     torch.cuda.synchronize()
     dt = reduce_max(dist, time.perf_counter() - t0)
     if res is None:     # not rank 0
         return None
     vox_it = sum(int(np.prod(A.shape[2:])) * sum(r['kit_primal']) for A, r in zip(coefs, res))
     return {'instances': count, 'sizes': list(sizes), 'loads': 2, 'precision': precision,
+            'mode': 'cells',
             'tol': tol, 'voxels': int(sum(np.prod(A.shape[2:]) for A in coefs)),
             'ranks': 1 if dist is None else dist.get_world_size(),
             'seconds': dt, 'Mvoxel_iter_per_s': vox_it / dt / 1e6,
@@ -532,6 +536,19 @@ def run_kernels_only(args, w, A, M, dist, world, rank):
                           'cg_iterations': info['kit'], 'seconds': dt,
                           'Mvoxel_iter_per_s': M * sum(kits) / max(dt, 1e-9) / 1e6}),
               flush=True)
+
+
+def _h2d_ms(torch, h):
+    """Milliseconds of one host-to-device copy of the host tensor h."""
+    d = torch.empty(h.shape, dtype=h.dtype, device='cuda')
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    d.copy_(h, non_blocking=True)
+    e1.record()
+    torch.cuda.synchronize()
+    return round(e0.elapsed_time(e1), 3)
 
 
 def _h2d_gbps(torch, nbytes=1 << 30):
@@ -712,13 +729,14 @@ def run_gpu(args):
 
     # end to end through the host-buffer C-ABI entry point
     # the coefficient as a user holds it: a pinned host array written by the
-    # CPU (a pinned buffer filled by a device-to-host copy uploaded at a tenth
-    # of the link rate on this machine, see e2e_phases)
+    # CPU; e2e_phases times torch's upload of the same buffer before and after
+    # the library calls, and of fresh pinned buffers
     A_np = A_iso.cpu().numpy()
     host_A = torch.empty(tuple(A_iso.shape), dtype=torch.float64, pin_memory=True)
     A_host = host_A.numpy()
     np.copyto(A_host, A_np)
-    del A_np
+    ph = {}
+    ph['torch_h2d_host_buffer_before_calls_ms'] = _h2d_ms(torch, host_A)
     e2e_plan = make_plan(w, args.precision, args.ga_mode)
     e2e_plan.set_coefficient(A.data)
     e2e_plan.autotune()     # the cached choice of the timed plan
@@ -740,7 +758,6 @@ def run_gpu(args):
            'seconds_per_step': e2e_s / e2e_steps}
     extras['AH_e2e_rel_diff'] = float(np.abs(AHe - AH).max() / np.abs(AH).max())
     # the same phases through the package API, each bracketed by CUDA events
-    ph = {}
     evs = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -777,6 +794,13 @@ def run_gpu(args):
     torch.cuda.synchronize()
     ph['torch_h2d_same_buffer_ms'] = round(evs[0].elapsed_time(evs[1]), 3)
     del dev_A
+    # a pinned buffer that does not come from torch's host-block cache
+    if hasattr(torch._C, '_host_emptyCache'):
+        torch._C._host_emptyCache()
+    fresh = torch.empty(tuple(A_iso.shape), dtype=torch.float64, pin_memory=True)
+    np.copyto(fresh.numpy(), A_np)
+    ph['torch_h2d_fresh_cpu_filled_ms'] = _h2d_ms(torch, fresh)
+    del fresh, A_np
     ph['h2d_fresh_pinned_GBps_at_start'] = h2d_start
     ph['h2d_fresh_pinned_GBps_here'] = _h2d_gbps(torch)
     extras['e2e_phases'] = ph

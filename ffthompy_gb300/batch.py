@@ -5,8 +5,11 @@ fields of possibly different grids - the reference would run
 applications.scalar / elasticity (ffthompy/applications.py:11-90, 93-176) once
 per instance - and returns one A_H per instance.
 
-mode='threads' (the default), mode='cells' and mode='batched' give the same
-per-cell results.
+mode='cells' (the default), mode='threads' and mode='batched' give the same
+per-cell results.  On the 512-cell 2D ensemble (n in 63..511, 2 loads, tol
+1e-6) a GB300 takes 1.8 s mixed and 8.7 s FP64 in mode='cells', 2.7 s and
+9.8 s in mode='threads', 4.5 s and 13.2 s in mode='batched'.  FP64 time is
+bound by the FP64 arithmetic of the Bluestein lines (127- and 511-point).
 
 mode='cells': the cells of one grid size share one plan of several cells
 (GalerkinPlan(ncells=K), fhp_plan_create_cells): every pass of an iteration is
@@ -60,7 +63,7 @@ def _pooled_plans(key, count, make):
 
 
 def homogenize_many(coefs, Y=None, physics='scalar', tol=1e-6, maxiter=1000,
-                    precision='f64', workers=16, primaldual=('primal',), mode='threads'):
+                    precision='f64', workers=16, primaldual=('primal',), mode='cells'):
     """coefs: sequence of (dv, dv) + N coefficient arrays (numpy or torch),
     origin-0 grid values as Material.get_A_GaNi returns them.  Returns a list
     of {'primal': A_H (L x L numpy), 'kit': [...], 'status': [...]} (and
