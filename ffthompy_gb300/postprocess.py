@@ -8,12 +8,18 @@ postprocess.py:60-66) - the upper bound from the primal problem and, through
 inv(A_H), the lower bound from the dual problem (postprocess.py:43-46).
 Energies A_H[i,j] = <A (X_i+E_i), X_j+E_j> are accumulated in FP64 by one GPU
 kernel over all load pairs (fhp_energy_matrix).
+
+The Ga coefficient is sampled on nice_size(2N-1) (factors 2, 3, 5, 7) instead
+of 2N-1 itself: the same trigonometric polynomial (its frequencies lie in the
+2N-1 band), and the energy with band-limited solutions is exact on any grid
+of at least 2N-1 points per axis, so A_H is the reference's; a 2N-1 with a
+large prime factor (253 = 11 x 23) would otherwise take Bluestein lines.
 """
 import time
 
 import numpy as np
 
-from .engine import GalerkinPlan, interpolate_fields
+from .engine import GalerkinPlan, interpolate_fields, nice_size
 from .tensors.objects import Tensor
 
 
@@ -96,13 +102,17 @@ def postprocess(pb, A, mat, solutions, results, primaldual):
             order_name = Nname = ''
             if 'order' in pp:
                 Npp = tuple(2 * N - 1)
+                G = tuple(nice_size(int(n)) for n in Npp)
+                if not all(g >= 2 * n - 1 for g, n in zip(G, solutions.plan.N)):
+                    G = Npp     # solutions on the double grid (full-grid Ga solve)
                 if pp['order'] is None:
-                    Ap = mat.get_A_Ga(Nbar=Npp, primaldual=primaldual, order=pp['order'])
+                    Ap = mat.get_A_Ga(Nbar=Npp, primaldual=primaldual, order=pp['order'],
+                                      grid=G)
                 else:
                     order_name = '_o' + str(pp['order'])
                     Nname = '_P%d' % np.mean(pp['P'])
                     Ap = mat.get_A_Ga(Nbar=Npp, primaldual=primaldual, order=pp['order'],
-                                      P=pp['P'])
+                                      P=pp['P'], grid=G)
         else:
             raise ValueError('postprocess kind %s' % pp['kind'])
         name = 'AH_%s%s%s_%s' % (pp['kind'], order_name, Nname, primaldual)
