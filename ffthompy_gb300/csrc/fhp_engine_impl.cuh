@@ -1448,7 +1448,10 @@ class Engine final : public EngineBase {
     FHP_ATTR((k_band_last<R, COEF_ISO>));
     FHP_ATTR((k_band_last<R, COEF_SYM>));
     FHP_ATTR((k_band_last<R, COEF_FULL>));
-    if constexpr (sizeof(R) == 4) FHP_ATTR((k_band_last_r512<R>));
+    if constexpr (sizeof(R) == 4) {
+      FHP_ATTR((k_band_last_r512<R, false>));
+      FHP_ATTR((k_band_last_r512<R, true>));
+    }
 #define FHP_ATTR_P2(P)                              \
     FHP_ATTR((k_band_last_p2<R, COEF_ISO, P>));     \
     FHP_ATTR((k_band_last_p2<R, COEF_SYM, P>));     \
@@ -1710,7 +1713,11 @@ class Engine final : public EngineBase {
         const long long need = (nrows + kR512Warps - 1) / kR512Warps;
         const unsigned ctas =
             (unsigned)std::min<long long>(need, (long long)reg512_ctas_per_sm_ * nsm_);
-        k_band_last_r512<R><<<ctas, 32 * kR512Warps, r512_smem_bytes(), s>>>(
+        // the full band (a 255-point solve line in a 512-point integration
+        // line) takes the instantiation without per-frequency tests
+        auto kern = (n2h == 128 && g_.n2 == 255) ? k_band_last_r512<R, true>
+                                                 : k_band_last_r512<R, false>;
+        kern<<<ctas, 32 * kR512Warps, r512_smem_bytes(), s>>>(
             reinterpret_cast<float2*>(Sbig), reinterpret_cast<const float*>(A_), g_, nrows,
             (int)n2h, g_.n2, reinterpret_cast<const float2*>(lb2_.dev.tw), (float)cs, ad);
         pend(pk, s);

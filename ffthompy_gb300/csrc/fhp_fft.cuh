@@ -225,7 +225,9 @@ __device__ __forceinline__ void dft8(cplx<R>* v) {
 
 // ENDS: only x[0..3] and x[12..15] are nonzero (the band of a pruned
 // 32-point line), so the first DFT4 of each b sees (x_b, 0, 0, x_{b+12}).
-template <typename R, bool ENDS = false>
+// OUT_ENDS: only X[0..3] and X[12..15] are wanted (outputs 0 and 3 of each
+// last DFT4); X[4..11] are left unspecified.
+template <typename R, bool ENDS = false, bool OUT_ENDS = false>
 __device__ __forceinline__ void dft16(cplx<R>* v) {
   // x[b + 4a]: u_b = DFT4_a, twiddle W16^(b k1), then DFT4 over b.
   const R c1 = R(0.92387953251128675612818318939679);  // cos(pi/8)
@@ -260,10 +262,17 @@ __device__ __forceinline__ void dft16(cplx<R>* v) {
   u[3][3] = cmul<R>(u[3][3], mkc<R>(-c1, s1));
 #pragma unroll
   for (int k1 = 0; k1 < 4; ++k1) {
-    cplx<R> t[4] = {u[0][k1], u[1][k1], u[2][k1], u[3][k1]};
-    dft4<R>(t);
+    if constexpr (OUT_ENDS) {
+      const cplx<R> a = cadd<R>(u[0][k1], u[2][k1]), b = csub<R>(u[0][k1], u[2][k1]);
+      const cplx<R> c = cadd<R>(u[1][k1], u[3][k1]), d = csub<R>(u[1][k1], u[3][k1]);
+      v[k1] = cadd<R>(a, c);
+      v[k1 + 12] = cadd<R>(b, cmul_pi<R>(d));
+    } else {
+      cplx<R> t[4] = {u[0][k1], u[1][k1], u[2][k1], u[3][k1]};
+      dft4<R>(t);
 #pragma unroll
-    for (int k2 = 0; k2 < 4; ++k2) v[k1 + 4 * k2] = t[k2];
+      for (int k2 = 0; k2 < 4; ++k2) v[k1 + 4 * k2] = t[k2];
+    }
   }
 }
 

@@ -2071,6 +2071,7 @@ __device__ __forceinline__ void r512_inverse(float2 (&v)[16], float2* tile, cons
 }
 
 // forward transform: space distribution in v, frequency distribution out
+// (registers 0..3 and 12..15 only: the band)
 __device__ __forceinline__ void r512_forward(float2 (&v)[16], float2* tile, const float2* twt,
                                              int lane) {
   dft16<float>(v);
@@ -2095,7 +2096,7 @@ __device__ __forceinline__ void r512_forward(float2 (&v)[16], float2* tile, cons
 #pragma unroll
     for (int r = 1; r < 16; ++r) v[r] = cmul<float>(v[r], w32f(r));
   }
-  dft16<float>(v);
+  dft16<float, false, true>(v);
 }
 
 // Per-warp shared memory of k_band_last_r512 (float2 units): the transpose
@@ -2109,12 +2110,14 @@ __host__ __device__ constexpr size_t r512_smem_bytes() {
 
 // S: band spectra [C][nrows][n2h] (in place); A: isotropic coefficient
 // [nrows][512]; tw: W512^k, k < 512.  Requires n2h <= 128 and 2 n2h - 1 <=
-// n2_solve + 1 (the band of the solve grid).  Each warp walks its pair lines
+// n2_solve + 1 (the band of the solve grid).  FULL: n2h = 128 and n2_solve =
+// 255 (every band slot holds a frequency below the solve line's Nyquist: no
+// per-frequency weights or tests).  Each warp walks its pair lines
 // (row by row, the np pair lines of a row in turn) and copies the next pair
 // line's spectra (and, at a new row, the next coefficient row) into shared
 // memory with cp.async while it transforms the current one.  A template
 // instantiated for float only, so the FP64 translation unit compiles none of it.
-template <typename R>
+template <typename R, bool FULL>
 __global__ void __launch_bounds__(32 * kR512Warps, 2) k_band_last_r512(
     float2* __restrict__ S, const float* __restrict__ A, const __grid_constant__ GridDims g,
     long long nrows, int n2h, int n2_solve, const float2* __restrict__ tw, float cs,
@@ -2187,7 +2190,12 @@ __global__ void __launch_bounds__(32 * kR512Warps, 2) k_band_last_r512(
     for (int r = 0; r < 4; ++r) {
       const int k = kl + 32 * r;
       float2 za = make_float2(0.f, 0.f), zb = make_float2(0.f, 0.f);
-      if (k < n2h) {
+      if constexpr (FULL) {
+        // k < 128 = n2h and 2k < 255 = n2_solve for every lane
+        za = sa[k];
+        zb = hb ? sb[k] : make_float2(0.f, 0.f);
+        if (r == 0 && kl == 0) { za.y = 0.f; zb.y = 0.f; }
+      } else if (k < n2h) {
         const float w = (2 * k < n2_solve) ? 1.f : 0.5f;
         za = sa[k];
         zb = hb ? sb[k] : make_float2(0.f, 0.f);
@@ -2197,7 +2205,13 @@ __global__ void __launch_bounds__(32 * kR512Warps, 2) k_band_last_r512(
       v[r] = make_float2(za.x - zb.y, za.y + zb.x);
       const int q = 512 - (kl + 32 * (15 - r));     // register 15 - r holds -q
       float2 ma = make_float2(0.f, 0.f), mb = make_float2(0.f, 0.f);
-      if (q < n2h) {
+      if constexpr (FULL) {
+        // q = 32 (r + 1) - kl: below 128 except q = 128 (r = 3, kl = 0)
+        if (r < 3 || kl != 0) {
+          ma = sa[q];
+          mb = hb ? sb[q] : make_float2(0.f, 0.f);
+        }
+      } else if (q < n2h) {
         const float w = (2 * q < n2_solve) ? 1.f : 0.5f;
         ma = sa[q];
         mb = hb ? sb[q] : make_float2(0.f, 0.f);
@@ -2222,11 +2236,11 @@ __global__ void __launch_bounds__(32 * kR512Warps, 2) k_band_last_r512(
       float2 zm = make_float2(mx, my);
       if (lane == 0) zm = v[(16 - r) & 15];   // k = 32 r: -k = 32 (16 - r)
       const int k = kl + 32 * r;
-      if (k < n2h) {
+      if (FULL || k < n2h) {
         const float2 zk = v[r];
         float2 xa = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
         float2 xb = make_float2(0.5f * (zk.y + zm.y), 0.5f * (zm.x - zk.x));
-        if (2 * k == n2_solve) { xa.y = 0.f; xb.y = 0.f; }
+        if (!FULL && 2 * k == n2_solve) { xa.y = 0.f; xb.y = 0.f; }
         da[k] = xa;
         if (hb) db[k] = xb;
       }
