@@ -590,7 +590,7 @@ int fhp_plan_set_band_cg(fhp_plan plan, int spectral) {
 
 int fhp_plan_set_integration_kernel(fhp_plan plan, int kind) {
   if (!plan) return bad("plan is NULL");
-  if (kind != 0 && kind != 1) return bad("kind must be 0 or 1");
+  if (kind < 0 || kind > 2) return bad("kind must be 0, 1 or 2");
   plan->eng->set_integration_kernel(kind);
   if (plan->lo) plan->lo->set_integration_kernel(kind);
   return FHP_OK;

@@ -15,6 +15,43 @@
 #include "fhp_kernels.cuh"
 
 namespace fhp {
+// cuTensorMapEncodeTiled, looked up once through the runtime (no link to the
+// driver library); null when the driver does not provide it
+using TmapEncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+inline TmapEncodeFn tmap_encoder() {
+  static TmapEncodeFn fn = []() -> TmapEncodeFn {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault,
+                                         &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      (void)cudaGetLastError();
+      return nullptr;
+    }
+    return reinterpret_cast<TmapEncodeFn>(f);
+  }();
+  return fn;
+}
+// a 2D map of rows of `inner` 8-byte elements (row pitch inner * 8 bytes), box
+// of one whole row; false if the driver rejects it
+inline bool tmap_rows(CUtensorMap* m, void* base, unsigned long long inner,
+                      unsigned long long rows) {
+  TmapEncodeFn enc = tmap_encoder();
+  if (!enc || inner > 256 || (inner * 8) % 16 != 0) return false;
+  const cuuint64_t dims[2] = {inner, rows};
+  const cuuint64_t strides[1] = {inner * 8};
+  const cuuint32_t box[2] = {(cuuint32_t)inner, 1};
+  const cuuint32_t estr[2] = {1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, base, dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+             CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+}  // namespace fhp
+
+namespace fhp {
 
 #define FHP_CHECK(call)                                                              \
   do {                                                                               \
@@ -161,6 +198,9 @@ class Engine final : public EngineBase {
     FHP_CHECK(cudaMalloc(&st_, K * kMaxLoads * sizeof(LoadState)));
     FHP_CHECK(cudaMalloc(&all_done_, sizeof(int)));
     FHP_CHECK(cudaMallocHost(&h_done_, sizeof(int)));
+    FHP_CHECK(cudaMalloc(&err_, sizeof(int)));
+    FHP_CHECK(cudaMemset(err_, 0, sizeof(int)));
+    FHP_CHECK(cudaMallocHost(&h_err_, sizeof(int)));
     FHP_CHECK(cudaMallocHost(&h_st_, K * kMaxLoads * sizeof(LoadState)));
     FHP_CHECK(cudaMalloc(&ad_, K * 2 * kMaxLoads * kMaxLoads * sizeof(double)));
     FHP_CHECK(cudaMalloc(&dscale_, K * 2 * kMaxLoads * sizeof(double)));
@@ -957,6 +997,16 @@ class Engine final : public EngineBase {
     return ST_OK;
   }
 
+  // a kernel's bounded wait ran out since the last check (*h_err_ read after a
+  // synchronisation): the error is reported once and the word cleared
+  int take_err(cudaStream_t s) {
+    if (!*h_err_) return ST_OK;
+    *h_err_ = 0;
+    cudaMemsetAsync(err_, 0, sizeof(int), s);
+    set_error("a tile load of the integration pass did not complete in its wait limit");
+    return ST_TIMEOUT;
+  }
+
   // per-load results of a solve (solver.py:137-138) from the device state
   int collect(double tol, int log_rows, const double* dlog, SolveResult& res, cudaStream_t s) {
     const int LK = g_.L * g_.K;   // every cell's loads, cell-major
@@ -964,7 +1014,9 @@ class Engine final : public EngineBase {
     res.res_log.assign((size_t)log_rows * LK, 0.0);
     FHP_CHECK(cudaMemcpyAsync(res.res_log.data(), dlog, (size_t)log_rows * LK * sizeof(double),
                               cudaMemcpyDeviceToHost, s));
+    FHP_CHECK(cudaMemcpyAsync(h_err_, err_, sizeof(int), cudaMemcpyDeviceToHost, s));
     FHP_CHECK(cudaStreamSynchronize(s));
+    if (int st = take_err(s)) return st;
     res.kit.resize(LK);
     res.norm_res.resize(LK);
     res.status.resize(LK);
@@ -1302,6 +1354,9 @@ class Engine final : public EngineBase {
   LoadState* h_st_ = nullptr;
   int* all_done_ = nullptr;
   int* h_done_ = nullptr;
+  // a bounded wait of a kernel ran out (device word, pinned host copy)
+  int* err_ = nullptr;
+  int* h_err_ = nullptr;
   int rows_ = 1, row_ctas_ = 1, T1_ = 1, Tp_ = 1, T0_ = 1;
   bool c2r_stage_ = false;   // k_c2r_last stages its input spectra in shared memory
   size_t smem_rows_ = 0;
@@ -1512,6 +1567,9 @@ class Engine final : public EngineBase {
     zx_ = nullptr;
     if (h_done_) cudaFreeHost(h_done_);
     if (h_st_) cudaFreeHost(h_st_);
+    if (err_) cudaFree(err_);
+    if (h_err_) cudaFreeHost(h_err_);
+    err_ = h_err_ = nullptr;
     S_ = nullptr; A_ = nullptr; r_ = p_ = ap_ = nullptr;
     ad_ = dscale_ = nullptr;
   }
@@ -1705,7 +1763,7 @@ class Engine final : public EngineBase {
     const int* ad = cg ? all_done_ : nullptr;
     const long long n2h = g_.n2h;
     if constexpr (sizeof(R) == 4) {
-      if (integ_kernel_ == 1 && reg512_applies(coef)) {
+      if (integ_kernel_ >= 1 && reg512_applies(coef)) {
         const long long nrows = (long long)gi_.n0 * gi_.n1;
         const double b4 = 2.0 * (double)(g_.L * g_.dv) * nrows * n2h * sizeof(cplx<R>) +
                           coef_bytes();
@@ -1714,12 +1772,20 @@ class Engine final : public EngineBase {
         const unsigned ctas =
             (unsigned)std::min<long long>(need, (long long)reg512_ctas_per_sm_ * nsm_);
         // the full band (a 255-point solve line in a 512-point integration
-        // line) takes the instantiation without per-frequency tests
-        auto kern = (n2h == 128 && g_.n2 == 255) ? k_band_last_r512<R, true>
-                                                 : k_band_last_r512<R, false>;
+        // line) takes the instantiation without per-frequency tests, and TMA
+        // row loads when both maps encode
+        const bool full = n2h == 128 && g_.n2 == 255;
+        auto kern = full ? k_band_last_r512<R, true> : k_band_last_r512<R, false>;
+        CUtensorMap tmS, tmA;
+        std::memset(&tmS, 0, sizeof(tmS));
+        std::memset(&tmA, 0, sizeof(tmA));
+        const int use_tma = (full && integ_kernel_ == 1 &&
+                             tmap_rows(&tmS, Sbig, 128, (unsigned long long)g_.L * g_.dv * nrows) &&
+                             tmap_rows(&tmA, A_, 256, (unsigned long long)nrows)) ? 1 : 0;
         kern<<<ctas, 32 * kR512Warps, r512_smem_bytes(), s>>>(
             reinterpret_cast<float2*>(Sbig), reinterpret_cast<const float*>(A_), g_, nrows,
-            (int)n2h, g_.n2, reinterpret_cast<const float2*>(lb2_.dev.tw), (float)cs, ad);
+            (int)n2h, g_.n2, reinterpret_cast<const float2*>(lb2_.dev.tw), (float)cs, ad, tmS,
+            tmA, use_tma, err_, cg ? all_done_ : nullptr);
         pend(pk, s);
         FHP_LAUNCHED();
         return ST_OK;
@@ -1888,7 +1954,9 @@ class Engine final : public EngineBase {
       FHP_LAUNCHED();
       FHP_CHECK(cudaMemcpyAsync(AH, ad_, (size_t)g_.L * g_.L * sizeof(double),
                                 cudaMemcpyDeviceToHost, s));
+      FHP_CHECK(cudaMemcpyAsync(h_err_, err_, sizeof(int), cudaMemcpyDeviceToHost, s));
       FHP_CHECK(cudaStreamSynchronize(s));
+      st = take_err(s);
     }
     return st;
   }
@@ -1940,7 +2008,8 @@ class Engine final : public EngineBase {
   int brows_ = 1, brow_ctas_ = 1;
   size_t bsmem_rows_ = 0;
   // integration pass kernel: 1 register-resident 512-point lines where they
-  // apply, 0 the shared-memory line cores
+  // apply (TMA row loads for the full band), 2 the same lines with per-lane
+  // cp.async loads, 0 the shared-memory line cores
   int integ_kernel_ = 1;
   int reg512_ctas_per_sm_ = 2;
   int axis_target_mult_ = 1;   // band axis passes: column-tile target x this

@@ -112,6 +112,59 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
+// ---------------------------------------------------------------------------
+// Tensor-memory-access (TMA) tile loads completing on an mbarrier: one thread
+// issues a 2D box copy global -> shared, the barrier counts the bytes, and the
+// consumers wait on the barrier's phase with a bounded number of tries.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(a), "r"(count) : "memory");
+}
+// the barrier initialisation is visible to the async proxy
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+// generic-proxy accesses of shared memory are ordered before later async copies
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(a), "r"(bytes)
+               : "memory");
+}
+// one try: 1 once the phase of the given parity has completed
+__device__ __forceinline__ unsigned mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.b32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(a), "r"(parity)
+      : "memory");
+  return ok;
+}
+// bounded wait: false when the phase has not completed after `tries` tries
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity,
+                                                  int tries) {
+  for (int i = 0; i < tries; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+// 2D box (x innermost, in elements) of the tensor map tm into shared memory
+__device__ __forceinline__ void tma_load_2d(void* smem, const void* tm, int x, int y,
+                                            unsigned long long* bar) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(smem);
+  const unsigned b = (unsigned)__cvta_generic_to_shared(bar);
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];\n" ::"r"(d),
+      "l"(reinterpret_cast<unsigned long long>(tm)), "r"(x), "r"(y), "r"(b)
+      : "memory");
+}
+
 // Block-cooperative copy of count elements of T (4, 8 or 16 bytes) from global
 // to shared memory: 16-byte copies when both ends are 16-byte aligned and the
 // length is a multiple of 16 bytes, element copies otherwise.

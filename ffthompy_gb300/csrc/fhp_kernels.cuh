@@ -9,6 +9,8 @@
 // (ffthompy/applications.py:58 with Operator's reversed factor order,
 // ffthompy/tensors/operators.py:119-144).
 #pragma once
+#include <cuda.h>   // CUtensorMap (a kernel parameter type; no driver call here)
+
 #include "fhp_fft.cuh"
 
 namespace fhp {
@@ -2104,15 +2106,26 @@ __device__ __forceinline__ void r512_forward(float2 (&v)[16], float2* tile, cons
 // each) and two for coefficient rows (512 floats each).
 constexpr int kR512Stage = 2 * 128;
 constexpr int kR512WarpSmem = kR512Tile + 2 * kR512Stage + 2 * 256;
+// + two mbarriers per warp (the TMA path's stage buffers 0 and 1)
 __host__ __device__ constexpr size_t r512_smem_bytes() {
-  return (size_t)(16 * 32 + kR512Warps * kR512WarpSmem) * sizeof(float2);
+  return (size_t)(16 * 32 + kR512Warps * kR512WarpSmem) * sizeof(float2) +
+         (size_t)kR512Warps * 2 * sizeof(unsigned long long);
 }
+// tries of a bounded wait for a stage buffer (each try waits up to a
+// hardware-chosen time): far beyond any copy, short of a hung launch
+constexpr int kR512WaitTries = 1 << 22;
 
 // S: band spectra [C][nrows][n2h] (in place); A: isotropic coefficient
 // [nrows][512]; tw: W512^k, k < 512.  Requires n2h <= 128 and 2 n2h - 1 <=
 // n2_solve + 1 (the band of the solve grid).  FULL: n2h = 128 and n2_solve =
 // 255 (every band slot holds a frequency below the solve line's Nyquist: no
-// per-frequency weights or tests).  Each warp walks its pair lines
+// per-frequency weights or tests).
+// use_tma (FULL only): lane 0 of a warp loads the next pair line's spectra
+// rows (tmS: S as [C * nrows][128] 8-byte elements) and coefficient row (tmA:
+// A as [nrows][256] 8-byte elements) with TMA boxes that complete on the
+// stage buffer's mbarrier, in place of per-lane cp.async.  A wait that runs
+// out sets *err (and *stop, the CG's all-done flag, when given); the warp then
+// waits (bounded) for its other copy and returns.  Each warp walks its pair lines
 // (row by row, the np pair lines of a row in turn) and copies the next pair
 // line's spectra (and, at a new row, the next coefficient row) into shared
 // memory with cp.async while it transforms the current one.  A template
@@ -2121,18 +2134,31 @@ template <typename R, bool FULL>
 __global__ void __launch_bounds__(32 * kR512Warps, 2) k_band_last_r512(
     float2* __restrict__ S, const float* __restrict__ A, const __grid_constant__ GridDims g,
     long long nrows, int n2h, int n2_solve, const float2* __restrict__ tw, float cs,
-    const int* __restrict__ all_done) {
+    const int* __restrict__ all_done, const __grid_constant__ CUtensorMap tmS,
+    const __grid_constant__ CUtensorMap tmA, int use_tma, int* __restrict__ err,
+    int* __restrict__ stop) {
   static_assert(sizeof(R) == 4, "FP32 lines");
   if (all_done && *all_done) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   float2* twt = reinterpret_cast<float2*>(smem_raw);   // W512^(l k1) at [k1][l]
-  for (int e = threadIdx.x; e < 16 * 32; e += blockDim.x) twt[e] = tw[(e & 31) * (e >> 5)];
-  __syncthreads();
+  unsigned long long* bars = reinterpret_cast<unsigned long long*>(
+      smem_raw + (size_t)(16 * 32 + kR512Warps * kR512WarpSmem) * sizeof(float2));
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   float2* wsm = twt + 16 * 32 + warp * kR512WarpSmem;
   float2* tile = wsm;
   float2* stg = wsm + kR512Tile;                                            // [2][2][128]
   float* cst = reinterpret_cast<float*>(wsm + kR512Tile + 2 * kR512Stage);  // [2][512]
+  unsigned long long* wbar = bars + 2 * warp;
+  // TMA boxes land on 128-byte aligned stage buffers (checked, not assumed)
+  const bool tma = FULL && use_tma &&
+                   ((((unsigned)__cvta_generic_to_shared(stg)) | ((unsigned)__cvta_generic_to_shared(cst))) & 127u) == 0;
+  if (tma && lane == 0) {
+    mbar_init(wbar, 1);
+    mbar_init(wbar + 1, 1);
+    mbar_init_fence();
+  }
+  for (int e = threadIdx.x; e < 16 * 32; e += blockDim.x) twt[e] = tw[(e & 31) * (e >> 5)];
+  __syncthreads();
   const int C = g.L * g.dv;
   const int np = (C + 1) / 2;
   const int k1 = lane >> 1, h = lane & 1;
@@ -2144,6 +2170,23 @@ __global__ void __launch_bounds__(32 * kR512Warps, 2) k_band_last_r512(
   const long long ntask = nrow_w * np;
   // copy task t (row gw + (t / np) nw, pair line t % np) into buffer t & 1
   auto prefetch = [&](long long t) {
+    if (tma) {
+      if (t < ntask && lane == 0) {
+        const long long row = gw + (t / np) * nw;
+        const int p = (int)(t % np);
+        const int b = (int)(t & 1);
+        const int halves = (2 * p + 1 < C) ? 2 : 1;
+        // the generic reads of these buffers (task t - 2) come first
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(wbar + b, (unsigned)(halves * 1024 + (p == 0 ? 2048 : 0)));
+        for (int half = 0; half < halves; ++half)
+          tma_load_2d(stg + (b * 2 + half) * 128, &tmS, 0, (int)((2 * p + half) * nrows + row),
+                      wbar + b);
+        if (p == 0)
+          tma_load_2d(cst + ((t / np) & 1) * 512, &tmA, 0, (int)row, wbar + b);
+      }
+      return;
+    }
     if (t < ntask) {
       const long long row = gw + (t / np) * nw;
       const int p = (int)(t % np);
@@ -2171,7 +2214,21 @@ __global__ void __launch_bounds__(32 * kR512Warps, 2) k_band_last_r512(
     const int b = (int)(t & 1);
     __syncwarp();       // every lane is done with the buffers of task t - 1
     prefetch(t + 1);
-    cp_async_wait<1>();
+    if (tma) {
+      if (!mbar_wait_bounded(wbar + b, (unsigned)((t >> 1) & 1), kR512WaitTries)) {
+        if (lane == 0) {
+          atomicExch(err, 1);
+          if (stop) atomicExch(stop, 1);
+        }
+        // the other buffer's copies (task t + 1) before the warp leaves
+        if (t + 1 < ntask)
+          (void)mbar_wait_bounded(wbar + ((b + 1) & 1), (unsigned)(((t + 1) >> 1) & 1),
+                                  kR512WaitTries);
+        return;
+      }
+    } else {
+      cp_async_wait<1>();
+    }
     __syncwarp();       // task t's copies of every lane are visible
     if (p == 0) {
       const float* ar = cst + ((t / np) & 1) * 512;
@@ -2246,7 +2303,7 @@ __global__ void __launch_bounds__(32 * kR512Warps, 2) k_band_last_r512(
       }
     }
   }
-  cp_async_wait<0>();
+  if (!tma) cp_async_wait<0>();
 }
 
 // W_i . u_j cross products per load pair on the solve grid (band energy):

@@ -89,8 +89,9 @@ class GalerkinPlan:
     band_cg (band plans): 'spectral' keeps the CG iterates as half spectra of
     N (no transform of the N grid inside an iteration), 'real' as real fields.
     integ_kernel (band plans): 'register' runs the integration pass with
-    lines held in registers where that kernel applies, 'shared' with the
-    shared-memory line cores.
+    lines held in registers where that kernel applies (TMA row loads for the
+    full band), 'register_cpasync' the same lines with per-lane cp.async
+    loads, 'shared' with the shared-memory line cores.
     ncells (GaNi / full-grid Ga): cells of the same grid solved together
     (fhp_plan_create_cells): fields (cells, loads, dv) + N, packed
     coefficients (cells, c) + N, per-load results cell-major, A_H
@@ -154,11 +155,12 @@ class GalerkinPlan:
         self.band_cg = band_cg
         _lib.check(self.lib.fhp_plan_set_band_cg(h, 1 if band_cg == 'spectral' else 0),
                    'fhp_plan_set_band_cg')
-        if integ_kernel not in ('register', 'shared'):
-            raise ValueError("integ_kernel must be 'register' or 'shared'")
+        kinds = {'register': 1, 'register_cpasync': 2, 'shared': 0}
+        if integ_kernel not in kinds:
+            raise ValueError("integ_kernel must be 'register', 'register_cpasync' or 'shared'")
         self.integ_kernel = integ_kernel
-        _lib.check(self.lib.fhp_plan_set_integration_kernel(
-            h, 1 if integ_kernel == 'register' else 0), 'fhp_plan_set_integration_kernel')
+        _lib.check(self.lib.fhp_plan_set_integration_kernel(h, kinds[integ_kernel]),
+                   'fhp_plan_set_integration_kernel')
 
     def __del__(self):
         h = getattr(self, 'handle', None)

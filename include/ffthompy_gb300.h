@@ -108,7 +108,10 @@ int fhp_plan_set_band_cg(fhp_plan plan, int spectral);
  * axis, coefficient, forward transform).  kind = 1 (default): lines held in
  * registers, one warp per line, where that kernel applies (FP32 fields, an
  * isotropic coefficient, a 512-point integration line with the band within a
- * quarter of it); kind = 0: the shared-memory line cores, for every plan.
+ * quarter of it), with TMA row loads on an mbarrier when the band fills the
+ * quarter (a 255-point solve line); kind = 2: the same register lines with
+ * per-lane cp.async loads; kind = 0: the shared-memory line cores, for every
+ * plan.
  * Both compute the same transforms.  No counterpart in the reference (its
  * transforms are numpy.fft.rfftn / irfftn, ffthompy/tensors/fft.py:39-43).
  */

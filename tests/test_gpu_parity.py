@@ -634,7 +634,7 @@ def test_band_spectral_cg_equals_real_cg(N, physics, precision):
 
 
 @pytest.mark.parametrize('N', [(3, 5, 255), (4, 3, 254), (2, 6, 253), (7, 255), (6, 254)])
-@pytest.mark.parametrize('integ_kernel', ['register', 'shared'])
+@pytest.mark.parametrize('integ_kernel', ['register', 'register_cpasync', 'shared'])
 def test_band_operator_512_register_lines(N, integ_kernel):
     """The integration pass with register-resident 512-point lines (FP32,
     isotropic coefficient, band within a quarter of the line: n2 in 253..255)
@@ -659,7 +659,7 @@ def test_band_cg_512_register_equals_shared_lines(N):
     integ = tuple(nice_size(n) for n in Ns)
     A = _project_comps(A, integ)
     out = {}
-    for kern in ('register', 'shared'):
+    for kern in ('register', 'register_cpasync', 'shared'):
         plan = GalerkinPlan(tuple(N), np.ones(d), integ=integ, precision='f32',
                             integ_kernel=kern)
         plan.set_coefficient(A)
@@ -667,6 +667,9 @@ def test_band_cg_512_register_equals_shared_lines(N):
         out[kern] = (info, plan.energy(X))
         print(kern, info['kit'], info['status'])
     (ir, AHr), (is_, AHs) = out['register'], out['shared']
+    # TMA and per-lane loads bring the same values: the same arithmetic
+    ic, AHc = out['register_cpasync']
+    assert ic['kit'] == ir['kit'] and np.array_equal(AHc, AHr), (ic['kit'], ir['kit'])
     assert all(s == 0 for s in ir['status'])
     assert all(abs(p - q) <= max(1, int(np.ceil(0.03 * q))) for p, q in zip(ir['kit'], is_['kit']))
     assert _relmax(AHr, AHs) < 1e-5
