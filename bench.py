@@ -343,6 +343,62 @@ def run_reference(args):
 # ----------------------------------------------------------------------------
 # the GPU arm
 # ----------------------------------------------------------------------------
+def _ensemble_cells(count=512, sizes=(63, 127, 255, 511), seed=12):
+    """The cfg4 ensemble's cells: (n, contrast, field seed) per instance."""
+    rng = np.random.default_rng(seed)
+    cells = []
+    for _ in range(count):
+        n = int(rng.choice(sizes))
+        contrast = float(np.exp(rng.uniform(np.log(2.), np.log(1000.))))
+        cells.append((n, contrast, int(rng.integers(1 << 30))))
+    return cells
+
+
+def _ens_cpu_worker(args):
+    """One host process: `iters` oracle CG iterations per load (GaNi, 2 loads,
+    solver-only) of each of its cells.  Returns (voxel-iterations, seconds of
+    CG)."""
+    cells, iters = args
+    sys.path.insert(0, ROOT)
+    import oracle
+    from ffthompy_gb300 import workloads
+    vox, t = 0, 0.
+    for n, contrast, gseed in cells:
+        A = workloads.grf_phase_coefficient((n, n), ell=0.1, quantile=0.4, contrast=contrast,
+                                            seed=gseed)
+        G, _ = oracle.green_operator('scalar', np.array([n, n]), np.ones(2), 'GaNi', 1)
+        Afun = lambda v, _G=G, _A=A: oracle.apply_GA(_G, _A, v)
+        for l in range(2):
+            E = np.zeros((2, n, n))
+            E[l] = 1.
+            B = Afun(-E)
+            t0 = time.perf_counter()
+            _, info = oracle.cg(Afun, B, np.zeros_like(B), tol=0., maxiter=iters)
+            t += time.perf_counter() - t0
+            vox += n * n * info['kit']
+    return vox, t
+
+
+def ensemble_cpu_baseline(iters=5):
+    """The cfg4 ensemble on all host cores: the oracle (NumPy restatement of
+    the reference's GaNi CG) on every one of the 512 cells for `iters`
+    iterations per load, the cells dealt round-robin by size to one spawned
+    process per core; aggregate Mvoxel-iter/s over the slowest process."""
+    import multiprocessing as mp
+    cells = sorted(_ensemble_cells(), key=lambda c: -c[0])
+    ncores = len(os.sched_getaffinity(0))
+    parts = [cells[i::ncores] for i in range(ncores)]
+    with mp.get_context('spawn').Pool(ncores) as pool:
+        res = pool.map(_ens_cpu_worker, [(p, iters) for p in parts], chunksize=1)
+    vox = sum(r[0] for r in res)
+    wall = max(r[1] for r in res)
+    return {'value': round(vox / wall / 1e6, 3), 'unit': 'Mvoxel-iter/s', 'cores': ncores,
+            'kind': 'port', 'cpu_model': host_cpu_model(),
+            'sample': 'all 512 cells of the ensemble, %d CG iterations per load (2 loads, '
+                      'GaNi, solver-only), NumPy restatement of the reference, one spawned '
+                      'process per host core' % iters}
+
+
 def ensemble_measure(count=512, sizes=(63, 127, 255, 511), seed=12, tol=1e-6, workers=16,
                      precision='f64', dist=None):
     """Many independent 2D GaNi cells (thresholded Gaussian random fields,
@@ -356,14 +412,9 @@ def ensemble_measure(count=512, sizes=(63, 127, 255, 511), seed=12, tol=1e-6, wo
     import torch
     from ffthompy_gb300 import workloads
     from ffthompy_gb300.batch import homogenize_many, homogenize_many_ranks
-    rng = np.random.default_rng(seed)
-    coefs = []
-    for _ in range(count):
-        n = int(rng.choice(sizes))
-        contrast = float(np.exp(rng.uniform(np.log(2.), np.log(1000.))))
-        coefs.append(workloads.grf_phase_coefficient((n, n), ell=0.1, quantile=0.4,
-                                                     contrast=contrast,
-                                                     seed=int(rng.integers(1 << 30))))
+    coefs = [workloads.grf_phase_coefficient((n, n), ell=0.1, quantile=0.4, contrast=contrast,
+                                             seed=gseed)
+             for n, contrast, gseed in _ensemble_cells(count, sizes, seed)]
     # warm: the plan pool (one plan per cell), the autotuned launch shapes
     homogenize_many(coefs, tol=tol, workers=workers, precision=precision, mode='cells')
     torch.cuda.synchronize()
@@ -852,6 +903,8 @@ def run_gpu(args):
     out.update(extras)
     if not args.no_cpu_baseline:
         out['cpu_baseline'] = cpu_baseline()
+        if not args.no_ensemble:
+            out['ensemble_cpu_baseline'] = ensemble_cpu_baseline()
     print(json.dumps(out), flush=True)
 
 
