@@ -1052,7 +1052,7 @@ class Engine final : public EngineBase {
     gz_.M = 2LL * g_.n0 * g_.n1 * g_.n2h;
     // partial sums of the spectral projection pass: one per CTA (the buffer
     // grows once per plan; cudaFree waits for work that still uses it)
-    projf_parts_ = band_axis_ctas(BAND_DOWN_PROJ_F, spectral_proj_axis(), lb1_.dev, l1_.dev);
+    projf_parts_ = band_axis_ctas(BAND_DOWN_F, spectral_proj_axis(), lb1_.dev, l1_.dev);
     if (projf_parts_ > nparts_max_) {
       double* np = nullptr;
       FHP_CHECK(cudaMalloc(&np, (size_t)projf_parts_ * kMaxLoads * kMaxLoads * sizeof(double)));
@@ -1101,8 +1101,9 @@ class Engine final : public EngineBase {
     return ST_OK;
   }
 
-  // zap = G A p in z form, p = r + beta p first (all in the spectral buffers),
-  // partial <p, Ap> per CTA of the last pass
+  // zap = A p in z form on the band (without G: the update projects it),
+  // p = r + beta p first (all in the spectral buffers), partial <p, Ap> per
+  // CTA of the last pass
   int spectral_operator(const cplx<R>* zr, cplx<R>* zp, cplx<R>* zap, cudaStream_t s) {
     int st;
     const long long n2h = g_.n2h;
@@ -1131,8 +1132,8 @@ class Engine final : public EngineBase {
       if ((st = band_axis(BAND_DOWN, SA, SB, a0, lb0_.dev, l0_.dev, true, s,
                           "band_down_axis0")) != ST_OK) return st;
     }
-    return band_axis(BAND_DOWN_PROJ_F, SB, zap, spectral_proj_axis(), lb1_.dev, l1_.dev, true, s,
-                     "band_projf_axis1", zp, partials_);
+    return band_axis(BAND_DOWN_F, SB, zap, spectral_proj_axis(), lb1_.dev, l1_.dev, true, s,
+                     "band_downf_axis1", zp, partials_);
   }
 
   int spectral_iteration(cplx<R>* zx, cplx<R>* zr, cplx<R>* zp, cplx<R>* zap, double* dlog,
@@ -1142,14 +1143,22 @@ class Engine final : public EngineBase {
     k_fin_pap<<<g_.L, kThreads, 0, s>>>(partials_, (int)projf_parts_, st_, g_.L, 1.0, all_done_);
     FHP_LAUNCHED();
     const int C = g_.L * g_.dv;
-    const int ux = std::max(1, red_ctas_ / C);
+    // x += alpha p, r -= alpha G(Ap): the operator's projection happens here
+    const int ux = std::max(1, red_ctas_ / g_.L);
     const int pk = pbeg("cg_update_spectral", 6.0 * (double)C * gz_.M * sizeof(R), s);
-    k_cg_update_comp<R><<<dim3((unsigned)ux, (unsigned)C), kThreads, 0, s>>>(
-        reinterpret_cast<R*>(zx), reinterpret_cast<R*>(zr), reinterpret_cast<const R*>(zp),
-        reinterpret_cast<const R*>(zap), partials_, gz_, st_, all_done_);
+    GreenParams gpo = gp_;
+    gpo.scale = 1.0;
+    const FastDiv dn1 = make_fastdiv((unsigned)g_.n1);
+    const dim3 ug((unsigned)ux, (unsigned)g_.L);
+    if (gp_.physics == 0)
+      k_cg_update_spec<R, 0><<<ug, kThreads, 0, s>>>(zx, zr, zp, zap, partials_, g_, gpo, dn1,
+                                                     st_, all_done_);
+    else
+      k_cg_update_spec<R, 1><<<ug, kThreads, 0, s>>>(zx, zr, zp, zap, partials_, g_, gpo, dn1,
+                                                     st_, all_done_);
     pend(pk, s);
     FHP_LAUNCHED();
-    k_fin_rr<<<g_.L, kThreads, 0, s>>>(partials_, ux * C, st_, g_.L, 1.0, dlog, log_rows,
+    k_fin_rr<<<g_.L, kThreads, 0, s>>>(partials_, ux * g_.L, st_, g_.L, 1.0, dlog, log_rows,
                                        all_done_);
     FHP_LAUNCHED();
     k_update_all_done<<<1, 1, 0, s>>>(st_, g_.L, all_done_);
@@ -1500,6 +1509,7 @@ class Engine final : public EngineBase {
     FHP_ATTR((k_band_axis<R, BAND_PAD_PUPD, 0>));
     FHP_ATTR((k_band_axis<R, BAND_DOWN_PROJ_F, 0>));
     FHP_ATTR((k_band_axis<R, BAND_DOWN_PROJ_F, 1>));
+    FHP_ATTR((k_band_axis<R, BAND_DOWN_F, 0>));
     FHP_ATTR((k_band_last<R, COEF_ISO>));
     FHP_ATTR((k_band_last<R, COEF_SYM>));
     FHP_ATTR((k_band_last<R, COEF_FULL>));
@@ -1674,7 +1684,9 @@ class Engine final : public EngineBase {
     const bool projm = mode == BAND_DOWN_PROJ || mode == BAND_UP_PROJ || mode == BAND_DOWN_PROJ_F;
     const bool padin = mode == BAND_PAD || mode == BAND_PAD_PUPD;
     const int nlc = projm ? g_.dv : 1;
-    const int nf = (padin ? 0 : L1.ld) + ((mode == BAND_DOWN || mode == BAND_DOWN_PROJ_F) ? 0 : L2.ld);
+    const int nf = (padin ? 0 : L1.ld) +
+                   ((mode == BAND_DOWN || mode == BAND_DOWN_PROJ_F || mode == BAND_DOWN_F) ? 0
+                                                                                    : L2.ld);
     // twice the usual line target: the axis passes are bound by instruction
     // issue, and more columns per CTA fill the radix stages of every line
     // length (and lengthen the contiguous rows); the register file still
@@ -1693,7 +1705,9 @@ class Engine final : public EngineBase {
     const bool projm = mode == BAND_DOWN_PROJ || mode == BAND_UP_PROJ || mode == BAND_DOWN_PROJ_F;
     const bool padin = mode == BAND_PAD || mode == BAND_PAD_PUPD;
     const int nlc = projm ? g_.dv : 1;
-    const int nf = (padin ? 0 : L1.ld) + ((mode == BAND_DOWN || mode == BAND_DOWN_PROJ_F) ? 0 : L2.ld);
+    const int nf = (padin ? 0 : L1.ld) +
+                   ((mode == BAND_DOWN || mode == BAND_DOWN_PROJ_F || mode == BAND_DOWN_F) ? 0
+                                                                                    : L2.ld);
     const int T = band_axis_tile(mode, ax, L1, L2);
     const size_t smem = (size_t)nlc * T * nf * sizeof(cplx<R>);
     if (smem > kSmemMax) { set_error("band line too long for shared memory"); return ST_BAD_ARG; }
@@ -1708,7 +1722,7 @@ class Engine final : public EngineBase {
                    (ax.n_in + ax.n_out) * sizeof(cplx<R>);
     if (mode == BAND_PAD_PUPD)
       bytes += 2.0 * (g_.L * g_.dv) * ax.mid * ax.inner * ax.n_in * sizeof(cplx<R>);
-    if (mode == BAND_DOWN_PROJ_F && parts)
+    if ((mode == BAND_DOWN_PROJ_F || mode == BAND_DOWN_F) && parts)
       bytes += (double)(g_.L * g_.dv) * ax.mid * ax.inner * ax.n_out * sizeof(cplx<R>);
     // the input projection of G A G is the plain orthogonal projection (scale 1);
     // the output projection carries s / prod(B)
@@ -1739,6 +1753,9 @@ class Engine final : public EngineBase {
         k<<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st, aux, parts);
         break;
       }
+      case BAND_DOWN_F:
+        k_band_axis<R, BAND_DOWN_F, 0><<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st, aux, parts);
+        break;
       default: {
         auto k = scalar ? k_band_axis<R, BAND_DOWN_PROJ, 0> : k_band_axis<R, BAND_DOWN_PROJ, 1>;
         k<<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st, nullptr, nullptr);

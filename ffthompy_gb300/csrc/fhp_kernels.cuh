@@ -1125,8 +1125,10 @@ __global__ void k_ga_gather(const cplx<R>* __restrict__ Sp, cplx<R>* __restrict_
 //                    spectral iterates, updated first (p = r + beta p)
 //   BAND_DOWN_PROJ_F : space B -> DFT_B -> band -> G(xi) -> frequency (N
 //                    layout) of the spectral iterates, with the partial <p, Ap>
+//   BAND_DOWN_F    : as BAND_DOWN_PROJ_F without G (one comp per CTA): the
+//                    spectral CG projects A p in its update instead
 enum BandMode { BAND_UP = 0, BAND_DOWN = 1, BAND_DOWN_PROJ = 2, BAND_UP_PROJ = 3, BAND_PAD = 4,
-                BAND_PAD_PUPD = 5, BAND_DOWN_PROJ_F = 6 };
+                BAND_PAD_PUPD = 5, BAND_DOWN_PROJ_F = 6, BAND_DOWN_F = 7 };
 
 struct BandAxis {
   int n_in, n_out;     // line lengths in / out
@@ -1247,12 +1249,13 @@ __global__ void __launch_bounds__(256, band_axis_min_blocks<R, MODE>()) k_band_a
   const int c0 = PROJ ? cl * g.dv : cl;
   const int load = c0 / g.dv;
   if (st && st[load].done) {
-    if (MODE == BAND_DOWN_PROJ_F && partials && threadIdx.x < g.L)
+    if ((MODE == BAND_DOWN_PROJ_F || MODE == BAND_DOWN_F) && partials && threadIdx.x < g.L)
       partials[((long long)blockIdx.y * gridDim.x + blockIdx.x) * g.L + threadIdx.x] = 0.;
     return;
   }
   const int ld1 = PADIN ? 0 : L1.ld;
-  const int ld2 = (MODE == BAND_DOWN || MODE == BAND_DOWN_PROJ_F) ? 0 : L2.ld;
+  const int ld2 = (MODE == BAND_DOWN || MODE == BAND_DOWN_PROJ_F || MODE == BAND_DOWN_F) ? 0
+                                                                                     : L2.ld;
   cplx<R>* buf1 = reinterpret_cast<cplx<R>*>(smem_raw);
   cplx<R>* buf2 = buf1 + (size_t)nlc * T * ld1;
   const long long t0 = (long long)blockIdx.x * T;
@@ -1263,7 +1266,8 @@ __global__ void __launch_bounds__(256, band_axis_min_blocks<R, MODE>()) k_band_a
   // are read at |q| <= n_out/2 only; zeros on the pruned digits are not written
   const bool pr2 = (MODE == BAND_UP || MODE == BAND_UP_PROJ || PADIN) &&
                    line_prunable<R>(L2, ax.n_in / 2);
-  const bool pr1 = (MODE == BAND_DOWN || MODE == BAND_DOWN_PROJ || MODE == BAND_DOWN_PROJ_F) &&
+  const bool pr1 = (MODE == BAND_DOWN || MODE == BAND_DOWN_PROJ || MODE == BAND_DOWN_PROJ_F ||
+                    MODE == BAND_DOWN_F) &&
                    line_prunable<R>(L1, ax.n_out / 2);
   const int pq0 = L2.nf / 4, pq1 = 3 * (L2.nf / 4);  // pruned range of the B line (pr2)
   if constexpr (MODE == BAND_PAD) {
@@ -1444,7 +1448,8 @@ __global__ void __launch_bounds__(256, band_axis_min_blocks<R, MODE>()) k_band_a
       cplx<R>* dst = Sout + (((long long)(c0 + c) * ax.mid + m) * ax.n_out) * ax.inner + col;
       dst[(long long)k * ax.inner] = v;
     });
-  } else if constexpr (MODE == BAND_DOWN_PROJ_F) {
+  } else if constexpr (MODE == BAND_DOWN_PROJ_F || MODE == BAND_DOWN_F) {
+    if constexpr (MODE == BAND_DOWN_PROJ_F) {
     // G(xi) on the band, written back in place into the B-line slot of each
     // N frequency (lanes over the frequencies of one column)
     for (int t = 0; t < T; ++t)
@@ -1466,16 +1471,19 @@ __global__ void __launch_bounds__(256, band_axis_min_blocks<R, MODE>()) k_band_a
         if (c < g.dv) set_fwd<R>(buf1 + (c * T + t) * ld1, L1, kb, x[c]);
     }
     __syncthreads();
+    }
     // rows of T columns to global (z form: times sqrt(w)), with <p, Ap>: a
     // thread keeps one column and takes its frequencies four at a time, the
-    // four loads of p issued before their products
+    // four loads of p issued before their products.  Without G in the pass
+    // (BAND_DOWN_F) the operator's scale (s / prod(B)) is applied here.
+    const R osc = MODE == BAND_DOWN_F ? R(gp.scale) : R(1);
     R dot = R(0);
     if (T <= (int)blockDim.x) {
       const int t = threadIdx.x & (T - 1);
       const int kst = (int)blockDim.x >> lgT;
       const long long col = t0 + t;
       if (col < ax.inner) {
-        const R fo = half_weight_root<R>(ax, g, col, false);
+        const R fo = half_weight_root<R>(ax, g, col, false) * osc;
         for (int c = 0; c < nlc; ++c) {
           const long long base = (((long long)(c0 + c) * ax.mid + m) * ax.n_out) * ax.inner + col;
           const cplx<R>* line = buf1 + (c * T + t) * ld1;
@@ -1505,7 +1513,7 @@ __global__ void __launch_bounds__(256, band_axis_min_blocks<R, MODE>()) k_band_a
         if (col >= ax.inner) return;
         const int q = signed_freq(k, ax.n_out);
         cplx<R> v = get_fwd<R>(buf1 + (c * T + t) * ld1, L1, q < 0 ? q + ax.n_in : q);
-        v = cscale<R>(v, half_weight_root<R>(ax, g, col, false));
+        v = cscale<R>(v, half_weight_root<R>(ax, g, col, false) * osc);
         const long long idx = (((long long)(c0 + c) * ax.mid + m) * ax.n_out + k) * ax.inner + col;
         Sout[idx] = v;
         if (partials) {
@@ -2780,6 +2788,72 @@ __global__ void k_half_weight(const cplx<R>* __restrict__ in, cplx<R>* __restric
 }
 
 // z <- G(xi) z at every frequency of half spectra in the N layout, all loads
+// x += alpha p ; r -= alpha G(Ap) on the spectral iterates (z form, half
+// spectra of the solve grid [load][comp][n0][n1][n2h]), partial <r, r> per
+// CTA and load (grid y = load).  Ap arrives from the last axis pass without
+// G: p lies in range(G) and G is self-adjoint, so <p, Ap> = <p, G Ap> was
+// taken there, and G maps Ap onto range(G) here, where r stays
+// (ffthompy/general/solver.py:127-129 with the operator's final projection
+// moved into the update; gp.scale 1: the orthogonal projection).
+template <typename R, int PHYS>
+__global__ void __launch_bounds__(256) k_cg_update_spec(cplx<R>* __restrict__ x,
+                                                        cplx<R>* __restrict__ r,
+                                                        const cplx<R>* __restrict__ p,
+                                                        const cplx<R>* __restrict__ ap,
+                                                        double* __restrict__ partials,
+                                                        const __grid_constant__ GridDims g,
+                                                        const __grid_constant__ GreenParams gp,
+                                                        FastDiv dn1,
+                                                        const LoadState* __restrict__ st,
+                                                        const int* __restrict__ all_done) {
+  if (all_done && *all_done) return;
+  __shared__ double red[8];
+  const int l = blockIdx.y;
+  const int F = g.n0 * g.n1 * g.n2h;
+  double acc = 0.;
+  if (!st[l].done) {
+    const R a = (R)st[l].alpha;
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < F; f += gridDim.x * blockDim.x) {
+      const int q = fdiv(f, g.dn2h);
+      const int k2 = f - q * g.n2h;
+      const int i0 = fdiv(q, dn1), i1 = q - i0 * g.n1;
+      int kv[3];
+      if (g.dim == 3) {
+        kv[0] = signed_freq(i0, g.n0);
+        kv[1] = signed_freq(i1, g.n1);
+        kv[2] = k2;
+      } else {
+        kv[0] = signed_freq(i1, g.n1);
+        kv[1] = k2;
+      }
+      cplx<R> v[kMaxDv];
+#pragma unroll
+      for (int c = 0; c < kMaxDv; ++c)
+        if (c < g.dv) v[c] = ap[(long long)(l * g.dv + c) * F + f];
+      green_apply<R, PHYS>(gp, g.dim, kv, v);
+#pragma unroll
+      for (int c = 0; c < kMaxDv; ++c) {
+        if (c >= g.dv) break;
+        const long long i = (long long)(l * g.dv + c) * F + f;
+        const cplx<R> pc = p[i], xc = x[i], rc = r[i];
+        x[i] = mkc<R>(xc.x + a * pc.x, xc.y + a * pc.y);
+        const cplx<R> rn = mkc<R>(rc.x - a * v[c].x, rc.y - a * v[c].y);
+        r[i] = rn;
+        acc += (double)(rn.x * rn.x + rn.y * rn.y);
+      }
+    }
+  }
+  const double t = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot = 0.;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
+    double* out = partials + ((long long)blockIdx.y * gridDim.x + blockIdx.x) * g.L;
+    for (int k = 0; k < g.L; ++k) out[k] = k == l ? tot : 0.;
+  }
+}
+
 // (the orthogonal projection: gp.scale 1; zero outside the band)
 template <typename R, int PHYS>
 __global__ void k_spec_green(cplx<R>* __restrict__ z, GridDims g, GreenParams gp) {
