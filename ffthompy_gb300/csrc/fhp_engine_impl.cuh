@@ -1507,8 +1507,6 @@ class Engine final : public EngineBase {
     FHP_ATTR((k_band_axis<R, BAND_UP_PROJ, 1>));
     FHP_ATTR((k_band_axis<R, BAND_PAD, 0>));
     FHP_ATTR((k_band_axis<R, BAND_PAD_PUPD, 0>));
-    FHP_ATTR((k_band_axis<R, BAND_DOWN_PROJ_F, 0>));
-    FHP_ATTR((k_band_axis<R, BAND_DOWN_PROJ_F, 1>));
     FHP_ATTR((k_band_axis<R, BAND_DOWN_F, 0>));
     FHP_ATTR((k_band_last<R, COEF_ISO>));
     FHP_ATTR((k_band_last<R, COEF_SYM>));
@@ -1671,30 +1669,26 @@ class Engine final : public EngineBase {
   }
 
   // ---- band representation (Ga on the solve grid, A on the integration grid) ----
-  // CTAs of a band pass (the partial-sum count of BAND_DOWN_PROJ_F)
+  // CTAs of a band pass (the partial-sum count of BAND_DOWN_F)
   long long band_axis_ctas(int mode, const BandAxis& ax, const LineDev<R>& L1,
                            const LineDev<R>& L2) const {
     const int T = band_axis_tile(mode, ax, L1, L2);
-    const bool projm = mode == BAND_DOWN_PROJ || mode == BAND_UP_PROJ || mode == BAND_DOWN_PROJ_F;
+    const bool projm = mode == BAND_DOWN_PROJ || mode == BAND_UP_PROJ;
     return ((ax.inner + T - 1) / T) * (long long)((projm ? g_.L : g_.L * g_.dv) * ax.mid);
   }
 
   int band_axis_tile(int mode, const BandAxis& ax, const LineDev<R>& L1,
                      const LineDev<R>& L2) const {
-    const bool projm = mode == BAND_DOWN_PROJ || mode == BAND_UP_PROJ || mode == BAND_DOWN_PROJ_F;
+    const bool projm = mode == BAND_DOWN_PROJ || mode == BAND_UP_PROJ;
     const bool padin = mode == BAND_PAD || mode == BAND_PAD_PUPD;
     const int nlc = projm ? g_.dv : 1;
     const int nf = (padin ? 0 : L1.ld) +
-                   ((mode == BAND_DOWN || mode == BAND_DOWN_PROJ_F || mode == BAND_DOWN_F) ? 0
-                                                                                    : L2.ld);
+                   ((mode == BAND_DOWN || mode == BAND_DOWN_F) ? 0 : L2.ld);
     // twice the usual line target: the axis passes are bound by instruction
     // issue, and more columns per CTA fill the radix stages of every line
     // length (and lengthen the contiguous rows); the register file still
-    // allows two CTAs per SM.  The spectral projection pass holds one line
-    // buffer per column, so its tile may use the integration pass's budget.
-    const size_t budget = (mode == BAND_DOWN_PROJ_F && sizeof(R) == 4) ? kBandLastBudget32
-                                                                        : kSmemBudget;
-    return tile_cols(nf, nlc, ax.inner, 2 * kTargetElems * axis_target_mult_, budget);
+    // allows two CTAs per SM.
+    return tile_cols(nf, nlc, ax.inner, 2 * kTargetElems * axis_target_mult_, kSmemBudget);
   }
 
   int band_axis(int mode, const cplx<R>* in, cplx<R>* out, const BandAxis& ax_in,
@@ -1702,12 +1696,11 @@ class Engine final : public EngineBase {
                 const char* name, cplx<R>* aux = nullptr, double* parts = nullptr) {
     BandAxis ax = ax_in;
     set_band_divs(ax);
-    const bool projm = mode == BAND_DOWN_PROJ || mode == BAND_UP_PROJ || mode == BAND_DOWN_PROJ_F;
+    const bool projm = mode == BAND_DOWN_PROJ || mode == BAND_UP_PROJ;
     const bool padin = mode == BAND_PAD || mode == BAND_PAD_PUPD;
     const int nlc = projm ? g_.dv : 1;
     const int nf = (padin ? 0 : L1.ld) +
-                   ((mode == BAND_DOWN || mode == BAND_DOWN_PROJ_F || mode == BAND_DOWN_F) ? 0
-                                                                                    : L2.ld);
+                   ((mode == BAND_DOWN || mode == BAND_DOWN_F) ? 0 : L2.ld);
     const int T = band_axis_tile(mode, ax, L1, L2);
     const size_t smem = (size_t)nlc * T * nf * sizeof(cplx<R>);
     if (smem > kSmemMax) { set_error("band line too long for shared memory"); return ST_BAD_ARG; }
@@ -1722,7 +1715,7 @@ class Engine final : public EngineBase {
                    (ax.n_in + ax.n_out) * sizeof(cplx<R>);
     if (mode == BAND_PAD_PUPD)
       bytes += 2.0 * (g_.L * g_.dv) * ax.mid * ax.inner * ax.n_in * sizeof(cplx<R>);
-    if ((mode == BAND_DOWN_PROJ_F || mode == BAND_DOWN_F) && parts)
+    if (mode == BAND_DOWN_F && parts)
       bytes += (double)(g_.L * g_.dv) * ax.mid * ax.inner * ax.n_out * sizeof(cplx<R>);
     // the input projection of G A G is the plain orthogonal projection (scale 1);
     // the output projection carries s / prod(B)
@@ -1748,11 +1741,6 @@ class Engine final : public EngineBase {
       case BAND_PAD_PUPD:
         k_band_axis<R, BAND_PAD_PUPD, 0><<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st, aux, nullptr);
         break;
-      case BAND_DOWN_PROJ_F: {
-        auto k = scalar ? k_band_axis<R, BAND_DOWN_PROJ_F, 0> : k_band_axis<R, BAND_DOWN_PROJ_F, 1>;
-        k<<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st, aux, parts);
-        break;
-      }
       case BAND_DOWN_F:
         k_band_axis<R, BAND_DOWN_F, 0><<<grid, kThreads, smem, s>>>(in, out, g_, ax, L1, L2, T, gp_, ad, st, aux, parts);
         break;

@@ -1123,12 +1123,11 @@ __global__ void k_ga_gather(const cplx<R>* __restrict__ Sp, cplx<R>* __restrict_
 //   BAND_PAD       : frequency (N layout) -> band pad -> iDFT_B -> space B
 //   BAND_PAD_PUPD  : as BAND_PAD, the input being the CG direction of the
 //                    spectral iterates, updated first (p = r + beta p)
-//   BAND_DOWN_PROJ_F : space B -> DFT_B -> band -> G(xi) -> frequency (N
-//                    layout) of the spectral iterates, with the partial <p, Ap>
-//   BAND_DOWN_F    : as BAND_DOWN_PROJ_F without G (one comp per CTA): the
-//                    spectral CG projects A p in its update instead
+//   BAND_DOWN_F    : space B -> DFT_B -> band -> times the operator scale ->
+//                    frequency (N layout) of the spectral iterates, with the
+//                    partial <p, Ap>; the spectral CG applies G in its update
 enum BandMode { BAND_UP = 0, BAND_DOWN = 1, BAND_DOWN_PROJ = 2, BAND_UP_PROJ = 3, BAND_PAD = 4,
-                BAND_PAD_PUPD = 5, BAND_DOWN_PROJ_F = 6, BAND_DOWN_F = 7 };
+                BAND_PAD_PUPD = 5, BAND_DOWN_F = 7 };
 
 struct BandAxis {
   int n_in, n_out;     // line lengths in / out
@@ -1216,7 +1215,7 @@ __device__ __forceinline__ void tile_loop(int nlc, int n, int T, int lgT, F&& bo
 }
 
 // aux: BAND_PAD_PUPD the CG direction p (read and updated in place, Sin = r);
-// BAND_DOWN_PROJ_F the direction p read for the partial <p, Ap>, written to
+// BAND_DOWN_F the direction p read for the partial <p, Ap>, written to
 // partials[(blockIdx.y * gridDim.x + blockIdx.x) * L + l] (zero for l other
 // than the CTA's load) when partials is not null.
 // FP32 pad passes hold one line buffer per column and no per-frequency
@@ -1239,8 +1238,7 @@ __global__ void __launch_bounds__(256, band_axis_min_blocks<R, MODE>()) k_band_a
                                                    double* __restrict__ partials) {
   if (all_done && *all_done) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr bool PROJ = (MODE == BAND_DOWN_PROJ || MODE == BAND_UP_PROJ ||
-                         MODE == BAND_DOWN_PROJ_F);
+  constexpr bool PROJ = (MODE == BAND_DOWN_PROJ || MODE == BAND_UP_PROJ);
   constexpr bool PADIN = (MODE == BAND_PAD || MODE == BAND_PAD_PUPD);
   const int nlc = PROJ ? g.dv : 1;   // comps per CTA
   // blockIdx.y: (comp or load) * mid + m
@@ -1249,13 +1247,12 @@ __global__ void __launch_bounds__(256, band_axis_min_blocks<R, MODE>()) k_band_a
   const int c0 = PROJ ? cl * g.dv : cl;
   const int load = c0 / g.dv;
   if (st && st[load].done) {
-    if ((MODE == BAND_DOWN_PROJ_F || MODE == BAND_DOWN_F) && partials && threadIdx.x < g.L)
+    if (MODE == BAND_DOWN_F && partials && threadIdx.x < g.L)
       partials[((long long)blockIdx.y * gridDim.x + blockIdx.x) * g.L + threadIdx.x] = 0.;
     return;
   }
   const int ld1 = PADIN ? 0 : L1.ld;
-  const int ld2 = (MODE == BAND_DOWN || MODE == BAND_DOWN_PROJ_F || MODE == BAND_DOWN_F) ? 0
-                                                                                     : L2.ld;
+  const int ld2 = (MODE == BAND_DOWN || MODE == BAND_DOWN_F) ? 0 : L2.ld;
   cplx<R>* buf1 = reinterpret_cast<cplx<R>*>(smem_raw);
   cplx<R>* buf2 = buf1 + (size_t)nlc * T * ld1;
   const long long t0 = (long long)blockIdx.x * T;
@@ -1266,8 +1263,7 @@ __global__ void __launch_bounds__(256, band_axis_min_blocks<R, MODE>()) k_band_a
   // are read at |q| <= n_out/2 only; zeros on the pruned digits are not written
   const bool pr2 = (MODE == BAND_UP || MODE == BAND_UP_PROJ || PADIN) &&
                    line_prunable<R>(L2, ax.n_in / 2);
-  const bool pr1 = (MODE == BAND_DOWN || MODE == BAND_DOWN_PROJ || MODE == BAND_DOWN_PROJ_F ||
-                    MODE == BAND_DOWN_F) &&
+  const bool pr1 = (MODE == BAND_DOWN || MODE == BAND_DOWN_PROJ || MODE == BAND_DOWN_F) &&
                    line_prunable<R>(L1, ax.n_out / 2);
   const int pq0 = L2.nf / 4, pq1 = 3 * (L2.nf / 4);  // pruned range of the B line (pr2)
   if constexpr (MODE == BAND_PAD) {
@@ -1448,35 +1444,12 @@ __global__ void __launch_bounds__(256, band_axis_min_blocks<R, MODE>()) k_band_a
       cplx<R>* dst = Sout + (((long long)(c0 + c) * ax.mid + m) * ax.n_out) * ax.inner + col;
       dst[(long long)k * ax.inner] = v;
     });
-  } else if constexpr (MODE == BAND_DOWN_PROJ_F || MODE == BAND_DOWN_F) {
-    if constexpr (MODE == BAND_DOWN_PROJ_F) {
-    // G(xi) on the band, written back in place into the B-line slot of each
-    // N frequency (lanes over the frequencies of one column)
-    for (int t = 0; t < T; ++t)
-    for (int k = threadIdx.x; k < ax.n_out; k += blockDim.x) {
-      const long long col = t0 + t;
-      const int q = signed_freq(k, ax.n_out);
-      cplx<R> x[kMaxDv];
-#pragma unroll
-      for (int c = 0; c < kMaxDv; ++c)
-        if (c < g.dv) x[c] = band_down_value<R>(buf1 + (c * T + t) * ld1, L1, k, ax.n_out, ax.n_in);
-      if (col < ax.inner) {
-        int kv[3];
-        band_freqs(ax, g.dim, q, m, col, kv);
-        green_apply<R, PHYS>(gp, g.dim, kv, x);
-      }
-      const int kb = q < 0 ? q + ax.n_in : q;
-#pragma unroll
-      for (int c = 0; c < kMaxDv; ++c)
-        if (c < g.dv) set_fwd<R>(buf1 + (c * T + t) * ld1, L1, kb, x[c]);
-    }
-    __syncthreads();
-    }
-    // rows of T columns to global (z form: times sqrt(w)), with <p, Ap>: a
-    // thread keeps one column and takes its frequencies four at a time, the
-    // four loads of p issued before their products.  Without G in the pass
-    // (BAND_DOWN_F) the operator's scale (s / prod(B)) is applied here.
-    const R osc = MODE == BAND_DOWN_F ? R(gp.scale) : R(1);
+  } else if constexpr (MODE == BAND_DOWN_F) {
+    // rows of T columns to global (z form: times sqrt(w) and the operator's
+    // scale s / prod(B)), with <p, Ap>: a thread keeps one column and takes
+    // its frequencies four at a time, the four loads of p issued before their
+    // products
+    const R osc = R(gp.scale);
     R dot = R(0);
     if (T <= (int)blockDim.x) {
       const int t = threadIdx.x & (T - 1);
