@@ -905,16 +905,31 @@ template <typename R>
 __device__ __forceinline__ void put_fwd(cplx<R>* line, const LineDev<R>& L, int j, cplx<R> v) {
   line[sp(j)] = L.blue ? cmul<R>(v, L.chirp[j]) : v;
 }
+// digit-reversed slot of frequency k in a direct line: shifts and masks when
+// the line runs the compile-time power-of-two stages (the same positions as
+// the plan's table), the table otherwise
+template <typename R>
+__device__ __forceinline__ int line_pos(const LineDev<R>& L, int k) {
+  switch (L.lg2) {
+    case 5: return p2_pos<5, p2_k_for<R>(5)>(k);
+    case 6: return p2_pos<6, p2_k_for<R>(6)>(k);
+    case 7: return p2_pos<7, p2_k_for<R>(7)>(k);
+    case 8: return p2_pos<8, p2_k_for<R>(8)>(k);
+    case 9: return p2_pos<9, p2_k_for<R>(9)>(k);
+    case 10: return p2_pos<10, p2_k_for<R>(10)>(k);
+    default: return L.pos[k];
+  }
+}
 // forward output X_k (k < n)
 template <typename R>
 __device__ __forceinline__ cplx<R> get_fwd(const cplx<R>* line, const LineDev<R>& L, int k) {
-  return L.blue ? cmul<R>(line[sp(k)], L.chirp[k]) : line[sp(L.pos[k])];
+  return L.blue ? cmul<R>(line[sp(k)], L.chirp[k]) : line[sp(line_pos<R>(L, k))];
 }
 // inverse input X_k (k < n)
 template <typename R>
 __device__ __forceinline__ void put_inv(cplx<R>* line, const LineDev<R>& L, int k, cplx<R> v) {
   if (L.blue) line[sp(k)] = cmul<R>(cconj<R>(v), L.chirp[k]);
-  else line[sp(L.pos[k])] = v;
+  else line[sp(line_pos<R>(L, k))] = v;
 }
 // inverse output x_j (j < n), unnormalised
 template <typename R>
@@ -934,7 +949,7 @@ template <typename R>
 __device__ __forceinline__ int slot_fwd(const LineDev<R>& L, int j) { return sp(j); }
 template <typename R>
 __device__ __forceinline__ int slot_inv(const LineDev<R>& L, int k) {
-  return L.blue ? sp(k) : sp(L.pos[k]);
+  return L.blue ? sp(k) : sp(line_pos<R>(L, k));
 }
 // Bluestein lines loaded raw into slots j < n: forward input x_j chirp_j,
 // inverse input conj(X_k) chirp_k (what put_fwd / put_inv store).

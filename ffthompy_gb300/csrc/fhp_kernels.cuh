@@ -1190,7 +1190,7 @@ __device__ __forceinline__ R half_weight_root(const BandAxis& ax, const GridDims
 template <typename R>
 __device__ __forceinline__ void set_fwd(cplx<R>* line, const LineDev<R>& L, int k, cplx<R> v) {
   if (L.blue) line[sp(k)] = cmulc<R>(v, L.chirp[k]);
-  else line[sp(L.pos[k])] = v;
+  else line[sp(line_pos<R>(L, k))] = v;
 }
 
 // Visits every (tile line c < nlc, line index k < n, column t < T) of a
