@@ -1224,7 +1224,8 @@ __device__ __forceinline__ void tile_loop(int nlc, int n, int T, int lgT, F&& bo
 // and 0.99 -> 0.85 ms at the 509^3 workload; the down pass was not faster).
 template <typename R, int MODE>
 constexpr int band_axis_min_blocks() {
-  return (sizeof(R) == 4 && (MODE == 4 || MODE == 5)) ? 3 : kFftMinBlocks<R>;
+  return (sizeof(R) == 4 && (MODE == 4 || MODE == 5 || MODE == 1 || MODE == 7)) ? 3
+                                                                                 : kFftMinBlocks<R>;
 }
 
 template <typename R, int MODE, int PHYS>
