@@ -1218,14 +1218,17 @@ __device__ __forceinline__ void tile_loop(int nlc, int n, int T, int lgT, F&& bo
 // BAND_DOWN_F the direction p read for the partial <p, Ap>, written to
 // partials[(blockIdx.y * gridDim.x + blockIdx.x) * L + l] (zero for l other
 // than the CTA's load) when partials is not null.
-// FP32 pad passes hold one line buffer per column and no per-frequency
-// projection: three CTAs per SM fit their registers (80) and shared memory,
-// which hides more of their global-memory latency (measured: 1.13 -> 1.06 ms
-// and 0.99 -> 0.85 ms at the 509^3 workload; the down pass was not faster).
+// The FP32 pad and down passes of the spectral CG hold one line buffer per
+// column and no per-frequency projection: three CTAs per SM fit their
+// registers (80) and shared memory, which hides more of their global-memory
+// latency (measured at the 509^3 workload: pad 1.13 -> 1.06 ms and 0.99 ->
+// 0.85 ms; with table-free line slots, down 0.98 -> 0.92 ms and 0.63 -> 0.56).
 template <typename R, int MODE>
 constexpr int band_axis_min_blocks() {
-  return (sizeof(R) == 4 && (MODE == 4 || MODE == 5 || MODE == 1 || MODE == 7)) ? 3
-                                                                                 : kFftMinBlocks<R>;
+  return (sizeof(R) == 4 && (MODE == BAND_PAD || MODE == BAND_PAD_PUPD || MODE == BAND_DOWN ||
+                             MODE == BAND_DOWN_F))
+             ? 3
+             : kFftMinBlocks<R>;
 }
 
 template <typename R, int MODE, int PHYS>
