@@ -469,6 +469,53 @@ def fibres_measure(n=127, tol=1e-6, seed=0):
     return out
 
 
+def _cfg1_problem():
+    """The 2D 45^2 GaNi square-inclusion problem (side 0.6, 11 I / 1 I), both
+    loads, primal and dual, tol 1e-8, with GaNi and Ga (order None) bounds."""
+    N = np.array([45, 45])
+    mat = {'inclusions': ['square', 'otherwise'], 'positions': [np.zeros(2), ''],
+           'params': [0.6 * np.ones(2), ''], 'vals': [11 * np.eye(2), np.eye(2)],
+           'Y': np.ones(2), 'order': None}
+    return {'name': 'square45', 'physics': 'scalar', 'material': mat,
+            'solve': {'kind': 'GaNi', 'N': N, 'primaldual': ['primal', 'dual']},
+            'solver': {'kind': 'CG', 'tol': 1e-8, 'maxiter': 1000},
+            'postprocess': [{'kind': 'GaNi'}, {'kind': 'Ga', 'order': None}]}
+
+
+def cfg1_measure(with_cpu=True, reps=5):
+    """Time to solution of the 45^2 square-inclusion problem (latency-bound):
+    the whole Problem.calculate() through the drop-in API in FP64 (median of
+    reps after one warm run), and, on the host, the oracle (NumPy restatement
+    of the reference, as shipped with its CallBack) on the same problem."""
+    import torch
+    from ffthompy_gb300.problem import Problem
+    times = []
+    for i in range(reps + 1):
+        pb = Problem(_cfg1_problem(), None)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pb.calculate()
+        torch.cuda.synchronize()
+        if i:
+            times.append(time.perf_counter() - t0)
+    out = {'grid': [45, 45], 'loads': 2, 'tol': 1e-8, 'precision': 'f64',
+           'seconds_median': float(np.median(times)),
+           'kit_primal': [int(r['info']['kit']) for r in pb.output['res_primal']],
+           'AH_GaNi_primal_00': float(pb.output['mat_primal']['AH_GaNi_primal'][0, 0]),
+           'AH_Ga_primal_00': float(pb.output['mat_primal']['AH_Ga_primal'][0, 0]),
+           'AH_Ga_dual_00': float(pb.output['mat_dual']['AH_Ga_dual'][0, 0])}
+    if with_cpu:
+        sys.path.insert(0, ROOT)
+        import oracle
+        t0 = time.perf_counter()
+        ref = oracle.solve_problem(_cfg1_problem(), as_shipped=True)
+        out['oracle_cpu_seconds'] = time.perf_counter() - t0
+        a = pb.output['mat_primal']['AH_GaNi_primal']
+        b = ref['mat_primal']['AH_GaNi_primal']
+        out['AH_rel_diff_vs_oracle'] = float(np.abs(a - b).max() / np.abs(b).max())
+    return out
+
+
 def adjoint_measure(n=127, tol=1e-10):
     """dA_H/da(x) of the scalar GaNi problem with a(x) = exp(g(x)) on n^3
     (g a seeded Gaussian random field, length 0.15), 3 loads, mixed
@@ -866,6 +913,7 @@ def run_gpu(args):
     if not args.no_fibres:
         extras['adjoint127'] = adjoint_measure()
         extras['fibres127'] = fibres_measure()
+        extras['cfg1_square45'] = cfg1_measure(with_cpu=not args.no_cpu_baseline)
         extras['coefficient_inverse'] = inverse_measure()
     if not args.no_ensemble:
         extras['ensemble_grf2d'] = ensemble_measure(dist=dist)

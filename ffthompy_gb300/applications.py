@@ -21,7 +21,7 @@ import time
 import numpy as np
 import torch
 
-from .engine import GalerkinPlan, nice_size
+from .engine import nice_size, shared_plan
 from .general.solver_pp import CallBack
 from .materials import Material
 from .postprocess import Solutions, postprocess
@@ -50,16 +50,16 @@ def _solve(pb, physics):
         proj = 1 if primaldual == 'primal' else 2
         if kind == 'GaNi':
             A = mat.get_A_GaNi(N, primaldual)
-            plan = GalerkinPlan(tuple(N), pb.Y, physics=physics, precision=precision)
+            plan = shared_plan(tuple(N), pb.Y, physics=physics, precision=precision)
         elif ga_mode == 'full':
             A = mat.get_A_Ga(Nbar=Nbar, primaldual=primaldual)
-            plan = GalerkinPlan(tuple(Nbar), pb.Y, physics=physics, band=tuple(N),
-                                precision=precision)
+            plan = shared_plan(tuple(Nbar), pb.Y, physics=physics, band=tuple(N),
+                               precision=precision)
         else:
             integ = tuple(nice_size(n) for n in Nbar)
             A = mat.get_A_Ga(Nbar=Nbar, primaldual=primaldual, grid=integ)
-            plan = GalerkinPlan(tuple(N), pb.Y, physics=physics, integ=integ,
-                                precision=precision)
+            plan = shared_plan(tuple(N), pb.Y, physics=physics, integ=integ,
+                               precision=precision)
         ph = phases.setdefault(primaldual, {})
         ph['coefficient_s'] = tp()
         plan.set_coefficient(A.data)

@@ -3,7 +3,9 @@
 Device memory for fields is allocated with torch (plumbing only); all
 arithmetic on the hot path runs in the library's own CUDA kernels.
 """
+import collections
 import ctypes
+import threading
 
 import numpy as np
 
@@ -491,6 +493,41 @@ class GalerkinPlan:
         return AH, list(kit), list(nres), xh
 
 
+# Plans of small grids reused across calls of the drop-in API (creation
+# allocates and uploads line tables: a latency-bound problem would pay it on
+# every call); least recently used first out
+_PLAN_CACHE = collections.OrderedDict()
+_PLAN_CACHE_LOCK = threading.Lock()
+_PLAN_CACHE_SIZE = 4
+_PLAN_CACHE_MAX_POINTS = 1 << 21
+
+
+def shared_plan(N, Y, **kw):
+    """GalerkinPlan(N, Y, **kw) from a small process-wide cache when its grids
+    are small (at most 2^21 points), else a new plan.  A cached plan is the
+    caller's until its next request of the same geometry; one thread at a
+    time (the Problem / applications path)."""
+    N = tuple(int(n) for n in N)
+    integ = kw.get('integ')
+    pts = max(int(np.prod(N)), int(np.prod(integ)) if integ is not None else 0)
+    if pts > _PLAN_CACHE_MAX_POINTS:
+        return GalerkinPlan(N, Y, **kw)
+    norm = tuple(sorted((k, tuple(v) if isinstance(v, (list, tuple, np.ndarray)) else v)
+                        for k, v in kw.items()))
+    key = (torch.cuda.current_device(), N, tuple(np.asarray(Y, dtype=np.float64).tolist()), norm)
+    with _PLAN_CACHE_LOCK:
+        plan = _PLAN_CACHE.get(key)
+        if plan is not None:
+            _PLAN_CACHE.move_to_end(key)
+            return plan
+    plan = GalerkinPlan(N, Y, **kw)
+    with _PLAN_CACHE_LOCK:
+        _PLAN_CACHE[key] = plan
+        while len(_PLAN_CACHE) > _PLAN_CACHE_SIZE:
+            _PLAN_CACHE.popitem(last=False)
+    return plan
+
+
 def cg_many(plans, bs, tol=1e-6, maxiter=1000, proj=1):
     """CG on several plans at once (fhp_cg_solve_many): plan i solves its own
     loads from bs[i], zero start, with its own scalars and stopping tests; all
@@ -533,6 +570,14 @@ def _fft_plan(grid, ncomp, precision):
     return h
 
 
+# FFT plans of small grids, kept for the process (creation uploads line
+# tables and allocates; a latency-bound problem would pay it on every call);
+# a plan is not re-entrant, so its use is serialised
+_FFT_CACHE = {}
+_FFT_CACHE_LOCK = threading.Lock()
+_FFT_CACHE_MAX = 1 << 22     # grid points x components of a cached plan
+
+
 def interpolate_fields(x, src, dst):
     """Trigonometric interpolation (Tensor.project, objects.py:488-511) of the
     fields x[..., src] onto grid dst >= src on the GPU (fhp_fourier_interp)."""
@@ -546,13 +591,22 @@ def interpolate_fields(x, src, dst):
     stream = ctypes.c_void_p(torch.cuda.current_stream(x.device).cuda_stream)
     for k0 in range(0, ncomp, 6):
         k1 = min(ncomp, k0 + 6)
+        args = (ctypes.c_void_p(xs[k0:k1].data_ptr()), ctypes.c_void_p(out[k0:k1].data_ptr()),
+                stream)
+        if int(np.prod(dst)) * (k1 - k0) <= _FFT_CACHE_MAX:
+            key = (x.device.index, src, dst, k1 - k0, x.dtype)
+            with _FFT_CACHE_LOCK:
+                if key not in _FFT_CACHE:
+                    _FFT_CACHE[key] = (_fft_plan(src, k1 - k0, x.dtype),
+                                       _fft_plan(dst, k1 - k0, x.dtype))
+                hs, hd = _FFT_CACHE[key]
+                _lib.check(lib.fhp_fourier_interp(hs, hd, *args), 'fhp_fourier_interp')
+            continue
         hs = _fft_plan(src, k1 - k0, x.dtype)
         try:
             hd = _fft_plan(dst, k1 - k0, x.dtype)
             try:
-                _lib.check(lib.fhp_fourier_interp(hs, hd, ctypes.c_void_p(xs[k0:k1].data_ptr()),
-                                                  ctypes.c_void_p(out[k0:k1].data_ptr()), stream),
-                           'fhp_fourier_interp')
+                _lib.check(lib.fhp_fourier_interp(hs, hd, *args), 'fhp_fourier_interp')
             finally:
                 lib.fhp_plan_destroy(hd)
         finally:

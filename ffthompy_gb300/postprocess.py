@@ -19,7 +19,7 @@ import time
 
 import numpy as np
 
-from .engine import GalerkinPlan, interpolate_fields, nice_size
+from .engine import interpolate_fields, nice_size, shared_plan
 from .tensors.objects import Tensor
 
 
@@ -73,14 +73,14 @@ def assembly_matrix(A, solutions):
     if getattr(plan, '_coef_tensor', None) is A:
         return plan.energy(solutions.X, add_macro=True)
     if G == N and plan.integ is None:
-        plan_e = GalerkinPlan(N, plan.Y, physics=plan.physics, nloads=plan.nloads,
-                              band=plan.band, scale=plan.scale, precision=plan.precision)
+        plan_e = shared_plan(N, plan.Y, physics=plan.physics, nloads=plan.nloads,
+                             band=plan.band, scale=plan.scale, precision=plan.precision)
     elif all(g >= 2 * n - 1 for g, n in zip(G, N)):
-        plan_e = GalerkinPlan(N, plan.Y, physics=plan.physics, nloads=plan.nloads, integ=G,
-                              precision=plan.precision)
+        plan_e = shared_plan(N, plan.Y, physics=plan.physics, nloads=plan.nloads, integ=G,
+                             precision=plan.precision)
     elif G == N:
-        plan_e = GalerkinPlan(N, plan.Y, physics=plan.physics, nloads=plan.nloads,
-                              precision=plan.precision)
+        plan_e = shared_plan(N, plan.Y, physics=plan.physics, nloads=plan.nloads,
+                             precision=plan.precision)
     else:
         raise NotImplementedError('energy of solutions on %s with a coefficient on %s'
                                   % (N, G))
