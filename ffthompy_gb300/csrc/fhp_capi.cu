@@ -16,6 +16,18 @@ struct fhp_plan_s {
   std::unique_ptr<fhp::EngineBase> lo;   // MIXED: FP32 engine of the inner CG
   double eta = 1e-4;                     // MIXED: inner relative tolerance floor
   int max_outer = 30;
+  // the plan's own stream for solves requested on the legacy default stream
+  // (which cannot be captured into CUDA graphs), and its ordering events
+  cudaStream_t own = nullptr;
+  cudaEvent_t fence_in = nullptr, fence_out = nullptr;
+  ~fhp_plan_s() {
+    if (own) {
+      cudaStreamSynchronize(own);
+      cudaStreamDestroy(own);
+    }
+    if (fence_in) cudaEventDestroy(fence_in);
+    if (fence_out) cudaEventDestroy(fence_out);
+  }
 };
 
 namespace {
@@ -42,6 +54,41 @@ int cuda_status(cudaError_t e, const char* what) {
   fhp::set_error(std::string(what) + ": " + cudaGetErrorString(e));
   return e == cudaErrorMemoryAllocation ? FHP_OOM : FHP_CUDA;
 }
+
+// A solve requested on the legacy default stream runs on the plan's own
+// non-blocking stream instead, so that its iterations can be captured and
+// replayed as CUDA graphs: the plan stream first waits for the caller's
+// earlier work, and the caller's stream waits for the solve at the end.
+class PlanStream {
+ public:
+  PlanStream(fhp_plan_s* p, cudaStream_t caller) : p_(p), caller_(caller), s_(caller) {
+    if (caller != nullptr && caller != cudaStreamLegacy) return;
+    if (!p->own) {
+      if (cudaStreamCreateWithFlags(&p->own, cudaStreamNonBlocking) != cudaSuccess ||
+          cudaEventCreateWithFlags(&p->fence_in, cudaEventDisableTiming) != cudaSuccess ||
+          cudaEventCreateWithFlags(&p->fence_out, cudaEventDisableTiming) != cudaSuccess) {
+        (void)cudaGetLastError();   // keep the caller's stream (no graphs)
+        return;
+      }
+    }
+    if (cudaEventRecord(p->fence_in, caller) != cudaSuccess ||
+        cudaStreamWaitEvent(p->own, p->fence_in, 0) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return;
+    }
+    s_ = p->own;
+  }
+  ~PlanStream() {
+    if (s_ == caller_) return;
+    cudaEventRecord(p_->fence_out, s_);
+    cudaStreamWaitEvent(caller_, p_->fence_out, 0);
+  }
+  cudaStream_t get() const { return s_; }
+
+ private:
+  fhp_plan_s* p_;
+  cudaStream_t caller_, s_;
+};
 
 
 // The inner tolerance of each cell of a plan of several cells: the cell's own
@@ -690,9 +737,12 @@ int fhp_cg_solve(fhp_plan plan, int proj, const void* b, const void* x0, double 
   if (!(tol >= 0)) return bad("tol must be >= 0");
   fhp::SolveResult r;
   const int rows = res_log ? std::max(1, log_rows) : 1;
-  int st = plan->lo ? cg_mixed(*plan, proj, b, x0, tol, maxiter, x, r, rows, as_stream(stream))
-                    : plan->eng->cg_solve(proj, b, x0, tol, maxiter, x, r, rows,
-                                          as_stream(stream));
+  int st;
+  {
+    PlanStream ps(plan, as_stream(stream));
+    st = plan->lo ? cg_mixed(*plan, proj, b, x0, tol, maxiter, x, r, rows, ps.get())
+                  : plan->eng->cg_solve(proj, b, x0, tol, maxiter, x, r, rows, ps.get());
+  }
   if (st != FHP_OK && r.kit.empty()) return st;
   const int L = loads_all(*plan->eng);
   for (int l = 0; l < L && l < (int)r.kit.size(); ++l) {
@@ -721,7 +771,8 @@ int fhp_cg_solve_many(int count, const fhp_plan* plans, int proj, const void* co
     for (int j = 0; j < i; ++j)
       if (plans[j] == plans[i]) return bad("a plan appears twice");
   }
-  cudaStream_t s = as_stream(stream);
+  PlanStream pstream(plans[0], as_stream(stream));
+  cudaStream_t s = pstream.get();
   std::vector<fhp::SolveResult> r;
   std::vector<const void*> bv(b, b + count);
   std::vector<void*> xv(x, x + count);
@@ -757,8 +808,9 @@ int solve_other_c(int kind, fhp_plan plan, int proj, const void* b, const void* 
   if (maxiter < 0) return bad("maxiter must be >= 0");
   if (!(tol >= 0)) return bad("tol must be >= 0");
   fhp::SolveResult r;
+  PlanStream ps(plan, as_stream(stream));
   const int st = plan->eng->solve_other(kind, proj, b, x0, p0, p1, tol, maxiter, x, r, 1,
-                                        as_stream(stream));
+                                        ps.get());
   const int L = plan->eng->loads();
   for (int l = 0; l < L && l < (int)r.kit.size(); ++l) {
     if (kit) kit[l] = r.kit[l];
@@ -835,9 +887,10 @@ int fhp_homogenize_host(fhp_plan plan, int proj, int coef_kind, const double* co
                         double tol, int maxiter, double* AH_host, int* kit_host,
                         double* norm_res_host, void* x_host, void* stream) {
   if (!plan || !coef_host || !AH_host) return bad("plan, coef_host and AH_host are required");
-  cudaStream_t s = as_stream(stream);
+  PlanStream ps(plan, as_stream(stream));
+  cudaStream_t s = ps.get();
   fhp::EngineBase& e = *plan->eng;
-  int st = fhp_set_coefficient(plan, coef_kind, coef_host, 0, stream);
+  int st = fhp_set_coefficient(plan, coef_kind, coef_host, 0, s);
   if (st != FHP_OK) return st;
   const size_t bytes = (size_t)loads_all(e) * e.dv() * e.voxels() * e.elem_size();
   // the plan's persistent scratch: repeated calls allocate nothing

@@ -158,35 +158,39 @@ class Engine final : public EngineBase {
     g_.ss = (long long)C * g_.n0 * g_.n1 * g_.n2h;
     spec_elems_ = (size_t)g_.K * g_.ss;
     FHP_CHECK(cudaMalloc(&S_, spec_elems_ * sizeof(cplx<R>)));
+    int dev = 0;
+    FHP_CHECK(cudaGetDevice(&dev));
+    FHP_CHECK(cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, dev));
     // launch geometry
     const int np = (C + 1) / 2;
-    const size_t srow = (size_t)np * l2_.dev.ld * sizeof(cplx<R>);
     // rows per CTA for the last-axis passes: pair lines plus (when it fits
-    // the per-CTA budget) a staging area for the c2r input spectra
-    (void)srow;
-    rows_ = set_row_geometry(std::max(1, kTargetElems / (np * l2_.dev.ld)));
+    // the per-CTA budget) a staging area for the c2r input spectra; on small
+    // grids fewer rows, so that the passes still spread over the SMs
+    rows_ = set_row_geometry(std::min(std::max(1, kTargetElems / (np * l2_.dev.ld)),
+                                      small_grid_cap((long long)g_.n0 * g_.n1)));
     if (smem_rows_ > kSmemMax) { set_error("line too long for shared memory"); return ST_BAD_ARG; }
     // strided c2c on axis 1 (3D) and projection on the first real axis
     if (d == 3) {
       // column passes: twice the line target (as the band-axis passes) fills
       // the radix stages of short lines and lengthens the contiguous rows
       T1_ = tile_cols(l1_.dev.ld, 1, (long long)g_.n2h, 2 * kTargetElems);
+      T1_ = std::min(T1_, small_grid_cap((long long)g_.n2h * C * g_.n0, true));
     }
     const LineDev<R>& lp = (d == 3) ? l0_.dev : l1_.dev;
     const long long pin = (d == 3) ? (long long)g_.n1 * g_.n2h : (long long)g_.n2h;
     Tp_ = tile_cols(lp.ld, g_.dv, pin);
+    Tp_ = std::min(Tp_, small_grid_cap(pin * g_.L, true));
     if ((size_t)Tp_ * g_.dv * lp.ld * sizeof(cplx<R>) > kSmemMax) {
       set_error("projection line too long for shared memory");
       return ST_BAD_ARG;
     }
     if (d == 3) T0_ = tile_cols(l0_.dev.ld, 1, (long long)g_.n1 * g_.n2h, 2 * kTargetElems);
+    if (d == 3)
+      T0_ = std::min(T0_, small_grid_cap((long long)g_.n1 * g_.n2h * C, true));
     if (cfg_.integ[0] > 0) {
       if ((st = init_band()) != ST_OK) return st;
     }
     // reduction scratch
-    int dev = 0;
-    FHP_CHECK(cudaGetDevice(&dev));
-    FHP_CHECK(cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, dev));
     red_ctas_ = (int)std::max<long long>(1, std::min<long long>(4LL * nsm_, (g_.M + kThreads - 1) / kThreads));
     // parts of the reductions: row passes, grid-stride kernels, and the
     // component-split CG update (at least one part per component)
@@ -249,6 +253,20 @@ class Engine final : public EngineBase {
   // rows per CTA of the last-axis passes: pair lines plus (when it fits the
   // per-CTA budget) a staging area for the c2r input spectra; the request is
   // reduced until it fits.  Sets rows_, c2r_stage_, smem_rows_, row_ctas_.
+  // Largest rows (columns) per CTA that still give about two CTAs per SM when
+  // a pass has `units` rows (columns) per cell: small grids spread over the
+  // SMs instead of running a few long CTAs (a power of two for column tiles).
+  // Per cell, so a plan of several cells computes each cell as a plan of that
+  // cell alone does.
+  int small_grid_cap(long long units, bool pow2 = false) const {
+    long long c = std::max<long long>(1, units / (2LL * std::max(1, nsm_)));
+    c = std::min<long long>(c, 1 << 20);
+    int r = (int)c;
+    if (pow2)
+      while (r & (r - 1)) r &= r - 1;
+    return std::max(1, r);
+  }
+
   int set_row_geometry(int want) {
     const int C = g_.L * g_.dv, np = (C + 1) / 2;
     const size_t srow = (size_t)np * l2_.dev.ld * sizeof(cplx<R>);
