@@ -453,6 +453,16 @@ class Engine final : public EngineBase {
     pp.Yg[2] = cfg_.Y[d - 1];
     pp.scale = (double)g_.M / ((double)pp.nb[0] * pp.nb[1] * pp.nb[2]);
     pp.zs = 1.0 / ((double)pp.nb[0] * pp.nb[1] * pp.nb[2]);
+    for (int a = 0; a < 3; ++a) {
+      pp.tpy[a] = 6.283185307179586476925286766559 / pp.Yg[a];
+      pp.tpy_f[a] = (float)pp.tpy[a];
+    }
+    pp.izs = 1.0 / pp.zs;
+    pp.iscale = 1.0 / pp.scale;
+    pp.scale_f = (float)pp.scale;
+    pp.zs_f = (float)pp.zs;
+    pp.izs_f = (float)pp.izs;
+    pp.iscale_f = (float)pp.iscale;
     if (!pe_) {
       FHP_CHECK(cudaMalloc(&pe_, (size_t)g_.K * g_.L * g_.dv * g_.M * sizeof(R)));
       const int T = d == 3 ? T0_ : tile_cols(l1_.dev.ld, 1, (long long)g_.n2h);
@@ -498,14 +508,21 @@ class Engine final : public EngineBase {
   // y = P (-div) decrease F A iF enlarge grad P x ; zio: x and y z-scaled
   int pot_operator(const cplx<R>* x, cplx<R>* y, bool zio, bool cg, cudaStream_t s) {
     const int* ad = cg ? all_done_ : nullptr;
-    const long long ns = (long long)g_.L * g_.n0 * g_.n1 * g_.n2h;
-    k_pot_expand<R><<<grid_for((size_t)ns), kThreads, 0, s>>>(x, S_, g_, pp_, zio ? 1 : 0, ad);
+    const long long ns = (long long)g_.n0 * g_.n1 * g_.n2h;
+    const int pke = pbeg("pot_expand", (double)pot_spectrum_elems() * sizeof(cplx<R>) +
+                                           g_.dim * spec_bytes() / g_.dv, s);
+    k_pot_expand<R><<<dim3(grid_for((size_t)ns), g_.L), kThreads, 0, s>>>(x, S_, g_, pp_,
+                                                                        zio ? 1 : 0, ad);
+    pend(pke, s);
     FHP_LAUNCHED();
     int rc = pot_inv(pe_, cg, s);
     if (rc == ST_OK) rc = pot_fwd(pe_, cg, s);
     if (rc != ST_OK) return rc;
-    k_pot_contract<R><<<grid_for((size_t)pot_spectrum_elems()), kThreads, 0, s>>>(
-        S_, y, g_, pp_, -1.0, zio ? 1 : 0, ad);
+    const int pkc = pbeg("pot_contract", (double)pot_spectrum_elems() * sizeof(cplx<R>) +
+                                             g_.dim * spec_bytes() / g_.dv, s);
+    k_pot_contract<R><<<dim3(grid_for((size_t)(pot_spectrum_elems() / g_.L)), g_.L), kThreads,
+                        0, s>>>(S_, y, g_, pp_, -1.0, zio ? 1 : 0, ad);
+    pend(pkc, s);
     FHP_LAUNCHED();
     return ST_OK;
   }
@@ -517,8 +534,8 @@ class Engine final : public EngineBase {
     k_fill_macro<R><<<grid_for(n), kThreads, 0, s>>>(pe_, g_, 1.0);
     FHP_LAUNCHED();
     if ((rc = pot_fwd(pe_, false, s)) != ST_OK) return rc;
-    k_pot_contract<R><<<grid_for((size_t)pot_spectrum_elems()), kThreads, 0, s>>>(
-        S_, static_cast<cplx<R>*>(bh), g_, pp_, 1.0, 0, nullptr);
+    k_pot_contract<R><<<dim3(grid_for((size_t)(pot_spectrum_elems() / g_.L)), g_.L), kThreads,
+                        0, s>>>(S_, static_cast<cplx<R>*>(bh), g_, pp_, 1.0, 0, nullptr);
     FHP_LAUNCHED();
     return ST_OK;
   }
@@ -533,8 +550,8 @@ class Engine final : public EngineBase {
   int pot_field(const void* xh, void* X, cudaStream_t s) override {
     int rc = pot_check();
     if (rc != ST_OK) return rc;
-    const long long ns = (long long)g_.L * g_.n0 * g_.n1 * g_.n2h;
-    k_pot_expand<R><<<grid_for((size_t)ns), kThreads, 0, s>>>(
+    const long long ns = (long long)g_.n0 * g_.n1 * g_.n2h;
+    k_pot_expand<R><<<dim3(grid_for((size_t)ns), g_.L), kThreads, 0, s>>>(
         static_cast<const cplx<R>*>(xh), S_, g_, pp_, 0, nullptr);
     FHP_LAUNCHED();
     return pot_inv(static_cast<R*>(X), false, s);
@@ -598,17 +615,24 @@ class Engine final : public EngineBase {
       for (int it = 0; it < nit && rc == ST_OK; ++it) {
         rc = pot_operator(zp, zap, true, true, s);
         if (rc != ST_OK) break;
+        const double zb = (double)nz * sizeof(cplx<R>);   // one z vector
+        int pk = pbeg("pot_dot", 2.0 * zb, s);
         k_dot<R><<<red_ctas_, kThreads, 0, s>>>(rp, rap, partials_, gz);
+        pend(pk, s);
         FHP_LAUNCHED();
         k_fin_pap<<<g_.L, kThreads, 0, s>>>(partials_, red_ctas_, st_, g_.L, 1.0, all_done_);
         FHP_LAUNCHED();
+        pk = pbeg("pot_cg_update", 6.0 * zb, s);
         k_cg_update<R><<<red_ctas_, kThreads, 0, s>>>(rx, rr, rp, rap, partials_, gz, st_,
                                                       all_done_);
+        pend(pk, s);
         FHP_LAUNCHED();
         k_fin_rr<<<g_.L, kThreads, 0, s>>>(partials_, red_ctas_, st_, g_.L, 1.0, dlog, log_rows,
                                            all_done_);
         FHP_LAUNCHED();
+        pk = pbeg("pot_p_update", 3.0 * zb, s);
         k_p_update<R><<<grid_for(2 * nz), kThreads, 0, s>>>(rr, rp, gz, st_, all_done_);
+        pend(pk, s);
         FHP_LAUNCHED();
         k_update_all_done<<<1, 1, 0, s>>>(st_, g_.L, all_done_);
         FHP_LAUNCHED();

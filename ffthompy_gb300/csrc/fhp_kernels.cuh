@@ -640,18 +640,34 @@ __global__ void __launch_bounds__(256) k_dot(const R* __restrict__ x, const R* _
   partials += (long long)blockIdx.y * gridDim.x * g.L;
   __shared__ double red[8 * kMaxLoads];
   double acc[kMaxLoads];
-  for (int i = 0; i < kMaxLoads; ++i) acc[i] = 0.;
+  R part[kMaxLoads];   // up to 8 voxels per thread in the field precision
+  for (int i = 0; i < kMaxLoads; ++i) {
+    acc[i] = 0.;
+    part[i] = R(0);
+  }
   const long long stride = (long long)gridDim.x * blockDim.x;
+  int cnt = 0;
   for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < g.M; v += stride) {
 #pragma unroll
     for (int l = 0; l < kMaxLoads; ++l) {
       if (l >= g.L) break;
       for (int c = 0; c < g.dv; ++c) {
         const long long i = (long long)(l * g.dv + c) * g.M + v;
-        acc[l] += (double)x[i] * (double)y[i];
+        part[l] += x[i] * y[i];
       }
     }
+    // into FP64 every 8 voxels: FP64 arithmetic is the slow pipe on this GPU
+    if (++cnt == 8) {
+#pragma unroll
+      for (int l = 0; l < kMaxLoads; ++l) {
+        acc[l] += (double)part[l];
+        part[l] = R(0);
+      }
+      cnt = 0;
+    }
   }
+#pragma unroll
+  for (int l = 0; l < kMaxLoads; ++l) acc[l] += (double)part[l];
   block_sum_n(acc, g.L, red, partials + (long long)blockIdx.x * g.L);
 }
 
@@ -2401,48 +2417,60 @@ struct PotParams {
   double Yg[3];    // cell size per GridDims axis
   double scale;    // enlargement prod(Ns)/prod(N)
   double zs;       // 1 / prod(N)
+  // the per-launch factors, formed on the host (an FP64 division per thread
+  // runs on the slow FP64 pipe): 2 pi / Yg, 1 / zs, 1 / scale, in both precisions
+  double tpy[3], izs, iscale;
+  float tpy_f[3], scale_f, zs_f, izs_f, iscale_f;
 };
+
+template <typename R>
+__device__ __forceinline__ R pot_pick(float f, double d) {
+  if constexpr (sizeof(R) == 4) return f; else return d;
+}
 
 // frequency of index k on an n-point axis in the reference's 'r' form
 // (trigpol.py:27-40): 0..ceil(n/2)-1, then negative; the even-n Nyquist
 // index carries -n/2, also on the half axis
 __device__ __forceinline__ int ref_freq(int k, int n) { return k < (n + 1) / 2 ? k : k - n; }
 
-__device__ __forceinline__ double pot_weight(int k2, int n2) {
-  return (k2 == 0 || 2 * k2 == n2) ? 1.0 : 2.0;
-}
 
-// 2 pi xi per axis and P at frequency q (dim 2: q[0] = 0)
-__device__ __forceinline__ double pot_symbols(const PotParams& pp, int dim, const int* q,
-                                              double* tpx) {
-  const double tp = 6.283185307179586476925286766559;
-  double k2 = 0.;
+// 2 pi xi per axis and P at frequency q in the field precision T (dim 2:
+// q[0] = 0); tpy = 2 pi / Y per axis
+template <typename T>
+__device__ __forceinline__ T pot_symbols_t(int dim, const int* q, const T* tpy, T* tpx) {
+  T k2 = T(0);
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    tpx[a] = (a == 0 && dim == 2) ? 0. : tp * (double)q[a] / pp.Yg[a];
+    tpx[a] = (a == 0 && dim == 2) ? T(0) : tpy[a] * (T)q[a];
     k2 += tpx[a] * tpx[a];
   }
-  return (q[0] == 0 && q[1] == 0 && q[2] == 0) ? 1.0 : 1.0 / sqrt(k2);
+  return (q[0] == 0 && q[1] == 0 && q[2] == 0) ? T(1) : T(1) / sqrt(k2);
 }
 
 // S[l*d + a] (solve grid half spectrum) = scale * 2 pi i xi_a * P * x_l on the
-// band of N, 0 elsewhere; x natural (zin = 0) or z-scaled (zin = 1)
+// band of N, 0 elsewhere; x natural (zin = 0) or z-scaled (zin = 1).  Grid y
+// is the load; the symbols are evaluated in the field precision.
 template <typename R>
 __global__ void k_pot_expand(const cplx<R>* __restrict__ xin, cplx<R>* __restrict__ S,
-                             GridDims g, PotParams pp, int zin,
+                             const __grid_constant__ GridDims g,
+                             const __grid_constant__ PotParams pp, int zin,
                              const int* __restrict__ all_done) {
   if (all_done && *all_done) return;
-  const long long Ms = (long long)g.n0 * g.n1 * g.n2h;
+  const int Ms = g.n0 * g.n1 * g.n2h;
   const long long Mn = (long long)pp.nb[0] * pp.nb[1] * pp.nbh;
-  const long long tot = (long long)g.L * Ms;
   const int d = g.dim;
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += stride) {
-    const int l = (int)(e / Ms);
-    const long long v = e - (long long)l * Ms;
-    const int i2 = (int)(v % g.n2h);
-    const long long r = v / g.n2h;
-    const int i1 = (int)(r % g.n1), i0 = (int)(r / g.n1);
+  const int l = blockIdx.y;
+  R tpy[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) tpy[a] = pot_pick<R>(pp.tpy_f[a], pp.tpy[a]);
+  const R fs = pot_pick<R>(pp.scale_f, pp.scale);
+  const R fz = pot_pick<R>(pp.izs_f, pp.izs);
+  const cplx<R>* xl = xin + (long long)l * Mn;
+  cplx<R>* Sl = S + (long long)(l * d) * Ms;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < Ms; v += gridDim.x * blockDim.x) {
+    const int r = fdiv(v, g.dn2h);
+    const int i2 = v - r * g.n2h;
+    const int i0 = r / g.n1, i1 = r - i0 * g.n1;
     const int q[3] = {ref_freq(i0, g.n0), ref_freq(i1, g.n1), ref_freq(i2, g.n2)};
     const int ns[3] = {g.n0, g.n1, g.n2};
     bool in = true;
@@ -2453,73 +2481,82 @@ __global__ void k_pot_expand(const cplx<R>* __restrict__ xin, cplx<R>* __restric
       if (ns[a] != n) in = in && (2 * (q[a] < 0 ? -q[a] : q[a]) < n);
       kn[a] = q[a] >= 0 ? q[a] : q[a] + n;
     }
-    cplx<R>* out = S + (long long)(l * d) * Ms + v;
+    cplx<R>* out = Sl + v;
     if (!in) {
       for (int a = 0; a < d; ++a) out[(long long)a * Ms] = mkc<R>(R(0), R(0));
       continue;
     }
-    const cplx<R> u0 = xin[(long long)l * Mn + ((long long)kn[0] * pp.nb[1] + kn[1]) * pp.nbh + kn[2]];
-    double tpx[3];
-    double f = pot_symbols(pp, d, q, tpx) * pp.scale;
-    if (zin) f /= pp.zs * sqrt(pot_weight(kn[2], pp.nb[2]));
-    const double ux = (double)u0.x * f, uy = (double)u0.y * f;
+    const cplx<R> u0 = xl[((long long)kn[0] * pp.nb[1] + kn[1]) * pp.nbh + kn[2]];
+    R tpx[3];
+    R f = pot_symbols_t<R>(d, q, tpy, tpx) * fs;
+    // z form: divide by zs sqrt(w), w = 1 on k2 = 0 and the even Nyquist, else 2
+    if (zin) f *= fz * ((kn[2] == 0 || 2 * kn[2] == pp.nb[2]) ? R(1) : R(0.70710678118654752440));
+    const R ux = u0.x * f, uy = u0.y * f;
     for (int a = 0; a < d; ++a) {
-      const double t = tpx[3 - d + a];
-      out[(long long)a * Ms] = mkc<R>((R)(-t * uy), (R)(t * ux));
+      const R t = tpx[3 - d + a];
+      out[(long long)a * Ms] = mkc<R>(-t * uy, t * ux);
     }
   }
 }
 
 // y_l (potential grid half spectrum) = sign * P / scale * sum_a 2 pi i xi_a
 // S[l*d + a] read at the band frequencies of the solve grid; y natural
-// (zout = 0) or z-scaled (zout = 1)
+// (zout = 0) or z-scaled (zout = 1).  Grid y is the load.
 template <typename R>
 __global__ void k_pot_contract(const cplx<R>* __restrict__ S, cplx<R>* __restrict__ y,
-                               GridDims g, PotParams pp, double sign, int zout,
+                               const __grid_constant__ GridDims g,
+                               const __grid_constant__ PotParams pp, double sign, int zout,
                                const int* __restrict__ all_done) {
   if (all_done && *all_done) return;
   const long long Ms = (long long)g.n0 * g.n1 * g.n2h;
-  const long long Mn = (long long)pp.nb[0] * pp.nb[1] * pp.nbh;
-  const long long tot = (long long)g.L * Mn;
+  const int Mn = pp.nb[0] * pp.nb[1] * pp.nbh;
   const int d = g.dim;
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += stride) {
-    const int l = (int)(e / Mn);
-    const long long v = e - (long long)l * Mn;
-    const int k2 = (int)(v % pp.nbh);
-    const long long r = v / pp.nbh;
-    const int k1 = (int)(r % pp.nb[1]), k0 = (int)(r / pp.nb[1]);
+  const int l = blockIdx.y;
+  R tpy[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) tpy[a] = pot_pick<R>(pp.tpy_f[a], pp.tpy[a]);
+  const R fs = pot_pick<R>(pp.iscale_f, pp.iscale) * (sign < 0 ? R(-1) : R(1));
+  const R fz = pot_pick<R>(pp.zs_f, pp.zs);
+  const cplx<R>* Sl = S + (long long)(l * d) * Ms;
+  cplx<R>* yl = y + (long long)l * Mn;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < Mn; v += gridDim.x * blockDim.x) {
+    const int r = v / pp.nbh;
+    const int k2 = v - r * pp.nbh;
+    const int k0 = r / pp.nb[1], k1 = r - k0 * pp.nb[1];
     const int q[3] = {ref_freq(k0, pp.nb[0]), ref_freq(k1, pp.nb[1]), ref_freq(k2, pp.nb[2])};
     const int ns[3] = {g.n0, g.n1, g.n2};
     int ks[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) ks[a] = q[a] >= 0 ? q[a] : q[a] + ns[a];
     const long long sv = ((long long)ks[0] * g.n1 + ks[1]) * g.n2h + ks[2];
-    double tpx[3];
-    double f = sign * pot_symbols(pp, d, q, tpx) / pp.scale;
-    if (zout) f *= pp.zs * sqrt(pot_weight(k2, pp.nb[2]));
-    double ax = 0., ay = 0.;
+    R tpx[3];
+    R f = pot_symbols_t<R>(d, q, tpy, tpx) * fs;
+    if (zout) f *= fz * ((k2 == 0 || 2 * k2 == pp.nb[2]) ? R(1) : R(1.4142135623730950488));
+    R ax = R(0), ay = R(0);
     for (int a = 0; a < d; ++a) {
-      const cplx<R> s = S[(long long)(l * d + a) * Ms + sv];
-      const double t = tpx[3 - d + a];
-      ax -= t * (double)s.y;
-      ay += t * (double)s.x;
+      const cplx<R> sa = Sl[(long long)a * Ms + sv];
+      const R t = tpx[3 - d + a];
+      ax -= t * sa.y;
+      ay += t * sa.x;
     }
-    y[(long long)l * Mn + v] = mkc<R>((R)(f * ax), (R)(f * ay));
+    yl[v] = mkc<R>(f * ax, f * ay);
   }
 }
 
-// natural <-> z scaling of potential spectra (to_z: z = zs sqrt(w) x)
+// natural <-> z scaling of potential spectra (to_z: z = zs sqrt(w) x; w = 1
+// on k2 = 0 and the even Nyquist, else 2)
 template <typename R>
 __global__ void k_pot_zscale(const cplx<R>* __restrict__ in, cplx<R>* __restrict__ out,
-                             long long tot, PotParams pp, int to_z) {
+                             long long tot, const __grid_constant__ PotParams pp, int to_z) {
   const long long stride = (long long)gridDim.x * blockDim.x;
+  const R zs = pot_pick<R>(pp.zs_f, pp.zs), izs = pot_pick<R>(pp.izs_f, pp.izs);
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += stride) {
     const int k2 = (int)(e % pp.nbh);
-    const double w = pp.zs * sqrt(pot_weight(k2, pp.nb[2]));
-    const double f = to_z ? w : 1.0 / w;
+    const bool one = k2 == 0 || 2 * k2 == pp.nb[2];
+    const R f = to_z ? zs * (one ? R(1) : R(1.4142135623730950488))
+                     : izs * (one ? R(1) : R(0.70710678118654752440));
     const cplx<R> u = in[e];
-    out[e] = mkc<R>((R)(f * (double)u.x), (R)(f * (double)u.y));
+    out[e] = mkc<R>(f * u.x, f * u.y);
   }
 }
 
