@@ -2827,6 +2827,8 @@ __global__ void __launch_bounds__(256) k_cg_update_spec(cplx<R>* __restrict__ x,
   double acc = 0.;
   if (!st[l].done) {
     const R a = (R)st[l].alpha;
+    R part = R(0);   // up to 8 frequencies in the field precision, then FP64
+    int cnt = 0;
     for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < F; f += gridDim.x * blockDim.x) {
       const int q = fdiv(f, g.dn2h);
       const int k2 = f - q * g.n2h;
@@ -2853,9 +2855,15 @@ __global__ void __launch_bounds__(256) k_cg_update_spec(cplx<R>* __restrict__ x,
         x[i] = mkc<R>(xc.x + a * pc.x, xc.y + a * pc.y);
         const cplx<R> rn = mkc<R>(rc.x - a * v[c].x, rc.y - a * v[c].y);
         r[i] = rn;
-        acc += (double)(rn.x * rn.x + rn.y * rn.y);
+        part += rn.x * rn.x + rn.y * rn.y;
+      }
+      if (++cnt == 8) {
+        acc += (double)part;
+        part = R(0);
+        cnt = 0;
       }
     }
+    acc += (double)part;
   }
   const double t = warp_sum(acc);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
