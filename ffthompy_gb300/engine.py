@@ -573,9 +573,10 @@ def _fft_plan(grid, ncomp, precision):
 # FFT plans of small grids, kept for the process (creation uploads line
 # tables and allocates; a latency-bound problem would pay it on every call);
 # a plan is not re-entrant, so its use is serialised
-_FFT_CACHE = {}
+_FFT_CACHE = collections.OrderedDict()
 _FFT_CACHE_LOCK = threading.Lock()
 _FFT_CACHE_MAX = 1 << 22     # grid points x components of a cached plan
+_FFT_CACHE_SIZE = 16         # cached plan pairs (least recently used out)
 
 
 def interpolate_fields(x, src, dst):
@@ -599,6 +600,10 @@ def interpolate_fields(x, src, dst):
                 if key not in _FFT_CACHE:
                     _FFT_CACHE[key] = (_fft_plan(src, k1 - k0, x.dtype),
                                        _fft_plan(dst, k1 - k0, x.dtype))
+                    while len(_FFT_CACHE) > _FFT_CACHE_SIZE:
+                        for h in _FFT_CACHE.popitem(last=False)[1]:
+                            lib.fhp_plan_destroy(h)
+                _FFT_CACHE.move_to_end(key)
                 hs, hd = _FFT_CACHE[key]
                 _lib.check(lib.fhp_fourier_interp(hs, hd, *args), 'fhp_fourier_interp')
             continue
