@@ -891,12 +891,14 @@ static __global__ void k_fin_init(const double* __restrict__ partials, int npart
   if (res_log && log_cap > 0) res_log[l] = S.norm_res;
 }
 
-// y = a*x + b*y elementwise over n values
+// y = a*x + b*y elementwise over n values, in the field precision (FP64
+// arithmetic is the slow pipe on this GPU)
 template <typename R>
 __global__ void k_axpby(long long n, double a, const R* __restrict__ x, double b, R* __restrict__ y) {
   const long long stride = (long long)gridDim.x * blockDim.x;
+  const R ar = (R)a, br = (R)b;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
-    y[i] = (R)(a * (double)x[i] + b * (double)y[i]);
+    y[i] = ar * x[i] + br * y[i];
 }
 
 // x[l*dv + c] = val * delta(c, l)  (the constant macroscopic field E_N of load l,
@@ -2790,14 +2792,14 @@ template <typename R>
 __global__ void k_half_weight(const cplx<R>* __restrict__ in, cplx<R>* __restrict__ out,
                               long long tot, int n2h, int n2, double f, int to_z) {
   const long long stride = (long long)gridDim.x * blockDim.x;
+  const R fr = (R)f;   // the field precision per element (FP64 is the slow pipe)
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += stride) {
     const int k2 = (int)(e % n2h);
     const bool single = k2 == 0 || 2 * k2 == n2;
-    const double w = single ? 1.0 : (to_z ? 1.4142135623730950488016887242097
-                                          : 0.70710678118654752440084436210485);
-    const double fw = f * w;
+    const R fw = single ? fr : fr * (to_z ? R(1.4142135623730950488016887242097)
+                                          : R(0.70710678118654752440084436210485));
     const cplx<R> u = in[e];
-    out[e] = mkc<R>((R)(fw * (double)u.x), (R)(fw * (double)u.y));
+    out[e] = mkc<R>(fw * u.x, fw * u.y);
   }
 }
 
