@@ -7,8 +7,13 @@
  * are DEVICE pointers of the plan's element type (double for FHP_F64, float
  * for FHP_F32) with layout [load][component][n0][n1][n2] in C order, unless a
  * function says "host".  `stream` is a cudaStream_t (NULL = legacy default
- * stream).  Every function returns an FHP_* status code; no function aborts
- * or traps.  Plans are not re-entrant: one thread and one stream per plan.
+ * stream).  The solvers (fhp_cg_solve, fhp_cg_solve_many, the other solvers,
+ * fhp_homogenize_host) asked for the legacy default stream run on a stream of
+ * the plan instead, ordered after the caller's earlier work and before its
+ * later work by events, so that their iterations replay as CUDA graphs (the
+ * legacy stream cannot be captured).  Every function returns an FHP_* status
+ * code; no function aborts or traps.  Plans are not re-entrant: one thread
+ * and one stream per plan.
  *
  * The reference (vondrejc/FFTHomPy, pure Python/NumPy) has no C interface;
  * each entry point below names the Python call it replaces.  The ctypes
