@@ -68,6 +68,9 @@ SIGNATURES = {
     'fhp_homogenize_host': (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _vp, ctypes.c_double,
                                            ctypes.c_int, _c_double_p, _c_int_p, _c_double_p, _vp,
                                            _vp]),
+    'fhp_homogenize_host_many': (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                ctypes.POINTER(_vp), ctypes.c_double, ctypes.c_int,
+                                                _c_double_p, _c_int_p, _c_double_p, _vp]),
     'fhp_fft_plan_create': (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.c_int, _c_int_p,
                                            ctypes.c_int, ctypes.c_int]),
     'fhp_ga_grid_coefficient': (ctypes.c_int, [_vp, _vp, _vp, _c_int_p, _c_double_p, _vp, _vp]),

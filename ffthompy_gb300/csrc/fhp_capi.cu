@@ -20,13 +20,20 @@ struct fhp_plan_s {
   // (which cannot be captured into CUDA graphs), and its ordering events
   cudaStream_t own = nullptr;
   cudaEvent_t fence_in = nullptr, fence_out = nullptr;
+  // fhp_homogenize_host_many: the upload stream and its two buffers' events
+  cudaStream_t copy = nullptr;
+  cudaEvent_t copied[2] = {nullptr, nullptr}, freed[2] = {nullptr, nullptr};
   ~fhp_plan_s() {
     if (own) {
       cudaStreamSynchronize(own);
       cudaStreamDestroy(own);
     }
-    if (fence_in) cudaEventDestroy(fence_in);
-    if (fence_out) cudaEventDestroy(fence_out);
+    if (copy) {
+      cudaStreamSynchronize(copy);
+      cudaStreamDestroy(copy);
+    }
+    for (cudaEvent_t e : {fence_in, fence_out, copied[0], copied[1], freed[0], freed[1]})
+      if (e) cudaEventDestroy(e);
   }
 };
 
@@ -911,6 +918,81 @@ int fhp_homogenize_host(fhp_plan plan, int proj, int coef_kind, const double* co
     if (kit_host) kit_host[l] = r.kit[l];
     if (norm_res_host) norm_res_host[l] = r.norm_res[l];
   }
+  return st;
+}
+
+int fhp_homogenize_host_many(fhp_plan plan, int proj, int coef_kind, int count,
+                             const double* const* coef_host, double tol, int maxiter,
+                             double* AH_host, int* kit_host, double* norm_res_host,
+                             void* stream) {
+  if (!plan || count < 0 || (count > 0 && (!coef_host || !AH_host)))
+    return bad("plan, coef_host and AH_host are required");
+  if (proj != 1 && proj != 2) return bad("proj must be 1 or 2");
+  if (coef_kind < FHP_COEF_ISO || coef_kind > FHP_COEF_FULL) return bad("bad coefficient kind");
+  for (int k = 0; k < count; ++k)
+    if (!coef_host[k]) return bad("every coefficient is required");
+  if (count == 0) return FHP_OK;
+  PlanStream ps(plan, as_stream(stream));
+  cudaStream_t s = ps.get();
+  fhp::EngineBase& e = *plan->eng;
+  const int dv = e.dv();
+  const int c = coef_kind == FHP_COEF_ISO ? 1 : coef_kind == FHP_COEF_SYM ? dv * (dv + 1) / 2
+                                                                          : dv * dv;
+  const size_t ncoef = (size_t)e.instances() * c * e.coef_voxels() * sizeof(double);
+  const size_t bytes = (size_t)loads_all(e) * dv * e.voxels() * e.elem_size();
+  void* stage[2] = {e.scratch(fhp::SCR_COEF_STAGE, ncoef), e.scratch(fhp::SCR_COEF_STAGE2, ncoef)};
+  void* b = e.scratch(fhp::SCR_HOST_B, bytes);
+  void* x = e.scratch(fhp::SCR_HOST_X, bytes);
+  if (!stage[0] || !stage[1] || !b || !x) return FHP_OOM;
+  if (!plan->copy) {
+    cudaError_t ce = cudaStreamCreateWithFlags(&plan->copy, cudaStreamNonBlocking);
+    for (int i = 0; i < 2 && ce == cudaSuccess; ++i) {
+      ce = cudaEventCreateWithFlags(&plan->copied[i], cudaEventDisableTiming);
+      if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&plan->freed[i], cudaEventDisableTiming);
+    }
+    if (ce != cudaSuccess) return cuda_status(ce, "upload stream");
+  }
+  cudaStream_t cp = plan->copy;
+  const int L = loads_all(e);
+  const int Lc = e.loads();
+  // the upload of coefficient k + 1 (on the plan's upload stream, into the
+  // other buffer) runs while problem k is solved; a buffer is reused once
+  // its coefficient has been converted into the plan
+  auto upload = [&](int k) -> int {
+    const int i = k & 1;
+    int st = cuda_status(cudaStreamWaitEvent(cp, plan->freed[i], 0), "wait");
+    if (st == FHP_OK)
+      st = cuda_status(cudaMemcpyAsync(stage[i], coef_host[k], ncoef, cudaMemcpyHostToDevice, cp),
+                       "upload");
+    if (st == FHP_OK) st = cuda_status(cudaEventRecord(plan->copied[i], cp), "record");
+    return st;
+  };
+  // the buffers start free (events recorded on the solve stream)
+  int st = cuda_status(cudaEventRecord(plan->freed[0], s), "record");
+  if (st == FHP_OK) st = cuda_status(cudaEventRecord(plan->freed[1], s), "record");
+  if (st == FHP_OK) st = upload(0);
+  for (int k = 0; k < count && st == FHP_OK; ++k) {
+    const int i = k & 1;
+    st = cuda_status(cudaStreamWaitEvent(s, plan->copied[i], 0), "wait");
+    if (st == FHP_OK)
+      st = e.set_coefficient(coef_kind, static_cast<const double*>(stage[i]), true, s);
+    if (st == FHP_OK && plan->lo)
+      st = plan->lo->set_coefficient(coef_kind, static_cast<const double*>(stage[i]), true, s);
+    if (st == FHP_OK) st = cuda_status(cudaEventRecord(plan->freed[i], s), "record");
+    if (st == FHP_OK && k + 1 < count) st = upload(k + 1);
+    if (st == FHP_OK) st = e.rhs_macro(proj, b, s);
+    fhp::SolveResult r;
+    if (st == FHP_OK)
+      st = plan->lo ? cg_mixed(*plan, proj, b, nullptr, tol, maxiter, x, r, 1, s)
+                    : e.cg_solve(proj, b, nullptr, tol, maxiter, x, r, 1, s);
+    if (st == FHP_OK) st = e.energy(x, 1, AH_host + (size_t)k * e.instances() * Lc * Lc, s);
+    for (int l = 0; l < L && l < (int)r.kit.size(); ++l) {
+      if (kit_host) kit_host[(size_t)k * L + l] = r.kit[l];
+      if (norm_res_host) norm_res_host[(size_t)k * L + l] = r.norm_res[l];
+    }
+  }
+  if (st == FHP_OK) st = cuda_status(cudaStreamSynchronize(s), "sync");
+  (void)cudaStreamSynchronize(cp);
   return st;
 }
 

@@ -50,6 +50,7 @@ enum ScratchSlot {
   SCR_SOLV_A,          // Richardson / Chebyshev / BiCG vectors
   SCR_SOLV_B,
   SCR_SOLV_C,
+  SCR_COEF_STAGE2,     // fhp_homogenize_host_many: the second coefficient upload buffer
   kScratchSlots
 };
 
@@ -125,6 +126,8 @@ class EngineBase {
   virtual size_t elem_size() const = 0;
   // coefficient (c values per voxel, component-major, f64 on host or device)
   virtual int set_coefficient(int kind, const double* values, bool on_device, cudaStream_t s) = 0;
+  // voxels of the coefficient grid per cell (the integration grid of band plans)
+  virtual long long coef_voxels() const = 0;
   virtual int coef_kind() const = 0;
   virtual int apply(int proj, const void* x, void* y, cudaStream_t s) = 0;
   // apply with the input projected first (G A G, band plans; same as apply otherwise)

@@ -414,6 +414,7 @@ class Engine final : public EngineBase {
   int dv() const override { return g_.dv; }
   int loads() const override { return g_.L; }
   int instances() const override { return g_.K; }
+  long long coef_voxels() const override { return band_ ? gi_.M : g_.M; }
   void set_load_tols(const double* tols, int n) override { load_tol_.assign(tols, tols + n); }
   size_t elem_size() const override { return sizeof(R); }
   size_t spectrum_elems() const override { return spec_elems_; }

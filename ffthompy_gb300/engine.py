@@ -528,6 +528,31 @@ def shared_plan(N, Y, **kw):
     return plan
 
 
+def homogenize_host_many(plan, packed, kind, proj=1, tol=1e-6, maxiter=1000):
+    """fhp_homogenize_host_many: A_H of several host coefficients (packed
+    values of `kind`, each (cells, c) + grid or (c,) + grid) on one plan, the
+    next upload overlapping the current solve (pinned host arrays overlap).
+    Returns (AH list, kit list, norm_res list) per coefficient."""
+    require_cuda()
+    vals = [np.ascontiguousarray(v, dtype=np.float64) for v in packed]
+    n = len(vals)
+    lead = (plan.ncells,) if plan.ncells > 1 else ()
+    L = plan.nloads
+    AH = np.zeros((n,) + lead + (L, L))
+    kit = (ctypes.c_int * (n * plan._lk))()
+    nres = (ctypes.c_double * (n * plan._lk))()
+    ptrs = (ctypes.c_void_p * n)(*[v.ctypes.data for v in vals])
+    st = plan.lib.fhp_homogenize_host_many(plan.handle, int(proj), int(kind), n, ptrs,
+                                           float(tol), int(maxiter),
+                                           AH.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                           kit, nres, plan._stream())
+    _lib.check(st, 'fhp_homogenize_host_many')
+    plan.coef_kind = kind
+    k = plan._lk
+    return ([AH[i] for i in range(n)], [list(kit[i * k:(i + 1) * k]) for i in range(n)],
+            [list(nres[i * k:(i + 1) * k]) for i in range(n)])
+
+
 def cg_many(plans, bs, tol=1e-6, maxiter=1000, proj=1):
     """CG on several plans at once (fhp_cg_solve_many): plan i solves its own
     loads from bs[i], zero start, with its own scalars and stopping tests; all

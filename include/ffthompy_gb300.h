@@ -269,6 +269,19 @@ int fhp_fourier_interp(fhp_plan src, fhp_plan dst, const void* x_src, void* x_ds
 int fhp_homogenize_host(fhp_plan plan, int proj, int coef_kind, const double* coef_host,
                         double tol, int maxiter, double* AH_host, int* kit_host,
                         double* norm_res_host, void* x_host, void* stream);
+/*
+ * fhp_homogenize_host for `count` coefficients of the same plan in turn
+ * (coef_host[k] host arrays; pinned memory lets the uploads overlap): the
+ * upload of coefficient k + 1 runs on a second stream of the plan while
+ * problem k is solved.  AH_host holds count x (cells x L x L) values, kit_host
+ * and norm_res_host count x (cells x L).  Replaces: the reference's loop of
+ * applications.scalar / elasticity runs over several materials of one grid
+ * (ffthompy/applications.py:11-176).
+ */
+int fhp_homogenize_host_many(fhp_plan plan, int proj, int coef_kind, int count,
+                             const double* const* coef_host, double tol, int maxiter,
+                             double* AH_host, int* kit_host, double* norm_res_host,
+                             void* stream);
 
 /*
  * Potential formulation with the 1/|xi| preconditioner (scalar physics; plans
