@@ -48,6 +48,8 @@ def test_status_strings_and_bad_args(lib):
     assert lib.fhp_plan_create_cells(ctypes.byref(h), 2, n, n, y, 0, 2, 1.0, 0, 0) == 5
     assert lib.fhp_plan_create_cells(ctypes.byref(h), 2, n, n, y, 0, 2, 1.0, 0, 65536) == 5
     assert lib.fhp_plan_cells(None) == 0
+    assert lib.fhp_homogenize_host_many(None, 1, 1, 1, None, 1e-6, 10, None, None, None,
+                                        None) == 5
     assert lib.fhp_apply(None, 1, None, None, None) == 5
     assert b'required' in lib.fhp_last_error()
 

@@ -108,3 +108,20 @@ def test_two_gloo_ranks_gather_equals_single_process():
     assert len(out0) == len(single)
     for a, b in zip(out0, single):
         assert np.array_equal(np.asarray(a), b)
+
+
+def test_cell_groups_cover_each_cell_once_within_the_field_cap():
+    """homogenize_many's cell plans: the cells of one grid size in parts whose
+    FP64 fields stay below the cap, every cell in exactly one part."""
+    from ffthompy_gb300.batch import _cell_groups
+    rng = np.random.default_rng(3)
+    sizes = [(int(n), int(n)) for n in rng.choice([15, 31, 63], size=40)]
+    coefs = [np.zeros((2, 2) + N) for N in sizes]
+    groups = _cell_groups(coefs, None, 'scalar', field_cap=63 * 63 * 4 * 8 * 5)
+    seen = sorted(i for idx in groups.values() for i in idx)
+    assert seen == list(range(len(coefs)))
+    for (N, Y, part), idx in groups.items():
+        assert all(tuple(coefs[i].shape[2:]) == N for i in idx)
+        assert len(idx) * np.prod(N) * 4 * 8 <= max(63 * 63 * 4 * 8 * 5, np.prod(N) * 4 * 8)
+    big = [k for k in groups if k[0] == (63, 63)]
+    assert all(len(groups[k]) <= 5 for k in big)
