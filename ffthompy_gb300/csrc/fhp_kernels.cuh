@@ -2317,21 +2317,55 @@ __global__ void __launch_bounds__(128) k_cross_dot(const R* __restrict__ W, cons
                                                    int add_macro) {
   __shared__ double red[4 * kMaxLoads * kMaxLoads];
   const int L = g.L, dv = g.dv;
+  // per-voxel products in the field precision, summed over up to 8 voxels,
+  // then into FP64 (FP64 arithmetic is the slow pipe on this GPU); constant
+  // indices keep both arrays in registers
   double acc[kMaxLoads * kMaxLoads];
-  for (int i = 0; i < kMaxLoads * kMaxLoads; ++i) acc[i] = 0.;
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < g.M; v += stride) {
-    for (int i = 0; i < L; ++i)
-      for (int j = 0; j < L; ++j) {
-        double s = 0.;
-        for (int c = 0; c < dv; ++c) {
-          const double u = (double)X[(long long)(j * dv + c) * g.M + v] +
-                           ((add_macro && c == j) ? 1.0 : 0.0);
-          s += (double)W[(long long)(i * dv + c) * g.M + v] * u;
-        }
-        acc[i * L + j] += s;
-      }
+  R part[kMaxLoads * kMaxLoads];
+#pragma unroll
+  for (int i = 0; i < kMaxLoads * kMaxLoads; ++i) {
+    acc[i] = 0.;
+    part[i] = R(0);
   }
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  int cnt = 0;
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < g.M; v += stride) {
+#pragma unroll
+    for (int i = 0; i < kMaxLoads; ++i) {
+      if (i >= L) break;
+#pragma unroll
+      for (int j = 0; j < kMaxLoads; ++j) {
+        if (j >= L) break;
+        R s = R(0);
+        for (int c = 0; c < dv; ++c) {
+          const R u = X[(long long)(j * dv + c) * g.M + v] +
+                      ((add_macro && c == j) ? R(1) : R(0));
+          s += W[(long long)(i * dv + c) * g.M + v] * u;
+        }
+        part[i * kMaxLoads + j] += s;
+      }
+    }
+    if (++cnt == 8) {
+#pragma unroll
+      for (int i = 0; i < kMaxLoads * kMaxLoads; ++i) {
+        acc[i] += (double)part[i];
+        part[i] = R(0);
+      }
+      cnt = 0;
+    }
+  }
+  double out[kMaxLoads * kMaxLoads];
+#pragma unroll
+  for (int i = 0; i < kMaxLoads; ++i)
+#pragma unroll
+    for (int j = 0; j < kMaxLoads; ++j)
+      out[i * kMaxLoads + j] = acc[i * kMaxLoads + j] + (double)part[i * kMaxLoads + j];
+  // the L x L block first (the layout block_sum_n writes)
+#pragma unroll
+  for (int i = 0; i < kMaxLoads; ++i)
+#pragma unroll
+    for (int j = 0; j < kMaxLoads; ++j)
+      if (i < L && j < L) acc[i * L + j] = out[i * kMaxLoads + j];
   block_sum_n(acc, L * L, red, partials + (long long)blockIdx.x * L * L);
 }
 
