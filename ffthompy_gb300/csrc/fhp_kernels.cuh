@@ -2129,9 +2129,10 @@ constexpr int kR512WaitTries = 1 << 22;
 // stage buffer's mbarrier, in place of per-lane cp.async.  A wait that runs
 // out sets *err (and *stop, the CG's all-done flag, when given); the warp then
 // waits (bounded) for its other copy and returns.  Each warp walks its pair lines
-// (row by row, the np pair lines of a row in turn) and copies the next pair
-// line's spectra (and, at a new row, the next coefficient row) into shared
-// memory with cp.async while it transforms the current one.  A template
+// (row by row, the np pair lines of a row in turn; with an odd component count
+// two consecutive rows of the warp share the pair line of their last lines)
+// and copies the next pair line's spectra (and, at a new row, the next
+// coefficient row) into shared memory while it transforms the current one.  A template
 // instantiated for float only, so the FP64 translation unit compiles none of it.
 template <typename R, bool FULL>
 __global__ void __launch_bounds__(32 * kR512Warps, 2) k_band_last_r512(
@@ -2170,41 +2171,69 @@ __global__ void __launch_bounds__(32 * kR512Warps, 2) k_band_last_r512(
   const long long gw = (long long)blockIdx.x * kR512Warps + warp;
   const long long nw = (long long)gridDim.x * kR512Warps;
   const long long nrow_w = gw < nrows ? (nrows - gw + nw - 1) / nw : 0;   // rows of this warp
-  const long long ntask = nrow_w * np;
-  // copy task t (row gw + (t / np) nw, pair line t % np) into buffer t & 1
+  // An odd component count leaves one real line per row without a partner:
+  // the warp's rows i and i + 1 (i even) put their last lines into one pair
+  // line ("two"), X_a from row i and X_b from row i + 1, each multiplied by its
+  // own coefficient row.  Tasks of such a row pair: row i's pair lines
+  // 0..np-2, the shared line (its copy brings row i + 1's coefficient row),
+  // row i + 1's pair lines 0..np-2; 2 np - 1 transforms for two rows instead
+  // of 2 np.  A last unpaired row runs its np tasks alone.
+  const bool comb = (C & 1) && np > 1;
+  const long long T2 = 2 * np - 1;
+  const long long npr = comb ? nrow_w / 2 : 0;
+  const long long ntask = comb ? npr * T2 + (nrow_w & 1) * np : nrow_w * np;
+  // task t: row index i of this warp (row gw + i nw), pair line p, shared line
+  auto decode = [&](long long t, long long& i, int& p, bool& two) {
+    if (comb) {
+      const long long m = t / T2;
+      const int u = (int)(t - m * T2);
+      two = m < npr && u == np - 1;
+      i = (m < npr && u >= np) ? 2 * m + 1 : 2 * m;
+      p = (m < npr && u >= np) ? u - np : u;
+    } else {
+      i = t / np;
+      p = (int)(t - i * np);
+      two = false;
+    }
+  };
+  // copy task t into buffer t & 1; the coefficient row of row index i goes to
+  // coefficient buffer i & 1 (the shared line brings row i + 1's)
   auto prefetch = [&](long long t) {
+    long long i = 0;
+    int p = 0;
+    bool two = false;
+    if (t < ntask) decode(t, i, p, two);
+    const long long row = gw + i * nw;
+    const int b = (int)(t & 1);
+    const bool loadc = two || (p == 0 && !(comb && (i & 1)));
+    const long long crow = two ? row + nw : row;
+    float* cdst = cst + ((i + (two ? 1 : 0)) & 1) * 512;
+    const int halves = (two || 2 * p + 1 < C) ? 2 : 1;
+    // spectra row of half h: line 2p + h of this row, or line C - 1 of rows i, i + 1
+    auto srow = [&](int half) {
+      return two ? (long long)(C - 1) * nrows + row + half * nw
+                 : (long long)(2 * p + half) * nrows + row;
+    };
     if (tma) {
       if (t < ntask && lane == 0) {
-        const long long row = gw + (t / np) * nw;
-        const int p = (int)(t % np);
-        const int b = (int)(t & 1);
-        const int halves = (2 * p + 1 < C) ? 2 : 1;
         // the generic reads of these buffers (task t - 2) come first
         fence_proxy_async_smem();
-        mbar_arrive_expect_tx(wbar + b, (unsigned)(halves * 1024 + (p == 0 ? 2048 : 0)));
+        mbar_arrive_expect_tx(wbar + b, (unsigned)(halves * 1024 + (loadc ? 2048 : 0)));
         for (int half = 0; half < halves; ++half)
-          tma_load_2d(stg + (b * 2 + half) * 128, &tmS, 0, (int)((2 * p + half) * nrows + row),
-                      wbar + b);
-        if (p == 0)
-          tma_load_2d(cst + ((t / np) & 1) * 512, &tmA, 0, (int)row, wbar + b);
+          tma_load_2d(stg + (b * 2 + half) * 128, &tmS, 0, (int)srow(half), wbar + b);
+        if (loadc) tma_load_2d(cdst, &tmA, 0, (int)crow, wbar + b);
       }
       return;
     }
     if (t < ntask) {
-      const long long row = gw + (t / np) * nw;
-      const int p = (int)(t % np);
-      const int b = (int)(t & 1);
-      for (int half = 0; half < 2; ++half) {
-        const int c = 2 * p + half;
-        if (c >= C) break;
-        const float2* src = S + ((long long)c * nrows + row) * n2h;
+      for (int half = 0; half < halves; ++half) {
+        const float2* src = S + srow(half) * n2h;
         float2* dst = stg + (b * 2 + half) * 128;
         for (int k = lane; k < n2h; k += 32) cp_async_small<8>(dst + k, src + k);
       }
-      if (p == 0) {
-        const float* src = A + row * 512;
-        float* dst = cst + ((t / np) & 1) * 512;
-        for (int j = lane; j < 128; j += 32) cp_async_16(dst + 4 * j, src + 4 * j);
+      if (loadc) {
+        const float* src = A + crow * 512;
+        for (int j = lane; j < 128; j += 32) cp_async_16(cdst + 4 * j, src + 4 * j);
       }
     }
     cp_async_commit();
@@ -2212,8 +2241,11 @@ __global__ void __launch_bounds__(32 * kR512Warps, 2) k_band_last_r512(
   prefetch(0);
   float a[16];
   for (long long t = 0; t < ntask; ++t) {
-    const long long row = gw + (t / np) * nw;
-    const int p = (int)(t % np);
+    long long i;
+    int p;
+    bool two;
+    decode(t, i, p, two);
+    const long long row = gw + i * nw;
     const int b = (int)(t & 1);
     __syncwarp();       // every lane is done with the buffers of task t - 1
     prefetch(t + 1);
@@ -2233,13 +2265,13 @@ __global__ void __launch_bounds__(32 * kR512Warps, 2) k_band_last_r512(
       cp_async_wait<1>();
     }
     __syncwarp();       // task t's copies of every lane are visible
-    if (p == 0) {
-      const float* ar = cst + ((t / np) & 1) * 512;
+    if (p == 0 && !two) {
+      const float* ar = cst + (i & 1) * 512;
 #pragma unroll
       for (int j = 0; j < 16; ++j) a[j] = ar[32 * j + lane] * cs;
     }
     const int ca = 2 * p, cb = 2 * p + 1;
-    const bool hb = cb < C;
+    const bool hb = two || cb < C;
     const float2* sa = stg + (b * 2) * 128;
     const float2* sb = stg + (b * 2 + 1) * 128;
     float2 v[16];
@@ -2282,13 +2314,21 @@ __global__ void __launch_bounds__(32 * kR512Warps, 2) k_band_last_r512(
     }
     r512_inverse(v, tile, twt, lane);
     // q = a x cs on both real fields of the pair (the imaginary part is zero
-    // when the line has no second field)
+    // when the line has no second field); the shared line takes row i's
+    // coefficient (buffer 0, i even) on X_a and row i + 1's (buffer 1) on X_b
+    if (two) {
 #pragma unroll
-    for (int j = 0; j < 16; ++j) v[j] = make_float2(a[j] * v[j].x, hb ? a[j] * v[j].y : 0.f);
+      for (int j = 0; j < 16; ++j)
+        v[j] = make_float2((cst[32 * j + lane] * cs) * v[j].x,
+                           (cst[512 + 32 * j + lane] * cs) * v[j].y);
+    } else {
+#pragma unroll
+      for (int j = 0; j < 16; ++j) v[j] = make_float2(a[j] * v[j].x, hb ? a[j] * v[j].y : 0.f);
+    }
     r512_forward(v, tile, twt, lane);
     // split: X_a = (Z_k + conj Z_-k) / 2, X_b = (Z_k - conj Z_-k) / 2i
-    float2* da = S + ((long long)ca * nrows + row) * n2h;
-    float2* db = S + ((long long)cb * nrows + row) * n2h;
+    float2* da = S + (two ? (long long)(C - 1) * nrows + row : (long long)ca * nrows + row) * n2h;
+    float2* db = S + (two ? (long long)(C - 1) * nrows + row + nw : (long long)cb * nrows + row) * n2h;
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
       const float mx = __shfl_sync(0xffffffffu, v[15 - r].x, plane);

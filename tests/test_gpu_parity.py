@@ -422,7 +422,8 @@ def test_band_operator_pow2_integration_grid(N, physics, coef, precision):
                          iso=(coef == 'iso'))
 
 
-def _check_band_operator(N, physics, precision, integ, iso=False, integ_kernel='register'):
+def _check_band_operator(N, physics, precision, integ, iso=False, integ_kernel='register',
+                         nloads=2):
     from ffthompy_gb300.engine import GalerkinPlan
     rng = np.random.default_rng(len(N) + sum(N))
     d = len(N)
@@ -439,15 +440,15 @@ def _check_band_operator(N, physics, precision, integ, iso=False, integ_kernel='
         A = np.einsum('ik...,jk...->ij...', Bc, Bc) + 3 * np.einsum('ij,...->ij...', np.eye(dv),
                                                                     np.ones(tuple(Nb)))
     A_int = _project_comps(A, integ)
-    xN = rng.standard_normal((2, dv) + tuple(N))
-    plan = GalerkinPlan(tuple(N), Y, physics=physics, nloads=2, integ=integ,
+    xN = rng.standard_normal((nloads, dv) + tuple(N))
+    plan = GalerkinPlan(tuple(N), Y, physics=physics, nloads=nloads, integ=integ,
                         precision=precision, integ_kernel=integ_kernel)
     plan.set_coefficient(A_int)
     tol = 1e-11 if precision == 'f64' else 5e-5
     for proj in (1, 2):
         G, _ = oracle.green_operator(physics, Nn, Y, 'Ga', proj)
         y = plan.apply(xN, proj=proj).double().cpu().numpy()
-        for l in range(2):
+        for l in range(nloads):
             xb = _project_comps(xN[l], Nb)
             ref = oracle.apply_GA(G, A, xb)
             got = _project_comps(y[l], Nb)
@@ -460,7 +461,7 @@ def _check_band_operator(N, physics, precision, integ, iso=False, integ_kernel='
     def energy_check(x, plan_e, Ag):
         AH = plan_e.energy(x, add_macro=True)
         sols = []
-        for l in range(2):
+        for l in range(nloads):
             u = _project_comps(x[l], Nb).copy()
             u[l] += 1.
             sols.append(u)
@@ -478,7 +479,7 @@ def _check_band_operator(N, physics, precision, integ, iso=False, integ_kernel='
     xq = np.fft.ifftn(F, axes=axes).real
     energy_check(xq, plan, A_int)
     if any(n % 2 == 0 for n in N):
-        pe = GalerkinPlan(tuple(N), Y, physics=physics, nloads=2, integ=tuple(Nb),
+        pe = GalerkinPlan(tuple(N), Y, physics=physics, nloads=nloads, integ=tuple(Nb),
                           precision=precision)
         pe.set_coefficient(A)
         energy_check(xN, pe, A)
@@ -645,7 +646,23 @@ def test_band_operator_512_register_lines(N, integ_kernel):
     _check_band_operator(N, 'scalar', 'f32', integ, iso=True, integ_kernel=integ_kernel)
 
 
-@pytest.mark.parametrize('N', [(5, 7, 255), (9, 254)])
+@pytest.mark.parametrize('nloads', [1, 3])
+@pytest.mark.parametrize('integ_kernel', ['register', 'register_cpasync'])
+def test_band_operator_512_odd_components_share_lines(nloads, integ_kernel):
+    """An odd component count (3D scalar, 1 or 3 loads: 3 or 9 lines per row)
+    with several rows per warp: the last lines of two rows share one pair
+    line, each with its own coefficient row.  63 x 125 integration rows over
+    the kernel's 2 x 152 CTAs of 8 warps give each warp three or four rows,
+    so shared lines and a last unpaired row both occur."""
+    from ffthompy_gb300.engine import nice_size
+    N = (31, 63, 255)
+    integ = tuple(nice_size(2 * n - 1) for n in N)
+    assert integ == (63, 125, 512)
+    _check_band_operator(N, 'scalar', 'f32', integ, iso=True, integ_kernel=integ_kernel,
+                         nloads=nloads)
+
+
+@pytest.mark.parametrize('N', [(5, 7, 255), (9, 254), (31, 63, 255)])
 def test_band_cg_512_register_equals_shared_lines(N):
     """CG with either integration kernel: the same iteration counts (band
     rule) and A_H within FP32 accuracy."""
