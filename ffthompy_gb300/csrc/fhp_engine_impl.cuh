@@ -741,6 +741,7 @@ class Engine final : public EngineBase {
   }
 
   int rhs_macro(int proj, void* b, cudaStream_t s) override {
+    if (band_ && spectral_cg_) return spectral_rhs(proj, static_cast<R*>(b), s);
     const size_t n = (size_t)g_.K * g_.L * g_.dv * g_.M;
     R* tmp = static_cast<R*>(scratch(SCR_RHS_TMP, n * sizeof(R)));
     if (!tmp) return ST_OOM;
@@ -1179,6 +1180,119 @@ class Engine final : public EngineBase {
                      "band_downf_axis1", zp, partials_);
   }
 
+  // zout = A u on the band in z form, times gp_.scale, from the plain
+  // normalised half spectra of u in S_ (N layout, consumed): the passes of
+  // spectral_operator without the direction update, every load
+  int spectral_apply_plain(cplx<R>* zout, cudaStream_t s) {
+    int st;
+    const long long n2h = g_.n2h;
+    cplx<R>* Sbig;
+    if (g_.dim == 3) {
+      BandAxis a0{g_.n0, gi_.n0, g_.n0, gi_.n0, gp_.h[0], (long long)g_.n1 * n2h, 1, 1, 2,
+                  (int)n2h, g_.n1};
+      if ((st = band_axis(BAND_PAD, S_, SB_, a0, lb0_.dev, lb0_.dev, false, s,
+                          "band_pad_axis0")) != ST_OK) return st;
+      BandAxis a1{g_.n1, gi_.n1, g_.n1, gi_.n1, gp_.h[1], n2h, gi_.n0, g_.n0, 1, 0, 0};
+      if ((st = band_axis(BAND_PAD, SB_, S_, a1, lb1_.dev, lb1_.dev, false, s,
+                          "band_pad_axis1")) != ST_OK) return st;
+      Sbig = S_;
+    } else {
+      BandAxis a1{g_.n1, gi_.n1, g_.n1, gi_.n1, gp_.h[0], n2h, 1, 1, 0, 0, 0};
+      if ((st = band_axis(BAND_PAD, S_, SB_, a1, lb1_.dev, lb1_.dev, false, s,
+                          "band_pad_axis0")) != ST_OK) return st;
+      Sbig = SB_;
+    }
+    if ((st = band_last_pass(coef_kind_, Sbig, (R)1, false, s)) != ST_OK) return st;
+    if (g_.dim == 3) {
+      BandAxis a0{gi_.n0, g_.n0, g_.n0, gi_.n0, gp_.h[0], (long long)gi_.n1 * n2h, 1, 1, 2, 0, 0};
+      if ((st = band_axis(BAND_DOWN, S_, SB_, a0, lb0_.dev, l0_.dev, false, s,
+                          "band_down_axis0")) != ST_OK) return st;
+    }
+    return band_axis(BAND_DOWN_F, SB_, zout, spectral_proj_axis(), lb1_.dev, l1_.dev, false, s,
+                     "band_downf_axis1");
+  }
+
+  // B = G A (-E) of every load (applications.py:58 Afun(-E)) through the
+  // spectral passes: the constant field -E has the single frequency 0, so the
+  // solve-grid transforms of the real-field operator reduce to a zeroed
+  // spectrum and one write; G in z form, then the real field.
+  int spectral_rhs(int proj, R* b, cudaStream_t s) {
+    if (!A_) { set_error("coefficient not set"); return ST_BAD_ARG; }
+    int st = ensure_spectral();
+    if (st != ST_OK) return st;
+    const long long nzc = (long long)g_.n0 * g_.n1 * g_.n2h;
+    const size_t nz = (size_t)g_.L * g_.dv * nzc;
+    cplx<R>* zo = zb_ + 3 * nz;
+    FHP_CHECK(cudaMemsetAsync(S_, 0, nz * sizeof(cplx<R>), s));
+    k_z_macro<R><<<1, 32, 0, s>>>(S_, nzc, g_.L, g_.dv, -1.0);
+    FHP_LAUNCHED();
+    gp_.proj = proj;
+    // s A (-E) on the band (the operator scale s / prod(B)), then G (unit scale)
+    if ((st = spectral_apply_plain(zo, s)) != ST_OK) return st;
+    if ((st = spec_green(zo, s)) != ST_OK) return st;
+    return from_z(zo, b, s);
+  }
+
+  // A_H[i][j] = <A u_i, u_j> (postprocess.py:53-70) through the spectral
+  // passes: u in z form (+ E at frequency 0), A u on the band in z form with
+  // the unscaled coefficient (1 / prod(B)), then the Euclidean sums over the
+  // z entries, which are grid means (Parseval)
+  int spectral_energy(const R* X, int add_macro, double* AH, cudaStream_t s) {
+    int st = ensure_spectral();
+    if (st != ST_OK) return st;
+    const long long nzc = (long long)g_.n0 * g_.n1 * g_.n2h;
+    const size_t nz = (size_t)g_.L * g_.dv * nzc;
+    cplx<R>* zu = zb_ + 2 * nz;
+    cplx<R>* zw = zb_ + 3 * nz;
+    if ((st = to_z(X, zu, s)) != ST_OK) return st;
+    if (add_macro) {
+      k_z_macro<R><<<1, 32, 0, s>>>(zu, nzc, g_.L, g_.dv, 1.0);
+      FHP_LAUNCHED();
+    }
+    k_half_weight<R><<<grid_for(nz), kThreads, 0, s>>>(zu, S_, (long long)nz, g_.n2h, g_.n2, 1.0,
+                                                       0);
+    FHP_LAUNCHED();
+    const int proj_saved = gp_.proj;
+    const double scale_saved = gp_.scale;
+    gp_.proj = 0;
+    gp_.scale = 1.0 / (double)gi_.M;
+    st = spectral_apply_plain(zw, s);
+    gp_.proj = proj_saved;
+    gp_.scale = scale_saved;
+    if (st != ST_OK) return st;
+    if ((st = cross_dot(reinterpret_cast<const R*>(zw), reinterpret_cast<const R*>(zu), gz_, 0,
+                        (double)gz_.M * sizeof(R), s)) != ST_OK) return st;
+    return finish_energy(1.0, AH, s);
+  }
+
+  // per-CTA partial sums of W_i . (X_j (+ E_j)) over g.M values per component
+  int cross_dot(const R* W, const R* X, const GridDims& g, int add_macro, double comp_bytes,
+                cudaStream_t s) {
+    const int pk = pbeg("band_cross_dot", 2.0 * g.L * g.dv * comp_bytes, s);
+    switch (g.L) {
+      case 1: k_cross_dot<R, 1><<<red_ctas_, 256, 0, s>>>(W, X, partials_, g, add_macro); break;
+      case 2: k_cross_dot<R, 2><<<red_ctas_, 256, 0, s>>>(W, X, partials_, g, add_macro); break;
+      case 3: k_cross_dot<R, 3><<<red_ctas_, 256, 0, s>>>(W, X, partials_, g, add_macro); break;
+      case 4: k_cross_dot<R, 4><<<red_ctas_, 256, 0, s>>>(W, X, partials_, g, add_macro); break;
+      case 5: k_cross_dot<R, 5><<<red_ctas_, 256, 0, s>>>(W, X, partials_, g, add_macro); break;
+      default: k_cross_dot<R, 6><<<red_ctas_, 256, 0, s>>>(W, X, partials_, g, add_macro); break;
+    }
+    pend(pk, s);
+    FHP_LAUNCHED();
+    return ST_OK;
+  }
+
+  // A_H = factor x the sum of the cross-dot partials, to the host
+  int finish_energy(double factor, double* AH, cudaStream_t s) {
+    k_sum_partials<<<1, kThreads, 0, s>>>(partials_, red_ctas_, g_.L * g_.L, factor, ad_);
+    FHP_LAUNCHED();
+    FHP_CHECK(cudaMemcpyAsync(AH, ad_, (size_t)g_.L * g_.L * sizeof(double),
+                              cudaMemcpyDeviceToHost, s));
+    FHP_CHECK(cudaMemcpyAsync(h_err_, err_, sizeof(int), cudaMemcpyDeviceToHost, s));
+    FHP_CHECK(cudaStreamSynchronize(s));
+    return take_err(s);
+  }
+
   int spectral_iteration(cplx<R>* zx, cplx<R>* zr, cplx<R>* zp, cplx<R>* zap, double* dlog,
                          int log_rows, cudaStream_t s) {
     int st = spectral_operator(zr, zp, zap, s);
@@ -1252,7 +1366,8 @@ class Engine final : public EngineBase {
     if (!A_) { set_error("coefficient not set"); return ST_BAD_ARG; }
     const R* X = static_cast<const R*>(Xv);
     const int L = g_.L;
-    if (band_) return band_energy(X, add_macro, AH, s);
+    if (band_) return spectral_cg_ ? spectral_energy(X, add_macro, AH, s)
+                                   : band_energy(X, add_macro, AH, s);
     switch (coef_kind_) {
       case COEF_ISO: k_energy<R, COEF_ISO><<<dim3(red_ctas_, g_.K), 128, 0, s>>>(X, A_, partials_, g_, add_macro); break;
       case COEF_SYM: k_energy<R, COEF_SYM><<<dim3(red_ctas_, g_.K), 128, 0, s>>>(X, A_, partials_, g_, add_macro); break;
@@ -1994,19 +2109,9 @@ class Engine final : public EngineBase {
     int st = band_operator(coef_kind_, false, U, nullptr, nullptr, W, nullptr, s, false, false);
     gp_.proj = proj_saved;
     gp_.scale = scale_saved;
-    if (st == ST_OK) {
-      k_cross_dot<R><<<red_ctas_, 128, 0, s>>>(W, X, partials_, g_, add_macro);
-      FHP_LAUNCHED();
-      k_sum_partials<<<1, kThreads, 0, s>>>(partials_, red_ctas_, g_.L * g_.L,
-                                            1.0 / (double)g_.M, ad_);
-      FHP_LAUNCHED();
-      FHP_CHECK(cudaMemcpyAsync(AH, ad_, (size_t)g_.L * g_.L * sizeof(double),
-                                cudaMemcpyDeviceToHost, s));
-      FHP_CHECK(cudaMemcpyAsync(h_err_, err_, sizeof(int), cudaMemcpyDeviceToHost, s));
-      FHP_CHECK(cudaStreamSynchronize(s));
-      st = take_err(s);
-    }
-    return st;
+    if (st != ST_OK) return st;
+    if ((st = cross_dot(W, X, g_, add_macro, (double)g_.M * sizeof(R), s)) != ST_OK) return st;
+    return finish_energy(1.0 / (double)g_.M, AH, s);
   }
 
   int run_operator(int coef, bool pupd, const R* x, R* pio, const R* rvec, R* y, const R* pdot,

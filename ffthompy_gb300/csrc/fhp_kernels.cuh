@@ -1470,7 +1470,9 @@ __global__ void __launch_bounds__(256, band_axis_min_blocks<R, MODE>()) k_band_a
     // rows of T columns to global (z form: times sqrt(w) and the operator's
     // scale s / prod(B)), with <p, Ap>: a thread keeps one column and takes
     // its frequencies four at a time, the four loads of p issued before their
-    // products
+    // products.  The Nyquist index of an even N takes the mean of the B-line
+    // coefficients at +-N/2 (band_down_value): CG iterates have none there,
+    // the energies of arbitrary fields do.
     const R osc = R(gp.scale);
     R dot = R(0);
     if (T <= (int)blockDim.x) {
@@ -1494,8 +1496,7 @@ __global__ void __launch_bounds__(256, band_axis_min_blocks<R, MODE>()) k_band_a
             for (int u = 0; u < 4; ++u) {
               const int ku = k + u * kst;
               if (ku >= ax.n_out) break;
-              const int q = signed_freq(ku, ax.n_out);
-              const cplx<R> v = cscale<R>(get_fwd<R>(line, L1, q < 0 ? q + ax.n_in : q), fo);
+              const cplx<R> v = cscale<R>(band_down_value<R>(line, L1, ku, ax.n_out, ax.n_in), fo);
               Sout[base + (long long)ku * ax.inner] = v;
               dot += pv[u].x * v.x + pv[u].y * v.y;
             }
@@ -1506,8 +1507,7 @@ __global__ void __launch_bounds__(256, band_axis_min_blocks<R, MODE>()) k_band_a
       tile_loop(nlc, ax.n_out, T, lgT, [&](int c, int k, int t) {
         const long long col = t0 + t;
         if (col >= ax.inner) return;
-        const int q = signed_freq(k, ax.n_out);
-        cplx<R> v = get_fwd<R>(buf1 + (c * T + t) * ld1, L1, q < 0 ? q + ax.n_in : q);
+        cplx<R> v = band_down_value<R>(buf1 + (c * T + t) * ld1, L1, k, ax.n_out, ax.n_in);
         v = cscale<R>(v, half_weight_root<R>(ax, g, col, false) * osc);
         const long long idx = (((long long)(c0 + c) * ax.mid + m) * ax.n_out + k) * ax.inner + col;
         Sout[idx] = v;
@@ -2350,63 +2350,60 @@ __global__ void __launch_bounds__(32 * kR512Warps, 2) k_band_last_r512(
 }
 
 // W_i . u_j cross products per load pair on the solve grid (band energy):
-// partial sums of sum_v sum_c W[i][c] (X[j][c] + delta_cj) (postprocess.py:53-70)
-template <typename R>
-__global__ void __launch_bounds__(128) k_cross_dot(const R* __restrict__ W, const R* __restrict__ X,
+// partial sums of sum_v sum_c W[i][c] (X[j][c] + delta_cj) (postprocess.py:53-70).
+// LT = the plan's load count, so the per-thread sums are registers of fixed
+// size and every value is loaded once: per voxel and component the L values
+// of W and of X, then the L x L products.  Per-voxel products in the field
+// precision, summed over 8 voxels, then into FP64 (FP64 arithmetic is the
+// slow pipe on this GPU).  256 threads.
+template <typename R, int LT>
+__global__ void __launch_bounds__(256) k_cross_dot(const R* __restrict__ W, const R* __restrict__ X,
                                                    double* __restrict__ partials, GridDims g,
                                                    int add_macro) {
-  __shared__ double red[4 * kMaxLoads * kMaxLoads];
-  const int L = g.L, dv = g.dv;
-  // per-voxel products in the field precision, summed over up to 8 voxels,
-  // then into FP64 (FP64 arithmetic is the slow pipe on this GPU); constant
-  // indices keep both arrays in registers
-  double acc[kMaxLoads * kMaxLoads];
-  R part[kMaxLoads * kMaxLoads];
+  __shared__ double red[8 * LT * LT];
+  const int dv = g.dv;
+  double acc[LT * LT];
+  R part[LT * LT];
 #pragma unroll
-  for (int i = 0; i < kMaxLoads * kMaxLoads; ++i) {
+  for (int i = 0; i < LT * LT; ++i) {
     acc[i] = 0.;
     part[i] = R(0);
   }
   const long long stride = (long long)gridDim.x * blockDim.x;
   int cnt = 0;
   for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < g.M; v += stride) {
+    for (int c = 0; c < dv; ++c) {
+      R w[LT], x[LT];
 #pragma unroll
-    for (int i = 0; i < kMaxLoads; ++i) {
-      if (i >= L) break;
-#pragma unroll
-      for (int j = 0; j < kMaxLoads; ++j) {
-        if (j >= L) break;
-        R s = R(0);
-        for (int c = 0; c < dv; ++c) {
-          const R u = X[(long long)(j * dv + c) * g.M + v] +
-                      ((add_macro && c == j) ? R(1) : R(0));
-          s += W[(long long)(i * dv + c) * g.M + v] * u;
-        }
-        part[i * kMaxLoads + j] += s;
+      for (int i = 0; i < LT; ++i) {
+        w[i] = W[(long long)(i * dv + c) * g.M + v];
+        x[i] = X[(long long)(i * dv + c) * g.M + v] + ((add_macro && c == i) ? R(1) : R(0));
       }
+#pragma unroll
+      for (int i = 0; i < LT; ++i)
+#pragma unroll
+        for (int j = 0; j < LT; ++j) part[i * LT + j] += w[i] * x[j];
     }
     if (++cnt == 8) {
 #pragma unroll
-      for (int i = 0; i < kMaxLoads * kMaxLoads; ++i) {
+      for (int i = 0; i < LT * LT; ++i) {
         acc[i] += (double)part[i];
         part[i] = R(0);
       }
       cnt = 0;
     }
   }
-  double out[kMaxLoads * kMaxLoads];
 #pragma unroll
-  for (int i = 0; i < kMaxLoads; ++i)
-#pragma unroll
-    for (int j = 0; j < kMaxLoads; ++j)
-      out[i * kMaxLoads + j] = acc[i * kMaxLoads + j] + (double)part[i * kMaxLoads + j];
-  // the L x L block first (the layout block_sum_n writes)
-#pragma unroll
-  for (int i = 0; i < kMaxLoads; ++i)
-#pragma unroll
-    for (int j = 0; j < kMaxLoads; ++j)
-      if (i < L && j < L) acc[i * L + j] = out[i * kMaxLoads + j];
-  block_sum_n(acc, L * L, red, partials + (long long)blockIdx.x * L * L);
+  for (int i = 0; i < LT * LT; ++i) acc[i] += (double)part[i];
+  block_sum_n(acc, LT * LT, red, partials + (long long)blockIdx.x * LT * LT);
+}
+
+// v E at frequency 0 of half spectra in the N layout [load][comp][n0][n1][n2h]
+// (normalised, plain or z form: both are the mean there): comp l of load l
+template <typename R>
+__global__ void k_z_macro(cplx<R>* __restrict__ z, long long nzc, int L, int dv, double v) {
+  const int l = threadIdx.x;
+  if (l < L && l < dv) z[(long long)(l * dv + l) * nzc].x += (R)v;
 }
 
 // x + E (macroscopic field added per load), for the band energy

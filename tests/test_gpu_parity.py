@@ -634,6 +634,60 @@ def test_band_spectral_cg_equals_real_cg(N, physics, precision):
     assert _relmax(X_s, X_r) < tolX, _relmax(X_s, X_r)
 
 
+@pytest.mark.parametrize('N,physics', [((7, 7, 7), 'scalar'), ((6, 5, 8), 'scalar'),
+                                       ((15, 16), 'scalar'), ((5, 5, 5), 'elasticity'),
+                                       ((9, 8), 'elasticity'), ((31, 63, 255), 'scalar')])
+@pytest.mark.parametrize('precision', ['f64', 'f32'])
+def test_band_spectral_rhs_and_energy_equal_real_path(N, physics, precision):
+    """Band plans with spectral CG take the right-hand sides G A (-E) and the
+    energies <A (X + E), X + E> through the spectral passes (a zeroed spectrum
+    with frequency 0 set, no solve-grid transforms before the pads); with
+    band_cg='real' both run through the real-field operator.  They agree to
+    the field precision for both projections and with / without E."""
+    from ffthompy_gb300.engine import GalerkinPlan, nice_size
+    N = np.asarray(N)
+    d = N.size
+    rng = np.random.default_rng(int(np.prod(N)) + 3 * d)
+    dv = d if physics == 'scalar' else d * (d + 1) // 2
+    Ns = 2 * N - 1
+    if physics == 'scalar':
+        a = 1. + 20. * (rng.random(tuple(Ns)) < 0.4)
+        A = np.einsum('ij,...->ij...', np.eye(dv), a)
+    else:
+        C1 = oracle.mandel_isotropic(1., 0.5, d)
+        C2 = oracle.mandel_isotropic(10., 3., d)
+        m = rng.random(tuple(Ns)) < 0.4
+        A = np.einsum('ij,...->ij...', C1, ~m) + np.einsum('ij,...->ij...', C2, m)
+    integ = tuple(nice_size(n) for n in Ns)
+    A = _project_comps(A, integ)
+    plans = {}
+    for mode in ('spectral', 'real'):
+        plans[mode] = GalerkinPlan(tuple(N), np.ones(d), physics=physics, integ=integ,
+                                   precision=precision, band_cg=mode)
+        plans[mode].set_coefficient(A)
+    tol = 1e-12 if precision == 'f64' else 2e-5
+    ps, pr = plans['spectral'], plans['real']
+    E = np.zeros((dv, dv) + tuple(N))
+    for l in range(dv):
+        E[l, l] = -1.
+    for proj in (1, 2):
+        bs = ps.rhs_macro(proj).double().cpu().numpy()
+        br = pr.rhs_macro(proj).double().cpu().numpy()
+        assert _relmax(bs, br) < tol, (proj, _relmax(bs, br))
+        # and the operator applied to -E by the real-field passes
+        bo = pr.apply(E, proj=proj).double().cpu().numpy()
+        assert _relmax(bs, bo) < tol, (proj, _relmax(bs, bo))
+    # energies of a field in range(G) and of an arbitrary one
+    X, _ = pr.cg(pr.rhs_macro(1), tol=1e-6, maxiter=300)
+    Xr = rng.standard_normal((dv, dv) + tuple(N))
+    for x in (X, Xr):
+        for add in (True, False):
+            AHs = ps.energy(x, add_macro=add)
+            AHr = pr.energy(x, add_macro=add)
+            assert _relmax(AHs, AHr) < (1e-12 if precision == 'f64' else 2e-6), (
+                add, _relmax(AHs, AHr))
+
+
 @pytest.mark.parametrize('N', [(3, 5, 255), (4, 3, 254), (2, 6, 253), (7, 255), (6, 254)])
 @pytest.mark.parametrize('integ_kernel', ['register', 'register_cpasync', 'shared'])
 def test_band_operator_512_register_lines(N, integ_kernel):
