@@ -890,6 +890,19 @@ int fhp_fourier_interp(fhp_plan src, fhp_plan dst, const void* x_src, void* x_ds
   return st;
 }
 
+// right-hand sides, CG from zero and A_H of the plan's coefficient (the
+// driver of applications.py:58-86): the engine's fused call, or for mixed
+// plans the refined solve between the FP64 right-hand side and energy
+static int homogenize_once(fhp_plan_s& plan, int proj, double tol, int maxiter, void* b, void* x,
+                           bool keep_x, double* AH_host, fhp::SolveResult& r, cudaStream_t s) {
+  fhp::EngineBase& e = *plan.eng;
+  if (!plan.lo) return e.homogenize(proj, tol, maxiter, b, x, keep_x, AH_host, r, s);
+  int st = e.rhs_macro(proj, b, s);
+  if (st == FHP_OK) st = cg_mixed(plan, proj, b, nullptr, tol, maxiter, x, r, 1, s);
+  if (st == FHP_OK) st = e.energy(x, 1, AH_host, s);
+  return st;
+}
+
 int fhp_homogenize_host(fhp_plan plan, int proj, int coef_kind, const double* coef_host,
                         double tol, int maxiter, double* AH_host, int* kit_host,
                         double* norm_res_host, void* x_host, void* stream) {
@@ -904,12 +917,9 @@ int fhp_homogenize_host(fhp_plan plan, int proj, int coef_kind, const double* co
   void* b = e.scratch(fhp::SCR_HOST_B, bytes);
   void* x = e.scratch(fhp::SCR_HOST_X, bytes);
   st = (b && x) ? FHP_OK : FHP_OOM;
-  if (st == FHP_OK) st = e.rhs_macro(proj, b, s);
   fhp::SolveResult r;
-  if (st == FHP_OK)
-    st = plan->lo ? cg_mixed(*plan, proj, b, nullptr, tol, maxiter, x, r, 1, s)
-                  : e.cg_solve(proj, b, nullptr, tol, maxiter, x, r, 1, s);
-  if (st == FHP_OK) st = e.energy(x, 1, AH_host, s);
+  if (st == FHP_OK) st = homogenize_once(*plan, proj, tol, maxiter, b, x, x_host != nullptr,
+                                         AH_host, r, s);
   if (st == FHP_OK && x_host)
     st = cuda_status(cudaMemcpyAsync(x_host, x, bytes, cudaMemcpyDeviceToHost, s), "copy");
   if (st == FHP_OK) st = cuda_status(cudaStreamSynchronize(s), "sync");
@@ -980,12 +990,10 @@ int fhp_homogenize_host_many(fhp_plan plan, int proj, int coef_kind, int count,
       st = plan->lo->set_coefficient(coef_kind, static_cast<const double*>(stage[i]), true, s);
     if (st == FHP_OK) st = cuda_status(cudaEventRecord(plan->freed[i], s), "record");
     if (st == FHP_OK && k + 1 < count) st = upload(k + 1);
-    if (st == FHP_OK) st = e.rhs_macro(proj, b, s);
     fhp::SolveResult r;
     if (st == FHP_OK)
-      st = plan->lo ? cg_mixed(*plan, proj, b, nullptr, tol, maxiter, x, r, 1, s)
-                    : e.cg_solve(proj, b, nullptr, tol, maxiter, x, r, 1, s);
-    if (st == FHP_OK) st = e.energy(x, 1, AH_host + (size_t)k * e.instances() * Lc * Lc, s);
+      st = homogenize_once(*plan, proj, tol, maxiter, b, x, false,
+                           AH_host + (size_t)k * e.instances() * Lc * Lc, r, s);
     for (int l = 0; l < L && l < (int)r.kit.size(); ++l) {
       if (kit_host) kit_host[(size_t)k * L + l] = r.kit[l];
       if (norm_res_host) norm_res_host[(size_t)k * L + l] = r.norm_res[l];

@@ -156,6 +156,18 @@ class EngineBase {
                           double tol, int maxiter, void* x, SolveResult& res, int log_cap,
                           cudaStream_t s) = 0;
   virtual int energy(const void* X, int add_macro, double* AH, cudaStream_t s) = 0;
+  // rhs_macro, cg_solve from x0 = 0 (log_cap 1) and energy(x, add_macro = 1)
+  // in one call, the driver of applications.py:58-86: b and x are field-sized
+  // device buffers, and x holds the solution on return when keep_x is set
+  // (an engine may keep the iterates in another form throughout and skip it)
+  virtual int homogenize(int proj, double tol, int maxiter, void* b, void* x, bool keep_x,
+                         double* AH, SolveResult& res, cudaStream_t s) {
+    (void)keep_x;
+    int st = rhs_macro(proj, b, s);
+    if (st == 0) st = cg_solve(proj, b, nullptr, tol, maxiter, x, res, 1, s);
+    if (st == 0) st = energy(x, 1, AH, s);
+    return st;
+  }
   // grad[c][v] = sum_ij W[i*L+j] dA_H[i][j]/dA_c(v) (W on host, grad FP64 device)
   virtual int energy_gradient(const void* X, int add_macro, const double* W, double* grad,
                               cudaStream_t s) = 0;

@@ -1220,17 +1220,24 @@ class Engine final : public EngineBase {
     if (!A_) { set_error("coefficient not set"); return ST_BAD_ARG; }
     int st = ensure_spectral();
     if (st != ST_OK) return st;
+    const size_t nz = (size_t)g_.L * g_.dv * g_.n0 * g_.n1 * g_.n2h;
+    cplx<R>* zo = zb_ + 3 * nz;
+    if ((st = spectral_rhs_z(proj, zo, s)) != ST_OK) return st;
+    return from_z(zo, b, s);
+  }
+
+  // G A (-E) in z form into zo (not one of the pass buffers S_, SB_)
+  int spectral_rhs_z(int proj, cplx<R>* zo, cudaStream_t s) {
     const long long nzc = (long long)g_.n0 * g_.n1 * g_.n2h;
     const size_t nz = (size_t)g_.L * g_.dv * nzc;
-    cplx<R>* zo = zb_ + 3 * nz;
     FHP_CHECK(cudaMemsetAsync(S_, 0, nz * sizeof(cplx<R>), s));
     k_z_macro<R><<<1, 32, 0, s>>>(S_, nzc, g_.L, g_.dv, -1.0);
     FHP_LAUNCHED();
     gp_.proj = proj;
     // s A (-E) on the band (the operator scale s / prod(B)), then G (unit scale)
-    if ((st = spectral_apply_plain(zo, s)) != ST_OK) return st;
-    if ((st = spec_green(zo, s)) != ST_OK) return st;
-    return from_z(zo, b, s);
+    int st = spectral_apply_plain(zo, s);
+    if (st != ST_OK) return st;
+    return spec_green(zo, s);
   }
 
   // A_H[i][j] = <A u_i, u_j> (postprocess.py:53-70) through the spectral
@@ -1240,11 +1247,18 @@ class Engine final : public EngineBase {
   int spectral_energy(const R* X, int add_macro, double* AH, cudaStream_t s) {
     int st = ensure_spectral();
     if (st != ST_OK) return st;
+    const size_t nz = (size_t)g_.L * g_.dv * g_.n0 * g_.n1 * g_.n2h;
+    cplx<R>* zu = zb_ + 2 * nz;
+    if ((st = to_z(X, zu, s)) != ST_OK) return st;
+    return spectral_energy_z(zu, add_macro, AH, s);
+  }
+
+  // the same from the z form of X in zu (a spectral buffer other than the
+  // last, which takes A u; E is added in place)
+  int spectral_energy_z(cplx<R>* zu, int add_macro, double* AH, cudaStream_t s) {
     const long long nzc = (long long)g_.n0 * g_.n1 * g_.n2h;
     const size_t nz = (size_t)g_.L * g_.dv * nzc;
-    cplx<R>* zu = zb_ + 2 * nz;
     cplx<R>* zw = zb_ + 3 * nz;
-    if ((st = to_z(X, zu, s)) != ST_OK) return st;
     if (add_macro) {
       k_z_macro<R><<<1, 32, 0, s>>>(zu, nzc, g_.L, g_.dv, 1.0);
       FHP_LAUNCHED();
@@ -1256,7 +1270,7 @@ class Engine final : public EngineBase {
     const double scale_saved = gp_.scale;
     gp_.proj = 0;
     gp_.scale = 1.0 / (double)gi_.M;
-    st = spectral_apply_plain(zw, s);
+    int st = spectral_apply_plain(zw, s);
     gp_.proj = proj_saved;
     gp_.scale = scale_saved;
     if (st != ST_OK) return st;
@@ -1348,7 +1362,17 @@ class Engine final : public EngineBase {
       FHP_CHECK(cudaMemsetAsync(zx, 0, nz * sizeof(cplx<R>), s));
     }
     if ((st = to_z(rsrc, zr, s)) != ST_OK) return st;
-    if ((st = spec_green(zr, s)) != ST_OK) return st;
+    return spectral_cg_start(tol, maxiter, log_cap, s);
+  }
+
+  // the rest of the spectral CG set-up, x and r (z form) in place: r
+  // projected onto range(G), p = r, the per-load state and <r, r>
+  int spectral_cg_start(double tol, int maxiter, int log_cap, cudaStream_t s) {
+    const size_t nz = (size_t)g_.L * g_.dv * g_.n0 * g_.n1 * g_.n2h;
+    cplx<R>* zr = zb_ + nz;
+    cplx<R>* zp = zb_ + 2 * nz;
+    int st = spec_green(zr, s);
+    if (st != ST_OK) return st;
     FHP_CHECK(cudaMemcpyAsync(zp, zr, nz * sizeof(cplx<R>), cudaMemcpyDeviceToDevice, s));
     if ((st = init_state(tol, maxiter, log_cap, s)) != ST_OK) return st;
     k_dot<R><<<red_ctas_, kThreads, 0, s>>>(reinterpret_cast<const R*>(zr),
@@ -1359,6 +1383,35 @@ class Engine final : public EngineBase {
     k_update_all_done<<<1, 1, 0, s>>>(st_, g_.L, all_done_);
     FHP_LAUNCHED();
     return ST_OK;
+  }
+
+  // rhs_macro, CG from x = 0 and the energy with every vector kept in z form:
+  // the right-hand side goes straight into r, the solution's z form into the
+  // energy, and the real solution field is made only when asked for
+  int homogenize(int proj, double tol, int maxiter, void* bv, void* xv, bool keep_x, double* AH,
+                 SolveResult& res, cudaStream_t s) override {
+    if (!(band_ && spectral_cg_))
+      return EngineBase::homogenize(proj, tol, maxiter, bv, xv, keep_x, AH, res, s);
+    if (!A_) { set_error("coefficient not set"); return ST_BAD_ARG; }
+    int st = ensure_spectral();
+    if (st != ST_OK) return st;
+    const size_t nz = (size_t)g_.L * g_.dv * g_.n0 * g_.n1 * g_.n2h;
+    cplx<R>* zx = zb_;
+    cplx<R>* zr = zb_ + nz;
+    gp_.proj = proj;
+    cg_spectral_ = true;
+    cg_proj_ = proj;
+    cg_tol_ = tol;
+    cg_x_ = static_cast<R*>(xv);
+    FHP_CHECK(cudaMemsetAsync(zx, 0, nz * sizeof(cplx<R>), s));
+    if ((st = spectral_rhs_z(proj, zr, s)) != ST_OK) return st;   // r = b - A 0
+    if ((st = spectral_cg_start(tol, maxiter, 1, s)) != ST_OK) return st;
+    if ((st = iterate(maxiter, s, [&]() { return cg_step(s); })) != ST_OK) return st;
+    // as cg_end: FP32 iterates projected once more
+    if (sizeof(R) == 4 && (st = spec_green(zx, s)) != ST_OK) return st;
+    if (keep_x && (st = from_z(zx, cg_x_, s)) != ST_OK) return st;
+    if ((st = collect(tol, cg_log_rows_, cg_log_, res, s)) != ST_OK) return st;
+    return spectral_energy_z(zx, 1, AH, s);   // x is not needed after this
   }
 
   // A_H[i][j] = <A u_i, u_j>, u_i = X_i (+ E_i)  (postprocess.py:53-70)

@@ -45,6 +45,39 @@ def test_host_many_equals_single_calls(precision):
         assert np.array_equal(AH, AH1), (AH, AH1)
 
 
+@pytest.mark.parametrize('N', [(15, 15, 15), (15, 16)])
+@pytest.mark.parametrize('precision', ['f64', 'f32'])
+def test_host_band_fused_equals_device_calls(N, precision):
+    """Band plans run the host call's right-hand side, CG and energy with
+    every vector in the spectral form (no real fields in between): the same
+    iterations, A_H and solution as rhs_macro / cg / energy on device buffers
+    (FP64 to roundoff; FP32 to its precision, iteration counts within 3 % or 1)."""
+    from ffthompy_gb300 import _lib
+    from ffthompy_gb300.engine import GalerkinPlan, nice_size
+    d = len(N)
+    integ = tuple(nice_size(2 * n - 1) for n in N)
+    v = _coefs(integ, 1, seed=11)[0]
+    tol = 1e-9 if precision == 'f64' else 1e-4
+    p1 = GalerkinPlan(N, np.ones(d), precision=precision, integ=integ)
+    AH, kit, _, xh = p1.homogenize_host(packed=v, kind=_lib.FHP_COEF_ISO, tol=tol, maxiter=500,
+                                        return_solution=True)
+    p2 = GalerkinPlan(N, np.ones(d), precision=precision, integ=integ)
+    p2.set_coefficient_packed(v, _lib.FHP_COEF_ISO)
+    X, info = p2.cg(p2.rhs_macro(1), tol=tol, maxiter=500)
+    AH2 = p2.energy(X)
+    Xn = X.double().cpu().numpy()
+    rel = lambda a, b: float(np.abs(a - b).max() / np.abs(b).max())
+    if precision == 'f64':
+        assert kit == info['kit'], (kit, info['kit'])
+        assert rel(AH, AH2) < 1e-12, rel(AH, AH2)
+        assert rel(xh, Xn) < 1e-10, rel(xh, Xn)
+    else:
+        assert all(abs(p - q) <= max(1, int(np.ceil(0.03 * q)))
+                   for p, q in zip(kit, info['kit'])), (kit, info['kit'])
+        assert rel(AH, AH2) < 1e-5, rel(AH, AH2)
+        assert rel(xh, Xn) < 1e-2, rel(xh, Xn)
+
+
 def test_host_many_band_plan():
     from ffthompy_gb300 import _lib
     from ffthompy_gb300.engine import GalerkinPlan, homogenize_host_many, nice_size
