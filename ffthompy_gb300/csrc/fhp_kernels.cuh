@@ -2182,27 +2182,39 @@ __global__ void __launch_bounds__(32 * kR512Warps, 2) k_band_last_r512(
   const long long T2 = 2 * np - 1;
   const long long npr = comb ? nrow_w / 2 : 0;
   const long long ntask = comb ? npr * T2 + (nrow_w & 1) * np : nrow_w * np;
-  // task t: row index i of this warp (row gw + i nw), pair line p, shared line
-  auto decode = [&](long long t, long long& i, int& p, bool& two) {
-    if (comb) {
-      const long long m = t / T2;
-      const int u = (int)(t - m * T2);
-      two = m < npr && u == np - 1;
-      i = (m < npr && u >= np) ? 2 * m + 1 : 2 * m;
-      p = (m < npr && u >= np) ? u - np : u;
+  // Task position: block m (a row; with shared lines a row pair, then a last
+  // unpaired row) and index u in it, advanced by one per task without integer
+  // division.  place(): row index i of this warp (row gw + i nw), pair line p,
+  // shared line.
+  struct TaskPos {
+    long long m;
+    int u;
+  };
+  auto advance = [&](TaskPos& q) {
+    const int lim = (comb && q.m < npr) ? (int)T2 : np;
+    if (++q.u == lim) {
+      q.u = 0;
+      ++q.m;
+    }
+  };
+  auto place = [&](const TaskPos& q, long long& i, int& p, bool& two) {
+    if (comb && q.m < npr) {
+      two = q.u == np - 1;
+      i = q.u >= np ? 2 * q.m + 1 : 2 * q.m;
+      p = q.u >= np ? q.u - np : q.u;
     } else {
-      i = t / np;
-      p = (int)(t - i * np);
+      i = comb ? 2 * q.m : q.m;
+      p = q.u;
       two = false;
     }
   };
   // copy task t into buffer t & 1; the coefficient row of row index i goes to
   // coefficient buffer i & 1 (the shared line brings row i + 1's)
-  auto prefetch = [&](long long t) {
+  auto prefetch = [&](long long t, const TaskPos& q) {
     long long i = 0;
     int p = 0;
     bool two = false;
-    if (t < ntask) decode(t, i, p, two);
+    if (t < ntask) place(q, i, p, two);
     const long long row = gw + i * nw;
     const int b = (int)(t & 1);
     const bool loadc = two || (p == 0 && !(comb && (i & 1)));
@@ -2238,17 +2250,21 @@ __global__ void __launch_bounds__(32 * kR512Warps, 2) k_band_last_r512(
     }
     cp_async_commit();
   };
-  prefetch(0);
+  TaskPos cur{0, 0};
+  prefetch(0, cur);
   float a[16];
   for (long long t = 0; t < ntask; ++t) {
     long long i;
     int p;
     bool two;
-    decode(t, i, p, two);
+    place(cur, i, p, two);
+    TaskPos nxt = cur;
+    advance(nxt);
     const long long row = gw + i * nw;
     const int b = (int)(t & 1);
     __syncwarp();       // every lane is done with the buffers of task t - 1
-    prefetch(t + 1);
+    prefetch(t + 1, nxt);
+    cur = nxt;
     if (tma) {
       if (!mbar_wait_bounded(wbar + b, (unsigned)((t >> 1) & 1), kR512WaitTries)) {
         if (lane == 0) {
