@@ -117,7 +117,7 @@ int fhp_plan_set_band_cg(fhp_plan plan, int spectral);
  * quarter (a 255-point solve line); kind = 2: the same register lines with
  * per-lane cp.async loads; kind = 0: the shared-memory line cores, for every
  * plan.
- * Both compute the same transforms.  No counterpart in the reference (its
+ * All compute the same transforms.  No counterpart in the reference (its
  * transforms are numpy.fft.rfftn / irfftn, ffthompy/tensors/fft.py:39-43).
  */
 int fhp_plan_set_integration_kernel(fhp_plan plan, int kind);
